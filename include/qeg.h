@@ -1,0 +1,214 @@
+/*
+ * qeg.h -- C ABI of the GB300 (sm_103a) hash GROUP BY / hash equi-join engine.
+ *
+ * This is the drop-in boundary beneath the reference engine's pull-based
+ * operators (explorer-skp/query-engine). A host operator that implements the
+ * reference's `Operator` contract (ops/operator.h:40-47) drains its children,
+ * hands each batch's columns to these entry points, and re-emits the result as
+ * ordinary `Batch` views. The ABI uses plain pointers, sizes and status codes:
+ * no C++ types, no exceptions, no torch types.
+ *
+ * Column layout is the reference's (core/column.h:55-67, core/validity.h:21-63):
+ * one contiguous value array per column (I32/STR 4 bytes, I64/F64/TS 8 bytes,
+ * BOOL 1 byte) and an optional validity bitmap of 64-bit words, bit i of word
+ * i/64, LSB-first, 1 = valid. `all_valid != 0` means "no nulls, ignore the
+ * bitmap". Pointers may be device pointers (used in place) or host pointers
+ * (copied to the device inside the call).
+ *
+ * Threading: a qeg_ctx and the objects created from it are single-threaded,
+ * like the reference's operators (exec/parallel.h:15-19). Independent contexts
+ * may be used concurrently from different threads; they share no mutable state.
+ */
+#ifndef QEG_H
+#define QEG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------
+ * The reference reports errors with C++ exceptions; across this ABI each has a
+ * status code and qeg_last_error() holds the message:
+ *   QEG_ERR_INVALID   <- std::invalid_argument (ops/join.cpp:118-122,
+ *                        ops/aggregate.cpp:85-90, ops/scan.cpp:15-18)
+ *   QEG_ERR_OVERFLOW  <- std::overflow_error (ops/hashtable.cpp:64-65)
+ *   QEG_ERR_OOM       <- std::bad_alloc (core/buffer.cpp:23)
+ *   QEG_ERR_TIMEOUT   a bounded device-side wait ran out (no reference analogue)
+ *   QEG_ERR_CUDA      any other CUDA runtime failure                        */
+typedef int32_t qeg_status;
+#define QEG_OK 0
+#define QEG_ERR_INVALID (-1)
+#define QEG_ERR_OVERFLOW (-2)
+#define QEG_ERR_OOM (-3)
+#define QEG_ERR_CUDA (-4)
+#define QEG_ERR_TIMEOUT (-5)
+#define QEG_ERR_UNSUPPORTED (-6)
+#define QEG_ERR_NO_DEVICE (-7)
+
+/* qe::Type (core/types.h:18), same numbering. */
+#define QEG_I32 0
+#define QEG_I64 1
+#define QEG_F64 2
+#define QEG_BOOL 3
+#define QEG_TS 4
+#define QEG_STR 5
+
+/* qe::AggFunc (ops/aggregate.h:61), same numbering. */
+#define QEG_COUNT_STAR 0
+#define QEG_COUNT 1
+#define QEG_SUM 2
+#define QEG_MIN 3
+#define QEG_MAX 4
+#define QEG_AVG 5
+
+/* qe::JoinType (ops/join.h:59), same numbering. */
+#define QEG_INNER 0
+#define QEG_LEFT 1
+
+/* Aggregation strategy (no reference analogue: the reference has one CPU path). */
+#define QEG_AGG_AUTO 0   /* chosen from the key-column sketch + estimator     */
+#define QEG_AGG_SMEM 1   /* shared-memory private tables + global merge       */
+#define QEG_AGG_GLOBAL 2 /* global-atomic table only                          */
+
+/* Table sizing. */
+#define QEG_SIZE_LEARNED 0 /* capacity from the learned estimator             */
+#define QEG_SIZE_FIXED 1   /* fixed initial capacity, overflow -> resize      */
+
+/* Join strategy. */
+#define QEG_JOIN_AUTO 0
+#define QEG_JOIN_HASH 1        /* one global hash table                      */
+#define QEG_JOIN_PARTITIONED 2 /* radix-partitioned build and probe          */
+#define QEG_JOIN_DENSE 3       /* direct-mapped table over the key range     */
+
+/* A column view: the fields of qe::Column (core/column.h:55-67). For QEG_STR,
+ * `code_map` (host or device, `code_map_len` entries) translates each
+ * dictionary code to a canonical value id; equal string values must map to
+ * equal ids, which is how the reference compares STR by value
+ * (ops/aggregate.cpp:164-187, ops/join.cpp:48-71). */
+typedef struct qeg_column {
+  int32_t type;
+  int32_t all_valid;
+  uint64_t len;
+  const void* data;
+  const uint64_t* validity;
+  const int32_t* code_map;
+  uint64_t code_map_len;
+} qeg_column;
+
+/* An output column: caller-owned buffers (host or device) with room for the
+ * requested rows. `validity` receives ceil(rows/64) words; `all_valid` (may be
+ * NULL) receives 1 when the fetched range holds no NULL. */
+typedef struct qeg_out_column {
+  void* data;
+  uint64_t* validity;
+  int32_t* all_valid;
+} qeg_out_column;
+
+/* One aggregate: qe::AggSpec (ops/aggregate.h:75-89) without the name. */
+typedef struct qeg_agg_spec {
+  int32_t func;
+  uint32_t input_col; /* ignored for QEG_COUNT_STAR */
+} qeg_agg_spec;
+
+typedef struct qeg_agg_config {
+  int32_t strategy;          /* QEG_AGG_*                                   */
+  int32_t sizing;            /* QEG_SIZE_*                                  */
+  uint64_t initial_capacity; /* QEG_SIZE_FIXED: first table capacity (0 = 2^20) */
+  uint64_t expected_groups;  /* > 0: skip estimation, size for this many    */
+  int32_t block_threads;     /* 0 = tuned                                   */
+  int32_t rows_per_thread;   /* 0 = tuned                                   */
+  int32_t smem_slots;        /* 0 = tuned                                   */
+  int32_t hot_keys;          /* register-resident heavy hitters; -1 = tuned */
+} qeg_agg_config;
+
+typedef struct qeg_join_config {
+  int32_t strategy;       /* QEG_JOIN_*                                     */
+  int32_t partition_bits; /* QEG_JOIN_PARTITIONED: 0 = tuned                */
+} qeg_join_config;
+
+typedef struct qeg_ctx qeg_ctx;
+typedef struct qeg_agg qeg_agg;
+typedef struct qeg_join qeg_join;
+
+/* ---- context --------------------------------------------------------------*/
+/* Creates a context on CUDA device `device` with its own stream. */
+qeg_status qeg_ctx_create(int device, qeg_ctx** out);
+void qeg_ctx_destroy(qeg_ctx* ctx);
+/* Message of the last failing call on this context (thread-local when ctx is
+ * NULL or creation failed). */
+const char* qeg_last_error(const qeg_ctx* ctx);
+/* The CUDA stream (cudaStream_t) all work of this context is ordered on. */
+void* qeg_ctx_stream(qeg_ctx* ctx);
+/* Waits for all work of the context; returns the first device error seen. */
+qeg_status qeg_ctx_synchronize(qeg_ctx* ctx);
+/* Number of kernels this context has launched (for launch accounting). */
+uint64_t qeg_ctx_kernel_launches(const qeg_ctx* ctx);
+
+/* ---- hash aggregation: replaces qe::Aggregate (ops/aggregate.h:102-144) ----
+ * create  ~ Aggregate::Aggregate + open()'s setup (ops/aggregate.cpp:206-241)
+ * consume ~ one pulled batch of drain_and_build (ops/aggregate.cpp:243-437);
+ *           `sel` (sel_len rows, host or device) is the batch's SelectionVector
+ *           (core/column.h:73-76); sel == NULL means dense rows 0..len-1
+ * finish  ~ end of the drain: the number of output rows (groups; exactly 1 for
+ *           a global aggregate, even over empty input)
+ * fetch   ~ Aggregate::next (ops/aggregate.cpp:439-493): rows
+ *           [first, first+count) of the result, key columns then aggregates,
+ *           typed by qe::agg_result_type (ops/aggregate.cpp:78-97)          */
+qeg_status qeg_agg_create(qeg_ctx* ctx, const int32_t* col_types, int ncols,
+                          const uint32_t* key_cols, int nkeys, const qeg_agg_spec* aggs,
+                          int naggs, const qeg_agg_config* cfg, qeg_agg** out);
+qeg_status qeg_agg_consume(qeg_agg* agg, const qeg_column* cols, int ncols,
+                           const uint32_t* sel, uint64_t sel_len);
+qeg_status qeg_agg_finish(qeg_agg* agg, uint64_t* num_rows);
+qeg_status qeg_agg_result_types(const qeg_agg* agg, int32_t* types);
+qeg_status qeg_agg_fetch(qeg_agg* agg, uint64_t first, uint64_t count,
+                         const qeg_out_column* outs);
+/* Diagnostics of the finished aggregation: table capacity, resize rounds,
+ * strategy and hot-key count actually used, estimated group count. */
+qeg_status qeg_agg_stats(const qeg_agg* agg, uint64_t* capacity, uint32_t* resizes,
+                         int32_t* strategy, int32_t* hot_keys, double* est_groups);
+void qeg_agg_destroy(qeg_agg* agg);
+
+/* ---- hash equi-join: replaces qe::HashJoin (ops/join.h:69-123) ------------
+ * create      ~ HashJoin::HashJoin (ops/join.cpp:101-123), same key-type check
+ * build       ~ one build batch of build_side (ops/join.cpp:133-197): inserts
+ *               the keys (NULL keys never match) and materialises the batch's
+ *               columns like BuildStore::append_row (ops/join_internal.h:64-87)
+ * build_finish~ end of build_side
+ * probe       ~ build_pairs_for_probe (ops/join.cpp:199-247) for one probe
+ *               batch; *out_rows = rows the batch joins to (LEFT: unmatched
+ *               probe rows once, build columns NULL)
+ * fetch       ~ HashJoin::next (ops/join.cpp:260-299): output rows
+ *               [first, first+count) of the last probed batch, probe columns
+ *               then build columns                                          */
+qeg_status qeg_join_create(qeg_ctx* ctx, const int32_t* probe_types, int nprobe,
+                           const int32_t* build_types, int nbuild, const uint32_t* probe_keys,
+                           const uint32_t* build_keys, int nkeys, int32_t join_type,
+                           const qeg_join_config* cfg, qeg_join** out);
+qeg_status qeg_join_build(qeg_join* j, const qeg_column* cols, int ncols);
+qeg_status qeg_join_build_finish(qeg_join* j);
+qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64_t* out_rows);
+qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count,
+                          const qeg_out_column* outs);
+/* The aggregate sink of scan(probe).join(scan(build)).aggregate({},
+ * {COUNT(*), SUM(probe_val)}) fused into the probe: adds this batch's matched
+ * row count and payload sum to the running totals (single key column). */
+qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key,
+                                    const qeg_column* probe_val);
+/* Totals of all qeg_join_probe_count_sum calls so far; *sum_valid = 0 when no
+ * matched row carried a non-null payload (SQL SUM over nothing is NULL). */
+qeg_status qeg_join_count_sum_result(qeg_join* j, int64_t* count, int64_t* sum,
+                                     int32_t* sum_valid);
+/* Strategy actually used by the build (QEG_JOIN_*), the partition bits and the
+ * number of distinct non-null build keys. */
+qeg_status qeg_join_stats(const qeg_join* j, int32_t* strategy, int32_t* partition_bits,
+                          uint64_t* distinct_keys);
+void qeg_join_destroy(qeg_join* j);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

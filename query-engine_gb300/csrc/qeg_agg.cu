@@ -1,0 +1,974 @@
+// qeg_agg.cu -- hash GROUP BY on sm_103a: replaces qe::Aggregate
+// (ops/aggregate.h:102-144, ops/aggregate.cpp).
+//
+// Table layout (HBM). One row of 64-bit words per group:
+//   single key : [key word][fields...]            + 2 side rows at index cap
+//                (key word 0, which doubles as the empty marker) and cap+1
+//                (the NULL key group)
+//   multi key  : [state][null mask][key words...][fields...]; state 0 = empty,
+//                1 = being published, >= 2 = the row's hash tag
+//   global     : one row [unused][fields...]
+// Fields hold the reference's AggCell state (ops/agg_internal.h:47-51) in a
+// form where all-zero bits are the identity of every aggregate, so tables are
+// initialised by memset: row count, per-column NULL count (non-null count =
+// rows - nulls), integer / F64 sums, and MIN/MAX as order-preserving unsigned
+// encodings updated with atomicMax (qeg_device.cuh).
+//
+// Kernel: each CTA keeps a private shared-memory table (first-come insertion,
+// or preloaded with heavy hitters) and falls back to the global table, whose
+// key words are claimed with one CAS. Rows whose key cannot be placed within
+// the probe limit are spilled (row index) and re-run after the host grows the
+// table (rehash) -- the GPU form of HashTable::grow (ops/hashtable.cpp:75-91).
+#include <algorithm>
+#include <cmath>
+
+#include "qeg_agg.h"
+
+namespace qeg {
+
+namespace {
+
+__device__ __forceinline__ uint64_t ld_relaxed(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ uint64_t ld_volatile_shared(const uint64_t* p) {
+  return *reinterpret_cast<const volatile uint64_t*>(p);
+}
+
+// Applies one value to one state word. `row` points at the field block.
+template <bool SHARED>
+__device__ __forceinline__ void apply_field(uint64_t* w, uint8_t kind, bool valid, uint64_t bits,
+                                            int32_t vtype) {
+  unsigned long long* u = reinterpret_cast<unsigned long long*>(w);
+  switch (kind) {
+    case F_NULLS:
+      if (!valid) atomicAdd(u, 1ull);
+      break;
+    case F_SUMI:
+      if (valid) atomicAdd(u, static_cast<unsigned long long>(bits));
+      break;
+    case F_SUMF:
+      if (valid) atomicAdd(reinterpret_cast<double*>(w), __longlong_as_double(static_cast<long long>(bits)));
+      break;
+    case F_MINI:
+      if (valid) atomicMax(u, static_cast<unsigned long long>(~enc_i64(static_cast<int64_t>(bits))));
+      break;
+    case F_MAXI:
+      if (valid) atomicMax(u, static_cast<unsigned long long>(enc_i64(static_cast<int64_t>(bits))));
+      break;
+    case F_MINF:
+      if (valid) atomicMax(u, static_cast<unsigned long long>(~enc_f64_bits(bits)));
+      break;
+    case F_MAXF:
+      if (valid) atomicMax(u, static_cast<unsigned long long>(enc_f64_bits(bits)));
+      break;
+    default: break;
+  }
+  (void)vtype;
+}
+
+// Loads the values of one row for every referenced value column.
+__device__ __forceinline__ void load_values(const AggK& P, uint64_t p, bool (&vv)[kMaxVals],
+                                            uint64_t (&vb)[kMaxVals]) {
+#pragma unroll
+  for (int c = 0; c < kMaxVals; ++c) {
+    vv[c] = false;
+    vb[c] = 0;
+    if (c < P.nvals) {
+      const DevCol& col = P.val[c];
+      vv[c] = col_valid(col, p);
+      if (vv[c]) {
+        if (col.type == kF64)
+          vb[c] = static_cast<uint64_t>(__ldg(static_cast<const long long*>(col.data) + p));
+        else
+          vb[c] = static_cast<uint64_t>(int_value(col, p));
+      }
+    }
+  }
+}
+
+// Applies a row to the field block `f` (row count + every value field).
+template <bool SHARED>
+__device__ __forceinline__ void apply_row(uint64_t* f, const AggK& P, const bool (&vv)[kMaxVals],
+                                          const uint64_t (&vb)[kMaxVals]) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(f), 1ull);  // F_ROWS is field 0
+#pragma unroll
+  for (int c = 0; c < kMaxVals; ++c) {
+    if (c < P.nvals) {
+      const int first = P.cfirst[c];
+      const int n = P.cnf[c];
+      for (int k = 0; k < n; ++k)
+        apply_field<SHARED>(f + first + k, P.fkind[first + k], vv[c], vb[c], P.val[c].type);
+    }
+  }
+}
+
+__device__ __forceinline__ uint64_t key_hash1(uint64_t k) { return hash_fold(kHashSeed, k); }
+
+// Single-key global lookup/insert. Returns the row, or nullptr when the key
+// could not be placed within the probe limit.
+__device__ __forceinline__ uint64_t* global_row1(const AggK& P, bool kv, uint64_t k, uint64_t h,
+                                                 unsigned long long& inserted) {
+  const int W = P.row_words;
+  if (!kv) return P.table + (P.cap + 1) * W;
+  if (k == 0) return P.table + P.cap * W;
+  uint64_t s = h & (P.cap - 1);
+  for (int t = 0; t < P.probe_limit; ++t) {
+    uint64_t* r = P.table + s * W;
+    const uint64_t cur = ld_relaxed(r);
+    if (cur == k) return r;
+    if (cur == 0) {
+      const unsigned long long old =
+          atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, static_cast<unsigned long long>(k));
+      if (old == 0) {
+        ++inserted;
+        return r;
+      }
+      if (old == k) return r;
+    }
+    s = (s + 1) & (P.cap - 1);
+  }
+  return nullptr;
+}
+
+// Multi-key global lookup/insert with a publish protocol: claim (0 -> 1), write
+// null mask and key words, fence, publish the tag. Readers wait (bounded) on a
+// row being published.
+__device__ __forceinline__ uint64_t* global_rowN(const AggK& P, const uint64_t* words, uint64_t nullmask,
+                                                 uint64_t h, unsigned long long& inserted) {
+  const int W = P.row_words;
+  const uint64_t tag = (h >> 32) | 2ull;
+  uint64_t s = h & (P.cap - 1);
+  for (int t = 0; t < P.probe_limit; ++t) {
+    uint64_t* r = P.table + s * W;
+    uint64_t st = ld_relaxed(r);
+    if (st == 0) {
+      const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, 1ull);
+      if (old == 0) {
+        r[1] = nullmask;
+        for (int j = 0; j < P.nkeys; ++j) r[2 + j] = words[j];
+        __threadfence();
+        atomicExch(reinterpret_cast<unsigned long long*>(r), static_cast<unsigned long long>(tag));
+        ++inserted;
+        return r;
+      }
+      st = old;
+    }
+    int spins = 0;
+    while (st == 1) {
+      if (++spins > kSpinLimit) {
+        atomicOr(P.err, kDevSpinTimeout);
+        return nullptr;
+      }
+      st = ld_relaxed(r);
+    }
+    if (st == tag) {
+      __threadfence();
+      bool eq = ld_relaxed(r + 1) == nullmask;
+      for (int j = 0; eq && j < P.nkeys; ++j) eq = ld_relaxed(r + 2 + j) == words[j];
+      if (eq) return r;
+    }
+    s = (s + 1) & (P.cap - 1);
+  }
+  return nullptr;
+}
+
+__device__ __forceinline__ void spill_row(const AggK& P, uint64_t p) {
+  const unsigned long long i = atomicAdd(P.counters + 0, 1ull);
+  if (i < P.spill_cap)
+    P.spill_rows[i] = static_cast<uint32_t>(p);
+  else
+    atomicOr(P.err, kDevSpillOverflow);
+}
+
+// Merges one field block `src` (a partial aggregate) into `dst`.
+__device__ __forceinline__ void merge_fields(uint64_t* dst, const uint64_t* src, const AggK& P) {
+  for (int f = 0; f < P.nfields; ++f) {
+    const uint64_t v = src[f];
+    if (v == 0) continue;  // zero is the identity of every field
+    unsigned long long* d = reinterpret_cast<unsigned long long*>(dst + f);
+    switch (P.fkind[f]) {
+      case F_ROWS:
+      case F_NULLS:
+      case F_SUMI: atomicAdd(d, static_cast<unsigned long long>(v)); break;
+      case F_SUMF: atomicAdd(reinterpret_cast<double*>(d), __longlong_as_double(static_cast<long long>(v))); break;
+      default: atomicMax(d, static_cast<unsigned long long>(v)); break;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The aggregation kernel. MODE 0: global (no key), 1: single key, 2: multi key.
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
+  extern __shared__ uint64_t sm[];
+  const int W = P.row_words;
+  const int S = (MODE == 0) ? 1 : P.smem_slots;  // power of two, or 0 = off
+  const int srows = (MODE == 0) ? 1 : (S > 0 ? S + 2 : 0);
+  const int fo = (MODE == 2) ? 2 + P.nkeys : 1;  // field offset within a global row
+
+  for (int i = threadIdx.x; i < srows * W; i += blockDim.x) sm[i] = 0;
+  __syncthreads();
+  if (MODE == 1 && S > 0 && P.nhot > 0) {
+    for (int i = threadIdx.x; i < P.nhot; i += blockDim.x) {
+      const uint64_t k = P.hot[i];
+      if (k == 0) continue;
+      uint64_t s = key_hash1(k) & (S - 1);
+      for (int t = 0; t < S; ++t) {
+        const unsigned long long old =
+            atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * W]), 0ull, static_cast<unsigned long long>(k));
+        if (old == 0 || old == k) break;
+        s = (s + 1) & (S - 1);
+      }
+    }
+    __syncthreads();
+  }
+
+  unsigned long long inserted = 0;
+  const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < P.nrows; i += step) {
+    uint64_t p = i;
+    if (P.sel) {
+      p = P.sel[i];
+      if (p >= P.len) {
+        atomicOr(P.err, kDevBadInput);
+        continue;
+      }
+    }
+    bool vv[kMaxVals];
+    uint64_t vb[kMaxVals];
+    load_values(P, p, vv, vb);
+
+    if (MODE == 0) {
+      apply_row<true>(&sm[1], P, vv, vb);
+      continue;
+    }
+    if (MODE == 1) {
+      const DevCol& kc = P.key[0];
+      const bool kv = col_valid(kc, p);
+      const uint64_t k = kv ? key_word(kc, p) : 0;
+      const uint64_t h = key_hash1(k);
+      int srow = -1;
+      if (S > 0) {
+        if (!kv) {
+          srow = S + 1;
+        } else if (k == 0) {
+          srow = S;
+        } else {
+          uint64_t s = h & (S - 1);
+          for (int t = 0; t < P.smem_probe; ++t) {
+            const uint64_t cur = ld_volatile_shared(&sm[s * W]);
+            if (cur == k) {
+              srow = static_cast<int>(s);
+              break;
+            }
+            if (cur == 0) {
+              if (!P.smem_insert) break;
+              const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * W]), 0ull,
+                                                       static_cast<unsigned long long>(k));
+              if (old == 0 || old == k) {
+                srow = static_cast<int>(s);
+                break;
+              }
+            }
+            s = (s + 1) & (S - 1);
+          }
+        }
+      }
+      if (srow >= 0) {
+        apply_row<true>(&sm[srow * W + 1], P, vv, vb);
+      } else {
+        uint64_t* r = global_row1(P, kv, k, h, inserted);
+        if (r)
+          apply_row<false>(r + 1, P, vv, vb);
+        else
+          spill_row(P, p);
+      }
+      continue;
+    }
+    // MODE 2: composite key, global table only.
+    uint64_t words[kMaxKeys];
+    uint64_t nullmask = 0, h = kHashSeed;
+#pragma unroll
+    for (int j = 0; j < kMaxKeys; ++j) {
+      if (j < P.nkeys) {
+        const bool kv = col_valid(P.key[j], p);
+        words[j] = kv ? key_word(P.key[j], p) : 0;
+        if (!kv) nullmask |= 1ull << j;
+        h = hash_fold(h, kv ? words[j] : 0x9E3779B97F4A7C15ull);
+      }
+    }
+    uint64_t* r = global_rowN(P, words, nullmask, h, inserted);
+    if (r)
+      apply_row<false>(r + fo, P, vv, vb);
+    else
+      spill_row(P, p);
+  }
+
+  // Flush the CTA-private table into the global table.
+  if (MODE != 2 && srows > 0) {
+    __syncthreads();
+    for (int sr = threadIdx.x; sr < srows; sr += blockDim.x) {
+      const uint64_t* src = &sm[sr * W];
+      if (src[1] == 0) continue;  // no row landed here
+      uint64_t* dst;
+      if (MODE == 0) {
+        dst = P.table;
+      } else if (sr == S + 1) {
+        dst = P.table + (P.cap + 1) * W;
+      } else if (sr == S) {
+        dst = P.table + P.cap * W;
+      } else {
+        const uint64_t k = src[0];
+        dst = global_row1(P, true, k, key_hash1(k), inserted);
+      }
+      if (dst) {
+        merge_fields(dst + 1, src + 1, P);
+      } else {
+        const unsigned long long i = atomicAdd(P.counters + 1, 1ull);
+        if (i < P.part_cap) {
+          for (int w = 0; w < W; ++w) P.spill_parts[i * W + w] = src[w];
+        } else {
+          atomicOr(P.err, kDevSpillOverflow);
+        }
+      }
+    }
+  }
+  // Occupancy accounting: one atomic per warp.
+  for (int o = 16; o > 0; o >>= 1) inserted += __shfl_down_sync(0xffffffffu, inserted, o);
+  if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
+}
+
+// Re-inserts every occupied row of `old` into the (zeroed) table of P.
+template <int MODE>
+__global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, uint64_t old_cap) {
+  const int W = P.row_words;
+  unsigned long long inserted = 0;
+  const uint64_t total = (MODE == 1) ? old_cap + 2 : old_cap;
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < total;
+       s += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t* src = old + s * W;
+    uint64_t* dst = nullptr;
+    if (MODE == 1) {
+      if (s == old_cap) {
+        dst = P.table + P.cap * W;
+      } else if (s == old_cap + 1) {
+        dst = P.table + (P.cap + 1) * W;
+      } else {
+        const uint64_t k = src[0];
+        if (k == 0) continue;
+        dst = global_row1(P, true, k, key_hash1(k), inserted);
+      }
+      if (!dst) {
+        atomicOr(P.err, kDevSpillOverflow);
+        continue;
+      }
+      for (int f = 1; f < W; ++f) dst[f] = src[f];
+    } else {
+      const uint64_t st = src[0];
+      if (st < 2) continue;
+      uint64_t words[kMaxKeys];
+      for (int j = 0; j < P.nkeys; ++j) words[j] = src[2 + j];
+      uint64_t h = kHashSeed;
+      for (int j = 0; j < P.nkeys; ++j) h = hash_fold(h, ((src[1] >> j) & 1) ? 0x9E3779B97F4A7C15ull : words[j]);
+      dst = global_rowN(P, words, src[1], h, inserted);
+      if (!dst) {
+        atomicOr(P.err, kDevSpillOverflow);
+        continue;
+      }
+      for (int f = 2 + P.nkeys; f < W; ++f) dst[f] = src[f];
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) inserted += __shfl_down_sync(0xffffffffu, inserted, o);
+  if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
+}
+
+// Merges spilled partial rows (single-key mode) into the table.
+__global__ void merge_parts_kernel(const AggK P, const uint64_t* __restrict__ parts, uint64_t n) {
+  const int W = P.row_words;
+  unsigned long long inserted = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t* src = parts + i * W;
+    const uint64_t k = src[0];
+    uint64_t* dst = global_row1(P, true, k, key_hash1(k), inserted);
+    if (!dst) {
+      atomicOr(P.err, kDevSpillOverflow);
+      continue;
+    }
+    merge_fields(dst + 1, src + 1, P);
+  }
+  for (int o = 16; o > 0; o >>= 1) inserted += __shfl_down_sync(0xffffffffu, inserted, o);
+  if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
+}
+
+// Writes one output value of result type `t` from a 64-bit word.
+__device__ __forceinline__ void store_typed(void* base, uint64_t i, int32_t t, uint64_t w) {
+  switch (t) {
+    case kI32:
+    case kSTR: static_cast<int32_t*>(base)[i] = static_cast<int32_t>(static_cast<uint32_t>(w)); break;
+    case kBOOL: static_cast<uint8_t*>(base)[i] = static_cast<uint8_t>(w & 1ull); break;
+    default: static_cast<uint64_t*>(base)[i] = w; break;
+  }
+}
+
+// Compacts occupied rows into dense output columns (keys, then aggregates),
+// applying the reference's finalisation (ops/agg_internal.h:169-229).
+template <int MODE>
+__global__ void finalize_kernel(const AggK P, const FinK F) {
+  const int W = P.row_words;
+  const int fo = (MODE == 2) ? 2 + P.nkeys : 1;
+  const uint64_t total = (MODE == 0) ? 1 : (MODE == 1 ? P.cap + 2 : P.cap);
+  const int lane = threadIdx.x & 31;
+  for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < total; base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t s = base + threadIdx.x;
+    bool occ = false;
+    const uint64_t* r = nullptr;
+    if (s < total) {
+      r = P.table + s * W;
+      if (MODE == 0) occ = true;
+      else if (MODE == 1) occ = (s < P.cap) ? (r[0] != 0) : (r[1] != 0);
+      else occ = r[0] >= 2;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, occ);
+    if (m == 0) continue;
+    unsigned long long wbase = 0;
+    if (lane == 0) wbase = atomicAdd(F.out_count, static_cast<unsigned long long>(__popc(m)));
+    wbase = __shfl_sync(0xffffffffu, wbase, 0);
+    if (!occ) continue;
+    const uint64_t o = wbase + __popc(m & ((1u << lane) - 1u));
+    if (o >= F.out_cap) {
+      atomicOr(P.err, kDevSpillOverflow);
+      continue;
+    }
+    // keys
+    for (int j = 0; j < P.nkeys; ++j) {
+      bool isnull;
+      uint64_t w;
+      if (MODE == 1) {
+        isnull = (s == P.cap + 1);
+        w = (s == P.cap) ? 0 : r[0];
+      } else {
+        isnull = (r[1] >> j) & 1ull;
+        w = r[2 + j];
+      }
+      F.valid[j][o] = isnull ? 0 : 1;
+      store_typed(F.vals[j], o, F.rtype[j], isnull ? 0 : w);
+    }
+    // aggregates
+    const uint64_t* f = r + fo;
+    const uint64_t rows = f[0];
+    for (int a = 0; a < F.naggs; ++a) {
+      const int oc = P.nkeys + a;
+      const int vf = F.vfield[a];
+      const uint64_t nulls = F.nfield[a] >= 0 ? f[F.nfield[a]] : 0;
+      const uint64_t nn = rows - nulls;
+      const int32_t rt = F.rtype[oc];
+      uint8_t ok = 1;
+      uint64_t w = 0;
+      switch (F.func[a]) {
+        case 0: w = rows; break;  // COUNT(*)
+        case 1: w = nn; break;    // COUNT(col)
+        case 2:                   // SUM
+          if (nn == 0) ok = 0;
+          else w = f[vf];
+          break;
+        case 5: {  // AVG = sum / non-null count, in double (ops/agg_internal.h:217-227)
+          if (nn == 0) {
+            ok = 0;
+          } else {
+            const double sum = (P.fkind[vf] == F_SUMF) ? __longlong_as_double(static_cast<long long>(f[vf]))
+                                                        : static_cast<double>(static_cast<int64_t>(f[vf]));
+            w = static_cast<uint64_t>(__double_as_longlong(sum / static_cast<double>(nn)));
+          }
+          break;
+        }
+        default: {  // MIN / MAX
+          if (nn == 0) {
+            ok = 0;
+            break;
+          }
+          const uint8_t k = P.fkind[vf];
+          const uint64_t e = f[vf];
+          if (k == F_MINF) w = dec_f64_bits(~e);
+          else if (k == F_MAXF) w = dec_f64_bits(e);
+          else if (k == F_MINI) w = static_cast<uint64_t>(dec_i64(~e));
+          else w = static_cast<uint64_t>(dec_i64(e));
+          break;
+        }
+      }
+      F.valid[oc][o] = ok;
+      store_typed(F.vals[oc], o, rt, ok ? w : 0);
+    }
+  }
+}
+
+int32_t agg_result_type(int32_t func, int32_t in) {
+  switch (func) {
+    case QEG_COUNT_STAR:
+    case QEG_COUNT: return QEG_I64;
+    case QEG_SUM: return in == QEG_F64 ? QEG_F64 : QEG_I64;
+    case QEG_AVG: return QEG_F64;
+    default: return in;
+  }
+}
+
+uint64_t next_pow2(uint64_t v) {
+  uint64_t c = 1;
+  while (c < v) c <<= 1;
+  return c;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+void AggState::plan(const int32_t* col_types, int ncols, const uint32_t* key_cols, int nk,
+                    const qeg_agg_spec* aggs_in, int na) {
+  require(ncols > 0 && col_types != nullptr, "aggregate needs an input schema");
+  require(na >= 1 && aggs_in != nullptr, "Aggregate needs >=1 aggregate");
+  require(nk >= 0 && nk <= kMaxKeys, "GPU aggregate supports 0..8 key columns");
+  require(na <= kMaxAggs, "GPU aggregate supports at most 32 aggregates");
+  types.assign(col_types, col_types + ncols);
+  for (int32_t t : types) require(t >= QEG_I32 && t <= QEG_STR, "unknown column type");
+  keys.assign(key_cols, key_cols + nk);
+  for (uint32_t k : keys) require(k < static_cast<uint32_t>(ncols), "key column index out of range");
+  aggs.assign(aggs_in, aggs_in + na);
+  mode = nk == 0 ? 0 : (nk == 1 ? 1 : 2);
+
+  // Distinct value columns and their fields, grouped by column.
+  val_cols.clear();
+  fkind.assign(1, F_ROWS);
+  std::vector<std::vector<uint8_t>> per_col;
+  vfield.assign(na, -1);
+  nfield.assign(na, -1);
+  rtypes.clear();
+  for (uint32_t k : keys) rtypes.push_back(types[k]);
+  struct Want { int col; uint8_t kind; };
+  std::vector<Want> wants;
+  for (int a = 0; a < na; ++a) {
+    const qeg_agg_spec& s = aggs[a];
+    require(s.func >= QEG_COUNT_STAR && s.func <= QEG_AVG, "unknown aggregate function");
+    if (s.func == QEG_COUNT_STAR) {
+      rtypes.push_back(QEG_I64);
+      continue;
+    }
+    require(s.input_col < static_cast<uint32_t>(ncols), "aggregate input column out of range");
+    const int32_t in = types[s.input_col];
+    if (in == QEG_STR && (s.func == QEG_SUM || s.func == QEG_AVG))
+      require(false, s.func == QEG_SUM ? "SUM is not defined on STR (VARCHAR)"
+                                       : "AVG is not defined on STR (VARCHAR)");
+    rtypes.push_back(agg_result_type(s.func, in));
+  }
+  // Assign fields per distinct column.
+  std::vector<int> colslot(ncols, -1);
+  for (int a = 0; a < na; ++a) {
+    const qeg_agg_spec& s = aggs[a];
+    if (s.func == QEG_COUNT_STAR) continue;
+    if (colslot[s.input_col] < 0) {
+      require(static_cast<int>(val_cols.size()) < kMaxVals, "GPU aggregate supports at most 8 input columns");
+      colslot[s.input_col] = static_cast<int>(val_cols.size());
+      val_cols.push_back(s.input_col);
+      per_col.emplace_back();
+    }
+    const int vc = colslot[s.input_col];
+    const bool isf = types[s.input_col] == QEG_F64;
+    uint8_t kind = F_NULLS;
+    if (s.func == QEG_SUM || s.func == QEG_AVG) kind = isf ? F_SUMF : F_SUMI;
+    if (s.func == QEG_MIN) kind = isf ? F_MINF : F_MINI;
+    if (s.func == QEG_MAX) kind = isf ? F_MAXF : F_MAXI;
+    auto& v = per_col[vc];
+    if (std::find(v.begin(), v.end(), F_NULLS) == v.end()) v.insert(v.begin(), F_NULLS);
+    if (kind != F_NULLS && std::find(v.begin(), v.end(), kind) == v.end()) v.push_back(kind);
+  }
+  cfirst.assign(val_cols.size(), 0);
+  cnf.assign(val_cols.size(), 0);
+  for (size_t c = 0; c < val_cols.size(); ++c) {
+    cfirst[c] = static_cast<int>(fkind.size());
+    cnf[c] = static_cast<int>(per_col[c].size());
+    for (uint8_t k : per_col[c]) fkind.push_back(k);
+  }
+  require(static_cast<int>(fkind.size()) <= kMaxFields, "too many aggregate state fields for the GPU path");
+  for (int a = 0; a < na; ++a) {
+    const qeg_agg_spec& s = aggs[a];
+    if (s.func == QEG_COUNT_STAR) continue;
+    const int vc = colslot[s.input_col];
+    const bool isf = types[s.input_col] == QEG_F64;
+    uint8_t kind = F_NULLS;
+    if (s.func == QEG_SUM || s.func == QEG_AVG) kind = isf ? F_SUMF : F_SUMI;
+    if (s.func == QEG_MIN) kind = isf ? F_MINF : F_MINI;
+    if (s.func == QEG_MAX) kind = isf ? F_MAXF : F_MAXI;
+    for (int k = 0; k < cnf[vc]; ++k) {
+      if (fkind[cfirst[vc] + k] == F_NULLS) nfield[a] = cfirst[vc] + k;
+      if (fkind[cfirst[vc] + k] == kind) vfield[a] = cfirst[vc] + k;
+    }
+  }
+  nfields = static_cast<int>(fkind.size());
+  row_words = (mode == 2 ? 2 + nk : 1) + nfields;
+}
+
+AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel, uint64_t nrows,
+                       uint64_t len) const {
+  AggK P{};
+  P.nkeys = static_cast<int>(keys.size());
+  for (size_t j = 0; j < keys.size(); ++j) P.key[j] = staged[keys[j]].dev;
+  P.nvals = static_cast<int>(val_cols.size());
+  for (size_t c = 0; c < val_cols.size(); ++c) {
+    P.val[c] = staged[val_cols[c]].dev;
+    P.cfirst[c] = static_cast<uint8_t>(cfirst[c]);
+    P.cnf[c] = static_cast<uint8_t>(cnf[c]);
+  }
+  P.nfields = nfields;
+  for (int f = 0; f < nfields; ++f) P.fkind[f] = fkind[f];
+  P.row_words = row_words;
+  P.table = table.get<uint64_t>();
+  P.cap = cap;
+  P.sel = sel;
+  P.nrows = nrows;
+  P.len = len;
+  P.smem_slots = smem_slots;
+  P.smem_insert = smem_insert;
+  P.smem_probe = 8;
+  P.hot = hot_keys_dev.get<uint64_t>();
+  P.nhot = nhot;
+  P.probe_limit = probe_limit;
+  P.spill_rows = spill_rows.get<uint32_t>();
+  P.spill_cap = spill_cap;
+  P.spill_parts = spill_parts.get<uint64_t>();
+  P.part_cap = part_cap;
+  P.counters = counters.get<unsigned long long>();
+  P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+  return P;
+}
+
+void AggState::alloc_table(uint64_t new_cap) {
+  cap = std::max<uint64_t>(next_pow2(new_cap), 1024);
+  const uint64_t rows = (mode == 1) ? cap + 2 : (mode == 0 ? 1 : cap);
+  table.alloc(rows * row_words * 8, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(table.get(), 0, rows * row_words * 8, ctx->stream));
+}
+
+size_t AggState::smem_bytes() const {
+  const int srows = mode == 0 ? 1 : (smem_slots > 0 ? smem_slots + 2 : 0);
+  return static_cast<size_t>(srows) * row_words * 8;
+}
+
+void AggState::launch(const AggK& P, uint64_t nrows) {
+  const size_t sb = smem_bytes();
+  int block = cfg.block_threads > 0 ? cfg.block_threads : 512;
+  int per_sm = 1;
+  auto set_attr = [&](auto kern) {
+    if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
+  };
+  if (mode == 0) set_attr(agg_kernel<0>);
+  else if (mode == 1) set_attr(agg_kernel<1>);
+  else set_attr(agg_kernel<2>);
+  require(per_sm > 0, "aggregate kernel does not fit on an SM with this configuration");
+  // Enough CTAs to cover the rows, but each CTA should aggregate a sizeable
+  // morsel so the flush of its private table stays small next to its input.
+  const uint64_t min_rows_per_cta = (mode == 2 || smem_slots == 0) ? 4096 : std::max<uint64_t>(16384, 8ull * smem_slots);
+  uint64_t want = (nrows + min_rows_per_cta - 1) / min_rows_per_cta;
+  uint64_t grid = std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * per_sm);
+  if (grid == 0) grid = 1;
+  if (mode == 0) agg_kernel<0><<<(unsigned)grid, block, sb, ctx->stream>>>(P);
+  else if (mode == 1) agg_kernel<1><<<(unsigned)grid, block, sb, ctx->stream>>>(P);
+  else agg_kernel<2><<<(unsigned)grid, block, sb, ctx->stream>>>(P);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+}
+
+void AggState::read_counters(uint64_t out[3]) {
+  QEG_CUDA(cudaMemcpyAsync(out, counters.get(), 24, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void AggState::grow(uint64_t new_cap) {
+  DevBuf old;
+  old.swap(table);
+  const uint64_t old_cap = cap;
+  alloc_table(new_cap);
+  QEG_CUDA(cudaMemsetAsync(counters.get<uint8_t>() + 16, 0, 8, ctx->stream));
+  std::vector<StagedCol> none;
+  AggK P = kparams_base();
+  const uint64_t n = (mode == 1) ? old_cap + 2 : old_cap;
+  const unsigned g = grid_for(ctx, n, 256, 8);
+  if (mode == 1) rehash_kernel<1><<<g, 256, 0, ctx->stream>>>(P, old.get<uint64_t>(), old_cap);
+  else rehash_kernel<2><<<g, 256, 0, ctx->stream>>>(P, old.get<uint64_t>(), old_cap);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+  ++resizes;
+}
+
+AggK AggState::kparams_base() const {
+  std::vector<StagedCol> dummy;
+  AggK P{};
+  P.nkeys = static_cast<int>(keys.size());
+  P.nvals = static_cast<int>(val_cols.size());
+  for (size_t c = 0; c < val_cols.size(); ++c) {
+    P.cfirst[c] = static_cast<uint8_t>(cfirst[c]);
+    P.cnf[c] = static_cast<uint8_t>(cnf[c]);
+  }
+  P.nfields = nfields;
+  for (int f = 0; f < nfields; ++f) P.fkind[f] = fkind[f];
+  P.row_words = row_words;
+  P.table = table.get<uint64_t>();
+  P.cap = cap;
+  P.probe_limit = probe_limit;
+  P.counters = counters.get<unsigned long long>();
+  P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+  return P;
+}
+
+void AggState::consume(const qeg_column* cols, int ncols, const uint32_t* sel, uint64_t sel_len) {
+  require(!finished, "consume() after finish()");
+  require(ncols == static_cast<int>(types.size()), "batch column count does not match the schema");
+  require(cols != nullptr, "cols is NULL");
+  const uint64_t len = cols[0].len;
+  for (int c = 0; c < ncols; ++c) {
+    require(cols[c].type == types[c], "batch column type does not match the schema");
+    require(cols[c].len == len, "batch columns differ in length");
+    require(cols[c].all_valid || cols[c].validity != nullptr,
+            "column with all_valid=0 must carry a validity bitmap");
+  }
+  const uint64_t nrows = sel ? sel_len : len;
+  require(len <= 0xffffffffull, "a batch holds at most 2^32-1 rows");
+  std::vector<StagedCol> staged(ncols);
+  for (uint32_t k : keys) stage_column(ctx, cols[k], staged[k]);
+  for (uint32_t v : val_cols) stage_column(ctx, cols[v], staged[v]);
+  DevBuf selbuf;
+  const uint32_t* dsel = nullptr;
+  stage_sel(ctx, sel, sel_len, selbuf, &dsel);
+  if (!table.get()) first_consume(staged, nrows, len, dsel);
+  rows_seen += nrows;
+  if (nrows == 0) return;
+
+  AggK P = kparams(staged, dsel, nrows, len);
+  launch(P, nrows);
+  uint64_t c[3];
+  read_counters(c);
+  check_device_error(ctx);
+  inserted = c[2];
+  uint64_t nspill = c[0], nparts = c[1];
+  int rounds = 0;
+  while (nspill > 0 || nparts > 0) {
+    require(++rounds < 64, "aggregate table failed to converge after 64 resize rounds");
+    // Copy the spill lists out of the way, grow the table, then replay.
+    DevBuf rows_copy(std::max<uint64_t>(nspill, 1) * 4, ctx->stream), parts_copy(std::max<uint64_t>(nparts, 1) * row_words * 8, ctx->stream);
+    if (nspill) QEG_CUDA(cudaMemcpyAsync(rows_copy.get(), spill_rows.get(), nspill * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (nparts) QEG_CUDA(cudaMemcpyAsync(parts_copy.get(), spill_parts.get(), nparts * row_words * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    const uint64_t want = std::max<uint64_t>(cap * 2, next_pow2(2 * (inserted + nparts + nspill / 4)));
+    grow(want);
+    QEG_CUDA(cudaMemsetAsync(counters.get(), 0, 16, ctx->stream));
+    if (nparts) {
+      AggK Q = kparams_base();
+      merge_parts_kernel<<<grid_for(ctx, nparts, 256, 8), 256, 0, ctx->stream>>>(Q, parts_copy.get<uint64_t>(), nparts);
+      ctx->launches++;
+      QEG_CUDA(cudaGetLastError());
+    }
+    if (nspill) {
+      AggK Q = kparams(staged, rows_copy.get<uint32_t>(), nspill, len);
+      launch(Q, nspill);
+    }
+    read_counters(c);
+    check_device_error(ctx);
+    inserted = c[2];
+    nspill = c[0];
+    nparts = c[1];
+  }
+}
+
+void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len,
+                             const uint32_t* dsel) {
+  (void)staged;
+  (void)len;
+  (void)dsel;
+  // Sizing. QEG_SIZE_FIXED: the configured (or default) first capacity, grown on
+  // overflow. QEG_SIZE_LEARNED: the estimator's group count (see qeg_estimate),
+  // falling back to the row count bound when no estimate is available.
+  uint64_t want;
+  est_groups = 0;
+  if (mode == 0) {
+    want = 1;
+  } else if (cfg.expected_groups > 0) {
+    want = 2 * cfg.expected_groups;
+    est_groups = static_cast<double>(cfg.expected_groups);
+  } else if (cfg.sizing == QEG_SIZE_FIXED) {
+    want = cfg.initial_capacity ? cfg.initial_capacity : (1ull << 20);
+  } else {
+    est_groups = estimate_groups(staged, nrows, len, dsel);
+    want = static_cast<uint64_t>(std::max(2.0 * est_groups * 1.15, 1024.0));
+  }
+  alloc_table(want);
+  counters.alloc(64, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(counters.get(), 0, 64, ctx->stream));
+  spill_cap = std::max<uint64_t>(1u << 20, std::min<uint64_t>(nrows, 64ull << 20));
+  spill_rows.alloc(spill_cap * 4, ctx->stream);
+  part_cap = 1u << 20;
+  spill_parts.alloc(part_cap * row_words * 8, ctx->stream);
+
+  // Strategy.
+  strategy = cfg.strategy;
+  if (mode == 2) strategy = QEG_AGG_GLOBAL;
+  if (mode == 0) strategy = QEG_AGG_SMEM;
+  const int max_slots = static_cast<int>(std::min<size_t>(8192, (ctx->smem_optin / (row_words * 8)) - 2));
+  int slots = 1;
+  while (slots * 2 <= max_slots) slots *= 2;
+  if (strategy == QEG_AGG_AUTO) {
+    // Private tables pay off when a CTA sees each key many times: few groups
+    // (all fit) or a heavy head of the key distribution.
+    strategy = (est_groups > 0 && est_groups > 64.0 * slots && hot_share < 0.3) ? QEG_AGG_GLOBAL : QEG_AGG_SMEM;
+  }
+  if (strategy == QEG_AGG_SMEM && mode == 1) {
+    smem_slots = cfg.smem_slots > 0 ? static_cast<int>(next_pow2(cfg.smem_slots)) : std::min(slots, 4096);
+    smem_slots = std::min(smem_slots, slots);
+    smem_insert = 1;
+  } else {
+    smem_slots = 0;
+  }
+}
+
+void AggState::finish(uint64_t* nrows_out) {
+  if (finished) {
+    *nrows_out = nout;
+    return;
+  }
+  if (!table.get()) {
+    // Nothing consumed: set up an empty table so the global case emits its row.
+    std::vector<StagedCol> none;
+    first_consume(none, 0, 0, nullptr);
+  }
+  const uint64_t out_cap = (mode == 0) ? 1 : std::max<uint64_t>(inserted + 2, 1);
+  const int ncolsout = static_cast<int>(keys.size() + aggs.size());
+  out_vals.clear();
+  out_valid.clear();
+  out_vals.resize(ncolsout);
+  out_valid.resize(ncolsout);
+  FinK F{};
+  F.naggs = static_cast<int>(aggs.size());
+  for (int c = 0; c < ncolsout; ++c) {
+    out_vals[c].alloc(out_cap * 8, ctx->stream);
+    out_valid[c].alloc(out_cap, ctx->stream);
+    F.vals[c] = out_vals[c].get();
+    F.valid[c] = out_valid[c].get<uint8_t>();
+    F.rtype[c] = rtypes[c];
+  }
+  for (size_t a = 0; a < aggs.size(); ++a) {
+    F.func[a] = aggs[a].func;
+    F.vfield[a] = vfield[a];
+    F.nfield[a] = nfield[a];
+  }
+  DevBuf cnt(8, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(cnt.get(), 0, 8, ctx->stream));
+  F.out_count = cnt.get<unsigned long long>();
+  F.out_cap = out_cap;
+  AggK P = kparams_base();
+  const uint64_t total = (mode == 0) ? 1 : (mode == 1 ? cap + 2 : cap);
+  const unsigned g = grid_for(ctx, total, 256, 8);
+  if (mode == 0) finalize_kernel<0><<<g, 256, 0, ctx->stream>>>(P, F);
+  else if (mode == 1) finalize_kernel<1><<<g, 256, 0, ctx->stream>>>(P, F);
+  else finalize_kernel<2><<<g, 256, 0, ctx->stream>>>(P, F);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+  unsigned long long n = 0;
+  QEG_CUDA(cudaMemcpyAsync(&n, cnt.get(), 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  check_device_error(ctx);
+  nout = n;
+  finished = true;
+  *nrows_out = nout;
+}
+
+void AggState::fetch(uint64_t first, uint64_t count, const qeg_out_column* outs) {
+  require(finished, "fetch() before finish()");
+  require(first <= nout && count <= nout - first, "fetch range outside the result");
+  require(outs != nullptr, "outs is NULL");
+  for (size_t c = 0; c < out_vals.size(); ++c)
+    fetch_column(ctx, out_vals[c].get(), out_valid[c].get<uint8_t>(), type_width(rtypes[c]), first, count, outs[c]);
+}
+
+}  // namespace qeg
+
+using qeg::AggState;
+
+struct qeg_agg {
+  AggState st;
+};
+
+extern "C" {
+
+qeg_status qeg_agg_create(qeg_ctx* ctx, const int32_t* col_types, int ncols, const uint32_t* key_cols,
+                          int nkeys, const qeg_agg_spec* aggs, int naggs, const qeg_agg_config* cfg,
+                          qeg_agg** out) {
+  return qeg::guarded(ctx, [&] {
+    qeg::require(ctx != nullptr && out != nullptr, "ctx/out is NULL");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    auto a = std::make_unique<qeg_agg>();
+    a->st.ctx = ctx;
+    if (cfg) a->st.cfg = *cfg;
+    a->st.plan(col_types, ncols, key_cols, nkeys, aggs, naggs);
+    *out = a.release();
+  });
+}
+
+qeg_status qeg_agg_consume(qeg_agg* agg, const qeg_column* cols, int ncols, const uint32_t* sel,
+                           uint64_t sel_len) {
+  qeg_ctx* ctx = agg ? agg->st.ctx : nullptr;
+  return qeg::guarded(ctx, [&] {
+    qeg::require(agg != nullptr, "agg is NULL");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    agg->st.consume(cols, ncols, sel, sel_len);
+  });
+}
+
+qeg_status qeg_agg_finish(qeg_agg* agg, uint64_t* num_rows) {
+  qeg_ctx* ctx = agg ? agg->st.ctx : nullptr;
+  return qeg::guarded(ctx, [&] {
+    qeg::require(agg != nullptr && num_rows != nullptr, "agg/num_rows is NULL");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    agg->st.finish(num_rows);
+  });
+}
+
+qeg_status qeg_agg_result_types(const qeg_agg* agg, int32_t* types) {
+  qeg_ctx* ctx = agg ? agg->st.ctx : nullptr;
+  return qeg::guarded(ctx, [&] {
+    qeg::require(agg != nullptr && types != nullptr, "agg/types is NULL");
+    for (size_t c = 0; c < agg->st.rtypes.size(); ++c) types[c] = agg->st.rtypes[c];
+  });
+}
+
+qeg_status qeg_agg_fetch(qeg_agg* agg, uint64_t first, uint64_t count, const qeg_out_column* outs) {
+  qeg_ctx* ctx = agg ? agg->st.ctx : nullptr;
+  return qeg::guarded(ctx, [&] {
+    qeg::require(agg != nullptr, "agg is NULL");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    agg->st.fetch(first, count, outs);
+  });
+}
+
+qeg_status qeg_agg_stats(const qeg_agg* agg, uint64_t* capacity, uint32_t* resizes, int32_t* strategy,
+                         int32_t* hot_keys, double* est_groups) {
+  qeg_ctx* ctx = agg ? agg->st.ctx : nullptr;
+  return qeg::guarded(ctx, [&] {
+    qeg::require(agg != nullptr, "agg is NULL");
+    if (capacity) *capacity = agg->st.cap;
+    if (resizes) *resizes = agg->st.resizes;
+    if (strategy) *strategy = agg->st.strategy;
+    if (hot_keys) *hot_keys = agg->st.nhot;
+    if (est_groups) *est_groups = agg->st.est_groups;
+  });
+}
+
+void qeg_agg_destroy(qeg_agg* agg) {
+  if (!agg) return;
+  cudaSetDevice(agg->st.ctx->device);
+  delete agg;
+}
+
+}  // extern "C"

@@ -1,0 +1,132 @@
+// qeg_agg.h -- GROUP BY plan, kernel parameter blocks and host state.
+#pragma once
+
+#include "qeg_internal.h"
+
+namespace qeg {
+
+// Aggregate state fields of one group (see qeg_agg.cu for the encodings).
+enum FieldKind : uint8_t {
+  F_ROWS = 0,   // COUNT(*) of the group; also the occupancy marker of side rows
+  F_NULLS = 1,  // NULL inputs of one column (non-null count = rows - nulls)
+  F_SUMI = 2,   // SUM over I32/I64/TS/BOOL, two's complement
+  F_SUMF = 3,   // SUM over F64
+  F_MINI = 4,   // MIN over an integer column, ~enc_i64
+  F_MAXI = 5,   // MAX over an integer column, enc_i64
+  F_MINF = 6,   // MIN over F64, ~enc_f64 (NaN-greatest order)
+  F_MAXF = 7,   // MAX over F64, enc_f64
+};
+
+constexpr int kMaxKeys = 8;
+constexpr int kMaxVals = 8;
+constexpr int kMaxFields = 24;
+constexpr int kMaxAggs = 32;
+
+// Parameter block of the aggregation kernels (passed by value).
+struct AggK {
+  DevCol key[kMaxKeys];
+  DevCol val[kMaxVals];
+  int nkeys, nvals, nfields, row_words;
+  uint8_t fkind[kMaxFields];
+  uint8_t cfirst[kMaxVals];
+  uint8_t cnf[kMaxVals];
+  uint64_t* table;
+  uint64_t cap;  // power of two
+  const uint32_t* sel;
+  uint64_t nrows;  // rows to process (sel length, or len when dense)
+  uint64_t len;    // physical column length
+  int smem_slots;  // power of two, 0 = no private table
+  int smem_insert; // 1: first-come insertion into the private table
+  int smem_probe;
+  const uint64_t* hot;  // heavy hitters preloaded into the private table
+  int nhot;
+  int probe_limit;
+  uint32_t* spill_rows;
+  uint64_t spill_cap;
+  uint64_t* spill_parts;
+  uint64_t part_cap;
+  unsigned long long* counters;  // [0] spilled rows, [1] spilled partials, [2] inserted keys
+  uint32_t* err;
+};
+
+// Parameter block of the finalize kernel.
+struct FinK {
+  void* vals[kMaxKeys + kMaxAggs];
+  uint8_t* valid[kMaxKeys + kMaxAggs];
+  int32_t rtype[kMaxKeys + kMaxAggs];
+  int32_t func[kMaxAggs];
+  int32_t vfield[kMaxAggs];
+  int32_t nfield[kMaxAggs];
+  int naggs;
+  unsigned long long* out_count;
+  uint64_t out_cap;
+};
+
+// Key-column sketch: the estimator's inputs and the heavy-hitter candidates.
+constexpr int kSketchFeatures = 80;
+struct SketchResult {
+  float features[kSketchFeatures];
+  double hll_estimate = 0;  // HyperLogLog distinct estimate over the sample
+  double sample_rows = 0;
+  double total_rows = 0;
+  double null_frac = 0;
+  double top_share[16] = {};  // share of sampled rows in the top 2^i candidates
+  std::vector<uint64_t> heavy;  // candidate heavy-hitter key words, most frequent first
+};
+
+// Builds the sketch of one key column (qeg_sketch.cu).
+void sketch_key_column(qeg_ctx* ctx, const DevCol& key, const uint32_t* sel, uint64_t nrows, uint64_t len,
+                       uint64_t sample_target, int want_heavy, SketchResult& out);
+// Classic (non-learned) distinct-count extrapolation from a sketch.
+double classic_estimate(const SketchResult& s);
+// Learned estimate (qeg_estimator.cu): predicted distinct groups and the share of
+// rows covered by the top heavy hitters. Returns false when no trained model
+// is loaded in this context.
+bool learned_estimate(qeg_ctx* ctx, const SketchResult& s, double* groups, double* hot_share);
+
+struct AggState {
+  qeg_ctx* ctx = nullptr;
+  qeg_agg_config cfg{};
+  std::vector<int32_t> types;
+  std::vector<uint32_t> keys;
+  std::vector<qeg_agg_spec> aggs;
+  int mode = 0;  // 0 global, 1 single key, 2 multi key
+  std::vector<uint32_t> val_cols;
+  std::vector<uint8_t> fkind;
+  std::vector<int> cfirst, cnf, vfield, nfield;
+  std::vector<int32_t> rtypes;
+  int nfields = 0, row_words = 0;
+
+  DevBuf table;
+  uint64_t cap = 0;
+  DevBuf counters, spill_rows, spill_parts, hot_keys_dev;
+  uint64_t spill_cap = 0, part_cap = 0;
+  int smem_slots = 0, smem_insert = 0, nhot = 0;
+  int probe_limit = 128;
+  uint64_t inserted = 0, rows_seen = 0;
+  uint32_t resizes = 0;
+  int32_t strategy = QEG_AGG_AUTO;
+  double est_groups = 0, hot_share = 0;
+  std::vector<uint64_t> heavy_candidates;
+
+  bool finished = false;
+  uint64_t nout = 0;
+  std::vector<DevBuf> out_vals, out_valid;
+
+  void plan(const int32_t* col_types, int ncols, const uint32_t* key_cols, int nk, const qeg_agg_spec* aggs,
+            int na);
+  AggK kparams(const std::vector<StagedCol>& staged, const uint32_t* sel, uint64_t nrows, uint64_t len) const;
+  AggK kparams_base() const;
+  void alloc_table(uint64_t new_cap);
+  size_t smem_bytes() const;
+  void launch(const AggK& P, uint64_t nrows);
+  void read_counters(uint64_t out[3]);
+  void grow(uint64_t new_cap);
+  void first_consume(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len, const uint32_t* dsel);
+  double estimate_groups(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len, const uint32_t* dsel);
+  void consume(const qeg_column* cols, int ncols, const uint32_t* sel, uint64_t sel_len);
+  void finish(uint64_t* nrows_out);
+  void fetch(uint64_t first, uint64_t count, const qeg_out_column* outs);
+};
+
+}  // namespace qeg

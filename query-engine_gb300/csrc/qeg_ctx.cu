@@ -1,0 +1,181 @@
+// qeg_ctx.cu -- context, staging of host inputs, result fetch, device error word.
+#include "qeg_internal.h"
+
+thread_local std::string g_qeg_tls_err;
+
+namespace qeg {
+
+namespace {
+
+// Packs one byte per row (1 = valid) into 64-bit validity words, LSB-first
+// (core/validity.h:21-40). Padding bits of the last word are set to 1, the
+// reference's canonical representation (core/validity.h:53-58).
+__global__ void pack_validity_kernel(const uint8_t* __restrict__ valid, uint64_t n,
+                                     uint64_t* __restrict__ words, uint32_t* __restrict__ any_null) {
+  const uint64_t nw = (n + 63) / 64;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nw;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t bits = ~0ull;
+    const uint64_t base = w * 64;
+    for (int b = 0; b < 64; ++b) {
+      const uint64_t r = base + b;
+      if (r < n && !valid[r]) bits &= ~(1ull << b);
+    }
+    words[w] = bits;
+    if (bits != ~0ull) atomicOr(any_null, 1u);
+  }
+}
+
+}  // namespace
+
+void stage_column(qeg_ctx* ctx, const qeg_column& c, StagedCol& out) {
+  require(c.type >= QEG_I32 && c.type <= QEG_STR, "unknown column type");
+  out.len = c.len;
+  out.dev.type = c.type;
+  out.dev.all_valid = (c.all_valid || c.validity == nullptr) ? 1 : 0;
+  const size_t w = type_width(c.type);
+  if (c.len == 0) {
+    out.dev.data = nullptr;
+    out.dev.validity = nullptr;
+  } else if (is_device_ptr(c.data)) {
+    out.dev.data = c.data;
+  } else {
+    require(c.data != nullptr, "column data is NULL");
+    out.data.alloc(c.len * w, ctx->stream);
+    QEG_CUDA(cudaMemcpyAsync(out.data.get(), c.data, c.len * w, cudaMemcpyHostToDevice, ctx->stream));
+    out.dev.data = out.data.get();
+  }
+  if (!out.dev.all_valid && c.len > 0) {
+    const size_t vb = ((c.len + 63) / 64) * 8;
+    if (is_device_ptr(c.validity)) {
+      out.dev.validity = c.validity;
+    } else {
+      out.validity.alloc(vb, ctx->stream);
+      QEG_CUDA(cudaMemcpyAsync(out.validity.get(), c.validity, vb, cudaMemcpyHostToDevice, ctx->stream));
+      out.dev.validity = out.validity.get<uint64_t>();
+    }
+  } else {
+    out.dev.validity = nullptr;
+  }
+  out.dev.code_map = nullptr;
+  if (c.type == QEG_STR && c.code_map != nullptr && c.code_map_len > 0) {
+    if (is_device_ptr(c.code_map)) {
+      out.dev.code_map = c.code_map;
+    } else {
+      out.code_map.alloc(c.code_map_len * 4, ctx->stream);
+      QEG_CUDA(cudaMemcpyAsync(out.code_map.get(), c.code_map, c.code_map_len * 4,
+                               cudaMemcpyHostToDevice, ctx->stream));
+      out.dev.code_map = out.code_map.get<int32_t>();
+    }
+  }
+}
+
+void stage_sel(qeg_ctx* ctx, const uint32_t* sel, uint64_t n, DevBuf& buf, const uint32_t** dev) {
+  if (sel == nullptr || n == 0) {
+    *dev = nullptr;
+    return;
+  }
+  if (is_device_ptr(sel)) {
+    *dev = sel;
+    return;
+  }
+  buf.alloc(n * 4, ctx->stream);
+  QEG_CUDA(cudaMemcpyAsync(buf.get(), sel, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+  *dev = buf.get<uint32_t>();
+}
+
+void check_device_error(qeg_ctx* ctx) {
+  uint32_t e = 0;
+  QEG_CUDA(cudaMemcpyAsync(&e, ctx->dev_err.get(), 4, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (e == kDevOk) return;
+  QEG_CUDA(cudaMemsetAsync(ctx->dev_err.get(), 0, 4, ctx->stream));
+  if (e & kDevSpinTimeout)
+    throw Error(QEG_ERR_TIMEOUT, "a bounded device-side wait ran out (slot publication)");
+  if (e & kDevBadInput)
+    throw Error(QEG_ERR_INVALID, "an input index (selection or dictionary code) is out of range");
+  throw Error(QEG_ERR_CUDA, "device error word " + std::to_string(e));
+}
+
+void fetch_column(qeg_ctx* ctx, const void* dev_vals, const uint8_t* dev_valid, size_t width,
+                  uint64_t first, uint64_t count, const qeg_out_column& out) {
+  if (count == 0) {
+    if (out.all_valid) *out.all_valid = 1;
+    return;
+  }
+  const bool dev_out = is_device_ptr(out.data);
+  const auto kind = dev_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (out.data)
+    QEG_CUDA(cudaMemcpyAsync(out.data, static_cast<const uint8_t*>(dev_vals) + first * width,
+                             count * width, kind, ctx->stream));
+  const uint64_t nw = (count + 63) / 64;
+  DevBuf words(nw * 8 + 8, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(words.get<uint8_t>() + nw * 8, 0, 4, ctx->stream));
+  uint32_t* any_null = reinterpret_cast<uint32_t*>(words.get<uint8_t>() + nw * 8);
+  pack_validity_kernel<<<grid_for(ctx, nw, 256, 4), 256, 0, ctx->stream>>>(dev_valid + first, count,
+                                                                         words.get<uint64_t>(), any_null);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+  uint32_t has_null = 0;
+  if (out.validity) {
+    const auto vk = is_device_ptr(out.validity) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    QEG_CUDA(cudaMemcpyAsync(out.validity, words.get(), nw * 8, vk, ctx->stream));
+  }
+  QEG_CUDA(cudaMemcpyAsync(&has_null, any_null, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (out.all_valid) *out.all_valid = has_null ? 0 : 1;
+}
+
+}  // namespace qeg
+
+extern "C" {
+
+qeg_status qeg_ctx_create(int device, qeg_ctx** out) {
+  return qeg::guarded(nullptr, [&] {
+    qeg::require(out != nullptr, "out is NULL");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+      cudaGetLastError();
+      throw qeg::Error(QEG_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    qeg::require(device >= 0 && device < n, "device index out of range");
+    QEG_CUDA(cudaSetDevice(device));
+    auto c = std::make_unique<qeg_ctx>();
+    c->device = device;
+    cudaDeviceProp p{};
+    QEG_CUDA(cudaGetDeviceProperties(&p, device));
+    c->sms = p.multiProcessorCount;
+    c->smem_optin = p.sharedMemPerBlockOptin;
+    QEG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->dev_err.alloc(64, c->stream);
+    QEG_CUDA(cudaMemsetAsync(c->dev_err.get(), 0, 64, c->stream));
+    QEG_CUDA(cudaStreamSynchronize(c->stream));
+    *out = c.release();
+  });
+}
+
+void qeg_ctx_destroy(qeg_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  ctx->dev_err.release();
+  cudaStreamSynchronize(ctx->stream);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* qeg_last_error(const qeg_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : g_qeg_tls_err.c_str();
+}
+
+void* qeg_ctx_stream(qeg_ctx* ctx) { return ctx ? static_cast<void*>(ctx->stream) : nullptr; }
+
+qeg_status qeg_ctx_synchronize(qeg_ctx* ctx) {
+  return qeg::guarded(ctx, [&] {
+    qeg::require(ctx != nullptr, "ctx is NULL");
+    qeg::check_device_error(ctx);
+  });
+}
+
+uint64_t qeg_ctx_kernel_launches(const qeg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+}  // extern "C"

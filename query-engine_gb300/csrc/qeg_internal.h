@@ -1,0 +1,162 @@
+// qeg_internal.h -- host-side internals shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/qeg.h"
+#include "qeg_device.cuh"
+
+namespace qeg {
+
+// Error carrying a qeg_status; thrown inside the library, converted to a status
+// code at the C-ABI boundary (no exception crosses it).
+struct Error : std::runtime_error {
+  qeg_status code;
+  Error(qeg_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  if (e == cudaErrorMemoryAllocation)
+    throw Error(QEG_ERR_OOM, std::string(what) + ": out of device memory");
+  throw Error(QEG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define QEG_CUDA(x) ::qeg::cuda_check((x), #x)
+
+inline void require(bool ok, const std::string& msg) {
+  if (!ok) throw Error(QEG_ERR_INVALID, msg);
+}
+
+// Stream-ordered device buffer (cudaMallocAsync on the context stream).
+class DevBuf {
+ public:
+  DevBuf() = default;
+  DevBuf(size_t bytes, cudaStream_t s) { alloc(bytes, s); }
+  ~DevBuf() { release(); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept { swap(o); }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    release();
+    swap(o);
+    return *this;
+  }
+  void alloc(size_t bytes, cudaStream_t s) {
+    release();
+    stream_ = s;
+    bytes_ = bytes;
+    if (bytes) QEG_CUDA(cudaMallocAsync(&ptr_, bytes, s));
+  }
+  void release() {
+    if (ptr_) cudaFreeAsync(ptr_, stream_);
+    ptr_ = nullptr;
+    bytes_ = 0;
+  }
+  void swap(DevBuf& o) noexcept {
+    std::swap(ptr_, o.ptr_);
+    std::swap(bytes_, o.bytes_);
+    std::swap(stream_, o.stream_);
+  }
+  template <class T = void>
+  T* get() const { return static_cast<T*>(ptr_); }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  void* ptr_ = nullptr;
+  size_t bytes_ = 0;
+  cudaStream_t stream_ = nullptr;
+};
+
+inline size_t type_width(int32_t t) {
+  switch (t) {
+    case QEG_I32: return 4;
+    case QEG_I64: return 8;
+    case QEG_F64: return 8;
+    case QEG_BOOL: return 1;
+    case QEG_TS: return 8;
+    case QEG_STR: return 4;
+  }
+  return 0;
+}
+
+inline bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace qeg
+
+struct qeg_ctx {
+  int device = 0;
+  int sms = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  uint64_t launches = 0;
+  qeg::DevBuf dev_err;  // uint32 device error word (qeg::DevError bits)
+};
+
+namespace qeg {
+
+// Resolves a caller column to device pointers: device pointers are used in
+// place; host pointers are copied into buffers owned by this object.
+struct StagedCol {
+  DevCol dev{};
+  DevBuf data, validity, code_map;
+  uint64_t len = 0;
+};
+
+void stage_column(qeg_ctx* ctx, const qeg_column& c, StagedCol& out);
+void stage_sel(qeg_ctx* ctx, const uint32_t* sel, uint64_t n, DevBuf& buf, const uint32_t** dev);
+
+// Checks and clears the context's device error word (syncs the stream).
+void check_device_error(qeg_ctx* ctx);
+
+inline unsigned grid_for(qeg_ctx* ctx, uint64_t work_items, int block, int blocks_per_sm) {
+  const uint64_t want = (work_items + block - 1) / block;
+  const uint64_t cap = static_cast<uint64_t>(ctx->sms) * blocks_per_sm;
+  uint64_t g = want < cap ? want : cap;
+  return static_cast<unsigned>(g == 0 ? 1 : g);
+}
+
+// Copies `count` rows starting at `first` of a device column (values `width`
+// bytes, validity as one byte per row) into a caller output column (host or
+// device), packing validity into 64-bit words.
+void fetch_column(qeg_ctx* ctx, const void* dev_vals, const uint8_t* dev_valid, size_t width,
+                  uint64_t first, uint64_t count, const qeg_out_column& out);
+
+template <class F>
+qeg_status guarded(qeg_ctx* ctx, F&& fn);
+
+}  // namespace qeg
+
+extern thread_local std::string g_qeg_tls_err;
+
+template <class F>
+qeg_status qeg::guarded(qeg_ctx* ctx, F&& fn) {
+  try {
+    fn();
+    return QEG_OK;
+  } catch (const qeg::Error& e) {
+    (ctx ? ctx->err : g_qeg_tls_err) = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    (ctx ? ctx->err : g_qeg_tls_err) = "out of host memory";
+    return QEG_ERR_OOM;
+  } catch (const std::exception& e) {
+    (ctx ? ctx->err : g_qeg_tls_err) = e.what();
+    return QEG_ERR_CUDA;
+  }
+}

@@ -1,0 +1,825 @@
+// qeg_join.cu -- hash equi-join on sm_103a: replaces qe::HashJoin
+// (ops/join.h:69-123, ops/join.cpp).
+//
+// Build (ops/join.cpp:133-197): every build batch is appended to a device
+// BuildStore (column values + one validity byte per row, the GPU form of
+// ops/join_internal.h:38-93). build_finish() then builds a CSR multiplicity
+// map over the rows whose key tuple holds no NULL (NULL keys never match,
+// NullPolicy::kNeverMatch, ops/hashtable.h:36-43):
+//   slot  : a key's position in an open-addressing table (QEG_JOIN_HASH), or
+//           value - min over the key range (QEG_JOIN_DENSE, chosen when the
+//           non-null build keys are integers whose range is at most 4x their
+//           count);
+//   cnt   : build rows per slot; off: exclusive prefix sum of cnt;
+//   rows  : build row ids grouped by slot (the group_rows lists of
+//           ops/join.cpp:190-194, as one array).
+// A build whose keys are all distinct also gets a bitmap (DENSE) or a
+// "unique" flag (HASH) so a probe that only needs the match count reads one
+// bit / one key word per row.
+//
+// Probe: per probe batch, a count kernel sizes each probe row's output (LEFT:
+// at least one row), a scan turns the counts into offsets, an emit kernel
+// writes (probe row, build row | NULL) pairs (build_pairs_for_probe,
+// ops/join.cpp:199-247), and fetch() gathers the output columns, probe columns
+// then build columns (ops/join_internal.h:136-179). The COUNT(*)/SUM(payload)
+// sink is fused into one probe kernel.
+#include <algorithm>
+
+#include "qeg_agg.h"
+#include "qeg_scan.cuh"
+
+namespace qeg {
+
+namespace {
+
+constexpr uint32_t kNullRow = 0xffffffffu;  // ops/join_internal.h:31
+
+struct JTable {
+  int strategy;    // QEG_JOIN_HASH / QEG_JOIN_DENSE
+  int nkeys;
+  int kw;          // words per hash row: 1 (single key) or 1 + nkeys
+  uint64_t* keys;  // hash rows; single key: slot cap holds key word 0
+  uint64_t cap;    // hash: power of two; dense: range
+  int64_t dmin;    // dense: smallest key value
+  uint32_t* cnt;   // cap (+1 hash single key) entries
+  const uint64_t* off;
+  const uint32_t* rows;
+  const uint64_t* bitmap;  // dense and unique: one bit per slot
+  int unique;
+};
+
+__device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Loads the key tuple of row p. Returns false when any key column is NULL.
+__device__ __forceinline__ bool load_key(const DevCol* kc, int nk, uint64_t p, uint64_t* w, uint64_t& h) {
+  h = kHashSeed;
+  for (int j = 0; j < nk; ++j) {
+    if (!col_valid(kc[j], p)) return false;
+    w[j] = key_word(kc[j], p);
+    h = hash_fold(h, w[j]);
+  }
+  return true;
+}
+
+__device__ __forceinline__ int64_t dense_value(const DevCol& c, uint64_t p) { return int_value(c, p); }
+
+// Finds (insert = true: or inserts) the slot of a key tuple. -1: absent / full.
+template <bool INSERT>
+__device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w, uint64_t h, uint32_t* err) {
+  if (T.nkeys == 1) {
+    const uint64_t k = w[0];
+    if (k == 0) return static_cast<int64_t>(T.cap);
+    uint64_t s = h & (T.cap - 1);
+    for (uint64_t t = 0; t < T.cap; ++t) {
+      uint64_t* r = T.keys + s;
+      uint64_t cur = ld_relaxed64(r);
+      if (cur == k) return static_cast<int64_t>(s);
+      if (cur == 0) {
+        if (!INSERT) return -1;
+        cur = atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, static_cast<unsigned long long>(k));
+        if (cur == 0 || cur == k) return static_cast<int64_t>(s);
+      }
+      s = (s + 1) & (T.cap - 1);
+    }
+    return -1;
+  }
+  const uint64_t tag = (h >> 32) | 2ull;
+  uint64_t s = h & (T.cap - 1);
+  for (uint64_t t = 0; t < T.cap; ++t) {
+    uint64_t* r = T.keys + s * T.kw;
+    uint64_t st = ld_relaxed64(r);
+    if (st == 0) {
+      if (!INSERT) return -1;
+      const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, 1ull);
+      if (old == 0) {
+        for (int j = 0; j < T.nkeys; ++j) r[1 + j] = w[j];
+        __threadfence();
+        atomicExch(reinterpret_cast<unsigned long long*>(r), static_cast<unsigned long long>(tag));
+        return static_cast<int64_t>(s);
+      }
+      st = old;
+    }
+    int spins = 0;
+    while (st == 1) {
+      if (++spins > kSpinLimit) {
+        atomicOr(err, kDevSpinTimeout);
+        return -1;
+      }
+      st = ld_relaxed64(r);
+    }
+    if (st == tag) {
+      __threadfence();
+      bool eq = true;
+      for (int j = 0; eq && j < T.nkeys; ++j) eq = ld_relaxed64(r + 1 + j) == w[j];
+      if (eq) return static_cast<int64_t>(s);
+    }
+    s = (s + 1) & (T.cap - 1);
+  }
+  return -1;
+}
+
+struct BuildK {
+  DevCol key[kMaxKeys];
+  int nkeys;
+  uint64_t n;
+  JTable T;
+  uint32_t* fill;
+  uint32_t* rows_out;
+  uint32_t* dup;
+  uint32_t* err;
+};
+
+__global__ void build_count_kernel(BuildK P) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t w[kMaxKeys], h;
+    if (!load_key(P.key, P.nkeys, r, w, h)) continue;
+    int64_t s;
+    if (P.T.strategy == QEG_JOIN_DENSE) {
+      s = dense_value(P.key[0], r) - P.T.dmin;
+    } else {
+      s = hash_slot<true>(P.T, w, h, P.err);
+      if (s < 0) {
+        atomicOr(P.err, kDevSpillOverflow);
+        continue;
+      }
+    }
+    if (atomicAdd(&P.T.cnt[s], 1u) != 0) *P.dup = 1;
+  }
+}
+
+__global__ void build_scatter_kernel(BuildK P) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t w[kMaxKeys], h;
+    if (!load_key(P.key, P.nkeys, r, w, h)) continue;
+    int64_t s;
+    if (P.T.strategy == QEG_JOIN_DENSE) {
+      s = dense_value(P.key[0], r) - P.T.dmin;
+    } else {
+      s = hash_slot<false>(P.T, w, h, P.err);
+      if (s < 0) continue;
+    }
+    const uint64_t pos = P.T.off[s] + atomicAdd(&P.fill[s], 1u);
+    P.rows_out[pos] = static_cast<uint32_t>(r);
+  }
+}
+
+__global__ void dense_bitmap_kernel(const uint32_t* __restrict__ cnt, uint64_t n, uint64_t* __restrict__ bits) {
+  const uint64_t nw = (n + 63) / 64;
+  for (uint64_t wi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wi < nw; wi += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t b = 0;
+    for (int i = 0; i < 64; ++i) {
+      const uint64_t s = wi * 64 + i;
+      if (s < n && cnt[s]) b |= 1ull << i;
+    }
+    bits[wi] = b;
+  }
+}
+
+// Range of the non-null values of one integer key column.
+__global__ void minmax_kernel(DevCol c, uint64_t n, unsigned long long* out /* [0]=min enc, [1]=max enc, [2]=count */) {
+  unsigned long long mn = ~0ull, mx = 0, cnt = 0;
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+    if (!col_valid(c, r)) continue;
+    const unsigned long long e = enc_i64(int_value(c, r));
+    mn = e < mn ? e : mn;
+    mx = e > mx ? e : mx;
+    ++cnt;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = min(mn, __shfl_down_sync(0xffffffffu, mn, o));
+    mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0 && cnt) {
+    atomicMin(out + 0, mn);
+    atomicMax(out + 1, mx);
+    atomicAdd(out + 2, cnt);
+  }
+}
+
+// Slot of a probe key, or -1 on a miss (NULL keys are filtered by the caller).
+__device__ __forceinline__ int64_t probe_slot(const JTable& T, const DevCol* kc, uint64_t p, const uint64_t* w,
+                                              uint64_t h, uint32_t* err) {
+  if (T.strategy == QEG_JOIN_DENSE) {
+    const int64_t v = dense_value(kc[0], p);
+    const uint64_t s = static_cast<uint64_t>(v) - static_cast<uint64_t>(T.dmin);
+    if (v < T.dmin || s >= T.cap) return -1;
+    return static_cast<int64_t>(s);
+  }
+  return hash_slot<false>(T, w, h, err);
+}
+
+struct ProbeK {
+  DevCol key[kMaxKeys];
+  int nkeys;
+  DevCol val;  // count/sum sink payload
+  uint64_t n;
+  JTable T;
+  int left;
+  uint32_t* counts;    // per probe row output rows
+  const uint64_t* starts;
+  uint32_t* out_probe;
+  uint32_t* out_build;
+  unsigned long long* acc;  // sink: [0] count, [1] sum, [2] any payload
+  uint32_t* err;
+};
+
+// The COUNT(*) / SUM(payload) sink of an inner join, fused into the probe.
+template <int STRAT, bool UNIQUE>
+__global__ void __launch_bounds__(512) probe_count_sum_kernel(const ProbeK P) {
+  unsigned long long cnt = 0, sum = 0, seen = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P.n; p += stride) {
+    if (!col_valid(P.key[0], p)) continue;
+    uint64_t m = 0;
+    if (STRAT == QEG_JOIN_DENSE) {
+      const int64_t v = int_value(P.key[0], p);
+      const uint64_t s = static_cast<uint64_t>(v) - static_cast<uint64_t>(P.T.dmin);
+      if (s < P.T.cap) {
+        if (UNIQUE) m = (__ldg(P.T.bitmap + (s >> 6)) >> (s & 63)) & 1ull;
+        else m = __ldg(P.T.cnt + s);
+      }
+    } else {
+      uint64_t w[1];
+      w[0] = key_word(P.key[0], p);
+      const int64_t s = hash_slot<false>(P.T, w, hash_fold(kHashSeed, w[0]), P.err);
+      if (s >= 0) m = (UNIQUE && static_cast<uint64_t>(s) != P.T.cap) ? 1 : __ldg(P.T.cnt + s);
+    }
+    if (m == 0) continue;
+    cnt += m;
+    if (col_valid(P.val, p)) {
+      sum += static_cast<unsigned long long>(int_value(P.val, p)) * m;
+      seen = 1;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    seen |= __shfl_down_sync(0xffffffffu, seen, o);
+  }
+  __shared__ unsigned long long s_acc[3];
+  if (threadIdx.x == 0) s_acc[0] = s_acc[1] = s_acc[2] = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_acc[0], cnt);
+    atomicAdd(&s_acc[1], sum);
+    atomicOr(&s_acc[2], seen);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_acc[0]) atomicAdd(P.acc + 0, s_acc[0]);
+    if (s_acc[1]) atomicAdd(P.acc + 1, s_acc[1]);
+    if (s_acc[2]) atomicOr(P.acc + 2, s_acc[2]);
+  }
+}
+
+__global__ void probe_count_kernel(const ProbeK P) {
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P.n; p += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t w[kMaxKeys], h;
+    uint32_t m = 0;
+    if (load_key(P.key, P.nkeys, p, w, h)) {
+      const int64_t s = probe_slot(P.T, P.key, p, w, h, P.err);
+      if (s >= 0) m = P.T.cnt[s];
+    }
+    if (m == 0 && P.left) m = 1;
+    P.counts[p] = m;
+  }
+}
+
+__global__ void probe_emit_kernel(const ProbeK P) {
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P.n; p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t m = P.counts[p];
+    if (m == 0) continue;
+    uint64_t o = P.starts[p];
+    uint64_t w[kMaxKeys], h;
+    int64_t s = -1;
+    if (load_key(P.key, P.nkeys, p, w, h)) s = probe_slot(P.T, P.key, p, w, h, P.err);
+    if (s < 0 || P.T.cnt[s] == 0) {  // LEFT join, unmatched: one row, build side NULL
+      P.out_probe[o] = static_cast<uint32_t>(p);
+      P.out_build[o] = kNullRow;
+      continue;
+    }
+    const uint64_t b = P.T.off[s];
+    for (uint32_t t = 0; t < m; ++t) {
+      P.out_probe[o + t] = static_cast<uint32_t>(p);
+      P.out_build[o + t] = P.T.rows[b + t];
+    }
+  }
+}
+
+// out[k] = src[idx[k]] (width bytes), valid[k] from the source, NULL where
+// idx[k] is kNullRow. Source validity is either a bitmap (probe columns) or a
+// byte per row (build store).
+__global__ void gather_kernel(const void* __restrict__ src, const uint64_t* __restrict__ src_bits,
+                              const uint8_t* __restrict__ src_bytes, const int32_t* __restrict__ code_map, int width,
+                              const uint32_t* __restrict__ idx, uint64_t n, void* __restrict__ out,
+                              uint8_t* __restrict__ valid) {
+  for (uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t r = idx[k];
+    if (r == kNullRow) {
+      valid[k] = 0;
+      if (width == 8) static_cast<uint64_t*>(out)[k] = 0;
+      else if (width == 4) static_cast<uint32_t*>(out)[k] = 0;
+      else static_cast<uint8_t*>(out)[k] = 0;
+      continue;
+    }
+    uint8_t ok = 1;
+    if (src_bits) ok = (src_bits[r >> 6] >> (r & 63)) & 1ull;
+    else if (src_bytes) ok = src_bytes[r];
+    valid[k] = ok;
+    if (width == 8) static_cast<uint64_t*>(out)[k] = static_cast<const uint64_t*>(src)[r];
+    else if (code_map) static_cast<int32_t*>(out)[k] = ok ? code_map[static_cast<const int32_t*>(src)[r]] : 0;
+    else if (width == 4) static_cast<uint32_t*>(out)[k] = static_cast<const uint32_t*>(src)[r];
+    else static_cast<uint8_t*>(out)[k] = static_cast<const uint8_t*>(src)[r];
+  }
+}
+
+// Appends a batch column into the build store: values are copied, validity is
+// expanded to a byte per row; STR codes are translated to value ids.
+__global__ void store_append_kernel(DevCol c, uint64_t n, int width, void* __restrict__ dst,
+                                    uint8_t* __restrict__ dvalid) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+    const bool ok = col_valid(c, r);
+    dvalid[r] = ok ? 1 : 0;
+    if (c.type == kSTR) {
+      static_cast<int32_t*>(dst)[r] = ok ? static_cast<int32_t>(int_value(c, r)) : 0;
+    } else if (width == 8) {
+      static_cast<uint64_t*>(dst)[r] = __ldg(static_cast<const unsigned long long*>(c.data) + r);
+    } else if (width == 4) {
+      static_cast<uint32_t*>(dst)[r] = __ldg(static_cast<const unsigned int*>(c.data) + r);
+    } else {
+      static_cast<uint8_t*>(dst)[r] = __ldg(static_cast<const uint8_t*>(c.data) + r);
+    }
+  }
+}
+
+uint64_t next_pow2(uint64_t v) {
+  uint64_t c = 1;
+  while (c < v) c <<= 1;
+  return c;
+}
+
+bool dense_capable(int32_t t) { return t == QEG_I32 || t == QEG_I64 || t == QEG_TS || t == QEG_BOOL || t == QEG_STR; }
+
+}  // namespace
+
+struct JoinState {
+  qeg_ctx* ctx = nullptr;
+  std::vector<int32_t> ptypes, btypes;
+  std::vector<uint32_t> pkeys, bkeys;
+  int32_t join_type = QEG_INNER;
+  qeg_join_config cfg{};
+
+  // build store
+  std::vector<DevBuf> bvals, bvalid;
+  uint64_t nbuild = 0, bcap = 0;
+  bool built = false;
+
+  // table
+  int strategy = QEG_JOIN_HASH;
+  DevBuf keys, cnt, off, rows, bitmap;
+  uint64_t cap = 0, distinct = 0, nonnull = 0;
+  int64_t dmin = 0;
+  int unique = 1;
+
+  // last probe batch
+  std::vector<StagedCol> probe_staged;
+  DevBuf counts, starts, out_probe, out_build;
+  uint64_t nout = 0;
+
+  // count/sum sink totals
+  DevBuf acc;
+  bool acc_init = false;
+
+  JTable table() const {
+    JTable T{};
+    T.strategy = strategy;
+    T.nkeys = static_cast<int>(bkeys.size());
+    T.kw = bkeys.size() == 1 ? 1 : 1 + static_cast<int>(bkeys.size());
+    T.keys = keys.get<uint64_t>();
+    T.cap = cap;
+    T.dmin = dmin;
+    T.cnt = cnt.get<uint32_t>();
+    T.off = off.get<uint64_t>();
+    T.rows = rows.get<uint32_t>();
+    T.bitmap = bitmap.get<uint64_t>();
+    T.unique = unique;
+    return T;
+  }
+
+  void append(const qeg_column* cols, int ncols) {
+    require(!built, "build() after build_finish()");
+    require(ncols == static_cast<int>(btypes.size()), "build batch column count does not match the schema");
+    const uint64_t n = cols[0].len;
+    for (int c = 0; c < ncols; ++c) {
+      require(cols[c].type == btypes[c], "build batch column type does not match the schema");
+      require(cols[c].len == n, "build batch columns differ in length");
+    }
+    require(nbuild + n < 0xffffffffull, "the build side holds at most 2^32-2 rows");
+    if (n == 0) return;
+    if (nbuild + n > bcap) {
+      const uint64_t ncap = std::max<uint64_t>(nbuild + n, std::max<uint64_t>(bcap * 2, 4096));
+      for (int c = 0; c < ncols; ++c) {
+        DevBuf v(ncap * type_width(btypes[c]), ctx->stream), ok(ncap, ctx->stream);
+        if (nbuild) {
+          QEG_CUDA(cudaMemcpyAsync(v.get(), bvals[c].get(), nbuild * type_width(btypes[c]), cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
+          QEG_CUDA(cudaMemcpyAsync(ok.get(), bvalid[c].get(), nbuild, cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+        bvals[c] = std::move(v);
+        bvalid[c] = std::move(ok);
+      }
+      bcap = ncap;
+    }
+    for (int c = 0; c < ncols; ++c) {
+      StagedCol s;
+      stage_column(ctx, cols[c], s);
+      const int w = static_cast<int>(type_width(btypes[c]));
+      store_append_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(
+          s.dev, n, w, bvals[c].get<uint8_t>() + nbuild * w, bvalid[c].get<uint8_t>() + nbuild);
+      ctx->launches++;
+      QEG_CUDA(cudaGetLastError());
+    }
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));  // staged inputs die with this scope
+    nbuild += n;
+  }
+
+  // Key columns of the build store as kernel columns (validity as a byte array
+  // is exposed through a bitmap-free path: keys are re-read with col_valid, so
+  // the store keeps a packed bitmap per key column).
+  std::vector<DevBuf> key_bits;
+  DevCol store_key(int j) {
+    DevCol c{};
+    c.type = btypes[bkeys[j]] == QEG_STR ? QEG_I32 : btypes[bkeys[j]];  // STR stored as value ids
+    c.data = bvals[bkeys[j]].get();
+    c.validity = key_bits[j].get<uint64_t>();
+    c.all_valid = 0;
+    c.code_map = nullptr;
+    return c;
+  }
+
+  void finish_build();
+};
+
+namespace {
+
+__global__ void bytes_to_bits_kernel(const uint8_t* __restrict__ b, uint64_t n, uint64_t* __restrict__ w) {
+  const uint64_t nw = (n + 63) / 64;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nw; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t x = 0;
+    for (int k = 0; k < 64; ++k) {
+      const uint64_t r = i * 64 + k;
+      if (r < n && b[r]) x |= 1ull << k;
+    }
+    w[i] = x;
+  }
+}
+
+}  // namespace
+
+void JoinState::finish_build() {
+  require(!built, "build_finish() called twice");
+  built = true;
+  const int nk = static_cast<int>(bkeys.size());
+  key_bits.clear();
+  for (int j = 0; j < nk; ++j) {
+    key_bits.emplace_back(((nbuild + 63) / 64 + 1) * 8, ctx->stream);
+    if (nbuild) {
+      bytes_to_bits_kernel<<<grid_for(ctx, nbuild / 64 + 1, 256, 8), 256, 0, ctx->stream>>>(
+          bvalid[bkeys[j]].get<uint8_t>(), nbuild, key_bits[j].get<uint64_t>());
+      ctx->launches++;
+    }
+  }
+  BuildK P{};
+  P.nkeys = nk;
+  for (int j = 0; j < nk; ++j) P.key[j] = store_key(j);
+  P.n = nbuild;
+  P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+
+  // Strategy: dense when one integer key spans a small range.
+  strategy = cfg.strategy == QEG_JOIN_AUTO ? QEG_JOIN_HASH : cfg.strategy;
+  if (strategy == QEG_JOIN_PARTITIONED) strategy = QEG_JOIN_HASH;
+  nonnull = nbuild;
+  if (nk == 1 && dense_capable(btypes[bkeys[0]]) && nbuild > 0 &&
+      (cfg.strategy == QEG_JOIN_AUTO || cfg.strategy == QEG_JOIN_DENSE)) {
+    DevBuf mm(24, ctx->stream);
+    unsigned long long init[3] = {~0ull, 0ull, 0ull};
+    QEG_CUDA(cudaMemcpyAsync(mm.get(), init, 24, cudaMemcpyHostToDevice, ctx->stream));
+    minmax_kernel<<<grid_for(ctx, nbuild, 256, 8), 256, 0, ctx->stream>>>(P.key[0], nbuild, mm.get<unsigned long long>());
+    ctx->launches++;
+    unsigned long long r[3];
+    QEG_CUDA(cudaMemcpyAsync(r, mm.get(), 24, cudaMemcpyDeviceToHost, ctx->stream));
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+    nonnull = r[2];
+    if (r[2] > 0) {
+      const uint64_t range = (r[1] - r[0]) + 1;  // encodings preserve order; difference = value range
+      if (range != 0 && range <= 4 * r[2] + 64 && range < (1ull << 32)) {
+        strategy = QEG_JOIN_DENSE;
+        dmin = dec_i64(r[0]);
+        cap = range;
+      }
+    }
+    if (strategy != QEG_JOIN_DENSE && cfg.strategy == QEG_JOIN_DENSE) strategy = QEG_JOIN_HASH;
+  }
+  uint64_t slots;
+  if (strategy == QEG_JOIN_DENSE) {
+    slots = cap;
+  } else {
+    cap = std::max<uint64_t>(1024, next_pow2(2 * std::max<uint64_t>(nbuild, 1)));
+    const int kw = nk == 1 ? 1 : 1 + nk;
+    const uint64_t krows = nk == 1 ? cap + 1 : cap;
+    keys.alloc(krows * kw * 8, ctx->stream);
+    QEG_CUDA(cudaMemsetAsync(keys.get(), 0, krows * kw * 8, ctx->stream));
+    slots = nk == 1 ? cap + 1 : cap;
+  }
+  cnt.alloc(slots * 4, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(cnt.get(), 0, slots * 4, ctx->stream));
+  DevBuf dup(4, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(dup.get(), 0, 4, ctx->stream));
+  P.dup = dup.get<uint32_t>();
+  P.T = table();
+  const unsigned g = grid_for(ctx, nbuild, 256, 8);
+  if (nbuild) {
+    build_count_kernel<<<g, 256, 0, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  off.alloc((slots + 1) * 8, ctx->stream);
+  const uint64_t total = exclusive_scan(ctx, cnt.get<uint32_t>(), slots, off.get<uint64_t>());
+  nonnull = total;
+  rows.alloc(std::max<uint64_t>(total, 1) * 4, ctx->stream);
+  DevBuf fill(slots * 4, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(fill.get(), 0, slots * 4, ctx->stream));
+  P.T = table();
+  P.fill = fill.get<uint32_t>();
+  P.rows_out = rows.get<uint32_t>();
+  if (nbuild) {
+    build_scatter_kernel<<<g, 256, 0, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  uint32_t d = 0;
+  QEG_CUDA(cudaMemcpyAsync(&d, dup.get(), 4, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  check_device_error(ctx);
+  unique = d ? 0 : 1;
+  if (strategy == QEG_JOIN_DENSE && unique) {
+    bitmap.alloc(((cap + 63) / 64) * 8, ctx->stream);
+    dense_bitmap_kernel<<<grid_for(ctx, cap / 64 + 1, 256, 8), 256, 0, ctx->stream>>>(cnt.get<uint32_t>(), cap,
+                                                                                    bitmap.get<uint64_t>());
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  // Distinct keys: slots with a nonzero count (dense) or inserted hash rows.
+  distinct = 0;
+  {
+    std::vector<uint32_t> hc(slots);
+    QEG_CUDA(cudaMemcpyAsync(hc.data(), cnt.get(), slots * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t c : hc) distinct += c ? 1 : 0;
+  }
+  acc.alloc(24, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(acc.get(), 0, 24, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+}  // namespace qeg
+
+struct qeg_join {
+  qeg::JoinState st;
+};
+
+using namespace qeg;
+
+namespace {
+
+void validate_probe(const JoinState& st, const qeg_column* cols, int ncols) {
+  require(cols != nullptr, "cols is NULL");
+  require(ncols == static_cast<int>(st.ptypes.size()), "probe batch column count does not match the schema");
+  for (int c = 0; c < ncols; ++c) {
+    require(cols[c].type == st.ptypes[c], "probe batch column type does not match the schema");
+    require(cols[c].len == cols[0].len, "probe batch columns differ in length");
+  }
+}
+
+ProbeK probe_params(JoinState& st, uint64_t n) {
+  ProbeK P{};
+  P.nkeys = static_cast<int>(st.pkeys.size());
+  for (int j = 0; j < P.nkeys; ++j) P.key[j] = st.probe_staged[st.pkeys[j]].dev;
+  P.n = n;
+  P.T = st.table();
+  P.left = st.join_type == QEG_LEFT;
+  P.err = static_cast<uint32_t*>(st.ctx->dev_err.get());
+  return P;
+}
+
+}  // namespace
+
+extern "C" {
+
+qeg_status qeg_join_create(qeg_ctx* ctx, const int32_t* probe_types, int nprobe, const int32_t* build_types,
+                           int nbuild, const uint32_t* probe_keys, const uint32_t* build_keys, int nkeys,
+                           int32_t join_type, const qeg_join_config* cfg, qeg_join** out) {
+  return guarded(ctx, [&] {
+    require(ctx != nullptr && out != nullptr, "ctx/out is NULL");
+    require(nkeys >= 1, "equi-join needs >=1 key");
+    require(nkeys <= kMaxKeys, "GPU join supports at most 8 key columns");
+    require(join_type == QEG_INNER || join_type == QEG_LEFT, "unknown join type");
+    require(nprobe >= 1 && nbuild >= 1, "join sides need >=1 column");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    auto j = std::make_unique<qeg_join>();
+    JoinState& st = j->st;
+    st.ctx = ctx;
+    st.ptypes.assign(probe_types, probe_types + nprobe);
+    st.btypes.assign(build_types, build_types + nbuild);
+    st.pkeys.assign(probe_keys, probe_keys + nkeys);
+    st.bkeys.assign(build_keys, build_keys + nkeys);
+    for (int k = 0; k < nkeys; ++k) {
+      require(st.pkeys[k] < static_cast<uint32_t>(nprobe) && st.bkeys[k] < static_cast<uint32_t>(nbuild),
+              "join key column index out of range");
+      require(st.ptypes[st.pkeys[k]] == st.btypes[st.bkeys[k]],
+              "HashJoin: join key column types must match positionally");
+    }
+    st.join_type = join_type;
+    if (cfg) st.cfg = *cfg;
+    st.bvals.resize(nbuild);
+    st.bvalid.resize(nbuild);
+    *out = j.release();
+  });
+}
+
+qeg_status qeg_join_build(qeg_join* j, const qeg_column* cols, int ncols) {
+  qeg_ctx* ctx = j ? j->st.ctx : nullptr;
+  return guarded(ctx, [&] {
+    require(j != nullptr && cols != nullptr, "join/cols is NULL");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    j->st.append(cols, ncols);
+  });
+}
+
+qeg_status qeg_join_build_finish(qeg_join* j) {
+  qeg_ctx* ctx = j ? j->st.ctx : nullptr;
+  return guarded(ctx, [&] {
+    require(j != nullptr, "join is NULL");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    j->st.finish_build();
+  });
+}
+
+qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64_t* out_rows) {
+  qeg_ctx* ctx = j ? j->st.ctx : nullptr;
+  return guarded(ctx, [&] {
+    require(j != nullptr && out_rows != nullptr, "join/out_rows is NULL");
+    JoinState& st = j->st;
+    require(st.built, "probe() before build_finish()");
+    validate_probe(st, cols, ncols);
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    const uint64_t n = cols[0].len;
+    require(n < 0xffffffffull, "a probe batch holds at most 2^32-2 rows");
+    st.probe_staged.clear();
+    st.probe_staged.resize(ncols);
+    for (int c = 0; c < ncols; ++c) stage_column(ctx, cols[c], st.probe_staged[c]);
+    st.nout = 0;
+    if (n == 0) {
+      *out_rows = 0;
+      return;
+    }
+    st.counts.alloc(n * 4, ctx->stream);
+    st.starts.alloc((n + 1) * 8, ctx->stream);
+    ProbeK P = probe_params(st, n);
+    P.counts = st.counts.get<uint32_t>();
+    const unsigned g = grid_for(ctx, n, 256, 8);
+    probe_count_kernel<<<g, 256, 0, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+    const uint64_t total = exclusive_scan(ctx, st.counts.get<uint32_t>(), n, st.starts.get<uint64_t>());
+    st.out_probe.alloc(std::max<uint64_t>(total, 1) * 4, ctx->stream);
+    st.out_build.alloc(std::max<uint64_t>(total, 1) * 4, ctx->stream);
+    P.starts = st.starts.get<uint64_t>();
+    P.out_probe = st.out_probe.get<uint32_t>();
+    P.out_build = st.out_build.get<uint32_t>();
+    probe_emit_kernel<<<g, 256, 0, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+    check_device_error(ctx);
+    st.nout = total;
+    *out_rows = total;
+  });
+}
+
+qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg_out_column* outs) {
+  qeg_ctx* ctx = j ? j->st.ctx : nullptr;
+  return guarded(ctx, [&] {
+    require(j != nullptr && outs != nullptr, "join/outs is NULL");
+    JoinState& st = j->st;
+    require(first <= st.nout && count <= st.nout - first, "fetch range outside the probed batch's output");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    if (count == 0) {
+      for (size_t c = 0; c < st.ptypes.size() + st.btypes.size(); ++c)
+        if (outs[c].all_valid) *outs[c].all_valid = 1;
+      return;
+    }
+    DevBuf vals(count * 8, ctx->stream), valid(count, ctx->stream);
+    const unsigned g = grid_for(ctx, count, 256, 8);
+    for (size_t c = 0; c < st.ptypes.size(); ++c) {
+      const StagedCol& s = st.probe_staged[c];
+      const int w = static_cast<int>(type_width(st.ptypes[c]));
+      gather_kernel<<<g, 256, 0, ctx->stream>>>(s.dev.data, s.dev.all_valid ? nullptr : s.dev.validity, nullptr,
+                                               st.ptypes[c] == QEG_STR ? s.dev.code_map : nullptr, w,
+                                               st.out_probe.get<uint32_t>() + first, count, vals.get(),
+                                               valid.get<uint8_t>());
+      ctx->launches++;
+      QEG_CUDA(cudaGetLastError());
+      fetch_column(ctx, vals.get(), valid.get<uint8_t>(), w, 0, count, outs[c]);
+    }
+    for (size_t c = 0; c < st.btypes.size(); ++c) {
+      const int w = static_cast<int>(type_width(st.btypes[c]));
+      gather_kernel<<<g, 256, 0, ctx->stream>>>(st.bvals[c].get(), nullptr, st.bvalid[c].get<uint8_t>(), nullptr, w,
+                                               st.out_build.get<uint32_t>() + first, count, vals.get(),
+                                               valid.get<uint8_t>());
+      ctx->launches++;
+      QEG_CUDA(cudaGetLastError());
+      fetch_column(ctx, vals.get(), valid.get<uint8_t>(), w, 0, count, outs[st.ptypes.size() + c]);
+    }
+  });
+}
+
+qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, const qeg_column* probe_val) {
+  qeg_ctx* ctx = j ? j->st.ctx : nullptr;
+  return guarded(ctx, [&] {
+    require(j != nullptr && probe_key != nullptr && probe_val != nullptr, "join/columns are NULL");
+    JoinState& st = j->st;
+    require(st.built, "probe before build_finish()");
+    require(st.bkeys.size() == 1, "the count/sum sink takes a single key column");
+    require(st.join_type == QEG_INNER, "the count/sum sink is an inner join");
+    require(probe_key->type == st.btypes[st.bkeys[0]], "probe key type does not match the build key type");
+    require(probe_val->type != QEG_F64 && probe_val->type != QEG_STR, "the count/sum sink sums an integer column");
+    require(probe_key->len == probe_val->len, "probe columns differ in length");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    const uint64_t n = probe_key->len;
+    if (n == 0 || st.nonnull == 0) return;
+    StagedCol k, v;
+    stage_column(ctx, *probe_key, k);
+    stage_column(ctx, *probe_val, v);
+    ProbeK P{};
+    P.nkeys = 1;
+    P.key[0] = k.dev;
+    P.val = v.dev;
+    P.n = n;
+    P.T = st.table();
+    P.acc = st.acc.get<unsigned long long>();
+    P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+    int per_sm = 0;
+    const int block = 512;
+    const unsigned g0 = static_cast<unsigned>(std::min<uint64_t>((n + block - 1) / block, ctx->sms * 4ull));
+    if (st.strategy == QEG_JOIN_DENSE) {
+      if (st.unique) probe_count_sum_kernel<QEG_JOIN_DENSE, true><<<g0, block, 0, ctx->stream>>>(P);
+      else probe_count_sum_kernel<QEG_JOIN_DENSE, false><<<g0, block, 0, ctx->stream>>>(P);
+    } else {
+      if (st.unique) probe_count_sum_kernel<QEG_JOIN_HASH, true><<<g0, block, 0, ctx->stream>>>(P);
+      else probe_count_sum_kernel<QEG_JOIN_HASH, false><<<g0, block, 0, ctx->stream>>>(P);
+    }
+    (void)per_sm;
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));  // staged inputs die with this scope
+  });
+}
+
+qeg_status qeg_join_count_sum_result(qeg_join* j, int64_t* count, int64_t* sum, int32_t* sum_valid) {
+  qeg_ctx* ctx = j ? j->st.ctx : nullptr;
+  return guarded(ctx, [&] {
+    require(j != nullptr && count && sum && sum_valid, "NULL argument");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    unsigned long long a[3] = {0, 0, 0};
+    if (j->st.acc.get()) {
+      QEG_CUDA(cudaMemcpyAsync(a, j->st.acc.get(), 24, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    check_device_error(ctx);
+    *count = static_cast<int64_t>(a[0]);
+    *sum = static_cast<int64_t>(a[1]);
+    *sum_valid = a[2] ? 1 : 0;
+  });
+}
+
+qeg_status qeg_join_stats(const qeg_join* j, int32_t* strategy, int32_t* partition_bits, uint64_t* distinct_keys) {
+  qeg_ctx* ctx = j ? j->st.ctx : nullptr;
+  return guarded(ctx, [&] {
+    require(j != nullptr, "join is NULL");
+    if (strategy) *strategy = j->st.strategy;
+    if (partition_bits) *partition_bits = 0;
+    if (distinct_keys) *distinct_keys = j->st.distinct;
+  });
+}
+
+void qeg_join_destroy(qeg_join* j) {
+  if (!j) return;
+  cudaSetDevice(j->st.ctx->device);
+  delete j;
+}
+
+}  // extern "C"

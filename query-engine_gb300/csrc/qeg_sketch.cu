@@ -1,0 +1,277 @@
+// qeg_sketch.cu -- on-device sketch of a key column: HyperLogLog registers,
+// a count-min sketch and heavy-hitter candidates over a strided sample. The
+// sketch is the input of the distinct-group estimator that sizes the GROUP BY
+// table and picks its strategy (the reference sizes by growth only,
+// ops/hashtable.h:83-94; results never depend on the estimate, because an
+// overflowing table is grown and the affected rows replayed).
+#include <algorithm>
+#include <cmath>
+
+#include "qeg_agg.h"
+
+namespace qeg {
+
+namespace {
+
+constexpr int kHllP = 14;
+constexpr int kHllM = 1 << kHllP;
+constexpr int kCmsDepth = 4;
+constexpr int kCmsWidth = 2048;
+constexpr int kCandLocal = 1024;
+constexpr int kCandGlobal = 8192;
+constexpr int kSampleBlock = 256;
+
+struct SketchK {
+  DevCol key;
+  const uint32_t* sel;
+  uint64_t nrows, len;
+  uint64_t stride;   // rows between the starts of consecutive sample blocks
+  uint64_t nblocks;  // sample blocks
+  uint32_t* hll;     // kHllM
+  uint32_t* cms;     // kCmsDepth * kCmsWidth
+  unsigned long long* cand_key;  // kCandGlobal
+  unsigned long long* cand_cnt;  // kCandGlobal
+  unsigned long long* stats;     // [0] sampled rows, [1] sampled nulls
+  uint32_t* err;
+};
+
+__device__ __forceinline__ uint64_t sketch_hash(uint64_t w) { return mix64(w ^ 0x243F6A8885A308D3ull); }
+
+__global__ void __launch_bounds__(kSampleBlock) sketch_kernel(const SketchK P) {
+  extern __shared__ uint32_t sh[];
+  uint32_t* hll = sh;                                  // kHllM
+  uint32_t* cms = hll + kHllM;                         // kCmsDepth * kCmsWidth
+  unsigned long long* ck = reinterpret_cast<unsigned long long*>(cms + kCmsDepth * kCmsWidth);
+  uint32_t* cc = reinterpret_cast<uint32_t*>(ck + kCandLocal);
+  for (int i = threadIdx.x; i < kHllM + kCmsDepth * kCmsWidth; i += blockDim.x) sh[i] = 0;
+  for (int i = threadIdx.x; i < kCandLocal; i += blockDim.x) {
+    ck[i] = 0;
+    cc[i] = 0;
+  }
+  __shared__ unsigned long long s_rows, s_nulls;
+  if (threadIdx.x == 0) s_rows = s_nulls = 0;
+  __syncthreads();
+  unsigned long long rows = 0, nulls = 0;
+  for (uint64_t b = blockIdx.x; b < P.nblocks; b += gridDim.x) {
+    const uint64_t i = b * P.stride + threadIdx.x;
+    if (i >= P.nrows) continue;
+    uint64_t p = i;
+    if (P.sel) {
+      p = P.sel[i];
+      if (p >= P.len) {
+        atomicOr(P.err, kDevBadInput);
+        continue;
+      }
+    }
+    ++rows;
+    if (!col_valid(P.key, p)) {
+      ++nulls;
+      continue;
+    }
+    const uint64_t w = key_word(P.key, p);
+    const uint64_t h = sketch_hash(w);
+    const uint32_t idx = static_cast<uint32_t>(h >> (64 - kHllP));
+    const uint64_t rest = (h << kHllP) | (1ull << (kHllP - 1));
+    const uint32_t rho = static_cast<uint32_t>(__clzll(static_cast<long long>(rest))) + 1;
+    atomicMax(&hll[idx], rho);
+#pragma unroll
+    for (int d = 0; d < kCmsDepth; ++d) {
+      const uint32_t c = static_cast<uint32_t>(mix64(h + 0x9E3779B97F4A7C15ull * (d + 1)) >> 40) & (kCmsWidth - 1);
+      atomicAdd(&cms[d * kCmsWidth + c], 1u);
+    }
+    // First-come candidate table: a key seen early and often stays resident.
+    uint32_t s = static_cast<uint32_t>(h) & (kCandLocal - 1);
+    const unsigned long long kk = w + 1;  // 0 marks an empty candidate slot
+    for (int t = 0; t < 8; ++t) {
+      unsigned long long cur = ck[s];
+      if (cur == 0) cur = atomicCAS(&ck[s], 0ull, kk);
+      if (cur == 0 || cur == kk) {
+        atomicAdd(&cc[s], 1u);
+        break;
+      }
+      s = (s + 1) & (kCandLocal - 1);
+    }
+  }
+  atomicAdd(&s_rows, rows);
+  atomicAdd(&s_nulls, nulls);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kHllM; i += blockDim.x)
+    if (hll[i]) atomicMax(&P.hll[i], hll[i]);
+  for (int i = threadIdx.x; i < kCmsDepth * kCmsWidth; i += blockDim.x)
+    if (cms[i]) atomicAdd(&P.cms[i], cms[i]);
+  for (int i = threadIdx.x; i < kCandLocal; i += blockDim.x) {
+    if (cc[i] < 2) continue;
+    const unsigned long long kk = ck[i];
+    uint32_t s = static_cast<uint32_t>(mix64(kk)) & (kCandGlobal - 1);
+    for (int t = 0; t < 32; ++t) {
+      unsigned long long cur = atomicCAS(&P.cand_key[s], 0ull, kk);
+      if (cur == 0 || cur == kk) {
+        atomicAdd(&P.cand_cnt[s], static_cast<unsigned long long>(cc[i]));
+        break;
+      }
+      s = (s + 1) & (kCandGlobal - 1);
+    }
+  }
+  if (threadIdx.x == 0) {
+    atomicAdd(&P.stats[0], s_rows);
+    atomicAdd(&P.stats[1], s_nulls);
+  }
+}
+
+double hll_estimate(const std::vector<uint32_t>& regs) {
+  const double m = kHllM;
+  double sum = 0;
+  int zeros = 0;
+  for (uint32_t r : regs) {
+    sum += std::ldexp(1.0, -static_cast<int>(r));
+    if (r == 0) ++zeros;
+  }
+  const double alpha = 0.7213 / (1.0 + 1.079 / m);
+  double e = alpha * m * m / sum;
+  if (e <= 2.5 * m && zeros > 0) e = m * std::log(m / zeros);  // linear counting
+  return e;
+}
+
+}  // namespace
+
+void sketch_key_column(qeg_ctx* ctx, const DevCol& key, const uint32_t* sel, uint64_t nrows, uint64_t len,
+                       uint64_t sample_target, int want_heavy, SketchResult& out) {
+  out = SketchResult{};
+  out.total_rows = static_cast<double>(nrows);
+  const uint64_t target_blocks = std::max<uint64_t>(1, sample_target / kSampleBlock);
+  uint64_t stride = kSampleBlock;
+  uint64_t nblocks = (nrows + kSampleBlock - 1) / kSampleBlock;
+  if (nblocks > target_blocks) {
+    stride = ((nrows / target_blocks) / kSampleBlock) * kSampleBlock;
+    if (stride < kSampleBlock) stride = kSampleBlock;
+    nblocks = (nrows + stride - 1) / stride;
+  }
+  const size_t words = kHllM + kCmsDepth * kCmsWidth;
+  DevBuf buf(words * 4 + kCandGlobal * 16 + 16, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(buf.get(), 0, buf.bytes(), ctx->stream));
+  SketchK P{};
+  P.key = key;
+  P.sel = sel;
+  P.nrows = nrows;
+  P.len = len;
+  P.stride = stride;
+  P.nblocks = nblocks;
+  P.hll = buf.get<uint32_t>();
+  P.cms = P.hll + kHllM;
+  P.cand_key = reinterpret_cast<unsigned long long*>(P.cms + kCmsDepth * kCmsWidth);
+  P.cand_cnt = P.cand_key + kCandGlobal;
+  P.stats = P.cand_cnt + kCandGlobal;
+  P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+  const size_t sb = words * 4 + kCandLocal * 12;
+  QEG_CUDA(cudaFuncSetAttribute(sketch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+  const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(nblocks, ctx->sms * 2ull));
+  if (nblocks > 0) {
+    sketch_kernel<<<grid, kSampleBlock, sb, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  std::vector<uint32_t> regs(words);
+  std::vector<unsigned long long> cand(2 * kCandGlobal + 2);
+  QEG_CUDA(cudaMemcpyAsync(regs.data(), buf.get(), words * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaMemcpyAsync(cand.data(), P.cand_key, cand.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  check_device_error(ctx);
+
+  const std::vector<uint32_t> hll(regs.begin(), regs.begin() + kHllM);
+  out.sample_rows = static_cast<double>(cand[2 * kCandGlobal]);
+  const double nulls = static_cast<double>(cand[2 * kCandGlobal + 1]);
+  out.null_frac = out.sample_rows > 0 ? nulls / out.sample_rows : 0;
+  const double nonnull = out.sample_rows - nulls;
+  out.hll_estimate = nonnull > 0 ? hll_estimate(hll) : 0;
+
+  // Candidates ranked by their count-min estimate.
+  auto cms_est = [&](uint64_t w) {
+    const uint64_t h = mix64(w ^ 0x243F6A8885A308D3ull);
+    uint32_t best = UINT32_MAX;
+    for (int d = 0; d < kCmsDepth; ++d) {
+      const uint32_t c = static_cast<uint32_t>(mix64(h + 0x9E3779B97F4A7C15ull * (d + 1)) >> 40) & (kCmsWidth - 1);
+      best = std::min(best, regs[kHllM + d * kCmsWidth + c]);
+    }
+    return best;
+  };
+  std::vector<std::pair<uint32_t, uint64_t>> ranked;
+  for (int i = 0; i < kCandGlobal; ++i)
+    if (cand[i]) ranked.push_back({cms_est(cand[i] - 1), cand[i] - 1});
+  std::sort(ranked.begin(), ranked.end(), [](auto& a, auto& b) { return a.first > b.first; });
+
+  // Features: 64 normalised HLL register-value bins, then 16 frequency features.
+  float* f = out.features;
+  for (int i = 0; i < kSketchFeatures; ++i) f[i] = 0;
+  for (uint32_t r : hll) f[std::min<uint32_t>(r, 63)] += 1.0f / kHllM;
+  double cum = 0;
+  size_t k = 0;
+  for (int i = 0; i < 12; ++i) {
+    const size_t upto = size_t(1) << i;
+    while (k < ranked.size() && k < upto) cum += ranked[k++].first;
+    out.top_share[i] = nonnull > 0 ? std::min(1.0, cum / nonnull) : 0;
+  }
+  for (int i = 0; i < 10; ++i) f[64 + i] = static_cast<float>(out.top_share[i]);
+  double f2 = 0;
+  for (int c = 0; c < kCmsWidth; ++c) {
+    const double v = regs[kHllM + c];
+    f2 += v * v;
+  }
+  f[74] = nonnull > 0 ? static_cast<float>(f2 / (nonnull * nonnull)) : 0.f;
+  f[75] = static_cast<float>(std::log2(1.0 + out.sample_rows) / 32.0);
+  f[76] = static_cast<float>(std::log2(1.0 + out.total_rows) / 32.0);
+  f[77] = out.total_rows > 0 ? static_cast<float>(out.sample_rows / out.total_rows) : 1.f;
+  f[78] = static_cast<float>(out.null_frac);
+  f[79] = nonnull > 0 ? static_cast<float>(std::min(1.0, out.hll_estimate / nonnull)) : 0.f;
+
+  const size_t nh = std::min<size_t>(ranked.size(), static_cast<size_t>(std::max(0, want_heavy)));
+  for (size_t i = 0; i < nh; ++i) out.heavy.push_back(ranked[i].second);
+}
+
+double classic_estimate(const SketchResult& s) {
+  // Distinct count of the sample from HyperLogLog, scaled to the population by
+  // inverting E[d_sample] = D (1 - (1 - 1/D)^m) (a uniform-frequency model),
+  // plus the NULL group. Skewed data breaks the uniform model; that is what the
+  // learned estimator corrects.
+  const double nonnull_rows = s.total_rows * (1.0 - s.null_frac);
+  const double m = s.sample_rows * (1.0 - s.null_frac);
+  double d = s.hll_estimate;
+  if (m <= 0) return s.null_frac > 0 ? 1.0 : 0.0;
+  if (s.sample_rows < s.total_rows && d > 0) {
+    if (d >= m * 0.999) {
+      d = nonnull_rows;  // every sampled row distinct: assume all distinct
+    } else {
+      double lo = d, hi = std::max(d, nonnull_rows);
+      for (int it = 0; it < 100; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        const double e = mid * (1.0 - std::exp(m * std::log1p(-1.0 / std::max(mid, 1.0 + 1e-9))));
+        if (e < d) lo = mid;
+        else hi = mid;
+      }
+      d = 0.5 * (lo + hi);
+    }
+  }
+  d = std::min(d, nonnull_rows);
+  return d + (s.null_frac > 0 ? 1.0 : 0.0);
+}
+
+double AggState::estimate_groups(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len,
+                                 const uint32_t* dsel) {
+  if (mode != 1 || nrows == 0) {
+    // Composite keys: bounded by the row count (grown on overflow).
+    return static_cast<double>(std::min<uint64_t>(std::max<uint64_t>(nrows, 1), 1ull << 22));
+  }
+  SketchResult s;
+  const int want_heavy = (cfg.hot_keys != 0) ? 4096 : 0;
+  sketch_key_column(ctx, staged[keys[0]].dev, dsel, nrows, len, 1u << 20, want_heavy, s);
+  double groups = 0, share = 0;
+  if (learned_estimate(ctx, s, &groups, &share)) {
+    hot_share = share;
+  } else {
+    groups = classic_estimate(s);
+    hot_share = s.top_share[11];
+  }
+  heavy_candidates = s.heavy;
+  return std::max(groups, 1.0);
+}
+
+}  // namespace qeg

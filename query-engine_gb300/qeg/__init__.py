@@ -1,0 +1,379 @@
+"""Python binding of the qeg C ABI (include/qeg.h) through ctypes.
+
+Columns are numpy arrays (host memory: copied to the GPU inside each call) or
+torch CUDA tensors (device memory: used in place). The library is loaded from
+query-engine_gb300/libqeg.so; a missing library raises, there is no fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "libqeg.so")
+
+I32, I64, F64, BOOL, TS, STR = 0, 1, 2, 3, 4, 5
+COUNT_STAR, COUNT, SUM, MIN, MAX, AVG = 0, 1, 2, 3, 4, 5
+INNER, LEFT = 0, 1
+AGG_AUTO, AGG_SMEM, AGG_GLOBAL = 0, 1, 2
+SIZE_LEARNED, SIZE_FIXED = 0, 1
+JOIN_AUTO, JOIN_HASH, JOIN_PARTITIONED, JOIN_DENSE = 0, 1, 2, 3
+
+WIDTH = {I32: 4, I64: 8, F64: 8, BOOL: 1, TS: 8, STR: 4}
+NP_DTYPE = {I32: np.int32, I64: np.int64, F64: np.float64, BOOL: np.uint8, TS: np.int64, STR: np.int32}
+
+STATUS = {0: "OK", -1: "INVALID", -2: "OVERFLOW", -3: "OOM", -4: "CUDA", -5: "TIMEOUT",
+          -6: "UNSUPPORTED", -7: "NO_DEVICE"}
+
+
+class QegError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class Column(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("all_valid", ctypes.c_int32), ("len", ctypes.c_uint64),
+                ("data", ctypes.c_void_p), ("validity", ctypes.c_void_p),
+                ("code_map", ctypes.c_void_p), ("code_map_len", ctypes.c_uint64)]
+
+
+class OutColumn(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("validity", ctypes.c_void_p), ("all_valid", ctypes.c_void_p)]
+
+
+class AggSpec(ctypes.Structure):
+    _fields_ = [("func", ctypes.c_int32), ("input_col", ctypes.c_uint32)]
+
+
+class AggConfig(ctypes.Structure):
+    _fields_ = [("strategy", ctypes.c_int32), ("sizing", ctypes.c_int32),
+                ("initial_capacity", ctypes.c_uint64), ("expected_groups", ctypes.c_uint64),
+                ("block_threads", ctypes.c_int32), ("rows_per_thread", ctypes.c_int32),
+                ("smem_slots", ctypes.c_int32), ("hot_keys", ctypes.c_int32)]
+
+
+class JoinConfig(ctypes.Structure):
+    _fields_ = [("strategy", ctypes.c_int32), ("partition_bits", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libqeg.so (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libqeg.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        vp, u64, i32, c = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_int
+        P = ctypes.POINTER
+        sig = {
+            "qeg_ctx_create": (i32, [c, P(vp)]),
+            "qeg_ctx_destroy": (None, [vp]),
+            "qeg_last_error": (ctypes.c_char_p, [vp]),
+            "qeg_ctx_stream": (vp, [vp]),
+            "qeg_ctx_synchronize": (i32, [vp]),
+            "qeg_ctx_kernel_launches": (u64, [vp]),
+            "qeg_agg_create": (i32, [vp, vp, c, vp, c, vp, c, vp, P(vp)]),
+            "qeg_agg_consume": (i32, [vp, vp, c, vp, u64]),
+            "qeg_agg_finish": (i32, [vp, P(u64)]),
+            "qeg_agg_result_types": (i32, [vp, vp]),
+            "qeg_agg_fetch": (i32, [vp, u64, u64, vp]),
+            "qeg_agg_stats": (i32, [vp, P(u64), P(ctypes.c_uint32), P(i32), P(i32), P(ctypes.c_double)]),
+            "qeg_agg_destroy": (None, [vp]),
+        }
+        optional = {
+            "qeg_join_create": (i32, [vp, vp, c, vp, c, vp, vp, c, i32, vp, P(vp)]),
+            "qeg_join_build": (i32, [vp, vp, c]),
+            "qeg_join_build_finish": (i32, [vp]),
+            "qeg_join_probe": (i32, [vp, vp, c, P(u64)]),
+            "qeg_join_fetch": (i32, [vp, u64, u64, vp]),
+            "qeg_join_probe_count_sum": (i32, [vp, vp, vp]),
+            "qeg_join_count_sum_result": (i32, [vp, P(ctypes.c_int64), P(ctypes.c_int64), P(i32)]),
+            "qeg_join_stats": (i32, [vp, P(i32), P(i32), P(u64)]),
+            "qeg_join_destroy": (None, [vp]),
+        }
+        for name, (res, args) in list(sig.items()) + list(optional.items()):
+            if not hasattr(L, name):
+                if name in sig:
+                    raise RuntimeError("libqeg.so lacks %s" % name)
+                continue
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status, ctx_ptr):
+    if status != 0:
+        msg = lib().qeg_last_error(ctx_ptr)
+        raise QegError(status, msg.decode() if msg else "")
+
+
+def _ptr(a):
+    """Address of a numpy array or torch tensor (None -> NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+def _len(a):
+    return a.shape[0] if isinstance(a, np.ndarray) else a.numel()
+
+
+def pack_validity(valid):
+    """Packs a boolean mask (True = valid) into 64-bit LSB-first words."""
+    valid = np.asarray(valid, dtype=bool)
+    n = len(valid)
+    nw = (n + 63) // 64
+    padded = np.ones(nw * 64, dtype=bool)
+    padded[:n] = valid
+    return np.packbits(padded, bitorder="little").view(np.uint64).copy()
+
+
+def unpack_validity(words, n):
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    b = words.view(np.uint8).reshape(-1, 8)
+    bits = np.unpackbits(b, axis=1, bitorder="little").reshape(-1)
+    return bits[:n].astype(bool)
+
+
+class Col:
+    """A column view: values (numpy or torch CUDA), optional validity words,
+    optional STR code map. Keeps the referenced buffers alive."""
+
+    def __init__(self, values, validity=None, type=None, code_map=None):
+        self.values = values
+        self.validity = validity
+        self.code_map = code_map
+        if type is None:
+            dt = str(values.dtype)
+            type = {"int32": I32, "torch.int32": I32, "int64": I64, "torch.int64": I64,
+                    "float64": F64, "torch.float64": F64, "uint8": BOOL, "torch.uint8": BOOL,
+                    "bool": BOOL, "torch.bool": BOOL}[dt]
+        self.type = type
+        self.n = _len(values)
+
+    def c(self):
+        cm = self.code_map
+        return Column(self.type, 1 if self.validity is None else 0, self.n, _ptr(self.values),
+                      _ptr(self.validity), _ptr(cm), 0 if cm is None else _len(cm))
+
+
+def _cols(cols):
+    arr = (Column * max(1, len(cols)))()
+    for i, c in enumerate(cols):
+        arr[i] = c.c()
+    return arr
+
+
+class Context:
+    def __init__(self, device=0):
+        p = ctypes.c_void_p()
+        st = lib().qeg_ctx_create(device, ctypes.byref(p))
+        if st != 0:
+            msg = lib().qeg_last_error(None)
+            raise QegError(st, msg.decode() if msg else "")
+        self.p = p
+
+    @property
+    def stream(self):
+        return lib().qeg_ctx_stream(self.p)
+
+    def synchronize(self):
+        _check(lib().qeg_ctx_synchronize(self.p), self.p)
+
+    @property
+    def launches(self):
+        return lib().qeg_ctx_kernel_launches(self.p)
+
+    def close(self):
+        if self.p:
+            lib().qeg_ctx_destroy(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def agg_config(strategy=AGG_AUTO, sizing=SIZE_LEARNED, initial_capacity=0, expected_groups=0,
+               block_threads=0, rows_per_thread=0, smem_slots=0, hot_keys=0):
+    return AggConfig(strategy, sizing, initial_capacity, expected_groups, block_threads,
+                     rows_per_thread, smem_slots, hot_keys)
+
+
+class Aggregate:
+    """The GPU GROUP BY operator state behind one qeg_agg."""
+
+    def __init__(self, ctx, col_types, key_cols, aggs, config=None):
+        self.ctx = ctx
+        self.ncols = len(col_types)
+        self.nkeys = len(key_cols)
+        self.naggs = len(aggs)
+        types = (ctypes.c_int32 * len(col_types))(*col_types)
+        keys = (ctypes.c_uint32 * max(1, len(key_cols)))(*key_cols)
+        specs = (AggSpec * max(1, len(aggs)))()
+        for i, (f, c) in enumerate(aggs):
+            specs[i] = AggSpec(f, c)
+        cfg = config if config is not None else agg_config()
+        p = ctypes.c_void_p()
+        _check(lib().qeg_agg_create(ctx.p, types, len(col_types), keys, len(key_cols), specs,
+                                    len(aggs), ctypes.byref(cfg), ctypes.byref(p)), ctx.p)
+        self.p = p
+        rt = (ctypes.c_int32 * (self.nkeys + self.naggs))()
+        _check(lib().qeg_agg_result_types(p, rt), ctx.p)
+        self.result_types = list(rt)
+        self.rows = None
+
+    def consume(self, cols, sel=None):
+        arr = _cols(cols)
+        _check(lib().qeg_agg_consume(self.p, arr, len(cols), _ptr(sel), 0 if sel is None else _len(sel)),
+               self.ctx.p)
+
+    def finish(self):
+        n = ctypes.c_uint64()
+        _check(lib().qeg_agg_finish(self.p, ctypes.byref(n)), self.ctx.p)
+        self.rows = n.value
+        return self.rows
+
+    def fetch(self, first=0, count=None):
+        """Returns [(values ndarray, valid bool ndarray)] for keys then aggregates."""
+        if count is None:
+            count = self.rows - first
+        outs = (OutColumn * len(self.result_types))()
+        keep = []
+        for i, t in enumerate(self.result_types):
+            v = np.zeros(max(count, 1), dtype=NP_DTYPE[t])
+            w = np.zeros(max(1, (count + 63) // 64), dtype=np.uint64)
+            av = np.zeros(1, dtype=np.int32)
+            keep.append((v, w, av))
+            outs[i] = OutColumn(v.ctypes.data, w.ctypes.data, av.ctypes.data)
+        _check(lib().qeg_agg_fetch(self.p, first, count, outs), self.ctx.p)
+        return [(v[:count], unpack_validity(w, count)) for v, w, _ in keep]
+
+    def stats(self):
+        cap, rs, st, hk, est = (ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_int32(),
+                                ctypes.c_double())
+        _check(lib().qeg_agg_stats(self.p, ctypes.byref(cap), ctypes.byref(rs), ctypes.byref(st),
+                                   ctypes.byref(hk), ctypes.byref(est)), self.ctx.p)
+        return {"capacity": cap.value, "resizes": rs.value, "strategy": st.value, "hot_keys": hk.value,
+                "est_groups": est.value}
+
+    def close(self):
+        if self.p:
+            lib().qeg_agg_destroy(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def groupby(ctx, cols, key_cols, aggs, config=None, batch_rows=None, sel=None):
+    """Runs a whole GROUP BY: create, consume (in batches of batch_rows when
+    given), finish, fetch. Returns [(values, valid)] keys then aggregates."""
+    a = Aggregate(ctx, [c.type for c in cols], key_cols, aggs, config)
+    try:
+        n = cols[0].n if cols else 0
+        if batch_rows is None or batch_rows >= n:
+            a.consume(cols, sel)
+        else:
+            for s in range(0, n, batch_rows):
+                e = min(n, s + batch_rows)
+                part = []
+                for c in cols:
+                    v = c.values[s:e]
+                    w = None
+                    if c.validity is not None:
+                        assert s % 64 == 0
+                        w = c.validity[s // 64:(e + 63) // 64]
+                    part.append(Col(v, w, c.type, c.code_map))
+                a.consume(part)
+        a.finish()
+        return a.fetch()
+    finally:
+        a.close()
+
+
+class Join:
+    """The GPU hash-join operator state behind one qeg_join."""
+
+    def __init__(self, ctx, probe_types, build_types, probe_keys, build_keys, join_type=INNER,
+                 strategy=JOIN_AUTO, partition_bits=0):
+        self.ctx = ctx
+        self.probe_types = list(probe_types)
+        self.build_types = list(build_types)
+        pt = (ctypes.c_int32 * max(1, len(probe_types)))(*probe_types)
+        bt = (ctypes.c_int32 * max(1, len(build_types)))(*build_types)
+        pk = (ctypes.c_uint32 * len(probe_keys))(*probe_keys)
+        bk = (ctypes.c_uint32 * len(build_keys))(*build_keys)
+        cfg = JoinConfig(strategy, partition_bits)
+        p = ctypes.c_void_p()
+        _check(lib().qeg_join_create(ctx.p, pt, len(probe_types), bt, len(build_types), pk, bk,
+                                     len(probe_keys), join_type, ctypes.byref(cfg), ctypes.byref(p)), ctx.p)
+        self.p = p
+        self.rows = 0
+
+    def build(self, cols):
+        _check(lib().qeg_join_build(self.p, _cols(cols), len(cols)), self.ctx.p)
+
+    def build_finish(self):
+        _check(lib().qeg_join_build_finish(self.p), self.ctx.p)
+
+    def probe(self, cols):
+        n = ctypes.c_uint64()
+        _check(lib().qeg_join_probe(self.p, _cols(cols), len(cols), ctypes.byref(n)), self.ctx.p)
+        self.rows = n.value
+        return self.rows
+
+    def fetch(self, first=0, count=None):
+        if count is None:
+            count = self.rows - first
+        types = self.probe_types + self.build_types
+        outs = (OutColumn * len(types))()
+        keep = []
+        for i, t in enumerate(types):
+            v = np.zeros(max(count, 1), dtype=NP_DTYPE[t])
+            w = np.zeros(max(1, (count + 63) // 64), dtype=np.uint64)
+            av = np.zeros(1, dtype=np.int32)
+            keep.append((v, w, av))
+            outs[i] = OutColumn(v.ctypes.data, w.ctypes.data, av.ctypes.data)
+        _check(lib().qeg_join_fetch(self.p, first, count, outs), self.ctx.p)
+        return [(v[:count], unpack_validity(w, count)) for v, w, _ in keep]
+
+    def probe_count_sum(self, key, val):
+        k, v = Column(), Column()
+        k, v = key.c(), val.c()
+        _check(lib().qeg_join_probe_count_sum(self.p, ctypes.byref(k), ctypes.byref(v)), self.ctx.p)
+
+    def count_sum(self):
+        c, s, ok = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int32()
+        _check(lib().qeg_join_count_sum_result(self.p, ctypes.byref(c), ctypes.byref(s), ctypes.byref(ok)),
+               self.ctx.p)
+        return c.value, (s.value if ok.value else None)
+
+    def stats(self):
+        st, pb, dk = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint64()
+        _check(lib().qeg_join_stats(self.p, ctypes.byref(st), ctypes.byref(pb), ctypes.byref(dk)), self.ctx.p)
+        return {"strategy": st.value, "partition_bits": pb.value, "distinct_keys": dk.value}
+
+    def close(self):
+        if self.p:
+            lib().qeg_join_destroy(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

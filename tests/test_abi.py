@@ -1,0 +1,69 @@
+"""CPU-side checks of the drop-in boundary: libqeg.so loads and exports every
+entry point include/qeg.h declares; the host-side validity packing matches
+the reference's bitmap layout (core/validity.h:21-40 of the reference)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+
+import qeg
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in os.listdir(os.path.join(REPO, "include")):
+        if h.endswith(".h"):
+            src = open(os.path.join(REPO, "include", h)).read()
+            names |= set(re.findall(r"\b(qeg_[a-z0-9_]+)\s*\(", src))
+    return names
+
+
+def _ensure_built():
+    if not os.path.exists(qeg.LIB_PATH):
+        import build as qbuild
+
+        qbuild.build()
+
+
+def test_library_exports_every_declared_symbol():
+    _ensure_built()
+    L = ctypes.CDLL(qeg.LIB_PATH)
+    missing = [n for n in sorted(_declared()) if not hasattr(L, n)]
+    assert not missing, "declared in include/*.h but not exported: %s" % missing
+    out = subprocess.run(["nm", "-D", "--defined-only", qeg.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (qeg_[a-z0-9_]+)", out))
+    assert _declared() <= exported
+
+
+def test_context_without_gpu_reports_no_device():
+    _ensure_built()
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            return
+    except ImportError:
+        pass
+    try:
+        qeg.Context(0)
+    except qeg.QegError as e:
+        assert e.code == -7  # QEG_ERR_NO_DEVICE
+    else:
+        raise AssertionError("context creation without a GPU must fail loudly")
+
+
+def test_validity_packing_layout():
+    rng = np.random.default_rng(3)
+    for n in (0, 1, 63, 64, 65, 200, 2048):
+        v = rng.random(n) > 0.3
+        w = qeg.pack_validity(v)
+        assert len(w) == (n + 63) // 64
+        for i in range(n):
+            assert bool((int(w[i >> 6]) >> (i & 63)) & 1) == v[i]
+        assert (qeg.unpack_validity(w, n) == v).all()
+        if n % 64:
+            assert int(w[-1]) >> (n % 64) == (1 << (64 - n % 64)) - 1  # padding bits set

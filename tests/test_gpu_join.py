@@ -1,0 +1,198 @@
+"""GPU hash-join parity against the oracle, through the C ABI (libqeg.so).
+
+Mirrors the reference's tests/join_differential_test.cpp: the hand-built edge
+cases (single key with matches / misses / NULL key, composite (i32, f64) key,
+empty build side, empty probe side, all-match cross product, a 3000-row
+fan-out past the 2048-row output batch, NULL never equals NULL) for INNER and
+LEFT, then seeded random join cases, then the fused COUNT(*)/SUM sink under
+every strategy. Join output is unordered: both sides are canonicalised.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import qeg
+from util import StrCanon, assert_same, gen_column, gpu_rows, to_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def i32(v, nulls=()):
+    valid = None
+    if nulls:
+        valid = np.ones(len(v), bool)
+        valid[list(nulls)] = False
+    return O.TCol(O.I32, np.array(v, np.int32), valid)
+
+
+def i64(v, nulls=()):
+    valid = None
+    if nulls:
+        valid = np.ones(len(v), bool)
+        valid[list(nulls)] = False
+    return O.TCol(O.I64, np.array(v, np.int64), valid)
+
+
+def f64(v):
+    return O.TCol(O.F64, np.array(v, np.float64))
+
+
+def run_gpu(ctx, probe, build, pk, bk, jt, strategy=qeg.JOIN_AUTO, fetch_chunk=2048, build_batches=1):
+    canon = StrCanon([s for c in probe + build if c.type == O.STR for s in c.dictionary])
+    j = qeg.Join(ctx, [c.type for c in probe], [c.type for c in build], pk, bk, jt, strategy=strategy)
+    try:
+        nb = build[0].n
+        step = max(64, -(-nb // build_batches) // 64 * 64) if nb else 1
+        for s in range(0, max(nb, 1), step):
+            e = min(nb, s + step)
+            part = []
+            for c in build:
+                valid = None if c.valid is None else c.valid[s:e]
+                part.append(to_gpu(O.TCol(c.type, c.values[s:e], valid, c.dictionary), canon))
+            j.build(part)
+        j.build_finish()
+        n = j.probe([to_gpu(c, canon) for c in probe])
+        cols = None
+        for first in range(0, n, fetch_chunk):
+            part = j.fetch(first, min(fetch_chunk, n - first))
+            cols = part if cols is None else [(np.concatenate([a[0], b[0]]), np.concatenate([a[1], b[1]]))
+                                              for a, b in zip(cols, part)]
+        types = [c.type for c in probe] + [c.type for c in build]
+        if cols is None:
+            return types, []
+        return gpu_rows(cols, types, canon)
+    finally:
+        j.close()
+
+
+def check(ctx, probe, build, pk, bk, **kw):
+    for jt in (O.INNER, O.LEFT):
+        ot, orows = O.join(probe, build, pk, bk, jt)
+        gt, grows = run_gpu(ctx, probe, build, pk, bk, jt, **kw)
+        assert_same(gt, grows, ot, orows, "join type %d" % jt)
+
+
+def test_edge_single_key_match_miss_null(ctx):
+    build = [i32([1, 1, 2, 5, 5, 5]), i64([10, 11, 20, 50, 51, 52])]
+    probe = [i32([1, 2, 3, 5, 0], nulls=[4]), i64([100, 200, 300, 500, 999])]
+    check(ctx, probe, build, [0], [0])
+    check(ctx, probe, build, [0], [0], strategy=qeg.JOIN_HASH)
+
+
+def test_edge_composite_key(ctx):
+    build = [i32([1, 1, 2, 2]), f64([1.0, 2.0, 1.0, 2.0]), i64([11, 12, 21, 22])]
+    probe = [i32([1, 1, 2, 2]), f64([2.0, 9.0, 1.0, 2.0])]
+    check(ctx, probe, build, [0, 1], [0, 1])
+
+
+def test_edge_empty_build(ctx):
+    build = [i32([]), i64([])]
+    probe = [i32([1, 2, 3])]
+    check(ctx, probe, build, [0], [0])
+
+
+def test_edge_empty_probe(ctx):
+    build = [i32([1, 2, 3])]
+    probe = [i32([]), i64([])]
+    check(ctx, probe, build, [0], [0])
+
+
+def test_edge_all_match_cross(ctx):
+    build = [i32([7, 7, 7, 7]), i64([1, 2, 3, 4])]
+    probe = [i32([7, 7, 7])]
+    check(ctx, probe, build, [0], [0])
+
+
+def test_edge_fanout_over_output_batch(ctx):
+    build = [i32([7] * 3000), i64(list(range(3000)))]
+    probe = [i32([7, 9, 7]), i64([100, 200, 300])]
+    check(ctx, probe, build, [0], [0])
+    check(ctx, probe, build, [0], [0], strategy=qeg.JOIN_HASH, fetch_chunk=1000)
+
+
+def test_edge_null_never_matches_null(ctx):
+    build = [i32([1, 0, 2], nulls=[1]), i64([10, 11, 12])]
+    probe = [i32([1, 0, 0], nulls=[1, 2])]
+    check(ctx, probe, build, [0], [0])
+
+
+def test_f64_keys_canonicalised(ctx):
+    nan = float("nan")
+    build = [f64([0.0, nan, 1.5]), i64([1, 2, 3])]
+    probe = [f64([-0.0, nan, 1.5, 2.5])]
+    check(ctx, probe, build, [0], [0])
+
+
+def test_str_keys_join_by_value_across_dictionaries(ctx):
+    bdict = ["IBM", "AAPL", "MSFT"]
+    pdict = ["MSFT", "GOOG", "AAPL"]
+    build = [O.TCol(O.STR, np.array([0, 1, 2, 1], np.int32), None, bdict), i64([1, 2, 3, 4])]
+    probe = [O.TCol(O.STR, np.array([0, 1, 2, 2], np.int32), np.array([1, 1, 1, 0], bool), pdict)]
+    check(ctx, probe, build, [0], [0])
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_random_joins(ctx, seed):
+    rng = np.random.default_rng(0x301D + seed)
+    for it in range(40):
+        nk = int(rng.integers(1, 3))
+        kt = [int(rng.choice([O.I32, O.I64, O.F64])) for _ in range(nk)]
+        card = int(rng.integers(1, 80))
+        nb, npr = int(rng.integers(0, 3000)), int(rng.integers(0, 3000))
+        build = [gen_column(rng, t, nb, 10, card) for t in kt] + [gen_column(rng, O.I64, nb, 10)]
+        probe = [gen_column(rng, t, npr, 10, card * 2) for t in kt] + [gen_column(rng, O.F64, npr, 10)]
+        jt = int(rng.integers(0, 2))
+        strategy = int(rng.choice([qeg.JOIN_AUTO, qeg.JOIN_HASH]))
+        ot, orows = O.join(probe, build, list(range(nk)), list(range(nk)), jt)
+        gt, grows = run_gpu(ctx, probe, build, list(range(nk)), list(range(nk)), jt, strategy=strategy,
+                            build_batches=int(rng.integers(1, 4)))
+        assert_same(gt, grows, ot, orows, "seed %d iter %d" % (seed, it))
+
+
+@pytest.mark.parametrize("strategy", [qeg.JOIN_AUTO, qeg.JOIN_HASH, qeg.JOIN_DENSE])
+@pytest.mark.parametrize("dup", [False, True])
+def test_count_sum_sink(ctx, strategy, dup):
+    """The 16M x 256M join workload's shape at 1/64 scale: unique (or
+    duplicated) build keys, probe keys half hits and half from a disjoint
+    range, 2% NULL keys on both sides, SUM over an int64 payload."""
+    rng = np.random.default_rng(99 + strategy + 10 * dup)
+    nb, npr = 1 << 18, 1 << 22
+    bkey = rng.permutation(nb).astype(np.int64)
+    if dup:
+        bkey = bkey // 3
+    bvalid = rng.random(nb) >= 0.02
+    hit = rng.random(npr) < 0.5
+    pkey = np.where(hit, rng.integers(0, nb, npr), rng.integers(nb, 2 * nb, npr)).astype(np.int64)
+    pvalid = rng.random(npr) >= 0.02
+    pval = rng.integers(0, 1 << 20, npr).astype(np.int64)
+    exp = O.join_count_sum(O.TCol(O.I64, pkey, pvalid), O.TCol(O.I64, pval), O.TCol(O.I64, bkey, bvalid))
+    j = qeg.Join(ctx, [O.I64, O.I64], [O.I64], [0], [0], strategy=strategy)
+    j.build([qeg.Col(bkey, qeg.pack_validity(bvalid))])
+    j.build_finish()
+    half = npr // 2
+    j.probe_count_sum(qeg.Col(pkey[:half], qeg.pack_validity(pvalid[:half])), qeg.Col(pval[:half]))
+    j.probe_count_sum(qeg.Col(pkey[half:], qeg.pack_validity(pvalid[half:])), qeg.Col(pval[half:]))
+    got = j.count_sum()
+    st = j.stats()
+    j.close()
+    assert got == exp
+    if strategy == qeg.JOIN_HASH:
+        assert st["strategy"] == qeg.JOIN_HASH
+    else:
+        assert st["strategy"] == qeg.JOIN_DENSE
+
+
+def test_count_sum_sparse_keys_use_hash(ctx):
+    rng = np.random.default_rng(4)
+    nb, npr = 100_000, 1_000_000
+    bkey = rng.integers(-(1 << 62), 1 << 62, nb).astype(np.int64)
+    pkey = np.where(rng.random(npr) < 0.5, bkey[rng.integers(0, nb, npr)], rng.integers(-(1 << 62), 1 << 62, npr))
+    pval = rng.integers(-1000, 1000, npr).astype(np.int64)
+    exp = O.join_count_sum(O.TCol(O.I64, pkey.astype(np.int64)), O.TCol(O.I64, pval), O.TCol(O.I64, bkey))
+    j = qeg.Join(ctx, [O.I64, O.I64], [O.I64], [0], [0])
+    j.build([qeg.Col(bkey)])
+    j.build_finish()
+    j.probe_count_sum(qeg.Col(pkey.astype(np.int64)), qeg.Col(pval))
+    assert j.count_sum() == exp
+    assert j.stats()["strategy"] == qeg.JOIN_HASH
+    j.close()
