@@ -208,6 +208,70 @@ qeg_status qeg_join_stats(const qeg_join* j, int32_t* strategy, int32_t* partiti
                           uint64_t* distinct_keys);
 void qeg_join_destroy(qeg_join* j);
 
+/* ---- fused filter -> inner join -> GROUP BY --------------------------------
+ * Replaces the operator chain Plan::lower builds for
+ *   scan(probe).filter(probe[filter_col] <op> filter_value)
+ *              .join(scan(build), {probe_key}, {build_key}, JoinType::Inner)
+ *              .aggregate({group_col}, aggs)
+ * (plan/plan.cpp:340-404 and 581-590: Filter ops/filter.cpp:28-66, HashJoin,
+ * Aggregate) with one pass over the probe side. Restrictions of the fused
+ * form: the join key is STR (by value through the code maps) or an integer
+ * whose build values span < 2^24; the build side has <= 2^22 rows;
+ * `group_col` is a build-side column of the joined schema (probe columns then
+ * build columns) and the aggregates read probe-side columns. filter_col = -1:
+ * no filter; a NULL filter operand drops the row. Output: one row per group,
+ * the group column (STR as canonical value ids) then the aggregates, written
+ * to `outs` (capacity `out_capacity` rows; host or device). */
+#define QEG_CMP_LT 0
+#define QEG_CMP_LE 1
+#define QEG_CMP_GT 2
+#define QEG_CMP_GE 3
+#define QEG_CMP_EQ 4
+#define QEG_CMP_NE 5
+typedef struct qeg_pipeline_desc {
+  int32_t filter_col;
+  int32_t filter_op;
+  double filter_value;
+  uint32_t probe_key;
+  uint32_t build_key;
+  uint32_t group_col;
+  int32_t naggs;
+  qeg_agg_spec aggs[16];
+} qeg_pipeline_desc;
+qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe, const qeg_column* build,
+                               int nbuild, const qeg_pipeline_desc* desc, uint64_t out_capacity,
+                               const qeg_out_column* outs, uint64_t* num_groups);
+
+/* ---- key-column sketch and learned estimator ------------------------------
+ * No reference analogue: the reference sizes its table by growth alone
+ * (ops/hashtable.h:83-94). The estimator only picks table sizes and
+ * strategies; an undersized table still grows and replays, so results never
+ * depend on it.
+ * qeg_sketch: 80 features of a key column over a strided sample of about
+ *   `sample_rows` rows (0 = 2^20): 64 HyperLogLog register-value bins and 16
+ *   count-min / heavy-hitter features; also the classic (uniform-model)
+ *   distinct estimate and the sampled share of rows in the top 2048 keys.
+ * The estimator is an MLP 80 -> 64 -> 64 -> 2 (ReLU, BF16 weights, FP32
+ * accumulation) whose outputs are log2(1 + groups) / 32 and the share of rows
+ * carried by the 2048 most frequent keys. Weights are QEG_MLP_PARAMS float32
+ * (W1[64][80] b1 W2[64][64] b2 W3[2][64] b3); a context loads
+ * $QEG_ESTIMATOR_WEIGHTS or estimator_weights.f32 beside libqeg.so if present.
+ * qeg_estimator_grad returns the mean-squared-error loss over the batch and
+ * its gradient in the same layout; qeg_estimator_train runs Adam on the GPU. */
+#define QEG_SKETCH_FEATURES 80
+#define QEG_MLP_PARAMS 9474
+qeg_status qeg_sketch(qeg_ctx* ctx, const qeg_column* key, uint64_t sample_rows, float* features,
+                      double* classic_groups, double* top_share);
+qeg_status qeg_estimator_init(qeg_ctx* ctx, uint64_t seed);
+qeg_status qeg_estimator_set_weights(qeg_ctx* ctx, const float* params);
+qeg_status qeg_estimator_get_weights(qeg_ctx* ctx, float* params);
+qeg_status qeg_estimator_predict(qeg_ctx* ctx, const float* features, uint32_t n, float* out);
+qeg_status qeg_estimator_grad(qeg_ctx* ctx, const float* x, const float* targets, uint32_t n, float* loss,
+                              float* grad);
+qeg_status qeg_estimator_train(qeg_ctx* ctx, const float* x, const float* targets, uint32_t n,
+                               uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                               float* final_loss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,7 +115,7 @@ __device__ __forceinline__ uint64_t* global_row1(const AggK& P, bool kv, uint64_
   const int W = P.row_words;
   if (!kv) return P.table + (P.cap + 1) * W;
   if (k == 0) return P.table + P.cap * W;
-  uint64_t s = h & (P.cap - 1);
+  uint64_t s = __umul64hi(h, P.cap);
   for (int t = 0; t < P.probe_limit; ++t) {
     uint64_t* r = P.table + s * W;
     const uint64_t cur = ld_relaxed(r);
@@ -129,7 +129,7 @@ __device__ __forceinline__ uint64_t* global_row1(const AggK& P, bool kv, uint64_
       }
       if (old == k) return r;
     }
-    s = (s + 1) & (P.cap - 1);
+    s = (s + 1 == P.cap) ? 0 : s + 1;
   }
   return nullptr;
 }
@@ -141,7 +141,7 @@ __device__ __forceinline__ uint64_t* global_rowN(const AggK& P, const uint64_t* 
                                                  uint64_t h, unsigned long long& inserted) {
   const int W = P.row_words;
   const uint64_t tag = (h >> 32) | 2ull;
-  uint64_t s = h & (P.cap - 1);
+  uint64_t s = __umul64hi(h, P.cap);
   for (int t = 0; t < P.probe_limit; ++t) {
     uint64_t* r = P.table + s * W;
     uint64_t st = ld_relaxed(r);
@@ -171,7 +171,7 @@ __device__ __forceinline__ uint64_t* global_rowN(const AggK& P, const uint64_t* 
       for (int j = 0; eq && j < P.nkeys; ++j) eq = ld_relaxed(r + 2 + j) == words[j];
       if (eq) return r;
     }
-    s = (s + 1) & (P.cap - 1);
+    s = (s + 1 == P.cap) ? 0 : s + 1;
   }
   return nullptr;
 }
@@ -647,7 +647,7 @@ AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel
 }
 
 void AggState::alloc_table(uint64_t new_cap) {
-  cap = std::max<uint64_t>(next_pow2(new_cap), 1024);
+  cap = std::max<uint64_t>(new_cap, 1024);
   const uint64_t rows = (mode == 1) ? cap + 2 : (mode == 0 ? 1 : cap);
   table.alloc(rows * row_words * 8, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(table.get(), 0, rows * row_words * 8, ctx->stream));
@@ -796,13 +796,16 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   if (mode == 0) {
     want = 1;
   } else if (cfg.expected_groups > 0) {
-    want = 2 * cfg.expected_groups;
+    if (cfg.hot_keys != 0 && mode == 1) estimate_groups(staged, nrows, len, dsel);  // heavy hitters only
+    want = static_cast<uint64_t>(static_cast<double>(cfg.expected_groups) / kTargetLoad) + 64;
     est_groups = static_cast<double>(cfg.expected_groups);
   } else if (cfg.sizing == QEG_SIZE_FIXED) {
     want = cfg.initial_capacity ? cfg.initial_capacity : (1ull << 20);
   } else {
     est_groups = estimate_groups(staged, nrows, len, dsel);
-    want = static_cast<uint64_t>(std::max(2.0 * est_groups * 1.15, 1024.0));
+    // 15% head-room over the estimate keeps the probe short if it is low; an
+    // estimate that is far too low is caught by overflow -> grow -> replay.
+    want = static_cast<uint64_t>(std::max(1.15 * est_groups / kTargetLoad, 1024.0));
   }
   alloc_table(want);
   counters.alloc(64, ctx->stream);
@@ -824,10 +827,23 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
     // (all fit) or a heavy head of the key distribution.
     strategy = (est_groups > 0 && est_groups > 64.0 * slots && hot_share < 0.3) ? QEG_AGG_GLOBAL : QEG_AGG_SMEM;
   }
+  nhot = 0;
   if (strategy == QEG_AGG_SMEM && mode == 1) {
     smem_slots = cfg.smem_slots > 0 ? static_cast<int>(next_pow2(cfg.smem_slots)) : std::min(slots, 4096);
     smem_slots = std::min(smem_slots, slots);
     smem_insert = 1;
+    // Many groups but a heavy head: preload the heavy hitters found by the
+    // sketch and keep the private table read-only, so its slots hold the keys
+    // that carry the rows instead of whichever keys arrived first.
+    if (cfg.hot_keys != 0 && est_groups > 0.5 * smem_slots && !heavy_candidates.empty()) {
+      const int want_hot = cfg.hot_keys > 0 ? cfg.hot_keys : smem_slots / 2;
+      nhot = static_cast<int>(std::min<size_t>(heavy_candidates.size(), std::min(want_hot, smem_slots / 2)));
+      hot_keys_dev.alloc(std::max(nhot, 1) * 8, ctx->stream);
+      QEG_CUDA(cudaMemcpyAsync(hot_keys_dev.get(), heavy_candidates.data(), nhot * 8, cudaMemcpyHostToDevice,
+                               ctx->stream));
+      QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+      smem_insert = 0;
+    }
   } else {
     smem_slots = 0;
   }

@@ -21,6 +21,8 @@ constexpr int kMaxKeys = 8;
 constexpr int kMaxVals = 8;
 constexpr int kMaxFields = 24;
 constexpr int kMaxAggs = 32;
+// Target occupancy of a global GROUP BY table sized from a group-count estimate.
+constexpr double kTargetLoad = 0.6;
 
 // Parameter block of the aggregation kernels (passed by value).
 struct AggK {
@@ -31,7 +33,7 @@ struct AggK {
   uint8_t cfirst[kMaxVals];
   uint8_t cnf[kMaxVals];
   uint64_t* table;
-  uint64_t cap;  // power of two
+  uint64_t cap;  // slots; a key's first slot is mulhi(hash, cap)
   const uint32_t* sel;
   uint64_t nrows;  // rows to process (sel length, or len when dense)
   uint64_t len;    // physical column length

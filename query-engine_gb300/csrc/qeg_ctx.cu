@@ -147,9 +147,16 @@ qeg_status qeg_ctx_create(int device, qeg_ctx** out) {
     c->sms = p.multiProcessorCount;
     c->smem_optin = p.sharedMemPerBlockOptin;
     QEG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    // Keep freed stream-ordered allocations cached in this process's pool, so a
+    // query's tables and scratch are re-used instead of re-mapped every call.
+    cudaMemPool_t pool;
+    QEG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = UINT64_MAX;
+    QEG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     c->dev_err.alloc(64, c->stream);
     QEG_CUDA(cudaMemsetAsync(c->dev_err.get(), 0, 64, c->stream));
     QEG_CUDA(cudaStreamSynchronize(c->stream));
+    qeg::load_default_weights(c.get());
     *out = c.release();
   });
 }

@@ -96,6 +96,8 @@ inline bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+struct Mlp;
+
 }  // namespace qeg
 
 struct qeg_ctx {
@@ -106,7 +108,13 @@ struct qeg_ctx {
   std::string err;
   uint64_t launches = 0;
   qeg::DevBuf dev_err;  // uint32 device error word (qeg::DevError bits)
+  std::shared_ptr<qeg::Mlp> mlp;  // the learned estimator, when weights are loaded
 };
+
+namespace qeg {
+// Loads the shipped estimator weights into a new context (qeg_estimator.cu).
+void load_default_weights(qeg_ctx* ctx);
+}  // namespace qeg
 
 namespace qeg {
 

@@ -55,6 +55,10 @@ __device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t* p) {
 }
 
 // Loads the key tuple of row p. Returns false when any key column is NULL.
+// Slot hash of a key tuple: one splitmix64 round for a single key word, the
+// seeded fold of every word for composite keys.
+__device__ __forceinline__ uint64_t single_key_hash(uint64_t k) { return mix64(k ^ kHashSeed); }
+
 __device__ __forceinline__ bool load_key(const DevCol* kc, int nk, uint64_t p, uint64_t* w, uint64_t& h) {
   h = kHashSeed;
   for (int j = 0; j < nk; ++j) {
@@ -62,6 +66,7 @@ __device__ __forceinline__ bool load_key(const DevCol* kc, int nk, uint64_t p, u
     w[j] = key_word(kc[j], p);
     h = hash_fold(h, w[j]);
   }
+  if (nk == 1) h = single_key_hash(w[0]);
   return true;
 }
 
@@ -130,10 +135,13 @@ struct BuildK {
   uint32_t* fill;
   uint32_t* rows_out;
   uint32_t* dup;
+  unsigned long long* distinct;
   uint32_t* err;
 };
 
 __global__ void build_count_kernel(BuildK P) {
+  unsigned long long fresh = 0;
+  uint32_t dup = 0;
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t w[kMaxKeys], h;
     if (!load_key(P.key, P.nkeys, r, w, h)) continue;
@@ -147,7 +155,16 @@ __global__ void build_count_kernel(BuildK P) {
         continue;
       }
     }
-    if (atomicAdd(&P.T.cnt[s], 1u) != 0) *P.dup = 1;
+    if (atomicAdd(&P.T.cnt[s], 1u) != 0) dup = 1;
+    else ++fresh;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    fresh += __shfl_down_sync(0xffffffffu, fresh, o);
+    dup |= __shfl_down_sync(0xffffffffu, dup, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (fresh) atomicAdd(P.distinct, fresh);
+    if (dup) *P.dup = 1;
   }
 }
 
@@ -167,15 +184,25 @@ __global__ void build_scatter_kernel(BuildK P) {
   }
 }
 
-__global__ void dense_bitmap_kernel(const uint32_t* __restrict__ cnt, uint64_t n, uint64_t* __restrict__ bits) {
-  const uint64_t nw = (n + 63) / 64;
-  for (uint64_t wi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wi < nw; wi += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t b = 0;
-    for (int i = 0; i < 64; ++i) {
-      const uint64_t s = wi * 64 + i;
-      if (s < n && cnt[s]) b |= 1ull << i;
-    }
-    bits[wi] = b;
+// Dense build: sets one bit per key value; a bit that was already set means
+// the build keys are not unique.
+__global__ void dense_mark_kernel(BuildK P, unsigned long long* __restrict__ bits) {
+  unsigned long long fresh = 0;
+  uint32_t dup = 0;
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
+    if (!col_valid(P.key[0], r)) continue;
+    const uint64_t s = static_cast<uint64_t>(dense_value(P.key[0], r) - P.T.dmin);
+    const unsigned long long bit = 1ull << (s & 63);
+    if (atomicOr(bits + (s >> 6), bit) & bit) dup = 1;
+    else ++fresh;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    fresh += __shfl_down_sync(0xffffffffu, fresh, o);
+    dup |= __shfl_down_sync(0xffffffffu, dup, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (fresh) atomicAdd(P.distinct, fresh);
+    if (dup) *P.dup = 1;
   }
 }
 
@@ -228,7 +255,149 @@ struct ProbeK {
   uint32_t* err;
 };
 
-// The COUNT(*) / SUM(payload) sink of an inner join, fused into the probe.
+// Read-only lookup of one key in the finished table: match multiplicity.
+template <typename KT, int STRAT, bool UNIQUE>
+__device__ __forceinline__ uint64_t sink_lookup(const JTable& T, KT key) {
+  if (STRAT == QEG_JOIN_DENSE) {
+    const uint64_t s = static_cast<uint64_t>(static_cast<int64_t>(key)) - static_cast<uint64_t>(T.dmin);
+    if (s >= T.cap) return 0;
+    if (UNIQUE) return (__ldg(T.bitmap + (s >> 6)) >> (s & 63)) & 1ull;
+    return __ldg(T.cnt + s);
+  } else {
+    const uint64_t k = sizeof(KT) == 4 ? static_cast<uint64_t>(static_cast<uint32_t>(key))
+                                       : static_cast<uint64_t>(key);
+    if (k == 0) return __ldg(T.cnt + T.cap);
+    // Linear probing read four slots (one 32-byte sector) at a time: the
+    // aligned group holding the home slot, then the following groups. Slots
+    // before the home slot in the first group are not part of the probe.
+    const uint64_t home = single_key_hash(k) & (T.cap - 1);
+    uint64_t g = home & ~3ull;
+    int skip = static_cast<int>(home & 3);
+    const ulonglong2* base = reinterpret_cast<const ulonglong2*>(T.keys);
+    for (uint64_t t = 0; t < T.cap; t += 4) {
+      const ulonglong2 a = __ldg(base + (g >> 1));
+      const ulonglong2 b = __ldg(base + (g >> 1) + 1);
+      const uint64_t c[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        if (i < skip) continue;
+        if (c[i] == k) return UNIQUE ? 1 : __ldg(T.cnt + g + i);
+        if (c[i] == 0) return 0;
+      }
+      skip = 0;
+      g = (g + 4) & (T.cap - 1);
+    }
+    return 0;
+  }
+}
+
+struct SinkK {
+  const void* key;
+  const uint64_t* kvalid;  // nullptr: no NULL keys
+  const void* val;
+  const uint64_t* vvalid;  // nullptr: no NULL payloads
+  uint64_t n;
+  JTable T;
+  unsigned long long* acc;  // [0] count, [1] sum, [2] any non-null payload matched
+};
+
+template <typename T>
+__device__ __forceinline__ void load4(const T* p, T (&o)[4]) {
+  if (sizeof(T) == 8) {
+    const longlong2 a = __ldcs(reinterpret_cast<const longlong2*>(p));
+    const longlong2 b = __ldcs(reinterpret_cast<const longlong2*>(p) + 1);
+    o[0] = static_cast<T>(a.x);
+    o[1] = static_cast<T>(a.y);
+    o[2] = static_cast<T>(b.x);
+    o[3] = static_cast<T>(b.y);
+  } else {
+    const int4 a = __ldcs(reinterpret_cast<const int4*>(p));
+    o[0] = static_cast<T>(a.x);
+    o[1] = static_cast<T>(a.y);
+    o[2] = static_cast<T>(a.z);
+    o[3] = static_cast<T>(a.w);
+  }
+}
+
+// The COUNT(*) / SUM(payload) sink of an inner join fused into the probe:
+// each thread takes 4 consecutive rows per step (16-byte streaming loads, one
+// validity word read per 4 rows), looks the keys up with read-only loads, and
+// the partial count/sum are reduced per block before one atomic per block.
+template <typename KT, typename VT, int STRAT, bool UNIQUE>
+__global__ void __launch_bounds__(256) probe_sink_kernel(const SinkK P) {
+  unsigned long long cnt = 0, sum = 0, seen = 0;
+  const KT* keys = static_cast<const KT*>(P.key);
+  const VT* vals = static_cast<const VT*>(P.val);
+  const uint64_t nq = P.n >> 2;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // Two quads per step (q and q + stride), all loads issued before any lookup,
+  // so each thread keeps 64 bytes of the probe side in flight.
+  for (uint64_t q = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; q < nq; q += 2 * stride) {
+    KT k[2][4];
+    VT v[2][4];
+    uint32_t kb[2], vb[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const uint64_t qq = q + u * stride;
+      kb[u] = vb[u] = 0;
+      if (qq < nq) {
+        const uint64_t r0 = qq << 2;
+        load4(keys + r0, k[u]);
+        load4(vals + r0, v[u]);
+        kb[u] = P.kvalid ? static_cast<uint32_t>(__ldg(P.kvalid + (r0 >> 6)) >> (r0 & 63)) & 0xFu : 0xFu;
+        vb[u] = P.vvalid ? static_cast<uint32_t>(__ldg(P.vvalid + (r0 >> 6)) >> (r0 & 63)) & 0xFu : 0xFu;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      uint64_t m[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) m[j] = ((kb[u] >> j) & 1u) ? sink_lookup<KT, STRAT, UNIQUE>(P.T, k[u][j]) : 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        cnt += m[j];
+        if (m[j] && ((vb[u] >> j) & 1u)) {
+          sum += static_cast<unsigned long long>(static_cast<int64_t>(v[u][j])) * m[j];
+          seen = 1;
+        }
+      }
+    }
+  }
+  // Tail rows (n not a multiple of 4).
+  const uint64_t tail0 = nq << 2;
+  const uint64_t gt = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (gt < P.n - tail0) {
+    const uint64_t r = tail0 + gt;
+    const bool kv = !P.kvalid || ((P.kvalid[r >> 6] >> (r & 63)) & 1ull);
+    const uint64_t m = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, keys[r]) : 0;
+    cnt += m;
+    if (m && (!P.vvalid || ((P.vvalid[r >> 6] >> (r & 63)) & 1ull))) {
+      sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r])) * m;
+      seen = 1;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    seen |= __shfl_down_sync(0xffffffffu, seen, o);
+  }
+  __shared__ unsigned long long s_acc[3];
+  if (threadIdx.x == 0) s_acc[0] = s_acc[1] = s_acc[2] = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_acc[0], cnt);
+    atomicAdd(&s_acc[1], sum);
+    atomicOr(&s_acc[2], seen);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_acc[0]) atomicAdd(P.acc + 0, s_acc[0]);
+    if (s_acc[1]) atomicAdd(P.acc + 1, s_acc[1]);
+    if (s_acc[2]) atomicOr(P.acc + 2, s_acc[2]);
+  }
+}
+
+// The COUNT(*) / SUM(payload) sink for any key/payload type or alignment.
 template <int STRAT, bool UNIQUE>
 __global__ void __launch_bounds__(512) probe_count_sum_kernel(const ProbeK P) {
   unsigned long long cnt = 0, sum = 0, seen = 0;
@@ -246,7 +415,7 @@ __global__ void __launch_bounds__(512) probe_count_sum_kernel(const ProbeK P) {
     } else {
       uint64_t w[1];
       w[0] = key_word(P.key[0], p);
-      const int64_t s = hash_slot<false>(P.T, w, hash_fold(kHashSeed, w[0]), P.err);
+      const int64_t s = hash_slot<false>(P.T, w, single_key_hash(w[0]), P.err);
       if (s >= 0) m = (UNIQUE && static_cast<uint64_t>(s) != P.T.cap) ? 1 : __ldg(P.T.cnt + s);
     }
     if (m == 0) continue;
@@ -463,6 +632,17 @@ struct JoinState {
   }
 
   void finish_build();
+  uint64_t slots() const {
+    return strategy == QEG_JOIN_DENSE ? cap : (bkeys.size() == 1 ? cap + 1 : cap);
+  }
+  void alloc_counts() {
+    cnt.alloc(slots() * 4, ctx->stream);
+    QEG_CUDA(cudaMemsetAsync(cnt.get(), 0, slots() * 4, ctx->stream));
+  }
+  BuildK build_params(DevBuf& scratch);
+  void count_dense();
+  void ensure_csr();
+  bool csr_built = false;
 };
 
 namespace {
@@ -525,66 +705,99 @@ void JoinState::finish_build() {
     }
     if (strategy != QEG_JOIN_DENSE && cfg.strategy == QEG_JOIN_DENSE) strategy = QEG_JOIN_HASH;
   }
-  uint64_t slots;
+  DevBuf dup(16, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(dup.get(), 0, 16, ctx->stream));
+  P.dup = dup.get<uint32_t>();
+  P.distinct = reinterpret_cast<unsigned long long*>(dup.get<uint8_t>() + 8);
+  const unsigned g = grid_for(ctx, nbuild, 256, 8);
   if (strategy == QEG_JOIN_DENSE) {
-    slots = cap;
+    // One bit per key value; atomicOr's old word reveals duplicates.
+    bitmap.alloc(((cap + 63) / 64) * 8, ctx->stream);
+    QEG_CUDA(cudaMemsetAsync(bitmap.get(), 0, ((cap + 63) / 64) * 8, ctx->stream));
+    P.T = table();
+    if (nbuild) {
+      dense_mark_kernel<<<g, 256, 0, ctx->stream>>>(P, bitmap.get<unsigned long long>());
+      ctx->launches++;
+      QEG_CUDA(cudaGetLastError());
+    }
   } else {
     cap = std::max<uint64_t>(1024, next_pow2(2 * std::max<uint64_t>(nbuild, 1)));
     const int kw = nk == 1 ? 1 : 1 + nk;
     const uint64_t krows = nk == 1 ? cap + 1 : cap;
     keys.alloc(krows * kw * 8, ctx->stream);
     QEG_CUDA(cudaMemsetAsync(keys.get(), 0, krows * kw * 8, ctx->stream));
-    slots = nk == 1 ? cap + 1 : cap;
+    alloc_counts();
+    P.T = table();
+    if (nbuild) {
+      build_count_kernel<<<g, 256, 0, ctx->stream>>>(P);
+      ctx->launches++;
+      QEG_CUDA(cudaGetLastError());
+    }
   }
-  cnt.alloc(slots * 4, ctx->stream);
-  QEG_CUDA(cudaMemsetAsync(cnt.get(), 0, slots * 4, ctx->stream));
-  DevBuf dup(4, ctx->stream);
-  QEG_CUDA(cudaMemsetAsync(dup.get(), 0, 4, ctx->stream));
-  P.dup = dup.get<uint32_t>();
-  P.T = table();
-  const unsigned g = grid_for(ctx, nbuild, 256, 8);
-  if (nbuild) {
-    build_count_kernel<<<g, 256, 0, ctx->stream>>>(P);
-    ctx->launches++;
-    QEG_CUDA(cudaGetLastError());
-  }
-  off.alloc((slots + 1) * 8, ctx->stream);
-  const uint64_t total = exclusive_scan(ctx, cnt.get<uint32_t>(), slots, off.get<uint64_t>());
-  nonnull = total;
-  rows.alloc(std::max<uint64_t>(total, 1) * 4, ctx->stream);
-  DevBuf fill(slots * 4, ctx->stream);
-  QEG_CUDA(cudaMemsetAsync(fill.get(), 0, slots * 4, ctx->stream));
-  P.T = table();
-  P.fill = fill.get<uint32_t>();
-  P.rows_out = rows.get<uint32_t>();
-  if (nbuild) {
-    build_scatter_kernel<<<g, 256, 0, ctx->stream>>>(P);
-    ctx->launches++;
-    QEG_CUDA(cudaGetLastError());
-  }
-  uint32_t d = 0;
-  QEG_CUDA(cudaMemcpyAsync(&d, dup.get(), 4, cudaMemcpyDeviceToHost, ctx->stream));
+  uint64_t d[2] = {0, 0};
+  QEG_CUDA(cudaMemcpyAsync(d, dup.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
   QEG_CUDA(cudaStreamSynchronize(ctx->stream));
   check_device_error(ctx);
-  unique = d ? 0 : 1;
-  if (strategy == QEG_JOIN_DENSE && unique) {
-    bitmap.alloc(((cap + 63) / 64) * 8, ctx->stream);
-    dense_bitmap_kernel<<<grid_for(ctx, cap / 64 + 1, 256, 8), 256, 0, ctx->stream>>>(cnt.get<uint32_t>(), cap,
-                                                                                    bitmap.get<uint64_t>());
-    ctx->launches++;
-    QEG_CUDA(cudaGetLastError());
-  }
-  // Distinct keys: slots with a nonzero count (dense) or inserted hash rows.
-  distinct = 0;
-  {
-    std::vector<uint32_t> hc(slots);
-    QEG_CUDA(cudaMemcpyAsync(hc.data(), cnt.get(), slots * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
-    for (uint32_t c : hc) distinct += c ? 1 : 0;
-  }
+  unique = (d[0] & 0xffffffffull) ? 0 : 1;
+  distinct = d[1];
+  if (strategy == QEG_JOIN_DENSE && !unique) count_dense();
+  csr_built = false;
   acc.alloc(24, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(acc.get(), 0, 24, ctx->stream));
   QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+BuildK JoinState::build_params(DevBuf& scratch) {
+  BuildK P{};
+  P.nkeys = static_cast<int>(bkeys.size());
+  for (int j = 0; j < P.nkeys; ++j) P.key[j] = store_key(j);
+  P.n = nbuild;
+  P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+  scratch.alloc(16, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(scratch.get(), 0, 16, ctx->stream));
+  P.dup = scratch.get<uint32_t>();
+  P.distinct = reinterpret_cast<unsigned long long*>(scratch.get<uint8_t>() + 8);
+  P.T = table();
+  return P;
+}
+
+// Per-value build row counts of a dense table (needed when keys repeat, and
+// by the pair-materialising probe).
+void JoinState::count_dense() {
+  alloc_counts();
+  DevBuf scratch;
+  BuildK P = build_params(scratch);
+  if (nbuild) {
+    build_count_kernel<<<grid_for(ctx, nbuild, 256, 8), 256, 0, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+// Builds the CSR row lists (off, rows) on the first probe that materialises
+// pairs; the COUNT/SUM sink never needs them.
+void JoinState::ensure_csr() {
+  if (csr_built) return;
+  if (!cnt.get()) count_dense();
+  const uint64_t n = slots();
+  off.alloc((n + 1) * 8, ctx->stream);
+  const uint64_t total = exclusive_scan(ctx, cnt.get<uint32_t>(), n, off.get<uint64_t>());
+  rows.alloc(std::max<uint64_t>(total, 1) * 4, ctx->stream);
+  DevBuf fill(n * 4, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(fill.get(), 0, n * 4, ctx->stream));
+  DevBuf scratch;
+  BuildK P = build_params(scratch);
+  P.fill = fill.get<uint32_t>();
+  P.rows_out = rows.get<uint32_t>();
+  if (nbuild) {
+    build_scatter_kernel<<<grid_for(ctx, nbuild, 256, 8), 256, 0, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  check_device_error(ctx);
+  csr_built = true;
 }
 
 }  // namespace qeg
@@ -688,6 +901,7 @@ qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64
       *out_rows = 0;
       return;
     }
+    st.ensure_csr();
     st.counts.alloc(n * 4, ctx->stream);
     st.starts.alloc((n + 1) * 8, ctx->stream);
     ProbeK P = probe_params(st, n);
@@ -761,7 +975,7 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
     require(probe_key->len == probe_val->len, "probe columns differ in length");
     QEG_CUDA(cudaSetDevice(ctx->device));
     const uint64_t n = probe_key->len;
-    if (n == 0 || st.nonnull == 0) return;
+    if (n == 0 || st.distinct == 0) return;
     StagedCol k, v;
     stage_column(ctx, *probe_key, k);
     stage_column(ctx, *probe_val, v);
@@ -773,6 +987,48 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
     P.T = st.table();
     P.acc = st.acc.get<unsigned long long>();
     P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+    const int kt = probe_key->type, vt = probe_val->type;
+    const bool kfast = kt == QEG_I32 || kt == QEG_I64 || kt == QEG_TS;
+    const bool vfast = vt == QEG_I32 || vt == QEG_I64 || vt == QEG_TS;
+    const bool aligned = (reinterpret_cast<uintptr_t>(k.dev.data) % 16 == 0) &&
+                         (reinterpret_cast<uintptr_t>(v.dev.data) % 16 == 0);
+    if (kfast && vfast && aligned) {
+      SinkK S{};
+      S.key = k.dev.data;
+      S.kvalid = k.dev.all_valid ? nullptr : k.dev.validity;
+      S.val = v.dev.data;
+      S.vvalid = v.dev.all_valid ? nullptr : v.dev.validity;
+      S.n = n;
+      S.T = st.table();
+      S.acc = st.acc.get<unsigned long long>();
+      const bool k8 = type_width(kt) == 8, v8 = type_width(vt) == 8, dense = st.strategy == QEG_JOIN_DENSE;
+      // One wave of resident blocks; each thread strides over the probe side.
+      auto launch = [&](void (*kern)(SinkK)) {
+        int per_sm = 0;
+        QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+        const uint64_t want = (n / 8 + 255) / 256;
+        const unsigned grid = static_cast<unsigned>(
+            std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
+        kern<<<grid, 256, 0, ctx->stream>>>(S);
+      };
+#define QEG_SINK(KT, VT)                                                                 \
+  do {                                                                                   \
+    if (dense && st.unique) launch(probe_sink_kernel<KT, VT, QEG_JOIN_DENSE, true>);    \
+    else if (dense) launch(probe_sink_kernel<KT, VT, QEG_JOIN_DENSE, false>);           \
+    else if (st.unique) launch(probe_sink_kernel<KT, VT, QEG_JOIN_HASH, true>);         \
+    else launch(probe_sink_kernel<KT, VT, QEG_JOIN_HASH, false>);                       \
+  } while (0)
+      if (k8 && v8) QEG_SINK(long long, long long);
+      else if (k8) QEG_SINK(long long, int);
+      else if (v8) QEG_SINK(int, long long);
+      else QEG_SINK(int, int);
+#undef QEG_SINK
+      ctx->launches++;
+      QEG_CUDA(cudaGetLastError());
+      if (k.data.get() || v.data.get() || k.validity.get() || v.validity.get())
+        QEG_CUDA(cudaStreamSynchronize(ctx->stream));  // staged inputs die with this scope
+      return;
+    }
     int per_sm = 0;
     const int block = 512;
     const unsigned g0 = static_cast<unsigned>(std::min<uint64_t>((n + block - 1) / block, ctx->sms * 4ull));

@@ -1,0 +1,421 @@
+// gpu_operators.cpp -- GpuAggregate / GpuHashJoin (see gpu_operators.h).
+#include "gpu_operators.h"
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+
+namespace qe::gpu {
+
+namespace {
+
+int32_t to_qeg(Type t) { return static_cast<int32_t>(t); }
+
+int32_t agg_func(AggFunc f) { return static_cast<int32_t>(f); }
+
+Type result_type(AggFunc f, Type in) {  // ops/aggregate.cpp:78-97
+  switch (f) {
+    case AggFunc::CountStar:
+    case AggFunc::Count: return Type::I64;
+    case AggFunc::Sum:
+      if (in == Type::STR) throw std::invalid_argument("SUM is not defined on STR (VARCHAR)");
+      return in == Type::F64 ? Type::F64 : Type::I64;
+    case AggFunc::Avg:
+      if (in == Type::STR) throw std::invalid_argument("AVG is not defined on STR (VARCHAR)");
+      return Type::F64;
+    default: return in;
+  }
+}
+
+inline uint32_t sel_at(const SelectionVector* sel, std::size_t k) {
+  return sel ? sel->idx[k] : static_cast<uint32_t>(k);
+}
+
+}  // namespace
+
+Column HostColumn::view() const {
+  Column c;
+  c.type = type;
+  c.len = len;
+  c.data = reinterpret_cast<const std::byte*>(data.data());
+  const bool av = validity.empty();
+  c.all_valid = av;
+  c.validity = av ? nullptr : validity.data();
+  c.dict = dict.get();
+  return c;
+}
+
+void Staging::reset(const std::vector<Type>& t) {
+  types = t;
+  vals.assign(t.size(), {});
+  valid.assign(t.size(), {});
+  any_null.assign(t.size(), false);
+  rows = 0;
+}
+
+void Staging::append(const Batch& b, const std::vector<StringDict*>& ids) {
+  const std::size_t n = b.row_count;
+  if (n == 0) return;
+  const std::size_t new_rows = rows + n;
+  for (std::size_t c = 0; c < types.size(); ++c) {
+    const Column& col = b.cols[c];
+    const std::size_t w = byte_width(types[c]);
+    auto& v = vals[c];
+    auto& bits = valid[c];
+    v.resize(new_rows * w);
+    bits.resize(validity::words(new_rows), ~0ull);
+    for (std::size_t k = 0; k < n; ++k) {
+      const uint32_t p = sel_at(b.sel, k);
+      const std::size_t r = rows + k;
+      const bool ok = col.all_valid || validity::get_bit(col.validity, p);
+      if (!ok) {
+        validity::set_bit(bits.data(), r, false);
+        any_null[c] = true;
+      }
+      if (types[c] == Type::STR) {
+        int32_t id = 0;
+        if (ok) id = ids[c]->intern(col.dict->at(reinterpret_cast<const int32_t*>(col.data)[p]));
+        std::memcpy(v.data() + r * 4, &id, 4);
+      } else {
+        std::memcpy(v.data() + r * w, col.data + static_cast<std::size_t>(p) * w, w);
+      }
+    }
+  }
+  rows = new_rows;
+}
+
+std::vector<qeg_column> Staging::columns() const {
+  std::vector<qeg_column> out(types.size());
+  for (std::size_t c = 0; c < types.size(); ++c) {
+    qeg_column q{};
+    // STR values are already canonical ids: hand them over as I32.
+    q.type = types[c] == Type::STR ? QEG_I32 : to_qeg(types[c]);
+    q.len = rows;
+    q.data = vals[c].data();
+    q.all_valid = any_null[c] ? 0 : 1;
+    q.validity = any_null[c] ? valid[c].data() : nullptr;
+    out[c] = q;
+  }
+  return out;
+}
+
+Device::Device(int device) {
+  const qeg_status s = qeg_ctx_create(device, &ctx_);
+  if (s != QEG_OK) throw std::runtime_error(std::string("GPU context: ") + qeg_last_error(nullptr));
+}
+
+Device::~Device() { qeg_ctx_destroy(ctx_); }
+
+void Device::check(qeg_status s) const {
+  if (s == QEG_OK) return;
+  const std::string m = qeg_last_error(ctx_);
+  if (s == QEG_ERR_INVALID) throw std::invalid_argument(m);
+  if (s == QEG_ERR_OVERFLOW) throw std::overflow_error(m);
+  if (s == QEG_ERR_OOM) throw std::bad_alloc();
+  throw std::runtime_error(m);
+}
+
+// ---------------------------------------------------------------------------
+// GpuAggregate
+// ---------------------------------------------------------------------------
+GpuAggregate::GpuAggregate(std::unique_ptr<Operator> child, std::vector<std::uint32_t> key_cols,
+                           std::vector<AggSpec> aggs, qeg_agg_config cfg, int device)
+    : child_(std::move(child)), key_cols_(std::move(key_cols)), aggs_(std::move(aggs)), cfg_(cfg), device_(device) {
+  if (aggs_.empty()) throw std::invalid_argument("Aggregate needs >=1 aggregate");
+  child_schema_ = child_->output_schema();
+}
+
+GpuAggregate::~GpuAggregate() { close(); }
+
+Schema GpuAggregate::output_schema() const {
+  Schema s;
+  for (std::uint32_t k : key_cols_) s.fields.push_back(child_schema_.fields[k]);
+  for (const AggSpec& a : aggs_) {
+    const Type in = a.func == AggFunc::CountStar ? Type::I64 : child_schema_.fields[a.input_col].second;
+    s.fields.emplace_back(a.out_name, result_type(a.func, in));
+  }
+  return s;
+}
+
+void GpuAggregate::flush() {
+  if (staging_.rows == 0) return;
+  const auto cols = staging_.columns();
+  dev_->check(qeg_agg_consume(agg_, cols.data(), static_cast<int>(cols.size()), nullptr, 0));
+  staging_.reset(staging_.types);
+}
+
+void GpuAggregate::open() {
+  if (opened_) return;
+  opened_ = true;
+  dev_ = std::make_unique<Device>(device_);
+  std::vector<Type> types;
+  std::vector<int32_t> qtypes;
+  for (const auto& f : child_schema_.fields) {
+    types.push_back(f.second);
+    qtypes.push_back(f.second == Type::STR ? QEG_I32 : to_qeg(f.second));
+    if (f.second == Type::STR) has_str_ = true;
+  }
+  std::vector<qeg_agg_spec> specs;
+  for (const AggSpec& a : aggs_) {
+    const Type in = a.func == AggFunc::CountStar ? Type::I64 : child_schema_.fields[a.input_col].second;
+    result_type(a.func, in);  // raises the reference's errors (SUM/AVG on STR)
+    specs.push_back({agg_func(a.func), a.input_col});
+  }
+  dev_->check(qeg_agg_create(dev_->ctx(), qtypes.data(), static_cast<int>(qtypes.size()), key_cols_.data(),
+                             static_cast<int>(key_cols_.size()), specs.data(), static_cast<int>(specs.size()), &cfg_,
+                             &agg_));
+  staging_.reset(types);
+  str_ids_.assign(types.size(), nullptr);
+  std::vector<StringDict*> ids(types.size(), nullptr);
+  for (std::size_t c = 0; c < types.size(); ++c)
+    if (types[c] == Type::STR) {
+      str_ids_[c] = std::make_shared<StringDict>();
+      ids[c] = str_ids_[c].get();
+    }
+
+  // STR ids must be order-preserving for MIN/MAX by value: with STR columns
+  // the whole input is staged first and the ids re-ranked in string order.
+  child_->open();
+  while (std::optional<Batch> b = child_->next()) {
+    staging_.append(*b, ids);
+    if (!has_str_ && staging_.rows >= kChunkRows) flush();
+  }
+  child_->close();
+  std::vector<std::vector<int32_t>> rank_to_id(types.size());
+  if (has_str_) {
+    for (std::size_t c = 0; c < types.size(); ++c) {
+      if (!str_ids_[c]) continue;
+      const StringDict& d = *str_ids_[c];
+      std::vector<int32_t> order(d.size());
+      for (std::size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int32_t>(i);
+      std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return d.at(a) < d.at(b); });
+      std::vector<int32_t> rank(d.size());
+      for (std::size_t r = 0; r < order.size(); ++r) rank[order[r]] = static_cast<int32_t>(r);
+      auto* v = reinterpret_cast<int32_t*>(staging_.vals[c].data());
+      for (std::size_t r = 0; r < staging_.rows; ++r)
+        if (validity::get_bit(staging_.valid[c].data(), r)) v[r] = rank[v[r]];
+      rank_to_id[c] = std::move(order);
+    }
+  }
+  flush();
+  uint64_t n = 0;
+  dev_->check(qeg_agg_finish(agg_, &n));
+  nrows_ = n;
+  const Schema out = output_schema();
+  result_.assign(out.fields.size(), {});
+  std::vector<qeg_out_column> outs(out.fields.size());
+  std::vector<int32_t> all_valid(out.fields.size(), 1);
+  for (std::size_t c = 0; c < out.fields.size(); ++c) {
+    HostColumn& h = result_[c];
+    h.type = out.fields[c].second;
+    h.len = nrows_;
+    h.data.resize(std::max<std::size_t>(1, nrows_ * byte_width(h.type)));
+    h.validity.resize(std::max<std::size_t>(1, validity::words(nrows_)));
+    outs[c] = {h.data.data(), h.validity.data(), &all_valid[c]};
+  }
+  dev_->check(qeg_agg_fetch(agg_, 0, nrows_, outs.data()));
+  // STR results: ranks back to strings, published through an owned dict.
+  out_dicts_.assign(out.fields.size(), nullptr);
+  for (std::size_t c = 0; c < out.fields.size(); ++c) {
+    if (all_valid[c]) result_[c].validity.clear();
+    if (out.fields[c].second != Type::STR) continue;
+    const std::uint32_t src = c < key_cols_.size() ? key_cols_[c] : aggs_[c - key_cols_.size()].input_col;
+    const StringDict& d = *str_ids_[src];
+    auto dict = std::make_shared<StringDict>();
+    auto* v = reinterpret_cast<int32_t*>(result_[c].data.data());
+    for (std::size_t r = 0; r < nrows_; ++r) {
+      if (!result_[c].validity.empty() && !validity::get_bit(result_[c].validity.data(), r)) continue;
+      v[r] = dict->intern(d.at(rank_to_id[src][v[r]]));
+    }
+    out_dicts_[c] = dict;
+    result_[c].dict = dict;
+  }
+  cursor_ = 0;
+}
+
+std::optional<Batch> GpuAggregate::next() {
+  if (cursor_ >= nrows_) return std::nullopt;
+  const std::size_t m = std::min(kOutBatch, nrows_ - cursor_);
+  current_.assign(result_.size(), {});
+  Batch b;
+  for (std::size_t c = 0; c < result_.size(); ++c) {
+    const HostColumn& src = result_[c];
+    HostColumn& h = current_[c];
+    const std::size_t w = byte_width(src.type);
+    h.type = src.type;
+    h.len = m;
+    h.dict = src.dict;
+    h.data.assign(src.data.begin() + cursor_ * w, src.data.begin() + (cursor_ + m) * w);
+    if (!src.validity.empty()) {
+      h.validity.assign(validity::words(m), ~0ull);
+      bool any = false;
+      for (std::size_t r = 0; r < m; ++r)
+        if (!validity::get_bit(src.validity.data(), cursor_ + r)) {
+          validity::set_bit(h.validity.data(), r, false);
+          any = true;
+        }
+      if (!any) h.validity.clear();
+    }
+    b.cols.push_back(h.view());
+  }
+  b.sel = nullptr;
+  b.row_count = m;
+  cursor_ += m;
+  return b;
+}
+
+void GpuAggregate::close() {
+  if (agg_) qeg_agg_destroy(agg_);
+  agg_ = nullptr;
+  dev_.reset();
+  opened_ = false;
+}
+
+// ---------------------------------------------------------------------------
+// GpuHashJoin
+// ---------------------------------------------------------------------------
+GpuHashJoin::GpuHashJoin(std::unique_ptr<Operator> probe, std::unique_ptr<Operator> build,
+                         std::vector<std::uint32_t> probe_keys, std::vector<std::uint32_t> build_keys, JoinType type,
+                         qeg_join_config cfg, int device)
+    : probe_(std::move(probe)),
+      build_(std::move(build)),
+      probe_keys_(std::move(probe_keys)),
+      build_keys_(std::move(build_keys)),
+      type_(type),
+      cfg_(cfg),
+      device_(device) {
+  if (probe_keys_.size() != build_keys_.size() || probe_keys_.empty())
+    throw std::invalid_argument("join needs equal-length, non-empty key lists");
+  probe_schema_ = probe_->output_schema();
+  build_schema_ = build_->output_schema();
+  for (std::size_t i = 0; i < probe_keys_.size(); ++i)
+    if (probe_schema_.fields[probe_keys_[i]].second != build_schema_.fields[build_keys_[i]].second)
+      throw std::invalid_argument("HashJoin: join key column types must match positionally");
+}
+
+GpuHashJoin::~GpuHashJoin() { close(); }
+
+Schema GpuHashJoin::output_schema() const {
+  Schema s;
+  for (const auto& f : probe_schema_.fields) s.fields.push_back(f);
+  for (const auto& f : build_schema_.fields) s.fields.push_back(f);
+  return s;
+}
+
+void GpuHashJoin::open() {
+  if (opened_) return;
+  opened_ = true;
+  probe_done_ = false;
+  pending_ = cursor_ = 0;
+  dev_ = std::make_unique<Device>(device_);
+  std::vector<Type> ptypes, btypes;
+  std::vector<int32_t> qp, qb;
+  for (const auto& f : probe_schema_.fields) {
+    ptypes.push_back(f.second);
+    qp.push_back(f.second == Type::STR ? QEG_I32 : to_qeg(f.second));
+  }
+  for (const auto& f : build_schema_.fields) {
+    btypes.push_back(f.second);
+    qb.push_back(f.second == Type::STR ? QEG_I32 : to_qeg(f.second));
+  }
+  dev_->check(qeg_join_create(dev_->ctx(), qp.data(), static_cast<int>(qp.size()), qb.data(),
+                              static_cast<int>(qb.size()), probe_keys_.data(), build_keys_.data(),
+                              static_cast<int>(probe_keys_.size()), type_ == JoinType::Left ? QEG_LEFT : QEG_INNER,
+                              &cfg_, &join_));
+  // STR: key positions share one value-id space between the sides
+  // (ops/join.cpp:48-71); other STR columns get their own dict.
+  probe_ids_.assign(ptypes.size(), nullptr);
+  build_ids_.assign(btypes.size(), nullptr);
+  for (std::size_t i = 0; i < build_keys_.size(); ++i)
+    if (btypes[build_keys_[i]] == Type::STR) {
+      auto d = std::make_shared<StringDict>();
+      build_ids_[build_keys_[i]] = d;
+      probe_ids_[probe_keys_[i]] = d;
+    }
+  for (std::size_t c = 0; c < btypes.size(); ++c)
+    if (btypes[c] == Type::STR && !build_ids_[c]) build_ids_[c] = std::make_shared<StringDict>();
+  for (std::size_t c = 0; c < ptypes.size(); ++c)
+    if (ptypes[c] == Type::STR && !probe_ids_[c]) probe_ids_[c] = std::make_shared<StringDict>();
+  std::vector<StringDict*> bids(btypes.size(), nullptr);
+  for (std::size_t c = 0; c < btypes.size(); ++c) bids[c] = build_ids_[c].get();
+  Staging bs;
+  bs.reset(btypes);
+  build_->open();
+  while (std::optional<Batch> b = build_->next()) {
+    bs.append(*b, bids);
+    if (bs.rows >= (8u << 20)) {
+      const auto cols = bs.columns();
+      dev_->check(qeg_join_build(join_, cols.data(), static_cast<int>(cols.size())));
+      bs.reset(btypes);
+    }
+  }
+  build_->close();
+  if (bs.rows) {
+    const auto cols = bs.columns();
+    dev_->check(qeg_join_build(join_, cols.data(), static_cast<int>(cols.size())));
+  }
+  dev_->check(qeg_join_build_finish(join_));
+  probe_stage_.reset(ptypes);
+  probe_->open();
+}
+
+bool GpuHashJoin::probe_next_batch() {
+  std::optional<Batch> b = probe_->next();
+  if (!b) return false;
+  std::vector<StringDict*> pids(probe_stage_.types.size(), nullptr);
+  for (std::size_t c = 0; c < pids.size(); ++c) pids[c] = probe_ids_[c].get();
+  probe_stage_.reset(probe_stage_.types);
+  probe_stage_.append(*b, pids);
+  const auto cols = probe_stage_.columns();
+  uint64_t n = 0;
+  dev_->check(qeg_join_probe(join_, cols.data(), static_cast<int>(cols.size()), &n));
+  pending_ = n;
+  cursor_ = 0;
+  return true;
+}
+
+std::optional<Batch> GpuHashJoin::next() {
+  while (cursor_ >= pending_) {
+    if (probe_done_ || !probe_next_batch()) {
+      probe_done_ = true;
+      return std::nullopt;
+    }
+  }
+  const std::size_t m = std::min<std::uint64_t>(kOutBatch, pending_ - cursor_);
+  const Schema out = output_schema();
+  current_.assign(out.fields.size(), {});
+  std::vector<qeg_out_column> outs(out.fields.size());
+  std::vector<int32_t> all_valid(out.fields.size(), 1);
+  for (std::size_t c = 0; c < out.fields.size(); ++c) {
+    HostColumn& h = current_[c];
+    h.type = out.fields[c].second;
+    h.len = m;
+    h.data.resize(std::max<std::size_t>(1, m * byte_width(h.type)));
+    h.validity.resize(validity::words(m));
+    outs[c] = {h.data.data(), h.validity.data(), &all_valid[c]};
+  }
+  dev_->check(qeg_join_fetch(join_, cursor_, m, outs.data()));
+  Batch b;
+  const std::size_t np = probe_schema_.fields.size();
+  for (std::size_t c = 0; c < out.fields.size(); ++c) {
+    HostColumn& h = current_[c];
+    if (all_valid[c]) h.validity.clear();
+    if (h.type == Type::STR) h.dict = c < np ? probe_ids_[c] : build_ids_[c - np];
+    b.cols.push_back(h.view());
+  }
+  b.sel = nullptr;
+  b.row_count = m;
+  cursor_ += m;
+  return b;
+}
+
+void GpuHashJoin::close() {
+  if (opened_ && probe_) probe_->close();
+  if (join_) qeg_join_destroy(join_);
+  join_ = nullptr;
+  dev_.reset();
+  opened_ = false;
+}
+
+}  // namespace qe::gpu

@@ -1,0 +1,140 @@
+// qe_contract.h -- the reference engine's frozen operator contract, restated so
+// the GPU operators in this directory build standalone.
+//
+// The GPU operators must be drop-in replacements inside the reference's plan
+// trees, so these declarations are kept layout- and signature-identical to the
+// reference's frozen headers:
+//   Type / byte_width          core/types.h:18-48
+//   Column, SelectionVector,
+//   Batch, Schema              core/column.h:55-90
+//   validity word helpers      core/validity.h:21-63
+//   Operator                   ops/operator.h:40-47
+//   StringDict (interface)     core/string_dict.h:34-72
+//   AggFunc / AggSpec          ops/aggregate.h:61-89
+//   JoinType                   ops/join.h:59
+// When compiled inside the reference tree, define QEG_WITH_REFERENCE_HEADERS
+// and the reference's own headers are used instead of these.
+#pragma once
+
+#ifdef QEG_WITH_REFERENCE_HEADERS
+#include "core/column.h"
+#include "core/string_dict.h"
+#include "core/types.h"
+#include "core/validity.h"
+#include "ops/aggregate.h"
+#include "ops/join.h"
+#include "ops/operator.h"
+#else
+
+#include <cstddef>
+#include <cstdint>
+#include <optional>
+#include <string>
+#include <string_view>
+#include <unordered_map>
+#include <utility>
+#include <vector>
+
+namespace qe {
+
+enum class Type { I32, I64, F64, BOOL, TS, STR };
+
+inline constexpr std::size_t byte_width(Type t) {
+  switch (t) {
+    case Type::I32: return 4;
+    case Type::I64: return 8;
+    case Type::F64: return 8;
+    case Type::BOOL: return 1;
+    case Type::TS: return 8;
+    case Type::STR: return 4;
+  }
+  return 0;
+}
+
+class StringDict {
+ public:
+  StringDict() { offsets_.push_back(0); }
+  std::int32_t intern(std::string_view s) {
+    std::string key(s);
+    auto it = index_.find(key);
+    if (it != index_.end()) return it->second;
+    const auto code = static_cast<std::int32_t>(offsets_.size() - 1);
+    bytes_.insert(bytes_.end(), s.begin(), s.end());
+    offsets_.push_back(static_cast<std::uint32_t>(bytes_.size()));
+    index_.emplace(std::move(key), code);
+    return code;
+  }
+  std::string_view at(std::int32_t code) const {
+    const auto c = static_cast<std::size_t>(code);
+    return std::string_view(bytes_.data() + offsets_[c], offsets_[c + 1] - offsets_[c]);
+  }
+  std::size_t size() const noexcept { return offsets_.size() - 1; }
+
+ private:
+  std::vector<char> bytes_;
+  std::vector<std::uint32_t> offsets_;
+  std::unordered_map<std::string, std::int32_t> index_;
+};
+
+struct Column {
+  Type type;
+  size_t len;
+  const std::byte* data;
+  const uint64_t* validity;
+  bool all_valid;
+  const StringDict* dict;
+};
+
+struct SelectionVector {
+  const uint32_t* idx;
+  size_t len;
+};
+
+struct Batch {
+  std::vector<Column> cols;
+  const SelectionVector* sel;
+  size_t row_count;
+};
+
+struct Schema {
+  std::vector<std::pair<std::string, Type>> fields;
+};
+
+namespace validity {
+inline constexpr std::size_t words(std::size_t nbits) { return (nbits + 63) / 64; }
+inline bool get_bit(const std::uint64_t* w, std::size_t i) { return (w[i >> 6] >> (i & 63u)) & 1ull; }
+inline void set_bit(std::uint64_t* w, std::size_t i, bool valid) {
+  const std::uint64_t bit = std::uint64_t{1} << (i & 63u);
+  if (valid) w[i >> 6] |= bit;
+  else w[i >> 6] &= ~bit;
+}
+}  // namespace validity
+
+class Operator {
+ public:
+  virtual void open() = 0;
+  virtual std::optional<Batch> next() = 0;
+  virtual void close() = 0;
+  virtual Schema output_schema() const = 0;
+  virtual ~Operator() = default;
+};
+
+enum class AggFunc { CountStar, Count, Sum, Min, Max, Avg };
+
+struct AggSpec {
+  AggFunc func = AggFunc::CountStar;
+  std::uint32_t input_col = 0;
+  std::string out_name;
+  static AggSpec count_star(std::string name) { return {AggFunc::CountStar, 0, std::move(name)}; }
+  static AggSpec count(std::uint32_t col, std::string name) { return {AggFunc::Count, col, std::move(name)}; }
+  static AggSpec sum(std::uint32_t col, std::string name) { return {AggFunc::Sum, col, std::move(name)}; }
+  static AggSpec min(std::uint32_t col, std::string name) { return {AggFunc::Min, col, std::move(name)}; }
+  static AggSpec max(std::uint32_t col, std::string name) { return {AggFunc::Max, col, std::move(name)}; }
+  static AggSpec avg(std::uint32_t col, std::string name) { return {AggFunc::Avg, col, std::move(name)}; }
+};
+
+enum class JoinType { Inner, Left };
+
+}  // namespace qe
+
+#endif  // QEG_WITH_REFERENCE_HEADERS

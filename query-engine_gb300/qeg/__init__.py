@@ -94,6 +94,14 @@ def lib():
             "qeg_join_count_sum_result": (i32, [vp, P(ctypes.c_int64), P(ctypes.c_int64), P(i32)]),
             "qeg_join_stats": (i32, [vp, P(i32), P(i32), P(u64)]),
             "qeg_join_destroy": (None, [vp]),
+            "qeg_sketch": (i32, [vp, vp, u64, vp, P(ctypes.c_double), P(ctypes.c_double)]),
+            "qeg_estimator_init": (i32, [vp, u64]),
+            "qeg_estimator_set_weights": (i32, [vp, vp]),
+            "qeg_estimator_get_weights": (i32, [vp, vp]),
+            "qeg_estimator_predict": (i32, [vp, vp, ctypes.c_uint32, vp]),
+            "qeg_estimator_grad": (i32, [vp, vp, vp, ctypes.c_uint32, P(ctypes.c_float), vp]),
+            "qeg_estimator_train": (i32, [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                          ctypes.c_float, u64, P(ctypes.c_float)]),
         }
         for name, (res, args) in list(sig.items()) + list(optional.items()):
             if not hasattr(L, name):
@@ -259,6 +267,24 @@ class Aggregate:
         _check(lib().qeg_agg_fetch(self.p, first, count, outs), self.ctx.p)
         return [(v[:count], unpack_validity(w, count)) for v, w, _ in keep]
 
+    def fetch_torch(self, first=0, count=None):
+        """Like fetch(), into torch CUDA tensors: [(values, validity words)]."""
+        import torch
+
+        if count is None:
+            count = self.rows - first
+        tdt = {I32: torch.int32, I64: torch.int64, F64: torch.float64, BOOL: torch.uint8, TS: torch.int64,
+               STR: torch.int32}
+        outs = (OutColumn * len(self.result_types))()
+        keep = []
+        for i, t in enumerate(self.result_types):
+            v = torch.empty(max(count, 1), dtype=tdt[t], device="cuda")
+            w = torch.empty(max(1, (count + 63) // 64), dtype=torch.int64, device="cuda")
+            keep.append((v, w))
+            outs[i] = OutColumn(v.data_ptr(), w.data_ptr(), None)
+        _check(lib().qeg_agg_fetch(self.p, first, count, outs), self.ctx.p)
+        return [(v[:count], w) for v, w in keep]
+
     def stats(self):
         cap, rs, st, hk, est = (ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_int32(), ctypes.c_int32(),
                                 ctypes.c_double())
@@ -377,3 +403,61 @@ class Join:
             self.close()
         except Exception:
             pass
+
+
+# ---- sketch and learned estimator -------------------------------------------
+SKETCH_FEATURES = 80
+MLP_PARAMS = 9474
+
+
+def sketch(ctx, col, sample_rows=0):
+    """80 sketch features of a key column, the classic (non-learned) distinct
+    estimate, and the sampled share of rows in the top-2048 candidates."""
+    f = np.zeros(SKETCH_FEATURES, dtype=np.float32)
+    g, s = ctypes.c_double(), ctypes.c_double()
+    c = col.c()
+    _check(lib().qeg_sketch(ctx.p, ctypes.byref(c), sample_rows, f.ctypes.data, ctypes.byref(g), ctypes.byref(s)),
+           ctx.p)
+    return f, g.value, s.value
+
+
+def estimator_init(ctx, seed):
+    _check(lib().qeg_estimator_init(ctx.p, seed), ctx.p)
+
+
+def estimator_set_weights(ctx, params):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    assert p.size == MLP_PARAMS
+    _check(lib().qeg_estimator_set_weights(ctx.p, p.ctypes.data), ctx.p)
+
+
+def estimator_get_weights(ctx):
+    p = np.zeros(MLP_PARAMS, dtype=np.float32)
+    _check(lib().qeg_estimator_get_weights(ctx.p, p.ctypes.data), ctx.p)
+    return p
+
+
+def estimator_predict(ctx, features):
+    x = np.ascontiguousarray(features, dtype=np.float32).reshape(-1, SKETCH_FEATURES)
+    y = np.zeros((x.shape[0], 2), dtype=np.float32)
+    _check(lib().qeg_estimator_predict(ctx.p, x.ctypes.data, x.shape[0], y.ctypes.data), ctx.p)
+    return y
+
+
+def estimator_grad(ctx, x, t):
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, SKETCH_FEATURES)
+    t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, 2)
+    g = np.zeros(MLP_PARAMS, dtype=np.float32)
+    loss = ctypes.c_float()
+    _check(lib().qeg_estimator_grad(ctx.p, x.ctypes.data, t.ctypes.data, x.shape[0], ctypes.byref(loss),
+                                    g.ctypes.data), ctx.p)
+    return loss.value, g
+
+
+def estimator_train(ctx, x, t, epochs, batch, lr, seed):
+    x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, SKETCH_FEATURES)
+    t = np.ascontiguousarray(t, dtype=np.float32).reshape(-1, 2)
+    loss = ctypes.c_float()
+    _check(lib().qeg_estimator_train(ctx.p, x.ctypes.data, t.ctypes.data, x.shape[0], epochs, batch, lr, seed,
+                                     ctypes.byref(loss)), ctx.p)
+    return loss.value

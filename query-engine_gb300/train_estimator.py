@@ -1,0 +1,152 @@
+"""Trains the learned cardinality / skew estimator on the GPU.
+
+Training pairs are (sketch features, exact statistics) of seeded synthetic key
+columns: the features come from qeg_sketch (a 2^20-row strided sample), the
+targets from the exact GROUP BY engine over the whole column -- the number of
+groups and the share of rows carried by the 2048 largest groups. Families:
+uniform over a domain, Zipf(s) for s in [0.3, 1.6], a sequential key with
+duplication, and a mixture (uniform background plus a heavy head). Row counts
+and domains are log-uniform so the sample fraction varies from 1 to ~1/256.
+
+The network is trained with the project's forward / backward / Adam kernels
+(qeg_estimator_train) and written to query-engine_gb300/estimator_weights.f32,
+with a report of its error next to the classic estimator's on held-out data.
+
+    python query-engine_gb300/train_estimator.py [--datasets N] [--out PATH]
+"""
+import argparse
+import json
+import math
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+import qeg  # noqa: E402
+
+HOT_K = 2048
+
+
+def gen_keys(rng, g, dev):
+    """One seeded key column: (keys int64 tensor, description)."""
+    n = int(2 ** rng.uniform(14, 27.5))
+    fam = rng.choice(["uniform", "zipf", "sequential", "mixture"], p=[0.3, 0.4, 0.1, 0.2])
+    dom = int(2 ** rng.uniform(2, 28))
+    if fam == "uniform":
+        k = torch.randint(0, dom, (n,), generator=g, device=dev, dtype=torch.int64)
+        desc = {"family": fam, "domain": dom}
+    elif fam == "zipf":
+        s = float(rng.uniform(0.3, 1.6))
+        dom = min(dom, 1 << 26)
+        cdf = torch.arange(1, dom + 1, dtype=torch.float64, device=dev).pow_(-s).cumsum_(0)
+        cdf /= cdf[-1].clone()
+        r = torch.searchsorted(cdf, torch.rand(n, generator=g, device=dev, dtype=torch.float64)).clamp_(max=dom - 1)
+        perm = torch.randint(0, 1 << 62, (dom,), generator=g, device=dev, dtype=torch.int64)
+        k = perm[r]
+        desc = {"family": fam, "domain": dom, "s": s}
+    elif fam == "sequential":
+        rep = int(2 ** rng.uniform(0, 8))
+        k = torch.arange(n, device=dev, dtype=torch.int64) // rep
+        k = k[torch.randperm(n, generator=g, device=dev)]
+        desc = {"family": fam, "repeat": rep}
+    else:
+        head = int(2 ** rng.uniform(0, 12))
+        frac = float(rng.uniform(0.1, 0.9))
+        hot = torch.rand(n, generator=g, device=dev) < frac
+        k = torch.where(hot, torch.randint(0, head, (n,), generator=g, device=dev, dtype=torch.int64),
+                        torch.randint(head, head + dom, (n,), generator=g, device=dev, dtype=torch.int64))
+        desc = {"family": fam, "domain": dom, "head": head, "hot_frac": frac}
+    desc["rows"] = n
+    return k.contiguous(), desc
+
+
+def exact_stats(ctx, keys):
+    """Exact group count and top-2048 share, from the exact GROUP BY engine."""
+    cfg = qeg.agg_config(expected_groups=max(1024, min(keys.numel(), 1 << 27)))
+    a = qeg.Aggregate(ctx, [qeg.I64], [0], [(qeg.COUNT_STAR, 0)], cfg)
+    a.consume([qeg.Col(keys, None, qeg.I64)])
+    n = a.finish()
+    counts = a.fetch_torch()[1][0]
+    a.close()
+    share = float(torch.topk(counts, min(HOT_K, n)).values.sum().item()) / max(1, keys.numel())
+    return n, share
+
+
+def targets(groups, share):
+    return [math.log2(1.0 + groups) / 32.0, share]
+
+
+def build_set(ctx, rng, count, dev, seed):
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    X, T, C, D = [], [], [], []
+    for i in range(count):
+        keys, desc = gen_keys(rng, g, dev)
+        f, classic, _ = qeg.sketch(ctx, qeg.Col(keys, None, qeg.I64))
+        groups, share = exact_stats(ctx, keys)
+        X.append(f)
+        T.append(targets(groups, share))
+        C.append(classic)
+        desc.update({"groups": groups, "top_share": share, "classic": classic})
+        D.append(desc)
+        del keys
+    return np.array(X, np.float32), np.array(T, np.float32), np.array(C), D
+
+
+def log2_err(est, true):
+    return abs(math.log2(max(est, 1.0)) - math.log2(max(true, 1.0)))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--datasets", type=int, default=1200)
+    ap.add_argument("--heldout", type=int, default=200)
+    ap.add_argument("--epochs", type=int, default=400)
+    ap.add_argument("--out", default=os.path.join(HERE, "estimator_weights.f32"))
+    ap.add_argument("--report", default=None)
+    ap.add_argument("--seed", type=int, default=20260615)
+    args = ap.parse_args()
+    dev = torch.device("cuda", 0)
+    ctx = qeg.Context(0)
+    rng = np.random.default_rng(args.seed)
+    t0 = time.time()
+    X, T, C, D = build_set(ctx, rng, args.datasets, dev, args.seed)
+    Xh, Th, Ch, Dh = build_set(ctx, rng, args.heldout, dev, args.seed + 1)
+    t_data = time.time() - t0
+    qeg.estimator_init(ctx, args.seed)
+    t1 = time.time()
+    losses = []
+    for phase, lr in ((args.epochs // 2, 3e-3), (args.epochs // 4, 1e-3), (args.epochs - 3 * (args.epochs // 4), 3e-4)):
+        losses.append(qeg.estimator_train(ctx, X, T, phase, 64, lr, args.seed + len(losses)))
+    t_train = time.time() - t1
+    w = qeg.estimator_get_weights(ctx)
+    w.astype("<f4").tofile(args.out)
+    Y = qeg.estimator_predict(ctx, Xh)
+    learned = [2 ** (32 * float(y[0])) - 1 for y in Y]
+    true = [d["groups"] for d in Dh]
+    e_learned = [log2_err(a, b) for a, b in zip(learned, true)]
+    e_classic = [log2_err(a, b) for a, b in zip(Ch, true)]
+    share_err = [abs(float(y[1]) - d["top_share"]) for y, d in zip(Y, Dh)]
+    report = {
+        "datasets": args.datasets, "heldout": args.heldout, "epochs": args.epochs,
+        "train_loss": losses, "data_s": t_data, "train_s": t_train,
+        "heldout_median_abs_log2_error": {"learned": float(np.median(e_learned)),
+                                          "classic": float(np.median(e_classic))},
+        "heldout_p90_abs_log2_error": {"learned": float(np.percentile(e_learned, 90)),
+                                       "classic": float(np.percentile(e_classic, 90))},
+        "heldout_top_share_mae": float(np.mean(share_err)),
+    }
+    print(json.dumps(report))
+    if args.report:
+        with open(args.report, "w") as f:
+            json.dump(report, f, indent=1)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

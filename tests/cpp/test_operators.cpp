@@ -1,0 +1,364 @@
+// Drives qe::gpu::GpuAggregate / GpuHashJoin through the reference's pull
+// interface (Operator::open/next/close, Batch/Column views) exactly as a plan
+// tree would, and checks the drained results against values computed here on
+// the CPU and against expectations written in the reference's own tests.
+// Exit code 0 = all checks passed.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <random>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../query-engine_gb300/host/gpu_operators.h"
+
+using namespace qe;
+
+static int g_fail = 0;
+#define CHECK(c)                                                        \
+  do {                                                                  \
+    if (!(c)) {                                                         \
+      std::fprintf(stderr, "CHECK failed at line %d: %s\n", __LINE__, #c); \
+      ++g_fail;                                                         \
+    }                                                                   \
+  } while (0)
+
+// A columnar table and a Scan over it: zero-copy windows of `batch` rows
+// (a multiple of 64), validity re-based by whole words (ops/scan.cpp:27-64).
+struct TestTable {
+  Schema schema;
+  std::vector<gpu::HostColumn> cols;
+};
+
+class TestScan : public Operator {
+ public:
+  TestScan(const TestTable& t, std::size_t batch) : t_(t), batch_(batch) {}
+  void open() override { cur_ = 0; }
+  std::optional<Batch> next() override {
+    const std::size_t n = t_.cols.empty() ? 0 : t_.cols[0].len;
+    if (cur_ >= n) return std::nullopt;
+    const std::size_t m = std::min(batch_, n - cur_);
+    Batch b;
+    for (const auto& c : t_.cols) {
+      Column v = c.view();
+      v.len = m;
+      v.data += cur_ * byte_width(c.type);
+      if (!v.all_valid) v.validity += cur_ / 64;
+      b.cols.push_back(v);
+    }
+    b.sel = nullptr;
+    b.row_count = m;
+    cur_ += m;
+    return b;
+  }
+  void close() override {}
+  Schema output_schema() const override { return t_.schema; }
+
+ private:
+  const TestTable& t_;
+  std::size_t batch_, cur_ = 0;
+};
+
+// Emits prepared batches that carry selection vectors and their own dicts.
+class BatchSource : public Operator {
+ public:
+  Schema schema;
+  std::vector<std::vector<gpu::HostColumn>> batches;
+  std::vector<std::vector<uint32_t>> sels;  // empty => dense
+  void open() override { i_ = 0; }
+  std::optional<Batch> next() override {
+    if (i_ >= batches.size()) return std::nullopt;
+    Batch b;
+    for (const auto& c : batches[i_]) b.cols.push_back(c.view());
+    if (!sels[i_].empty()) {
+      sv_ = {sels[i_].data(), sels[i_].size()};
+      b.sel = &sv_;
+      b.row_count = sels[i_].size();
+    } else {
+      b.sel = nullptr;
+      b.row_count = batches[i_][0].len;
+    }
+    ++i_;
+    return b;
+  }
+  void close() override {}
+  Schema output_schema() const override { return schema; }
+
+ private:
+  std::size_t i_ = 0;
+  SelectionVector sv_{nullptr, 0};
+};
+
+template <class T>
+gpu::HostColumn make_col(Type t, const std::vector<T>& v, const std::vector<std::size_t>& nulls = {}) {
+  gpu::HostColumn c;
+  c.type = t;
+  c.len = v.size();
+  c.data.resize(std::max<std::size_t>(1, v.size() * sizeof(T)));
+  if (!v.empty()) std::memcpy(c.data.data(), v.data(), v.size() * sizeof(T));
+  if (!nulls.empty()) {
+    c.validity.assign(validity::words(v.size()), ~0ull);
+    for (auto k : nulls) validity::set_bit(c.validity.data(), k, false);
+  }
+  return c;
+}
+
+gpu::HostColumn str_col(const std::vector<std::string>& dict, const std::vector<int32_t>& codes) {
+  gpu::HostColumn c = make_col(Type::STR, codes);
+  auto d = std::make_shared<StringDict>();
+  for (const auto& s : dict) d->intern(s);
+  c.dict = d;
+  return c;
+}
+
+struct Cell {
+  bool null = true;
+  int64_t i = 0;
+  double f = 0;
+  std::string s;
+  bool operator<(const Cell& o) const { return std::tie(null, i, f, s) < std::tie(o.null, o.i, o.f, o.s); }
+};
+using Row = std::vector<Cell>;
+
+std::vector<Row> drain(Operator& op) {
+  std::vector<Row> rows;
+  const Schema sch = op.output_schema();
+  op.open();
+  while (auto b = op.next()) {
+    CHECK(b->row_count >= 1 && b->row_count <= 2048);
+    CHECK(b->cols.size() == sch.fields.size());
+    for (std::size_t k = 0; k < b->row_count; ++k) {
+      const uint32_t p = b->sel ? b->sel->idx[k] : static_cast<uint32_t>(k);
+      Row r;
+      for (const Column& c : b->cols) {
+        Cell x;
+        x.null = !(c.all_valid || validity::get_bit(c.validity, p));
+        if (!x.null) {
+          switch (c.type) {
+            case Type::I32: x.i = reinterpret_cast<const int32_t*>(c.data)[p]; break;
+            case Type::I64:
+            case Type::TS: x.i = reinterpret_cast<const int64_t*>(c.data)[p]; break;
+            case Type::BOOL: x.i = reinterpret_cast<const uint8_t*>(c.data)[p]; break;
+            case Type::F64: x.f = reinterpret_cast<const double*>(c.data)[p]; break;
+            case Type::STR: x.s = std::string(c.dict->at(reinterpret_cast<const int32_t*>(c.data)[p])); break;
+          }
+        }
+        r.push_back(x);
+      }
+      rows.push_back(r);
+    }
+  }
+  CHECK(!op.next().has_value());  // stays exhausted
+  op.close();
+  return rows;
+}
+
+void test_aggregate_edge_table() {
+  // tests/aggregate_differential_test.cpp edge table of the reference.
+  TestTable t;
+  t.schema.fields = {{"c0", Type::I32}, {"c1", Type::I32}, {"c2", Type::F64}};
+  t.cols.push_back(make_col<int32_t>(Type::I32, {1, 1, 2, 2, 3, 1, 2, 3, 0, 0}, {8, 9}));
+  t.cols.push_back(make_col<int32_t>(Type::I32, {10, 20, 30, 40, 50, 60, 70, 80, 90, 100}, {0}));
+  t.cols.push_back(make_col<double>(Type::F64, {1.5, 2.5, 3.5, 4.5, 5.5, 6.5, 7.5, 8.5, 9.5, 10.5}, {2}));
+  for (std::size_t bs : {64, 256, 2048}) {
+    gpu::GpuAggregate agg(std::make_unique<TestScan>(t, bs), {0},
+                          {AggSpec::count_star("cs"), AggSpec::count(1, "c1"), AggSpec::sum(1, "s1"),
+                           AggSpec::min(1, "mn"), AggSpec::max(1, "mx"), AggSpec::avg(1, "av"),
+                           AggSpec::sum(2, "s2"), AggSpec::avg(2, "a2")});
+    const Schema s = agg.output_schema();
+    CHECK(s.fields.size() == 9 && s.fields[0].second == Type::I32 && s.fields[3].second == Type::I64 &&
+          s.fields[4].second == Type::I32 && s.fields[6].second == Type::F64);
+    std::map<int64_t, Row> by;
+    Row null_group;
+    for (Row& r : drain(agg)) {
+      if (r[0].null) null_group = r;
+      else by[r[0].i] = r;
+    }
+    CHECK(by.size() == 3 && !null_group.empty());
+    // key 1: rows 0 (c1 NULL), 1, 5 -> COUNT(*)=3, COUNT(c1)=2, SUM=80, MIN=20, MAX=60, AVG=40
+    CHECK(by[1][1].i == 3 && by[1][2].i == 2 && by[1][3].i == 80 && by[1][4].i == 20 && by[1][5].i == 60);
+    CHECK(std::fabs(by[1][6].f - 40.0) < 1e-12);
+    // key 2: rows 2 (c2 NULL), 3, 6 -> SUM(c2) = 4.5 + 7.5
+    CHECK(by[2][1].i == 3 && std::fabs(by[2][7].f - 12.0) < 1e-12 && std::fabs(by[2][8].f - 6.0) < 1e-12);
+    // NULL key group: rows 8, 9
+    CHECK(null_group[1].i == 2 && null_group[3].i == 190);
+  }
+}
+
+void test_aggregate_random_vs_cpu() {
+  std::mt19937_64 rng(42);
+  const std::size_t n = 100000;
+  std::vector<int64_t> k(n);
+  std::vector<double> v(n);
+  std::vector<std::size_t> nulls;
+  for (std::size_t i = 0; i < n; ++i) {
+    k[i] = static_cast<int64_t>(rng() % 5000) - 2500;
+    v[i] = static_cast<double>(rng() % 100000) / 7.0;
+    if (rng() % 20 == 0) nulls.push_back(i);
+  }
+  TestTable t;
+  t.schema.fields = {{"k", Type::I64}, {"v", Type::F64}};
+  t.cols.push_back(make_col(Type::I64, k));
+  t.cols.push_back(make_col(Type::F64, v, nulls));
+  std::vector<bool> isnull(n, false);
+  for (auto i : nulls) isnull[i] = true;
+  std::map<int64_t, std::tuple<int64_t, double, double, int64_t>> exp;  // count, sum, max, nn
+  for (std::size_t i = 0; i < n; ++i) {
+    auto& e = exp[k[i]];
+    std::get<0>(e)++;
+    if (!isnull[i]) {
+      std::get<1>(e) += v[i];
+      std::get<2>(e) = std::get<3>(e) ? std::max(std::get<2>(e), v[i]) : v[i];
+      std::get<3>(e)++;
+    }
+  }
+  gpu::GpuAggregate agg(std::make_unique<TestScan>(t, 2048), {0},
+                        {AggSpec::count_star("n"), AggSpec::sum(1, "s"), AggSpec::max(1, "m")});
+  std::size_t groups = 0;
+  for (Row& r : drain(agg)) {
+    ++groups;
+    const auto& e = exp[r[0].i];
+    CHECK(r[1].i == std::get<0>(e));
+    CHECK(std::fabs(r[2].f - std::get<1>(e)) <= 1e-9 + 1e-9 * std::fabs(std::get<1>(e)));
+    CHECK(r[3].f == std::get<2>(e));
+  }
+  CHECK(groups == exp.size());
+}
+
+void test_aggregate_str_by_value_and_selection() {
+  // Two batches with different dictionaries and a selection vector.
+  BatchSource* src = new BatchSource();
+  src->schema.fields = {{"sym", Type::STR}, {"q", Type::I64}};
+  src->batches.push_back({str_col({"AAPL", "MSFT", "GOOG"}, {0, 1, 2, 0}), make_col<int64_t>(Type::I64, {1, 2, 3, 4})});
+  src->sels.push_back({});
+  src->batches.push_back(
+      {str_col({"GOOG", "AAPL", "IBM", "MSFT"}, {1, 0, 2, 3, 3}), make_col<int64_t>(Type::I64, {10, 30, 7, 20, 99})});
+  src->sels.push_back({0, 1, 2, 3});  // row 4 (MSFT 99) is filtered out
+  gpu::GpuAggregate agg(std::unique_ptr<Operator>(src), {0},
+                        {AggSpec::count_star("n"), AggSpec::sum(1, "s"), AggSpec::min(0, "mn"), AggSpec::max(0, "mx")});
+  std::map<std::string, Row> by;
+  for (Row& r : drain(agg)) by[r[0].s] = r;
+  CHECK(by.size() == 4);
+  CHECK(by["AAPL"][1].i == 3 && by["AAPL"][2].i == 15);
+  CHECK(by["MSFT"][1].i == 2 && by["MSFT"][2].i == 22);
+  CHECK(by["GOOG"][1].i == 2 && by["GOOG"][2].i == 33);
+  CHECK(by["IBM"][1].i == 1 && by["IBM"][2].i == 7 && by["IBM"][3].s == "IBM" && by["IBM"][4].s == "IBM");
+}
+
+void test_aggregate_errors_and_global_empty() {
+  TestTable t;
+  t.schema.fields = {{"s", Type::STR}};
+  t.cols.push_back(str_col({"a"}, {}));
+  bool threw = false;
+  try {
+    gpu::GpuAggregate agg(std::make_unique<TestScan>(t, 64), {}, {AggSpec::sum(0, "x")});
+    agg.output_schema();
+  } catch (const std::invalid_argument&) {
+    threw = true;
+  }
+  CHECK(threw);  // SUM(STR) is a type error (ops/aggregate.cpp:85-90)
+  TestTable e;
+  e.schema.fields = {{"v", Type::I64}};
+  e.cols.push_back(make_col<int64_t>(Type::I64, {}));
+  gpu::GpuAggregate g(std::make_unique<TestScan>(e, 64), {}, {AggSpec::count_star("n"), AggSpec::sum(0, "s")});
+  auto rows = drain(g);
+  CHECK(rows.size() == 1 && rows[0][0].i == 0 && rows[0][1].null);
+}
+
+void test_join_edge_cases() {
+  // tests/join_differential_test.cpp one-key case of the reference.
+  TestTable b, p;
+  b.schema.fields = {{"c0", Type::I32}, {"c1", Type::I64}};
+  b.cols.push_back(make_col<int32_t>(Type::I32, {1, 1, 2, 5, 5, 5}));
+  b.cols.push_back(make_col<int64_t>(Type::I64, {10, 11, 20, 50, 51, 52}));
+  p.schema.fields = {{"c0", Type::I32}, {"c1", Type::I64}};
+  p.cols.push_back(make_col<int32_t>(Type::I32, {1, 2, 3, 5, 0}, {4}));
+  p.cols.push_back(make_col<int64_t>(Type::I64, {100, 200, 300, 500, 999}));
+  for (JoinType jt : {JoinType::Inner, JoinType::Left}) {
+    gpu::GpuHashJoin j(std::make_unique<TestScan>(p, 64), std::make_unique<TestScan>(b, 64), {0}, {0}, jt);
+    auto rows = drain(j);
+    std::multiset<std::tuple<int64_t, int64_t, bool, int64_t>> got;
+    for (Row& r : rows) got.insert({r[1].i, r[0].null ? -1 : r[0].i, r[3].null, r[3].null ? 0 : r[3].i});
+    std::multiset<std::tuple<int64_t, int64_t, bool, int64_t>> exp = {
+        {100, 1, false, 10}, {100, 1, false, 11}, {200, 2, false, 20},
+        {500, 5, false, 50}, {500, 5, false, 51}, {500, 5, false, 52}};
+    if (jt == JoinType::Left) {
+      exp.insert({300, 3, true, 0});
+      exp.insert({999, -1, true, 0});
+    }
+    CHECK(got == exp);
+  }
+  // 3000-row fan-out crosses the 2048-row output batch.
+  TestTable fb, fp;
+  fb.schema.fields = {{"k", Type::I32}, {"v", Type::I64}};
+  std::vector<int32_t> fk(3000, 7);
+  std::vector<int64_t> fv(3000);
+  for (int i = 0; i < 3000; ++i) fv[i] = i;
+  fb.cols.push_back(make_col(Type::I32, fk));
+  fb.cols.push_back(make_col(Type::I64, fv));
+  fp.schema.fields = {{"k", Type::I32}};
+  fp.cols.push_back(make_col<int32_t>(Type::I32, {7, 9, 7}));
+  gpu::GpuHashJoin fj(std::make_unique<TestScan>(fp, 64), std::make_unique<TestScan>(fb, 2048), {0}, {0},
+                      JoinType::Inner);
+  auto rows = drain(fj);
+  CHECK(rows.size() == 6000);
+  int64_t s = 0;
+  for (Row& r : rows) s += r[2].i;
+  CHECK(s == 2 * (2999LL * 3000 / 2));
+  // key type mismatch is rejected like the reference (ops/join.cpp:118-122)
+  TestTable m;
+  m.schema.fields = {{"k", Type::I64}};
+  m.cols.push_back(make_col<int64_t>(Type::I64, {1}));
+  bool threw = false;
+  try {
+    gpu::GpuHashJoin bad(std::make_unique<TestScan>(m, 64), std::make_unique<TestScan>(fp, 64), {0}, {0},
+                         JoinType::Inner);
+  } catch (const std::invalid_argument&) {
+    threw = true;
+  }
+  CHECK(threw);
+}
+
+void test_join_str_keys() {
+  BatchSource* build = new BatchSource();
+  build->schema.fields = {{"sym", Type::STR}, {"sector", Type::I32}};
+  build->batches.push_back({str_col({"IBM", "AAPL", "MSFT"}, {0, 1, 2}), make_col<int32_t>(Type::I32, {1, 2, 3})});
+  build->sels.push_back({});
+  BatchSource* probe = new BatchSource();
+  probe->schema.fields = {{"sym", Type::STR}};
+  probe->batches.push_back({str_col({"MSFT", "GOOG", "AAPL"}, {0, 1, 2, 2})});
+  probe->sels.push_back({});
+  gpu::GpuHashJoin j(std::unique_ptr<Operator>(probe), std::unique_ptr<Operator>(build), {0}, {0}, JoinType::Inner);
+  auto rows = drain(j);
+  std::multiset<std::pair<std::string, int64_t>> got;
+  for (Row& r : rows) {
+    CHECK(r[0].s == r[1].s);
+    got.insert({r[0].s, r[2].i});
+  }
+  CHECK((got == std::multiset<std::pair<std::string, int64_t>>{{"MSFT", 3}, {"AAPL", 2}, {"AAPL", 2}}));
+}
+
+int main() {
+  try {
+    test_aggregate_edge_table();
+    test_aggregate_random_vs_cpu();
+    test_aggregate_str_by_value_and_selection();
+    test_aggregate_errors_and_global_empty();
+    test_join_edge_cases();
+    test_join_str_keys();
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "exception: %s\n", e.what());
+    return 2;
+  }
+  if (g_fail) {
+    std::fprintf(stderr, "%d check(s) failed\n", g_fail);
+    return 1;
+  }
+  std::printf("all operator checks passed\n");
+  return 0;
+}
