@@ -272,6 +272,31 @@ qeg_status qeg_estimator_train(qeg_ctx* ctx, const float* x, const float* target
                                uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
                                float* final_loss);
 
+/* ---- join COUNT/SUM sink without device allocation ------------------------
+ * No counterpart in the reference (whose CPU operators allocate freely).
+ * For callers that must not call cudaMalloc -- code running during CUDA graph
+ * capture, engines whose device memory belongs to another allocator, paths
+ * that cannot risk an allocation stall at query time -- this runs the inner
+ * join's COUNT(*) / SUM(probe_val) sink entirely in a fixed scratch area built
+ * into the library: a file-scope static __device__ array of about 24 MiB that
+ * every GPU loading the library holds until the process exits. It allocates
+ * nothing: no cudaMalloc/cudaFree, no library allocator.
+ *   - All columns and `out` must be device pointers (no staging copies).
+ *   - The build side is limited to 1,048,576 rows; larger builds are rejected
+ *     with QEG_ERR_INVALID before any GPU work (use qeg_join_build instead).
+ *   - Work is enqueued on `cuda_stream` (a cudaStream_t; NULL = the legacy
+ *     default stream) and not synchronised; out[0] = matched row count,
+ *     out[1] = SUM of the probe payload, out[2] = 1 if that SUM is non-NULL,
+ *     out[3] = nonzero if the scratch table overflowed.
+ *   - The first call on a device looks up the scratch's device address (with
+ *     that device current); make it before any stream capture begins.
+ *   - Every call shares the one scratch array and clears what must start at
+ *     zero; calls whose GPU work overlaps race and corrupt each other.
+ * Errors: qeg_last_error(NULL) holds the message. */
+qeg_status qeg_join_count_sum_noalloc(void* cuda_stream, const qeg_column* build_key,
+                                      const qeg_column* probe_key, const qeg_column* probe_val,
+                                      int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,7 @@ def lib():
             "qeg_join_count_sum_result": (i32, [vp, P(ctypes.c_int64), P(ctypes.c_int64), P(i32)]),
             "qeg_join_stats": (i32, [vp, P(i32), P(i32), P(u64)]),
             "qeg_join_destroy": (None, [vp]),
+            "qeg_join_count_sum_noalloc": (i32, [vp, vp, vp, vp, vp]),
             "qeg_sketch": (i32, [vp, vp, u64, vp, P(ctypes.c_double), P(ctypes.c_double)]),
             "qeg_estimator_init": (i32, [vp, u64]),
             "qeg_estimator_set_weights": (i32, [vp, vp]),
@@ -403,6 +404,17 @@ class Join:
             self.close()
         except Exception:
             pass
+
+
+def join_count_sum_noalloc(stream, build_key, probe_key, probe_val, out):
+    """The join COUNT/SUM sink without device allocation (see include/qeg.h).
+    All columns and `out` (4 int64 on the device) must be device tensors; the
+    work is enqueued on `stream` (a cudaStream_t handle) without a sync."""
+    b, k, v = build_key.c(), probe_key.c(), probe_val.c()
+    st = lib().qeg_join_count_sum_noalloc(stream, ctypes.byref(b), ctypes.byref(k), ctypes.byref(v), _ptr(out))
+    if st != 0:
+        msg = lib().qeg_last_error(None)
+        raise QegError(st, msg.decode() if msg else "")
 
 
 # ---- sketch and learned estimator -------------------------------------------
