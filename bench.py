@@ -70,7 +70,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append([time.time()] + [x.strip() for x in line.split(",")])
 
     def __exit__(self, *a):
         if self.proc:
@@ -80,15 +80,28 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
 
-    def summary(self):
-        if not self.rows:
+    def summary(self, t0=None, t1=None):
+        """Median SM clock and active throttle reasons of the samples taken
+        while [t0, t1] ran (the timed region, widened by one sampling period);
+        a timed region shorter than the period falls back to every sample of
+        the run, and says so."""
+        time.sleep(0.3)
+        rows = [r for r in self.rows if len(r) >= 10]
+        window = "timed region"
+        if t0 is not None:
+            sel = [r for r in rows if t0 - 0.25 <= r[0] <= t1 + 0.25]
+            if sel:
+                rows = sel
+            else:
+                window = "warm-up and timed region (timed region shorter than the 200 ms sampling period)"
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        sm = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 6 + i and r[6 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows), "window": window}
 
 
 def pack_bits_torch(valid):
@@ -333,6 +346,7 @@ def main():
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     step_ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
+    clk = ClockSampler(local).__enter__()
     for _ in range(max(args.warmup, 0)):
         res, st = W.run(qeg, ctx, strat)
     torch.cuda.synchronize()
@@ -348,17 +362,19 @@ def main():
     barrier()
     torch.cuda.synchronize()
     launches0 = ctx.launches
-    with ClockSampler(local) as clk:
-        step_ev[0].record(stream)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            pe = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), stream]
-            res, st = W.run(qeg, ctx, strat, events=pe)
-            probe_ms.append(pe)
-        step_ev[1].record(stream)
-        torch.cuda.synchronize()
-        ctx.synchronize()
-        wall = time.perf_counter() - t0
+    tw0 = time.time()
+    step_ev[0].record(stream)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pe = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), stream]
+        res, st = W.run(qeg, ctx, strat, events=pe)
+        probe_ms.append(pe)
+    step_ev[1].record(stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = clk.summary(tw0, time.time())
+    clk.__exit__(None, None, None)
     barrier()
     launches = ctx.launches - launches0
     total_ms = step_ev[0].elapsed_time(step_ev[1])
@@ -434,7 +450,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(launches),
-            "clocks": clk.summary(),
+            "clocks": clocks,
             "wall_s": wall,
         }
         if alt:

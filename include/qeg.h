@@ -134,7 +134,8 @@ typedef struct qeg_agg qeg_agg;
 typedef struct qeg_join qeg_join;
 
 /* ---- context --------------------------------------------------------------*/
-/* Creates a context on CUDA device `device` with its own stream. */
+/* Creates a context on CUDA device `device` with its own stream. Destroy every
+ * qeg_agg / qeg_join created from a context before destroying the context. */
 qeg_status qeg_ctx_create(int device, qeg_ctx** out);
 void qeg_ctx_destroy(qeg_ctx* ctx);
 /* Message of the last failing call on this context (thread-local when ctx is
@@ -271,6 +272,40 @@ qeg_status qeg_estimator_grad(qeg_ctx* ctx, const float* x, const float* targets
 qeg_status qeg_estimator_train(qeg_ctx* ctx, const float* x, const float* targets, uint32_t n,
                                uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
                                float* final_loss);
+
+/* ---- batched GROUP BY: many independent queries in one persistent kernel --
+ * Each query q is `SELECT key, <aggs> FROM rows [row_offsets[q],
+ * row_offsets[q+1]) GROUP BY key` over one integer key column and one value
+ * column stored back to back -- per query, the result of one qe::Aggregate
+ * (ops/aggregate.h:102-144) over that slice; the reference runs such queries
+ * one plan at a time. Aggregates read column 1 (the value) or are COUNT(*).
+ * With NULLs in either column every query starts on a 64-row boundary.
+ * qeg_batch_create plans every query (sketch + estimator -> table size and
+ * strategy through `tuning`, the autotuner's table: the first entry with
+ * log2(estimated groups) <= max_log2_groups and a matching skew class wins;
+ * none -> built-in defaults), allocates one table arena and captures the run
+ * into a CUDA graph. The column buffers must stay valid and unchanged while
+ * the batch lives. qeg_batch_run replays the graph (asynchronous);
+ * qeg_batch_finish waits for it, recomputes exactly any query whose table
+ * overflowed and returns the group count of every query (nqueries values);
+ * qeg_batch_fetch copies one query's result columns (key, then aggregates).
+ * qeg_batch_stats reports the plan of one query. */
+typedef struct qeg_batch qeg_batch;
+typedef struct qeg_batch_tuning {
+  double max_log2_groups; /* bucket upper bound on log2(estimated groups) */
+  int32_t skewed;         /* 1: bucket of queries whose top keys carry >= 30% of rows */
+  int32_t smem_slots;     /* CTA-private table slots (power of two <= 4096); 0 = global table only */
+  uint64_t rows_per_item; /* rows per work item of the persistent kernel */
+} qeg_batch_tuning;
+qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row_offsets, const qeg_column* key,
+                            const qeg_column* val, const qeg_agg_spec* aggs, int naggs,
+                            const qeg_batch_tuning* tuning, int ntuning, int block_threads, qeg_batch** out);
+qeg_status qeg_batch_run(qeg_batch* batch);
+qeg_status qeg_batch_finish(qeg_batch* batch, uint64_t* groups);
+qeg_status qeg_batch_fetch(qeg_batch* batch, uint32_t query, const qeg_out_column* outs);
+qeg_status qeg_batch_stats(const qeg_batch* batch, uint32_t query, double* est_groups, float* hot_share,
+                           int32_t* strategy, uint32_t* fell_back);
+void qeg_batch_destroy(qeg_batch* batch);
 
 /* ---- join COUNT/SUM sink without device allocation ------------------------
  * No counterpart in the reference (whose CPU operators allocate freely).

@@ -201,7 +201,118 @@ __device__ __forceinline__ void merge_fields(uint64_t* dst, const uint64_t* src,
 }
 
 // ---------------------------------------------------------------------------
+// Warp peer aggregation. Lanes of a warp whose rows fall in the same group
+// ("peers", found with __match_any_sync) combine their contributions in
+// registers before the group's lowest lane applies them with one atomic per
+// field, so a heavy hitter costs one shared/global atomic per warp instead of
+// one per row. The combine is a pairwise tree over the peers in lane order
+// (at most 5 rounds); its shuffle schedule depends only on the peer masks, so
+// it is computed once per row batch and replayed for every field.
+// ---------------------------------------------------------------------------
+struct PeerPlan {
+  uint32_t src;   // 5 bits per round: the lane to read from
+  uint32_t take;  // bit r: combine what round r read
+  int rounds;     // warp-uniform
+};
+
+__device__ __forceinline__ PeerPlan plan_peers(unsigned peers, unsigned lane) {
+  PeerPlan pp{0u, 0u, 0};
+  unsigned alive = peers;
+  unsigned rank = __popc(peers & ((1u << lane) - 1u));
+  const unsigned higher = lane == 31 ? 0u : (~0u << (lane + 1));
+#pragma unroll
+  for (int r = 0; r < 5; ++r) {
+    const unsigned above = alive & higher;
+    if (!__any_sync(0xffffffffu, above != 0)) break;
+    const unsigned nxt = above ? static_cast<unsigned>(__ffs(above) - 1) : lane;
+    pp.src |= nxt << (5 * r);
+    if (above && !(rank & 1u)) pp.take |= 1u << r;
+    // Odd ranks were just read by their even neighbour and leave the tree.
+    alive &= ~__ballot_sync(0xffffffffu, rank & 1u);
+    rank >>= 1;
+    pp.rounds = r + 1;
+  }
+  return pp;
+}
+
+// The contribution of one (valid, value bits) input to a field, in the
+// field's identity-is-zero encoding.
+__device__ __forceinline__ uint64_t field_contrib(uint8_t kind, bool valid, uint64_t bits) {
+  switch (kind) {
+    case F_ROWS: return 1;
+    case F_NULLS: return valid ? 0 : 1;
+    case F_SUMI:
+    case F_SUMF: return valid ? bits : 0;
+    case F_MINI: return valid ? ~enc_i64(static_cast<int64_t>(bits)) : 0;
+    case F_MAXI: return valid ? enc_i64(static_cast<int64_t>(bits)) : 0;
+    case F_MINF: return valid ? ~enc_f64_bits(bits) : 0;
+    case F_MAXF: return valid ? enc_f64_bits(bits) : 0;
+    default: return 0;
+  }
+}
+
+__device__ __forceinline__ uint64_t field_combine(uint8_t kind, uint64_t a, uint64_t b) {
+  switch (kind) {
+    case F_ROWS:
+    case F_NULLS:
+    case F_SUMI: return a + b;
+    case F_SUMF:
+      return static_cast<uint64_t>(__double_as_longlong(__longlong_as_double(static_cast<long long>(a)) +
+                                                        __longlong_as_double(static_cast<long long>(b))));
+    default: return a > b ? a : b;
+  }
+}
+
+// Merges one combined contribution into a table word (shared or global).
+__device__ __forceinline__ void field_apply(uint64_t* w, uint8_t kind, uint64_t x) {
+  unsigned long long* u = reinterpret_cast<unsigned long long*>(w);
+  switch (kind) {
+    case F_ROWS:
+    case F_NULLS:
+    case F_SUMI:
+      if (x) atomicAdd(u, static_cast<unsigned long long>(x));
+      break;
+    case F_SUMF:
+      if (x) atomicAdd(reinterpret_cast<double*>(w), __longlong_as_double(static_cast<long long>(x)));
+      break;
+    default:
+      if (x) atomicMax(u, static_cast<unsigned long long>(x));
+      break;
+  }
+}
+
+__device__ __forceinline__ uint64_t peer_reduce(uint64_t x, uint8_t kind, const PeerPlan& pp) {
+  for (int r = 0; r < pp.rounds; ++r) {
+    const uint64_t t = __shfl_sync(0xffffffffu, x, (pp.src >> (5 * r)) & 31u);
+    if ((pp.take >> r) & 1u) x = field_combine(kind, x, t);
+  }
+  return x;
+}
+
+// Combines the rows of every peer group and lets each group's leader apply the
+// result to `f` (its field block; ignored on other lanes).
+__device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, unsigned peers, const PeerPlan& pp,
+                                           const AggK& P, const bool (&vv)[kMaxVals],
+                                           const uint64_t (&vb)[kMaxVals]) {
+  if (leader) atomicAdd(reinterpret_cast<unsigned long long*>(f), static_cast<unsigned long long>(__popc(peers)));
+#pragma unroll
+  for (int c = 0; c < kMaxVals; ++c) {
+    if (c < P.nvals) {
+      const int first = P.cfirst[c];
+      const int n = P.cnf[c];
+      for (int k = 0; k < n; ++k) {
+        const uint8_t kind = P.fkind[first + k];
+        const uint64_t x = peer_reduce(field_contrib(kind, vv[c], vb[c]), kind, pp);
+        if (leader) field_apply(f + first + k, kind, x);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // The aggregation kernel. MODE 0: global (no key), 1: single key, 2: multi key.
+// Warps walk the rows 32 at a time (blockDim.x is a multiple of 32), so every
+// lane reaches the warp-wide intrinsics.
 // ---------------------------------------------------------------------------
 template <int MODE>
 __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
@@ -210,6 +321,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   const int S = (MODE == 0) ? 1 : P.smem_slots;  // power of two, or 0 = off
   const int srows = (MODE == 0) ? 1 : (S > 0 ? S + 2 : 0);
   const int fo = (MODE == 2) ? 2 + P.nkeys : 1;  // field offset within a global row
+  const unsigned lane = threadIdx.x & 31u;
 
   for (int i = threadIdx.x; i < srows * W; i += blockDim.x) sm[i] = 0;
   __syncthreads();
@@ -230,67 +342,94 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
 
   unsigned long long inserted = 0;
   const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < P.nrows; i += step) {
+  for (uint64_t base = static_cast<uint64_t>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < P.nrows;
+       base += step) {
+    const uint64_t i = base + lane;
+    bool live = i < P.nrows;
     uint64_t p = i;
-    if (P.sel) {
+    if (live && P.sel) {
       p = P.sel[i];
       if (p >= P.len) {
         atomicOr(P.err, kDevBadInput);
-        continue;
+        live = false;
       }
     }
     bool vv[kMaxVals];
     uint64_t vb[kMaxVals];
-    load_values(P, p, vv, vb);
+#pragma unroll
+    for (int c = 0; c < kMaxVals; ++c) {
+      vv[c] = false;
+      vb[c] = 0;
+    }
+    if (live) load_values(P, p, vv, vb);
+    const unsigned livemask = __ballot_sync(0xffffffffu, live);
 
     if (MODE == 0) {
-      apply_row<true>(&sm[1], P, vv, vb);
+      const unsigned peers = live ? livemask : (1u << lane);
+      const PeerPlan pp = plan_peers(peers, lane);
+      warp_apply(&sm[1], live && __ffs(peers) - 1 == static_cast<int>(lane), peers, pp, P, vv, vb);
       continue;
     }
     if (MODE == 1) {
       const DevCol& kc = P.key[0];
-      const bool kv = col_valid(kc, p);
+      const bool kv = live && col_valid(kc, p);
       const uint64_t k = kv ? key_word(kc, p) : 0;
-      const uint64_t h = key_hash1(k);
-      int srow = -1;
-      if (S > 0) {
-        if (!kv) {
-          srow = S + 1;
-        } else if (k == 0) {
-          srow = S;
-        } else {
-          uint64_t s = h & (S - 1);
-          for (int t = 0; t < P.smem_probe; ++t) {
-            const uint64_t cur = ld_volatile_shared(&sm[s * W]);
-            if (cur == k) {
-              srow = static_cast<int>(s);
-              break;
-            }
-            if (cur == 0) {
-              if (!P.smem_insert) break;
-              const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * W]), 0ull,
-                                                       static_cast<unsigned long long>(k));
-              if (old == 0 || old == k) {
+      // Peers: live lanes with the same key word and the same validity.
+      const unsigned same = __match_any_sync(0xffffffffu, k);
+      const unsigned vmask = __ballot_sync(0xffffffffu, kv);
+      unsigned peers = live ? (same & livemask & (kv ? vmask : ~vmask)) : (1u << lane);
+      const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
+      // The leader finds (or places) the group's row.
+      uint64_t* f = nullptr;
+      if (leader) {
+        const uint64_t h = key_hash1(k);
+        int srow = -1;
+        if (S > 0) {
+          if (!kv) {
+            srow = S + 1;
+          } else if (k == 0) {
+            srow = S;
+          } else {
+            uint64_t s = h & (S - 1);
+            for (int t = 0; t < P.smem_probe; ++t) {
+              const uint64_t cur = ld_volatile_shared(&sm[s * W]);
+              if (cur == k) {
                 srow = static_cast<int>(s);
                 break;
               }
+              if (cur == 0) {
+                if (!P.smem_insert) break;
+                const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * W]), 0ull,
+                                                         static_cast<unsigned long long>(k));
+                if (old == 0 || old == k) {
+                  srow = static_cast<int>(s);
+                  break;
+                }
+              }
+              s = (s + 1) & (S - 1);
             }
-            s = (s + 1) & (S - 1);
           }
         }
+        if (srow >= 0) {
+          f = &sm[srow * W + 1];
+        } else {
+          uint64_t* r = global_row1(P, kv, k, h, inserted);
+          if (r) f = r + 1;
+        }
       }
-      if (srow >= 0) {
-        apply_row<true>(&sm[srow * W + 1], P, vv, vb);
-      } else {
-        uint64_t* r = global_row1(P, kv, k, h, inserted);
-        if (r)
-          apply_row<false>(r + 1, P, vv, vb);
-        else
-          spill_row(P, p);
+      // A group whose row could not be placed spills each of its rows.
+      const unsigned placed = __ballot_sync(0xffffffffu, f != nullptr);
+      const bool ok = live && ((placed >> (__ffs(peers) - 1)) & 1u);
+      if (live && !ok) {
+        spill_row(P, p);
+        peers = 1u << lane;
       }
+      const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
+      warp_apply(f, leader && ok, peers, pp, P, vv, vb);
       continue;
     }
-    // MODE 2: composite key, global table only.
+    // MODE 2: composite key, global table only, one lane per row.
+    if (!live) continue;
     uint64_t words[kMaxKeys];
     uint64_t nullmask = 0, h = kHashSeed;
 #pragma unroll
@@ -745,6 +884,10 @@ void AggState::consume(const qeg_column* cols, int ncols, const uint32_t* sel, u
   const uint32_t* dsel = nullptr;
   stage_sel(ctx, sel, sel_len, selbuf, &dsel);
   if (!table.get()) first_consume(staged, nrows, len, dsel);
+  if (nrows > spill_cap) {  // a later, larger batch: the spill list must hold all of it
+    spill_cap = nrows;
+    spill_rows.alloc(spill_cap * 4, ctx->stream);
+  }
   rows_seen += nrows;
   if (nrows == 0) return;
 
@@ -801,6 +944,10 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
     est_groups = static_cast<double>(cfg.expected_groups);
   } else if (cfg.sizing == QEG_SIZE_FIXED) {
     want = cfg.initial_capacity ? cfg.initial_capacity : (1ull << 20);
+  } else if (nrows < kSketchMinRows) {
+    // Too few rows for the sketch to pay for its round trip: the row count
+    // bounds the group count, capped at the fixed default.
+    want = std::min<uint64_t>(static_cast<uint64_t>(static_cast<double>(nrows) / kTargetLoad) + 64, 1ull << 20);
   } else {
     est_groups = estimate_groups(staged, nrows, len, dsel);
     // 15% head-room over the estimate keeps the probe short if it is low; an
@@ -810,10 +957,10 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   alloc_table(want);
   counters.alloc(64, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(counters.get(), 0, 64, ctx->stream));
-  spill_cap = std::max<uint64_t>(1u << 20, std::min<uint64_t>(nrows, 64ull << 20));
+  // The spill list holds every row of a batch and the partial-row list every
+  // private-table slot of every resident CTA, so neither can overflow.
+  spill_cap = std::max<uint64_t>(1u << 16, nrows);
   spill_rows.alloc(spill_cap * 4, ctx->stream);
-  part_cap = 1u << 20;
-  spill_parts.alloc(part_cap * row_words * 8, ctx->stream);
 
   // Strategy.
   strategy = cfg.strategy;
@@ -847,6 +994,8 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   } else {
     smem_slots = 0;
   }
+  part_cap = static_cast<uint64_t>(ctx->sms) * 32 * (smem_slots + 2) + 64;
+  spill_parts.alloc(part_cap * row_words * 8, ctx->stream);
 }
 
 void AggState::finish(uint64_t* nrows_out) {
@@ -927,6 +1076,9 @@ qeg_status qeg_agg_create(qeg_ctx* ctx, const int32_t* col_types, int ncols, con
     auto a = std::make_unique<qeg_agg>();
     a->st.ctx = ctx;
     if (cfg) a->st.cfg = *cfg;
+    const int bt = a->st.cfg.block_threads;
+    qeg::require(bt == 0 || (bt >= 32 && bt <= 1024 && bt % 32 == 0),
+                 "block_threads must be 0 or a multiple of 32 in [32, 1024]");
     a->st.plan(col_types, ncols, key_cols, nkeys, aggs, naggs);
     *out = a.release();
   });

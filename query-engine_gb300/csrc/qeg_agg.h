@@ -23,6 +23,8 @@ constexpr int kMaxFields = 24;
 constexpr int kMaxAggs = 32;
 // Target occupancy of a global GROUP BY table sized from a group-count estimate.
 constexpr double kTargetLoad = 0.6;
+// Batches smaller than this are sized from their row count, not sketched.
+constexpr uint64_t kSketchMinRows = 1ull << 22;
 
 // Parameter block of the aggregation kernels (passed by value).
 struct AggK {

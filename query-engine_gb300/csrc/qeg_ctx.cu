@@ -164,7 +164,10 @@ qeg_status qeg_ctx_create(int device, qeg_ctx** out) {
 void qeg_ctx_destroy(qeg_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
+  // Every buffer owned by the context is freed on its stream: release them
+  // all while the stream still exists, then destroy it.
   ctx->dev_err.release();
+  ctx->mlp.reset();
   cudaStreamSynchronize(ctx->stream);
   cudaStreamDestroy(ctx->stream);
   delete ctx;

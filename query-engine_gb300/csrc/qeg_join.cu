@@ -397,6 +397,198 @@ __global__ void __launch_bounds__(256) probe_sink_kernel(const SinkK P) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// TMA-staged sink: the probe columns stream into shared memory through a ring
+// of kStages tiles filled by cp.async.bulk (completion on an mbarrier, L2
+// evict-first so the stream does not push the table out of L2); all threads
+// then do the lookups from shared memory while the next tiles are in flight.
+// Thread 0 waits on each tile's mbarrier with a bounded spin and shares the
+// outcome through shared memory, so a wait that runs out turns the whole block
+// to the drain path together.
+// ---------------------------------------------------------------------------
+constexpr int kTmaThreads = 512;
+constexpr int kTileRows = 4096;
+constexpr int kStages = 3;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+      : "memory");
+}
+// Bounded wait for phase `parity` of `bar`; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+template <typename KT, typename VT>
+struct TmaTile {
+  KT key[kTileRows];
+  VT val[kTileRows];
+  uint64_t kvalid[kTileRows / 64];
+  uint64_t vvalid[kTileRows / 64];
+};
+
+template <typename KT, typename VT, int STRAT, bool UNIQUE>
+__global__ void __launch_bounds__(kTmaThreads) probe_sink_tma_kernel(const SinkK P, uint32_t* err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  using Tile = TmaTile<KT, VT>;
+  Tile* tiles = reinterpret_cast<Tile*>(smem_raw);
+  __shared__ __align__(8) uint64_t full[kStages];
+  __shared__ int s_ok;
+  const KT* keys = static_cast<const KT*>(P.key);
+  const VT* vals = static_cast<const VT*>(P.val);
+  const uint64_t ntiles = P.n / kTileRows;  // full tiles; the rest is handled below
+  const uint32_t tx = kTileRows * (sizeof(KT) + sizeof(VT)) + (P.kvalid ? kTileRows / 8 : 0) +
+                      (P.vvalid ? kTileRows / 8 : 0);
+  uint64_t pol = 0;
+  auto issue = [&](uint64_t ti, int s) {
+    const uint64_t r0 = ti * kTileRows;
+    mbar_arrive_expect_tx(&full[s], tx);
+    bulk_g2s(tiles[s].key, keys + r0, kTileRows * sizeof(KT), &full[s], pol);
+    bulk_g2s(tiles[s].val, vals + r0, kTileRows * sizeof(VT), &full[s], pol);
+    if (P.kvalid) bulk_g2s(tiles[s].kvalid, P.kvalid + r0 / 64, kTileRows / 8, &full[s], pol);
+    if (P.vvalid) bulk_g2s(tiles[s].vvalid, P.vvalid + r0 / 64, kTileRows / 8, &full[s], pol);
+  };
+  if (threadIdx.x == 0) {
+    pol = evict_first_policy();
+    for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int s = 0; s < kStages; ++s) {
+      const uint64_t ti = blockIdx.x + static_cast<uint64_t>(s) * gridDim.x;
+      if (ti < ntiles) issue(ti, s);
+    }
+  }
+  __syncthreads();
+
+  unsigned long long cnt = 0, sum = 0, seen = 0;
+  uint64_t it = 0;
+  bool ok = true;
+  for (uint64_t ti = blockIdx.x; ti < ntiles; ti += gridDim.x, ++it) {
+    const int s = static_cast<int>(it % kStages);
+    const uint32_t parity = static_cast<uint32_t>((it / kStages) & 1);
+    if (threadIdx.x == 0) s_ok = mbar_wait_bounded(&full[s], parity) ? 1 : 0;
+    __syncthreads();
+    if (!s_ok) {
+      ok = false;
+      break;
+    }
+    const Tile& T = tiles[s];
+    constexpr int kPer = kTileRows / kTmaThreads;
+    uint64_t m[kPer];
+    if (STRAT == QEG_JOIN_DENSE) {
+      // Two phases so every lookup of the tile is in flight at once.
+      uint64_t w[kPer];
+      uint32_t b[kPer];
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) {
+        const int r = j * kTmaThreads + threadIdx.x;
+        const bool kv = !P.kvalid || ((T.kvalid[r >> 6] >> (r & 63)) & 1ull);
+        const uint64_t sl = static_cast<uint64_t>(static_cast<int64_t>(T.key[r])) - static_cast<uint64_t>(P.T.dmin);
+        const bool in = kv && sl < P.T.cap;
+        b[j] = static_cast<uint32_t>(sl & 63);
+        w[j] = in ? (UNIQUE ? __ldg(P.T.bitmap + (sl >> 6)) : __ldg(P.T.cnt + sl)) : 0;
+      }
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) m[j] = UNIQUE ? ((w[j] >> b[j]) & 1ull) : w[j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < kPer; ++j) {
+        const int r = j * kTmaThreads + threadIdx.x;
+        const bool kv = !P.kvalid || ((T.kvalid[r >> 6] >> (r & 63)) & 1ull);
+        m[j] = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, T.key[r]) : 0;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int r = j * kTmaThreads + threadIdx.x;
+      if (m[j]) {
+        cnt += m[j];
+        if (!P.vvalid || ((T.vvalid[r >> 6] >> (r & 63)) & 1ull)) {
+          sum += static_cast<unsigned long long>(static_cast<int64_t>(T.val[r])) * m[j];
+          seen = 1;
+        }
+      }
+    }
+    __syncthreads();  // stage s is free again
+    if (threadIdx.x == 0) {
+      const uint64_t nt = ti + static_cast<uint64_t>(kStages) * gridDim.x;
+      if (nt < ntiles) issue(nt, s);
+    }
+  }
+  if (!ok) {
+    // A wait ran out: report it, then let the copies this block still has in
+    // flight land (bounded) before the block's shared memory is released.
+    if (threadIdx.x == 0) {
+      atomicOr(err, kDevSpinTimeout);
+      for (uint64_t k = it; k < it + kStages; ++k) {
+        const uint64_t tk = blockIdx.x + k * gridDim.x;
+        if (tk >= ntiles) break;
+        mbar_wait_bounded(&full[k % kStages], static_cast<uint32_t>((k / kStages) & 1));
+      }
+    }
+    __syncthreads();
+    return;
+  }
+  // Rows after the last full tile.
+  const uint64_t rest0 = ntiles * kTileRows;
+  for (uint64_t r = rest0 + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n;
+       r += (uint64_t)gridDim.x * blockDim.x) {
+    const bool kv = !P.kvalid || ((P.kvalid[r >> 6] >> (r & 63)) & 1ull);
+    const uint64_t m = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, keys[r]) : 0;
+    cnt += m;
+    if (m && (!P.vvalid || ((P.vvalid[r >> 6] >> (r & 63)) & 1ull))) {
+      sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r])) * m;
+      seen = 1;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    seen |= __shfl_down_sync(0xffffffffu, seen, o);
+  }
+  __shared__ unsigned long long s_acc[3];
+  if (threadIdx.x == 0) s_acc[0] = s_acc[1] = s_acc[2] = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_acc[0], cnt);
+    atomicAdd(&s_acc[1], sum);
+    atomicOr(&s_acc[2], seen);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_acc[0]) atomicAdd(P.acc + 0, s_acc[0]);
+    if (s_acc[1]) atomicAdd(P.acc + 1, s_acc[1]);
+    if (s_acc[2]) atomicOr(P.acc + 2, s_acc[2]);
+  }
+}
+
 // The COUNT(*) / SUM(payload) sink for any key/payload type or alignment.
 template <int STRAT, bool UNIQUE>
 __global__ void __launch_bounds__(512) probe_count_sum_kernel(const ProbeK P) {
@@ -1011,12 +1203,28 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
             std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
         kern<<<grid, 256, 0, ctx->stream>>>(S);
       };
-#define QEG_SINK(KT, VT)                                                                 \
-  do {                                                                                   \
-    if (dense && st.unique) launch(probe_sink_kernel<KT, VT, QEG_JOIN_DENSE, true>);    \
-    else if (dense) launch(probe_sink_kernel<KT, VT, QEG_JOIN_DENSE, false>);           \
-    else if (st.unique) launch(probe_sink_kernel<KT, VT, QEG_JOIN_HASH, true>);         \
-    else launch(probe_sink_kernel<KT, VT, QEG_JOIN_HASH, false>);                       \
+      // Large probe sides stream through the TMA-staged kernel (one block of
+      // kTmaThreads per SM, a kStages ring of shared-memory tiles).
+      auto al16 = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };
+      const bool use_tma = n >= static_cast<uint64_t>(kTileRows) * ctx->sms * 2 && al16(S.kvalid) && al16(S.vvalid) &&
+                           getenv("QEG_NO_TMA") == nullptr;
+      auto launch_tma = [&](void (*kern)(SinkK, uint32_t*), size_t tile_bytes) {
+        const size_t sb = tile_bytes * kStages;
+        QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb)));
+        kern<<<ctx->sms, kTmaThreads, sb, ctx->stream>>>(S, static_cast<uint32_t*>(ctx->dev_err.get()));
+      };
+#define QEG_SINK(KT, VT)                                                                                           \
+  do {                                                                                                             \
+    const size_t tb = sizeof(TmaTile<KT, VT>);                                                                     \
+    if (use_tma) {                                                                                                 \
+      if (dense && st.unique) launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_DENSE, true>, tb);                \
+      else if (dense) launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_DENSE, false>, tb);                       \
+      else if (st.unique) launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_HASH, true>, tb);                     \
+      else launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_HASH, false>, tb);                                   \
+    } else if (dense && st.unique) launch(probe_sink_kernel<KT, VT, QEG_JOIN_DENSE, true>);                       \
+    else if (dense) launch(probe_sink_kernel<KT, VT, QEG_JOIN_DENSE, false>);                                    \
+    else if (st.unique) launch(probe_sink_kernel<KT, VT, QEG_JOIN_HASH, true>);                                  \
+    else launch(probe_sink_kernel<KT, VT, QEG_JOIN_HASH, false>);                                                \
   } while (0)
       if (k8 && v8) QEG_SINK(long long, long long);
       else if (k8) QEG_SINK(long long, int);

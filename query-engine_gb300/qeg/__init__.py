@@ -95,6 +95,7 @@ def lib():
             "qeg_join_stats": (i32, [vp, P(i32), P(i32), P(u64)]),
             "qeg_join_destroy": (None, [vp]),
             "qeg_join_count_sum_noalloc": (i32, [vp, vp, vp, vp, vp]),
+            "qeg_filter_join_agg": (i32, [vp, vp, c, vp, c, vp, u64, vp, P(u64)]),
             "qeg_sketch": (i32, [vp, vp, u64, vp, P(ctypes.c_double), P(ctypes.c_double)]),
             "qeg_estimator_init": (i32, [vp, u64]),
             "qeg_estimator_set_weights": (i32, [vp, vp]),
@@ -103,6 +104,13 @@ def lib():
             "qeg_estimator_grad": (i32, [vp, vp, vp, ctypes.c_uint32, P(ctypes.c_float), vp]),
             "qeg_estimator_train": (i32, [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                           ctypes.c_float, u64, P(ctypes.c_float)]),
+            "qeg_batch_create": (i32, [vp, ctypes.c_uint32, vp, vp, vp, vp, c, vp, c, c, P(vp)]),
+            "qeg_batch_run": (i32, [vp]),
+            "qeg_batch_finish": (i32, [vp, vp]),
+            "qeg_batch_fetch": (i32, [vp, ctypes.c_uint32, vp]),
+            "qeg_batch_stats": (i32, [vp, ctypes.c_uint32, P(ctypes.c_double), P(ctypes.c_float), P(i32),
+                                      P(ctypes.c_uint32)]),
+            "qeg_batch_destroy": (None, [vp]),
         }
         for name, (res, args) in list(sig.items()) + list(optional.items()):
             if not hasattr(L, name):
@@ -283,6 +291,9 @@ class Aggregate:
             w = torch.empty(max(1, (count + 63) // 64), dtype=torch.int64, device="cuda")
             keep.append((v, w))
             outs[i] = OutColumn(v.data_ptr(), w.data_ptr(), None)
+        # The library writes on its own stream: the new tensors' memory may
+        # still be in use by torch's stream until it drains.
+        torch.cuda.synchronize()
         _check(lib().qeg_agg_fetch(self.p, first, count, outs), self.ctx.p)
         return [(v[:count], w) for v, w in keep]
 
@@ -417,6 +428,45 @@ def join_count_sum_noalloc(stream, build_key, probe_key, probe_val, out):
         raise QegError(st, msg.decode() if msg else "")
 
 
+# ---- fused filter -> join -> GROUP BY ---------------------------------------
+CMP_LT, CMP_LE, CMP_GT, CMP_GE, CMP_EQ, CMP_NE = 0, 1, 2, 3, 4, 5
+
+
+class PipelineDesc(ctypes.Structure):
+    _fields_ = [("filter_col", ctypes.c_int32), ("filter_op", ctypes.c_int32), ("filter_value", ctypes.c_double),
+                ("probe_key", ctypes.c_uint32), ("build_key", ctypes.c_uint32), ("group_col", ctypes.c_uint32),
+                ("naggs", ctypes.c_int32), ("aggs", AggSpec * 16)]
+
+
+def filter_join_agg(ctx, probe, build, probe_key, build_key, group_col, aggs, filter_col=-1, filter_op=CMP_GT,
+                    filter_value=0.0, capacity=None):
+    """scan(probe).filter(...).join(scan(build)).aggregate({group_col}, aggs)
+    in one fused pass; returns [(values, valid)] group column then aggregates."""
+    d = PipelineDesc()
+    d.filter_col, d.filter_op, d.filter_value = filter_col, filter_op, filter_value
+    d.probe_key, d.build_key, d.group_col, d.naggs = probe_key, build_key, group_col, len(aggs)
+    for i, (f, c) in enumerate(aggs):
+        d.aggs[i] = AggSpec(f, c)
+    gtype = build[group_col - len(probe)].type
+    types = [gtype]
+    for f, c in aggs:
+        t = probe[c].type if f not in (COUNT_STAR, COUNT) else I64
+        types.append(I64 if f in (COUNT_STAR, COUNT) else F64 if f == AVG else
+                     (F64 if t == F64 else I64) if f == SUM else t)
+    cap = capacity or (build[0].n + 1)
+    outs = (OutColumn * len(types))()
+    keep = []
+    for i, t in enumerate(types):
+        v = np.zeros(max(cap, 1), dtype=NP_DTYPE[t])
+        w = np.zeros(max(1, (cap + 63) // 64), dtype=np.uint64)
+        keep.append((v, w))
+        outs[i] = OutColumn(v.ctypes.data, w.ctypes.data, None)
+    n = ctypes.c_uint64()
+    _check(lib().qeg_filter_join_agg(ctx.p, _cols(probe), len(probe), _cols(build), len(build), ctypes.byref(d),
+                                     cap, outs, ctypes.byref(n)), ctx.p)
+    return types, [(v[:n.value], unpack_validity(w, n.value)) for v, w in keep]
+
+
 # ---- sketch and learned estimator -------------------------------------------
 SKETCH_FEATURES = 80
 MLP_PARAMS = 9474
@@ -473,3 +523,77 @@ def estimator_train(ctx, x, t, epochs, batch, lr, seed):
     _check(lib().qeg_estimator_train(ctx.p, x.ctypes.data, t.ctypes.data, x.shape[0], epochs, batch, lr, seed,
                                      ctypes.byref(loss)), ctx.p)
     return loss.value
+
+
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("max_log2_groups", ctypes.c_double), ("skewed", ctypes.c_int32), ("smem_slots", ctypes.c_int32),
+                ("rows_per_item", ctypes.c_uint64)]
+
+
+class Batch:
+    """Many GROUP BY queries over slices of one (key, value) column pair, run
+    by one persistent kernel from a captured CUDA graph (qeg_batch_*).
+    `row_offsets` has nqueries + 1 ascending entries; `tuning` is a list of
+    (max_log2_groups, skewed, smem_slots, rows_per_item) buckets."""
+
+    def __init__(self, ctx, row_offsets, key, val, aggs, tuning=(), block_threads=0):
+        self.ctx = ctx
+        offs = np.ascontiguousarray(np.asarray(row_offsets, dtype=np.uint64))
+        self.nq = len(offs) - 1
+        specs = (AggSpec * max(1, len(aggs)))()
+        for i, (f, c) in enumerate(aggs):
+            specs[i] = AggSpec(f, c)
+        tun = (BatchTuning * max(1, len(tuning)))()
+        for i, t in enumerate(tuning):
+            tun[i] = BatchTuning(*t)
+        self._keep = (key, val)  # the batch reads these buffers on every run
+        kc, vc = key.c(), val.c()
+        p = ctypes.c_void_p()
+        _check(lib().qeg_batch_create(ctx.p, self.nq, offs.ctypes.data, ctypes.byref(kc), ctypes.byref(vc), specs,
+                                      len(aggs), tun, len(tuning), block_threads, ctypes.byref(p)), ctx.p)
+        self.p = p
+        a = Aggregate(ctx, [key.type, val.type], [0], aggs)
+        self.result_types = a.result_types
+        a.close()
+        self.aggs = list(aggs)
+        self.groups = None
+
+    def run(self):
+        _check(lib().qeg_batch_run(self.p), self.ctx.p)
+
+    def finish(self):
+        g = np.zeros(self.nq, dtype=np.uint64)
+        _check(lib().qeg_batch_finish(self.p, g.ctypes.data), self.ctx.p)
+        self.groups = g
+        return g
+
+    def fetch(self, query):
+        """Result of one query: [(values, valid)] for the key then the aggregates."""
+        count = int(self.groups[query])
+        outs = (OutColumn * len(self.result_types))()
+        keep = []
+        for i, t in enumerate(self.result_types):
+            v = np.zeros(max(count, 1), dtype=NP_DTYPE[t])
+            w = np.zeros(max(1, (count + 63) // 64), dtype=np.uint64)
+            av = np.zeros(1, dtype=np.int32)
+            keep.append((v, w, av))
+            outs[i] = OutColumn(v.ctypes.data, w.ctypes.data, av.ctypes.data)
+        _check(lib().qeg_batch_fetch(self.p, query, outs), self.ctx.p)
+        return [(v[:count], unpack_validity(w, count)) for v, w, _ in keep]
+
+    def stats(self, query):
+        est, hot, st, fb = ctypes.c_double(), ctypes.c_float(), ctypes.c_int32(), ctypes.c_uint32()
+        _check(lib().qeg_batch_stats(self.p, query, ctypes.byref(est), ctypes.byref(hot), ctypes.byref(st),
+                                     ctypes.byref(fb)), self.ctx.p)
+        return {"est_groups": est.value, "hot_share": hot.value, "strategy": st.value, "fell_back": fb.value}
+
+    def close(self):
+        if self.p:
+            lib().qeg_batch_destroy(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

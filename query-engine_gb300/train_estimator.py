@@ -32,11 +32,25 @@ import qeg  # noqa: E402
 HOT_K = 2048
 
 
+def scramble(x, salt):
+    """A bijective 64-bit mix of an int64 tensor (splitmix64 finaliser written
+    with logical shifts), so ranks map to spread-out keys without indexing."""
+    m30, m27, m31 = (1 << 34) - 1, (1 << 37) - 1, (1 << 33) - 1
+    x = x ^ salt
+    x = x ^ ((x >> 30) & m30)
+    x = x * -4658895280553007687  # 0xbf58476d1ce4e5b9 as int64
+    x = x ^ ((x >> 27) & m27)
+    x = x * -7723592293110705685  # 0x94d049bb133111eb as int64
+    return x ^ ((x >> 31) & m31)
+
+
 def gen_keys(rng, g, dev):
-    """One seeded key column: (keys int64 tensor, description)."""
+    """One seeded key column: (keys int64 tensor, description). Only
+    elementwise torch ops: no gathers."""
     n = int(2 ** rng.uniform(14, 27.5))
     fam = rng.choice(["uniform", "zipf", "sequential", "mixture"], p=[0.3, 0.4, 0.1, 0.2])
     dom = int(2 ** rng.uniform(2, 28))
+    salt = int(rng.integers(0, 1 << 62))
     if fam == "uniform":
         k = torch.randint(0, dom, (n,), generator=g, device=dev, dtype=torch.int64)
         desc = {"family": fam, "domain": dom}
@@ -45,14 +59,13 @@ def gen_keys(rng, g, dev):
         dom = min(dom, 1 << 26)
         cdf = torch.arange(1, dom + 1, dtype=torch.float64, device=dev).pow_(-s).cumsum_(0)
         cdf /= cdf[-1].clone()
-        r = torch.searchsorted(cdf, torch.rand(n, generator=g, device=dev, dtype=torch.float64)).clamp_(max=dom - 1)
-        perm = torch.randint(0, 1 << 62, (dom,), generator=g, device=dev, dtype=torch.int64)
-        k = perm[r]
+        r = torch.searchsorted(cdf, torch.rand(n, generator=g, device=dev, dtype=torch.float64)).clamp_(0, dom - 1)
+        del cdf
+        k = scramble(r, salt)
         desc = {"family": fam, "domain": dom, "s": s}
     elif fam == "sequential":
         rep = int(2 ** rng.uniform(0, 8))
-        k = torch.arange(n, device=dev, dtype=torch.int64) // rep
-        k = k[torch.randperm(n, generator=g, device=dev)]
+        k = scramble(torch.arange(n, device=dev, dtype=torch.int64) // rep, salt)
         desc = {"family": fam, "repeat": rep}
     else:
         head = int(2 ** rng.uniform(0, 12))
@@ -73,7 +86,11 @@ def exact_stats(ctx, keys):
     n = a.finish()
     counts = a.fetch_torch()[1][0]
     a.close()
-    share = float(torch.topk(counts, min(HOT_K, n)).values.sum().item()) / max(1, keys.numel())
+    torch.cuda.synchronize()
+    if counts.numel() != n or n < 1:
+        raise RuntimeError("group count mismatch: %d vs %d" % (counts.numel(), n))
+    top = torch.sort(counts, descending=True).values[: min(HOT_K, n)]
+    share = float(top.sum().item()) / max(1, keys.numel())
     return n, share
 
 
@@ -87,8 +104,12 @@ def build_set(ctx, rng, count, dev, seed):
     X, T, C, D = [], [], [], []
     for i in range(count):
         keys, desc = gen_keys(rng, g, dev)
+        torch.cuda.synchronize()
         f, classic, _ = qeg.sketch(ctx, qeg.Col(keys, None, qeg.I64))
+        ctx.synchronize()
         groups, share = exact_stats(ctx, keys)
+        ctx.synchronize()
+        print("dataset %d %s groups=%d share=%.3f" % (i, desc, groups, share), flush=True)
         X.append(f)
         T.append(targets(groups, share))
         C.append(classic)

@@ -80,8 +80,9 @@ def zipf_column(torch, n, dom, s, seed):
     cdf = torch.arange(1, dom + 1, dtype=torch.float64, device="cuda").pow_(-s).cumsum_(0)
     cdf /= cdf[-1].clone()
     r = torch.searchsorted(cdf, torch.rand(n, generator=g, device="cuda", dtype=torch.float64)).clamp_(max=dom - 1)
-    perm = torch.randint(0, 1 << 62, (dom,), generator=g, device="cuda", dtype=torch.int64)
-    return perm[r].contiguous()
+    keys = (r * -7046029254386353131) ^ 0x5DEECE66D  # an odd multiplier: a bijection on int64
+    torch.cuda.synchronize()  # the library reads these on its own stream
+    return keys.contiguous()
 
 
 @pytest.mark.gpu

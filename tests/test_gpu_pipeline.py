@@ -1,0 +1,92 @@
+"""The fused filter -> inner join -> GROUP BY (qeg_filter_join_agg) against the
+oracle's operators applied one after another, on data in the shape of the
+dictionary-string pipeline workload: trades (sym STR codes, Zipf-skewed; price
+F64 lognormal; qty I32) filtered on price > 100, joined by VALUE with a symbol
+table under a different dictionary (sym STR, sector I32 over 32 values), grouped
+by sector with COUNT(*), AVG(price), SUM(qty) (+ MIN/MAX/COUNT variants)."""
+import numpy as np
+import pytest
+
+import oracle as O
+import qeg
+from util import StrCanon, assert_same, gpu_rows, to_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def make_case(seed, n=300_000, nsym=1000, nulls=True, dup_syms=False):
+    rng = np.random.default_rng(seed)
+    syms = ["S%04d" % i for i in range(nsym)]
+    tdict = list(rng.permutation(syms))                   # trades dictionary order
+    bdict = list(rng.permutation(syms + ["ZZZ%d" % i for i in range(20)]))  # symbols dictionary
+    ranks = np.minimum(rng.zipf(1.3, n) - 1, nsym - 1)
+    codes = np.array([tdict.index(syms[r]) for r in range(nsym)], np.int32)[ranks]
+    price = np.exp(rng.normal(4.6, 0.3, n))
+    qty = rng.integers(1, 10001, n).astype(np.int32)
+    pv = (rng.random(n) > 0.01) if nulls else None
+    kv = (rng.random(n) > 0.01) if nulls else None
+    trades = [O.TCol(O.STR, codes, kv, tdict), O.TCol(O.F64, price, pv), O.TCol(O.I32, qty)]
+    brow = np.arange(len(bdict), dtype=np.int32)
+    if dup_syms:
+        brow = np.concatenate([brow, brow[:50]])
+    sector = rng.integers(0, 32, len(brow)).astype(np.int32)
+    svalid = (rng.random(len(brow)) > 0.05) if nulls else None
+    symbols = [O.TCol(O.STR, brow, None, bdict), O.TCol(O.I32, sector, svalid)]
+    return trades, symbols
+
+
+def oracle_pipeline(trades, symbols, aggs):
+    ok = trades[1].values > 100
+    if trades[1].valid is not None:
+        ok &= trades[1].valid
+    filt = [O.TCol(c.type, c.values[ok], None if c.valid is None else c.valid[ok], c.dictionary) for c in trades]
+    jt, jrows = O.join(filt, symbols, [0], [0], O.INNER)
+    # Joined schema: sym, price, qty, sym, sector -> group by sector (col 4).
+    cols = []
+    for i, t in enumerate(jt):
+        vals = [r[i] for r in jrows]
+        valid = np.array([v is not None for v in vals], bool)
+        if t == O.STR:
+            d = sorted({v for v in vals if v is not None}) or ["?"]
+            arr = np.array([d.index(v) if v is not None else 0 for v in vals], np.int32)
+            cols.append(O.TCol(t, arr, valid, d))
+        else:
+            dt = {O.I32: np.int32, O.I64: np.int64, O.F64: np.float64}[t]
+            arr = np.array([v if v is not None else 0 for v in vals], dt)
+            cols.append(O.TCol(t, arr, valid))
+    return O.groupby(cols, [4], aggs)
+
+
+@pytest.mark.parametrize("seed,nulls,dup", [(1, True, False), (2, False, False), (3, True, True)])
+def test_pipeline_matches_operator_chain(ctx, seed, nulls, dup):
+    trades, symbols = make_case(seed, nulls=nulls, dup_syms=dup)
+    aggs = [(O.COUNT_STAR, 0), (O.AVG, 1), (O.SUM, 2), (O.MIN, 1), (O.MAX, 2), (O.COUNT, 1)]
+    ot, orows = oracle_pipeline(trades, symbols, aggs)
+    canon = StrCanon(trades[0].dictionary + symbols[0].dictionary)
+    gp = [to_gpu(c, canon) for c in trades]
+    gb = [to_gpu(c, canon) for c in symbols]
+    types, res = qeg.filter_join_agg(ctx, gp, gb, 0, 0, 4, aggs, filter_col=1, filter_op=qeg.CMP_GT,
+                                     filter_value=100.0)
+    gt, grows = gpu_rows(res, types, canon)
+    assert_same(gt, grows, ot, orows)
+
+
+def test_pipeline_integer_keys_and_filter_on_int(ctx):
+    rng = np.random.default_rng(9)
+    n = 200_000
+    key = rng.integers(0, 5000, n).astype(np.int64)
+    qty = rng.integers(1, 100, n).astype(np.int32)
+    probe = [O.TCol(O.I64, key), O.TCol(O.I32, qty)]
+    bkey = rng.permutation(4000).astype(np.int64) + 500
+    build = [O.TCol(O.I64, bkey), O.TCol(O.I64, (bkey % 7).astype(np.int64))]
+    aggs = [(O.COUNT_STAR, 0), (O.SUM, 1)]
+    # qty >= 50.5 on an integer column behaves as qty > 50.
+    ok = qty > 50
+    filt = [O.TCol(c.type, c.values[ok]) for c in probe]
+    jt, jrows = O.join(filt, build, [0], [0], O.INNER)
+    cols = [O.TCol(t, np.array([r[i] for r in jrows], {O.I32: np.int32, O.I64: np.int64}[t])) for i, t in enumerate(jt)]
+    ot, orows = O.groupby(cols, [3], aggs)
+    types, res = qeg.filter_join_agg(ctx, [to_gpu(c) for c in probe], [to_gpu(c) for c in build], 0, 0, 3, aggs,
+                                     filter_col=1, filter_op=qeg.CMP_GE, filter_value=50.5)
+    gt, grows = gpu_rows(res, types)
+    assert_same(gt, grows, ot, orows)

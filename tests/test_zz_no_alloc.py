@@ -33,8 +33,11 @@ def _case(torch, seed, nbuild, nprobe, dup):
     def words(mask):
         return torch.from_numpy(qeg.pack_validity(mask.cpu().numpy()).view(np.int64)).cuda()
 
-    return (qeg.Col(bkey, words(bvalid), qeg.I64), qeg.Col(pkey.contiguous(), words(pvalid), qeg.I64),
+    cols = (qeg.Col(bkey, words(bvalid), qeg.I64), qeg.Col(pkey.contiguous(), words(pvalid), qeg.I64),
             qeg.Col(pval, None, qeg.I64))
+    # The allocating entry point runs on the library's own stream.
+    torch.cuda.synchronize()
+    return cols
 
 
 def _expected(ctx, bk, pk, pv):

@@ -100,6 +100,7 @@ def to_gpu(col, canon=None, device=False):
         vals = torch.from_numpy(np.ascontiguousarray(vals)).cuda()
         w = None if w is None else torch.from_numpy(w.view(np.int64)).cuda()
         cm = None if cm is None else torch.from_numpy(cm).cuda()
+        torch.cuda.synchronize()  # the library reads them on its own stream
     return qeg.Col(vals, w, col.type, cm)
 
 
