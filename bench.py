@@ -214,8 +214,8 @@ class AggWorkload:
         g.manual_seed(seed)
         self.kind = kind
         if kind == "skew":
-            self.name = "skew_agg_512M_zipf1.1_over_64M"
             self.n = nrows or (512 << 20)
+            self.name = "skew_agg_%dM_zipf1.1_over_64M" % (self.n >> 20)
             self.key = zipf_keys(self.n, 64 << 20, 1.1, g, dev)
             self.v1 = torch.randint(-(1 << 31), 1 << 31, (self.n,), generator=g, device=dev, dtype=torch.int64)
             self.v2 = torch.randn(self.n, generator=g, device=dev, dtype=torch.float64).mul_(1e3)
@@ -247,7 +247,7 @@ class AggWorkload:
 def run_agg_bench(args, dev, local):
     import qeg
 
-    W = AggWorkload(dev, args.workload)
+    W = AggWorkload(dev, args.workload, nrows=args.agg_rows)
     ctx = qeg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
     variants = {
@@ -255,6 +255,8 @@ def run_agg_bench(args, dev, local):
         "plain_fixed": qeg.agg_config(sizing=qeg.SIZE_FIXED, initial_capacity=1 << 20),
         "exact_size": qeg.agg_config(expected_groups=W.groups, hot_keys=-1),
     }
+    if args.variants:
+        variants = {k: v for k, v in variants.items() if k in args.variants.split(",")}
     out = {}
     for name, cfg in variants.items():
         for _ in range(args.warmup):
@@ -273,7 +275,7 @@ def run_agg_bench(args, dev, local):
                      "gb_per_s": W.n * W.row_bytes / (ms / 1e3) / 1e9,
                      "launches_per_step": (ctx.launches - launches0) / args.steps}
     peak, kind = peaks()
-    best = out["learned"]
+    best = out["learned"] if "learned" in out else next(iter(out.values()))
     print(json.dumps({
         "metric": "rows/s hash aggregate (%s)" % W.name, "value": best["rows_per_s"], "unit": "rows/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["ms_per_step"],
@@ -282,7 +284,148 @@ def run_agg_bench(args, dev, local):
         "roofline": {"bound": "hbm", "achieved": best["gb_per_s"], "peak": peak, "peak_kind": kind,
                      "unit": "GB/s", "frac": best["gb_per_s"] / peak},
         "variants": out,
-        "learned_vs_plain": out["plain_fixed"]["ms_per_step"] / best["ms_per_step"],
+        "learned_vs_plain": (out["plain_fixed"]["ms_per_step"] / best["ms_per_step"]
+                             if "plain_fixed" in out else None),
+    }))
+
+
+# ---------------------------------------------------------------------------
+# Workload: 4096 independent GROUP BY queries in one batch
+# ---------------------------------------------------------------------------
+class BatchWorkload:
+    """`batch` = 4096 GROUP BY queries over back-to-back slices: per-query row
+    counts log-uniform in [1e3, 1e7]; int32 keys with a distinct-value domain
+    log-uniform in [4, 1e6], half uniform and half Zipf(s), s uniform in
+    [0.5, 1.5]; F64 values uniform [0, 1); COUNT(*), SUM, AVG, MIN, MAX grouped
+    by key. Ranks are spread over int32 by an odd-multiplier bijection."""
+
+    name = "batch_4096q_loguniform_1e3_1e7"
+
+    def __init__(self, dev, nq=4096, lo=1e3, hi=1e7, seed=SEED + 4):
+        import qeg
+
+        rng = np.random.default_rng(seed)
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), nq)).astype(np.int64)
+        doms = np.exp(rng.uniform(np.log(4), np.log(1e6), nq)).astype(np.int64)
+        zipf = rng.random(nq) < 0.5
+        ss = rng.uniform(0.5, 1.5, nq)
+        self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+        self.n = int(self.offsets[-1])
+        self.key = torch.empty(self.n, dtype=torch.int32, device=dev)
+        self.val = torch.rand(self.n, generator=g, device=dev, dtype=torch.float64)
+        for q in range(nq):
+            a, b, d = int(self.offsets[q]), int(self.offsets[q + 1]), int(doms[q])
+            if zipf[q]:
+                cdf = torch.arange(1, d + 1, dtype=torch.float64, device=dev).pow_(-float(ss[q])).cumsum_(0)
+                cdf /= cdf[-1].clone()
+                r = torch.searchsorted(cdf, torch.rand(b - a, generator=g, device=dev, dtype=torch.float64))
+                r.clamp_(max=d - 1)
+            else:
+                r = torch.randint(0, d, (b - a,), generator=g, device=dev, dtype=torch.int64)
+            x = (r * 2654435761 + 12345 * q) & 0xFFFFFFFF
+            self.key[a:b] = torch.where(x >= (1 << 31), x - (1 << 32), x).to(torch.int32)
+        torch.cuda.synchronize()
+        self.meta = {"sizes": sizes, "domains": doms, "zipf": zipf, "s": ss}
+        self.aggs = [(qeg.COUNT_STAR, 0), (qeg.SUM, 1), (qeg.AVG, 1), (qeg.MIN, 1), (qeg.MAX, 1)]
+        self.row_bytes = 12
+
+    def cols(self):
+        import qeg
+
+        return qeg.Col(self.key, None, qeg.I32), qeg.Col(self.val, None, qeg.F64)
+
+
+def load_tuning():
+    path = os.path.join(REPO, "query-engine_gb300", "batch_tuning.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return [tuple(t) for t in d["tuning"]], int(d.get("block_threads", 0)), path
+    except Exception:
+        return [], 0, None
+
+
+def run_batch_bench(args, dev, local):
+    import qeg
+
+    W = BatchWorkload(dev)
+    ctx = qeg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    tuning, block, tpath = load_tuning()
+    k, v = W.cols()
+    t0 = time.perf_counter()
+    b = qeg.Batch(ctx, W.offsets, k, v, W.aggs, tuning=tuning, block_threads=block)
+    ctx.synchronize()
+    plan_s = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 0)):
+        b.run()
+        groups = b.finish()
+    clk = ClockSampler(local).__enter__()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = ctx.launches
+    tw0 = time.time()
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.run()
+        groups = b.finish()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.summary(tw0, time.time())
+    clk.__exit__(None, None, None)
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = (ctx.launches - launches0) / args.steps
+    fell = sum(b.stats(q)["fell_back"] for q in range(len(groups)))
+    # Exact group counts (torch.unique per query) for the estimate report.
+    true = np.array([int(torch.unique(W.key[int(W.offsets[q]):int(W.offsets[q + 1])]).numel())
+                     for q in range(len(groups))])
+    assert np.array_equal(true, groups.astype(np.int64)), "batch group counts differ from torch.unique"
+    est = np.array([b.stats(q)["est_groups"] for q in range(len(groups))])
+    lerr = np.abs(np.log2(np.maximum(est, 1)) - np.log2(np.maximum(true, 1)))
+    b.close()
+    rows_s = W.n / (ms / 1e3)
+    gbs = W.n * W.row_bytes / (ms / 1e3) / 1e9
+
+    # The plain GPU path: the same queries one at a time through the ordinary
+    # GROUP BY with fixed initial sizing (grow on overflow).
+    plain = None
+    if not args.no_plain:
+        nq = len(groups)
+        cfg = qeg.agg_config(sizing=qeg.SIZE_FIXED)
+        offs = W.offsets
+
+        def plain_step():
+            for q in range(nq):
+                a, z = int(offs[q]), int(offs[q + 1])
+                ag = qeg.Aggregate(ctx, [qeg.I32, qeg.F64], [0], W.aggs, cfg)
+                ag.consume([qeg.Col(W.key[a:z], None, qeg.I32), qeg.Col(W.val[a:z], None, qeg.F64)])
+                ag.finish()
+                ag.close()
+
+        plain_step()
+        torch.cuda.synchronize()
+        p0 = time.perf_counter()
+        plain_step()
+        ctx.synchronize()
+        pms = (time.perf_counter() - p0) * 1e3
+        plain = {"ms_per_step": pms, "rows_per_s": W.n / (pms / 1e3)}
+    peak, kind = peaks()
+    print(json.dumps({
+        "metric": "rows/s batched hash aggregate (%s)" % W.name, "value": rows_s, "unit": "rows/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
+        "data": "synthetic (seeded, generated on the GPU); inputs %.1f GB > L2" % (W.n * W.row_bytes / 1e9),
+        "config": {"workload": W.name, "queries": len(groups), "rows": W.n, "tuning": tpath,
+                   "block_threads": block or 512},
+        "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                     "peak_kind": kind, "note": "graph replay (aggregate + finalize) time"},
+        "gpu_launches": launches, "clocks": clocks, "plan_s": plan_s,
+        "estimate_log2_error": {"median": float(np.median(lerr)), "p90": float(np.percentile(lerr, 90))},
+        "fell_back_queries": int(fell),
+        "plain_sequential": plain,
+        "batched_vs_plain": (plain["ms_per_step"] / ms) if plain else None,
     }))
 
 
@@ -311,6 +454,9 @@ def main():
     ap.add_argument("--strategy", default="auto", choices=["auto", "hash", "dense"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--agg-rows", type=int, default=None)
+    ap.add_argument("--variants", default=None)
     ap.add_argument("--cpu-probe-rows", type=int, default=1 << 25)
     ap.add_argument("--build-rows", type=int, default=1 << 24)
     ap.add_argument("--probe-rows", type=int, default=1 << 28)
@@ -337,6 +483,9 @@ def main():
 
     if args.workload in ("skew", "agg1m"):
         run_agg_bench(args, dev, local)
+        return
+    if args.workload == "batch":
+        run_batch_bench(args, dev, local)
         return
 
     strat = {"auto": qeg.JOIN_AUTO, "hash": qeg.JOIN_HASH, "dense": qeg.JOIN_DENSE}[args.strategy]

@@ -253,8 +253,9 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
  *   count-min / heavy-hitter features; also the classic (uniform-model)
  *   distinct estimate and the sampled share of rows in the top 2048 keys.
  * The estimator is an MLP 80 -> 64 -> 64 -> 2 (ReLU, BF16 weights, FP32
- * accumulation) whose outputs are log2(1 + groups) / 32 and the share of rows
- * carried by the 2048 most frequent keys. Weights are QEG_MLP_PARAMS float32
+ * accumulation) with two outputs: a correction to the classic estimate,
+ * log2(1 + groups) = log2(1 + classic non-null groups) + 32 * out0, and the
+ * share of rows carried by the 2048 most frequent keys. Weights are QEG_MLP_PARAMS float32
  * (W1[64][80] b1 W2[64][64] b2 W3[2][64] b3); a context loads
  * $QEG_ESTIMATOR_WEIGHTS or estimator_weights.f32 beside libqeg.so if present.
  * qeg_estimator_grad returns the mean-squared-error loss over the batch and

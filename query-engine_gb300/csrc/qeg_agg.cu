@@ -23,6 +23,7 @@
 #include <cmath>
 
 #include "qeg_agg.h"
+#include "qeg_warpagg.cuh"
 
 namespace qeg {
 
@@ -33,6 +34,15 @@ __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t* p) {
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Probe length for new keys once the global table is nearly full.
+constexpr int kFullProbe = 16;
 
 __device__ __forceinline__ uint64_t ld_volatile_shared(const uint64_t* p) {
   return *reinterpret_cast<const volatile uint64_t*>(p);
@@ -111,12 +121,12 @@ __device__ __forceinline__ uint64_t key_hash1(uint64_t k) { return hash_fold(kHa
 // Single-key global lookup/insert. Returns the row, or nullptr when the key
 // could not be placed within the probe limit.
 __device__ __forceinline__ uint64_t* global_row1(const AggK& P, bool kv, uint64_t k, uint64_t h,
-                                                 unsigned long long& inserted) {
+                                                 unsigned long long& inserted, int limit) {
   const int W = P.row_words;
   if (!kv) return P.table + (P.cap + 1) * W;
   if (k == 0) return P.table + P.cap * W;
   uint64_t s = __umul64hi(h, P.cap);
-  for (int t = 0; t < P.probe_limit; ++t) {
+  for (int t = 0; t < limit; ++t) {
     uint64_t* r = P.table + s * W;
     const uint64_t cur = ld_relaxed(r);
     if (cur == k) return r;
@@ -200,101 +210,17 @@ __device__ __forceinline__ void merge_fields(uint64_t* dst, const uint64_t* src,
   }
 }
 
-// ---------------------------------------------------------------------------
-// Warp peer aggregation. Lanes of a warp whose rows fall in the same group
-// ("peers", found with __match_any_sync) combine their contributions in
-// registers before the group's lowest lane applies them with one atomic per
-// field, so a heavy hitter costs one shared/global atomic per warp instead of
-// one per row. The combine is a pairwise tree over the peers in lane order
-// (at most 5 rounds); its shuffle schedule depends only on the peer masks, so
-// it is computed once per row batch and replayed for every field.
-// ---------------------------------------------------------------------------
-struct PeerPlan {
-  uint32_t src;   // 5 bits per round: the lane to read from
-  uint32_t take;  // bit r: combine what round r read
-  int rounds;     // warp-uniform
-};
-
-__device__ __forceinline__ PeerPlan plan_peers(unsigned peers, unsigned lane) {
-  PeerPlan pp{0u, 0u, 0};
-  unsigned alive = peers;
-  unsigned rank = __popc(peers & ((1u << lane) - 1u));
-  const unsigned higher = lane == 31 ? 0u : (~0u << (lane + 1));
-#pragma unroll
-  for (int r = 0; r < 5; ++r) {
-    const unsigned above = alive & higher;
-    if (!__any_sync(0xffffffffu, above != 0)) break;
-    const unsigned nxt = above ? static_cast<unsigned>(__ffs(above) - 1) : lane;
-    pp.src |= nxt << (5 * r);
-    if (above && !(rank & 1u)) pp.take |= 1u << r;
-    // Odd ranks were just read by their even neighbour and leave the tree.
-    alive &= ~__ballot_sync(0xffffffffu, rank & 1u);
-    rank >>= 1;
-    pp.rounds = r + 1;
-  }
-  return pp;
-}
-
-// The contribution of one (valid, value bits) input to a field, in the
-// field's identity-is-zero encoding.
-__device__ __forceinline__ uint64_t field_contrib(uint8_t kind, bool valid, uint64_t bits) {
-  switch (kind) {
-    case F_ROWS: return 1;
-    case F_NULLS: return valid ? 0 : 1;
-    case F_SUMI:
-    case F_SUMF: return valid ? bits : 0;
-    case F_MINI: return valid ? ~enc_i64(static_cast<int64_t>(bits)) : 0;
-    case F_MAXI: return valid ? enc_i64(static_cast<int64_t>(bits)) : 0;
-    case F_MINF: return valid ? ~enc_f64_bits(bits) : 0;
-    case F_MAXF: return valid ? enc_f64_bits(bits) : 0;
-    default: return 0;
-  }
-}
-
-__device__ __forceinline__ uint64_t field_combine(uint8_t kind, uint64_t a, uint64_t b) {
-  switch (kind) {
-    case F_ROWS:
-    case F_NULLS:
-    case F_SUMI: return a + b;
-    case F_SUMF:
-      return static_cast<uint64_t>(__double_as_longlong(__longlong_as_double(static_cast<long long>(a)) +
-                                                        __longlong_as_double(static_cast<long long>(b))));
-    default: return a > b ? a : b;
-  }
-}
-
-// Merges one combined contribution into a table word (shared or global).
-__device__ __forceinline__ void field_apply(uint64_t* w, uint8_t kind, uint64_t x) {
-  unsigned long long* u = reinterpret_cast<unsigned long long*>(w);
-  switch (kind) {
-    case F_ROWS:
-    case F_NULLS:
-    case F_SUMI:
-      if (x) atomicAdd(u, static_cast<unsigned long long>(x));
-      break;
-    case F_SUMF:
-      if (x) atomicAdd(reinterpret_cast<double*>(w), __longlong_as_double(static_cast<long long>(x)));
-      break;
-    default:
-      if (x) atomicMax(u, static_cast<unsigned long long>(x));
-      break;
-  }
-}
-
-__device__ __forceinline__ uint64_t peer_reduce(uint64_t x, uint8_t kind, const PeerPlan& pp) {
-  for (int r = 0; r < pp.rounds; ++r) {
-    const uint64_t t = __shfl_sync(0xffffffffu, x, (pp.src >> (5 * r)) & 31u);
-    if ((pp.take >> r) & 1u) x = field_combine(kind, x, t);
-  }
-  return x;
-}
-
 // Combines the rows of every peer group and lets each group's leader apply the
 // result to `f` (its field block; ignored on other lanes).
-__device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, unsigned peers, const PeerPlan& pp,
+// `priv`: `f` is a warp-private row, updated without atomics (one leader per
+// group and one group per row within a warp).
+__device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, bool priv, unsigned peers, const PeerPlan& pp,
                                            const AggK& P, const bool (&vv)[kMaxVals],
                                            const uint64_t (&vb)[kMaxVals]) {
-  if (leader) atomicAdd(reinterpret_cast<unsigned long long*>(f), static_cast<unsigned long long>(__popc(peers)));
+  if (leader) {
+    if (priv) f[0] += __popc(peers);
+    else atomicAdd(reinterpret_cast<unsigned long long*>(f), static_cast<unsigned long long>(__popc(peers)));
+  }
 #pragma unroll
   for (int c = 0; c < kMaxVals; ++c) {
     if (c < P.nvals) {
@@ -303,7 +229,10 @@ __device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, unsigned pe
       for (int k = 0; k < n; ++k) {
         const uint8_t kind = P.fkind[first + k];
         const uint64_t x = peer_reduce(field_contrib(kind, vv[c], vb[c]), kind, pp);
-        if (leader) field_apply(f + first + k, kind, x);
+        if (leader) {
+          if (priv) f[first + k] = field_combine(kind, f[first + k], x);
+          else field_apply(f + first + k, kind, x);
+        }
       }
     }
   }
@@ -322,8 +251,20 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   const int srows = (MODE == 0) ? 1 : (S > 0 ? S + 2 : 0);
   const int fo = (MODE == 2) ? 2 + P.nkeys : 1;  // field offset within a global row
   const unsigned lane = threadIdx.x & 31u;
+  const int warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  // Warp-private rows after the table: MODE 0 one per warp; MODE 1 (preloaded
+  // table) one per warp for each of the WH hottest keys, with a rank byte per
+  // table slot (0 = not one of them) and the table slot of every rank.
+  const int WH = (MODE == 0) ? 1 : ((MODE == 1 && S > 0 && P.nhot > 0) ? P.warp_hot : 0);
+  uint64_t* wrows = sm + srows * W;
+  uint8_t* srank = reinterpret_cast<uint8_t*>(wrows + nwarps * WH * W);
+  uint16_t* hslot = reinterpret_cast<uint16_t*>(srank + ((srows + 7) & ~7));
+  const bool ranked = MODE == 1 && WH > 0;
 
-  for (int i = threadIdx.x; i < srows * W; i += blockDim.x) sm[i] = 0;
+  for (int i = threadIdx.x; i < (srows + nwarps * WH) * W; i += blockDim.x) sm[i] = 0;
+  if (ranked)
+    for (int i = threadIdx.x; i < srows; i += blockDim.x) srank[i] = 0;
   __syncthreads();
   if (MODE == 1 && S > 0 && P.nhot > 0) {
     for (int i = threadIdx.x; i < P.nhot; i += blockDim.x) {
@@ -333,7 +274,13 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       for (int t = 0; t < S; ++t) {
         const unsigned long long old =
             atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * W]), 0ull, static_cast<unsigned long long>(k));
-        if (old == 0 || old == k) break;
+        if (old == 0 || old == k) {
+          if (old == 0 && i < WH) {
+            srank[s] = static_cast<uint8_t>(i + 1);
+            hslot[i] = static_cast<uint16_t>(s);
+          }
+          break;
+        }
         s = (s + 1) & (S - 1);
       }
     }
@@ -341,9 +288,15 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   }
 
   unsigned long long inserted = 0;
+  // Table-full signal: inserts are counted per warp and published every 64;
+  // once the count passes P.full_at, lookups of new keys give up after a short
+  // probe and spill, instead of walking probe_limit slots of a full table.
+  unsigned pending = 0;
+  bool full = MODE == 1 && P.full_flag && ld_relaxed_u32(P.full_flag) != 0;
+  uint32_t iter = 0;
   const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
   for (uint64_t base = static_cast<uint64_t>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < P.nrows;
-       base += step) {
+       base += step, ++iter) {
     const uint64_t i = base + lane;
     bool live = i < P.nrows;
     uint64_t p = i;
@@ -367,7 +320,8 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
     if (MODE == 0) {
       const unsigned peers = live ? livemask : (1u << lane);
       const PeerPlan pp = plan_peers(peers, lane);
-      warp_apply(&sm[1], live && __ffs(peers) - 1 == static_cast<int>(lane), peers, pp, P, vv, vb);
+      warp_apply(&wrows[warp * W + 1], live && __ffs(peers) - 1 == static_cast<int>(lane), true, peers, pp, P, vv,
+                 vb);
       continue;
     }
     if (MODE == 1) {
@@ -381,6 +335,8 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
       // The leader finds (or places) the group's row.
       uint64_t* f = nullptr;
+      bool priv = false;
+      const unsigned long long ins0 = inserted;
       if (leader) {
         const uint64_t h = key_hash1(k);
         int srow = -1;
@@ -411,9 +367,15 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
           }
         }
         if (srow >= 0) {
-          f = &sm[srow * W + 1];
+          const int rk = (ranked && srow < S) ? srank[srow] : 0;
+          if (rk) {
+            f = &wrows[(warp * WH + rk - 1) * W + 1];
+            priv = true;
+          } else {
+            f = &sm[srow * W + 1];
+          }
         } else {
-          uint64_t* r = global_row1(P, kv, k, h, inserted);
+          uint64_t* r = global_row1(P, kv, k, h, inserted, full ? kFullProbe : P.probe_limit);
           if (r) f = r + 1;
         }
       }
@@ -425,7 +387,21 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
         peers = 1u << lane;
       }
       const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
-      warp_apply(f, leader && ok, peers, pp, P, vv, vb);
+      warp_apply(f, leader && ok, priv, peers, pp, P, vv, vb);
+      if (P.full_flag) {
+        pending += __popc(__ballot_sync(0xffffffffu, inserted != ins0));
+        if (pending >= 64 || (iter & 15) == 15) {
+          if (lane == 0) {
+            if (pending) {
+              const unsigned long long before = atomicAdd(P.counters + 3, static_cast<unsigned long long>(pending));
+              if (before + pending >= P.full_at) atomicExch(P.full_flag, 1u);
+            }
+            full = full || ld_relaxed_u32(P.full_flag) != 0;
+          }
+          pending = 0;
+          full = __shfl_sync(0xffffffffu, full, 0);
+        }
+      }
       continue;
     }
     // MODE 2: composite key, global table only, one lane per row.
@@ -448,6 +424,16 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       spill_row(P, p);
   }
 
+  // Fold the warp-private rows into the CTA table.
+  if (WH > 0) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nwarps * WH; i += blockDim.x) {
+      const uint64_t* src = &wrows[i * W];
+      if (src[1] == 0) continue;
+      const int slot = (MODE == 0) ? 0 : hslot[i % WH];
+      merge_fields(&sm[slot * W + 1], src + 1, P);
+    }
+  }
   // Flush the CTA-private table into the global table.
   if (MODE != 2 && srows > 0) {
     __syncthreads();
@@ -463,7 +449,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
         dst = P.table + P.cap * W;
       } else {
         const uint64_t k = src[0];
-        dst = global_row1(P, true, k, key_hash1(k), inserted);
+        dst = global_row1(P, true, k, key_hash1(k), inserted, P.probe_limit);
       }
       if (dst) {
         merge_fields(dst + 1, src + 1, P);
@@ -500,7 +486,7 @@ __global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, ui
       } else {
         const uint64_t k = src[0];
         if (k == 0) continue;
-        dst = global_row1(P, true, k, key_hash1(k), inserted);
+        dst = global_row1(P, true, k, key_hash1(k), inserted, P.probe_limit);
       }
       if (!dst) {
         atomicOr(P.err, kDevSpillOverflow);
@@ -533,7 +519,7 @@ __global__ void merge_parts_kernel(const AggK P, const uint64_t* __restrict__ pa
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t* src = parts + i * W;
     const uint64_t k = src[0];
-    uint64_t* dst = global_row1(P, true, k, key_hash1(k), inserted);
+    uint64_t* dst = global_row1(P, true, k, key_hash1(k), inserted, P.probe_limit);
     if (!dst) {
       atomicOr(P.err, kDevSpillOverflow);
       continue;
@@ -775,14 +761,30 @@ AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel
   P.smem_probe = 8;
   P.hot = hot_keys_dev.get<uint64_t>();
   P.nhot = nhot;
+  P.warp_hot = warp_hot();
   P.probe_limit = probe_limit;
   P.spill_rows = spill_rows.get<uint32_t>();
   P.spill_cap = spill_cap;
   P.spill_parts = spill_parts.get<uint64_t>();
   P.part_cap = part_cap;
   P.counters = counters.get<unsigned long long>();
+  if (mode == 1) {
+    // Raise the table-full signal at 85% occupancy (counting the keys already in).
+    const uint64_t at = static_cast<uint64_t>(0.85 * static_cast<double>(cap));
+    P.full_flag = reinterpret_cast<uint32_t*>(P.counters + 4);
+    P.full_at = at > inserted ? at - inserted : 1;
+  }
   P.err = static_cast<uint32_t*>(ctx->dev_err.get());
   return P;
+}
+
+int AggState::block_threads() const { return cfg.block_threads > 0 ? cfg.block_threads : 512; }
+
+int AggState::warp_hot() const {
+  if (mode != 1 || nhot <= 0 || smem_slots <= 0) return 0;
+  // Up to 32 keys, within 32 KB of warp-private rows.
+  const int fit = 32768 / ((block_threads() / 32) * row_words * 8);
+  return std::max(0, std::min({32, nhot, fit}));
 }
 
 void AggState::alloc_table(uint64_t new_cap) {
@@ -792,14 +794,19 @@ void AggState::alloc_table(uint64_t new_cap) {
   QEG_CUDA(cudaMemsetAsync(table.get(), 0, rows * row_words * 8, ctx->stream));
 }
 
-size_t AggState::smem_bytes() const {
+size_t AggState::smem_bytes(int block) const {
   const int srows = mode == 0 ? 1 : (smem_slots > 0 ? smem_slots + 2 : 0);
-  return static_cast<size_t>(srows) * row_words * 8;
+  const int wh = mode == 0 ? 1 : warp_hot();
+  size_t b = (static_cast<size_t>(srows) + static_cast<size_t>(block / 32) * wh) * row_words * 8;
+  if (mode == 1 && wh > 0) b += ((srows + 7) & ~7) + 2 * wh;  // slot ranks + rank slots
+  return b;
 }
 
 void AggState::launch(const AggK& P, uint64_t nrows) {
-  const size_t sb = smem_bytes();
-  int block = cfg.block_threads > 0 ? cfg.block_threads : 512;
+  const int block = block_threads();
+  const size_t sb = smem_bytes(block);
+  if (mode == 1)  // running insert count and table-full flag
+    QEG_CUDA(cudaMemsetAsync(counters.get<uint8_t>() + 24, 0, 16, ctx->stream));
   int per_sm = 1;
   auto set_attr = [&](auto kern) {
     if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
@@ -809,9 +816,9 @@ void AggState::launch(const AggK& P, uint64_t nrows) {
   else if (mode == 1) set_attr(agg_kernel<1>);
   else set_attr(agg_kernel<2>);
   require(per_sm > 0, "aggregate kernel does not fit on an SM with this configuration");
-  // Enough CTAs to cover the rows, but each CTA should aggregate a sizeable
-  // morsel so the flush of its private table stays small next to its input.
-  const uint64_t min_rows_per_cta = (mode == 2 || smem_slots == 0) ? 4096 : std::max<uint64_t>(16384, 8ull * smem_slots);
+  // Each CTA should aggregate a few thousand rows at least, so clearing and
+  // flushing its private table (which touches occupied rows only) stays small.
+  const uint64_t min_rows_per_cta = 4096;
   uint64_t want = (nrows + min_rows_per_cta - 1) / min_rows_per_cta;
   uint64_t grid = std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * per_sm);
   if (grid == 0) grid = 1;
@@ -966,7 +973,9 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   strategy = cfg.strategy;
   if (mode == 2) strategy = QEG_AGG_GLOBAL;
   if (mode == 0) strategy = QEG_AGG_SMEM;
-  const int max_slots = static_cast<int>(std::min<size_t>(8192, (ctx->smem_optin / (row_words * 8)) - 2));
+  // Leave room for the warp-private rows (<= 32 KB) and the slot ranks.
+  const int max_slots =
+      static_cast<int>(std::min<size_t>(8192, ((ctx->smem_optin - 32768) / (row_words * 8 + 1)) - 2));
   int slots = 1;
   while (slots * 2 <= max_slots) slots *= 2;
   if (strategy == QEG_AGG_AUTO) {
@@ -976,13 +985,15 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   }
   nhot = 0;
   if (strategy == QEG_AGG_SMEM && mode == 1) {
-    smem_slots = cfg.smem_slots > 0 ? static_cast<int>(next_pow2(cfg.smem_slots)) : std::min(slots, 4096);
-    smem_slots = std::min(smem_slots, slots);
-    smem_insert = 1;
     // Many groups but a heavy head: preload the heavy hitters found by the
     // sketch and keep the private table read-only, so its slots hold the keys
-    // that carry the rows instead of whichever keys arrived first.
-    if (cfg.hot_keys != 0 && est_groups > 0.5 * smem_slots && !heavy_candidates.empty()) {
+    // that carry the rows instead of whichever keys arrived first. A smaller
+    // table then keeps two CTAs per SM; first-come tables get 2048 slots.
+    const bool preload = cfg.hot_keys != 0 && est_groups > 1024 && !heavy_candidates.empty();
+    smem_slots = cfg.smem_slots > 0 ? static_cast<int>(next_pow2(cfg.smem_slots)) : (preload ? 1024 : 2048);
+    smem_slots = std::min(smem_slots, slots);
+    smem_insert = 1;
+    if (preload) {
       const int want_hot = cfg.hot_keys > 0 ? cfg.hot_keys : smem_slots / 2;
       nhot = static_cast<int>(std::min<size_t>(heavy_candidates.size(), std::min(want_hot, smem_slots / 2)));
       hot_keys_dev.alloc(std::max(nhot, 1) * 8, ctx->stream);

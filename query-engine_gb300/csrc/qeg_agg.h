@@ -44,12 +44,16 @@ struct AggK {
   int smem_probe;
   const uint64_t* hot;  // heavy hitters preloaded into the private table
   int nhot;
+  int warp_hot;  // the first warp_hot heavy hitters also get warp-private rows
   int probe_limit;
   uint32_t* spill_rows;
   uint64_t spill_cap;
   uint64_t* spill_parts;
   uint64_t part_cap;
-  unsigned long long* counters;  // [0] spilled rows, [1] spilled partials, [2] inserted keys
+  unsigned long long* counters;  // [0] spilled rows, [1] spilled partials, [2] inserted keys,
+                                 // [3] running insert count, [4] table-full flag (u32)
+  uint32_t* full_flag;           // NULL: no table-full signal
+  uint64_t full_at;              // running insert count that raises the flag
   uint32_t* err;
 };
 
@@ -81,12 +85,18 @@ struct SketchResult {
 // Builds the sketch of one key column (qeg_sketch.cu).
 void sketch_key_column(qeg_ctx* ctx, const DevCol& key, const uint32_t* sel, uint64_t nrows, uint64_t len,
                        uint64_t sample_target, int want_heavy, SketchResult& out);
+// Sketches every query [offsets[q], offsets[q+1]) of a batch's key column in
+// one launch (one CTA per query); `d_offsets` is the device copy of `offsets`.
+void batch_sketch(qeg_ctx* ctx, const DevCol& key, const uint64_t* d_offsets, const std::vector<uint64_t>& offsets,
+                  uint64_t sample_target, std::vector<SketchResult>& out);
 // Classic (non-learned) distinct-count extrapolation from a sketch.
 double classic_estimate(const SketchResult& s);
 // Learned estimate (qeg_estimator.cu): predicted distinct groups and the share of
 // rows covered by the top heavy hitters. Returns false when no trained model
 // is loaded in this context.
 bool learned_estimate(qeg_ctx* ctx, const SketchResult& s, double* groups, double* hot_share);
+// Non-null group count from the network's first output for sketch `s`.
+double learned_groups(const SketchResult& s, float out0);
 
 struct AggState {
   qeg_ctx* ctx = nullptr;
@@ -122,7 +132,9 @@ struct AggState {
   AggK kparams(const std::vector<StagedCol>& staged, const uint32_t* sel, uint64_t nrows, uint64_t len) const;
   AggK kparams_base() const;
   void alloc_table(uint64_t new_cap);
-  size_t smem_bytes() const;
+  size_t smem_bytes(int block) const;
+  int warp_hot() const;
+  int block_threads() const;
   void launch(const AggK& P, uint64_t nrows);
   void read_counters(uint64_t out[3]);
   void grow(uint64_t new_cap);

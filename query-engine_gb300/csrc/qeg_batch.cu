@@ -23,6 +23,7 @@
 
 #include "qeg_agg.h"
 #include "qeg_mlp.h"
+#include "qeg_warpagg.cuh"
 
 namespace qeg {
 
@@ -53,23 +54,6 @@ struct BatchK {
   int val_first, val_nf;  // value-column fields (cfirst/cnf of column 0)
   uint32_t* overflow;     // per query
 };
-
-__device__ __forceinline__ void batch_apply(uint64_t* f, const BatchK& P, bool v, uint64_t b) {
-  atomicAdd(reinterpret_cast<unsigned long long*>(f), 1ull);
-  for (int k = 0; k < P.val_nf; ++k) {
-    unsigned long long* w = reinterpret_cast<unsigned long long*>(f + P.val_first + k);
-    switch (P.fkind[P.val_first + k]) {
-      case F_NULLS: if (!v) atomicAdd(w, 1ull); break;
-      case F_SUMI: if (v) atomicAdd(w, static_cast<unsigned long long>(b)); break;
-      case F_SUMF: if (v) atomicAdd(reinterpret_cast<double*>(w), __longlong_as_double(static_cast<long long>(b))); break;
-      case F_MINI: if (v) atomicMax(w, static_cast<unsigned long long>(~enc_i64(static_cast<int64_t>(b)))); break;
-      case F_MAXI: if (v) atomicMax(w, static_cast<unsigned long long>(enc_i64(static_cast<int64_t>(b)))); break;
-      case F_MINF: if (v) atomicMax(w, static_cast<unsigned long long>(~enc_f64_bits(b))); break;
-      case F_MAXF: if (v) atomicMax(w, static_cast<unsigned long long>(enc_f64_bits(b))); break;
-      default: break;
-    }
-  }
-}
 
 __device__ __forceinline__ uint64_t* batch_global_row(const BatchK& P, const BatchQ& Q, bool kv, uint64_t k) {
   uint64_t* T = P.arena + Q.table_off * P.W;
@@ -107,40 +91,62 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
     const uint64_t start = P.item_start[item];
     const uint32_t len = P.item_len[item];
     bool ovf = false;
-    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
+    const unsigned lane = threadIdx.x & 31u;
+    // Warps walk the item 32 rows at a time; lanes of one group combine their
+    // rows first (warp peer aggregation) and the group's leader applies them.
+    for (uint32_t wb = threadIdx.x & ~31u; wb < len; wb += blockDim.x) {
+      const uint32_t i = wb + lane;
+      const bool live = i < len;
       const uint64_t p = start + i;
-      const bool kv = col_valid(P.key, p);
+      const bool kv = live && col_valid(P.key, p);
       const uint64_t k = kv ? key_word(P.key, p) : 0;
-      const bool v = col_valid(P.val, p);
+      const bool v = live && col_valid(P.val, p);
       const uint64_t b = !v ? 0
                          : (P.val.type == kF64 ? static_cast<uint64_t>(__double_as_longlong(f64_value(P.val, p)))
                                                : static_cast<uint64_t>(int_value(P.val, p)));
-      int srow = -1;
-      if (S) {
-        if (!kv) {
-          srow = S + 1;
-        } else if (k == 0) {
-          srow = S;
-        } else {
-          uint64_t s = hash_fold(kHashSeed, k) & (S - 1);
-          for (int t = 0; t < 8; ++t) {
-            unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(&sm[s * P.W]);
-            if (cur == 0)
-              cur = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * P.W]), 0ull, static_cast<unsigned long long>(k));
-            if (cur == 0 || cur == k) {
-              srow = static_cast<int>(s);
-              break;
+      const unsigned livemask = __ballot_sync(0xffffffffu, live);
+      const unsigned same = __match_any_sync(0xffffffffu, k);
+      const unsigned vmask = __ballot_sync(0xffffffffu, kv);
+      const unsigned peers = live ? (same & livemask & (kv ? vmask : ~vmask)) : (1u << lane);
+      const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
+      uint64_t* f = nullptr;
+      if (leader) {
+        int srow = -1;
+        if (S) {
+          if (!kv) {
+            srow = S + 1;
+          } else if (k == 0) {
+            srow = S;
+          } else {
+            uint64_t s = hash_fold(kHashSeed, k) & (S - 1);
+            for (int t = 0; t < 8; ++t) {
+              unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(&sm[s * P.W]);
+              if (cur == 0)
+                cur = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * P.W]), 0ull,
+                                static_cast<unsigned long long>(k));
+              if (cur == 0 || cur == k) {
+                srow = static_cast<int>(s);
+                break;
+              }
+              s = (s + 1) & (S - 1);
             }
-            s = (s + 1) & (S - 1);
           }
         }
+        if (srow >= 0) {
+          f = &sm[srow * P.W + 1];
+        } else {
+          uint64_t* r = batch_global_row(P, Q, kv, k);
+          if (r) f = r + 1;
+          else ovf = true;  // the query is recomputed exactly after the run
+        }
       }
-      if (srow >= 0) {
-        batch_apply(&sm[srow * P.W + 1], P, v, b);
-      } else {
-        uint64_t* r = batch_global_row(P, Q, kv, k);
-        if (r) batch_apply(r + 1, P, v, b);
-        else ovf = true;
+      const PeerPlan pp = plan_peers(peers, lane);
+      const bool apply = leader && f != nullptr;
+      if (apply) atomicAdd(reinterpret_cast<unsigned long long*>(f), static_cast<unsigned long long>(__popc(peers)));
+      for (int j = 0; j < P.val_nf; ++j) {
+        const uint8_t kind = P.fkind[P.val_first + j];
+        const uint64_t x = peer_reduce(field_contrib(kind, v, b), kind, pp);
+        if (apply) field_apply(f + P.val_first + j, kind, x);
       }
     }
     if (ovf) atomicOr(P.overflow + q, 1u);
@@ -284,7 +290,7 @@ struct BatchState {
   StagedCol key, val;
   uint32_t nq = 0, nitems = 0;
   int block = 512;
-  DevBuf dqs, ditem_q, ditem_start, ditem_len, dnext, arena, overflow, counts;
+  DevBuf doffs, dqs, ditem_q, ditem_start, ditem_len, dnext, arena, overflow, counts;
   std::vector<DevBuf> out_vals, out_valid;
   uint64_t arena_rows = 0, out_rows = 0;
   cudaGraph_t graph = nullptr;
@@ -388,18 +394,17 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
     S.qs.resize(nqueries);
     S.est.resize(nqueries);
     S.hot.resize(nqueries);
+    for (uint32_t q = 0; q < nqueries; ++q)
+      require((S.key.dev.all_valid && S.val.dev.all_valid) || S.offsets[q] % 64 == 0,
+              "queries over columns with NULLs must start on 64-row boundaries");
+    S.doffs.alloc((nqueries + 1) * 8, ctx->stream);
+    QEG_CUDA(cudaMemcpyAsync(S.doffs.get(), S.offsets.data(), (nqueries + 1) * 8, cudaMemcpyHostToDevice,
+                             ctx->stream));
+    std::vector<SketchResult> sk;
+    batch_sketch(ctx, S.key.dev, S.doffs.get<uint64_t>(), S.offsets, 1u << 16, sk);
     std::vector<float> feats((size_t)nqueries * kSketchFeatures);
     std::vector<double> classic(nqueries);
-    std::vector<SketchResult> sk(nqueries);
     for (uint32_t q = 0; q < nqueries; ++q) {
-      DevCol kq = S.key.dev;
-      const size_t w = type_width(key->type);
-      kq.data = static_cast<const uint8_t*>(kq.data) + S.offsets[q] * w;
-      require((kq.all_valid && S.val.dev.all_valid) || S.offsets[q] % 64 == 0,
-              "queries over columns with NULLs must start on 64-row boundaries");
-      if (!kq.all_valid) kq.validity += S.offsets[q] / 64;
-      const uint64_t n = S.offsets[q + 1] - S.offsets[q];
-      sketch_key_column(ctx, kq, nullptr, n, n, 1u << 16, 0, sk[q]);
       std::copy(sk[q].features, sk[q].features + kSketchFeatures, feats.begin() + (size_t)q * kSketchFeatures);
       classic[q] = classic_estimate(sk[q]);
     }
@@ -422,7 +427,7 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
       double g = classic[q];
       double share = sk[q].top_share[11];
       if (learned) {
-        g = std::exp2(std::min(40.0, std::max(0.0, 32.0 * y[(size_t)q * kOut]))) - 1.0;
+        g = learned_groups(sk[q], y[(size_t)q * kOut]) + (sk[q].null_frac > 0 ? 1.0 : 0.0);
         g = std::max(g, sk[q].hll_estimate * 0.95);
         share = std::min(1.0, std::max(0.0, static_cast<double>(y[(size_t)q * kOut + 1])));
       }

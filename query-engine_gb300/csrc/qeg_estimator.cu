@@ -35,11 +35,18 @@ std::vector<float> predict_host(qeg_ctx* ctx, const float* feats, uint32_t n) {
 
 }  // namespace
 
+// The network predicts a correction to the classic estimate in log space:
+// log2(1 + groups) = log2(1 + classic non-null groups) + 32 * out0.
+double learned_groups(const SketchResult& s, float out0) {
+  const double classic = classic_estimate(s) - (s.null_frac > 0 ? 1.0 : 0.0);
+  const double lg = std::log2(1.0 + std::max(classic, 0.0)) + 32.0 * static_cast<double>(out0);
+  return std::exp2(std::min(40.0, std::max(0.0, lg))) - 1.0;
+}
+
 bool learned_estimate(qeg_ctx* ctx, const SketchResult& s, double* groups, double* hot_share) {
   if (!ctx->mlp || !ctx->mlp->loaded) return false;
   const std::vector<float> y = predict_host(ctx, s.features, 1);
-  const double lg = std::min(40.0, std::max(0.0, 32.0 * static_cast<double>(y[0])));
-  double g = std::exp2(lg) - 1.0;
+  double g = learned_groups(s, y[0]);
   // Never below what the sample itself proves, never above the non-null rows.
   const double nonnull = s.total_rows * (1.0 - s.null_frac);
   g = std::max(g, s.hll_estimate * 0.95);

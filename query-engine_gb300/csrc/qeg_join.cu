@@ -1203,11 +1203,14 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
             std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
         kern<<<grid, 256, 0, ctx->stream>>>(S);
       };
-      // Large probe sides stream through the TMA-staged kernel (one block of
-      // kTmaThreads per SM, a kStages ring of shared-memory tiles).
+      // The TMA-staged kernel (one block of kTmaThreads per SM, a kStages ring
+      // of shared-memory tiles) is opt-in (QEG_SINK_TMA=1): on GB300 the
+      // register-pipelined kernel reads the probe side faster (1.05 ms against
+      // 1.38 ms for 256M dense-table probes; 5.9 against 10.4 ms hashed).
       auto al16 = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };
+      const char* tma_env = getenv("QEG_SINK_TMA");
       const bool use_tma = n >= static_cast<uint64_t>(kTileRows) * ctx->sms * 2 && al16(S.kvalid) && al16(S.vvalid) &&
-                           getenv("QEG_NO_TMA") == nullptr;
+                           tma_env != nullptr && tma_env[0] == '1';
       auto launch_tma = [&](void (*kern)(SinkK, uint32_t*), size_t tile_bytes) {
         const size_t sb = tile_bytes * kStages;
         QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb)));

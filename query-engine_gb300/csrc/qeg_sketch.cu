@@ -227,6 +227,231 @@ void sketch_key_column(qeg_ctx* ctx, const DevCol& key, const uint32_t* sel, uin
   for (size_t i = 0; i < nh; ++i) out.heavy.push_back(ranked[i].second);
 }
 
+// ---------------------------------------------------------------------------
+// Batched sketch: one CTA per query of a batch (qeg_batch.cu). The CTA walks
+// the query's whole sample (the same strided 256-row sample blocks as
+// sketch_key_column), builds HyperLogLog registers, the count-min sketch and a
+// first-come candidate table in shared memory, and computes the 80 features
+// itself, so planning a batch costs one launch and one small copy back.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kBSThreads = 1024;
+constexpr int kBSCand = 2048;
+
+struct BatchSketchOut {
+  float f[kSketchFeatures];
+  double hll, rows, nulls;
+  double top[12];
+};
+
+struct BatchSketchK {
+  DevCol key;
+  const uint64_t* offs;  // nq + 1 row offsets
+  uint64_t sample_target;
+  BatchSketchOut* out;
+};
+
+__global__ void __launch_bounds__(kBSThreads) batch_sketch_kernel(const BatchSketchK P) {
+  extern __shared__ uint32_t sh[];
+  uint32_t* hll = sh;                                                   // kHllM
+  uint32_t* cms = hll + kHllM;                                          // kCmsDepth * kCmsWidth
+  unsigned long long* ck = reinterpret_cast<unsigned long long*>(cms + kCmsDepth * kCmsWidth);  // kBSCand
+  uint32_t* cc = reinterpret_cast<uint32_t*>(ck + kBSCand);             // kBSCand
+  __shared__ unsigned long long s_rows, s_nulls;
+  __shared__ uint32_t s_hist[64];
+  __shared__ unsigned long long s_bucket[12];
+  __shared__ double s_sum, s_f2;
+  __shared__ uint32_t s_zeros;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kHllM + kCmsDepth * kCmsWidth; i += blockDim.x) sh[i] = 0;
+  for (int i = tid; i < kBSCand; i += blockDim.x) {
+    ck[i] = 0;
+    cc[i] = 0;
+  }
+  if (tid < 64) s_hist[tid] = 0;
+  if (tid < 12) s_bucket[tid] = 0;
+  if (tid == 0) {
+    s_rows = s_nulls = 0;
+    s_sum = s_f2 = 0;
+    s_zeros = 0;
+  }
+  __syncthreads();
+
+  const uint64_t base = P.offs[blockIdx.x];
+  const uint64_t n = P.offs[blockIdx.x + 1] - base;
+  const uint64_t target_blocks = P.sample_target / kSampleBlock > 0 ? P.sample_target / kSampleBlock : 1;
+  uint64_t stride = kSampleBlock;
+  uint64_t nblocks = (n + kSampleBlock - 1) / kSampleBlock;
+  if (nblocks > target_blocks) {
+    stride = ((n / target_blocks) / kSampleBlock) * kSampleBlock;
+    if (stride < kSampleBlock) stride = kSampleBlock;
+    nblocks = (n + stride - 1) / stride;
+  }
+  unsigned long long rows = 0, nulls = 0;
+  for (uint64_t j = tid; j < nblocks * kSampleBlock; j += blockDim.x) {
+    const uint64_t i = (j / kSampleBlock) * stride + (j % kSampleBlock);
+    if (i >= n) continue;
+    const uint64_t p = base + i;
+    ++rows;
+    if (!col_valid(P.key, p)) {
+      ++nulls;
+      continue;
+    }
+    const uint64_t w = key_word(P.key, p);
+    const uint64_t h = sketch_hash(w);
+    const uint32_t idx = static_cast<uint32_t>(h >> (64 - kHllP));
+    const uint64_t rest = (h << kHllP) | (1ull << (kHllP - 1));
+    const uint32_t rho = static_cast<uint32_t>(__clzll(static_cast<long long>(rest))) + 1;
+    atomicMax(&hll[idx], rho);
+#pragma unroll
+    for (int d = 0; d < kCmsDepth; ++d) {
+      const uint32_t c = static_cast<uint32_t>(mix64(h + 0x9E3779B97F4A7C15ull * (d + 1)) >> 40) & (kCmsWidth - 1);
+      atomicAdd(&cms[d * kCmsWidth + c], 1u);
+    }
+    uint32_t s = static_cast<uint32_t>(h) & (kBSCand - 1);
+    const unsigned long long kk = w + 1;
+    for (int t = 0; t < 8; ++t) {
+      unsigned long long cur = ck[s];
+      if (cur == 0) cur = atomicCAS(&ck[s], 0ull, kk);
+      if (cur == 0 || cur == kk) {
+        atomicAdd(&cc[s], 1u);
+        break;
+      }
+      s = (s + 1) & (kBSCand - 1);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    rows += __shfl_down_sync(0xffffffffu, rows, o);
+    nulls += __shfl_down_sync(0xffffffffu, nulls, o);
+  }
+  if ((tid & 31) == 0) {
+    atomicAdd(&s_rows, rows);
+    atomicAdd(&s_nulls, nulls);
+  }
+  __syncthreads();
+
+  // Register histogram, HyperLogLog sum and zero count, F2 of CMS row 0.
+  double hsum = 0, f2 = 0;
+  uint32_t zeros = 0;
+  for (int i = tid; i < kHllM; i += blockDim.x) {
+    const uint32_t r = hll[i];
+    atomicAdd(&s_hist[r < 63 ? r : 63], 1u);
+    hsum += ldexp(1.0, -static_cast<int>(r));
+    zeros += r == 0;
+  }
+  for (int c = tid; c < kCmsWidth; c += blockDim.x) {
+    const double v = cms[c];
+    f2 += v * v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    hsum += __shfl_down_sync(0xffffffffu, hsum, o);
+    f2 += __shfl_down_sync(0xffffffffu, f2, o);
+    zeros += __shfl_down_sync(0xffffffffu, zeros, o);
+  }
+  if ((tid & 31) == 0) {
+    atomicAdd(&s_sum, hsum);
+    atomicAdd(&s_f2, f2);
+    atomicAdd(&s_zeros, zeros);
+  }
+  // Count-min estimate of every candidate seen at least twice (0 otherwise),
+  // into cc, then a descending bitonic sort of those estimates.
+  for (int i = tid; i < kBSCand; i += blockDim.x) {
+    uint32_t est = 0;
+    if (cc[i] >= 2) {
+      const uint64_t h = sketch_hash(ck[i] - 1);
+      est = UINT32_MAX;
+#pragma unroll
+      for (int d = 0; d < kCmsDepth; ++d) {
+        const uint32_t c = static_cast<uint32_t>(mix64(h + 0x9E3779B97F4A7C15ull * (d + 1)) >> 40) & (kCmsWidth - 1);
+        est = min(est, cms[d * kCmsWidth + c]);
+      }
+    }
+    cc[i] = est;
+  }
+  __syncthreads();
+  for (int k = 2; k <= kBSCand; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = tid; i < kBSCand; i += blockDim.x) {
+        const int x = i ^ j;
+        if (x > i) {
+          const uint32_t a = cc[i], b = cc[x];
+          if (((i & k) == 0) ? (a < b) : (a > b)) {
+            cc[i] = b;
+            cc[x] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // Sum of the top 2^b estimates: the estimate at sorted position j counts
+  // toward every prefix longer than j, i.e. bucket bitlength(j) and above.
+  for (int j = tid; j < kBSCand; j += blockDim.x) {
+    const int b = j == 0 ? 0 : 32 - __clz(j);
+    if (b < 12 && cc[j]) atomicAdd(&s_bucket[b], static_cast<unsigned long long>(cc[j]));
+  }
+  __syncthreads();
+  if (tid == 0) {
+    BatchSketchOut& o = P.out[blockIdx.x];
+    const double srows = static_cast<double>(s_rows), snulls = static_cast<double>(s_nulls);
+    const double nonnull = srows - snulls;
+    const double m = kHllM;
+    double e = (0.7213 / (1.0 + 1.079 / m)) * m * m / s_sum;
+    if (e <= 2.5 * m && s_zeros > 0) e = m * log(m / s_zeros);
+    o.hll = nonnull > 0 ? e : 0;
+    o.rows = srows;
+    o.nulls = snulls;
+    for (int i = 0; i < kSketchFeatures; ++i) o.f[i] = 0;
+    for (int r = 0; r < 64; ++r) o.f[r] = static_cast<float>(s_hist[r]) / kHllM;
+    double cum = 0;
+    for (int i = 0; i < 12; ++i) {
+      cum += static_cast<double>(s_bucket[i]);
+      o.top[i] = nonnull > 0 ? fmin(1.0, cum / nonnull) : 0;
+    }
+    for (int i = 0; i < 10; ++i) o.f[64 + i] = static_cast<float>(o.top[i]);
+    o.f[74] = nonnull > 0 ? static_cast<float>(s_f2 / (nonnull * nonnull)) : 0.f;
+    o.f[75] = static_cast<float>(log2(1.0 + srows) / 32.0);
+    o.f[76] = static_cast<float>(log2(1.0 + static_cast<double>(n)) / 32.0);
+    o.f[77] = n > 0 ? static_cast<float>(srows / static_cast<double>(n)) : 1.f;
+    o.f[78] = srows > 0 ? static_cast<float>(snulls / srows) : 0.f;
+    o.f[79] = nonnull > 0 ? static_cast<float>(fmin(1.0, o.hll / nonnull)) : 0.f;
+  }
+}
+
+}  // namespace
+
+void batch_sketch(qeg_ctx* ctx, const DevCol& key, const uint64_t* d_offsets, const std::vector<uint64_t>& offsets,
+                  uint64_t sample_target, std::vector<SketchResult>& out) {
+  const uint32_t nq = static_cast<uint32_t>(offsets.size() - 1);
+  out.assign(nq, SketchResult{});
+  if (nq == 0) return;
+  DevBuf buf(static_cast<size_t>(nq) * sizeof(BatchSketchOut), ctx->stream);
+  BatchSketchK P{};
+  P.key = key;
+  P.offs = d_offsets;
+  P.sample_target = sample_target;
+  P.out = buf.get<BatchSketchOut>();
+  const size_t sb = (kHllM + kCmsDepth * kCmsWidth) * 4 + kBSCand * 12;
+  QEG_CUDA(cudaFuncSetAttribute(batch_sketch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+  batch_sketch_kernel<<<nq, kBSThreads, sb, ctx->stream>>>(P);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+  std::vector<BatchSketchOut> h(nq);
+  QEG_CUDA(cudaMemcpyAsync(h.data(), buf.get(), nq * sizeof(BatchSketchOut), cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  check_device_error(ctx);
+  for (uint32_t q = 0; q < nq; ++q) {
+    SketchResult& r = out[q];
+    std::copy(h[q].f, h[q].f + kSketchFeatures, r.features);
+    r.hll_estimate = h[q].hll;
+    r.sample_rows = h[q].rows;
+    r.total_rows = static_cast<double>(offsets[q + 1] - offsets[q]);
+    r.null_frac = h[q].rows > 0 ? h[q].nulls / h[q].rows : 0;
+    for (int i = 0; i < 12; ++i) r.top_share[i] = h[q].top[i];
+  }
+}
+
 double classic_estimate(const SketchResult& s) {
   // Distinct count of the sample from HyperLogLog, scaled to the population by
   // inverting E[d_sample] = D (1 - (1 - 1/D)^m) (a uniform-frequency model),

@@ -483,6 +483,14 @@ def sketch(ctx, col, sample_rows=0):
     return f, g.value, s.value
 
 
+def learned_groups(classic, out0):
+    """Group count from the classic estimate of a null-free key column and the
+    network's first output: log2(1 + g) = log2(1 + classic) + 32 * out0."""
+    import math
+
+    return 2.0 ** min(40.0, max(0.0, math.log2(1.0 + max(classic, 0.0)) + 32.0 * out0)) - 1.0
+
+
 def estimator_init(ctx, seed):
     _check(lib().qeg_estimator_init(ctx.p, seed), ctx.p)
 

@@ -47,7 +47,7 @@ def scramble(x, salt):
 def gen_keys(rng, g, dev):
     """One seeded key column: (keys int64 tensor, description). Only
     elementwise torch ops: no gathers."""
-    n = int(2 ** rng.uniform(14, 27.5))
+    n = int(2 ** rng.uniform(14, 29.5))
     fam = rng.choice(["uniform", "zipf", "sequential", "mixture"], p=[0.3, 0.4, 0.1, 0.2])
     dom = int(2 ** rng.uniform(2, 28))
     salt = int(rng.integers(0, 1 << 62))
@@ -56,7 +56,7 @@ def gen_keys(rng, g, dev):
         desc = {"family": fam, "domain": dom}
     elif fam == "zipf":
         s = float(rng.uniform(0.3, 1.6))
-        dom = min(dom, 1 << 26)
+        dom = min(dom, 1 << 27)
         cdf = torch.arange(1, dom + 1, dtype=torch.float64, device=dev).pow_(-s).cumsum_(0)
         cdf /= cdf[-1].clone()
         r = torch.searchsorted(cdf, torch.rand(n, generator=g, device=dev, dtype=torch.float64)).clamp_(0, dom - 1)
@@ -94,8 +94,9 @@ def exact_stats(ctx, keys):
     return n, share
 
 
-def targets(groups, share):
-    return [math.log2(1.0 + groups) / 32.0, share]
+def targets(groups, share, classic):
+    """The network's first output corrects the classic estimate in log space."""
+    return [(math.log2(1.0 + groups) - math.log2(1.0 + classic)) / 32.0, share]
 
 
 def build_set(ctx, rng, count, dev, seed):
@@ -111,7 +112,7 @@ def build_set(ctx, rng, count, dev, seed):
         ctx.synchronize()
         print("dataset %d %s groups=%d share=%.3f" % (i, desc, groups, share), flush=True)
         X.append(f)
-        T.append(targets(groups, share))
+        T.append(targets(groups, share, classic))
         C.append(classic)
         desc.update({"groups": groups, "top_share": share, "classic": classic})
         D.append(desc)
@@ -125,9 +126,9 @@ def log2_err(est, true):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--datasets", type=int, default=1200)
-    ap.add_argument("--heldout", type=int, default=200)
-    ap.add_argument("--epochs", type=int, default=400)
+    ap.add_argument("--datasets", type=int, default=2000)
+    ap.add_argument("--heldout", type=int, default=300)
+    ap.add_argument("--epochs", type=int, default=3000)
     ap.add_argument("--out", default=os.path.join(HERE, "estimator_weights.f32"))
     ap.add_argument("--report", default=None)
     ap.add_argument("--seed", type=int, default=20260615)
@@ -148,7 +149,7 @@ def main():
     w = qeg.estimator_get_weights(ctx)
     w.astype("<f4").tofile(args.out)
     Y = qeg.estimator_predict(ctx, Xh)
-    learned = [2 ** (32 * float(y[0])) - 1 for y in Y]
+    learned = [qeg.learned_groups(c, float(y[0])) for c, y in zip(Ch, Y)]
     true = [d["groups"] for d in Dh]
     e_learned = [log2_err(a, b) for a, b in zip(learned, true)]
     e_classic = [log2_err(a, b) for a, b in zip(Ch, true)]

@@ -97,7 +97,7 @@ def test_learned_estimator_beats_classic_and_sizes_tables():
         keys = zipf_column(torch, n, dom, s, seed)
         col = qeg.Col(keys, None, qeg.I64)
         f, classic, _ = qeg.sketch(ctx, col)
-        learned = 2 ** (32 * float(qeg.estimator_predict(ctx, f)[0][0])) - 1
+        learned = qeg.learned_groups(classic, float(qeg.estimator_predict(ctx, f)[0][0]))
         true = int(torch.unique(keys).numel())
         el.append(abs(math.log2(max(learned, 1)) - math.log2(true)))
         ec.append(abs(math.log2(max(classic, 1)) - math.log2(true)))

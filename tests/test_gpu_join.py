@@ -151,10 +151,14 @@ def test_random_joins(ctx, seed):
 
 @pytest.mark.parametrize("strategy", [qeg.JOIN_AUTO, qeg.JOIN_HASH, qeg.JOIN_DENSE])
 @pytest.mark.parametrize("dup", [False, True])
-def test_count_sum_sink(ctx, strategy, dup):
+@pytest.mark.parametrize("tma", [False, True])
+def test_count_sum_sink(ctx, strategy, dup, tma, monkeypatch):
     """The 16M x 256M join workload's shape at 1/64 scale: unique (or
     duplicated) build keys, probe keys half hits and half from a disjoint
-    range, 2% NULL keys on both sides, SUM over an int64 payload."""
+    range, 2% NULL keys on both sides, SUM over an int64 payload. `tma` runs
+    the opt-in TMA-staged sink kernel (each 2M-row half is large enough)."""
+    if tma:
+        monkeypatch.setenv("QEG_SINK_TMA", "1")
     rng = np.random.default_rng(99 + strategy + 10 * dup)
     nb, npr = 1 << 18, 1 << 22
     bkey = rng.permutation(nb).astype(np.int64)
