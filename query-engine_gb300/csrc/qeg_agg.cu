@@ -48,43 +48,12 @@ __device__ __forceinline__ uint64_t ld_volatile_shared(const uint64_t* p) {
   return *reinterpret_cast<const volatile uint64_t*>(p);
 }
 
-// Applies one value to one state word. `row` points at the field block.
-template <bool SHARED>
-__device__ __forceinline__ void apply_field(uint64_t* w, uint8_t kind, bool valid, uint64_t bits,
-                                            int32_t vtype) {
-  unsigned long long* u = reinterpret_cast<unsigned long long*>(w);
-  switch (kind) {
-    case F_NULLS:
-      if (!valid) atomicAdd(u, 1ull);
-      break;
-    case F_SUMI:
-      if (valid) atomicAdd(u, static_cast<unsigned long long>(bits));
-      break;
-    case F_SUMF:
-      if (valid) atomicAdd(reinterpret_cast<double*>(w), __longlong_as_double(static_cast<long long>(bits)));
-      break;
-    case F_MINI:
-      if (valid) atomicMax(u, static_cast<unsigned long long>(~enc_i64(static_cast<int64_t>(bits))));
-      break;
-    case F_MAXI:
-      if (valid) atomicMax(u, static_cast<unsigned long long>(enc_i64(static_cast<int64_t>(bits))));
-      break;
-    case F_MINF:
-      if (valid) atomicMax(u, static_cast<unsigned long long>(~enc_f64_bits(bits)));
-      break;
-    case F_MAXF:
-      if (valid) atomicMax(u, static_cast<unsigned long long>(enc_f64_bits(bits)));
-      break;
-    default: break;
-  }
-  (void)vtype;
-}
-
 // Loads the values of one row for every referenced value column.
+template <int NV>
 __device__ __forceinline__ void load_values(const AggK& P, uint64_t p, bool (&vv)[kMaxVals],
                                             uint64_t (&vb)[kMaxVals]) {
 #pragma unroll
-  for (int c = 0; c < kMaxVals; ++c) {
+  for (int c = 0; c < NV; ++c) {
     vv[c] = false;
     vb[c] = 0;
     if (c < P.nvals) {
@@ -100,19 +69,26 @@ __device__ __forceinline__ void load_values(const AggK& P, uint64_t p, bool (&vv
   }
 }
 
-// Applies a row to the field block `f` (row count + every value field).
-template <bool SHARED>
+// Applies one row to the field block `f` with atomics (row count + every
+// value field).
+template <int NV>
 __device__ __forceinline__ void apply_row(uint64_t* f, const AggK& P, const bool (&vv)[kMaxVals],
                                           const uint64_t (&vb)[kMaxVals]) {
   atomicAdd(reinterpret_cast<unsigned long long*>(f), 1ull);  // F_ROWS is field 0
+#pragma unroll 1
+  for (int fi = 1; fi < P.nfields; ++fi) {
+    const uint8_t kind = P.fkind[fi];
+    const int c = P.fcol[fi];
+    bool v = false;
+    uint64_t b = 0;
 #pragma unroll
-  for (int c = 0; c < kMaxVals; ++c) {
-    if (c < P.nvals) {
-      const int first = P.cfirst[c];
-      const int n = P.cnf[c];
-      for (int k = 0; k < n; ++k)
-        apply_field<SHARED>(f + first + k, P.fkind[first + k], vv[c], vb[c], P.val[c].type);
+    for (int j = 0; j < NV; ++j) {
+      if (j == c) {
+        v = vv[j];
+        b = vb[j];
+      }
     }
+    field_apply(f + fi, kind, field_contrib(kind, v, b));
   }
 }
 
@@ -125,21 +101,36 @@ __device__ __forceinline__ uint64_t* global_row1(const AggK& P, bool kv, uint64_
   const int W = P.row_words;
   if (!kv) return P.table + (P.cap + 1) * W;
   if (k == 0) return P.table + P.cap * W;
+  // Linear probing, four slots per step: the four key words are loaded
+  // together (independent loads), then examined in slot order, so a probe
+  // sequence costs a quarter of the dependent memory round trips. A key word
+  // never changes once set, so a stale non-empty value stays correct.
   uint64_t s = __umul64hi(h, P.cap);
-  for (int t = 0; t < limit; ++t) {
-    uint64_t* r = P.table + s * W;
-    const uint64_t cur = ld_relaxed(r);
-    if (cur == k) return r;
-    if (cur == 0) {
-      const unsigned long long old =
-          atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, static_cast<unsigned long long>(k));
-      if (old == 0) {
-        ++inserted;
-        return r;
-      }
-      if (old == k) return r;
+  for (int t = 0; t < limit; t += 4) {
+    uint64_t idx[4], cur[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      uint64_t x = s + j;
+      if (x >= P.cap) x -= P.cap;
+      idx[j] = x;
+      cur[j] = ld_relaxed(P.table + x * W);
     }
-    s = (s + 1 == P.cap) ? 0 : s + 1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      uint64_t* r = P.table + idx[j] * W;
+      if (cur[j] == k) return r;
+      if (cur[j] == 0) {
+        const unsigned long long old =
+            atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, static_cast<unsigned long long>(k));
+        if (old == 0) {
+          ++inserted;
+          return r;
+        }
+        if (old == k) return r;
+      }
+    }
+    s += 4;
+    if (s >= P.cap) s -= P.cap;
   }
   return nullptr;
 }
@@ -211,9 +202,10 @@ __device__ __forceinline__ void merge_fields(uint64_t* dst, const uint64_t* src,
 }
 
 // Combines the rows of every peer group and lets each group's leader apply the
-// result to `f` (its field block; ignored on other lanes).
-// `priv`: `f` is a warp-private row, updated without atomics (one leader per
-// group and one group per row within a warp).
+// result to `f` (its field block; ignored on other lanes). `priv`: `f` is a
+// warp-private row, updated without atomics (one leader per group and one
+// group per row within a warp). One loop over the fields keeps the code small.
+template <int NV>
 __device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, bool priv, unsigned peers, const PeerPlan& pp,
                                            const AggK& P, const bool (&vv)[kMaxVals],
                                            const uint64_t (&vb)[kMaxVals]) {
@@ -221,19 +213,23 @@ __device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, bool priv, 
     if (priv) f[0] += __popc(peers);
     else atomicAdd(reinterpret_cast<unsigned long long*>(f), static_cast<unsigned long long>(__popc(peers)));
   }
+#pragma unroll 1
+  for (int fi = 1; fi < P.nfields; ++fi) {
+    const uint8_t kind = P.fkind[fi];
+    const int c = P.fcol[fi];
+    bool v = false;
+    uint64_t b = 0;
 #pragma unroll
-  for (int c = 0; c < kMaxVals; ++c) {
-    if (c < P.nvals) {
-      const int first = P.cfirst[c];
-      const int n = P.cnf[c];
-      for (int k = 0; k < n; ++k) {
-        const uint8_t kind = P.fkind[first + k];
-        const uint64_t x = peer_reduce(field_contrib(kind, vv[c], vb[c]), kind, pp);
-        if (leader) {
-          if (priv) f[first + k] = field_combine(kind, f[first + k], x);
-          else field_apply(f + first + k, kind, x);
-        }
+    for (int j = 0; j < NV; ++j) {
+      if (j == c) {
+        v = vv[j];
+        b = vb[j];
       }
+    }
+    const uint64_t x = peer_reduce(field_contrib(kind, v, b), kind, pp);
+    if (leader) {
+      if (priv) f[fi] = field_combine(kind, f[fi], x);
+      else field_apply(f + fi, kind, x);
     }
   }
 }
@@ -243,7 +239,7 @@ __device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, bool priv, 
 // Warps walk the rows 32 at a time (blockDim.x is a multiple of 32), so every
 // lane reaches the warp-wide intrinsics.
 // ---------------------------------------------------------------------------
-template <int MODE>
+template <int MODE, int NV>
 __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   extern __shared__ uint64_t sm[];
   const int W = P.row_words;
@@ -314,13 +310,13 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       vv[c] = false;
       vb[c] = 0;
     }
-    if (live) load_values(P, p, vv, vb);
+    if (live) load_values<NV>(P, p, vv, vb);
     const unsigned livemask = __ballot_sync(0xffffffffu, live);
 
     if (MODE == 0) {
       const unsigned peers = live ? livemask : (1u << lane);
       const PeerPlan pp = plan_peers(peers, lane);
-      warp_apply(&wrows[warp * W + 1], live && __ffs(peers) - 1 == static_cast<int>(lane), true, peers, pp, P, vv,
+      warp_apply<NV>(&wrows[warp * W + 1], live && __ffs(peers) - 1 == static_cast<int>(lane), true, peers, pp, P, vv,
                  vb);
       continue;
     }
@@ -387,7 +383,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
         peers = 1u << lane;
       }
       const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
-      warp_apply(f, leader && ok, priv, peers, pp, P, vv, vb);
+      warp_apply<NV>(f, leader && ok, priv, peers, pp, P, vv, vb);
       if (P.full_flag) {
         pending += __popc(__ballot_sync(0xffffffffu, inserted != ins0));
         if (pending >= 64 || (iter & 15) == 15) {
@@ -419,7 +415,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
     }
     uint64_t* r = global_rowN(P, words, nullmask, h, inserted);
     if (r)
-      apply_row<false>(r + fo, P, vv, vb);
+      apply_row<NV>(r + fo, P, vv, vb);
     else
       spill_row(P, p);
   }
@@ -750,6 +746,7 @@ AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel
   }
   P.nfields = nfields;
   for (int f = 0; f < nfields; ++f) P.fkind[f] = fkind[f];
+  set_field_columns(P);
   P.row_words = row_words;
   P.table = table.get<uint64_t>();
   P.cap = cap;
@@ -776,6 +773,11 @@ AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel
   }
   P.err = static_cast<uint32_t*>(ctx->dev_err.get());
   return P;
+}
+
+void AggState::set_field_columns(AggK& P) const {
+  for (size_t c = 0; c < cfirst.size(); ++c)
+    for (int k = 0; k < cnf[c]; ++k) P.fcol[cfirst[c] + k] = static_cast<uint8_t>(c);
 }
 
 int AggState::block_threads() const { return cfg.block_threads > 0 ? cfg.block_threads : 512; }
@@ -807,14 +809,22 @@ void AggState::launch(const AggK& P, uint64_t nrows) {
   const size_t sb = smem_bytes(block);
   if (mode == 1)  // running insert count and table-full flag
     QEG_CUDA(cudaMemsetAsync(counters.get<uint8_t>() + 24, 0, 16, ctx->stream));
+  // Kernel variant: the mode and the number of value columns rounded up to 1,
+  // 2, 4 or 8 (loops over value columns are unrolled to that count).
+  void (*kern)(AggK) = nullptr;
+  const int nv = static_cast<int>(val_cols.size());
+#define QEG_AGG_VARIANT(M)                          \
+  (nv <= 1   ? agg_kernel<M, 1>                     \
+   : nv <= 2 ? agg_kernel<M, 2>                     \
+   : nv <= 4 ? agg_kernel<M, 4>                     \
+             : agg_kernel<M, 8>)
+  if (mode == 0) kern = QEG_AGG_VARIANT(0);
+  else if (mode == 1) kern = QEG_AGG_VARIANT(1);
+  else kern = QEG_AGG_VARIANT(2);
+#undef QEG_AGG_VARIANT
   int per_sm = 1;
-  auto set_attr = [&](auto kern) {
-    if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
-  };
-  if (mode == 0) set_attr(agg_kernel<0>);
-  else if (mode == 1) set_attr(agg_kernel<1>);
-  else set_attr(agg_kernel<2>);
+  if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
   require(per_sm > 0, "aggregate kernel does not fit on an SM with this configuration");
   // Each CTA should aggregate a few thousand rows at least, so clearing and
   // flushing its private table (which touches occupied rows only) stays small.
@@ -822,9 +832,7 @@ void AggState::launch(const AggK& P, uint64_t nrows) {
   uint64_t want = (nrows + min_rows_per_cta - 1) / min_rows_per_cta;
   uint64_t grid = std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * per_sm);
   if (grid == 0) grid = 1;
-  if (mode == 0) agg_kernel<0><<<(unsigned)grid, block, sb, ctx->stream>>>(P);
-  else if (mode == 1) agg_kernel<1><<<(unsigned)grid, block, sb, ctx->stream>>>(P);
-  else agg_kernel<2><<<(unsigned)grid, block, sb, ctx->stream>>>(P);
+  kern<<<(unsigned)grid, block, sb, ctx->stream>>>(P);
   ctx->launches++;
   QEG_CUDA(cudaGetLastError());
 }
@@ -862,6 +870,7 @@ AggK AggState::kparams_base() const {
   }
   P.nfields = nfields;
   for (int f = 0; f < nfields; ++f) P.fkind[f] = fkind[f];
+  set_field_columns(P);
   P.row_words = row_words;
   P.table = table.get<uint64_t>();
   P.cap = cap;

@@ -32,6 +32,7 @@ struct AggK {
   DevCol val[kMaxVals];
   int nkeys, nvals, nfields, row_words;
   uint8_t fkind[kMaxFields];
+  uint8_t fcol[kMaxFields];  // value column of each field (field 0: rows)
   uint8_t cfirst[kMaxVals];
   uint8_t cnf[kMaxVals];
   uint64_t* table;
@@ -135,6 +136,7 @@ struct AggState {
   size_t smem_bytes(int block) const;
   int warp_hot() const;
   int block_threads() const;
+  void set_field_columns(AggK& P) const;
   void launch(const AggK& P, uint64_t nrows);
   void read_counters(uint64_t out[3]);
   void grow(uint64_t new_cap);

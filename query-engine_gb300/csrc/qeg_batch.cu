@@ -180,12 +180,15 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
 
 struct BatchFinK {
   const BatchQ* qs;
+  const uint32_t* fin_q;      // per block: query
+  const uint64_t* fin_start;  // per block: first table row
+  const uint32_t* fin_len;    // per block: table rows
   uint64_t* arena;
   int W;
   int32_t key_type;
   FinK F;  // output columns (arena-wide) and aggregate finalisation
   uint8_t fkind[kMaxFields];
-  unsigned long long* counts;  // per query output rows
+  unsigned long long* counts;  // per query output rows (zeroed before the launch)
 };
 
 __device__ __forceinline__ void put_typed(void* base, uint64_t i, int32_t t, uint64_t w) {
@@ -197,18 +200,19 @@ __device__ __forceinline__ void put_typed(void* base, uint64_t i, int32_t t, uin
   }
 }
 
-// One block per query: compacts the query's occupied rows into the output
-// arena (keys then aggregates, ops/agg_internal.h:169-229) and zeroes every
-// row it read, leaving the arena ready for the next replay.
+// Each block compacts one range of one query's table (hash slots, then the
+// key-0 and NULL side rows) into that query's output rows (keys then
+// aggregates, ops/agg_internal.h:169-229), reserving output rows with one
+// atomic per warp, and zeroes every row it read, leaving the arena ready for
+// the next replay.
 __global__ void batch_finalize_kernel(const BatchFinK P) {
-  __shared__ unsigned long long s_n;
-  if (threadIdx.x == 0) s_n = 0;
-  __syncthreads();
-  const BatchQ Q = P.qs[blockIdx.x];
+  const uint32_t q = P.fin_q[blockIdx.x];
+  const BatchQ Q = P.qs[q];
   uint64_t* T = P.arena + Q.table_off * P.W;
-  const uint64_t total = Q.cap + 2;
+  const uint64_t first = P.fin_start[blockIdx.x];
+  const uint64_t total = first + P.fin_len[blockIdx.x];
   const int lane = threadIdx.x & 31;
-  for (uint64_t base = 0; base < total; base += blockDim.x) {
+  for (uint64_t base = first; base < total; base += blockDim.x) {
     const uint64_t s = base + threadIdx.x;
     bool occ = false;
     uint64_t* r = nullptr;
@@ -218,7 +222,7 @@ __global__ void batch_finalize_kernel(const BatchFinK P) {
     }
     const unsigned m = __ballot_sync(0xffffffffu, occ);
     unsigned long long wb = 0;
-    if (lane == 0 && m) wb = atomicAdd(&s_n, static_cast<unsigned long long>(__popc(m)));
+    if (lane == 0 && m) wb = atomicAdd(P.counts + q, static_cast<unsigned long long>(__popc(m)));
     wb = __shfl_sync(0xffffffffu, wb, 0);
     if (occ) {
       const uint64_t o = Q.out_off + wb + __popc(m & ((1u << lane) - 1u));
@@ -268,8 +272,6 @@ __global__ void batch_finalize_kernel(const BatchFinK P) {
     if (s < total && (occ || s >= Q.cap))
       for (int w = 0; w < P.W; ++w) r[w] = 0;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) P.counts[blockIdx.x] = s_n;
 }
 
 uint64_t pow2_floor(uint64_t v) {
@@ -280,24 +282,40 @@ uint64_t pow2_floor(uint64_t v) {
 
 }  // namespace
 
+// One execution round: a set of queries with their tables in one arena, the
+// work items of the persistent kernel and the finalize ranges. The first
+// round holds every query and is captured into a CUDA graph; queries whose
+// table overflowed are re-run together in a further round with larger tables.
+struct Round {
+  std::vector<uint32_t> qids;  // batch query id of each local query
+  std::vector<BatchQ> qs;
+  uint32_t nitems = 0, nfin = 0;
+  int32_t max_slots = 0;  // largest CTA-private table of the round (sizes the shared memory)
+  DevBuf dqs, ditem_q, ditem_start, ditem_len, dfin_q, dfin_start, dfin_len, dnext, arena, overflow, counts;
+  std::vector<DevBuf> out_vals, out_valid;
+};
+
+constexpr uint32_t kFinRows = 1u << 16;  // table rows per finalize block
+
 struct BatchState {
   qeg_ctx* ctx = nullptr;
   AggState plan;  // field layout of [key, value] with the batch's aggregates
   std::vector<uint64_t> offsets;
-  std::vector<BatchQ> qs;
   std::vector<double> est;
   std::vector<float> hot;
+  std::vector<int32_t> slots;   // per query: CTA-private table slots (0 = global table only)
+  std::vector<uint64_t> chunk;  // per query: rows per work item
   StagedCol key, val;
-  uint32_t nq = 0, nitems = 0;
+  uint32_t nq = 0;
   int block = 512;
-  DevBuf doffs, dqs, ditem_q, ditem_start, ditem_len, dnext, arena, overflow, counts;
-  std::vector<DevBuf> out_vals, out_valid;
-  uint64_t arena_rows = 0, out_rows = 0;
+  DevBuf doffs;
+  std::vector<Round> rounds;  // [0] = every query; later rounds = overflow re-runs
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> group_counts;
+  std::vector<uint32_t> where_round, where_local;  // result location of each query
   std::vector<uint32_t> fell_back;
-  // Results of queries re-run exactly after an overflow.
+  // Queries still overflowing after the re-run rounds: recomputed exactly.
   std::vector<std::unique_ptr<AggState>> fallback;
 
   ~BatchState() {
@@ -305,36 +323,106 @@ struct BatchState {
     if (graph) cudaGraphDestroy(graph);
   }
 
-  BatchK kparams() {
+  uint64_t rows_of(uint32_t q) const { return offsets[q + 1] - offsets[q]; }
+
+  // Lays out round R over `qids` with table capacities `caps`.
+  void setup_round(Round& R, const std::vector<uint32_t>& qids, const std::vector<uint64_t>& caps) {
+    R.qids = qids;
+    const uint32_t n = static_cast<uint32_t>(qids.size());
+    R.qs.assign(n, BatchQ{});
+    R.max_slots = 0;
+    std::vector<uint32_t> iq, il, fq, fl;
+    std::vector<uint64_t> is, fs;
+    uint64_t table_rows = 0;
+    for (uint32_t l = 0; l < n; ++l) {
+      const uint32_t q = qids[l];
+      const uint64_t cap = caps[l];
+      R.qs[l] = BatchQ{table_rows, cap, table_rows, slots[q] > 0 ? 1 : 0, std::max(slots[q], 64)};
+      R.max_slots = std::max(R.max_slots, slots[q]);
+      table_rows += cap + 2;
+      const uint64_t rows = rows_of(q);
+      for (uint64_t s0 = 0; s0 < rows; s0 += chunk[q]) {
+        iq.push_back(l);
+        is.push_back(offsets[q] + s0);
+        il.push_back(static_cast<uint32_t>(std::min<uint64_t>(chunk[q], rows - s0)));
+      }
+      for (uint64_t s0 = 0; s0 < cap + 2; s0 += kFinRows) {
+        fq.push_back(l);
+        fs.push_back(s0);
+        fl.push_back(static_cast<uint32_t>(std::min<uint64_t>(kFinRows, cap + 2 - s0)));
+      }
+    }
+    R.nitems = static_cast<uint32_t>(iq.size());
+    R.nfin = static_cast<uint32_t>(fq.size());
+    // Longest items first, so the tail of the queue holds only small ones.
+    std::vector<uint32_t> order(R.nitems);
+    for (uint32_t i = 0; i < R.nitems; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return il[a] > il[b]; });
+    std::vector<uint32_t> oq(R.nitems), ol(R.nitems);
+    std::vector<uint64_t> os(R.nitems);
+    for (uint32_t i = 0; i < R.nitems; ++i) {
+      oq[i] = iq[order[i]];
+      ol[i] = il[order[i]];
+      os[i] = is[order[i]];
+    }
+    auto up = [&](DevBuf& d, const void* src, size_t bytes) {
+      d.alloc(std::max<size_t>(bytes, 8), ctx->stream);
+      if (bytes) QEG_CUDA(cudaMemcpyAsync(d.get(), src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    };
+    up(R.dqs, R.qs.data(), R.qs.size() * sizeof(BatchQ));
+    up(R.ditem_q, oq.data(), oq.size() * 4);
+    up(R.ditem_start, os.data(), os.size() * 8);
+    up(R.ditem_len, ol.data(), ol.size() * 4);
+    up(R.dfin_q, fq.data(), fq.size() * 4);
+    up(R.dfin_start, fs.data(), fs.size() * 8);
+    up(R.dfin_len, fl.data(), fl.size() * 4);
+    R.dnext.alloc(8, ctx->stream);
+    R.arena.alloc(std::max<uint64_t>(table_rows, 1) * plan.row_words * 8, ctx->stream);
+    QEG_CUDA(cudaMemsetAsync(R.arena.get(), 0, R.arena.bytes(), ctx->stream));
+    R.overflow.alloc(std::max<uint32_t>(n, 1) * 4, ctx->stream);
+    QEG_CUDA(cudaMemsetAsync(R.overflow.get(), 0, R.overflow.bytes(), ctx->stream));
+    R.counts.alloc(std::max<uint32_t>(n, 1) * 8, ctx->stream);
+    R.out_vals.resize(plan.rtypes.size());
+    R.out_valid.resize(plan.rtypes.size());
+    for (size_t c = 0; c < plan.rtypes.size(); ++c) {
+      R.out_vals[c].alloc(std::max<uint64_t>(table_rows, 1) * 8, ctx->stream);
+      R.out_valid[c].alloc(std::max<uint64_t>(table_rows, 1), ctx->stream);
+    }
+  }
+
+  BatchK kparams(Round& R) {
     BatchK P{};
     P.key = key.dev;
     P.val = val.dev;
-    P.qs = dqs.get<BatchQ>();
-    P.item_q = ditem_q.get<uint32_t>();
-    P.item_start = ditem_start.get<uint64_t>();
-    P.item_len = ditem_len.get<uint32_t>();
-    P.nitems = nitems;
-    P.next = dnext.get<unsigned int>();
-    P.arena = arena.get<uint64_t>();
+    P.qs = R.dqs.get<BatchQ>();
+    P.item_q = R.ditem_q.get<uint32_t>();
+    P.item_start = R.ditem_start.get<uint64_t>();
+    P.item_len = R.ditem_len.get<uint32_t>();
+    P.nitems = R.nitems;
+    P.next = R.dnext.get<unsigned int>();
+    P.arena = R.arena.get<uint64_t>();
     P.W = plan.row_words;
     P.nfields = plan.nfields;
     for (int f = 0; f < plan.nfields; ++f) P.fkind[f] = plan.fkind[f];
     P.val_first = plan.cfirst.empty() ? 0 : plan.cfirst[0];
     P.val_nf = plan.cnf.empty() ? 0 : plan.cnf[0];
-    P.overflow = overflow.get<uint32_t>();
+    P.overflow = R.overflow.get<uint32_t>();
     return P;
   }
 
-  BatchFinK finparams() {
+  BatchFinK finparams(Round& R) {
     BatchFinK F{};
-    F.qs = dqs.get<BatchQ>();
-    F.arena = arena.get<uint64_t>();
+    F.qs = R.dqs.get<BatchQ>();
+    F.fin_q = R.dfin_q.get<uint32_t>();
+    F.fin_start = R.dfin_start.get<uint64_t>();
+    F.fin_len = R.dfin_len.get<uint32_t>();
+    F.arena = R.arena.get<uint64_t>();
     F.W = plan.row_words;
     F.key_type = plan.rtypes[0];
     F.F.naggs = static_cast<int>(plan.aggs.size());
     for (size_t c = 0; c < plan.rtypes.size(); ++c) {
-      F.F.vals[c] = out_vals[c].get();
-      F.F.valid[c] = out_valid[c].get<uint8_t>();
+      F.F.vals[c] = R.out_vals[c].get();
+      F.F.valid[c] = R.out_valid[c].get<uint8_t>();
       F.F.rtype[c] = plan.rtypes[c];
     }
     for (size_t a = 0; a < plan.aggs.size(); ++a) {
@@ -343,15 +431,49 @@ struct BatchState {
       F.F.nfield[a] = plan.nfield[a];
     }
     for (int f = 0; f < plan.nfields; ++f) F.fkind[f] = plan.fkind[f];
-    F.counts = counts.get<unsigned long long>();
+    F.counts = R.counts.get<unsigned long long>();
     return F;
   }
 
-  void enqueue_run() {
-    QEG_CUDA(cudaMemsetAsync(dnext.get(), 0, 4, ctx->stream));
-    const size_t sb = static_cast<size_t>(kBatchMaxSlots + 2) * plan.row_words * 8;
-    batch_agg_kernel<<<ctx->sms * std::max(1, 2048 / block / 2), block, sb, ctx->stream>>>(kparams());
-    batch_finalize_kernel<<<nq, 512, 0, ctx->stream>>>(finparams());
+  size_t smem_bytes(int32_t max_slots) const { return static_cast<size_t>(max_slots + 2) * plan.row_words * 8; }
+
+  void enqueue(Round& R) {
+    QEG_CUDA(cudaMemsetAsync(R.dnext.get(), 0, 4, ctx->stream));
+    QEG_CUDA(cudaMemsetAsync(R.counts.get(), 0, R.counts.bytes(), ctx->stream));
+    const size_t sb = smem_bytes(R.max_slots);
+    int per_sm = 1;
+    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_agg_kernel, block, sb));
+    const unsigned grid = static_cast<unsigned>(
+        std::max(1, std::min<int>(ctx->sms * std::max(per_sm, 1), static_cast<int>(std::max<uint32_t>(R.nitems, 1)))));
+    batch_agg_kernel<<<grid, block, sb, ctx->stream>>>(kparams(R));
+    if (R.nfin) batch_finalize_kernel<<<R.nfin, 512, 0, ctx->stream>>>(finparams(R));
+  }
+
+  // Reads the overflow flags and counts of round r into the per-query results.
+  std::vector<uint32_t> collect(uint32_t r) {
+    Round& R = rounds[r];
+    const size_t n = R.qids.size();
+    std::vector<uint32_t> ovf(n);
+    std::vector<uint64_t> cnt(n);
+    if (n) {
+      QEG_CUDA(cudaMemcpyAsync(ovf.data(), R.overflow.get(), n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      QEG_CUDA(cudaMemcpyAsync(cnt.data(), R.counts.get(), n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      QEG_CUDA(cudaMemsetAsync(R.overflow.get(), 0, n * 4, ctx->stream));
+    }
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+    check_device_error(ctx);
+    std::vector<uint32_t> again;
+    for (size_t l = 0; l < n; ++l) {
+      const uint32_t q = R.qids[l];
+      if (ovf[l]) {
+        again.push_back(static_cast<uint32_t>(l));
+        continue;
+      }
+      group_counts[q] = cnt[l];
+      where_round[q] = r;
+      where_local[q] = static_cast<uint32_t>(l);
+    }
+    return again;
   }
 };
 
@@ -374,6 +496,8 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
     require(key->len == val->len && row_offsets[nqueries] == key->len, "row offsets must cover the columns");
     for (uint32_t q = 0; q < nqueries; ++q) require(row_offsets[q] <= row_offsets[q + 1], "row offsets must ascend");
     require(key->type != QEG_F64 && key->type != QEG_STR, "batched GROUP BY keys are integer columns");
+    require(block_threads == 0 || (block_threads >= 32 && block_threads <= 1024 && block_threads % 32 == 0),
+            "block_threads must be 0 or a multiple of 32 in [32, 1024]");
     QEG_CUDA(cudaSetDevice(ctx->device));
     auto b = std::make_unique<qeg_batch>();
     BatchState& S = b->st;
@@ -390,24 +514,18 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
     stage_column(ctx, *key, S.key);
     stage_column(ctx, *val, S.val);
     S.block = block_threads > 0 ? block_threads : 512;
-    // ---- plan every query ----
-    S.qs.resize(nqueries);
-    S.est.resize(nqueries);
-    S.hot.resize(nqueries);
     for (uint32_t q = 0; q < nqueries; ++q)
       require((S.key.dev.all_valid && S.val.dev.all_valid) || S.offsets[q] % 64 == 0,
               "queries over columns with NULLs must start on 64-row boundaries");
+    // ---- plan every query: one sketch launch, one batched network pass ----
     S.doffs.alloc((nqueries + 1) * 8, ctx->stream);
     QEG_CUDA(cudaMemcpyAsync(S.doffs.get(), S.offsets.data(), (nqueries + 1) * 8, cudaMemcpyHostToDevice,
                              ctx->stream));
     std::vector<SketchResult> sk;
     batch_sketch(ctx, S.key.dev, S.doffs.get<uint64_t>(), S.offsets, 1u << 16, sk);
     std::vector<float> feats((size_t)nqueries * kSketchFeatures);
-    std::vector<double> classic(nqueries);
-    for (uint32_t q = 0; q < nqueries; ++q) {
+    for (uint32_t q = 0; q < nqueries; ++q)
       std::copy(sk[q].features, sk[q].features + kSketchFeatures, feats.begin() + (size_t)q * kSketchFeatures);
-      classic[q] = classic_estimate(sk[q]);
-    }
     const bool learned = ctx->mlp && ctx->mlp->loaded;
     std::vector<float> y;
     if (learned) {
@@ -419,12 +537,15 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
       QEG_CUDA(cudaMemcpyAsync(y.data(), m.y.get(), y.size() * 4, cudaMemcpyDeviceToHost, ctx->stream));
       QEG_CUDA(cudaStreamSynchronize(ctx->stream));
     }
-    uint64_t table_rows = 0, out_rows = 0;
-    std::vector<uint32_t> item_q, item_len;
-    std::vector<uint64_t> item_start;
+    S.est.resize(nqueries);
+    S.hot.resize(nqueries);
+    S.slots.resize(nqueries);
+    S.chunk.resize(nqueries);
+    std::vector<uint32_t> all(nqueries);
+    std::vector<uint64_t> caps(nqueries);
     for (uint32_t q = 0; q < nqueries; ++q) {
-      const uint64_t n = S.offsets[q + 1] - S.offsets[q];
-      double g = classic[q];
+      const uint64_t n = S.rows_of(q);
+      double g = classic_estimate(sk[q]);
       double share = sk[q].top_share[11];
       if (learned) {
         g = learned_groups(sk[q], y[(size_t)q * kOut]) + (sk[q].null_frac > 0 ? 1.0 : 0.0);
@@ -434,70 +555,36 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
       g = std::min(std::max(g, 1.0), static_cast<double>(std::max<uint64_t>(n, 1)));
       S.est[q] = g;
       S.hot[q] = static_cast<float>(share);
-      // Tuning table: the first entry whose bucket covers this query.
-      int smem = g <= 0.5 * kBatchMaxSlots || share >= 0.3 ? 1 : 0;
-      int slots = static_cast<int>(std::min<uint64_t>(kBatchMaxSlots, pow2_floor(std::max(64.0, 2.0 * g))));
-      uint64_t chunk = 1u << 16;
+      // Built-in defaults, then the tuning table: the first entry whose bucket
+      // covers this query's (log2 groups, skew class).
+      int32_t sl = (g <= 0.5 * kBatchMaxSlots || share >= 0.3)
+                       ? static_cast<int32_t>(std::min<uint64_t>(kBatchMaxSlots, pow2_floor(std::max(64.0, 2.0 * g))))
+                       : 0;
+      uint64_t ch = 1u << 16;
       const double lg = std::log2(std::max(g, 1.0));
       for (int t = 0; t < ntuning; ++t) {
         if (lg <= tuning[t].max_log2_groups && (share >= 0.3 ? 1 : 0) == tuning[t].skewed) {
-          smem = tuning[t].smem_slots > 0 ? 1 : 0;
-          if (tuning[t].smem_slots > 0) slots = std::min(kBatchMaxSlots, tuning[t].smem_slots);
-          chunk = tuning[t].rows_per_item;
+          sl = tuning[t].smem_slots > 0
+                   ? static_cast<int32_t>(pow2_floor(std::min<int32_t>(kBatchMaxSlots, std::max(64, tuning[t].smem_slots))))
+                   : 0;
+          if (tuning[t].rows_per_item > 0) ch = tuning[t].rows_per_item;
           break;
         }
       }
-      const uint64_t cap = std::max<uint64_t>(64, static_cast<uint64_t>(1.15 * g / kTargetLoad) + 16);
-      S.qs[q] = BatchQ{table_rows, cap, out_rows, smem, static_cast<int32_t>(pow2_floor(slots))};
-      table_rows += cap + 2;
-      out_rows += cap + 2;
-      for (uint64_t s0 = 0; s0 < n; s0 += chunk) {
-        item_q.push_back(q);
-        item_start.push_back(S.offsets[q] + s0);
-        item_len.push_back(static_cast<uint32_t>(std::min<uint64_t>(chunk, n - s0)));
-      }
+      S.slots[q] = sl;
+      S.chunk[q] = std::max<uint64_t>(ch, 256);
+      all[q] = q;
+      caps[q] = std::max<uint64_t>(64, static_cast<uint64_t>(1.15 * g / kTargetLoad) + 16);
     }
-    S.nitems = static_cast<uint32_t>(item_q.size());
-    S.arena_rows = table_rows;
-    S.out_rows = out_rows;
-    // Longest items first, so the tail of the queue holds only small ones.
-    std::vector<uint32_t> order(S.nitems);
-    for (uint32_t i = 0; i < S.nitems; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b2) { return item_len[a] > item_len[b2]; });
-    std::vector<uint32_t> iq(S.nitems), il(S.nitems);
-    std::vector<uint64_t> is(S.nitems);
-    for (uint32_t i = 0; i < S.nitems; ++i) {
-      iq[i] = item_q[order[i]];
-      il[i] = item_len[order[i]];
-      is[i] = item_start[order[i]];
-    }
-    auto up = [&](DevBuf& d, const void* src, size_t bytes) {
-      d.alloc(std::max<size_t>(bytes, 8), ctx->stream);
-      if (bytes) QEG_CUDA(cudaMemcpyAsync(d.get(), src, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    };
-    up(S.dqs, S.qs.data(), S.qs.size() * sizeof(BatchQ));
-    up(S.ditem_q, iq.data(), iq.size() * 4);
-    up(S.ditem_start, is.data(), is.size() * 8);
-    up(S.ditem_len, il.data(), il.size() * 4);
-    S.dnext.alloc(8, ctx->stream);
-    S.arena.alloc(S.arena_rows * S.plan.row_words * 8, ctx->stream);
-    QEG_CUDA(cudaMemsetAsync(S.arena.get(), 0, S.arena.bytes(), ctx->stream));
-    S.overflow.alloc(nqueries * 4, ctx->stream);
-    QEG_CUDA(cudaMemsetAsync(S.overflow.get(), 0, nqueries * 4, ctx->stream));
-    S.counts.alloc(nqueries * 8, ctx->stream);
-    S.out_vals.resize(S.plan.rtypes.size());
-    S.out_valid.resize(S.plan.rtypes.size());
-    for (size_t c = 0; c < S.plan.rtypes.size(); ++c) {
-      S.out_vals[c].alloc(S.out_rows * 8, ctx->stream);
-      S.out_valid[c].alloc(S.out_rows, ctx->stream);
-    }
-    const size_t sb = static_cast<size_t>(kBatchMaxSlots + 2) * S.plan.row_words * 8;
+    const size_t sb = S.smem_bytes(kBatchMaxSlots);
     require(sb <= ctx->smem_optin, "batch rows are too wide for the shared-memory tables");
     QEG_CUDA(cudaFuncSetAttribute(batch_agg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+    S.rounds.resize(1);
+    S.setup_round(S.rounds[0], all, caps);
     QEG_CUDA(cudaStreamSynchronize(ctx->stream));
-    // ---- capture the run into a CUDA graph ----
+    // ---- capture the first round into a CUDA graph ----
     QEG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    S.enqueue_run();
+    S.enqueue(S.rounds[0]);
     QEG_CUDA(cudaStreamEndCapture(ctx->stream, &S.graph));
     QEG_CUDA(cudaGraphInstantiate(&S.exec, S.graph, 0));
     *out = b.release();
@@ -511,7 +598,7 @@ qeg_status qeg_batch_run(qeg_batch* b) {
     BatchState& S = b->st;
     QEG_CUDA(cudaSetDevice(ctx->device));
     QEG_CUDA(cudaGraphLaunch(S.exec, ctx->stream));
-    ctx->launches += 2;
+    ctx->launches += S.rounds[0].nfin ? 2 : 1;
   });
 }
 
@@ -521,28 +608,48 @@ qeg_status qeg_batch_finish(qeg_batch* b, uint64_t* groups) {
     require(b != nullptr, "batch is NULL");
     BatchState& S = b->st;
     QEG_CUDA(cudaSetDevice(ctx->device));
-    std::vector<uint32_t> ovf(S.nq);
     S.group_counts.assign(S.nq, 0);
-    QEG_CUDA(cudaMemcpyAsync(ovf.data(), S.overflow.get(), S.nq * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    QEG_CUDA(cudaMemcpyAsync(S.group_counts.data(), S.counts.get(), S.nq * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
-    check_device_error(ctx);
-    // Queries whose table overflowed are recomputed exactly (grow-and-replay).
+    S.where_round.assign(S.nq, 0);
+    S.where_local.assign(S.nq, 0);
+    S.fell_back.clear();
     S.fallback.clear();
     S.fallback.resize(S.nq);
-    S.fell_back.clear();
-    for (uint32_t q = 0; q < S.nq; ++q) {
-      if (!ovf[q]) continue;
-      S.fell_back.push_back(q);
+    std::vector<uint32_t> again = S.collect(0);
+    // Overflowed queries (their estimate was far too low) run again, together,
+    // with 8x larger tables, up to the bound of one group per row.
+    uint32_t r = 0;
+    while (!again.empty() && r < 3) {
+      const Round& prev = S.rounds[r];
+      std::vector<uint32_t> qids;
+      std::vector<uint64_t> caps;
+      for (uint32_t l : again) {
+        const uint32_t q = prev.qids[l];
+        qids.push_back(q);
+        const uint64_t bound = static_cast<uint64_t>(static_cast<double>(S.rows_of(q)) / kTargetLoad) + 64;
+        caps.push_back(std::min<uint64_t>(8 * prev.qs[l].cap, bound));
+        S.fell_back.push_back(q);
+      }
+      ++r;
+      if (S.rounds.size() <= r) S.rounds.resize(r + 1);
+      Round& R = S.rounds[r];
+      if (R.qids != qids) S.setup_round(R, qids, caps);
+      S.enqueue(R);
+      ctx->launches += R.nfin ? 2 : 1;
+      again = S.collect(r);
+    }
+    // Still overflowing (not expected: the last tables hold one group per row
+    // at the target load): recompute exactly through the GROUP BY path.
+    for (uint32_t l : again) {
+      const uint32_t q = S.rounds[r].qids[l];
       auto a = std::make_unique<AggState>();
       a->ctx = ctx;
       a->cfg.sizing = QEG_SIZE_FIXED;
-      a->cfg.initial_capacity = 2 * S.qs[q].cap;
+      a->cfg.initial_capacity = 2 * S.rounds[r].qs[l].cap;
       const int32_t types[2] = {S.key.dev.type, S.val.dev.type};
       const uint32_t kc = 0;
       a->plan(types, 2, &kc, 1, S.plan.aggs.data(), static_cast<int>(S.plan.aggs.size()));
       qeg_column cols[2];
-      const uint64_t off = S.offsets[q], n = S.offsets[q + 1] - off;
+      const uint64_t off = S.offsets[q], n = S.rows_of(q);
       const DevCol* dv[2] = {&S.key.dev, &S.val.dev};
       for (int c = 0; c < 2; ++c) {
         const size_t w = type_width(dv[c]->type);
@@ -555,7 +662,8 @@ qeg_status qeg_batch_finish(qeg_batch* b, uint64_t* groups) {
       S.group_counts[q] = g;
       S.fallback[q] = std::move(a);
     }
-    QEG_CUDA(cudaMemsetAsync(S.overflow.get(), 0, S.nq * 4, ctx->stream));
+    std::sort(S.fell_back.begin(), S.fell_back.end());
+    S.fell_back.erase(std::unique(S.fell_back.begin(), S.fell_back.end()), S.fell_back.end());
     if (groups) std::copy(S.group_counts.begin(), S.group_counts.end(), groups);
   });
 }
@@ -572,9 +680,11 @@ qeg_status qeg_batch_fetch(qeg_batch* b, uint32_t query, const qeg_out_column* o
       S.fallback[query]->fetch(0, S.group_counts[query], outs);
       return;
     }
+    Round& R = S.rounds[S.where_round[query]];
+    const BatchQ& Q = R.qs[S.where_local[query]];
     for (size_t c = 0; c < S.plan.rtypes.size(); ++c)
-      fetch_column(ctx, S.out_vals[c].get(), S.out_valid[c].get<uint8_t>(), type_width(S.plan.rtypes[c]),
-                   S.qs[query].out_off, S.group_counts[query], outs[c]);
+      fetch_column(ctx, R.out_vals[c].get(), R.out_valid[c].get<uint8_t>(), type_width(S.plan.rtypes[c]),
+                   Q.out_off, S.group_counts[query], outs[c]);
   });
 }
 
@@ -586,8 +696,8 @@ qeg_status qeg_batch_stats(const qeg_batch* b, uint32_t query, double* est_group
     const BatchState& S = b->st;
     if (est_groups) *est_groups = S.est[query];
     if (hot_share) *hot_share = S.hot[query];
-    if (strategy) *strategy = S.qs[query].smem ? QEG_AGG_SMEM : QEG_AGG_GLOBAL;
-    if (fell_back) *fell_back = std::count(S.fell_back.begin(), S.fell_back.end(), query) ? 1 : 0;
+    if (strategy) *strategy = S.slots[query] > 0 ? QEG_AGG_SMEM : QEG_AGG_GLOBAL;
+    if (fell_back) *fell_back = std::binary_search(S.fell_back.begin(), S.fell_back.end(), query) ? 1 : 0;
   });
 }
 

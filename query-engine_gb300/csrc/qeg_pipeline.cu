@@ -24,6 +24,7 @@
 #include <unordered_map>
 
 #include "qeg_agg.h"
+#include "qeg_warpagg.cuh"
 
 namespace qeg {
 
@@ -89,30 +90,6 @@ __device__ __forceinline__ bool pass_filter(const PipeK& P, uint64_t p) {
   return r;
 }
 
-__device__ __forceinline__ void pipe_apply(unsigned long long* f, const PipeK& P, const bool (&vv)[kPipeMaxVals],
-                                           const uint64_t (&vb)[kPipeMaxVals]) {
-  atomicAdd(f, 1ull);  // rows
-#pragma unroll
-  for (int c = 0; c < kPipeMaxVals; ++c) {
-    if (c >= P.nvals) break;
-    for (int k = 0; k < P.cnf[c]; ++k) {
-      unsigned long long* w = f + P.cfirst[c] + k;
-      const bool v = vv[c];
-      const uint64_t b = vb[c];
-      switch (P.fkind[P.cfirst[c] + k]) {
-        case F_NULLS: if (!v) atomicAdd(w, 1ull); break;
-        case F_SUMI: if (v) atomicAdd(w, static_cast<unsigned long long>(b)); break;
-        case F_SUMF: if (v) atomicAdd(reinterpret_cast<double*>(w), __longlong_as_double(static_cast<long long>(b))); break;
-        case F_MINI: if (v) atomicMax(w, static_cast<unsigned long long>(~enc_i64(static_cast<int64_t>(b)))); break;
-        case F_MAXI: if (v) atomicMax(w, static_cast<unsigned long long>(enc_i64(static_cast<int64_t>(b)))); break;
-        case F_MINF: if (v) atomicMax(w, static_cast<unsigned long long>(~enc_f64_bits(b))); break;
-        case F_MAXF: if (v) atomicMax(w, static_cast<unsigned long long>(enc_f64_bits(b))); break;
-        default: break;
-      }
-    }
-  }
-}
-
 __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
   extern __shared__ unsigned long long sst[];
   const int warps = blockDim.x >> 5;
@@ -121,29 +98,63 @@ __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
   for (int i = threadIdx.x; i < copies * stride_g; i += blockDim.x) sst[i] = 0;
   __syncthreads();
   unsigned long long* mine = sst + (P.per_warp ? (threadIdx.x >> 5) * stride_g : 0);
-  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P.n; p += (uint64_t)gridDim.x * blockDim.x) {
-    if (!pass_filter(P, p)) continue;
-    if (!col_valid(P.key, p)) continue;  // NULL keys never join
-    const uint64_t slot = static_cast<uint64_t>(int_value(P.key, p) - P.key_min);
-    if (slot >= P.key_domain) continue;
-    const uint32_t cnt = __ldg(P.kcount + slot);
-    if (cnt == 0) continue;
+  const unsigned lane = threadIdx.x & 31u;
+  // Warps walk the rows 32 at a time. For every (row, matching build row)
+  // pair, lanes with the same group combine their rows in registers (warp peer
+  // aggregation) and the group's leader applies the result: without atomics
+  // to a warp-private copy, with shared atomics to the block's single copy.
+  for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + (threadIdx.x & ~31u); base < P.n;
+       base += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t p = base + lane;
+    bool ok = p < P.n && pass_filter(P, p) && col_valid(P.key, p);  // NULL keys never join
+    uint32_t cnt = 0, s0 = 0;
+    if (ok) {
+      const uint64_t slot = static_cast<uint64_t>(int_value(P.key, p) - P.key_min);
+      if (slot < P.key_domain) {
+        cnt = __ldg(P.kcount + slot);
+        if (cnt) s0 = __ldg(P.kstart + slot);
+      }
+      ok = cnt > 0;
+    }
     bool vv[kPipeMaxVals];
     uint64_t vb[kPipeMaxVals];
 #pragma unroll
     for (int c = 0; c < kPipeMaxVals; ++c) {
       vv[c] = false;
       vb[c] = 0;
-      if (c < P.nvals) {
+      if (ok && c < P.nvals) {
         vv[c] = col_valid(P.val[c], p);
         if (vv[c]) vb[c] = P.val[c].type == kF64 ? static_cast<uint64_t>(__double_as_longlong(f64_value(P.val[c], p)))
                                                  : static_cast<uint64_t>(int_value(P.val[c], p));
       }
     }
-    const uint32_t s0 = __ldg(P.kstart + slot);
-    for (uint32_t m = 0; m < cnt; ++m) {
-      const uint32_t g = __ldg(P.glist + s0 + m);
-      pipe_apply(mine + g * P.nfields, P, vv, vb);
+    const uint32_t rounds = __reduce_max_sync(0xffffffffu, ok ? cnt : 0u);
+    for (uint32_t m = 0; m < rounds; ++m) {
+      const bool act = ok && m < cnt;
+      const uint32_t g = act ? __ldg(P.glist + s0 + m) : 0xffffffffu;
+      const unsigned amask = __ballot_sync(0xffffffffu, act);
+      const unsigned same = __match_any_sync(0xffffffffu, g);
+      const unsigned peers = act ? (same & amask) : (1u << lane);
+      const bool leader = act && __ffs(peers) - 1 == static_cast<int>(lane);
+      const PeerPlan pp = plan_peers(peers, lane);
+      unsigned long long* f = leader ? mine + static_cast<size_t>(g) * P.nfields : nullptr;
+      if (leader) {
+        if (P.per_warp) f[0] += __popc(peers);
+        else atomicAdd(f, static_cast<unsigned long long>(__popc(peers)));
+      }
+#pragma unroll
+      for (int c = 0; c < kPipeMaxVals; ++c) {
+        if (c >= P.nvals) break;
+        for (int k = 0; k < P.cnf[c]; ++k) {
+          const int fi = P.cfirst[c] + k;
+          const uint8_t kind = P.fkind[fi];
+          const uint64_t x = peer_reduce(field_contrib(kind, vv[c], vb[c]), kind, pp);
+          if (leader) {
+            if (P.per_warp) f[fi] = field_combine(kind, f[fi], x);
+            else field_apply(reinterpret_cast<uint64_t*>(f + fi), kind, x);
+          }
+        }
+      }
     }
   }
   __syncthreads();

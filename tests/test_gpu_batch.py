@@ -110,13 +110,17 @@ def test_batch_empty_and_tiny_queries(ctx):
     check_batch(ctx, offs, k, v)
 
 
-def test_batch_underestimate_falls_back_exactly():
-    # A private context whose estimator predicts zero groups: every table is
-    # sized from the sample's HyperLogLog floor alone, so a query with far more
-    # groups than its sample shows overflows and is recomputed exactly.
+def test_batch_underestimate_reruns_exactly():
+    # A private context whose estimator always answers "far fewer groups than
+    # the classic estimate" (all weights zero, output bias -1, i.e. 2^-32 of
+    # it): tables are sized from the sample's HyperLogLog floor alone, so a
+    # query with far more groups than its sample shows overflows and is re-run
+    # with larger tables; its result must still be exact.
     ctx = qeg.Context(0)
     try:
-        qeg.estimator_set_weights(ctx, np.zeros(qeg.MLP_PARAMS, np.float32))
+        w = np.zeros(qeg.MLP_PARAMS, np.float32)
+        w[qeg.MLP_PARAMS - 2] = -1.0  # b3[0]
+        qeg.estimator_set_weights(ctx, w)
         rng = np.random.default_rng(7)
         n = 1 << 20
         key = O.TCol(O.I32, rng.permutation(n).astype(np.int32))
