@@ -966,9 +966,9 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
     want = std::min<uint64_t>(static_cast<uint64_t>(static_cast<double>(nrows) / kTargetLoad) + 64, 1ull << 20);
   } else {
     est_groups = estimate_groups(staged, nrows, len, dsel);
-    // 15% head-room over the estimate keeps the probe short if it is low; an
+    // Head-room over the estimate keeps the probe short if it is low; an
     // estimate that is far too low is caught by overflow -> grow -> replay.
-    want = static_cast<uint64_t>(std::max(1.15 * est_groups / kTargetLoad, 1024.0));
+    want = static_cast<uint64_t>(std::max(kEstimateHeadroom * est_groups / kTargetLoad, 1024.0));
   }
   alloc_table(want);
   counters.alloc(64, ctx->stream);

@@ -23,6 +23,10 @@ constexpr int kMaxFields = 24;
 constexpr int kMaxAggs = 32;
 // Target occupancy of a global GROUP BY table sized from a group-count estimate.
 constexpr double kTargetLoad = 0.6;
+// Tables sized from an estimate hold this many times the estimated groups at
+// the target load: an underestimate costs a grow-and-replay pass, an
+// overestimate only memory, so the margin leans high.
+constexpr double kEstimateHeadroom = 1.5;
 // Batches smaller than this are sized from their row count, not sketched.
 constexpr uint64_t kSketchMinRows = 1ull << 22;
 

@@ -574,7 +574,7 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
       S.slots[q] = sl;
       S.chunk[q] = std::max<uint64_t>(ch, 256);
       all[q] = q;
-      caps[q] = std::max<uint64_t>(64, static_cast<uint64_t>(1.15 * g / kTargetLoad) + 16);
+      caps[q] = std::max<uint64_t>(64, static_cast<uint64_t>(kEstimateHeadroom * g / kTargetLoad) + 16);
     }
     const size_t sb = S.smem_bytes(kBatchMaxSlots);
     require(sb <= ctx->smem_optin, "batch rows are too wide for the shared-memory tables");

@@ -24,6 +24,7 @@
 // then build columns (ops/join_internal.h:136-179). The COUNT(*)/SUM(payload)
 // sink is fused into one probe kernel.
 #include <algorithm>
+#include <cstdlib>
 
 #include "qeg_agg.h"
 #include "qeg_scan.cuh"
@@ -373,6 +374,116 @@ __global__ void __launch_bounds__(256) probe_sink_kernel(const SinkK P) {
     cnt += m;
     if (m && (!P.vvalid || ((P.vvalid[r >> 6] >> (r & 63)) & 1ull))) {
       sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r])) * m;
+      seen = 1;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    seen |= __shfl_down_sync(0xffffffffu, seen, o);
+  }
+  __shared__ unsigned long long s_acc[3];
+  if (threadIdx.x == 0) s_acc[0] = s_acc[1] = s_acc[2] = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_acc[0], cnt);
+    atomicAdd(&s_acc[1], sum);
+    atomicOr(&s_acc[2], seen);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_acc[0]) atomicAdd(P.acc + 0, s_acc[0]);
+    if (s_acc[1]) atomicAdd(P.acc + 1, s_acc[1]);
+    if (s_acc[2]) atomicOr(P.acc + 2, s_acc[2]);
+  }
+}
+
+// Two consecutive values with one load: 16 bytes for 8-byte types, 8 bytes
+// for 4-byte types (the caller guarantees 16-byte-aligned columns and an even
+// row index).
+template <typename T>
+__device__ __forceinline__ void load2(const T* p, T (&o)[2]) {
+  if (sizeof(T) == 8) {
+    const longlong2 a = __ldcs(reinterpret_cast<const longlong2*>(p));
+    o[0] = static_cast<T>(a.x);
+    o[1] = static_cast<T>(a.y);
+  } else {
+    const int2 a = __ldcs(reinterpret_cast<const int2*>(p));
+    o[0] = static_cast<T>(a.x);
+    o[1] = static_cast<T>(a.y);
+  }
+}
+
+// Software-pipelined sink. A warp owns tiles of U x 64 rows; in a tile, lane i
+// takes rows 2i and 2i+1 of every 64-row chunk, so each warp load instruction
+// reads one contiguous 256- or 512-byte span, and the chunk's validity is one
+// 64-bit word. The loads of the warp's next tile are issued before the
+// lookups of the current one, so the probe stream stays in flight while the
+// table lookups (L2-resident for the dense table) complete.
+template <typename KT, typename VT, int STRAT, bool UNIQUE, int U>
+__global__ void __launch_bounds__(256, 4) probe_sink_pipe_kernel(const SinkK P) {
+  unsigned long long cnt = 0, sum = 0, seen = 0;
+  const KT* keys = static_cast<const KT*>(P.key);
+  const VT* vals = static_cast<const VT*>(P.val);
+  const unsigned lane = threadIdx.x & 31u;
+  constexpr uint64_t kTile = 64ull * U;
+  const uint64_t ntiles = P.n / kTile;
+  const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  uint64_t t = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  KT k[U][2];
+  VT v[U][2];
+  uint64_t kw[U], vw[U];
+  auto load_tile = [&](uint64_t tile) {
+    const uint64_t base = tile * kTile;
+#pragma unroll
+    for (int c = 0; c < U; ++c) {
+      const uint64_t r = base + c * 64 + 2 * lane;
+      load2(keys + r, k[c]);
+      load2(vals + r, v[c]);
+      kw[c] = P.kvalid ? __ldg(P.kvalid + (base >> 6) + c) : ~0ull;
+      vw[c] = P.vvalid ? __ldg(P.vvalid + (base >> 6) + c) : ~0ull;
+    }
+  };
+  if (t < ntiles) load_tile(t);
+  for (; t < ntiles; t += nwarps) {
+    KT ck[U][2];
+    VT cv[U][2];
+    uint32_t kb[U], vb[U];
+#pragma unroll
+    for (int c = 0; c < U; ++c) {
+      ck[c][0] = k[c][0];
+      ck[c][1] = k[c][1];
+      cv[c][0] = v[c][0];
+      cv[c][1] = v[c][1];
+      kb[c] = static_cast<uint32_t>(kw[c] >> (2 * lane)) & 3u;
+      vb[c] = static_cast<uint32_t>(vw[c] >> (2 * lane)) & 3u;
+    }
+    if (t + nwarps < ntiles) load_tile(t + nwarps);
+    uint64_t m[U][2];
+#pragma unroll
+    for (int c = 0; c < U; ++c)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) m[c][j] = ((kb[c] >> j) & 1u) ? sink_lookup<KT, STRAT, UNIQUE>(P.T, ck[c][j]) : 0;
+#pragma unroll
+    for (int c = 0; c < U; ++c)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        cnt += m[c][j];
+        if (m[c][j] && ((vb[c] >> j) & 1u)) {
+          sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j])) * m[c][j];
+          seen = 1;
+        }
+      }
+  }
+  // Rows after the last full tile, one per thread.
+  const uint64_t tail0 = ntiles * kTile;
+  for (uint64_t r = tail0 + static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < P.n;
+       r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const bool kv = !P.kvalid || ((P.kvalid[r >> 6] >> (r & 63)) & 1ull);
+    const uint64_t mm = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, keys[r]) : 0;
+    cnt += mm;
+    if (mm && (!P.vvalid || ((P.vvalid[r >> 6] >> (r & 63)) & 1ull))) {
+      sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r])) * mm;
       seen = 1;
     }
   }
@@ -1209,6 +1320,10 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       // 1.38 ms for 256M dense-table probes; 5.9 against 10.4 ms hashed).
       auto al16 = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };
       const char* tma_env = getenv("QEG_SINK_TMA");
+      // Register-pipelined variants (tiles of 2 or 4 64-row chunks per warp):
+      // QEG_SINK_PIPE=2|4 selects one, for measurement.
+      const char* pipe_env = getenv("QEG_SINK_PIPE");
+      const int pipe = pipe_env ? atoi(pipe_env) : 0;
       const bool use_tma = n >= static_cast<uint64_t>(kTileRows) * ctx->sms * 2 && al16(S.kvalid) && al16(S.vvalid) &&
                            tma_env != nullptr && tma_env[0] == '1';
       auto launch_tma = [&](void (*kern)(SinkK, uint32_t*), size_t tile_bytes) {
@@ -1224,6 +1339,16 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       else if (dense) launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_DENSE, false>, tb);                       \
       else if (st.unique) launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_HASH, true>, tb);                     \
       else launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_HASH, false>, tb);                                   \
+    } else if (pipe == 2) {                                                                                        \
+      if (dense && st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, true, 2>);                    \
+      else if (dense) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, false, 2>);                           \
+      else if (st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_HASH, true, 2>);                         \
+      else launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_HASH, false, 2>);                                       \
+    } else if (pipe == 4) {                                                                                        \
+      if (dense && st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, true, 4>);                    \
+      else if (dense) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, false, 4>);                           \
+      else if (st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_HASH, true, 4>);                         \
+      else launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_HASH, false, 4>);                                       \
     } else if (dense && st.unique) launch(probe_sink_kernel<KT, VT, QEG_JOIN_DENSE, true>);                       \
     else if (dense) launch(probe_sink_kernel<KT, VT, QEG_JOIN_DENSE, false>);                                    \
     else if (st.unique) launch(probe_sink_kernel<KT, VT, QEG_JOIN_HASH, true>);                                  \

@@ -42,58 +42,69 @@ __device__ __forceinline__ PeerPlan plan_peers(unsigned peers, unsigned lane) {
   return pp;
 }
 
+// How a field merges: integer add (row / NULL counts, integer sums), F64 add
+// (F64 sums) or unsigned max (every MIN/MAX encoding). The kind of a field is
+// the same in every lane, so the branches below never diverge, and they are
+// plain compares rather than jump tables.
+enum FieldOp : int { kOpAdd = 0, kOpFAdd = 1, kOpMax = 2 };
+
+__device__ __forceinline__ int field_op(uint8_t kind) {
+  return kind <= F_SUMI ? kOpAdd : (kind == F_SUMF ? kOpFAdd : kOpMax);
+}
+
 // The contribution of one (valid, value bits) input to a field, in the
 // field's identity-is-zero encoding.
 __device__ __forceinline__ uint64_t field_contrib(uint8_t kind, bool valid, uint64_t bits) {
-  switch (kind) {
-    case F_ROWS: return 1;
-    case F_NULLS: return valid ? 0 : 1;
-    case F_SUMI:
-    case F_SUMF: return valid ? bits : 0;
-    case F_MINI: return valid ? ~enc_i64(static_cast<int64_t>(bits)) : 0;
-    case F_MAXI: return valid ? enc_i64(static_cast<int64_t>(bits)) : 0;
-    case F_MINF: return valid ? ~enc_f64_bits(bits) : 0;
-    case F_MAXF: return valid ? enc_f64_bits(bits) : 0;
-    default: return 0;
-  }
+  if (kind == F_ROWS) return 1;
+  if (kind == F_NULLS) return valid ? 0 : 1;
+  if (!valid) return 0;
+  if (kind <= F_SUMF) return bits;
+  const uint64_t e = (kind <= F_MAXI) ? enc_i64(static_cast<int64_t>(bits)) : enc_f64_bits(bits);
+  return (kind & 1) ? e : ~e;  // MAXI / MAXF are odd, MINI / MINF even
+}
+
+template <int OP>
+__device__ __forceinline__ uint64_t op_combine(uint64_t a, uint64_t b) {
+  if (OP == kOpAdd) return a + b;
+  if (OP == kOpFAdd)
+    return static_cast<uint64_t>(__double_as_longlong(__longlong_as_double(static_cast<long long>(a)) +
+                                                      __longlong_as_double(static_cast<long long>(b))));
+  return a > b ? a : b;
 }
 
 __device__ __forceinline__ uint64_t field_combine(uint8_t kind, uint64_t a, uint64_t b) {
-  switch (kind) {
-    case F_ROWS:
-    case F_NULLS:
-    case F_SUMI: return a + b;
-    case F_SUMF:
-      return static_cast<uint64_t>(__double_as_longlong(__longlong_as_double(static_cast<long long>(a)) +
-                                                        __longlong_as_double(static_cast<long long>(b))));
-    default: return a > b ? a : b;
-  }
+  const int op = field_op(kind);
+  if (op == kOpAdd) return op_combine<kOpAdd>(a, b);
+  if (op == kOpFAdd) return op_combine<kOpFAdd>(a, b);
+  return op_combine<kOpMax>(a, b);
 }
 
 // Merges one combined contribution into a table word (shared or global).
 __device__ __forceinline__ void field_apply(uint64_t* w, uint8_t kind, uint64_t x) {
+  if (!x) return;  // zero is the identity of every field
+  const int op = field_op(kind);
   unsigned long long* u = reinterpret_cast<unsigned long long*>(w);
-  switch (kind) {
-    case F_ROWS:
-    case F_NULLS:
-    case F_SUMI:
-      if (x) atomicAdd(u, static_cast<unsigned long long>(x));
-      break;
-    case F_SUMF:
-      if (x) atomicAdd(reinterpret_cast<double*>(w), __longlong_as_double(static_cast<long long>(x)));
-      break;
-    default:
-      if (x) atomicMax(u, static_cast<unsigned long long>(x));
-      break;
+  if (op == kOpAdd) atomicAdd(u, static_cast<unsigned long long>(x));
+  else if (op == kOpFAdd) atomicAdd(reinterpret_cast<double*>(w), __longlong_as_double(static_cast<long long>(x)));
+  else atomicMax(u, static_cast<unsigned long long>(x));
+}
+
+template <int OP>
+__device__ __forceinline__ uint64_t peer_reduce_op(uint64_t x, const PeerPlan& pp) {
+#pragma unroll 1
+  for (int r = 0; r < pp.rounds; ++r) {
+    const uint64_t t = __shfl_sync(0xffffffffu, x, (pp.src >> (5 * r)) & 31u);
+    if ((pp.take >> r) & 1u) x = op_combine<OP>(x, t);
   }
+  return x;
 }
 
 __device__ __forceinline__ uint64_t peer_reduce(uint64_t x, uint8_t kind, const PeerPlan& pp) {
-  for (int r = 0; r < pp.rounds; ++r) {
-    const uint64_t t = __shfl_sync(0xffffffffu, x, (pp.src >> (5 * r)) & 31u);
-    if ((pp.take >> r) & 1u) x = field_combine(kind, x, t);
-  }
-  return x;
+  if (pp.rounds == 0) return x;
+  const int op = field_op(kind);
+  if (op == kOpAdd) return peer_reduce_op<kOpAdd>(x, pp);
+  if (op == kOpFAdd) return peer_reduce_op<kOpFAdd>(x, pp);
+  return peer_reduce_op<kOpMax>(x, pp);
 }
 
 }  // namespace qeg

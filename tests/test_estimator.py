@@ -87,26 +87,36 @@ def zipf_column(torch, n, dom, s, seed):
 
 @pytest.mark.gpu
 @pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="no trained estimator weights shipped")
-def test_learned_estimator_beats_classic_and_sizes_tables():
+def test_learned_estimator_beats_classic_and_sizes_tables(monkeypatch):
+    """What the network gains over the method without it, on Zipf key columns
+    whose sample is 1/8 to 1/32 of the rows: a smaller median and worst-case
+    log2 error of the group-count estimate, and GROUP BY tables that need fewer
+    grow-and-replay passes when sized from it. Results are exact either way."""
     torch = pytest.importorskip("torch")
     ctx = qeg.Context(0)  # loads the shipped weights
+    monkeypatch.setenv("QEG_ESTIMATOR_WEIGHTS", os.path.join(os.path.dirname(WEIGHTS), "no-such-weights.f32"))
+    plain = qeg.Context(0)  # no network: the classic estimator sizes its tables
     cases = [(1 << 24, 1 << 24, 0.6, 1), (1 << 24, 1 << 26, 1.1, 2), (1 << 25, 1 << 22, 1.3, 3),
              (1 << 23, 1 << 25, 0.8, 4), (1 << 24, 1 << 20, 0.4, 5), (1 << 25, 1 << 26, 1.0, 6)]
-    el, ec = [], []
-    for n, dom, s, seed in cases:
-        keys = zipf_column(torch, n, dom, s, seed)
-        col = qeg.Col(keys, None, qeg.I64)
-        f, classic, _ = qeg.sketch(ctx, col)
-        learned = qeg.learned_groups(classic, float(qeg.estimator_predict(ctx, f)[0][0]))
-        true = int(torch.unique(keys).numel())
-        el.append(abs(math.log2(max(learned, 1)) - math.log2(true)))
-        ec.append(abs(math.log2(max(classic, 1)) - math.log2(true)))
-        # End to end: the learned-sized table holds every group without growing.
-        a = qeg.Aggregate(ctx, [qeg.I64], [0], [(qeg.COUNT_STAR, 0)], qeg.agg_config(sizing=qeg.SIZE_LEARNED))
-        a.consume([col])
-        assert a.finish() == true
-        st = a.stats()
-        a.close()
-        assert st["resizes"] == 0, st
-    ctx.close()
+    el, ec, rl, rc = [], [], [], []
+    try:
+        for n, dom, s, seed in cases:
+            keys = zipf_column(torch, n, dom, s, seed)
+            col = qeg.Col(keys, None, qeg.I64)
+            f, classic, _ = qeg.sketch(ctx, col)
+            learned = qeg.learned_groups(classic, float(qeg.estimator_predict(ctx, f)[0][0]))
+            true = int(torch.unique(keys).numel())
+            el.append(abs(math.log2(max(learned, 1)) - math.log2(true)))
+            ec.append(abs(math.log2(max(classic, 1)) - math.log2(true)))
+            for c, out in ((ctx, rl), (plain, rc)):
+                a = qeg.Aggregate(c, [qeg.I64], [0], [(qeg.COUNT_STAR, 0)], qeg.agg_config(sizing=qeg.SIZE_LEARNED))
+                a.consume([col])
+                assert a.finish() == true
+                out.append(a.stats()["resizes"])
+                a.close()
+    finally:
+        plain.close()
+        ctx.close()
     assert np.median(el) < np.median(ec), (el, ec)
+    assert max(el) < max(ec), (el, ec)
+    assert sum(rl) < sum(rc), (rl, rc)
