@@ -297,6 +297,9 @@ typedef struct qeg_batch_tuning {
   int32_t skewed;         /* 1: bucket of queries whose top keys carry >= 30% of rows */
   int32_t smem_slots;     /* CTA-private table slots (power of two <= 4096); 0 = global table only */
   uint64_t rows_per_item; /* rows per work item of the persistent kernel */
+  int32_t peer_rows;      /* 1: a warp combines its rows of one group before applying them; 0: every
+                             row is applied with atomics; -1: decided from the estimate */
+  int32_t reserved;
 } qeg_batch_tuning;
 qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row_offsets, const qeg_column* key,
                             const qeg_column* val, const qeg_agg_spec* aggs, int naggs,

@@ -2,12 +2,13 @@
 
 For every (group-count, skew) bucket of the batch planner it generates a
 seeded synthetic batch of queries of that bucket, runs the batch under every
-candidate (CTA-private table slots x rows per work item), times the graph
-replays with CUDA events and keeps the fastest; then it picks the block size
-on a mixed batch. The result is the tuning table qeg_batch_create takes,
-written as JSON beside libqeg.so (batch_tuning.json):
+candidate (CTA-private table slots x rows per work item x warp peer
+aggregation on/off), times the graph replays with CUDA events and keeps the
+fastest; then it picks the block size on a mixed batch. The result is the
+tuning table qeg_batch_create takes, written as JSON beside libqeg.so
+(batch_tuning.json):
 
-    {"tuning": [[max_log2_groups, skewed, smem_slots, rows_per_item], ...],
+    {"tuning": [[max_log2_groups, skewed, smem_slots, rows_per_item, peer_rows], ...],
      "block_threads": B, "measured": {...}}
 
     python query-engine_gb300/autotune.py [--out PATH] [--queries N]
@@ -28,7 +29,8 @@ import qeg  # noqa: E402
 
 BUCKETS = [2.0, 6.0, 10.0, 14.0, 17.0, 20.0]  # upper bounds on log2(groups)
 SLOTS = [0, 256, 1024, 4096]
-ITEMS = [1 << 14, 1 << 16, 1 << 18]
+ITEMS = [1 << 13, 1 << 14, 1 << 16]
+PEER = [0, 1]
 BLOCKS = [256, 512, 1024]
 AGGS = [(qeg.COUNT_STAR, 0), (qeg.SUM, 1), (qeg.AVG, 1), (qeg.MIN, 1), (qeg.MAX, 1)]
 
@@ -97,16 +99,17 @@ def main():
             res = {}
             for slots in SLOTS:
                 for item in ITEMS:
-                    # Every bucket maps to this candidate: the batch holds one bucket.
-                    tun = [(64.0, 0, slots, item), (64.0, 1, slots, item)]
-                    res[(slots, item)] = time_batch(ctx, offs, key, val, tun, 512)
+                    for peer in PEER:
+                        # Every bucket maps to this candidate: the batch holds one bucket.
+                        tun = [(64.0, 0, slots, item, peer), (64.0, 1, slots, item, peer)]
+                        res[(slots, item, peer)] = time_batch(ctx, offs, key, val, tun, 512)
             best = min(res, key=res.get)
-            table.append([hi, skewed, best[0], best[1]])
+            table.append([hi, skewed, best[0], best[1], best[2]])
             measured["log2<=%g,skewed=%d" % (hi, skewed)] = {
                 "rows": int(offs[-1]), "best": list(best), "best_ms": res[best],
-                "all_ms": {"%d/%d" % k: v for k, v in res.items()}}
-            print("bucket log2<=%g skewed=%d: slots=%d rows/item=%d %.3f ms" % (hi, skewed, best[0], best[1],
-                                                                               res[best]), flush=True)
+                "all_ms": {"%d/%d/%d" % k: v for k, v in res.items()}}
+            print("bucket log2<=%g skewed=%d: slots=%d rows/item=%d peer=%d %.3f ms" % (hi, skewed, best[0], best[1],
+                                                                                       best[2], res[best]), flush=True)
             del key, val
         lo = hi
     # Block size on a mixed batch, with the tuned table.

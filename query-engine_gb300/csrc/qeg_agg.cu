@@ -239,10 +239,61 @@ __device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, bool priv, 
 // Warps walk the rows 32 at a time (blockDim.x is a multiple of 32), so every
 // lane reaches the warp-wide intrinsics.
 // ---------------------------------------------------------------------------
-template <int MODE, int NV>
+// The CTA-private table row of a single key (side rows for key word 0 and the
+// NULL key), or -1: the key is not there (read-only table) or did not fit
+// within smem_probe slots.
+__device__ __forceinline__ int smem_row(uint64_t* sm, int S, int W, const AggK& P, bool kv, uint64_t k, uint64_t h) {
+  if (!kv) return S + 1;
+  if (k == 0) return S;
+  uint64_t s = h & (S - 1);
+  for (int t = 0; t < P.smem_probe; ++t) {
+    const uint64_t cur = ld_volatile_shared(&sm[s * W]);
+    if (cur == k) return static_cast<int>(s);
+    if (cur == 0) {
+      if (!P.smem_insert) return -1;
+      const unsigned long long old =
+          atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * W]), 0ull, static_cast<unsigned long long>(k));
+      if (old == 0 || old == k) return static_cast<int>(s);
+    }
+    s = (s + 1) & (S - 1);
+  }
+  return -1;
+}
+
+// Table-full signal (all lanes of the warp call it): inserts are counted per
+// warp and published every 64; once the count passes P.full_at, lookups of new
+// keys give up after a short probe and spill instead of walking probe_limit
+// slots of a full table.
+__device__ __forceinline__ void track_full(const AggK& P, unsigned lane, uint32_t iter, bool inserted_now,
+                                           unsigned& pending, bool& full) {
+  pending += __popc(__ballot_sync(0xffffffffu, inserted_now));
+  if (pending >= 64 || (iter & 15) == 15) {
+    if (lane == 0) {
+      if (pending) {
+        const unsigned long long before = atomicAdd(P.counters + 3, static_cast<unsigned long long>(pending));
+        if (before + pending >= P.full_at) atomicExch(P.full_flag, 1u);
+      }
+      full = full || ld_relaxed_u32(P.full_flag) != 0;
+    }
+    pending = 0;
+    full = __shfl_sync(0xffffffffu, full, 0);
+  }
+}
+
+// PEER (single key): combine the rows of a warp that share a group before
+// applying them (warp peer aggregation, warp-private rows for the hottest
+// keys). Without it every lane applies its own row with atomics, which is
+// cheaper unless many lanes of a warp hit the same few groups: measured on
+// GB300 over 64M rows, per-lane atomics run 1.3-1.5x faster for a 1024-group
+// column and for a Zipf(1.1) column with preloaded heavy hitters, while the
+// peer path runs 2x faster when a skewed column has no private table.
+template <int MODE, int NV, bool PEER>
 __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   extern __shared__ uint64_t sm[];
   const int W = P.row_words;
+  // Shared-memory rows use an odd stride in 8-byte words, so the same field of
+  // different rows falls in different banks.
+  const int SW = W | 1;
   const int S = (MODE == 0) ? 1 : P.smem_slots;  // power of two, or 0 = off
   const int srows = (MODE == 0) ? 1 : (S > 0 ? S + 2 : 0);
   const int fo = (MODE == 2) ? 2 + P.nkeys : 1;  // field offset within a global row
@@ -252,13 +303,13 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   // Warp-private rows after the table: MODE 0 one per warp; MODE 1 (preloaded
   // table) one per warp for each of the WH hottest keys, with a rank byte per
   // table slot (0 = not one of them) and the table slot of every rank.
-  const int WH = (MODE == 0) ? 1 : ((MODE == 1 && S > 0 && P.nhot > 0) ? P.warp_hot : 0);
-  uint64_t* wrows = sm + srows * W;
-  uint8_t* srank = reinterpret_cast<uint8_t*>(wrows + nwarps * WH * W);
+  const int WH = (MODE == 0) ? 1 : ((MODE == 1 && PEER && S > 0 && P.nhot > 0) ? P.warp_hot : 0);
+  uint64_t* wrows = sm + srows * SW;
+  uint8_t* srank = reinterpret_cast<uint8_t*>(wrows + nwarps * WH * SW);
   uint16_t* hslot = reinterpret_cast<uint16_t*>(srank + ((srows + 7) & ~7));
   const bool ranked = MODE == 1 && WH > 0;
 
-  for (int i = threadIdx.x; i < (srows + nwarps * WH) * W; i += blockDim.x) sm[i] = 0;
+  for (int i = threadIdx.x; i < (srows + nwarps * WH) * SW; i += blockDim.x) sm[i] = 0;
   if (ranked)
     for (int i = threadIdx.x; i < srows; i += blockDim.x) srank[i] = 0;
   __syncthreads();
@@ -269,7 +320,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       uint64_t s = key_hash1(k) & (S - 1);
       for (int t = 0; t < S; ++t) {
         const unsigned long long old =
-            atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * W]), 0ull, static_cast<unsigned long long>(k));
+            atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * SW]), 0ull, static_cast<unsigned long long>(k));
         if (old == 0 || old == k) {
           if (old == 0 && i < WH) {
             srank[s] = static_cast<uint8_t>(i + 1);
@@ -284,10 +335,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   }
 
   unsigned long long inserted = 0;
-  // Table-full signal: inserts are counted per warp and published every 64;
-  // once the count passes P.full_at, lookups of new keys give up after a short
-  // probe and spill, instead of walking probe_limit slots of a full table.
-  unsigned pending = 0;
+  unsigned pending = 0;  // table-full signal state (track_full)
   bool full = MODE == 1 && P.full_flag && ld_relaxed_u32(P.full_flag) != 0;
   uint32_t iter = 0;
   const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
@@ -316,8 +364,29 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
     if (MODE == 0) {
       const unsigned peers = live ? livemask : (1u << lane);
       const PeerPlan pp = plan_peers(peers, lane);
-      warp_apply<NV>(&wrows[warp * W + 1], live && __ffs(peers) - 1 == static_cast<int>(lane), true, peers, pp, P, vv,
+      warp_apply<NV>(&wrows[warp * SW + 1], live && __ffs(peers) - 1 == static_cast<int>(lane), true, peers, pp, P, vv,
                  vb);
+      continue;
+    }
+    if (MODE == 1 && !PEER) {
+      const unsigned long long ins0 = inserted;
+      if (live) {
+        const DevCol& kc = P.key[0];
+        const bool kv = col_valid(kc, p);
+        const uint64_t k = kv ? key_word(kc, p) : 0;
+        const uint64_t h = key_hash1(k);
+        uint64_t* f = nullptr;
+        const int srow = S > 0 ? smem_row(sm, S, SW, P, kv, k, h) : -1;
+        if (srow >= 0) {
+          f = &sm[srow * SW + 1];
+        } else {
+          uint64_t* r = global_row1(P, kv, k, h, inserted, full ? kFullProbe : P.probe_limit);
+          if (r) f = r + 1;
+        }
+        if (f) apply_row<NV>(f, P, vv, vb);
+        else spill_row(P, p);
+      }
+      if (P.full_flag) track_full(P, lane, iter, inserted != ins0, pending, full);
       continue;
     }
     if (MODE == 1) {
@@ -335,40 +404,14 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       const unsigned long long ins0 = inserted;
       if (leader) {
         const uint64_t h = key_hash1(k);
-        int srow = -1;
-        if (S > 0) {
-          if (!kv) {
-            srow = S + 1;
-          } else if (k == 0) {
-            srow = S;
-          } else {
-            uint64_t s = h & (S - 1);
-            for (int t = 0; t < P.smem_probe; ++t) {
-              const uint64_t cur = ld_volatile_shared(&sm[s * W]);
-              if (cur == k) {
-                srow = static_cast<int>(s);
-                break;
-              }
-              if (cur == 0) {
-                if (!P.smem_insert) break;
-                const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * W]), 0ull,
-                                                         static_cast<unsigned long long>(k));
-                if (old == 0 || old == k) {
-                  srow = static_cast<int>(s);
-                  break;
-                }
-              }
-              s = (s + 1) & (S - 1);
-            }
-          }
-        }
+        const int srow = S > 0 ? smem_row(sm, S, SW, P, kv, k, h) : -1;
         if (srow >= 0) {
           const int rk = (ranked && srow < S) ? srank[srow] : 0;
           if (rk) {
-            f = &wrows[(warp * WH + rk - 1) * W + 1];
+            f = &wrows[(warp * WH + rk - 1) * SW + 1];
             priv = true;
           } else {
-            f = &sm[srow * W + 1];
+            f = &sm[srow * SW + 1];
           }
         } else {
           uint64_t* r = global_row1(P, kv, k, h, inserted, full ? kFullProbe : P.probe_limit);
@@ -384,20 +427,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       }
       const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
       warp_apply<NV>(f, leader && ok, priv, peers, pp, P, vv, vb);
-      if (P.full_flag) {
-        pending += __popc(__ballot_sync(0xffffffffu, inserted != ins0));
-        if (pending >= 64 || (iter & 15) == 15) {
-          if (lane == 0) {
-            if (pending) {
-              const unsigned long long before = atomicAdd(P.counters + 3, static_cast<unsigned long long>(pending));
-              if (before + pending >= P.full_at) atomicExch(P.full_flag, 1u);
-            }
-            full = full || ld_relaxed_u32(P.full_flag) != 0;
-          }
-          pending = 0;
-          full = __shfl_sync(0xffffffffu, full, 0);
-        }
-      }
+      if (P.full_flag) track_full(P, lane, iter, inserted != ins0, pending, full);
       continue;
     }
     // MODE 2: composite key, global table only, one lane per row.
@@ -424,17 +454,17 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   if (WH > 0) {
     __syncthreads();
     for (int i = threadIdx.x; i < nwarps * WH; i += blockDim.x) {
-      const uint64_t* src = &wrows[i * W];
+      const uint64_t* src = &wrows[i * SW];
       if (src[1] == 0) continue;
       const int slot = (MODE == 0) ? 0 : hslot[i % WH];
-      merge_fields(&sm[slot * W + 1], src + 1, P);
+      merge_fields(&sm[slot * SW + 1], src + 1, P);
     }
   }
   // Flush the CTA-private table into the global table.
   if (MODE != 2 && srows > 0) {
     __syncthreads();
     for (int sr = threadIdx.x; sr < srows; sr += blockDim.x) {
-      const uint64_t* src = &sm[sr * W];
+      const uint64_t* src = &sm[sr * SW];
       if (src[1] == 0) continue;  // no row landed here
       uint64_t* dst;
       if (MODE == 0) {
@@ -782,10 +812,18 @@ void AggState::set_field_columns(AggK& P) const {
 
 int AggState::block_threads() const { return cfg.block_threads > 0 ? cfg.block_threads : 512; }
 
+bool AggState::peer_rows() const {
+  // Few groups (many lanes of a warp on the same group) or a skewed column
+  // aggregated in the global table alone.
+  if (mode != 1) return mode == 0;
+  if (est_groups > 0 && est_groups <= 512) return true;
+  return smem_slots == 0 && hot_share >= 0.3;
+}
+
 int AggState::warp_hot() const {
-  if (mode != 1 || nhot <= 0 || smem_slots <= 0) return 0;
+  if (mode != 1 || !peer_rows() || nhot <= 0 || smem_slots <= 0) return 0;
   // Up to 32 keys, within 32 KB of warp-private rows.
-  const int fit = 32768 / ((block_threads() / 32) * row_words * 8);
+  const int fit = 32768 / ((block_threads() / 32) * (row_words | 1) * 8);
   return std::max(0, std::min({32, nhot, fit}));
 }
 
@@ -799,7 +837,7 @@ void AggState::alloc_table(uint64_t new_cap) {
 size_t AggState::smem_bytes(int block) const {
   const int srows = mode == 0 ? 1 : (smem_slots > 0 ? smem_slots + 2 : 0);
   const int wh = mode == 0 ? 1 : warp_hot();
-  size_t b = (static_cast<size_t>(srows) + static_cast<size_t>(block / 32) * wh) * row_words * 8;
+  size_t b = (static_cast<size_t>(srows) + static_cast<size_t>(block / 32) * wh) * (row_words | 1) * 8;
   if (mode == 1 && wh > 0) b += ((srows + 7) & ~7) + 2 * wh;  // slot ranks + rank slots
   return b;
 }
@@ -813,14 +851,15 @@ void AggState::launch(const AggK& P, uint64_t nrows) {
   // 2, 4 or 8 (loops over value columns are unrolled to that count).
   void (*kern)(AggK) = nullptr;
   const int nv = static_cast<int>(val_cols.size());
-#define QEG_AGG_VARIANT(M)                          \
-  (nv <= 1   ? agg_kernel<M, 1>                     \
-   : nv <= 2 ? agg_kernel<M, 2>                     \
-   : nv <= 4 ? agg_kernel<M, 4>                     \
-             : agg_kernel<M, 8>)
-  if (mode == 0) kern = QEG_AGG_VARIANT(0);
-  else if (mode == 1) kern = QEG_AGG_VARIANT(1);
-  else kern = QEG_AGG_VARIANT(2);
+#define QEG_AGG_VARIANT(M, PEER)                          \
+  (nv <= 1   ? agg_kernel<M, 1, PEER>                     \
+   : nv <= 2 ? agg_kernel<M, 2, PEER>                     \
+   : nv <= 4 ? agg_kernel<M, 4, PEER>                     \
+             : agg_kernel<M, 8, PEER>)
+  if (mode == 0) kern = QEG_AGG_VARIANT(0, true);
+  else if (mode == 1 && peer_rows()) kern = QEG_AGG_VARIANT(1, true);
+  else if (mode == 1) kern = QEG_AGG_VARIANT(1, false);
+  else kern = QEG_AGG_VARIANT(2, false);
 #undef QEG_AGG_VARIANT
   int per_sm = 1;
   if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
@@ -984,7 +1023,7 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   if (mode == 0) strategy = QEG_AGG_SMEM;
   // Leave room for the warp-private rows (<= 32 KB) and the slot ranks.
   const int max_slots =
-      static_cast<int>(std::min<size_t>(8192, ((ctx->smem_optin - 32768) / (row_words * 8 + 1)) - 2));
+      static_cast<int>(std::min<size_t>(8192, ((ctx->smem_optin - 32768) / ((row_words | 1) * 8 + 1)) - 2));
   int slots = 1;
   while (slots * 2 <= max_slots) slots *= 2;
   if (strategy == QEG_AGG_AUTO) {

@@ -37,6 +37,8 @@ struct BatchQ {
   uint64_t out_off;    // first output row
   int32_t smem;        // 1: CTA-private shared-memory table first
   int32_t smem_slots;  // power of two <= kBatchMaxSlots
+  int32_t peer;        // 1: lanes of a warp combine rows of one group first
+  int32_t pad;
 };
 
 struct BatchK {
@@ -75,6 +77,7 @@ __device__ __forceinline__ uint64_t* batch_global_row(const BatchK& P, const Bat
 
 __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
   extern __shared__ uint64_t sm[];
+  const int SW = P.W | 1;  // odd row stride in shared memory: fewer bank conflicts
   __shared__ uint32_t s_item;
   for (;;) {
     if (threadIdx.x == 0) s_item = atomicAdd(P.next, 1u);
@@ -85,15 +88,16 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
     const BatchQ Q = P.qs[q];
     const int S = Q.smem ? Q.smem_slots : 0;
     if (S) {
-      for (int i = threadIdx.x; i < (S + 2) * P.W; i += blockDim.x) sm[i] = 0;
+      for (int i = threadIdx.x; i < (S + 2) * SW; i += blockDim.x) sm[i] = 0;
       __syncthreads();
     }
     const uint64_t start = P.item_start[item];
     const uint32_t len = P.item_len[item];
     bool ovf = false;
     const unsigned lane = threadIdx.x & 31u;
-    // Warps walk the item 32 rows at a time; lanes of one group combine their
-    // rows first (warp peer aggregation) and the group's leader applies them.
+    // Warps walk the item 32 rows at a time. With Q.peer, lanes of one group
+    // combine their rows first (warp peer aggregation) and the group's leader
+    // applies them; otherwise every lane applies its own row.
     for (uint32_t wb = threadIdx.x & ~31u; wb < len; wb += blockDim.x) {
       const uint32_t i = wb + lane;
       const bool live = i < len;
@@ -104,10 +108,13 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
       const uint64_t b = !v ? 0
                          : (P.val.type == kF64 ? static_cast<uint64_t>(__double_as_longlong(f64_value(P.val, p)))
                                                : static_cast<uint64_t>(int_value(P.val, p)));
-      const unsigned livemask = __ballot_sync(0xffffffffu, live);
-      const unsigned same = __match_any_sync(0xffffffffu, k);
-      const unsigned vmask = __ballot_sync(0xffffffffu, kv);
-      const unsigned peers = live ? (same & livemask & (kv ? vmask : ~vmask)) : (1u << lane);
+      unsigned peers = 1u << lane;
+      if (Q.peer) {
+        const unsigned livemask = __ballot_sync(0xffffffffu, live);
+        const unsigned same = __match_any_sync(0xffffffffu, k);
+        const unsigned vmask = __ballot_sync(0xffffffffu, kv);
+        if (live) peers = same & livemask & (kv ? vmask : ~vmask);
+      }
       const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
       uint64_t* f = nullptr;
       if (leader) {
@@ -120,9 +127,9 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
           } else {
             uint64_t s = hash_fold(kHashSeed, k) & (S - 1);
             for (int t = 0; t < 8; ++t) {
-              unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(&sm[s * P.W]);
+              unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(&sm[s * SW]);
               if (cur == 0)
-                cur = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * P.W]), 0ull,
+                cur = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * SW]), 0ull,
                                 static_cast<unsigned long long>(k));
               if (cur == 0 || cur == k) {
                 srow = static_cast<int>(s);
@@ -133,7 +140,7 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
           }
         }
         if (srow >= 0) {
-          f = &sm[srow * P.W + 1];
+          f = &sm[srow * SW + 1];
         } else {
           uint64_t* r = batch_global_row(P, Q, kv, k);
           if (r) f = r + 1;
@@ -153,7 +160,7 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
     if (S) {
       __syncthreads();
       for (int sr = threadIdx.x; sr < S + 2; sr += blockDim.x) {
-        const uint64_t* src = &sm[sr * P.W];
+        const uint64_t* src = &sm[sr * SW];
         if (src[1] == 0) continue;
         uint64_t* dst;
         if (sr == S + 1) dst = batch_global_row(P, Q, false, 0);
@@ -305,6 +312,7 @@ struct BatchState {
   std::vector<float> hot;
   std::vector<int32_t> slots;   // per query: CTA-private table slots (0 = global table only)
   std::vector<uint64_t> chunk;  // per query: rows per work item
+  std::vector<int32_t> peer;    // per query: warp peer aggregation
   StagedCol key, val;
   uint32_t nq = 0;
   int block = 512;
@@ -337,7 +345,7 @@ struct BatchState {
     for (uint32_t l = 0; l < n; ++l) {
       const uint32_t q = qids[l];
       const uint64_t cap = caps[l];
-      R.qs[l] = BatchQ{table_rows, cap, table_rows, slots[q] > 0 ? 1 : 0, std::max(slots[q], 64)};
+      R.qs[l] = BatchQ{table_rows, cap, table_rows, slots[q] > 0 ? 1 : 0, std::max(slots[q], 64), peer[q], 0};
       R.max_slots = std::max(R.max_slots, slots[q]);
       table_rows += cap + 2;
       const uint64_t rows = rows_of(q);
@@ -435,7 +443,7 @@ struct BatchState {
     return F;
   }
 
-  size_t smem_bytes(int32_t max_slots) const { return static_cast<size_t>(max_slots + 2) * plan.row_words * 8; }
+  size_t smem_bytes(int32_t max_slots) const { return static_cast<size_t>(max_slots + 2) * (plan.row_words | 1) * 8; }
 
   void enqueue(Round& R) {
     QEG_CUDA(cudaMemsetAsync(R.dnext.get(), 0, 4, ctx->stream));
@@ -541,6 +549,7 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
     S.hot.resize(nqueries);
     S.slots.resize(nqueries);
     S.chunk.resize(nqueries);
+    S.peer.resize(nqueries);
     std::vector<uint32_t> all(nqueries);
     std::vector<uint64_t> caps(nqueries);
     for (uint32_t q = 0; q < nqueries; ++q) {
@@ -561,6 +570,8 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
                        ? static_cast<int32_t>(std::min<uint64_t>(kBatchMaxSlots, pow2_floor(std::max(64.0, 2.0 * g))))
                        : 0;
       uint64_t ch = 1u << 16;
+      // Few groups: many lanes of a warp land on the same group.
+      int32_t pr = g <= 256 ? 1 : 0;
       const double lg = std::log2(std::max(g, 1.0));
       for (int t = 0; t < ntuning; ++t) {
         if (lg <= tuning[t].max_log2_groups && (share >= 0.3 ? 1 : 0) == tuning[t].skewed) {
@@ -568,11 +579,13 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
                    ? static_cast<int32_t>(pow2_floor(std::min<int32_t>(kBatchMaxSlots, std::max(64, tuning[t].smem_slots))))
                    : 0;
           if (tuning[t].rows_per_item > 0) ch = tuning[t].rows_per_item;
+          if (tuning[t].peer_rows >= 0) pr = tuning[t].peer_rows ? 1 : 0;
           break;
         }
       }
       S.slots[q] = sl;
       S.chunk[q] = std::max<uint64_t>(ch, 256);
+      S.peer[q] = pr;
       all[q] = q;
       caps[q] = std::max<uint64_t>(64, static_cast<uint64_t>(kEstimateHeadroom * g / kTargetLoad) + 16);
     }

@@ -94,7 +94,10 @@ __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
   extern __shared__ unsigned long long sst[];
   const int warps = blockDim.x >> 5;
   const int copies = P.per_warp ? warps : 1;
-  const int stride_g = P.ngroups * P.nfields;
+  // A group's fields at an odd stride (in 8-byte words), so the same field of
+  // different groups falls in different shared-memory banks.
+  const int GS = P.nfields | 1;
+  const int stride_g = P.ngroups * GS;
   for (int i = threadIdx.x; i < copies * stride_g; i += blockDim.x) sst[i] = 0;
   __syncthreads();
   unsigned long long* mine = sst + (P.per_warp ? (threadIdx.x >> 5) * stride_g : 0);
@@ -137,7 +140,7 @@ __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
       const unsigned peers = act ? (same & amask) : (1u << lane);
       const bool leader = act && __ffs(peers) - 1 == static_cast<int>(lane);
       const PeerPlan pp = plan_peers(peers, lane);
-      unsigned long long* f = leader ? mine + static_cast<size_t>(g) * P.nfields : nullptr;
+      unsigned long long* f = leader ? mine + static_cast<size_t>(g) * GS : nullptr;
       if (leader) {
         if (P.per_warp) f[0] += __popc(peers);
         else atomicAdd(f, static_cast<unsigned long long>(__popc(peers)));
@@ -160,7 +163,9 @@ __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
   __syncthreads();
   // Merge the shared copies into the global state (zero is every identity).
   for (int i = threadIdx.x; i < stride_g; i += blockDim.x) {
-    const int f = i % P.nfields;
+    const int f = i % GS;
+    if (f >= P.nfields) continue;
+    const int gi = (i / GS) * P.nfields + f;  // index into the unpadded global state
     const uint8_t kind = P.fkind[f];
     unsigned long long acc = 0;
     double accf = 0;
@@ -171,10 +176,10 @@ __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
       else acc += v;
     }
     if (kind == F_SUMF) {
-      if (accf != 0.0) atomicAdd(reinterpret_cast<double*>(P.state + i), accf);
+      if (accf != 0.0) atomicAdd(reinterpret_cast<double*>(P.state + gi), accf);
     } else if (acc) {
-      if (kind >= F_MINI) atomicMax(P.state + i, acc);
-      else atomicAdd(P.state + i, acc);
+      if (kind >= F_MINI) atomicMax(P.state + gi, acc);
+      else atomicAdd(P.state + gi, acc);
     }
   }
 }
@@ -447,7 +452,7 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
     P.glist = dg.get<uint32_t>();
     P.state = dstate.get<unsigned long long>();
     const int block = 512;
-    const size_t per_copy = static_cast<size_t>(P.ngroups) * P.nfields * 8;
+    const size_t per_copy = static_cast<size_t>(P.ngroups) * (P.nfields | 1) * 8;
     P.per_warp = per_copy * (block / 32) <= 96 * 1024 ? 1 : 0;
     const size_t sb = P.per_warp ? per_copy * (block / 32) : per_copy;
     require(sb <= ctx->smem_optin, "too many groups for the fused pipeline's shared-memory state");

@@ -535,14 +535,14 @@ def estimator_train(ctx, x, t, epochs, batch, lr, seed):
 
 class BatchTuning(ctypes.Structure):
     _fields_ = [("max_log2_groups", ctypes.c_double), ("skewed", ctypes.c_int32), ("smem_slots", ctypes.c_int32),
-                ("rows_per_item", ctypes.c_uint64)]
+                ("rows_per_item", ctypes.c_uint64), ("peer_rows", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Batch:
     """Many GROUP BY queries over slices of one (key, value) column pair, run
     by one persistent kernel from a captured CUDA graph (qeg_batch_*).
     `row_offsets` has nqueries + 1 ascending entries; `tuning` is a list of
-    (max_log2_groups, skewed, smem_slots, rows_per_item) buckets."""
+    (max_log2_groups, skewed, smem_slots, rows_per_item[, peer_rows]) buckets."""
 
     def __init__(self, ctx, row_offsets, key, val, aggs, tuning=(), block_threads=0):
         self.ctx = ctx
@@ -553,7 +553,8 @@ class Batch:
             specs[i] = AggSpec(f, c)
         tun = (BatchTuning * max(1, len(tuning)))()
         for i, t in enumerate(tuning):
-            tun[i] = BatchTuning(*t)
+            t = tuple(t) + (-1,) * (5 - len(t))  # peer_rows defaults to "decide from the estimate"
+            tun[i] = BatchTuning(*t[:5], 0)
         self._keep = (key, val)  # the batch reads these buffers on every run
         kc, vc = key.c(), val.c()
         p = ctypes.c_void_p()
