@@ -202,17 +202,16 @@ __device__ __forceinline__ void merge_fields(uint64_t* dst, const uint64_t* src,
 }
 
 // Combines the rows of every peer group and lets each group's leader apply the
-// result to `f` (its field block; ignored on other lanes). `priv`: `f` is a
-// warp-private row, updated without atomics (one leader per group and one
-// group per row within a warp). One loop over the fields keeps the code small.
+// result to `f` (its field block; ignored on other lanes). `space` says where
+// `f` lives (RowSpace): a warp-private row is updated without atomics (one
+// leader per group and one group per row within a warp), shared and global
+// rows with reductions of their state space. One loop over the fields keeps
+// the code small.
 template <int NV>
-__device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, bool priv, unsigned peers, const PeerPlan& pp,
+__device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, int space, unsigned peers, const PeerPlan& pp,
                                            const AggK& P, const bool (&vv)[kMaxVals],
                                            const uint64_t (&vb)[kMaxVals]) {
-  if (leader) {
-    if (priv) f[0] += __popc(peers);
-    else atomicAdd(reinterpret_cast<unsigned long long*>(f), static_cast<unsigned long long>(__popc(peers)));
-  }
+  if (leader) field_red_at(space, f, F_ROWS, static_cast<uint64_t>(__popc(peers)));
 #pragma unroll 1
   for (int fi = 1; fi < P.nfields; ++fi) {
     const uint8_t kind = P.fkind[fi];
@@ -227,10 +226,7 @@ __device__ __forceinline__ void warp_apply(uint64_t* f, bool leader, bool priv, 
       }
     }
     const uint64_t x = peer_reduce(field_contrib(kind, v, b), kind, pp);
-    if (leader) {
-      if (priv) f[fi] = field_combine(kind, f[fi], x);
-      else field_apply(f + fi, kind, x);
-    }
+    if (leader) field_red_at(space, f + fi, kind, x);
   }
 }
 
@@ -280,14 +276,13 @@ __device__ __forceinline__ void track_full(const AggK& P, unsigned lane, uint32_
   }
 }
 
-// PEER (single key): combine the rows of a warp that share a group before
-// applying them (warp peer aggregation, warp-private rows for the hottest
-// keys). Without it every lane applies its own row with atomics, which is
-// cheaper unless many lanes of a warp hit the same few groups: measured on
-// GB300 over 64M rows, per-lane atomics run 1.3-1.5x faster for a 1024-group
-// column and for a Zipf(1.1) column with preloaded heavy hitters, while the
-// peer path runs 2x faster when a skewed column has no private table.
-template <int MODE, int NV, bool PEER>
+// The global (MODE 0) and single-key (MODE 1) kernels combine the rows of a
+// warp that share a group before applying them (warp peer aggregation, with
+// warp-private rows for the hottest keys); measured on GB300 over 64M rows
+// this runs 1.3x faster than every lane applying its own row with atomics,
+// for a 1024-group column as for a Zipf(1.1) column with preloaded heavy
+// hitters. The composite-key kernel (MODE 2) applies rows per lane.
+template <int MODE, int NV>
 __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   extern __shared__ uint64_t sm[];
   const int W = P.row_words;
@@ -303,7 +298,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   // Warp-private rows after the table: MODE 0 one per warp; MODE 1 (preloaded
   // table) one per warp for each of the WH hottest keys, with a rank byte per
   // table slot (0 = not one of them) and the table slot of every rank.
-  const int WH = (MODE == 0) ? 1 : ((MODE == 1 && PEER && S > 0 && P.nhot > 0) ? P.warp_hot : 0);
+  const int WH = (MODE == 0) ? 1 : ((MODE == 1 && S > 0 && P.nhot > 0) ? P.warp_hot : 0);
   uint64_t* wrows = sm + srows * SW;
   uint8_t* srank = reinterpret_cast<uint8_t*>(wrows + nwarps * WH * SW);
   uint16_t* hslot = reinterpret_cast<uint16_t*>(srank + ((srows + 7) & ~7));
@@ -364,29 +359,8 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
     if (MODE == 0) {
       const unsigned peers = live ? livemask : (1u << lane);
       const PeerPlan pp = plan_peers(peers, lane);
-      warp_apply<NV>(&wrows[warp * SW + 1], live && __ffs(peers) - 1 == static_cast<int>(lane), true, peers, pp, P, vv,
+      warp_apply<NV>(&wrows[warp * SW + 1], live && __ffs(peers) - 1 == static_cast<int>(lane), kRowPrivate, peers, pp, P, vv,
                  vb);
-      continue;
-    }
-    if (MODE == 1 && !PEER) {
-      const unsigned long long ins0 = inserted;
-      if (live) {
-        const DevCol& kc = P.key[0];
-        const bool kv = col_valid(kc, p);
-        const uint64_t k = kv ? key_word(kc, p) : 0;
-        const uint64_t h = key_hash1(k);
-        uint64_t* f = nullptr;
-        const int srow = S > 0 ? smem_row(sm, S, SW, P, kv, k, h) : -1;
-        if (srow >= 0) {
-          f = &sm[srow * SW + 1];
-        } else {
-          uint64_t* r = global_row1(P, kv, k, h, inserted, full ? kFullProbe : P.probe_limit);
-          if (r) f = r + 1;
-        }
-        if (f) apply_row<NV>(f, P, vv, vb);
-        else spill_row(P, p);
-      }
-      if (P.full_flag) track_full(P, lane, iter, inserted != ins0, pending, full);
       continue;
     }
     if (MODE == 1) {
@@ -400,7 +374,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
       // The leader finds (or places) the group's row.
       uint64_t* f = nullptr;
-      bool priv = false;
+      int space = kRowGlobal;
       const unsigned long long ins0 = inserted;
       if (leader) {
         const uint64_t h = key_hash1(k);
@@ -409,9 +383,10 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
           const int rk = (ranked && srow < S) ? srank[srow] : 0;
           if (rk) {
             f = &wrows[(warp * WH + rk - 1) * SW + 1];
-            priv = true;
+            space = kRowPrivate;
           } else {
             f = &sm[srow * SW + 1];
+            space = kRowShared;
           }
         } else {
           uint64_t* r = global_row1(P, kv, k, h, inserted, full ? kFullProbe : P.probe_limit);
@@ -426,7 +401,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
         peers = 1u << lane;
       }
       const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
-      warp_apply<NV>(f, leader && ok, priv, peers, pp, P, vv, vb);
+      warp_apply<NV>(f, leader && ok, space, peers, pp, P, vv, vb);
       if (P.full_flag) track_full(P, lane, iter, inserted != ins0, pending, full);
       continue;
     }
@@ -812,16 +787,8 @@ void AggState::set_field_columns(AggK& P) const {
 
 int AggState::block_threads() const { return cfg.block_threads > 0 ? cfg.block_threads : 512; }
 
-bool AggState::peer_rows() const {
-  // Few groups (many lanes of a warp on the same group) or a skewed column
-  // aggregated in the global table alone.
-  if (mode != 1) return mode == 0;
-  if (est_groups > 0 && est_groups <= 512) return true;
-  return smem_slots == 0 && hot_share >= 0.3;
-}
-
 int AggState::warp_hot() const {
-  if (mode != 1 || !peer_rows() || nhot <= 0 || smem_slots <= 0) return 0;
+  if (mode != 1 || nhot <= 0 || smem_slots <= 0) return 0;
   // Up to 32 keys, within 32 KB of warp-private rows.
   const int fit = 32768 / ((block_threads() / 32) * (row_words | 1) * 8);
   return std::max(0, std::min({32, nhot, fit}));
@@ -851,15 +818,14 @@ void AggState::launch(const AggK& P, uint64_t nrows) {
   // 2, 4 or 8 (loops over value columns are unrolled to that count).
   void (*kern)(AggK) = nullptr;
   const int nv = static_cast<int>(val_cols.size());
-#define QEG_AGG_VARIANT(M, PEER)                          \
-  (nv <= 1   ? agg_kernel<M, 1, PEER>                     \
-   : nv <= 2 ? agg_kernel<M, 2, PEER>                     \
-   : nv <= 4 ? agg_kernel<M, 4, PEER>                     \
-             : agg_kernel<M, 8, PEER>)
-  if (mode == 0) kern = QEG_AGG_VARIANT(0, true);
-  else if (mode == 1 && peer_rows()) kern = QEG_AGG_VARIANT(1, true);
-  else if (mode == 1) kern = QEG_AGG_VARIANT(1, false);
-  else kern = QEG_AGG_VARIANT(2, false);
+#define QEG_AGG_VARIANT(M)                          \
+  (nv <= 1   ? agg_kernel<M, 1>                     \
+   : nv <= 2 ? agg_kernel<M, 2>                     \
+   : nv <= 4 ? agg_kernel<M, 4>                     \
+             : agg_kernel<M, 8>)
+  if (mode == 0) kern = QEG_AGG_VARIANT(0);
+  else if (mode == 1) kern = QEG_AGG_VARIANT(1);
+  else kern = QEG_AGG_VARIANT(2);
 #undef QEG_AGG_VARIANT
   int per_sm = 1;
   if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));

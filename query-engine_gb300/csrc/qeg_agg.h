@@ -139,7 +139,6 @@ struct AggState {
   void alloc_table(uint64_t new_cap);
   size_t smem_bytes(int block) const;
   int warp_hot() const;
-  bool peer_rows() const;
   int block_threads() const;
   void set_field_columns(AggK& P) const;
   void launch(const AggK& P, uint64_t nrows);

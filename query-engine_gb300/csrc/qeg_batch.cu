@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
       }
       const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
       uint64_t* f = nullptr;
+      int space = kRowGlobal;
       if (leader) {
         int srow = -1;
         if (S) {
@@ -141,6 +142,7 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
         }
         if (srow >= 0) {
           f = &sm[srow * SW + 1];
+          space = kRowShared;
         } else {
           uint64_t* r = batch_global_row(P, Q, kv, k);
           if (r) f = r + 1;
@@ -149,11 +151,11 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
       }
       const PeerPlan pp = plan_peers(peers, lane);
       const bool apply = leader && f != nullptr;
-      if (apply) atomicAdd(reinterpret_cast<unsigned long long*>(f), static_cast<unsigned long long>(__popc(peers)));
+      if (apply) field_red_at(space, f, F_ROWS, static_cast<uint64_t>(__popc(peers)));
       for (int j = 0; j < P.val_nf; ++j) {
         const uint8_t kind = P.fkind[P.val_first + j];
         const uint64_t x = peer_reduce(field_contrib(kind, v, b), kind, pp);
-        if (apply) field_apply(f + P.val_first + j, kind, x);
+        if (apply) field_red_at(space, f + P.val_first + j, kind, x);
       }
     }
     if (ovf) atomicOr(P.overflow + q, 1u);

@@ -141,10 +141,8 @@ __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
       const bool leader = act && __ffs(peers) - 1 == static_cast<int>(lane);
       const PeerPlan pp = plan_peers(peers, lane);
       unsigned long long* f = leader ? mine + static_cast<size_t>(g) * GS : nullptr;
-      if (leader) {
-        if (P.per_warp) f[0] += __popc(peers);
-        else atomicAdd(f, static_cast<unsigned long long>(__popc(peers)));
-      }
+      const int space = P.per_warp ? kRowPrivate : kRowShared;
+      if (leader) field_red_at(space, reinterpret_cast<uint64_t*>(f), F_ROWS, static_cast<uint64_t>(__popc(peers)));
 #pragma unroll
       for (int c = 0; c < kPipeMaxVals; ++c) {
         if (c >= P.nvals) break;
@@ -152,10 +150,7 @@ __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
           const int fi = P.cfirst[c] + k;
           const uint8_t kind = P.fkind[fi];
           const uint64_t x = peer_reduce(field_contrib(kind, vv[c], vb[c]), kind, pp);
-          if (leader) {
-            if (P.per_warp) f[fi] = field_combine(kind, f[fi], x);
-            else field_apply(reinterpret_cast<uint64_t*>(f + fi), kind, x);
-          }
+          if (leader) field_red_at(space, reinterpret_cast<uint64_t*>(f + fi), kind, x);
         }
       }
     }

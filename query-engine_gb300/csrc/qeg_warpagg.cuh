@@ -89,6 +89,38 @@ __device__ __forceinline__ void field_apply(uint64_t* w, uint8_t kind, uint64_t 
   else atomicMax(u, static_cast<unsigned long long>(x));
 }
 
+// Where a field block lives, so a merge uses the matching instruction: a
+// warp-private row (plain read-modify-write), a CTA table row (shared-memory
+// reduction) or a global table row (global reduction).
+enum RowSpace : int { kRowPrivate = 0, kRowShared = 1, kRowGlobal = 2 };
+
+// Merges `x` into a field word with a reduction of the given state space.
+// Zero is the identity of every field and is skipped.
+template <int SPACE>
+__device__ __forceinline__ void field_red(uint64_t* w, uint8_t kind, uint64_t x) {
+  if (!x) return;
+  const int op = field_op(kind);
+  if (SPACE == kRowPrivate) {
+    *w = field_combine(kind, *w, x);
+  } else if (SPACE == kRowShared) {
+    const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(w));
+    if (op == kOpAdd) asm volatile("red.shared.add.u64 [%0], %1;" ::"r"(a), "l"(x) : "memory");
+    else if (op == kOpFAdd) asm volatile("red.shared.add.f64 [%0], %1;" ::"r"(a), "d"(__longlong_as_double(static_cast<long long>(x))) : "memory");
+    else asm volatile("red.shared.max.u64 [%0], %1;" ::"r"(a), "l"(x) : "memory");
+  } else {
+    if (op == kOpAdd) asm volatile("red.global.add.u64 [%0], %1;" ::"l"(w), "l"(x) : "memory");
+    else if (op == kOpFAdd) asm volatile("red.global.add.f64 [%0], %1;" ::"l"(w), "d"(__longlong_as_double(static_cast<long long>(x))) : "memory");
+    else asm volatile("red.global.max.u64 [%0], %1;" ::"l"(w), "l"(x) : "memory");
+  }
+}
+
+// field_red with the space chosen at run time.
+__device__ __forceinline__ void field_red_at(int space, uint64_t* w, uint8_t kind, uint64_t x) {
+  if (space == kRowPrivate) field_red<kRowPrivate>(w, kind, x);
+  else if (space == kRowShared) field_red<kRowShared>(w, kind, x);
+  else field_red<kRowGlobal>(w, kind, x);
+}
+
 template <int OP>
 __device__ __forceinline__ uint64_t peer_reduce_op(uint64_t x, const PeerPlan& pp) {
 #pragma unroll 1
