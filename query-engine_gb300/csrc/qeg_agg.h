@@ -141,6 +141,7 @@ struct AggState {
   int warp_hot() const;
   int block_threads() const;
   void set_field_columns(AggK& P) const;
+  uint32_t field_spec(const AggK& P) const;  // qeg_warpagg.cuh field-set code
   void launch(const AggK& P, uint64_t nrows);
   void read_counters(uint64_t out[3]);
   void grow(uint64_t new_cap);

@@ -30,6 +30,12 @@ namespace qeg {
 namespace {
 
 constexpr int kBatchMaxSlots = 4096;
+// COUNT(*), SUM, AVG, MIN, MAX over an F64 value column, without and with its
+// NULL count (qeg_warpagg.cuh field-set codes).
+constexpr uint32_t kBatchSpecF64 = 4u | spec_field(1, 0, 0) | spec_field(2, F_SUMF, 0) | spec_field(3, F_MINF, 0) |
+                                   spec_field(4, F_MAXF, 0);
+constexpr uint32_t kBatchSpecF64Nulls = 4u | spec_field(1, F_NULLS, 0) | spec_field(2, F_SUMF, 0) |
+                                        spec_field(3, F_MINF, 0) | spec_field(4, F_MAXF, 0);
 
 struct BatchQ {
   uint64_t table_off;  // first row of the query's table in the arena
@@ -75,6 +81,8 @@ __device__ __forceinline__ uint64_t* batch_global_row(const BatchK& P, const Bat
   return nullptr;
 }
 
+// SPEC: the value fields' set (qeg_warpagg.cuh), or kGenericSpec.
+template <uint32_t SPEC>
 __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
   extern __shared__ uint64_t sm[];
   const int SW = P.W | 1;  // odd row stride in shared memory: fewer bank conflicts
@@ -151,11 +159,17 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
       }
       const PeerPlan pp = plan_peers(peers, lane);
       const bool apply = leader && f != nullptr;
-      if (apply) field_red_at(space, f, F_ROWS, static_cast<uint64_t>(__popc(peers)));
-      for (int j = 0; j < P.val_nf; ++j) {
-        const uint8_t kind = P.fkind[P.val_first + j];
-        const uint64_t x = peer_reduce(field_contrib(kind, v, b), kind, pp);
-        if (apply) field_red_at(space, f + P.val_first + j, kind, x);
+      if constexpr (SPEC != kGenericSpec) {
+        bool vv[8] = {v};
+        uint64_t vb[8] = {b};
+        spec_apply<SPEC, 1>(f, apply, space, peers, pp, vv, vb);
+      } else {
+        if (apply) field_red_at(space, f, F_ROWS, static_cast<uint64_t>(__popc(peers)));
+        for (int j = 0; j < P.val_nf; ++j) {
+          const uint8_t kind = P.fkind[P.val_first + j];
+          const uint64_t x = peer_reduce(field_contrib(kind, v, b), kind, pp);
+          if (apply) field_red_at(space, f + P.val_first + j, kind, x);
+        }
       }
     }
     if (ovf) atomicOr(P.overflow + q, 1u);
@@ -445,6 +459,22 @@ struct BatchState {
     return F;
   }
 
+  // The batch kernel for this plan's field set: COUNT/SUM/AVG/MIN/MAX over
+  // one value column (with or without its NULL count) has its own kernel.
+  void (*agg_kernel_for() const)(BatchK) {
+    const int n = plan.nfields - 1;
+    if (n > 7) return batch_agg_kernel<kGenericSpec>;
+    uint32_t spec = static_cast<uint32_t>(n);
+    for (int i = 1; i <= n; ++i) {
+      int kind = plan.fkind[i];
+      if (kind == F_NULLS && val.dev.all_valid) kind = 0;
+      spec |= spec_field(i, kind, 0);
+    }
+    if (spec == kBatchSpecF64) return batch_agg_kernel<kBatchSpecF64>;
+    if (spec == kBatchSpecF64Nulls) return batch_agg_kernel<kBatchSpecF64Nulls>;
+    return batch_agg_kernel<kGenericSpec>;
+  }
+
   size_t smem_bytes(int32_t max_slots) const { return static_cast<size_t>(max_slots + 2) * (plan.row_words | 1) * 8; }
 
   void enqueue(Round& R) {
@@ -452,10 +482,11 @@ struct BatchState {
     QEG_CUDA(cudaMemsetAsync(R.counts.get(), 0, R.counts.bytes(), ctx->stream));
     const size_t sb = smem_bytes(R.max_slots);
     int per_sm = 1;
-    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_agg_kernel, block, sb));
+    void (*kern)(BatchK) = agg_kernel_for();
+    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
     const unsigned grid = static_cast<unsigned>(
         std::max(1, std::min<int>(ctx->sms * std::max(per_sm, 1), static_cast<int>(std::max<uint32_t>(R.nitems, 1)))));
-    batch_agg_kernel<<<grid, block, sb, ctx->stream>>>(kparams(R));
+    kern<<<grid, block, sb, ctx->stream>>>(kparams(R));
     if (R.nfin) batch_finalize_kernel<<<R.nfin, 512, 0, ctx->stream>>>(finparams(R));
   }
 
@@ -593,7 +624,7 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
     }
     const size_t sb = S.smem_bytes(kBatchMaxSlots);
     require(sb <= ctx->smem_optin, "batch rows are too wide for the shared-memory tables");
-    QEG_CUDA(cudaFuncSetAttribute(batch_agg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+    QEG_CUDA(cudaFuncSetAttribute(S.agg_kernel_for(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
     S.rounds.resize(1);
     S.setup_round(S.rounds[0], all, caps);
     QEG_CUDA(cudaStreamSynchronize(ctx->stream));

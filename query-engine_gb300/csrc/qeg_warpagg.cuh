@@ -139,4 +139,60 @@ __device__ __forceinline__ uint64_t peer_reduce(uint64_t x, uint8_t kind, const 
   return peer_reduce_op<kOpMax>(x, pp);
 }
 
+// ---------------------------------------------------------------------------
+// Field-set specialisation. A SPEC packs the value fields of a row (fields
+// 1..n; field 0 is the row count): bits 0-3 hold n (<= 7), and field i (1-based)
+// has 4 bits at 4*i: the FieldKind in bits 0-2 (0 = skip: a NULL count of a
+// column without NULLs, which stays 0) and the value column (0 or 1) in bit 3.
+// Kernels instantiated for a SPEC unroll the field loop with every kind known
+// at compile time; kGenericSpec means "read the kinds from the parameter block".
+// ---------------------------------------------------------------------------
+constexpr uint32_t kGenericSpec = 0xffffffffu;
+
+__host__ __device__ constexpr int spec_n(uint32_t spec) { return static_cast<int>(spec & 15u); }
+__host__ __device__ constexpr int spec_kind(uint32_t spec, int i) { return static_cast<int>((spec >> (4 * i)) & 7u); }
+__host__ __device__ constexpr int spec_col(uint32_t spec, int i) { return static_cast<int>((spec >> (4 * i + 3)) & 1u); }
+__host__ __device__ constexpr uint32_t spec_field(int i, int kind, int col) {
+  return (static_cast<uint32_t>(kind) | (static_cast<uint32_t>(col) << 3)) << (4 * i);
+}
+
+// Reduces every field of SPEC across the peers (all lanes call it), then lets
+// the leader merge the results into the field block `f` in state space SPACE.
+template <uint32_t SPEC, int SPACE>
+__device__ __forceinline__ void spec_merge(uint64_t* f, const uint64_t (&xs)[8]) {
+#pragma unroll
+  for (int i = 1; i <= spec_n(SPEC); ++i)
+    if (spec_kind(SPEC, i) != 0) field_red<SPACE>(f + i, static_cast<uint8_t>(spec_kind(SPEC, i)), xs[i]);
+}
+
+template <uint32_t SPEC, int NV>
+__device__ __forceinline__ void spec_apply(uint64_t* f, bool leader, int space, unsigned peers, const PeerPlan& pp,
+                                           const bool (&vv)[8], const uint64_t (&vb)[8]) {
+  uint64_t xs[8];
+  xs[0] = static_cast<uint64_t>(__popc(peers));
+#pragma unroll
+  for (int i = 1; i <= spec_n(SPEC); ++i) {
+    const int kind = spec_kind(SPEC, i);
+    const int col = spec_col(SPEC, i) < NV ? spec_col(SPEC, i) : 0;
+    xs[i] = 0;
+    if (kind != 0) {
+      const uint64_t x = field_contrib(static_cast<uint8_t>(kind), vv[col], vb[col]);
+      if (field_op(static_cast<uint8_t>(kind)) == kOpAdd) xs[i] = peer_reduce_op<kOpAdd>(x, pp);
+      else if (field_op(static_cast<uint8_t>(kind)) == kOpFAdd) xs[i] = peer_reduce_op<kOpFAdd>(x, pp);
+      else xs[i] = peer_reduce_op<kOpMax>(x, pp);
+    }
+  }
+  if (!leader) return;
+  if (space == kRowPrivate) {
+    field_red<kRowPrivate>(f, F_ROWS, xs[0]);
+    spec_merge<SPEC, kRowPrivate>(f, xs);
+  } else if (space == kRowShared) {
+    field_red<kRowShared>(f, F_ROWS, xs[0]);
+    spec_merge<SPEC, kRowShared>(f, xs);
+  } else {
+    field_red<kRowGlobal>(f, F_ROWS, xs[0]);
+    spec_merge<SPEC, kRowGlobal>(f, xs);
+  }
+}
+
 }  // namespace qeg
