@@ -504,12 +504,15 @@ def run_batch_bench(args, dev, local):
     clk.__exit__(None, None, None)
     ms = e0.elapsed_time(e1) / args.steps
     launches = (ctx.launches - launches0) / args.steps
-    fell = sum(b.stats(q)["fell_back"] for q in range(len(groups)))
+    stats = [b.stats(q) for q in range(len(groups))]
+    fell = sum(st["fell_back"] for st in stats)
     # Exact group counts (torch.unique per query) for the estimate report.
     true = np.array([int(torch.unique(W.key[int(W.offsets[q]):int(W.offsets[q + 1])]).numel())
                      for q in range(len(groups))])
     assert np.array_equal(true, groups.astype(np.int64)), "batch group counts differ from torch.unique"
-    est = np.array([b.stats(q)["est_groups"] for q in range(len(groups))])
+    est = np.array([st["est_groups"] for st in stats])
+    fb = [q for q in range(len(groups)) if stats[q]["fell_back"]]
+    fell_ratio = sorted(float(true[q] / max(est[q], 1.0)) for q in fb)
     lerr = np.abs(np.log2(np.maximum(est, 1)) - np.log2(np.maximum(true, 1)))
     b.close()
     rows_s = W.n / (ms / 1e3)
@@ -551,6 +554,9 @@ def run_batch_bench(args, dev, local):
         "gpu_launches": launches, "clocks": clocks, "plan_s": plan_s,
         "estimate_log2_error": {"median": float(np.median(lerr)), "p90": float(np.percentile(lerr, 90))},
         "fell_back_queries": int(fell),
+        "fell_back_true_over_est": {"min": fell_ratio[0] if fell_ratio else None,
+                                    "median": fell_ratio[len(fell_ratio) // 2] if fell_ratio else None,
+                                    "max": fell_ratio[-1] if fell_ratio else None},
         "plain_sequential": plain,
         "batched_vs_plain": (plain["ms_per_step"] / ms) if plain else None,
     }))

@@ -32,6 +32,12 @@ namespace {
 
 constexpr int kPipeMaxAggs = 16;
 constexpr int kPipeMaxVals = 4;
+// COUNT(*), AVG/SUM(F64 column 0), SUM(integer column 1) without and with NULL
+// counts (qeg_warpagg.cuh field-set codes).
+constexpr uint32_t kPipeSpecAvgSum = 4u | spec_field(1, 0, 0) | spec_field(2, F_SUMF, 0) | spec_field(3, 0, 1) |
+                                     spec_field(4, F_SUMI, 1);
+constexpr uint32_t kPipeSpecAvgSumNulls = 4u | spec_field(1, F_NULLS, 0) | spec_field(2, F_SUMF, 0) |
+                                          spec_field(3, F_NULLS, 1) | spec_field(4, F_SUMI, 1);
 
 enum CmpOp : int32_t { kLT = 0, kLE = 1, kGT = 2, kGE = 3, kEQ = 4, kNE = 5, kNever = -1, kAlways = -2 };
 
@@ -90,6 +96,8 @@ __device__ __forceinline__ bool pass_filter(const PipeK& P, uint64_t p) {
   return r;
 }
 
+// SPEC: the aggregate fields' set (qeg_warpagg.cuh), or kGenericSpec.
+template <uint32_t SPEC>
 __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
   extern __shared__ unsigned long long sst[];
   const int warps = blockDim.x >> 5;
@@ -142,15 +150,21 @@ __global__ void __launch_bounds__(512) pipeline_kernel(const PipeK P) {
       const PeerPlan pp = plan_peers(peers, lane);
       unsigned long long* f = leader ? mine + static_cast<size_t>(g) * GS : nullptr;
       const int space = P.per_warp ? kRowPrivate : kRowShared;
-      if (leader) field_red_at(space, reinterpret_cast<uint64_t*>(f), F_ROWS, static_cast<uint64_t>(__popc(peers)));
+      if constexpr (SPEC != kGenericSpec) {
+        bool v8[8] = {vv[0], vv[1]};
+        uint64_t b8[8] = {vb[0], vb[1]};
+        spec_apply<SPEC, 2>(reinterpret_cast<uint64_t*>(f), leader, space, peers, pp, v8, b8);
+      } else {
+        if (leader) field_red_at(space, reinterpret_cast<uint64_t*>(f), F_ROWS, static_cast<uint64_t>(__popc(peers)));
 #pragma unroll
-      for (int c = 0; c < kPipeMaxVals; ++c) {
-        if (c >= P.nvals) break;
-        for (int k = 0; k < P.cnf[c]; ++k) {
-          const int fi = P.cfirst[c] + k;
-          const uint8_t kind = P.fkind[fi];
-          const uint64_t x = peer_reduce(field_contrib(kind, vv[c], vb[c]), kind, pp);
-          if (leader) field_red_at(space, reinterpret_cast<uint64_t*>(f + fi), kind, x);
+        for (int c = 0; c < kPipeMaxVals; ++c) {
+          if (c >= P.nvals) break;
+          for (int k = 0; k < P.cnf[c]; ++k) {
+            const int fi = P.cfirst[c] + k;
+            const uint8_t kind = P.fkind[fi];
+            const uint64_t x = peer_reduce(field_contrib(kind, vv[c], vb[c]), kind, pp);
+            if (leader) field_red_at(space, reinterpret_cast<uint64_t*>(f + fi), kind, x);
+          }
         }
       }
     }
@@ -447,19 +461,34 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
     P.glist = dg.get<uint32_t>();
     P.state = dstate.get<unsigned long long>();
     const int block = 512;
+    // The kernel for this field set: COUNT(*) with SUM/AVG over an F64 column
+    // and SUM over an integer column (the trades pipeline's AVG(price),
+    // SUM(qty)), with or without NULL counts, has its own kernel.
+    void (*kern)(PipeK) = pipeline_kernel<kGenericSpec>;
+    if (P.nvals == 2 && P.nfields == 5) {
+      uint32_t spec = 4u;
+      for (int i = 1; i <= 4; ++i) {
+        const int col = i <= P.cnf[0] ? 0 : 1;
+        int kind = P.fkind[i];
+        if (kind == F_NULLS && P.val[col].all_valid) kind = 0;
+        spec |= spec_field(i, kind, col);
+      }
+      if (spec == kPipeSpecAvgSum) kern = pipeline_kernel<kPipeSpecAvgSum>;
+      else if (spec == kPipeSpecAvgSumNulls) kern = pipeline_kernel<kPipeSpecAvgSumNulls>;
+    }
     const size_t per_copy = static_cast<size_t>(P.ngroups) * (P.nfields | 1) * 8;
     P.per_warp = per_copy * (block / 32) <= 96 * 1024 ? 1 : 0;
     const size_t sb = P.per_warp ? per_copy * (block / 32) : per_copy;
     require(sb <= ctx->smem_optin, "too many groups for the fused pipeline's shared-memory state");
     if (sb > 48 * 1024)
-      QEG_CUDA(cudaFuncSetAttribute(pipeline_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+      QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
     int per_sm = 1;
-    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pipeline_kernel, block, sb));
+    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
     const uint64_t want = (np + block * 16 - 1) / (block * 16);
     const unsigned grid = static_cast<unsigned>(
         std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
     if (np > 0 && domain > 0 && ngroups > 0) {
-      pipeline_kernel<<<grid, block, sb, ctx->stream>>>(P);
+      kern<<<grid, block, sb, ctx->stream>>>(P);
       ctx->launches++;
       QEG_CUDA(cudaGetLastError());
     }
