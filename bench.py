@@ -278,6 +278,9 @@ def run_agg_bench(args, dev, local):
         out[name] = {"ms_per_step": ms, "rows_per_s": W.n / (ms / 1e3), "groups": n, "stats": st,
                      "gb_per_s": W.n * W.row_bytes / (ms / 1e3) / 1e9,
                      "launches_per_step": (ctx.launches - launches0) / args.steps}
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_agg_baseline(W, os.cpu_count() or 1)
     peak, kind = peaks()
     best = out["learned"] if "learned" in out else next(iter(out.values()))
     print(json.dumps({
@@ -288,6 +291,7 @@ def run_agg_bench(args, dev, local):
         "roofline": {"bound": "hbm", "achieved": best["gb_per_s"], "peak": peak, "peak_kind": kind,
                      "unit": "GB/s", "frac": best["gb_per_s"] / peak},
         "variants": out,
+        "cpu_baseline": cpu,
         "learned_vs_plain": (out["plain_fixed"]["ms_per_step"] / best["ms_per_step"]
                              if "plain_fixed" in out else None),
     }))
@@ -560,6 +564,29 @@ def run_batch_bench(args, dev, local):
         "plain_sequential": plain,
         "batched_vs_plain": (plain["ms_per_step"] / ms) if plain else None,
     }))
+
+
+def cpu_agg_baseline(W, threads, sample_rows=1 << 23):
+    """Times the oracle's port of the reference's morsel-parallel GROUP BY
+    (exec/parallel.cpp:402-599, per-worker partial tables and a serial merge)
+    on the first `sample_rows` rows of the workload with every host thread."""
+    import oracle as O
+
+    n = min(W.n, sample_rows)
+    cols = []
+    for c in W.cols:
+        vals = c.values[:n].cpu().numpy()
+        valid = None
+        if c.validity is not None:
+            valid = np.unpackbits(c.validity[: (n + 63) // 64].cpu().numpy().view(np.uint8),
+                                  bitorder="little")[:n].astype(bool)
+        cols.append(O.TCol(c.type, vals, valid))
+    morsel = max(1024, -(-n // (threads * 4)) // 64 * 64)
+    t0 = time.perf_counter()
+    O.parallel_groupby(cols, [0], W.aggs, threads=threads, morsel_rows=morsel)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "rows/s", "cores": threads, "kind": "port",
+            "sample": "first %d rows (%.1f s), morsels of %d rows" % (n, dt, morsel)}
 
 
 def cpu_reference(sample, threads, probe_rows, nbuild):

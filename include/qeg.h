@@ -264,6 +264,12 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
 #define QEG_MLP_PARAMS 9474
 qeg_status qeg_sketch(qeg_ctx* ctx, const qeg_column* key, uint64_t sample_rows, float* features,
                       double* classic_groups, double* top_share);
+/* The batch planner's sketch (qeg_batch_create): the features and classic
+ * estimate of every row range [row_offsets[q], row_offsets[q+1]) of a key
+ * column, one sample of about `sample_rows` rows (0 = 2^16) per range, all in
+ * one launch; features holds nqueries x QEG_SKETCH_FEATURES floats. */
+qeg_status qeg_sketch_batch(qeg_ctx* ctx, const qeg_column* key, uint32_t nqueries, const uint64_t* row_offsets,
+                            uint64_t sample_rows, float* features, double* classic_groups);
 qeg_status qeg_estimator_init(qeg_ctx* ctx, uint64_t seed);
 qeg_status qeg_estimator_set_weights(qeg_ctx* ctx, const float* params);
 qeg_status qeg_estimator_get_weights(qeg_ctx* ctx, float* params);

@@ -101,12 +101,28 @@ __device__ __forceinline__ uint64_t* global_row1(const AggK& P, bool kv, uint64_
   const int W = P.row_words;
   if (!kv) return P.table + (P.cap + 1) * W;
   if (k == 0) return P.table + P.cap * W;
-  // Linear probing, four slots per step: the four key words are loaded
-  // together (independent loads), then examined in slot order, so a probe
-  // sequence costs a quarter of the dependent memory round trips. A key word
-  // never changes once set, so a stale non-empty value stays correct.
+  // Linear probing. The home slot alone first (one sector, and the answer for
+  // most keys at the target load), then four slots per step: their key words
+  // are loaded together (independent loads) and examined in slot order, so a
+  // long probe costs a quarter of the dependent memory round trips. A key
+  // word never changes once set, so a stale non-empty value stays correct.
   uint64_t s = __umul64hi(h, P.cap);
-  for (int t = 0; t < limit; t += 4) {
+  {
+    uint64_t* r = P.table + s * W;
+    const uint64_t cur = ld_relaxed(r);
+    if (cur == k) return r;
+    if (cur == 0) {
+      const unsigned long long old =
+          atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, static_cast<unsigned long long>(k));
+      if (old == 0) {
+        ++inserted;
+        return r;
+      }
+      if (old == k) return r;
+    }
+    if (++s == P.cap) s = 0;
+  }
+  for (int t = 1; t < limit; t += 4) {
     uint64_t idx[4], cur[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {

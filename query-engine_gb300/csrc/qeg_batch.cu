@@ -67,16 +67,37 @@ __device__ __forceinline__ uint64_t* batch_global_row(const BatchK& P, const Bat
   uint64_t* T = P.arena + Q.table_off * P.W;
   if (!kv) return T + (Q.cap + 1) * P.W;
   if (k == 0) return T + Q.cap * P.W;
+  // Linear probing: the home slot alone, then four slots per step whose key
+  // words are loaded together (see global_row1 in qeg_agg.cu).
   uint64_t s = __umul64hi(hash_fold(kHashSeed, k), Q.cap);
-  for (int t = 0; t < 128; ++t) {
-    uint64_t* r = T + s * P.W;
-    unsigned long long cur = *reinterpret_cast<volatile unsigned long long*>(r);
-    if (cur == k) return r;
-    if (cur == 0) {
-      cur = atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, static_cast<unsigned long long>(k));
-      if (cur == 0 || cur == k) return r;
+  for (int t = 0; t < 128;) {
+    const int width = t == 0 ? 1 : 4;
+    uint64_t idx[4];
+    unsigned long long cur[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j < width) {
+        uint64_t x = s + j;
+        if (x >= Q.cap) x -= Q.cap;
+        idx[j] = x;
+        cur[j] = *reinterpret_cast<volatile unsigned long long*>(T + x * P.W);
+      }
     }
-    s = (s + 1 == Q.cap) ? 0 : s + 1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j < width) {
+        uint64_t* r = T + idx[j] * P.W;
+        if (cur[j] == k) return r;
+        if (cur[j] == 0) {
+          const unsigned long long old =
+              atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, static_cast<unsigned long long>(k));
+          if (old == 0 || old == k) return r;
+        }
+      }
+    }
+    t += width;
+    s += width;
+    if (s >= Q.cap) s -= Q.cap;
   }
   return nullptr;
 }

@@ -108,6 +108,27 @@ qeg_status qeg_sketch(qeg_ctx* ctx, const qeg_column* key, uint64_t sample_rows,
   });
 }
 
+qeg_status qeg_sketch_batch(qeg_ctx* ctx, const qeg_column* key, uint32_t nqueries, const uint64_t* row_offsets,
+                            uint64_t sample_rows, float* features, double* classic_groups) {
+  return guarded(ctx, [&] {
+    require(ctx && key && row_offsets && features, "NULL argument");
+    require(nqueries >= 1 && row_offsets[nqueries] == key->len, "row offsets must cover the column");
+    for (uint32_t q = 0; q < nqueries; ++q) require(row_offsets[q] <= row_offsets[q + 1], "row offsets must ascend");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    StagedCol s;
+    stage_column(ctx, *key, s);
+    std::vector<uint64_t> offs(row_offsets, row_offsets + nqueries + 1);
+    DevBuf doffs((nqueries + 1) * 8, ctx->stream);
+    QEG_CUDA(cudaMemcpyAsync(doffs.get(), offs.data(), (nqueries + 1) * 8, cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<SketchResult> r;
+    batch_sketch(ctx, s.dev, doffs.get<uint64_t>(), offs, sample_rows ? sample_rows : (1u << 16), r);
+    for (uint32_t q = 0; q < nqueries; ++q) {
+      std::copy(r[q].features, r[q].features + kSketchFeatures, features + static_cast<size_t>(q) * kSketchFeatures);
+      if (classic_groups) classic_groups[q] = classic_estimate(r[q]);
+    }
+  });
+}
+
 qeg_status qeg_estimator_init(qeg_ctx* ctx, uint64_t seed) {
   return guarded(ctx, [&] {
     require(ctx, "NULL ctx");

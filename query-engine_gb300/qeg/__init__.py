@@ -97,6 +97,7 @@ def lib():
             "qeg_join_count_sum_noalloc": (i32, [vp, vp, vp, vp, vp]),
             "qeg_filter_join_agg": (i32, [vp, vp, c, vp, c, vp, u64, vp, P(u64)]),
             "qeg_sketch": (i32, [vp, vp, u64, vp, P(ctypes.c_double), P(ctypes.c_double)]),
+            "qeg_sketch_batch": (i32, [vp, vp, ctypes.c_uint32, vp, u64, vp, vp]),
             "qeg_estimator_init": (i32, [vp, u64]),
             "qeg_estimator_set_weights": (i32, [vp, vp]),
             "qeg_estimator_get_weights": (i32, [vp, vp]),
@@ -481,6 +482,18 @@ def sketch(ctx, col, sample_rows=0):
     _check(lib().qeg_sketch(ctx.p, ctypes.byref(c), sample_rows, f.ctypes.data, ctypes.byref(g), ctypes.byref(s)),
            ctx.p)
     return f, g.value, s.value
+
+
+def sketch_batch(ctx, col, row_offsets, sample_rows=0):
+    """The batch planner's per-range sketch: (features [n, 80], classic [n])."""
+    offs = np.ascontiguousarray(np.asarray(row_offsets, dtype=np.uint64))
+    n = len(offs) - 1
+    f = np.zeros((n, SKETCH_FEATURES), np.float32)
+    c = np.zeros(n, np.float64)
+    cc = col.c()
+    _check(lib().qeg_sketch_batch(ctx.p, ctypes.byref(cc), n, offs.ctypes.data, sample_rows, f.ctypes.data,
+                                  c.ctypes.data), ctx.p)
+    return f, c
 
 
 def learned_groups(classic, out0):

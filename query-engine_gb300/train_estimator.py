@@ -1,9 +1,11 @@
 """Trains the learned cardinality / skew estimator on the GPU.
 
 Training pairs are (sketch features, exact statistics) of seeded synthetic key
-columns: the features come from qeg_sketch (a 2^20-row strided sample), the
-targets from the exact GROUP BY engine over the whole column -- the number of
-groups and the share of rows carried by the 2048 largest groups. Families:
+columns: the features come from qeg_sketch (a 2^20-row strided sample, what
+the ordinary GROUP BY plans with) and from qeg_sketch_batch (the batch
+planner's one-CTA sketch of a 2^16-row sample), the targets from the exact
+GROUP BY engine over the whole column -- the number of groups and the share of
+rows carried by the 2048 largest groups. Families:
 uniform over a domain, Zipf(s) for s in [0.3, 1.6], a sequential key with
 duplication, and a mixture (uniform background plus a heavy head). Row counts
 and domains are log-uniform so the sample fraction varies from 1 to ~1/256.
@@ -100,22 +102,29 @@ def targets(groups, share, classic):
 
 
 def build_set(ctx, rng, count, dev, seed):
+    """Two examples per column: the column sketch of the ordinary GROUP BY
+    (a 2^20-row sample) and the batch planner's per-query sketch (one CTA,
+    a 2^16-row sample), with the same exact targets."""
     g = torch.Generator(device=dev)
     g.manual_seed(seed)
     X, T, C, D = [], [], [], []
     for i in range(count):
         keys, desc = gen_keys(rng, g, dev)
         torch.cuda.synchronize()
-        f, classic, _ = qeg.sketch(ctx, qeg.Col(keys, None, qeg.I64))
+        col = qeg.Col(keys, None, qeg.I64)
+        f, classic, _ = qeg.sketch(ctx, col)
+        fb, cb = qeg.sketch_batch(ctx, col, [0, keys.numel()], 1 << 16)
         ctx.synchronize()
         groups, share = exact_stats(ctx, keys)
         ctx.synchronize()
         print("dataset %d %s groups=%d share=%.3f" % (i, desc, groups, share), flush=True)
-        X.append(f)
-        T.append(targets(groups, share, classic))
-        C.append(classic)
-        desc.update({"groups": groups, "top_share": share, "classic": classic})
-        D.append(desc)
+        for feat, cl, kind in ((f, classic, "column"), (fb[0], float(cb[0]), "batch")):
+            X.append(feat)
+            T.append(targets(groups, share, cl))
+            C.append(cl)
+            d = dict(desc)
+            d.update({"groups": groups, "top_share": share, "classic": cl, "sketch": kind})
+            D.append(d)
         del keys
     return np.array(X, np.float32), np.array(T, np.float32), np.array(C), D
 
@@ -154,6 +163,13 @@ def main():
     e_learned = [log2_err(a, b) for a, b in zip(learned, true)]
     e_classic = [log2_err(a, b) for a, b in zip(Ch, true)]
     share_err = [abs(float(y[1]) - d["top_share"]) for y, d in zip(Y, Dh)]
+    by_kind = {}
+    for kind in ("column", "batch"):
+        idx = [i for i, d in enumerate(Dh) if d["sketch"] == kind]
+        by_kind[kind] = {"median_learned": float(np.median([e_learned[i] for i in idx])),
+                         "median_classic": float(np.median([e_classic[i] for i in idx])),
+                         "p90_learned": float(np.percentile([e_learned[i] for i in idx], 90)),
+                         "p90_classic": float(np.percentile([e_classic[i] for i in idx], 90))}
     report = {
         "datasets": args.datasets, "heldout": args.heldout, "epochs": args.epochs,
         "train_loss": losses, "data_s": t_data, "train_s": t_train,
@@ -162,6 +178,7 @@ def main():
         "heldout_p90_abs_log2_error": {"learned": float(np.percentile(e_learned, 90)),
                                        "classic": float(np.percentile(e_classic, 90))},
         "heldout_top_share_mae": float(np.mean(share_err)),
+        "heldout_by_sketch": by_kind,
     }
     print(json.dumps(report))
     if args.report:
