@@ -320,37 +320,44 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
       std::memcpy(bmap.data(), b.data(), b.size());
       std::memcpy(pmap.data(), p.data(), p.size());
     }
-    std::unordered_map<int64_t, std::vector<uint32_t>> by_key;  // join value -> group ids
+    // (join value, group id) of every build row with a non-NULL key, sorted by
+    // value: the group list of a probe value is one contiguous run.
+    std::vector<std::pair<int64_t, uint32_t>> by_key;
+    by_key.reserve(nb);
     for (uint64_t b = 0; b < nb; ++b) {
       if (!valid_at(bkw, bk_all, b)) continue;
       int64_t v = ival(bkv, bk.type, b);
-      if (kt == QEG_STR) v = bmap.at(static_cast<size_t>(v));
-      by_key[v].push_back(static_cast<uint32_t>(row_group[b]));
+      if (kt == QEG_STR) {
+        require(v >= 0 && static_cast<uint64_t>(v) < bmap.size(), "STR code outside its code map");
+        v = bmap[static_cast<size_t>(v)];
+      }
+      by_key.push_back({v, static_cast<uint32_t>(row_group[b])});
     }
+    std::stable_sort(by_key.begin(), by_key.end(),
+                     [](const std::pair<int64_t, uint32_t>& a, const std::pair<int64_t, uint32_t>& b) {
+                       return a.first < b.first;
+                     });
     // Probe-key domain: the probe dictionary (STR) or the build keys' range.
     int64_t kmin = 0;
     uint64_t domain = 0;
     if (kt == QEG_STR) {
       domain = pmap.size();
     } else if (!by_key.empty()) {
-      int64_t lo = INT64_MAX, hi = INT64_MIN;
-      for (auto& e : by_key) {
-        lo = std::min(lo, e.first);
-        hi = std::max(hi, e.first);
-      }
+      const int64_t lo = by_key.front().first, hi = by_key.back().first;
       require(static_cast<uint64_t>(hi - lo) < (1ull << 24),
               "integer join keys must span fewer than 2^24 values for the fused pipeline");
       kmin = lo;
       domain = static_cast<uint64_t>(hi - lo) + 1;
     }
     std::vector<uint32_t> kstart(std::max<uint64_t>(domain, 1), 0), kcount(std::max<uint64_t>(domain, 1), 0), glist;
+    glist.reserve(by_key.size());
     for (uint64_t s = 0; s < domain; ++s) {
       const int64_t v = kt == QEG_STR ? pmap[s] : kmin + static_cast<int64_t>(s);
-      auto it = by_key.find(v);
       kstart[s] = static_cast<uint32_t>(glist.size());
-      if (it == by_key.end()) continue;
-      kcount[s] = static_cast<uint32_t>(it->second.size());
-      glist.insert(glist.end(), it->second.begin(), it->second.end());
+      auto it = std::lower_bound(by_key.begin(), by_key.end(), v,
+                                 [](const std::pair<int64_t, uint32_t>& e, int64_t x) { return e.first < x; });
+      for (; it != by_key.end() && it->first == v; ++it) glist.push_back(it->second);
+      kcount[s] = static_cast<uint32_t>(glist.size() - kstart[s]);
     }
 
     // ---- aggregate fields over probe columns (the AggState encodings) ------
