@@ -187,24 +187,23 @@ __global__ void build_scatter_kernel(BuildK P) {
 
 // Dense build: sets one bit per key value; a bit that was already set means
 // the build keys are not unique.
+// Sets the bit of every non-NULL build key (fire-and-forget reductions; the
+// distinct count comes from a population count of the bitmap afterwards).
 __global__ void dense_mark_kernel(BuildK P, unsigned long long* __restrict__ bits) {
-  unsigned long long fresh = 0;
-  uint32_t dup = 0;
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
     if (!col_valid(P.key[0], r)) continue;
     const uint64_t s = static_cast<uint64_t>(dense_value(P.key[0], r) - P.T.dmin);
-    const unsigned long long bit = 1ull << (s & 63);
-    if (atomicOr(bits + (s >> 6), bit) & bit) dup = 1;
-    else ++fresh;
+    atomicOr(bits + (s >> 6), 1ull << (s & 63));
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    fresh += __shfl_down_sync(0xffffffffu, fresh, o);
-    dup |= __shfl_down_sync(0xffffffffu, dup, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (fresh) atomicAdd(P.distinct, fresh);
-    if (dup) *P.dup = 1;
-  }
+}
+
+// Number of set bits of `nw` words, added to *out.
+__global__ void popc_kernel(const unsigned long long* __restrict__ w, uint64_t nw, unsigned long long* out) {
+  unsigned long long c = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nw; i += (uint64_t)gridDim.x * blockDim.x)
+    c += __popcll(w[i]);
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
 // Range of the non-null values of one integer key column.
@@ -477,6 +476,134 @@ __global__ void __launch_bounds__(256, 4) probe_sink_pipe_kernel(const SinkK P) 
   }
   // Rows after the last full tile, one per thread.
   const uint64_t tail0 = ntiles * kTile;
+  for (uint64_t r = tail0 + static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < P.n;
+       r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const bool kv = !P.kvalid || ((P.kvalid[r >> 6] >> (r & 63)) & 1ull);
+    const uint64_t mm = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, keys[r]) : 0;
+    cnt += mm;
+    if (mm && (!P.vvalid || ((P.vvalid[r >> 6] >> (r & 63)) & 1ull))) {
+      sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r])) * mm;
+      seen = 1;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    seen |= __shfl_down_sync(0xffffffffu, seen, o);
+  }
+  __shared__ unsigned long long s_acc[3];
+  if (threadIdx.x == 0) s_acc[0] = s_acc[1] = s_acc[2] = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_acc[0], cnt);
+    atomicAdd(&s_acc[1], sum);
+    atomicOr(&s_acc[2], seen);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_acc[0]) atomicAdd(P.acc + 0, s_acc[0]);
+    if (s_acc[1]) atomicAdd(P.acc + 1, s_acc[1]);
+    if (s_acc[2]) atomicOr(P.acc + 2, s_acc[2]);
+  }
+}
+
+// cp.async-staged sink. Each warp streams its tiles of 128 rows through a
+// private ring of kAsyncStages shared-memory stages filled with 16-byte
+// cp.async copies (keys, payloads, and the two validity words per column), so
+// kAsyncStages - 1 tiles per warp are in flight without holding registers;
+// lane i then takes rows i, i+32, i+64, i+96 of the landed tile.
+constexpr int kAsyncStages = 4;
+constexpr int kAsyncTile = 128;
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+template <typename KT, typename VT>
+constexpr size_t async_stage_bytes() {
+  return kAsyncTile * sizeof(KT) + kAsyncTile * sizeof(VT) + 32;
+}
+
+template <typename KT, typename VT, int STRAT, bool UNIQUE>
+__global__ void __launch_bounds__(256) probe_sink_async_kernel(const SinkK P) {
+  extern __shared__ __align__(16) uint8_t async_smem[];
+  constexpr size_t KB = kAsyncTile * sizeof(KT), VB = kAsyncTile * sizeof(VT);
+  constexpr size_t SB = async_stage_bytes<KT, VT>();
+  unsigned long long cnt = 0, sum = 0, seen = 0;
+  const KT* keys = static_cast<const KT*>(P.key);
+  const VT* vals = static_cast<const VT*>(P.val);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned warp = threadIdx.x >> 5;
+  uint8_t* ring = async_smem + static_cast<size_t>(warp) * kAsyncStages * SB;
+  const uint64_t ntiles = P.n / kAsyncTile;
+  const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  const uint64_t first = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  auto issue = [&](uint64_t t, int st) {
+    uint8_t* sp = ring + st * SB;
+    const uint8_t* kg = reinterpret_cast<const uint8_t*>(keys + t * kAsyncTile);
+    const uint8_t* vg = reinterpret_cast<const uint8_t*>(vals + t * kAsyncTile);
+    for (unsigned c = lane; c < KB / 16; c += 32) cp_async16(sp + c * 16, kg + c * 16);
+    for (unsigned c = lane; c < VB / 16; c += 32) cp_async16(sp + KB + c * 16, vg + c * 16);
+    uint64_t* w = reinterpret_cast<uint64_t*>(sp + KB + VB);
+    if (lane < 2) {
+      if (P.kvalid) cp_async8(w + lane, P.kvalid + t * 2 + lane);
+      else w[lane] = ~0ull;
+    } else if (lane < 4) {
+      if (P.vvalid) cp_async8(w + lane, P.vvalid + t * 2 + (lane - 2));
+      else w[lane] = ~0ull;
+    }
+  };
+  // Prologue: the first kAsyncStages - 1 tiles of this warp.
+#pragma unroll
+  for (int st = 0; st < kAsyncStages - 1; ++st) {
+    const uint64_t t = first + st * nwarps;
+    if (t < ntiles) issue(t, st);
+    cp_async_commit();
+  }
+  int st = 0;
+  for (uint64_t t = first; t < ntiles; t += nwarps) {
+    const uint64_t tn = t + (kAsyncStages - 1) * nwarps;
+    if (tn < ntiles) issue(tn, (st + kAsyncStages - 1) % kAsyncStages);
+    cp_async_commit();
+    cp_async_wait<kAsyncStages - 1>();  // this thread's copies of tile t have landed
+    __syncwarp();                        // and every lane's
+    const uint8_t* sp = ring + st * SB;
+    const KT* sk = reinterpret_cast<const KT*>(sp);
+    const VT* sv = reinterpret_cast<const VT*>(sp + KB);
+    const uint64_t* w = reinterpret_cast<const uint64_t*>(sp + KB + VB);
+    uint64_t m[4];
+    VT v[4];
+    bool vok[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const unsigned r = lane + 32 * j;
+      const bool kok = (w[r >> 6] >> (r & 63)) & 1ull;
+      vok[j] = (w[2 + (r >> 6)] >> (r & 63)) & 1ull;
+      v[j] = sv[r];
+      m[j] = kok ? sink_lookup<KT, STRAT, UNIQUE>(P.T, sk[r]) : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      cnt += m[j];
+      if (m[j] && vok[j]) {
+        sum += static_cast<unsigned long long>(static_cast<int64_t>(v[j])) * m[j];
+        seen = 1;
+      }
+    }
+    __syncwarp();  // every lane is done with this stage before it is refilled
+    st = (st + 1) % kAsyncStages;
+  }
+  cp_async_wait<0>();
+  // Rows after the last full tile, one per thread.
+  const uint64_t tail0 = ntiles * kAsyncTile;
   for (uint64_t r = tail0 + static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; r < P.n;
        r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
     const bool kv = !P.kvalid || ((P.kvalid[r >> 6] >> (r & 63)) & 1ull);
@@ -950,15 +1077,17 @@ struct JoinState {
 
 namespace {
 
+// Validity bytes -> 64-bit LSB-first words: a warp turns 64 bytes into one
+// word with two ballots.
 __global__ void bytes_to_bits_kernel(const uint8_t* __restrict__ b, uint64_t n, uint64_t* __restrict__ w) {
   const uint64_t nw = (n + 63) / 64;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < nw; i += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t x = 0;
-    for (int k = 0; k < 64; ++k) {
-      const uint64_t r = i * 64 + k;
-      if (r < n && b[r]) x |= 1ull << k;
-    }
-    w[i] = x;
+  const unsigned lane = threadIdx.x & 31u;
+  const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t i = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; i < nw; i += nwarps) {
+    const uint64_t r = i * 64 + lane;
+    const unsigned lo = __ballot_sync(0xffffffffu, r < n && b[r]);
+    const unsigned hi = __ballot_sync(0xffffffffu, r + 32 < n && b[r + 32]);
+    if (lane == 0) w[i] = static_cast<uint64_t>(lo) | (static_cast<uint64_t>(hi) << 32);
   }
 }
 
@@ -972,7 +1101,7 @@ void JoinState::finish_build() {
   for (int j = 0; j < nk; ++j) {
     key_bits.emplace_back(((nbuild + 63) / 64 + 1) * 8, ctx->stream);
     if (nbuild) {
-      bytes_to_bits_kernel<<<grid_for(ctx, nbuild / 64 + 1, 256, 8), 256, 0, ctx->stream>>>(
+      bytes_to_bits_kernel<<<grid_for(ctx, (nbuild / 64 + 1) * 32, 256, 8), 256, 0, ctx->stream>>>(
           bvalid[bkeys[j]].get<uint8_t>(), nbuild, key_bits[j].get<uint64_t>());
       ctx->launches++;
     }
@@ -1020,7 +1149,10 @@ void JoinState::finish_build() {
     P.T = table();
     if (nbuild) {
       dense_mark_kernel<<<g, 256, 0, ctx->stream>>>(P, bitmap.get<unsigned long long>());
-      ctx->launches++;
+      const uint64_t nw = (cap + 63) / 64;
+      popc_kernel<<<grid_for(ctx, nw, 256, 8), 256, 0, ctx->stream>>>(bitmap.get<unsigned long long>(), nw,
+                                                                       P.distinct);
+      ctx->launches += 2;
       QEG_CUDA(cudaGetLastError());
     }
   } else {
@@ -1041,13 +1173,13 @@ void JoinState::finish_build() {
   QEG_CUDA(cudaMemcpyAsync(d, dup.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
   QEG_CUDA(cudaStreamSynchronize(ctx->stream));
   check_device_error(ctx);
-  unique = (d[0] & 0xffffffffull) ? 0 : 1;
   distinct = d[1];
+  // Dense: the keys are unique when every non-NULL key set its own bit.
+  unique = strategy == QEG_JOIN_DENSE ? (distinct == nonnull ? 1 : 0) : ((d[0] & 0xffffffffull) ? 0 : 1);
   if (strategy == QEG_JOIN_DENSE && !unique) count_dense();
   csr_built = false;
   acc.alloc(24, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(acc.get(), 0, 24, ctx->stream));
-  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 BuildK JoinState::build_params(DevBuf& scratch) {
@@ -1329,6 +1461,15 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       const int pipe = pipe_env ? atoi(pipe_env) : 2;
       const bool use_tma = n >= static_cast<uint64_t>(kTileRows) * ctx->sms * 2 && al16(S.kvalid) && al16(S.vvalid) &&
                            tma_env != nullptr && tma_env[0] == '1';
+      auto launch_async = [&](void (*kern)(SinkK), size_t sb) {
+        QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb)));
+        int per_sm = 0;
+        QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, sb));
+        const uint64_t want = (n / kAsyncTile + 7) / 8;
+        const unsigned grid = static_cast<unsigned>(
+            std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
+        kern<<<grid, 256, sb, ctx->stream>>>(S);
+      };
       auto launch_tma = [&](void (*kern)(SinkK, uint32_t*), size_t tile_bytes) {
         const size_t sb = tile_bytes * kStages;
         QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb)));
@@ -1342,6 +1483,12 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       else if (dense) launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_DENSE, false>, tb);                       \
       else if (st.unique) launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_HASH, true>, tb);                     \
       else launch_tma(probe_sink_tma_kernel<KT, VT, QEG_JOIN_HASH, false>, tb);                                   \
+    } else if (pipe == 8) {                                                                                        \
+      const size_t sb = async_stage_bytes<KT, VT>() * kAsyncStages * 8;                                            \
+      if (dense && st.unique) launch_async(probe_sink_async_kernel<KT, VT, QEG_JOIN_DENSE, true>, sb);            \
+      else if (dense) launch_async(probe_sink_async_kernel<KT, VT, QEG_JOIN_DENSE, false>, sb);                   \
+      else if (st.unique) launch_async(probe_sink_async_kernel<KT, VT, QEG_JOIN_HASH, true>, sb);                 \
+      else launch_async(probe_sink_async_kernel<KT, VT, QEG_JOIN_HASH, false>, sb);                               \
     } else if (pipe == 2) {                                                                                        \
       if (dense && st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, true, 2>);                    \
       else if (dense) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, false, 2>);                           \

@@ -151,14 +151,14 @@ def test_random_joins(ctx, seed):
 
 @pytest.mark.parametrize("strategy", [qeg.JOIN_AUTO, qeg.JOIN_HASH, qeg.JOIN_DENSE])
 @pytest.mark.parametrize("dup", [False, True])
-@pytest.mark.parametrize("kernel", ["default", "pipe0", "pipe4", "tma"])
+@pytest.mark.parametrize("kernel", ["default", "pipe0", "pipe4", "pipe8", "tma"])
 def test_count_sum_sink(ctx, strategy, dup, kernel, monkeypatch):
     """The 16M x 256M join workload's shape at 1/64 scale: unique (or
     duplicated) build keys, probe keys half hits and half from a disjoint
     range, 2% NULL keys on both sides, SUM over an int64 payload. `kernel`
     picks the sink kernel: the default (128-row pipelined warp tiles), the
-    4-rows-per-thread kernel, 256-row tiles, or the opt-in TMA-staged kernel
-    (each 2M-row half is large enough for it)."""
+    4-rows-per-thread kernel, 256-row tiles, the cp.async-staged kernel, or the
+    opt-in TMA-staged kernel (each 2M-row half is large enough for it)."""
     if kernel == "tma":
         monkeypatch.setenv("QEG_SINK_TMA", "1")
     elif kernel != "default":
