@@ -611,7 +611,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="join")
-    ap.add_argument("--strategy", default="auto", choices=["auto", "hash", "dense"])
+    ap.add_argument("--strategy", default="auto", choices=["auto", "hash", "dense", "partitioned"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
@@ -651,7 +651,8 @@ def main():
         run_pipeline_bench(args, dev, local)
         return
 
-    strat = {"auto": qeg.JOIN_AUTO, "hash": qeg.JOIN_HASH, "dense": qeg.JOIN_DENSE}[args.strategy]
+    strat = {"auto": qeg.JOIN_AUTO, "hash": qeg.JOIN_HASH, "dense": qeg.JOIN_DENSE,
+             "partitioned": qeg.JOIN_PARTITIONED}[args.strategy]
     W = JoinWorkload(dev, args.build_rows, args.probe_rows)
     ctx = qeg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -703,24 +704,26 @@ def main():
     peak, peak_kind = peaks()
     achieved = W.algorithmic_probe_bytes() / (probe_avg_ms / 1e3) / 1e9
 
-    # hash-strategy reference point on the same data (same step definition)
-    alt = None
+    # hash and radix-partitioned strategies on the same data (same step definition)
+    alts = {}
     if args.strategy == "auto":
-        tt = []
-        for i in range(3):
-            e = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), stream]
-            a0 = torch.cuda.Event(enable_timing=True)
-            a1 = torch.cuda.Event(enable_timing=True)
-            a0.record(stream)
-            W.run(qeg, ctx, qeg.JOIN_HASH, events=e)
-            a1.record(stream)
-            torch.cuda.synchronize()
-            if i:
-                tt.append((a0.elapsed_time(a1), e[0].elapsed_time(e[1])))
-        step = float(np.mean([x[0] for x in tt]))
-        pms = float(np.mean([x[1] for x in tt]))
-        alt = {"strategy": "hash", "value": W.rows() / (step / 1e3), "ms_per_step": step,
-               "probe_ms": pms, "probe_gbs": W.algorithmic_probe_bytes() / (pms / 1e3) / 1e9}
+        for name, sid in (("hash", qeg.JOIN_HASH), ("partitioned", qeg.JOIN_PARTITIONED)):
+            tt = []
+            for i in range(3):
+                e = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), stream]
+                a0 = torch.cuda.Event(enable_timing=True)
+                a1 = torch.cuda.Event(enable_timing=True)
+                a0.record(stream)
+                ares, _ = W.run(qeg, ctx, sid, events=e)
+                a1.record(stream)
+                torch.cuda.synchronize()
+                assert ares == res, (name, ares, res)
+                if i:
+                    tt.append((a0.elapsed_time(a1), e[0].elapsed_time(e[1])))
+            step = float(np.mean([x[0] for x in tt]))
+            pms = float(np.mean([x[1] for x in tt]))
+            alts[name] = {"strategy": name, "value": W.rows() / (step / 1e3), "ms_per_step": step,
+                          "probe_ms": pms, "probe_gbs": W.algorithmic_probe_bytes() / (pms / 1e3) / 1e9}
 
     e2e = None
     if not args.no_e2e:
@@ -768,8 +771,8 @@ def main():
             "clocks": clocks,
             "wall_s": wall,
         }
-        if alt:
-            out["hash_strategy"] = alt
+        for name, a in alts.items():
+            out[name + "_strategy"] = a
         print(json.dumps(out))
 
 

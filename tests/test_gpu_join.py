@@ -204,3 +204,59 @@ def test_count_sum_sparse_keys_use_hash(ctx):
     assert j.count_sum() == exp
     assert j.stats()["strategy"] == qeg.JOIN_HASH
     j.close()
+
+
+@pytest.mark.parametrize("dup", [False, True])
+@pytest.mark.parametrize("ktype", [O.I64, O.I32])
+@pytest.mark.parametrize("bits", [0, 6])
+def test_partitioned_count_sum_sink(ctx, dup, ktype, bits):
+    """The radix-partitioned join (probe and build split by key hash, one
+    shared-memory table per partition) against the oracle: unique or
+    duplicated build keys, NULL keys and payloads on both sides, 64-bit and
+    32-bit keys (negative values included), automatic or fixed partition
+    bits."""
+    rng = np.random.default_rng(500 + dup + 2 * (ktype == O.I32) + bits)
+    nb, npr = 1 << 17, (1 << 21) + 77
+    dt = np.int64 if ktype == O.I64 else np.int32
+    bkey = (rng.permutation(nb) - nb // 3).astype(dt)
+    if dup:
+        bkey = (bkey // 3).astype(dt)
+    bkey[:5] = 0  # key word 0 marks an empty slot: it must still join
+    bvalid = rng.random(nb) >= 0.02
+    hit = rng.random(npr) < 0.5
+    pkey = np.where(hit, bkey[rng.integers(0, nb, npr)], rng.integers(nb, 2 * nb, npr)).astype(dt)
+    pvalid = rng.random(npr) >= 0.02
+    pval = rng.integers(-(1 << 20), 1 << 20, npr).astype(np.int64)
+    vvalid = rng.random(npr) >= 0.05
+    exp = O.join_count_sum(O.TCol(ktype, pkey, pvalid), O.TCol(O.I64, pval, vvalid), O.TCol(ktype, bkey, bvalid))
+    j = qeg.Join(ctx, [ktype, O.I64], [ktype], [0], [0], strategy=qeg.JOIN_PARTITIONED, partition_bits=bits)
+    j.build([qeg.Col(bkey, qeg.pack_validity(bvalid))])
+    j.build_finish()
+    st = j.stats()
+    assert st["strategy"] == qeg.JOIN_PARTITIONED and st["partition_bits"] == (bits or st["partition_bits"]) > 0, st
+    j.probe_count_sum(qeg.Col(pkey, qeg.pack_validity(pvalid)), qeg.Col(pval, qeg.pack_validity(vvalid)))
+    got = j.count_sum()
+    j.close()
+    assert got == exp
+
+
+def test_partitioned_join_materialises_pairs(ctx):
+    """A materialising probe of a partitioned build falls back to the global
+    table and returns the oracle's rows."""
+    rng = np.random.default_rng(77)
+    nb, npr = 3000, 20000
+    bkey = rng.integers(-500, 500, nb).astype(np.int64)
+    pkey = rng.integers(-600, 600, npr).astype(np.int64)
+    pv = rng.integers(0, 100, npr).astype(np.int64)
+    probe = [O.TCol(O.I64, pkey), O.TCol(O.I64, pv)]
+    build = [O.TCol(O.I64, bkey)]
+    ot, orows = O.join(probe, build, [0], [0], O.INNER)
+    j = qeg.Join(ctx, [O.I64, O.I64], [O.I64], [0], [0], strategy=qeg.JOIN_PARTITIONED)
+    j.build([qeg.Col(bkey)])
+    j.build_finish()
+    assert j.stats()["strategy"] == qeg.JOIN_PARTITIONED
+    j.probe([qeg.Col(pkey), qeg.Col(pv)])
+    res = j.fetch()
+    j.close()
+    gt, grows = gpu_rows(res, ot)
+    assert_same(gt, grows, ot, orows, "partitioned join pairs")
