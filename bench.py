@@ -704,6 +704,22 @@ def main():
     peak, peak_kind = peaks()
     achieved = W.algorithmic_probe_bytes() / (probe_avg_ms / 1e3) / 1e9
 
+    e2e = None
+    if not args.no_e2e:
+        host = W.host_copy()
+        W.run(qeg, ctx, strat, host=host)
+        torch.cuda.synchronize()
+        n_e2e = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            r2, _ = W.run(qeg, ctx, strat, host=host)
+        ctx.synchronize()
+        dt = time.perf_counter() - t0
+        assert r2 == res
+        e2e = {"value": W.rows() / (dt / n_e2e), "unit": "rows/s", "h2d_bytes_per_step": W.h2d_bytes(),
+               "d2h_bytes_per_step": 24, "steps": n_e2e}
+        del host
+
     # hash and radix-partitioned strategies on the same data (same step definition)
     alts = {}
     if args.strategy == "auto":
@@ -724,22 +740,6 @@ def main():
             pms = float(np.mean([x[1] for x in tt]))
             alts[name] = {"strategy": name, "value": W.rows() / (step / 1e3), "ms_per_step": step,
                           "probe_ms": pms, "probe_gbs": W.algorithmic_probe_bytes() / (pms / 1e3) / 1e9}
-
-    e2e = None
-    if not args.no_e2e:
-        host = W.host_copy()
-        W.run(qeg, ctx, strat, host=host)
-        torch.cuda.synchronize()
-        n_e2e = max(1, min(args.steps, 3))
-        t0 = time.perf_counter()
-        for _ in range(n_e2e):
-            r2, _ = W.run(qeg, ctx, strat, host=host)
-        ctx.synchronize()
-        dt = time.perf_counter() - t0
-        assert r2 == res
-        e2e = {"value": W.rows() / (dt / n_e2e), "unit": "rows/s", "h2d_bytes_per_step": W.h2d_bytes(),
-               "d2h_bytes_per_step": 24, "steps": n_e2e}
-        del host
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -47,6 +47,7 @@ struct JTable {
   const uint32_t* rows;
   const uint64_t* bitmap;  // dense and unique: one bit per slot
   int unique;
+  int shift;  // hash, single key: home slot = hash >> shift (64 - log2 cap)
 };
 
 __device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t* p) {
@@ -79,7 +80,7 @@ __device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w,
   if (T.nkeys == 1) {
     const uint64_t k = w[0];
     if (k == 0) return static_cast<int64_t>(T.cap);
-    uint64_t s = h & (T.cap - 1);
+    uint64_t s = h >> T.shift;  // home slot: the top bits of the hash
     for (uint64_t t = 0; t < T.cap; ++t) {
       uint64_t* r = T.keys + s;
       uint64_t cur = ld_relaxed64(r);
@@ -270,7 +271,7 @@ __device__ __forceinline__ uint64_t sink_lookup(const JTable& T, KT key) {
     // Linear probing read four slots (one 32-byte sector) at a time: the
     // aligned group holding the home slot, then the following groups. Slots
     // before the home slot in the first group are not part of the probe.
-    const uint64_t home = single_key_hash(k) & (T.cap - 1);
+    const uint64_t home = single_key_hash(k) >> T.shift;
     uint64_t g = home & ~3ull;
     int skip = static_cast<int>(home & 3);
     const ulonglong2* base = reinterpret_cast<const ulonglong2*>(T.keys);
@@ -636,184 +637,130 @@ __global__ void __launch_bounds__(256) probe_sink_async_kernel(const SinkK P) {
 }
 
 // ---------------------------------------------------------------------------
-// Radix-partitioned COUNT/SUM join (QEG_JOIN_PARTITIONED). Build and probe
-// rows are split by the top `bits` bits of their key hash into P = 2^bits
-// partitions; then one CTA per partition loads its build keys into a
-// shared-memory hash table and streams its probe rows through it, so the
-// random table traffic of a large hashed build side stays on chip and HBM
-// sees only sequential passes (probe keys and payloads are read twice and
-// written once).
-//
-// Probe partitioning is a two-pass radix scatter: pass 1 histograms each
-// CTA's contiguous row range into counts[p][cta]; an exclusive scan of that
-// matrix gives every (partition, CTA) pair its output offset; pass 2 re-reads
-// the range and scatters (key, payload, payload validity) with shared-memory
-// cursors, so the hot loop has no global atomics. NULL probe keys never match
-// and are dropped.
+// Radix-partitioned COUNT/SUM join (QEG_JOIN_PARTITIONED). A single-key hash
+// table puts a key's home slot at the top bits of its hash, so the keys of
+// one hash partition (top `bits` bits) occupy one contiguous window of the
+// table. The probe side is split into those partitions in one pass (per CTA
+// tile: a shared-memory counting sort, one global reservation per partition,
+// then coalesced writes of each partition's run), and the ordinary sink then
+// streams the partitioned probe rows in order: at any moment the warps probe
+// a window of one or two partitions, whose slice of the table stays in L2
+// instead of every probe missing to HBM.
 // ---------------------------------------------------------------------------
+constexpr int kPartTile = 4096;  // probe rows per CTA tile of the scatter
+
 __device__ __forceinline__ uint32_t key_part(uint64_t k, int bits) {
   return static_cast<uint32_t>(single_key_hash(k) >> (64 - bits));
 }
-
-__global__ void bpart_hist_kernel(DevCol key, uint64_t n, int bits, unsigned int* __restrict__ hist) {
-  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
-    if (!col_valid(key, r)) continue;
-    atomicAdd(hist + key_part(key_word(key, r), bits), 1u);
-  }
-}
-
-__global__ void bpart_scatter_kernel(DevCol key, uint64_t n, int bits, unsigned long long* __restrict__ cursor,
-                                     uint64_t* __restrict__ out) {
-  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
-    if (!col_valid(key, r)) continue;
-    const uint64_t k = key_word(key, r);
-    out[atomicAdd(cursor + key_part(k, bits), 1ull)] = k;
-  }
-}
-
-struct PartK {
-  const void* key;
-  const uint64_t* kvalid;  // nullptr: no NULL keys
-  const void* val;
-  const uint64_t* vvalid;  // nullptr: no NULL payloads
-  uint64_t n;
-  uint64_t range;  // rows per CTA (a multiple of 64)
-  int bits;
-  uint32_t P, G;
-  unsigned int* counts;              // [P][G]
-  const unsigned long long* offs;    // exclusive scan of counts, P*G + 1 entries
-  uint64_t* okey;
-  uint64_t* oval;
-  uint8_t* ovalid;  // nullptr when the payload has no NULLs
-};
 
 template <typename KT>
 __device__ __forceinline__ uint64_t sink_word(KT k) {
   return sizeof(KT) == 4 ? static_cast<uint64_t>(static_cast<uint32_t>(k)) : static_cast<uint64_t>(k);
 }
 
+struct PartK {
+  const void* key;
+  const uint64_t* kvalid;  // nullptr: no NULL keys
+  const void* val;         // payloads (no NULLs on this path)
+  uint64_t n;
+  int bits;
+  unsigned long long* hist;    // [P] partition sizes (pass 1)
+  unsigned long long* cursor;  // [P] next free row of each partition (pass 2)
+  uint64_t* okey;              // key words, partition order
+  int64_t* oval;               // payloads, partition order
+};
+
+// Pass 1: partition sizes (shared-memory histogram per CTA, then reductions).
 template <typename KT>
 __global__ void __launch_bounds__(512) ppart_hist_kernel(const PartK P) {
   extern __shared__ unsigned int phist[];
-  for (uint32_t i = threadIdx.x; i < P.P; i += blockDim.x) phist[i] = 0;
+  const uint32_t np = 1u << P.bits;
+  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) phist[i] = 0;
   __syncthreads();
   const KT* keys = static_cast<const KT*>(P.key);
-  const uint64_t a = blockIdx.x * P.range, z = min(P.n, a + P.range);
-  for (uint64_t r = a + threadIdx.x; r < z; r += blockDim.x) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
     if (P.kvalid && !((__ldg(P.kvalid + (r >> 6)) >> (r & 63)) & 1ull)) continue;
     atomicAdd(phist + key_part(sink_word(__ldg(keys + r)), P.bits), 1u);
   }
   __syncthreads();
-  for (uint32_t i = threadIdx.x; i < P.P; i += blockDim.x) P.counts[static_cast<uint64_t>(i) * P.G + blockIdx.x] = phist[i];
+  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
+    if (phist[i]) atomicAdd(P.hist + i, static_cast<unsigned long long>(phist[i]));
 }
 
+// Pass 2: tiles of kPartTile rows are counting-sorted by partition in shared
+// memory, each partition's run reserved with one global atomic and written
+// contiguously. NULL keys are dropped (they never match).
 template <typename KT, typename VT>
 __global__ void __launch_bounds__(512) ppart_scatter_kernel(const PartK P) {
-  extern __shared__ unsigned long long pcur[];
-  for (uint32_t i = threadIdx.x; i < P.P; i += blockDim.x) pcur[i] = P.offs[static_cast<uint64_t>(i) * P.G + blockIdx.x];
-  __syncthreads();
+  extern __shared__ __align__(16) unsigned char pscratch[];
+  const uint32_t np = 1u << P.bits;
+  uint64_t* skey = reinterpret_cast<uint64_t*>(pscratch);                 // [kPartTile]
+  int64_t* sval = reinterpret_cast<int64_t*>(skey + kPartTile);           // [kPartTile]
+  uint16_t* spart = reinterpret_cast<uint16_t*>(sval + kPartTile);        // [kPartTile]
+  unsigned int* cnt = reinterpret_cast<unsigned int*>(spart + kPartTile); // [np]
+  unsigned int* loff = cnt + np;                                          // [np]
+  unsigned long long* gbase = reinterpret_cast<unsigned long long*>(loff + np + (np & 1));  // [np]
+  constexpr int kPer = kPartTile / 512;
   const KT* keys = static_cast<const KT*>(P.key);
   const VT* vals = static_cast<const VT*>(P.val);
-  const uint64_t a = blockIdx.x * P.range, z = min(P.n, a + P.range);
-  for (uint64_t r = a + threadIdx.x; r < z; r += blockDim.x) {
-    if (P.kvalid && !((__ldg(P.kvalid + (r >> 6)) >> (r & 63)) & 1ull)) continue;
-    const uint64_t k = sink_word(__ldg(keys + r));
-    const uint64_t pos = atomicAdd(pcur + key_part(k, P.bits), 1ull);
-    P.okey[pos] = k;
-    P.oval[pos] = static_cast<uint64_t>(static_cast<int64_t>(__ldg(vals + r)));
-    if (P.ovalid) P.ovalid[pos] = static_cast<uint8_t>((__ldg(P.vvalid + (r >> 6)) >> (r & 63)) & 1ull);
-  }
-}
-
-struct PartJoinK {
-  const uint64_t* bkeys;              // build keys in partition order
-  const unsigned long long* boff;     // [P + 1]
-  const uint64_t* pkeys;              // probe keys in partition order
-  const uint64_t* pvals;
-  const uint8_t* pvalid;              // nullptr: every payload valid
-  const unsigned long long* poffs;    // probe scan (partition p starts at poffs[p * G])
-  uint32_t G;
-  uint32_t slots;                     // shared table slots (power of two, >= 2 x the largest build partition)
-  unsigned long long* acc;            // [0] count, [1] sum, [2] any non-null payload matched
-};
-
-// One CTA per partition: build keys -> shared (key, count) table, then the
-// partition's probe rows look up their counts.
-__global__ void __launch_bounds__(512) ppart_join_kernel(const PartJoinK J) {
-  extern __shared__ unsigned long long ptab[];
-  unsigned int* pcnt = reinterpret_cast<unsigned int*>(ptab + J.slots);
-  __shared__ unsigned int zero_cnt;  // build rows whose key word is 0 (0 marks an empty slot)
-  __shared__ unsigned long long s_acc[3];
-  const uint32_t p = blockIdx.x;
-  const uint32_t mask = J.slots - 1;
-  for (uint32_t i = threadIdx.x; i < J.slots; i += blockDim.x) {
-    ptab[i] = 0;
-    pcnt[i] = 0;
-  }
-  if (threadIdx.x == 0) {
-    zero_cnt = 0;
-    s_acc[0] = s_acc[1] = s_acc[2] = 0;
-  }
-  __syncthreads();
-  for (uint64_t i = J.boff[p] + threadIdx.x; i < J.boff[p + 1]; i += blockDim.x) {
-    const uint64_t k = J.bkeys[i];
-    if (k == 0) {
-      atomicAdd(&zero_cnt, 1u);
-      continue;
-    }
-    uint32_t s = static_cast<uint32_t>(single_key_hash(k)) & mask;
-    for (uint32_t t = 0; t < J.slots; ++t) {  // the table is at most half full
-      const unsigned long long old = atomicCAS(ptab + s, 0ull, static_cast<unsigned long long>(k));
-      if (old == 0 || old == k) {
-        atomicAdd(pcnt + s, 1u);
-        break;
-      }
-      s = (s + 1) & mask;
-    }
-  }
-  __syncthreads();
-  unsigned long long cnt = 0, sum = 0, seen = 0;
-  const uint64_t a = J.poffs[static_cast<uint64_t>(p) * J.G], z = J.poffs[static_cast<uint64_t>(p + 1) * J.G];
-  for (uint64_t i = a + threadIdx.x; i < z; i += blockDim.x) {
-    const uint64_t k = J.pkeys[i];
-    uint64_t m = 0;
-    if (k == 0) {
-      m = zero_cnt;
-    } else {
-      uint32_t s = static_cast<uint32_t>(single_key_hash(k)) & mask;
-      for (uint32_t t = 0; t < J.slots; ++t) {
-        const unsigned long long c = ptab[s];
-        if (c == k) {
-          m = pcnt[s];
-          break;
-        }
-        if (c == 0) break;
-        s = (s + 1) & mask;
+  const uint64_t ntiles = (P.n + kPartTile - 1) / kPartTile;
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
+    uint64_t k[kPer];
+    int64_t v[kPer];
+    uint32_t part[kPer], rank[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const uint64_t r = t * kPartTile + j * 512 + threadIdx.x;
+      part[j] = 0xffffffffu;
+      if (r < P.n && (!P.kvalid || ((__ldg(P.kvalid + (r >> 6)) >> (r & 63)) & 1ull))) {
+        k[j] = sink_word(__ldg(keys + r));
+        v[j] = static_cast<int64_t>(__ldg(vals + r));
+        part[j] = key_part(k[j], P.bits);
+        rank[j] = atomicAdd(cnt + part[j], 1u);
       }
     }
-    if (m) {
-      cnt += m;
-      if (!J.pvalid || J.pvalid[i]) {
-        sum += J.pvals[i] * m;
-        seen = 1;
+    __syncthreads();
+    // Exclusive scan of the tile's partition counts (one thread per 32 bins,
+    // then a scan over the bins' totals by one warp).
+    if (threadIdx.x < 32) {
+      const uint32_t per = (np + 31) / 32;
+      const uint32_t a = threadIdx.x * per, z = min(np, a + per);
+      uint32_t sum = 0;
+      for (uint32_t i = a; i < z; ++i) sum += cnt[i];
+      uint32_t incl = sum;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (threadIdx.x >= static_cast<unsigned>(o)) incl += y;
+      }
+      uint32_t run = incl - sum;
+      for (uint32_t i = a; i < z; ++i) {
+        loff[i] = run;
+        run += cnt[i];
       }
     }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    sum += __shfl_down_sync(0xffffffffu, sum, o);
-    seen |= __shfl_down_sync(0xffffffffu, seen, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&s_acc[0], cnt);
-    atomicAdd(&s_acc[1], sum);
-    atomicOr(&s_acc[2], seen);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (s_acc[0]) atomicAdd(J.acc + 0, s_acc[0]);
-    if (s_acc[1]) atomicAdd(J.acc + 1, s_acc[1]);
-    if (s_acc[2]) atomicOr(J.acc + 2, s_acc[2]);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
+      if (cnt[i]) gbase[i] = atomicAdd(P.cursor + i, static_cast<unsigned long long>(cnt[i]));
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      if (part[j] != 0xffffffffu) {
+        const uint32_t pos = loff[part[j]] + rank[j];
+        skey[pos] = k[j];
+        sval[pos] = v[j];
+        spart[pos] = static_cast<uint16_t>(part[j]);
+      }
+    }
+    __syncthreads();
+    const uint32_t kept = loff[np - 1] + cnt[np - 1];
+    for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
+      const uint32_t p = spart[i];
+      const uint64_t o = gbase[p] + (i - loff[p]);
+      P.okey[o] = skey[i];
+      P.oval[o] = sval[i];
+    }
+    __syncthreads();
   }
 }
 
@@ -1167,10 +1114,8 @@ struct JoinState {
   int64_t dmin = 0;
   int unique = 1;
 
-  // radix-partitioned build (QEG_JOIN_PARTITIONED)
+  // radix-partitioned probe (QEG_JOIN_PARTITIONED)
   int part_bits = 0;
-  uint32_t part_slots = 0;  // shared table slots of the per-partition join
-  DevBuf bpart_keys, bpart_off;
 
   // last probe batch
   std::vector<StagedCol> probe_staged;
@@ -1183,7 +1128,11 @@ struct JoinState {
 
   JTable table() const {
     JTable T{};
-    T.strategy = strategy;
+    // A partitioned join probes the same global hash table.
+    T.strategy = strategy == QEG_JOIN_PARTITIONED ? QEG_JOIN_HASH : strategy;
+    int lg = 0;
+    while ((1ull << lg) < cap && lg < 63) ++lg;
+    T.shift = 64 - lg;
     T.nkeys = static_cast<int>(bkeys.size());
     T.kw = bkeys.size() == 1 ? 1 : 1 + static_cast<int>(bkeys.size());
     T.keys = keys.get<uint64_t>();
@@ -1250,8 +1199,6 @@ struct JoinState {
 
   void finish_build();
   void build_hash(BuildK& P);
-  bool build_partitioned();
-  void ensure_hash();
   uint64_t slots() const {
     return strategy == QEG_JOIN_DENSE ? cap : (bkeys.size() == 1 ? cap + 1 : cap);
   }
@@ -1302,9 +1249,8 @@ void JoinState::finish_build() {
   P.n = nbuild;
   P.err = static_cast<uint32_t*>(ctx->dev_err.get());
 
-  // Strategy: dense when one integer key spans a small range; otherwise the
-  // radix-partitioned join for a single key whose hashed table would not fit
-  // in L2 (or when asked for), else one global hash table.
+  // Strategy: dense when one integer key spans a small range; otherwise one
+  // global hash table, or the radix-partitioned join when asked for.
   strategy = QEG_JOIN_HASH;
   nonnull = nbuild;
   if (nk == 1 && dense_capable(btypes[bkeys[0]]) && nbuild > 0 &&
@@ -1328,15 +1274,6 @@ void JoinState::finish_build() {
     }
     if (strategy != QEG_JOIN_DENSE && cfg.strategy == QEG_JOIN_DENSE) strategy = QEG_JOIN_HASH;
   }
-  if (strategy != QEG_JOIN_DENSE && nk == 1 && nbuild > 0 &&
-      (cfg.strategy == QEG_JOIN_PARTITIONED || (cfg.strategy == QEG_JOIN_AUTO && nbuild >= (1ull << 22)))) {
-    if (build_partitioned()) {
-      csr_built = false;
-      acc.alloc(24, ctx->stream);
-      QEG_CUDA(cudaMemsetAsync(acc.get(), 0, 24, ctx->stream));
-      return;
-    }
-  }
   DevBuf dup(16, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(dup.get(), 0, 16, ctx->stream));
   P.dup = dup.get<uint32_t>();
@@ -1357,6 +1294,11 @@ void JoinState::finish_build() {
     }
   } else {
     build_hash(P);
+  }
+  // The radix-partitioned join probes the same table (single key only).
+  if (strategy == QEG_JOIN_HASH && nk == 1 && cfg.strategy == QEG_JOIN_PARTITIONED) {
+    strategy = QEG_JOIN_PARTITIONED;
+    part_bits = cfg.partition_bits > 0 ? std::min(cfg.partition_bits, 12) : 8;
   }
   uint64_t d[2] = {0, 0};
   QEG_CUDA(cudaMemcpyAsync(d, dup.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1388,127 +1330,73 @@ void JoinState::build_hash(BuildK& P) {
   }
 }
 
-// The radix-partitioned build: the non-NULL build key words in partition
-// order and the partition offsets. Returns false (nothing kept) when the
-// largest partition would not fit a shared-memory table.
-bool JoinState::build_partitioned() {
-  const DevCol key = store_key(0);
-  int bits = cfg.partition_bits;
-  if (bits <= 0) {
-    // About 2048 build keys per partition.
-    bits = 1;
-    while (bits < 14 && (nbuild >> bits) > 2048) ++bits;
-  }
-  bits = std::min(std::max(bits, 1), 14);
-  const uint32_t P = 1u << bits;
-  DevBuf hist(static_cast<size_t>(P) * 4, ctx->stream), offs((static_cast<size_t>(P) + 1) * 8, ctx->stream);
-  QEG_CUDA(cudaMemsetAsync(hist.get(), 0, hist.bytes(), ctx->stream));
-  bpart_hist_kernel<<<grid_for(ctx, nbuild, 256, 8), 256, 0, ctx->stream>>>(key, nbuild, bits, hist.get<unsigned int>());
-  const uint64_t total = exclusive_scan(ctx, hist.get<uint32_t>(), P, offs.get<uint64_t>());
-  std::vector<unsigned long long> h(P + 1);
-  QEG_CUDA(cudaMemcpyAsync(h.data(), offs.get(), (P + 1) * 8, cudaMemcpyDeviceToHost, ctx->stream));
-  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
-  uint64_t largest = 0;
-  for (uint32_t i = 0; i < P; ++i) largest = std::max<uint64_t>(largest, h[i + 1] - h[i]);
-  const uint64_t slots = std::max<uint64_t>(1024, next_pow2(2 * std::max<uint64_t>(largest, 1)));
-  if (slots > 8192) return false;  // 8192 x 12 B of shared memory per partition at most
-  DevBuf cursor(static_cast<size_t>(P) * 8, ctx->stream);
-  QEG_CUDA(cudaMemcpyAsync(cursor.get(), offs.get(), static_cast<size_t>(P) * 8, cudaMemcpyDeviceToDevice, ctx->stream));
-  bpart_keys.alloc(std::max<uint64_t>(total, 1) * 8, ctx->stream);
-  bpart_scatter_kernel<<<grid_for(ctx, nbuild, 256, 8), 256, 0, ctx->stream>>>(
-      key, nbuild, bits, cursor.get<unsigned long long>(), bpart_keys.get<uint64_t>());
-  bpart_off = std::move(offs);
-  QEG_CUDA(cudaStreamSynchronize(ctx->stream));  // cursor dies with this scope
-  ctx->launches += 2;
-  QEG_CUDA(cudaGetLastError());
-  check_device_error(ctx);
-  strategy = QEG_JOIN_PARTITIONED;
-  part_bits = bits;
-  part_slots = static_cast<uint32_t>(slots);
-  nonnull = total;
-  distinct = total;  // an upper bound: only the per-partition tables see duplicates
-  unique = 0;
-  return true;
-}
-
-// Builds the global hash table for operations other than the COUNT/SUM sink
-// of a partitioned join.
-void JoinState::ensure_hash() {
-  if (strategy != QEG_JOIN_PARTITIONED) return;
-  strategy = QEG_JOIN_HASH;
-  DevBuf scratch;
-  BuildK P = build_params(scratch);
-  build_hash(P);
-  uint64_t d[2] = {0, 0};
-  QEG_CUDA(cudaMemcpyAsync(d, scratch.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
-  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
-  check_device_error(ctx);
-  distinct = d[1];
-  unique = (d[0] & 0xffffffffull) ? 0 : 1;
-  csr_built = false;
-}
-
-// COUNT/SUM sink of a partitioned join: probe partitioning (histogram, scan,
-// scatter), then one CTA per partition (ppart_join_kernel).
+// COUNT/SUM sink of a partitioned join: the probe side split by partition
+// (histogram, scan, tile-sorted scatter), then the ordinary hashed sink over
+// the partitioned rows in order.
 template <typename KT, typename VT>
-void partitioned_sink(JoinState& st, const DevCol& key, const DevCol& val, uint64_t n) {
+void partitioned_sink(JoinState& st, const DevCol& key, const DevCol& val, uint64_t n, SinkK S,
+                      void (*sink)(SinkK)) {
   qeg_ctx* ctx = st.ctx;
-  const uint32_t Pn = 1u << st.part_bits;
-  const uint32_t G = static_cast<uint32_t>(std::max<uint64_t>(1, std::min<uint64_t>(ctx->sms * 2ull, (n + 4095) / 4096)));
-  uint64_t range = (n + G - 1) / G;
-  range = (range + 63) & ~63ull;
+  const uint32_t np = 1u << st.part_bits;
   PartK K{};
   K.key = key.data;
   K.kvalid = key.all_valid ? nullptr : key.validity;
   K.val = val.data;
-  K.vvalid = val.all_valid ? nullptr : val.validity;
   K.n = n;
-  K.range = range;
   K.bits = st.part_bits;
-  K.P = Pn;
-  K.G = G;
-  DevBuf counts(static_cast<size_t>(Pn) * G * 4, ctx->stream), offs((static_cast<size_t>(Pn) * G + 1) * 8, ctx->stream);
-  K.counts = counts.get<unsigned int>();
-  const size_t hb = static_cast<size_t>(Pn) * 4, cb = static_cast<size_t>(Pn) * 8;
-  require(cb <= ctx->smem_optin, "too many join partitions for the shared-memory cursors");
-  if (hb > 48 * 1024)
-    QEG_CUDA(cudaFuncSetAttribute(ppart_hist_kernel<KT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hb));
-  if (cb > 48 * 1024)
-    QEG_CUDA(cudaFuncSetAttribute(ppart_scatter_kernel<KT, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cb));
-  ppart_hist_kernel<KT><<<G, 512, hb, ctx->stream>>>(K);
-  const uint64_t total = exclusive_scan(ctx, K.counts, static_cast<uint64_t>(Pn) * G, offs.get<uint64_t>());
-  K.offs = offs.get<unsigned long long>();
+  DevBuf hist(static_cast<size_t>(np) * 8, ctx->stream), cursor((static_cast<size_t>(np) + 1) * 8, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(hist.get(), 0, hist.bytes(), ctx->stream));
+  K.hist = hist.get<unsigned long long>();
+  const size_t hb = static_cast<size_t>(np) * 4;
+  ppart_hist_kernel<KT><<<grid_for(ctx, n, 512, 4), 512, hb, ctx->stream>>>(K);
+  // Partition starts: an exclusive scan of the sizes (tiny, on the host).
+  std::vector<unsigned long long> h(np), c(np + 1);
+  QEG_CUDA(cudaMemcpyAsync(h.data(), hist.get(), np * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  c[0] = 0;
+  for (uint32_t i = 0; i < np; ++i) c[i + 1] = c[i] + h[i];
+  const uint64_t total = c[np];
+  QEG_CUDA(cudaMemcpyAsync(cursor.get(), c.data(), (np + 1) * 8, cudaMemcpyHostToDevice, ctx->stream));
+  K.cursor = cursor.get<unsigned long long>();
   DevBuf okey(std::max<uint64_t>(total, 1) * 8, ctx->stream), oval(std::max<uint64_t>(total, 1) * 8, ctx->stream);
-  DevBuf ovalid;
-  if (K.vvalid) ovalid.alloc(std::max<uint64_t>(total, 1), ctx->stream);
   K.okey = okey.get<uint64_t>();
-  K.oval = oval.get<uint64_t>();
-  K.ovalid = K.vvalid ? ovalid.get<uint8_t>() : nullptr;
-  ppart_scatter_kernel<KT, VT><<<G, 512, cb, ctx->stream>>>(K);
-  PartJoinK J{};
-  J.bkeys = st.bpart_keys.get<uint64_t>();
-  J.boff = st.bpart_off.get<unsigned long long>();
-  J.pkeys = K.okey;
-  J.pvals = K.oval;
-  J.pvalid = K.ovalid;
-  J.poffs = K.offs;
-  J.G = G;
-  J.slots = st.part_slots;
-  J.acc = st.acc.get<unsigned long long>();
-  const size_t jb = static_cast<size_t>(J.slots) * 12;
-  if (jb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(ppart_join_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jb));
-  ppart_join_kernel<<<Pn, 512, jb, ctx->stream>>>(J);
+  K.oval = oval.get<int64_t>();
+  const size_t sb = static_cast<size_t>(kPartTile) * 18 + static_cast<size_t>(np) * 16 + 16;
+  QEG_CUDA(cudaFuncSetAttribute(ppart_scatter_kernel<KT, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+  int per_sm = 1;
+  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppart_scatter_kernel<KT, VT>, 512, sb));
+  const uint64_t ntiles = (n + kPartTile - 1) / kPartTile;
+  const unsigned g = static_cast<unsigned>(
+      std::max<uint64_t>(1, std::min<uint64_t>(ntiles, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
+  ppart_scatter_kernel<KT, VT><<<g, 512, sb, ctx->stream>>>(K);
+  // The partitioned rows: 64-bit key words and payloads, no NULL keys.
+  S.key = K.okey;
+  S.kvalid = nullptr;
+  S.val = K.oval;
+  S.vvalid = nullptr;
+  S.n = total;
+  if (total) {
+    int sink_per_sm = 0;
+    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sink_per_sm, sink, 256, 0));
+    const uint64_t want = (total / 8 + 255) / 256;
+    const unsigned gs = static_cast<unsigned>(std::max<uint64_t>(
+        1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(sink_per_sm, 1))));
+    sink<<<gs, 256, 0, ctx->stream>>>(S);
+  }
   ctx->launches += 3;
   QEG_CUDA(cudaGetLastError());
   QEG_CUDA(cudaStreamSynchronize(ctx->stream));  // the partition buffers die with this scope
 }
 
-void probe_count_sum_partitioned(JoinState& st, const DevCol& key, const DevCol& val, uint64_t n) {
+void probe_count_sum_partitioned(JoinState& st, const DevCol& key, const DevCol& val, uint64_t n, const SinkK& S) {
   const bool k8 = type_width(key.type) == 8, v8 = type_width(val.type) == 8;
-  if (k8 && v8) partitioned_sink<long long, long long>(st, key, val, n);
-  else if (k8) partitioned_sink<long long, int>(st, key, val, n);
-  else if (v8) partitioned_sink<int, long long>(st, key, val, n);
-  else partitioned_sink<int, int>(st, key, val, n);
+  // The partitioned rows are 64-bit key words and payloads.
+  void (*sink)(SinkK) = st.unique ? probe_sink_pipe_kernel<long long, long long, QEG_JOIN_HASH, true, 2>
+                                  : probe_sink_pipe_kernel<long long, long long, QEG_JOIN_HASH, false, 2>;
+  if (k8 && v8) partitioned_sink<long long, long long>(st, key, val, n, S, sink);
+  else if (k8) partitioned_sink<long long, int>(st, key, val, n, S, sink);
+  else if (v8) partitioned_sink<int, long long>(st, key, val, n, S, sink);
+  else partitioned_sink<int, int>(st, key, val, n, S, sink);
 }
 
 BuildK JoinState::build_params(DevBuf& scratch) {
@@ -1654,7 +1542,6 @@ qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64
     JoinState& st = j->st;
     require(st.built, "probe() before build_finish()");
     validate_probe(st, cols, ncols);
-    st.ensure_hash();  // pairs come from the global table
     QEG_CUDA(cudaSetDevice(ctx->device));
     const uint64_t n = cols[0].len;
     require(n < 0xffffffffull, "a probe batch holds at most 2^32-2 rows");
@@ -1757,12 +1644,6 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
     const bool vfast = vt == QEG_I32 || vt == QEG_I64 || vt == QEG_TS;
     const bool aligned = (reinterpret_cast<uintptr_t>(k.dev.data) % 16 == 0) &&
                          (reinterpret_cast<uintptr_t>(v.dev.data) % 16 == 0);
-    if (st.strategy == QEG_JOIN_PARTITIONED && kfast && vfast) {
-      probe_count_sum_partitioned(st, k.dev, v.dev, n);
-      return;
-    }
-    st.ensure_hash();
-    P.T = st.table();
     if (kfast && vfast && aligned) {
       SinkK S{};
       S.key = k.dev.data;
@@ -1772,6 +1653,12 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       S.n = n;
       S.T = st.table();
       S.acc = st.acc.get<unsigned long long>();
+      if (st.strategy == QEG_JOIN_PARTITIONED && v.dev.all_valid) {
+        // (Payload NULLs would need a partitioned validity column: the direct
+        // hashed sink below handles them.)
+        probe_count_sum_partitioned(st, k.dev, v.dev, n, S);
+        return;
+      }
       const bool k8 = type_width(kt) == 8, v8 = type_width(vt) == 8, dense = st.strategy == QEG_JOIN_DENSE;
       // One wave of resident blocks; each thread strides over the probe side.
       auto launch = [&](void (*kern)(SinkK)) {

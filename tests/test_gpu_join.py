@@ -209,13 +209,14 @@ def test_count_sum_sparse_keys_use_hash(ctx):
 @pytest.mark.parametrize("dup", [False, True])
 @pytest.mark.parametrize("ktype", [O.I64, O.I32])
 @pytest.mark.parametrize("bits", [0, 6])
-def test_partitioned_count_sum_sink(ctx, dup, ktype, bits):
-    """The radix-partitioned join (probe and build split by key hash, one
-    shared-memory table per partition) against the oracle: unique or
-    duplicated build keys, NULL keys and payloads on both sides, 64-bit and
-    32-bit keys (negative values included), automatic or fixed partition
-    bits."""
-    rng = np.random.default_rng(500 + dup + 2 * (ktype == O.I32) + bits)
+@pytest.mark.parametrize("vnulls", [False, True])
+def test_partitioned_count_sum_sink(ctx, dup, ktype, bits, vnulls):
+    """The radix-partitioned join (the probe side split by key-hash partition
+    in one tile-sorted pass, then probed in partition order against the hash
+    table) against the oracle: unique or duplicated build keys, NULL keys on
+    both sides, 64-bit and 32-bit keys (negative values included), automatic
+    or fixed partition bits; with payload NULLs the direct hashed sink runs."""
+    rng = np.random.default_rng(500 + dup + 2 * (ktype == O.I32) + bits + 7 * vnulls)
     nb, npr = 1 << 17, (1 << 21) + 77
     dt = np.int64 if ktype == O.I64 else np.int32
     bkey = (rng.permutation(nb) - nb // 3).astype(dt)
@@ -227,22 +228,23 @@ def test_partitioned_count_sum_sink(ctx, dup, ktype, bits):
     pkey = np.where(hit, bkey[rng.integers(0, nb, npr)], rng.integers(nb, 2 * nb, npr)).astype(dt)
     pvalid = rng.random(npr) >= 0.02
     pval = rng.integers(-(1 << 20), 1 << 20, npr).astype(np.int64)
-    vvalid = rng.random(npr) >= 0.05
+    vvalid = (rng.random(npr) >= 0.05) if vnulls else np.ones(npr, bool)
     exp = O.join_count_sum(O.TCol(ktype, pkey, pvalid), O.TCol(O.I64, pval, vvalid), O.TCol(ktype, bkey, bvalid))
     j = qeg.Join(ctx, [ktype, O.I64], [ktype], [0], [0], strategy=qeg.JOIN_PARTITIONED, partition_bits=bits)
     j.build([qeg.Col(bkey, qeg.pack_validity(bvalid))])
     j.build_finish()
     st = j.stats()
     assert st["strategy"] == qeg.JOIN_PARTITIONED and st["partition_bits"] == (bits or st["partition_bits"]) > 0, st
-    j.probe_count_sum(qeg.Col(pkey, qeg.pack_validity(pvalid)), qeg.Col(pval, qeg.pack_validity(vvalid)))
+    j.probe_count_sum(qeg.Col(pkey, qeg.pack_validity(pvalid)),
+                      qeg.Col(pval, qeg.pack_validity(vvalid) if vnulls else None))
     got = j.count_sum()
     j.close()
     assert got == exp
 
 
 def test_partitioned_join_materialises_pairs(ctx):
-    """A materialising probe of a partitioned build falls back to the global
-    table and returns the oracle's rows."""
+    """A materialising probe of a partitioned join uses the global table and
+    returns the oracle's rows."""
     rng = np.random.default_rng(77)
     nb, npr = 3000, 20000
     bkey = rng.integers(-500, 500, nb).astype(np.int64)
