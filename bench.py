@@ -40,6 +40,20 @@ SEED = 20260615
 SINK_TRAFFIC_PER_ROW = (1082.670e6 + 3.291e6) / (1 << 26)
 
 
+def replica_throughput(total_ms, rows_per_rank, steps, world, device):
+    """Replicas only: every rank runs the whole workload on its own GPU. The
+    job's time is the slowest rank's (an all-reduce MAX over the ranks; the
+    only collective, outside the data path) and its throughput counts the rows
+    of every rank: (max ms, rows/s)."""
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([float(total_ms)], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, rows_per_rank * steps * world / (total_ms / 1e3)
+
+
 def peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -262,6 +276,8 @@ def run_agg_bench(args, dev, local):
     if args.variants:
         variants = {k: v for k, v in variants.items() if k in args.variants.split(",")}
     out = {}
+    clk = ClockSampler(local).__enter__()
+    tw0 = time.time()
     for name, cfg in variants.items():
         for _ in range(args.warmup):
             W.run(qeg, ctx, cfg)
@@ -278,6 +294,8 @@ def run_agg_bench(args, dev, local):
         out[name] = {"ms_per_step": ms, "rows_per_s": W.n / (ms / 1e3), "groups": n, "stats": st,
                      "gb_per_s": W.n * W.row_bytes / (ms / 1e3) / 1e9,
                      "launches_per_step": (ctx.launches - launches0) / args.steps}
+    clocks = clk.summary(tw0, time.time())
+    clk.__exit__(None, None, None)
     cpu = None
     if not args.no_cpu:
         cpu = cpu_agg_baseline(W, os.cpu_count() or 1)
@@ -292,6 +310,8 @@ def run_agg_bench(args, dev, local):
                      "unit": "GB/s", "frac": best["gb_per_s"] / peak},
         "variants": out,
         "cpu_baseline": cpu,
+        "gpu_launches": out[next(iter(out))]["launches_per_step"] if out else None,
+        "clocks": clocks,
         "learned_vs_plain": (out["plain_fixed"]["ms_per_step"] / best["ms_per_step"]
                              if "plain_fixed" in out else None),
     }))
@@ -690,17 +710,10 @@ def main():
     clk.__exit__(None, None, None)
     barrier()
     launches = ctx.launches - launches0
-    total_ms = step_ev[0].elapsed_time(step_ev[1])
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, value = replica_throughput(step_ev[0].elapsed_time(step_ev[1]), W.rows(), args.steps, world, dev)
     kms = [a.elapsed_time(b) for a, b, _ in probe_ms]
     probe_avg_ms = float(np.mean(kms))
     ms_per_step = total_ms / args.steps
-    value = W.rows() * args.steps * world / (total_ms / 1e3)
     peak, peak_kind = peaks()
     achieved = W.algorithmic_probe_bytes() / (probe_avg_ms / 1e3) / 1e9
 
