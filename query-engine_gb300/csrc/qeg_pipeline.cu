@@ -320,10 +320,12 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
       std::memcpy(bmap.data(), b.data(), b.size());
       std::memcpy(pmap.data(), p.data(), p.size());
     }
-    // (join value, group id) of every build row with a non-NULL key, sorted by
-    // value: the group list of a probe value is one contiguous run.
-    std::vector<std::pair<int64_t, uint32_t>> by_key;
-    by_key.reserve(nb);
+    // (join value, group id) of every build row with a non-NULL key.
+    std::vector<int64_t> bval;
+    std::vector<uint32_t> bgrp;
+    bval.reserve(nb);
+    bgrp.reserve(nb);
+    int64_t vmin = INT64_MAX, vmax = INT64_MIN;
     for (uint64_t b = 0; b < nb; ++b) {
       if (!valid_at(bkw, bk_all, b)) continue;
       int64_t v = ival(bkv, bk.type, b);
@@ -331,33 +333,41 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
         require(v >= 0 && static_cast<uint64_t>(v) < bmap.size(), "STR code outside its code map");
         v = bmap[static_cast<size_t>(v)];
       }
-      by_key.push_back({v, static_cast<uint32_t>(row_group[b])});
+      bval.push_back(v);
+      bgrp.push_back(static_cast<uint32_t>(row_group[b]));
+      vmin = std::min(vmin, v);
+      vmax = std::max(vmax, v);
     }
-    std::stable_sort(by_key.begin(), by_key.end(),
-                     [](const std::pair<int64_t, uint32_t>& a, const std::pair<int64_t, uint32_t>& b) {
-                       return a.first < b.first;
-                     });
     // Probe-key domain: the probe dictionary (STR) or the build keys' range.
     int64_t kmin = 0;
     uint64_t domain = 0;
     if (kt == QEG_STR) {
       domain = pmap.size();
-    } else if (!by_key.empty()) {
-      const int64_t lo = by_key.front().first, hi = by_key.back().first;
-      require(static_cast<uint64_t>(hi - lo) < (1ull << 24),
+    } else if (!bval.empty()) {
+      require(static_cast<uint64_t>(vmax - vmin) < (1ull << 24),
               "integer join keys must span fewer than 2^24 values for the fused pipeline");
-      kmin = lo;
-      domain = static_cast<uint64_t>(hi - lo) + 1;
+      kmin = vmin;
+      domain = static_cast<uint64_t>(vmax - vmin) + 1;
     }
-    std::vector<uint32_t> kstart(std::max<uint64_t>(domain, 1), 0), kcount(std::max<uint64_t>(domain, 1), 0), glist;
-    glist.reserve(by_key.size());
+    // Counting sort of the build rows by join value (values span < 2^24, STR
+    // value ids are dense): glist holds the group ids value by value, and a
+    // probe key's run is [vstart[v], vstart[v] + vcount[v]).
+    const uint64_t vrange = bval.empty() ? 0 : static_cast<uint64_t>(vmax - vmin) + 1;
+    require(vrange < (1ull << 26), "join key values span too many values for the fused pipeline");
+    std::vector<uint32_t> vstart(vrange + 1, 0), glist(bval.size());
+    for (int64_t v : bval) ++vstart[static_cast<size_t>(v - vmin) + 1];
+    for (uint64_t i = 0; i < vrange; ++i) vstart[i + 1] += vstart[i];
+    {
+      std::vector<uint32_t> fill(vstart.begin(), vstart.end() - 1);
+      for (size_t i = 0; i < bval.size(); ++i) glist[fill[static_cast<size_t>(bval[i] - vmin)]++] = bgrp[i];
+    }
+    std::vector<uint32_t> kstart(std::max<uint64_t>(domain, 1), 0), kcount(std::max<uint64_t>(domain, 1), 0);
     for (uint64_t s = 0; s < domain; ++s) {
       const int64_t v = kt == QEG_STR ? pmap[s] : kmin + static_cast<int64_t>(s);
-      kstart[s] = static_cast<uint32_t>(glist.size());
-      auto it = std::lower_bound(by_key.begin(), by_key.end(), v,
-                                 [](const std::pair<int64_t, uint32_t>& e, int64_t x) { return e.first < x; });
-      for (; it != by_key.end() && it->first == v; ++it) glist.push_back(it->second);
-      kcount[s] = static_cast<uint32_t>(glist.size() - kstart[s]);
+      if (v < vmin || v > vmax) continue;
+      const size_t i = static_cast<size_t>(v - vmin);
+      kstart[s] = vstart[i];
+      kcount[s] = vstart[i + 1] - vstart[i];
     }
 
     // ---- aggregate fields over probe columns (the AggState encodings) ------
@@ -547,6 +557,23 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
     }
     require(out <= out_capacity, "output capacity too small for the groups");
     for (int c = 0; c < ncol; ++c) {
+      const qeg_out_column& oc = outs[c];
+      if ((!oc.data || !is_device_ptr(oc.data)) && (!oc.validity || !is_device_ptr(oc.validity))) {
+        // Host outputs: write the (few) group rows directly.
+        if (oc.data && out) std::memcpy(oc.data, vals[c].data(), vals[c].size());
+        bool all = true;
+        const uint64_t nw = (out + 63) / 64;
+        std::vector<uint64_t> words(nw, ~0ull);  // padding bits set, as in the column format
+        for (uint64_t i = 0; i < out; ++i) {
+          if (!ok[c][i]) {
+            words[i >> 6] &= ~(1ull << (i & 63));
+            all = false;
+          }
+        }
+        if (oc.validity && nw) std::memcpy(oc.validity, words.data(), nw * 8);
+        if (oc.all_valid) *oc.all_valid = all ? 1 : 0;
+        continue;
+      }
       DevBuf dv(std::max<size_t>(vals[c].size(), 8), ctx->stream), dok(std::max<uint64_t>(out, 1), ctx->stream);
       if (out) {
         QEG_CUDA(cudaMemcpyAsync(dv.get(), vals[c].data(), vals[c].size(), cudaMemcpyHostToDevice, ctx->stream));
