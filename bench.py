@@ -204,9 +204,11 @@ class JoinWorkload:
 def zipf_keys(n, domain, s, g, dev, chunk=1 << 25):
     """n keys with an exact discrete Zipf(s) rank distribution over `domain`
     values (inverse-CDF sampling), mapped through a seeded permutation so hot
-    keys are spread over the key space."""
-    cdf = torch.arange(1, domain + 1, dtype=torch.float64, device=dev).pow_(-s).cumsum_(0)
-    cdf /= cdf[-1].clone()
+    keys are spread over the key space. The CDF is summed on the host: a
+    parallel float scan on the device may associate differently from run to
+    run, which moves a few samples across rank boundaries."""
+    cdf = torch.arange(1, domain + 1, dtype=torch.float64).pow_(-s).cumsum_(0)
+    cdf = (cdf / cdf[-1]).to(dev)
     perm = torch.randperm(domain, generator=g, device=dev, dtype=torch.int64)
     out = torch.empty(n, dtype=torch.int64, device=dev)
     for a in range(0, n, chunk):

@@ -118,6 +118,76 @@ __global__ void __launch_bounds__(kSampleBlock) sketch_kernel(const SketchK P) {
   }
 }
 
+// Exact counts of the sampled keys (the heavy-hitter candidates of a GROUP BY
+// are the sample's most frequent keys): a linear-probing table of key words
+// (0 = empty; key word 0 has a side row in the aggregation and is skipped)
+// and counts, over the same strided sample blocks as sketch_kernel.
+constexpr int kHeavyBins = 4096;
+
+struct HeavyK {
+  DevCol key;
+  const uint32_t* sel;
+  uint64_t nrows, len, stride, nblocks;
+  unsigned long long* keys;  // [cap]
+  unsigned int* cnt;         // [cap]
+  uint64_t cap;              // power of two, >= 2 x the sampled rows
+  unsigned int* hist;        // [kHeavyBins] keys per count (the last bin: >= kHeavyBins - 1)
+  unsigned long long* out;   // [2 * out_cap] (key, count) of the kept keys
+  unsigned int* nout;
+  uint32_t out_cap, min_count;
+  uint32_t* err;
+};
+
+__global__ void __launch_bounds__(kSampleBlock) heavy_count_kernel(const HeavyK P) {
+  for (uint64_t b = blockIdx.x; b < P.nblocks; b += gridDim.x) {
+    const uint64_t i = b * P.stride + threadIdx.x;
+    if (i >= P.nrows) continue;
+    uint64_t p = i;
+    if (P.sel) {
+      p = P.sel[i];
+      if (p >= P.len) continue;  // reported by sketch_kernel
+    }
+    if (!col_valid(P.key, p)) continue;
+    const uint64_t w = key_word(P.key, p);
+    if (w == 0) continue;
+    uint64_t s = mix64(w ^ 0x3C6EF372FE94F82Bull) & (P.cap - 1);
+    for (uint64_t t = 0; t < P.cap; ++t) {  // at most half full: ends at a free slot
+      unsigned long long cur = P.keys[s];
+      if (cur == 0) cur = atomicCAS(P.keys + s, 0ull, static_cast<unsigned long long>(w));
+      if (cur == 0 || cur == w) {
+        atomicAdd(P.cnt + s, 1u);
+        break;
+      }
+      s = (s + 1) & (P.cap - 1);
+    }
+  }
+}
+
+__global__ void heavy_hist_kernel(const HeavyK P) {
+  __shared__ unsigned int h[kHeavyBins];
+  for (int b = threadIdx.x; b < kHeavyBins; b += blockDim.x) h[b] = 0;
+  __syncthreads();
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < P.cap; s += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned int c = P.cnt[s];
+    if (c) atomicAdd(&h[min(c, kHeavyBins - 1u)], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < kHeavyBins; b += blockDim.x)
+    if (h[b]) atomicAdd(P.hist + b, h[b]);
+}
+
+__global__ void heavy_compact_kernel(const HeavyK P) {
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < P.cap; s += (uint64_t)gridDim.x * blockDim.x) {
+    const unsigned int c = P.cnt[s];
+    if (c < P.min_count) continue;
+    const unsigned int o = atomicAdd(P.nout, 1u);
+    if (o < P.out_cap) {
+      P.out[2 * o] = P.keys[s];
+      P.out[2 * o + 1] = c;
+    }
+  }
+}
+
 double hll_estimate(const std::vector<uint32_t>& regs) {
   const double m = kHllM;
   double sum = 0;
@@ -223,8 +293,59 @@ void sketch_key_column(qeg_ctx* ctx, const DevCol& key, const uint32_t* sel, uin
   f[78] = static_cast<float>(out.null_frac);
   f[79] = nonnull > 0 ? static_cast<float>(std::min(1.0, out.hll_estimate / nonnull)) : 0.f;
 
-  const size_t nh = std::min<size_t>(ranked.size(), static_cast<size_t>(std::max(0, want_heavy)));
-  for (size_t i = 0; i < nh; ++i) out.heavy.push_back(ranked[i].second);
+  if (want_heavy <= 0 || nblocks == 0) return;
+  // Heavy hitters: the sample's want_heavy most frequent keys, by exact counts.
+  HeavyK H{};
+  H.key = key;
+  H.sel = sel;
+  H.nrows = nrows;
+  H.len = len;
+  H.stride = stride;
+  H.nblocks = nblocks;
+  H.cap = 1;
+  while (H.cap < 2 * nblocks * kSampleBlock) H.cap <<= 1;
+  H.out_cap = static_cast<uint32_t>(4 * want_heavy);
+  const size_t head = H.cap * 12 + kHeavyBins * 4 + 16;
+  DevBuf hb(head + static_cast<size_t>(H.out_cap) * 16, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(hb.get(), 0, head, ctx->stream));
+  H.keys = hb.get<unsigned long long>();
+  H.cnt = reinterpret_cast<unsigned int*>(H.keys + H.cap);
+  H.hist = H.cnt + H.cap;
+  H.nout = H.hist + kHeavyBins;
+  H.out = reinterpret_cast<unsigned long long*>(hb.get<uint8_t>() + head);
+  H.err = P.err;
+  heavy_count_kernel<<<grid, kSampleBlock, 0, ctx->stream>>>(H);
+  heavy_hist_kernel<<<grid_for(ctx, H.cap, 256, 4), 256, 0, ctx->stream>>>(H);
+  std::vector<uint32_t> hist(kHeavyBins);
+  QEG_CUDA(cudaMemcpyAsync(hist.data(), H.hist, kHeavyBins * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  // The smallest count threshold that keeps at most out_cap keys (whole bins
+  // only, so the kept set does not depend on the order of the atomics; the
+  // top bin holds at most sample/(kHeavyBins-1) keys, fewer than out_cap).
+  uint64_t kept = 0;
+  uint32_t c = kHeavyBins - 1;
+  while (c > 1 && kept + hist[c] <= H.out_cap) kept += hist[c--];
+  if (c == 1 && kept + hist[1] <= H.out_cap) c = 0;
+  H.min_count = c + 1;
+  heavy_compact_kernel<<<grid_for(ctx, H.cap, 256, 4), 256, 0, ctx->stream>>>(H);
+  ctx->launches += 3;
+  QEG_CUDA(cudaGetLastError());
+  uint32_t n = 0;
+  QEG_CUDA(cudaMemcpyAsync(&n, H.nout, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  n = std::min(n, H.out_cap);
+  std::vector<unsigned long long> kc(2 * static_cast<size_t>(n));
+  if (n) {
+    QEG_CUDA(cudaMemcpyAsync(kc.data(), H.out, kc.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  std::vector<std::pair<uint64_t, uint64_t>> top(n);
+  for (uint32_t i = 0; i < n; ++i) top[i] = {kc[2 * i + 1], kc[2 * i]};
+  std::sort(top.begin(), top.end(), [](const auto& a, const auto& b) {
+    return a.first != b.first ? a.first > b.first : a.second < b.second;
+  });
+  const size_t nh = std::min<size_t>(top.size(), static_cast<size_t>(want_heavy));
+  for (size_t i = 0; i < nh; ++i) out.heavy.push_back(top[i].second);
 }
 
 // ---------------------------------------------------------------------------

@@ -90,3 +90,20 @@ def test_pipeline_integer_keys_and_filter_on_int(ctx):
                                      filter_col=1, filter_op=qeg.CMP_GE, filter_value=50.5)
     gt, grows = gpu_rows(res, types)
     assert_same(gt, grows, ot, orows)
+
+
+@pytest.mark.parametrize("seed,nulls", [(4, False), (5, True)])
+def test_pipeline_trades_aggregates_specialised_kernel(ctx, seed, nulls):
+    """The trades workload's exact aggregate list -- COUNT(*), AVG(price),
+    SUM(qty) -- runs the field-set-specialised kernel (with NULL counts when
+    the columns have NULLs); device-resident columns as in the benchmark."""
+    trades, symbols = make_case(seed, nulls=nulls)
+    aggs = [(O.COUNT_STAR, 0), (O.AVG, 1), (O.SUM, 2)]
+    ot, orows = oracle_pipeline(trades, symbols, aggs)
+    canon = StrCanon(trades[0].dictionary + symbols[0].dictionary)
+    gp = [to_gpu(c, canon, device=True) for c in trades]
+    gb = [to_gpu(c, canon, device=True) for c in symbols]
+    types, res = qeg.filter_join_agg(ctx, gp, gb, 0, 0, 4, aggs, filter_col=1, filter_op=qeg.CMP_GT,
+                                     filter_value=100.0)
+    gt, grows = gpu_rows(res, types, canon)
+    assert_same(gt, grows, ot, orows)
