@@ -173,6 +173,22 @@ qeg_status qeg_agg_stats(const qeg_agg* agg, uint64_t* capacity, uint32_t* resiz
                          int32_t* strategy, int32_t* hot_keys, double* est_groups);
 void qeg_agg_destroy(qeg_agg* agg);
 
+/* ---- tumbling window: replaces qe::tsx::Window in WindowMode::Tumbling
+ * (tsx/window.h:82-100, tsx/window.cpp:305-394) --------------------------
+ * GROUP BY (key_cols..., bucket_start) with bucket_start = (t / width) * width
+ * of the time column (C++ truncating division, typed as the time column; a
+ * NULL time is a NULL bucket, and NULL keys group together). The result is an
+ * ordinary qeg_agg: consume / finish / fetch / destroy as above, output
+ * columns [keys..., bucket_start, aggregates...] like Window::output_schema
+ * (tsx/window.cpp:243-262). Errors mirror the Window constructor
+ * (tsx/window.cpp:214-241): STR partition keys or aggregate inputs, a time
+ * column that is not I32/I64/TS, or width <= 0 -> QEG_ERR_INVALID. At most 7
+ * partition keys. The sliding mode (a sort, not a hash table) is not here.  */
+qeg_status qeg_window_create(qeg_ctx* ctx, const int32_t* col_types, int ncols,
+                             const uint32_t* key_cols, int nkeys, uint32_t time_col,
+                             int64_t width, const qeg_agg_spec* aggs, int naggs,
+                             const qeg_agg_config* cfg, qeg_agg** out);
+
 /* ---- hash equi-join: replaces qe::HashJoin (ops/join.h:69-123) ------------
  * create      ~ HashJoin::HashJoin (ops/join.cpp:101-123), same key-type check
  * build       ~ one build batch of build_side (ops/join.cpp:133-197): inserts
@@ -194,6 +210,24 @@ qeg_status qeg_join_build_finish(qeg_join* j);
 qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64_t* out_rows);
 qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count,
                           const qeg_out_column* outs);
+/* ---- backward as-of join: replaces qe::tsx::AsofJoin (tsx/asof.h:94-150) --
+ * For each probe row with key tuple k and time t: the build row with key k
+ * whose time tb is the greatest tb <= t (equal times match); with
+ * has_tolerance, only when t - tb <= tolerance (uint64 arithmetic, as
+ * tsx/asof.cpp:283-293). NULL keys or times never match; INNER drops an
+ * unmatched probe row, LEFT emits it once with the build columns NULL. Among
+ * build rows with equal (key, time) the one built last is taken (the
+ * reference's stable sort then last-<=, tsx/asof.cpp:269-296). nkeys may be 0
+ * (one global partition). Time columns are I32/I64/TS, read as int64.
+ * The result is a qeg_join: build / build_finish / probe / fetch / destroy
+ * as above; probe output rows come in probe-batch order (the reference emits
+ * them in (key, time) order of its sorted probe side; the row multiset is the
+ * same). Errors mirror the AsofJoin constructor (tsx/asof.cpp:130-160).      */
+qeg_status qeg_asof_create(qeg_ctx* ctx, const int32_t* probe_types, int nprobe,
+                           const int32_t* build_types, int nbuild, const uint32_t* probe_keys,
+                           const uint32_t* build_keys, int nkeys, uint32_t probe_time,
+                           uint32_t build_time, int32_t asof_type, int32_t has_tolerance,
+                           int64_t tolerance, qeg_join** out);
 /* The aggregate sink of scan(probe).join(scan(build)).aggregate({},
  * {COUNT(*), SUM(probe_val)}) fused into the probe: adds this batch's matched
  * row count and payload sum to the running totals (single key column). */

@@ -120,6 +120,9 @@ def orc():
             "orc_parallel_join_count_sum": (c, [vp, vp, vp, vp, ctypes.c_uint, u64, P(ctypes.c_int64),
                                                 P(ctypes.c_int64), P(i32)]),
             "orc_result_str": (c, [vp, c, ctypes.c_int64, P(ctypes.c_char_p), P(u64)]),
+            "orc_window_tumbling": (c, [vp, c, vp, c, ctypes.c_uint32, ctypes.c_int64, vp, vp, c, u64, P(vp)]),
+            "orc_asof_join": (c, [vp, c, vp, c, vp, vp, c, ctypes.c_uint32, ctypes.c_uint32, i32, i32,
+                                  ctypes.c_int64, P(vp)]),
         }.items():
             f = getattr(L, name)
             f.restype, f.argtypes = r, a
@@ -143,6 +146,9 @@ def ref():
             "ref_parallel_join_count_sum": (c, [vp, vp, ctypes.c_uint, u64, P(ctypes.c_int64),
                                                 P(ctypes.c_int64), P(i32)]),
             "ref_result_str": (c, [vp, c, u64, P(ctypes.c_char_p), P(u64)]),
+            "ref_window_tumbling": (c, [vp, c, vp, c, ctypes.c_uint32, ctypes.c_int64, vp, vp, c, u64, c, P(vp)]),
+            "ref_asof_join": (c, [vp, c, vp, c, vp, vp, c, ctypes.c_uint32, ctypes.c_uint32, i32, i32,
+                                  ctypes.c_int64, u64, c, P(vp)]),
         }.items():
             f = getattr(L, name)
             f.restype, f.argtypes = r, a
@@ -239,6 +245,30 @@ def join(probe, build_, pkeys, bkeys, jtype=INNER, batch_rows=2048):
     return _rows(L, "orc", res)
 
 
+def window_tumbling(cols, keys, time_col, width, aggs, batch_rows=2048):
+    """GROUP BY (keys..., (t / width) * width of time_col): the tumbling Window."""
+    L = orc()
+    arr = _cols(cols)
+    k, f, c = _agg_arrays(keys, aggs)
+    res = ctypes.c_void_p()
+    _check(L, "orc", L.orc_window_tumbling(arr, len(cols), k, len(keys), time_col, width, f, c, len(aggs),
+                                           batch_rows, ctypes.byref(res)))
+    return _rows(L, "orc", res)
+
+
+def asof_join(probe, build_, pkeys, bkeys, ptime, btime, jtype=INNER, tolerance=None):
+    """Backward as-of join: probe columns then build columns."""
+    L = orc()
+    pa, ba = _cols(probe), _cols(build_)
+    pk = (ctypes.c_uint32 * max(1, len(pkeys)))(*pkeys)
+    bk = (ctypes.c_uint32 * max(1, len(bkeys)))(*bkeys)
+    res = ctypes.c_void_p()
+    _check(L, "orc", L.orc_asof_join(pa, len(probe), ba, len(build_), pk, bk, len(pkeys), ptime, btime, jtype,
+                                     0 if tolerance is None else 1, 0 if tolerance is None else int(tolerance),
+                                     ctypes.byref(res)))
+    return _rows(L, "orc", res)
+
+
 def join_count_sum(pkey, pval, bkey):
     L = orc()
     a, b, c = pkey.orc(), pval.orc(), bkey.orc()
@@ -278,6 +308,33 @@ def ref_join(probe, build_, pkeys, bkeys, jtype=INNER, batch_rows=2048, mode=0):
     res = ctypes.c_void_p()
     _check(L, "ref", L.ref_join(pa, len(probe), ba, len(build_), pk, bk, len(pkeys), jtype, batch_rows, mode,
                                 ctypes.byref(res)))
+    return _rows(L, "ref", res)
+
+
+def ref_window_tumbling(cols, keys, time_col, width, aggs, batch_rows=2048, mode=0):
+    """The reference's tumbling Window (mode 0 operator tree, 1 its
+    independent reference oracle)."""
+    L = ref()
+    arr = _cols(cols)
+    k, f, c = _agg_arrays(keys, aggs)
+    res = ctypes.c_void_p()
+    _check(L, "ref", L.ref_window_tumbling(arr, len(cols), k, len(keys), time_col, width, f, c, len(aggs),
+                                           batch_rows, mode, ctypes.byref(res)))
+    return _rows(L, "ref", res)
+
+
+def ref_asof_join(probe, build_, pkeys, bkeys, ptime, btime, jtype=INNER, tolerance=None, batch_rows=2048,
+                  mode=0):
+    """The reference's AsofJoin (mode 0 operator tree, 1 its independent
+    reference oracle)."""
+    L = ref()
+    pa, ba = _cols(probe), _cols(build_)
+    pk = (ctypes.c_uint32 * max(1, len(pkeys)))(*pkeys)
+    bk = (ctypes.c_uint32 * max(1, len(bkeys)))(*bkeys)
+    res = ctypes.c_void_p()
+    _check(L, "ref", L.ref_asof_join(pa, len(probe), ba, len(build_), pk, bk, len(pkeys), ptime, btime, jtype,
+                                     0 if tolerance is None else 1, 0 if tolerance is None else int(tolerance),
+                                     batch_rows, mode, ctypes.byref(res)))
     return _rows(L, "ref", res)
 
 

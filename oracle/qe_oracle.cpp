@@ -800,6 +800,159 @@ int orc_join(const orc_column* probe_in, int nprobe, const orc_column* build_in,
   });
 }
 
+// Tumbling window (tsx/window.cpp:305-394): the bucket lower edge
+// (t / W) * W of every row (C++ truncating division, typed as the time column,
+// NULL when t is NULL) becomes one more key column of an ordinary GROUP BY
+// (keys..., bucket) with NULL keys grouping together -- the same table, cells
+// and first-seen group order as the reference's Window.
+int orc_window_tumbling(const orc_column* cols_in, int ncols, const uint32_t* key_cols, int nkeys,
+                        uint32_t time_col, int64_t width, const int32_t* agg_funcs,
+                        const uint32_t* agg_cols, int naggs, uint64_t batch_rows, orc_result** out) {
+  return guarded([&] {
+    if (batch_rows == 0 || batch_rows % 64 != 0)
+      throw std::invalid_argument(
+          "Scan batch_size must be a positive multiple of 64 (validity word alignment)");
+    std::vector<Col> cols = to_cols(cols_in, ncols);
+    if (time_col >= static_cast<uint32_t>(ncols)) throw std::invalid_argument("time column out of range");
+    const T tt = cols[time_col].type;
+    if (tt != T::I32 && tt != T::I64 && tt != T::TS)
+      throw std::invalid_argument("Window: time column must be I32/I64/TS");
+    if (width <= 0) throw std::invalid_argument("Window: tumbling width W must be > 0");
+    std::vector<uint32_t> keys(key_cols, key_cols + nkeys);
+    for (uint32_t k : keys) {
+      if (k >= static_cast<uint32_t>(ncols)) throw std::invalid_argument("key column out of range");
+      if (cols[k].type == T::STR)
+        throw std::invalid_argument("Window: STR partition keys are not supported (out of grammar)");
+    }
+    const std::vector<AggSpecX> aggs = to_aggs(agg_funcs, agg_cols, naggs, ncols);
+    for (const AggSpecX& a : aggs)
+      if (a.f != Fn::CountStar && cols[a.col].type == T::STR)
+        throw std::invalid_argument("Window: STR aggregate inputs are not supported (out of grammar)");
+    const Col& tc = cols[time_col];
+    const uint64_t n = tc.len;
+    const size_t w = (tt == T::I32) ? 4 : 8;
+    std::vector<uint8_t> bdata(std::max<uint64_t>(n, 1) * w, 0);
+    std::vector<uint64_t> bvalid((n + 63) / 64 + 1, ~0ull);
+    for (uint64_t p = 0; p < n; ++p) {
+      if (!tc.valid(p)) {
+        bvalid[p >> 6] &= ~(1ull << (p & 63));
+        continue;
+      }
+      const int64_t t = tc.ival(p);
+      const int64_t b = (t / width) * width;
+      if (w == 4) {
+        const int32_t v = static_cast<int32_t>(b);
+        std::memcpy(bdata.data() + p * 4, &v, 4);
+      } else {
+        std::memcpy(bdata.data() + p * 8, &b, 8);
+      }
+    }
+    Col bc = tc;
+    bc.data = bdata.data();
+    bc.validity = bvalid.data();
+    bc.all_valid = false;
+    cols.push_back(bc);
+    keys.push_back(static_cast<uint32_t>(ncols));
+    *out = run_aggregate(cols, keys, aggs, 0, n, batch_rows).release();
+  });
+}
+
+// Backward as-of join (tsx/asof.cpp): build rows with non-NULL keys and a
+// non-NULL time are grouped by key (kNeverMatch; STR keys by value, as the
+// hash join) and ordered by time stably (tsx/asof.cpp:158-219, the sorted
+// build lists); each probe row with non-NULL keys and time t takes the last
+// build row of its key whose time is <= t (tsx/asof.cpp:269-296), kept only
+// when t - tb <= tolerance in uint64 arithmetic if a tolerance is set
+// (tsx/asof.cpp:283-293). INNER drops unmatched probe rows, LEFT emits them
+// with NULL build columns. Rows are emitted in probe order.
+int orc_asof_join(const orc_column* probe_in, int nprobe, const orc_column* build_in, int nbuild,
+                  const uint32_t* probe_keys, const uint32_t* build_keys, int nkeys,
+                  uint32_t probe_time, uint32_t build_time, int32_t asof_type, int32_t has_tol,
+                  int64_t tol, orc_result** out) {
+  return guarded([&] {
+    const std::vector<Col> probe = to_cols(probe_in, nprobe);
+    const std::vector<Col> build = to_cols(build_in, nbuild);
+    if (probe_time >= static_cast<uint32_t>(nprobe) || build_time >= static_cast<uint32_t>(nbuild))
+      throw std::invalid_argument("time column out of range");
+    auto ts_ok = [](T t) { return t == T::I32 || t == T::I64 || t == T::TS; };
+    if (!ts_ok(probe[probe_time].type) || !ts_ok(build[build_time].type))
+      throw std::invalid_argument("AsofJoin: time columns must be I32/I64/TS");
+    std::vector<uint32_t> pk(probe_keys, probe_keys + nkeys), bk(build_keys, build_keys + nkeys);
+    for (int j = 0; j < nkeys; ++j) {
+      if (pk[j] >= static_cast<uint32_t>(nprobe) || bk[j] >= static_cast<uint32_t>(nbuild))
+        throw std::invalid_argument("join key column out of range");
+      if (probe[pk[j]].type != build[bk[j]].type)
+        throw std::invalid_argument("AsofJoin: key column types must match positionally");
+    }
+    const Col& ptc = probe[probe_time];
+    const Col& btc = build[build_time];
+    // Build: group id per key tuple, rows per group as (time, row) by time.
+    HashTable ht(bk.size(), /*never_match=*/true);
+    std::vector<std::shared_ptr<Dict>> idmaps(bk.size());
+    for (size_t j = 0; j < bk.size(); ++j)
+      if (build[bk[j]].type == T::STR) idmaps[j] = std::make_shared<Dict>();
+    std::vector<std::vector<std::pair<int64_t, uint32_t>>> groups(nkeys == 0 ? 1 : 0);
+    const uint64_t nb = build.empty() ? 0 : build[0].len;
+    for (uint64_t r = 0; r < nb; ++r) {
+      if (!btc.valid(r)) continue;
+      uint32_t g = 0;
+      if (nkeys > 0) {
+        const KeyRow kr = key_row(build, bk, idmaps, r, true);
+        if (kr.nullmask) continue;
+        g = ht.insert_or_find(kr);
+        if (g >= groups.size()) groups.resize(g + 1);
+      }
+      groups[g].emplace_back(btc.ival(r), static_cast<uint32_t>(r));
+    }
+    for (auto& v : groups)
+      std::stable_sort(v.begin(), v.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    auto res = std::make_unique<orc_result>();
+    res->cols.resize(probe.size() + build.size());
+    for (size_t c = 0; c < probe.size(); ++c) {
+      res->cols[c].type = probe[c].type;
+      if (probe[c].type == T::STR) res->cols[c].dict = dict_of(probe[c]);
+    }
+    for (size_t c = 0; c < build.size(); ++c) {
+      res->cols[probe.size() + c].type = build[c].type;
+      if (build[c].type == T::STR) res->cols[probe.size() + c].dict = dict_of(build[c]);
+    }
+    const uint64_t np = probe.empty() ? 0 : probe[0].len;
+    const bool left = asof_type == ORC_LEFT;
+    uint64_t rows = 0;
+    for (uint64_t p = 0; p < np; ++p) {
+      int64_t match = -1;
+      if (ptc.valid(p)) {
+        uint32_t g = 0;
+        bool ok = true;
+        if (nkeys > 0) {
+          const KeyRow kr = key_row(probe, pk, idmaps, p, false);
+          g = kr.nullmask ? kNoGroup : ht.find(kr);
+          ok = g != kNoGroup && g < groups.size();
+        }
+        if (ok) {
+          const auto& v = groups[g];
+          const int64_t t = ptc.ival(p);
+          auto it = std::upper_bound(v.begin(), v.end(), t,
+                                     [](int64_t x, const std::pair<int64_t, uint32_t>& e) { return x < e.first; });
+          if (it != v.begin()) {
+            --it;
+            if (!has_tol || static_cast<uint64_t>(t) - static_cast<uint64_t>(it->first) <=
+                                static_cast<uint64_t>(tol))
+              match = it->second;
+          }
+        }
+      }
+      if (match < 0 && !left) continue;
+      for (size_t c = 0; c < probe.size(); ++c) push_value(res->cols[c], probe[c], p, false);
+      for (size_t c = 0; c < build.size(); ++c)
+        push_value(res->cols[probe.size() + c], build[c], match < 0 ? 0 : static_cast<uint64_t>(match), match < 0);
+      ++rows;
+    }
+    res->rows = rows;
+    *out = res.release();
+  });
+}
+
 int orc_join_count_sum(const orc_column* probe_key, const orc_column* probe_val,
                        const orc_column* build_key, uint64_t batch_rows, int64_t* out_count,
                        int64_t* out_sum, int32_t* sum_valid) {

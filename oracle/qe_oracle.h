@@ -29,6 +29,8 @@
  *   - STR keys canonicalised by VALUE               ops/aggregate.cpp:164-187,
  *                                                  ops/join.cpp:48-71
  *   - morsel-parallel CPU driver (baseline only)    exec/parallel.cpp:189-599
+ *   - tumbling window: bucket key + GROUP BY        tsx/window.cpp:305-394
+ *   - backward as-of join                           tsx/asof.cpp:158-296
  *
  * All functions return 0 on success and a negative code on a usage error
  * (orc_last_error() then holds a message). No exceptions cross this boundary.
@@ -78,6 +80,20 @@ int orc_groupby(const orc_column* cols, int ncols, const uint32_t* key_cols, int
 int orc_join(const orc_column* probe, int nprobe, const orc_column* build, int nbuild,
              const uint32_t* probe_keys, const uint32_t* build_keys, int nkeys,
              int32_t join_type, uint64_t batch_rows, orc_result** out);
+
+/* Tumbling window (tsx/window.cpp:305-394): GROUP BY (key_cols..., bucket)
+ * with bucket = (t / width) * width of time_col, typed as the time column;
+ * output keys, bucket, aggregates in first-seen group order. */
+int orc_window_tumbling(const orc_column* cols, int ncols, const uint32_t* key_cols, int nkeys,
+                        uint32_t time_col, int64_t width, const int32_t* agg_funcs,
+                        const uint32_t* agg_cols, int naggs, uint64_t batch_rows, orc_result** out);
+
+/* Backward as-of join (tsx/asof.cpp): probe columns then build columns, one
+ * row per matched probe row (LEFT: every probe row), in probe order. */
+int orc_asof_join(const orc_column* probe, int nprobe, const orc_column* build, int nbuild,
+                  const uint32_t* probe_keys, const uint32_t* build_keys, int nkeys,
+                  uint32_t probe_time, uint32_t build_time, int32_t asof_type, int32_t has_tol,
+                  int64_t tol, orc_result** out);
 
 /* COUNT(*) and SUM(probe_col) over the INNER join of probe and build on
  * single I64/I32 key columns -- the sink of the 16M x 256M join workload.

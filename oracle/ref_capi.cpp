@@ -9,6 +9,8 @@
 //   oracle::drain_operator                          oracle/result_set.h:64
 //   oracle::run_reference / run_join_reference      oracle/reference_oracle.h:30-56
 //   exec::ParallelEngine::run                       exec/parallel.h:72-111
+//   plan window_tumbling / asof_join                plan/plan.h:215-243
+//   oracle::run_window_reference / run_asof_reference oracle/reference_oracle.h:65-87
 //   ops::hash_combine_scalar                        ops/hash_kernels.h:56-58
 // The result accessor functions mirror the orc_result_* ones.
 
@@ -152,6 +154,67 @@ int ref_join(const orc_column* probe, int nprobe, const orc_column* build, int n
                 rk.emplace_back(build_keys[k]);
             }
             auto op = qe::plan::scan(*pt).join(qe::plan::scan(*bt), lk, rk, jt).build(batch_rows);
+            r->rs = qe::oracle::drain_operator(*op);
+        }
+        *out = r.release();
+    });
+}
+
+// Tumbling window: mode 0 the engine operator (plan window_tumbling + drain),
+// 1 the independent reference oracle (run_window_reference).
+int ref_window_tumbling(const orc_column* cols, int ncols, const uint32_t* key_cols, int nkeys,
+                        uint32_t time_col, int64_t width, const int32_t* agg_funcs,
+                        const uint32_t* agg_cols, int naggs, uint64_t batch_rows, int mode,
+                        ref_result** out) {
+    return guarded([&] {
+        auto t = std::make_unique<qe::Table>(make_table(cols, ncols));
+        auto aggs = make_aggs(agg_funcs, agg_cols, naggs);
+        auto r = std::make_unique<ref_result>();
+        if (mode == 1) {
+            r->rs = qe::oracle::run_window_reference(
+                *t, qe::tsx::WindowMode::Tumbling,
+                std::vector<uint32_t>(key_cols, key_cols + nkeys), time_col, width, aggs);
+        } else {
+            std::vector<qe::plan::ColRef> keys;
+            for (int k = 0; k < nkeys; ++k) keys.emplace_back(key_cols[k]);
+            auto op = qe::plan::scan(*t)
+                          .window_tumbling(keys, qe::plan::ColRef(time_col), width, aggs)
+                          .build(batch_rows);
+            r->rs = qe::oracle::drain_operator(*op);
+        }
+        *out = r.release();
+    });
+}
+
+// Backward as-of join: mode 0 the engine operator (plan asof_join + drain), 1
+// the independent reference oracle (run_asof_reference).
+int ref_asof_join(const orc_column* probe, int nprobe, const orc_column* build, int nbuild,
+                  const uint32_t* probe_keys, const uint32_t* build_keys, int nkeys,
+                  uint32_t probe_time, uint32_t build_time, int32_t asof_type, int32_t has_tol,
+                  int64_t tol, uint64_t batch_rows, int mode, ref_result** out) {
+    return guarded([&] {
+        auto pt = std::make_unique<qe::Table>(make_table(probe, nprobe));
+        auto bt = std::make_unique<qe::Table>(make_table(build, nbuild));
+        const qe::tsx::AsofType at =
+            asof_type == ORC_LEFT ? qe::tsx::AsofType::Left : qe::tsx::AsofType::Inner;
+        std::optional<std::int64_t> tolerance;
+        if (has_tol) tolerance = tol;
+        auto r = std::make_unique<ref_result>();
+        if (mode == 1) {
+            r->rs = qe::oracle::run_asof_reference(
+                *pt, *bt, std::vector<uint32_t>(probe_keys, probe_keys + nkeys),
+                std::vector<uint32_t>(build_keys, build_keys + nkeys), probe_time, build_time, at,
+                tolerance);
+        } else {
+            std::vector<qe::plan::ColRef> lk, rk;
+            for (int k = 0; k < nkeys; ++k) {
+                lk.emplace_back(probe_keys[k]);
+                rk.emplace_back(build_keys[k]);
+            }
+            auto op = qe::plan::scan(*pt)
+                          .asof_join(qe::plan::scan(*bt), lk, rk, qe::plan::ColRef(probe_time),
+                                     qe::plan::ColRef(build_time), at, tolerance)
+                          .build(batch_rows);
             r->rs = qe::oracle::drain_operator(*op);
         }
         *out = r.release();

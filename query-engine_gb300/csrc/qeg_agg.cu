@@ -773,11 +773,17 @@ void AggState::plan(const int32_t* col_types, int ncols, const uint32_t* key_col
   row_words = (mode == 2 ? 2 + nk : 1) + nfields;
 }
 
+DevCol AggState::key_col(const std::vector<StagedCol>& staged, size_t j) const {
+  DevCol c = staged[keys[j]].dev;
+  c.bucket = (bucket_width > 0 && j + 1 == keys.size()) ? bucket_width : 0;
+  return c;
+}
+
 AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel, uint64_t nrows,
                        uint64_t len) const {
   AggK P{};
   P.nkeys = static_cast<int>(keys.size());
-  for (size_t j = 0; j < keys.size(); ++j) P.key[j] = staged[keys[j]].dev;
+  for (size_t j = 0; j < keys.size(); ++j) P.key[j] = key_col(staged, j);
   P.nvals = static_cast<int>(val_cols.size());
   for (size_t c = 0; c < val_cols.size(); ++c) {
     P.val[c] = staged[val_cols[c]].dev;
@@ -1168,6 +1174,43 @@ qeg_status qeg_agg_create(qeg_ctx* ctx, const int32_t* col_types, int ncols, con
     qeg::require(bt == 0 || (bt >= 32 && bt <= 1024 && bt % 32 == 0),
                  "block_threads must be 0 or a multiple of 32 in [32, 1024]");
     a->st.plan(col_types, ncols, key_cols, nkeys, aggs, naggs);
+    *out = a.release();
+  });
+}
+
+qeg_status qeg_window_create(qeg_ctx* ctx, const int32_t* col_types, int ncols, const uint32_t* key_cols,
+                             int nkeys, uint32_t time_col, int64_t width, const qeg_agg_spec* aggs, int naggs,
+                             const qeg_agg_config* cfg, qeg_agg** out) {
+  return qeg::guarded(ctx, [&] {
+    qeg::require(ctx != nullptr && out != nullptr, "ctx/out is NULL");
+    qeg::require(ncols > 0 && col_types != nullptr, "window needs an input schema");
+    qeg::require(nkeys >= 0 && (nkeys == 0 || key_cols != nullptr), "key_cols is NULL");
+    qeg::require(nkeys + 1 <= qeg::kMaxKeys, "GPU window supports at most 7 partition keys");
+    qeg::require(naggs >= 1 && aggs != nullptr, "Window needs >=1 aggregate");
+    qeg::require(time_col < static_cast<uint32_t>(ncols), "window time column out of range");
+    for (int k = 0; k < nkeys; ++k) {
+      qeg::require(key_cols[k] < static_cast<uint32_t>(ncols), "window key column out of range");
+      qeg::require(col_types[key_cols[k]] != QEG_STR,
+                   "Window: STR partition keys are not supported (out of grammar)");
+    }
+    for (int a = 0; a < naggs; ++a)
+      if (aggs[a].func != QEG_COUNT_STAR && aggs[a].input_col < static_cast<uint32_t>(ncols))
+        qeg::require(col_types[aggs[a].input_col] != QEG_STR,
+                     "Window: STR aggregate inputs are not supported (out of grammar)");
+    const int32_t tt = col_types[time_col];
+    qeg::require(tt == QEG_I32 || tt == QEG_I64 || tt == QEG_TS, "Window: time column must be I32/I64/TS");
+    qeg::require(width > 0, "Window: tumbling width W must be > 0");
+    std::vector<uint32_t> k(key_cols, key_cols + nkeys);
+    k.push_back(time_col);
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    auto a = std::make_unique<qeg_agg>();
+    a->st.ctx = ctx;
+    if (cfg) a->st.cfg = *cfg;
+    const int bt = a->st.cfg.block_threads;
+    qeg::require(bt == 0 || (bt >= 32 && bt <= 1024 && bt % 32 == 0),
+                 "block_threads must be 0 or a multiple of 32 in [32, 1024]");
+    a->st.plan(col_types, ncols, k.data(), nkeys + 1, aggs, naggs);
+    a->st.bucket_width = width;
     *out = a.release();
   });
 }

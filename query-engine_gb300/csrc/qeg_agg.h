@@ -127,6 +127,9 @@ struct AggState {
   int32_t strategy = QEG_AGG_AUTO;
   double est_groups = 0, hot_share = 0;
   std::vector<uint64_t> heavy_candidates;
+  // Tumbling window (qeg_window_create): the last key is the time column, read
+  // as its bucket's lower edge with this width; 0 for a plain GROUP BY.
+  int64_t bucket_width = 0;
 
   bool finished = false;
   uint64_t nout = 0;
@@ -136,6 +139,7 @@ struct AggState {
             int na);
   AggK kparams(const std::vector<StagedCol>& staged, const uint32_t* sel, uint64_t nrows, uint64_t len) const;
   AggK kparams_base() const;
+  DevCol key_col(const std::vector<StagedCol>& staged, size_t j) const;
   void alloc_table(uint64_t new_cap);
   size_t smem_bytes(int block) const;
   int warp_hot() const;

@@ -30,6 +30,10 @@ struct DevCol {
   const int32_t* code_map;   // STR only: dictionary code -> canonical value id
   int32_t type;
   int32_t all_valid;
+  // Tumbling-window key (I32/I64/TS only): when > 0 the key word is the lower
+  // edge of the value's bucket, (v / bucket) * bucket with C++ truncating
+  // division, in the column's own type (tsx/window.cpp:318-330).
+  int64_t bucket;
 };
 
 __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
@@ -53,13 +57,21 @@ __device__ __forceinline__ bool col_valid(const DevCol& c, uint64_t p) {
 // Canonical 64-bit key word of row p (valid rows only).
 __device__ __forceinline__ uint64_t key_word(const DevCol& c, uint64_t p) {
   switch (c.type) {
-    case kI32: return static_cast<uint32_t>(__ldg(static_cast<const int32_t*>(c.data) + p));
+    case kI32: {
+      int32_t v = __ldg(static_cast<const int32_t*>(c.data) + p);
+      if (c.bucket > 0) v = static_cast<int32_t>(static_cast<int64_t>(v) / c.bucket * c.bucket);
+      return static_cast<uint32_t>(v);
+    }
     case kSTR: {
       const int32_t code = __ldg(static_cast<const int32_t*>(c.data) + p);
       return static_cast<uint32_t>(c.code_map ? __ldg(c.code_map + code) : code);
     }
     case kI64:
-    case kTS: return static_cast<uint64_t>(__ldg(static_cast<const long long*>(c.data) + p));
+    case kTS: {
+      long long v = __ldg(static_cast<const long long*>(c.data) + p);
+      if (c.bucket > 0) v = v / c.bucket * c.bucket;
+      return static_cast<uint64_t>(v);
+    }
     case kBOOL: return __ldg(static_cast<const uint8_t*>(c.data) + p);
     case kF64: {
       const uint64_t b = static_cast<uint64_t>(__ldg(static_cast<const long long*>(c.data) + p));

@@ -28,6 +28,7 @@
 
 #include "qeg_agg.h"
 #include "qeg_scan.cuh"
+#include "qeg_sort.h"
 
 namespace qeg {
 
@@ -1039,6 +1040,117 @@ __global__ void probe_emit_kernel(const ProbeK P) {
   }
 }
 
+// ---- as-of join (tsx/asof.cpp) ---------------------------------------------
+// Build: every build row becomes an item (partition slot, timestamp - tmin,
+// row); rows with a NULL key or a NULL timestamp get the sentinel slot
+// `nslots` and sort after every partition (they never match,
+// tsx/asof.cpp:211-216). After a stable sort by (slot, timestamp) each
+// partition is one timestamp-ascending run whose equal timestamps keep the
+// build order, like the reference's sorted build lists (tsx/asof.cpp:158-219).
+struct AsofItemsK {
+  DevCol key[kMaxKeys];
+  int nkeys;
+  DevCol ts;
+  uint64_t n;
+  JTable T;
+  uint32_t nslots;
+  int64_t tmin;
+  uint64_t* lo;
+  uint32_t* hi;
+  uint32_t* val;
+  uint32_t* cnt;  // matchable rows per slot
+  uint32_t* err;
+};
+
+__global__ void asof_items_kernel(const AsofItemsK P) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t slot = P.nslots;
+    uint64_t rel = 0;
+    if (col_valid(P.ts, r)) {
+      int64_t s = 0;
+      if (P.nkeys > 0) {
+        uint64_t w[kMaxKeys], h;
+        s = load_key(P.key, P.nkeys, r, w, h) ? probe_slot(P.T, P.key, r, w, h, P.err) : -1;
+      }
+      if (s >= 0) {
+        slot = static_cast<uint32_t>(s);
+        rel = static_cast<uint64_t>(int_value(P.ts, r)) - static_cast<uint64_t>(P.tmin);
+        atomicAdd(P.cnt + s, 1u);
+      }
+    }
+    P.lo[r] = rel;
+    P.hi[r] = slot;
+    P.val[r] = static_cast<uint32_t>(r);
+  }
+}
+
+// Probe: a probe row with non-NULL keys and timestamp t finds its partition,
+// then the last build timestamp <= t by binary search over the partition's
+// run (the reference walks a cursor over the sorted probe side to the same
+// row, tsx/asof.cpp:269-296); with a tolerance the match is kept only when
+// t - tb <= tolerance in uint64 arithmetic (tsx/asof.cpp:283-293).
+struct AsofProbeK {
+  DevCol key[kMaxKeys];
+  int nkeys;
+  DevCol ts;
+  uint64_t n;
+  JTable T;
+  int64_t tmin;
+  const uint64_t* ats;   // sorted timestamps - tmin
+  const uint32_t* arow;  // build rows in the same order
+  const uint64_t* aoff;  // partition runs: [aoff[s], aoff[s+1])
+  int left, tol_set;
+  uint64_t tol;
+  uint32_t* match;
+  uint32_t* counts;
+  uint32_t* out_probe;
+  uint32_t* out_build;
+  uint32_t* err;
+};
+
+__global__ void asof_probe_kernel(const AsofProbeK P) {
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P.n; p += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t m = kNullRow;
+    if (col_valid(P.ts, p)) {
+      int64_t s = 0;
+      if (P.nkeys > 0) {
+        uint64_t w[kMaxKeys], h;
+        s = load_key(P.key, P.nkeys, p, w, h) ? probe_slot(P.T, P.key, p, w, h, P.err) : -1;
+      }
+      if (s >= 0) {
+        const int64_t t = int_value(P.ts, p);
+        const uint64_t b = P.aoff[s], e = P.aoff[s + 1];
+        if (e > b && t >= P.tmin) {
+          const uint64_t rel = static_cast<uint64_t>(t) - static_cast<uint64_t>(P.tmin);
+          uint64_t lo = b, hi = e;  // first position whose timestamp is > t
+          while (lo < hi) {
+            const uint64_t mid = lo + ((hi - lo) >> 1);
+            if (P.ats[mid] <= rel) lo = mid + 1;
+            else hi = mid;
+          }
+          if (lo > b && (!P.tol_set || rel - P.ats[lo - 1] <= P.tol)) m = P.arow[lo - 1];
+        }
+      }
+    }
+    if (P.left) {
+      P.out_probe[p] = static_cast<uint32_t>(p);
+      P.out_build[p] = m;
+    } else {
+      P.match[p] = m;
+      P.counts[p] = m != kNullRow ? 1u : 0u;
+    }
+  }
+}
+
+__global__ void asof_emit_kernel(const AsofProbeK P, const uint64_t* __restrict__ starts) {
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P.n; p += (uint64_t)gridDim.x * blockDim.x) {
+    if (!P.counts[p]) continue;
+    const uint64_t o = starts[p];
+    P.out_probe[o] = static_cast<uint32_t>(p);
+    P.out_build[o] = P.match[p];
+  }
+}
+
 // out[k] = src[idx[k]] (width bytes), valid[k] from the source, NULL where
 // idx[k] is kNullRow. Source validity is either a bitmap (probe columns) or a
 // byte per row (build store).
@@ -1063,6 +1175,52 @@ __global__ void gather_kernel(const void* __restrict__ src, const uint64_t* __re
     else if (code_map) static_cast<int32_t*>(out)[k] = ok ? code_map[static_cast<const int32_t*>(src)[r]] : 0;
     else if (width == 4) static_cast<uint32_t*>(out)[k] = static_cast<const uint32_t*>(src)[r];
     else static_cast<uint8_t*>(out)[k] = static_cast<const uint8_t*>(src)[r];
+  }
+}
+
+// Device outputs: the same gather written straight into the caller's column,
+// validity packed on the fly (a warp covers 64 rows and makes one word from
+// two ballots; padding bits set), so an output row is written once.
+__global__ void gather_out_kernel(const void* __restrict__ src, const uint64_t* __restrict__ src_bits,
+                                  const uint8_t* __restrict__ src_bytes, const int32_t* __restrict__ code_map,
+                                  int width, const uint32_t* __restrict__ idx, uint64_t n, void* __restrict__ out,
+                                  uint64_t* __restrict__ out_words, unsigned int* __restrict__ any_null) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint64_t nw = (n + 63) / 64;
+  const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t w = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w < nw; w += nwarps) {
+    unsigned half[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const uint64_t k = w * 64 + h * 32 + lane;
+      bool ok = true;  // padding rows count as valid
+      if (k < n) {
+        const uint32_t r = idx[k];
+        ok = r != kNullRow;
+        if (ok) {
+          if (src_bits) ok = (src_bits[r >> 6] >> (r & 63)) & 1ull;
+          else if (src_bytes) ok = src_bytes[r];
+        }
+        if (width == 8) {
+          static_cast<uint64_t*>(out)[k] = r == kNullRow ? 0 : static_cast<const uint64_t*>(src)[r];
+        } else if (width == 4) {
+          uint32_t v = 0;
+          if (r != kNullRow) {
+            v = static_cast<const uint32_t*>(src)[r];
+            if (code_map) v = ok ? static_cast<uint32_t>(code_map[static_cast<int32_t>(v)]) : 0;
+          }
+          static_cast<uint32_t*>(out)[k] = v;
+        } else {
+          static_cast<uint8_t*>(out)[k] = r == kNullRow ? 0 : static_cast<const uint8_t*>(src)[r];
+        }
+      }
+      half[h] = __ballot_sync(0xffffffffu, ok);
+    }
+    if (lane == 0) {
+      const uint64_t word = static_cast<uint64_t>(half[0]) | (static_cast<uint64_t>(half[1]) << 32);
+      if (out_words) out_words[w] = word;
+      if (word != ~0ull) atomicOr(any_null, 1u);
+    }
   }
 }
 
@@ -1125,6 +1283,18 @@ struct JoinState {
   // count/sum sink totals
   DevBuf acc;
   bool acc_init = false;
+
+  // as-of join (qeg_asof_create): time columns, tolerance, and the build side
+  // sorted by (partition slot, timestamp)
+  bool asof = false;
+  uint32_t ptime = 0, btime = 0;
+  int32_t tol_set = 0;
+  int64_t tol = 0;
+  int64_t tmin = 0;
+  uint32_t aslots = 0;
+  DevBuf ats, arow, aoff, tbits, amatch;
+  void asof_build();
+  void asof_probe(uint64_t n);
 
   JTable table() const {
     JTable T{};
@@ -1234,6 +1404,10 @@ void JoinState::finish_build() {
   require(!built, "build_finish() called twice");
   built = true;
   const int nk = static_cast<int>(bkeys.size());
+  if (asof && nk == 0) {  // one global partition: no table
+    asof_build();
+    return;
+  }
   key_bits.clear();
   for (int j = 0; j < nk; ++j) {
     key_bits.emplace_back(((nbuild + 63) / 64 + 1) * 8, ctx->stream);
@@ -1311,6 +1485,78 @@ void JoinState::finish_build() {
   csr_built = false;
   acc.alloc(24, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(acc.get(), 0, 24, ctx->stream));
+  if (asof) asof_build();
+}
+
+// As-of build: items per build row, a stable radix sort by (slot, timestamp),
+// partition runs from the per-slot counts.
+void JoinState::asof_build() {
+  const int nk = static_cast<int>(bkeys.size());
+  const uint64_t ns = nk == 0 ? 1 : slots();
+  require(ns < 0xffffffffull, "as-of join: too many partitions");
+  aslots = static_cast<uint32_t>(ns);
+  tbits.alloc(((nbuild + 63) / 64 + 1) * 8, ctx->stream);
+  if (nbuild) {
+    bytes_to_bits_kernel<<<grid_for(ctx, (nbuild / 64 + 1) * 32, 256, 8), 256, 0, ctx->stream>>>(
+        bvalid[btime].get<uint8_t>(), nbuild, tbits.get<uint64_t>());
+    ctx->launches++;
+  }
+  DevCol ts{};
+  ts.type = btypes[btime];
+  ts.data = bvals[btime].get();
+  ts.validity = tbits.get<uint64_t>();
+  // Timestamp range of the build side (relative timestamps need its low end).
+  DevBuf mm(24, ctx->stream);
+  unsigned long long init[3] = {~0ull, 0ull, 0ull};
+  QEG_CUDA(cudaMemcpyAsync(mm.get(), init, 24, cudaMemcpyHostToDevice, ctx->stream));
+  if (nbuild) {
+    minmax_kernel<<<grid_for(ctx, nbuild, 256, 8), 256, 0, ctx->stream>>>(ts, nbuild, mm.get<unsigned long long>());
+    ctx->launches++;
+  }
+  unsigned long long r[3];
+  QEG_CUDA(cudaMemcpyAsync(r, mm.get(), 24, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  tmin = r[2] ? dec_i64(r[0]) : 0;
+  const uint64_t range = r[2] ? r[1] - r[0] : 0;
+  int lo_bits = 0, hi_bits = 0;
+  while (lo_bits < 64 && (range >> lo_bits) != 0) ++lo_bits;
+  while (hi_bits < 32 && (static_cast<uint64_t>(aslots) >> hi_bits) != 0) ++hi_bits;
+
+  DevBuf cntb((ns + 1) * 4, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(cntb.get(), 0, (ns + 1) * 4, ctx->stream));
+  const uint64_t n = nbuild;
+  DevBuf a_lo(std::max<uint64_t>(n, 1) * 8, ctx->stream), b_lo(std::max<uint64_t>(n, 1) * 8, ctx->stream);
+  DevBuf a_hi(std::max<uint64_t>(n, 1) * 4, ctx->stream), b_hi(std::max<uint64_t>(n, 1) * 4, ctx->stream);
+  DevBuf a_val(std::max<uint64_t>(n, 1) * 4, ctx->stream), b_val(std::max<uint64_t>(n, 1) * 4, ctx->stream);
+  if (n) {
+    AsofItemsK P{};
+    P.nkeys = nk;
+    for (int j = 0; j < nk; ++j) P.key[j] = store_key(j);
+    P.ts = ts;
+    P.n = n;
+    if (nk) P.T = table();
+    P.nslots = aslots;
+    P.tmin = tmin;
+    P.lo = a_lo.get<uint64_t>();
+    P.hi = a_hi.get<uint32_t>();
+    P.val = a_val.get<uint32_t>();
+    P.cnt = cntb.get<uint32_t>();
+    P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+    asof_items_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  SortItems A{a_lo.get<uint64_t>(), a_hi.get<uint32_t>(), a_val.get<uint32_t>()};
+  SortItems B{b_lo.get<uint64_t>(), b_hi.get<uint32_t>(), b_val.get<uint32_t>()};
+  const SortItems R = radix_sort_items(ctx, A, B, n, lo_bits, hi_bits);
+  aoff.alloc((ns + 1) * 8, ctx->stream);
+  exclusive_scan(ctx, cntb.get<uint32_t>(), ns, aoff.get<uint64_t>());
+  // Keep the sorted timestamps and rows; the slot words are no longer needed.
+  const bool in_a = R.lo == A.lo;
+  ats = in_a ? std::move(a_lo) : std::move(b_lo);
+  arow = in_a ? std::move(a_val) : std::move(b_val);
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  check_device_error(ctx);
 }
 
 // One global hash table of the build keys (+ per-slot row counts).
@@ -1471,6 +1717,60 @@ void validate_probe(const JoinState& st, const qeg_column* cols, int ncols) {
   }
 }
 
+}  // namespace
+
+void JoinState::asof_probe(uint64_t n) {
+  AsofProbeK P{};
+  P.nkeys = static_cast<int>(pkeys.size());
+  for (int j = 0; j < P.nkeys; ++j) P.key[j] = probe_staged[pkeys[j]].dev;
+  P.ts = probe_staged[ptime].dev;
+  P.n = n;
+  if (P.nkeys) P.T = table();
+  P.tmin = tmin;
+  P.ats = ats.get<uint64_t>();
+  P.arow = arow.get<uint32_t>();
+  P.aoff = aoff.get<uint64_t>();
+  P.left = join_type == QEG_LEFT;
+  P.tol_set = tol_set;
+  P.tol = static_cast<uint64_t>(tol);
+  P.err = static_cast<uint32_t*>(ctx->dev_err.get());
+  const unsigned g = grid_for(ctx, n, 256, 8);
+  if (P.left) {
+    out_probe.alloc(n * 4, ctx->stream);
+    out_build.alloc(n * 4, ctx->stream);
+    P.out_probe = out_probe.get<uint32_t>();
+    P.out_build = out_build.get<uint32_t>();
+    asof_probe_kernel<<<g, 256, 0, ctx->stream>>>(P);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+    check_device_error(ctx);
+    nout = n;
+    return;
+  }
+  amatch.alloc(n * 4, ctx->stream);
+  counts.alloc(n * 4, ctx->stream);
+  starts.alloc((n + 1) * 8, ctx->stream);
+  P.match = amatch.get<uint32_t>();
+  P.counts = counts.get<uint32_t>();
+  asof_probe_kernel<<<g, 256, 0, ctx->stream>>>(P);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+  const uint64_t total = exclusive_scan(ctx, counts.get<uint32_t>(), n, starts.get<uint64_t>());
+  out_probe.alloc(std::max<uint64_t>(total, 1) * 4, ctx->stream);
+  out_build.alloc(std::max<uint64_t>(total, 1) * 4, ctx->stream);
+  P.out_probe = out_probe.get<uint32_t>();
+  P.out_build = out_build.get<uint32_t>();
+  if (total) {
+    asof_emit_kernel<<<g, 256, 0, ctx->stream>>>(P, starts.get<uint64_t>());
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  check_device_error(ctx);
+  nout = total;
+}
+
+namespace {
+
 ProbeK probe_params(JoinState& st, uint64_t n) {
   ProbeK P{};
   P.nkeys = static_cast<int>(st.pkeys.size());
@@ -1517,6 +1817,48 @@ qeg_status qeg_join_create(qeg_ctx* ctx, const int32_t* probe_types, int nprobe,
   });
 }
 
+qeg_status qeg_asof_create(qeg_ctx* ctx, const int32_t* probe_types, int nprobe, const int32_t* build_types,
+                           int nbuild, const uint32_t* probe_keys, const uint32_t* build_keys, int nkeys,
+                           uint32_t probe_time, uint32_t build_time, int32_t asof_type, int32_t has_tolerance,
+                           int64_t tolerance, qeg_join** out) {
+  return guarded(ctx, [&] {
+    require(ctx != nullptr && out != nullptr, "ctx/out is NULL");
+    require(nkeys >= 0 && (nkeys == 0 || (probe_keys != nullptr && build_keys != nullptr)), "key lists are NULL");
+    require(nkeys <= kMaxKeys, "GPU as-of join supports at most 8 key columns");
+    require(asof_type == QEG_INNER || asof_type == QEG_LEFT, "unknown as-of join type");
+    require(nprobe >= 1 && nbuild >= 1 && probe_types != nullptr && build_types != nullptr,
+            "join sides need >=1 column");
+    require(probe_time < static_cast<uint32_t>(nprobe) && build_time < static_cast<uint32_t>(nbuild),
+            "as-of time column index out of range");
+    auto ts_ok = [](int32_t t) { return t == QEG_I32 || t == QEG_I64 || t == QEG_TS; };
+    require(ts_ok(probe_types[probe_time]) && ts_ok(build_types[build_time]),
+            "AsofJoin: time columns must be I32/I64/TS");
+    for (int k = 0; k < nkeys; ++k) {
+      require(probe_keys[k] < static_cast<uint32_t>(nprobe) && build_keys[k] < static_cast<uint32_t>(nbuild),
+              "as-of key column index out of range");
+      require(probe_types[probe_keys[k]] == build_types[build_keys[k]],
+              "AsofJoin: key column types must match positionally");
+    }
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    auto j = std::make_unique<qeg_join>();
+    JoinState& st = j->st;
+    st.ctx = ctx;
+    st.ptypes.assign(probe_types, probe_types + nprobe);
+    st.btypes.assign(build_types, build_types + nbuild);
+    st.pkeys.assign(probe_keys, probe_keys + nkeys);
+    st.bkeys.assign(build_keys, build_keys + nkeys);
+    st.join_type = asof_type;
+    st.asof = true;
+    st.ptime = probe_time;
+    st.btime = build_time;
+    st.tol_set = has_tolerance ? 1 : 0;
+    st.tol = tolerance;
+    st.bvals.resize(nbuild);
+    st.bvalid.resize(nbuild);
+    *out = j.release();
+  });
+}
+
 qeg_status qeg_join_build(qeg_join* j, const qeg_column* cols, int ncols) {
   qeg_ctx* ctx = j ? j->st.ctx : nullptr;
   return guarded(ctx, [&] {
@@ -1551,6 +1893,11 @@ qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64
     st.nout = 0;
     if (n == 0) {
       *out_rows = 0;
+      return;
+    }
+    if (st.asof) {
+      st.asof_probe(n);
+      *out_rows = st.nout;
       return;
     }
     st.ensure_csr();
@@ -1589,6 +1936,44 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
         if (outs[c].all_valid) *outs[c].all_valid = 1;
       return;
     }
+    const size_t ncol = st.ptypes.size() + st.btypes.size();
+    bool dev_out = true;
+    for (size_t c = 0; c < ncol; ++c)
+      dev_out = dev_out && outs[c].data && is_device_ptr(outs[c].data) &&
+                (!outs[c].validity || is_device_ptr(outs[c].validity));
+    if (dev_out) {
+      // One pass per column into the caller's device buffers, one sync.
+      DevBuf flags(ncol * 4, ctx->stream);
+      QEG_CUDA(cudaMemsetAsync(flags.get(), 0, ncol * 4, ctx->stream));
+      const unsigned gw = grid_for(ctx, (count + 63) / 64 * 32, 256, 8);
+      for (size_t c = 0; c < ncol; ++c) {
+        const bool pc = c < st.ptypes.size();
+        const size_t bc = pc ? 0 : c - st.ptypes.size();
+        const int w = static_cast<int>(type_width(pc ? st.ptypes[c] : st.btypes[bc]));
+        const void* src = pc ? st.probe_staged[c].dev.data : st.bvals[bc].get();
+        const uint64_t* bits = nullptr;
+        const uint8_t* bytes = nullptr;
+        const int32_t* cm = nullptr;
+        const uint32_t* idx = (pc ? st.out_probe.get<uint32_t>() : st.out_build.get<uint32_t>()) + first;
+        if (pc) {
+          const StagedCol& sc = st.probe_staged[c];
+          bits = sc.dev.all_valid ? nullptr : sc.dev.validity;
+          cm = st.ptypes[c] == QEG_STR ? sc.dev.code_map : nullptr;
+        } else {
+          bytes = st.bvalid[bc].get<uint8_t>();
+        }
+        gather_out_kernel<<<gw, 256, 0, ctx->stream>>>(src, bits, bytes, cm, w, idx, count, outs[c].data,
+                                                      outs[c].validity, flags.get<unsigned int>() + c);
+        ctx->launches++;
+        QEG_CUDA(cudaGetLastError());
+      }
+      std::vector<uint32_t> f(ncol);
+      QEG_CUDA(cudaMemcpyAsync(f.data(), flags.get(), ncol * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (size_t c = 0; c < ncol; ++c)
+        if (outs[c].all_valid) *outs[c].all_valid = f[c] ? 0 : 1;
+      return;
+    }
     DevBuf vals(count * 8, ctx->stream), valid(count, ctx->stream);
     const unsigned g = grid_for(ctx, count, 256, 8);
     for (size_t c = 0; c < st.ptypes.size(); ++c) {
@@ -1620,6 +2005,7 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
     require(j != nullptr && probe_key != nullptr && probe_val != nullptr, "join/columns are NULL");
     JoinState& st = j->st;
     require(st.built, "probe before build_finish()");
+    require(!st.asof, "the count/sum sink is not an as-of join");
     require(st.bkeys.size() == 1, "the count/sum sink takes a single key column");
     require(st.join_type == QEG_INNER, "the count/sum sink is an inner join");
     require(probe_key->type == st.btypes[st.bkeys[0]], "probe key type does not match the build key type");

@@ -608,7 +608,7 @@ double AggState::estimate_groups(const std::vector<StagedCol>& staged, uint64_t 
   }
   SketchResult s;
   const int want_heavy = (cfg.hot_keys != 0) ? 4096 : 0;
-  sketch_key_column(ctx, staged[keys[0]].dev, dsel, nrows, len, 1u << 20, want_heavy, s);
+  sketch_key_column(ctx, key_col(staged, 0), dsel, nrows, len, 1u << 20, want_heavy, s);
   double groups = 0, share = 0;
   if (learned_estimate(ctx, s, &groups, &share)) {
     hot_share = share;

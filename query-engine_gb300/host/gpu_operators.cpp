@@ -126,11 +126,41 @@ GpuAggregate::GpuAggregate(std::unique_ptr<Operator> child, std::vector<std::uin
   child_schema_ = child_->output_schema();
 }
 
+GpuAggregate::GpuAggregate(std::unique_ptr<Operator> child, std::vector<std::uint32_t> key_cols,
+                           std::uint32_t time_col, std::int64_t width, std::vector<AggSpec> aggs, qeg_agg_config cfg,
+                           int device)
+    : window_(true),
+      time_col_(time_col),
+      width_(width),
+      child_(std::move(child)),
+      key_cols_(std::move(key_cols)),
+      aggs_(std::move(aggs)),
+      cfg_(cfg),
+      device_(device) {
+  if (aggs_.empty()) throw std::invalid_argument("Window needs >=1 aggregate");
+  child_schema_ = child_->output_schema();
+  const std::size_t nc = child_schema_.fields.size();
+  for (std::uint32_t k : key_cols_) {
+    if (k >= nc) throw std::invalid_argument("Window: partition key column out of range");
+    if (child_schema_.fields[k].second == Type::STR)
+      throw std::invalid_argument("Window: STR partition keys are not supported (out of grammar)");
+  }
+  for (const AggSpec& a : aggs_)
+    if (a.func != AggFunc::CountStar && a.input_col < nc && child_schema_.fields[a.input_col].second == Type::STR)
+      throw std::invalid_argument("Window: STR aggregate inputs are not supported (out of grammar)");
+  if (time_col_ >= nc) throw std::invalid_argument("Window: time column out of range");
+  const Type tt = child_schema_.fields[time_col_].second;
+  if (tt != Type::I32 && tt != Type::I64 && tt != Type::TS)
+    throw std::invalid_argument("Window: time column must be I32/I64/TS");
+  if (width_ <= 0) throw std::invalid_argument("Window: tumbling width W must be > 0");
+}
+
 GpuAggregate::~GpuAggregate() { close(); }
 
 Schema GpuAggregate::output_schema() const {
   Schema s;
   for (std::uint32_t k : key_cols_) s.fields.push_back(child_schema_.fields[k]);
+  if (window_) s.fields.push_back(child_schema_.fields[time_col_]);  // bucket_start
   for (const AggSpec& a : aggs_) {
     const Type in = a.func == AggFunc::CountStar ? Type::I64 : child_schema_.fields[a.input_col].second;
     s.fields.emplace_back(a.out_name, result_type(a.func, in));
@@ -162,9 +192,14 @@ void GpuAggregate::open() {
     result_type(a.func, in);  // raises the reference's errors (SUM/AVG on STR)
     specs.push_back({agg_func(a.func), a.input_col});
   }
-  dev_->check(qeg_agg_create(dev_->ctx(), qtypes.data(), static_cast<int>(qtypes.size()), key_cols_.data(),
-                             static_cast<int>(key_cols_.size()), specs.data(), static_cast<int>(specs.size()), &cfg_,
-                             &agg_));
+  if (window_)
+    dev_->check(qeg_window_create(dev_->ctx(), qtypes.data(), static_cast<int>(qtypes.size()), key_cols_.data(),
+                                  static_cast<int>(key_cols_.size()), time_col_, width_, specs.data(),
+                                  static_cast<int>(specs.size()), &cfg_, &agg_));
+  else
+    dev_->check(qeg_agg_create(dev_->ctx(), qtypes.data(), static_cast<int>(qtypes.size()), key_cols_.data(),
+                               static_cast<int>(key_cols_.size()), specs.data(), static_cast<int>(specs.size()),
+                               &cfg_, &agg_));
   staging_.reset(types);
   str_ids_.assign(types.size(), nullptr);
   std::vector<StringDict*> ids(types.size(), nullptr);
@@ -219,7 +254,7 @@ void GpuAggregate::open() {
   out_dicts_.assign(out.fields.size(), nullptr);
   for (std::size_t c = 0; c < out.fields.size(); ++c) {
     if (all_valid[c]) result_[c].validity.clear();
-    if (out.fields[c].second != Type::STR) continue;
+    if (out.fields[c].second != Type::STR) continue;  // (a window has no STR outputs)
     const std::uint32_t src = c < key_cols_.size() ? key_cols_[c] : aggs_[c - key_cols_.size()].input_col;
     const StringDict& d = *str_ids_[src];
     auto dict = std::make_shared<StringDict>();
@@ -294,6 +329,34 @@ GpuHashJoin::GpuHashJoin(std::unique_ptr<Operator> probe, std::unique_ptr<Operat
       throw std::invalid_argument("HashJoin: join key column types must match positionally");
 }
 
+GpuHashJoin::GpuHashJoin(std::unique_ptr<Operator> probe, std::unique_ptr<Operator> build,
+                         std::vector<std::uint32_t> probe_keys, std::vector<std::uint32_t> build_keys,
+                         std::uint32_t probe_time, std::uint32_t build_time, tsx::AsofType type,
+                         std::optional<std::int64_t> tolerance, int device)
+    : asof_(true),
+      probe_time_(probe_time),
+      build_time_(build_time),
+      tolerance_(tolerance),
+      probe_(std::move(probe)),
+      build_(std::move(build)),
+      probe_keys_(std::move(probe_keys)),
+      build_keys_(std::move(build_keys)),
+      type_(type == tsx::AsofType::Left ? JoinType::Left : JoinType::Inner),
+      cfg_{},
+      device_(device) {
+  if (probe_keys_.size() != build_keys_.size()) throw std::invalid_argument("asof needs equal-length key lists");
+  probe_schema_ = probe_->output_schema();
+  build_schema_ = build_->output_schema();
+  if (probe_time_ >= probe_schema_.fields.size() || build_time_ >= build_schema_.fields.size())
+    throw std::invalid_argument("AsofJoin: time column out of range");
+  auto ts_ok = [](Type t) { return t == Type::I32 || t == Type::I64 || t == Type::TS; };
+  if (!ts_ok(probe_schema_.fields[probe_time_].second) || !ts_ok(build_schema_.fields[build_time_].second))
+    throw std::invalid_argument("AsofJoin: time columns must be I32/I64/TS");
+  for (std::size_t i = 0; i < probe_keys_.size(); ++i)
+    if (probe_schema_.fields[probe_keys_[i]].second != build_schema_.fields[build_keys_[i]].second)
+      throw std::invalid_argument("AsofJoin: key column types must match positionally");
+}
+
 GpuHashJoin::~GpuHashJoin() { close(); }
 
 Schema GpuHashJoin::output_schema() const {
@@ -319,10 +382,17 @@ void GpuHashJoin::open() {
     btypes.push_back(f.second);
     qb.push_back(f.second == Type::STR ? QEG_I32 : to_qeg(f.second));
   }
-  dev_->check(qeg_join_create(dev_->ctx(), qp.data(), static_cast<int>(qp.size()), qb.data(),
-                              static_cast<int>(qb.size()), probe_keys_.data(), build_keys_.data(),
-                              static_cast<int>(probe_keys_.size()), type_ == JoinType::Left ? QEG_LEFT : QEG_INNER,
-                              &cfg_, &join_));
+  if (asof_)
+    dev_->check(qeg_asof_create(dev_->ctx(), qp.data(), static_cast<int>(qp.size()), qb.data(),
+                                static_cast<int>(qb.size()), probe_keys_.data(), build_keys_.data(),
+                                static_cast<int>(probe_keys_.size()), probe_time_, build_time_,
+                                type_ == JoinType::Left ? QEG_LEFT : QEG_INNER, tolerance_ ? 1 : 0,
+                                tolerance_.value_or(0), &join_));
+  else
+    dev_->check(qeg_join_create(dev_->ctx(), qp.data(), static_cast<int>(qp.size()), qb.data(),
+                                static_cast<int>(qb.size()), probe_keys_.data(), build_keys_.data(),
+                                static_cast<int>(probe_keys_.size()), type_ == JoinType::Left ? QEG_LEFT : QEG_INNER,
+                                &cfg_, &join_));
   // STR: key positions share one value-id space between the sides
   // (ops/join.cpp:48-71); other STR columns get their own dict.
   probe_ids_.assign(ptypes.size(), nullptr);
@@ -417,5 +487,29 @@ void GpuHashJoin::close() {
   dev_.reset();
   opened_ = false;
 }
+
+// ---------------------------------------------------------------------------
+// GpuWindow / GpuAsofJoin
+// ---------------------------------------------------------------------------
+namespace {
+std::int64_t tumbling_width(tsx::WindowMode mode, std::int64_t param) {
+  if (mode != tsx::WindowMode::Tumbling)
+    throw std::invalid_argument("GPU window: only WindowMode::Tumbling runs on the GPU (sliding uses qe::tsx::Window)");
+  return param;
+}
+}  // namespace
+
+GpuWindow::GpuWindow(std::unique_ptr<Operator> child, tsx::WindowMode mode, std::vector<std::uint32_t> keys,
+                     std::uint32_t time, std::int64_t param, std::vector<AggSpec> aggs, qeg_agg_config cfg,
+                     int device)
+    : GpuAggregate(std::move(child), std::move(keys), time, tumbling_width(mode, param), std::move(aggs), cfg,
+                   device) {}
+
+GpuAsofJoin::GpuAsofJoin(std::unique_ptr<Operator> probe, std::unique_ptr<Operator> build,
+                         std::vector<std::uint32_t> probe_keys, std::vector<std::uint32_t> build_keys,
+                         std::uint32_t probe_time, std::uint32_t build_time, tsx::AsofType type,
+                         std::optional<std::int64_t> tolerance, int device)
+    : GpuHashJoin(std::move(probe), std::move(build), std::move(probe_keys), std::move(build_keys), probe_time,
+                  build_time, type, tolerance, device) {}
 
 }  // namespace qe::gpu

@@ -12,6 +12,12 @@
 //                 builds the table; next() probes one probe batch at a time
 //                 and emits <= 2048 output rows per batch, probe columns then
 //                 build columns (ops/join.cpp:260-299).
+//   GpuWindow     qe::tsx::Window (tsx/window.h:82-100) in Tumbling mode: a
+//                 GpuAggregate over (keys..., bucket start of the time
+//                 column), output [keys..., bucket_start, aggregates...].
+//   GpuAsofJoin   qe::tsx::AsofJoin (tsx/asof.h:94-150): a GpuHashJoin whose
+//                 build side is sorted by (key, time) on the GPU and whose
+//                 probe takes the nearest preceding build row per probe row.
 // Errors surface as the reference's exception types: std::invalid_argument,
 // std::overflow_error, std::bad_alloc, std::runtime_error otherwise.
 #pragma once
@@ -83,8 +89,18 @@ class GpuAggregate : public Operator {
   void close() override;
   Schema output_schema() const override;
 
+ protected:
+  // Tumbling window: GROUP BY (key_cols..., (t / width) * width of time_col),
+  // with the Window constructor's checks (tsx/window.cpp:214-241).
+  GpuAggregate(std::unique_ptr<Operator> child, std::vector<std::uint32_t> key_cols, std::uint32_t time_col,
+               std::int64_t width, std::vector<AggSpec> aggs, qeg_agg_config cfg, int device);
+
  private:
   void flush();
+
+  bool window_ = false;
+  std::uint32_t time_col_ = 0;
+  std::int64_t width_ = 0;
 
   std::unique_ptr<Operator> child_;
   std::vector<std::uint32_t> key_cols_;
@@ -117,8 +133,19 @@ class GpuHashJoin : public Operator {
   void close() override;
   Schema output_schema() const override;
 
+ protected:
+  // Backward as-of join, with the AsofJoin constructor's checks
+  // (tsx/asof.cpp:130-160); key lists may be empty.
+  GpuHashJoin(std::unique_ptr<Operator> probe, std::unique_ptr<Operator> build, std::vector<std::uint32_t> probe_keys,
+              std::vector<std::uint32_t> build_keys, std::uint32_t probe_time, std::uint32_t build_time,
+              tsx::AsofType type, std::optional<std::int64_t> tolerance, int device);
+
  private:
   bool probe_next_batch();
+
+  bool asof_ = false;
+  std::uint32_t probe_time_ = 0, build_time_ = 0;
+  std::optional<std::int64_t> tolerance_;
 
   std::unique_ptr<Operator> probe_, build_;
   std::vector<std::uint32_t> probe_keys_, build_keys_;
@@ -133,6 +160,28 @@ class GpuHashJoin : public Operator {
   std::uint64_t pending_ = 0, cursor_ = 0;
   std::vector<HostColumn> current_;
   bool opened_ = false, probe_done_ = false;
+};
+
+// qe::tsx::Window on the GPU. WindowMode::Sliding (a sort and a running
+// frame, not a hash-table caller) is rejected with std::invalid_argument.
+class GpuWindow : public GpuAggregate {
+ public:
+  static constexpr std::size_t kOutBatch = 2048;  // tsx/window.h:85
+
+  GpuWindow(std::unique_ptr<Operator> child, tsx::WindowMode mode, std::vector<std::uint32_t> keys,
+            std::uint32_t time, std::int64_t param, std::vector<AggSpec> aggs, qeg_agg_config cfg = {},
+            int device = 0);
+};
+
+// qe::tsx::AsofJoin on the GPU: same constructor arguments and output schema
+// (all probe columns, then all build columns).
+class GpuAsofJoin : public GpuHashJoin {
+ public:
+  static constexpr std::size_t kOutBatch = 2048;  // tsx/asof.h:97
+
+  GpuAsofJoin(std::unique_ptr<Operator> probe, std::unique_ptr<Operator> build, std::vector<std::uint32_t> probe_keys,
+              std::vector<std::uint32_t> build_keys, std::uint32_t probe_time, std::uint32_t build_time,
+              tsx::AsofType type, std::optional<std::int64_t> tolerance = std::nullopt, int device = 0);
 };
 
 }  // namespace qe::gpu

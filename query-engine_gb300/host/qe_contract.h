@@ -12,6 +12,8 @@
 //   StringDict (interface)     core/string_dict.h:34-72
 //   AggFunc / AggSpec          ops/aggregate.h:61-89
 //   JoinType                   ops/join.h:59
+//   tsx::WindowMode            tsx/window.h:79
+//   tsx::AsofType              tsx/asof.h:90
 // When compiled inside the reference tree, define QEG_WITH_REFERENCE_HEADERS
 // and the reference's own headers are used instead of these.
 #pragma once
@@ -24,6 +26,8 @@
 #include "ops/aggregate.h"
 #include "ops/join.h"
 #include "ops/operator.h"
+#include "tsx/asof.h"
+#include "tsx/window.h"
 #else
 
 #include <cstddef>
@@ -134,6 +138,11 @@ struct AggSpec {
 };
 
 enum class JoinType { Inner, Left };
+
+namespace tsx {
+enum class WindowMode { Tumbling, Sliding };
+enum class AsofType { Inner, Left };
+}  // namespace tsx
 
 }  // namespace qe
 

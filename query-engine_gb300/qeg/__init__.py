@@ -86,6 +86,9 @@ def lib():
         }
         optional = {
             "qeg_join_create": (i32, [vp, vp, c, vp, c, vp, vp, c, i32, vp, P(vp)]),
+            "qeg_asof_create": (i32, [vp, vp, c, vp, c, vp, vp, c, ctypes.c_uint32, ctypes.c_uint32, i32, i32,
+                                      ctypes.c_int64, P(vp)]),
+            "qeg_window_create": (i32, [vp, vp, c, vp, c, ctypes.c_uint32, ctypes.c_int64, vp, c, vp, P(vp)]),
             "qeg_join_build": (i32, [vp, vp, c]),
             "qeg_join_build_finish": (i32, [vp]),
             "qeg_join_probe": (i32, [vp, vp, c, P(u64)]),
@@ -344,6 +347,32 @@ def groupby(ctx, cols, key_cols, aggs, config=None, batch_rows=None, sel=None):
         a.close()
 
 
+class Window(Aggregate):
+    """Tumbling window (qeg_window_create): GROUP BY (key_cols..., bucket
+    start of time_col with bucket width `width`); results are keys, the bucket
+    start (typed as the time column), then the aggregates."""
+
+    def __init__(self, ctx, col_types, key_cols, time_col, width, aggs, config=None):
+        self.ctx = ctx
+        self.ncols = len(col_types)
+        self.nkeys = len(key_cols) + 1
+        self.naggs = len(aggs)
+        types = (ctypes.c_int32 * len(col_types))(*col_types)
+        keys = (ctypes.c_uint32 * max(1, len(key_cols)))(*key_cols)
+        specs = (AggSpec * max(1, len(aggs)))()
+        for i, (f, c) in enumerate(aggs):
+            specs[i] = AggSpec(f, c)
+        cfg = config if config is not None else agg_config()
+        p = ctypes.c_void_p()
+        _check(lib().qeg_window_create(ctx.p, types, len(col_types), keys, len(key_cols), time_col, width, specs,
+                                       len(aggs), ctypes.byref(cfg), ctypes.byref(p)), ctx.p)
+        self.p = p
+        rt = (ctypes.c_int32 * (self.nkeys + self.naggs))()
+        _check(lib().qeg_agg_result_types(p, rt), ctx.p)
+        self.result_types = list(rt)
+        self.rows = None
+
+
 class Join:
     """The GPU hash-join operator state behind one qeg_join."""
 
@@ -390,6 +419,27 @@ class Join:
         _check(lib().qeg_join_fetch(self.p, first, count, outs), self.ctx.p)
         return [(v[:count], unpack_validity(w, count)) for v, w, _ in keep]
 
+    def fetch_device(self, first=0, count=None, bufs=None):
+        """Like fetch(), into torch CUDA tensors [(values, validity words)]:
+        one gather pass per column straight into them. `bufs` (a previous
+        result, large enough) is reused when given."""
+        import torch
+
+        if count is None:
+            count = self.rows - first
+        types = self.probe_types + self.build_types
+        tdt = {I32: torch.int32, I64: torch.int64, F64: torch.float64, BOOL: torch.uint8, TS: torch.int64,
+               STR: torch.int32}
+        if bufs is None:
+            bufs = [(torch.empty(max(count, 1), dtype=tdt[t], device="cuda"),
+                     torch.empty(max(1, (count + 63) // 64), dtype=torch.int64, device="cuda")) for t in types]
+            torch.cuda.synchronize()  # the library writes them on its own stream
+        outs = (OutColumn * len(types))()
+        for i, (v, w) in enumerate(bufs):
+            outs[i] = OutColumn(v.data_ptr(), w.data_ptr(), None)
+        _check(lib().qeg_join_fetch(self.p, first, count, outs), self.ctx.p)
+        return bufs
+
     def probe_count_sum(self, key, val):
         k, v = Column(), Column()
         k, v = key.c(), val.c()
@@ -416,6 +466,29 @@ class Join:
             self.close()
         except Exception:
             pass
+
+
+class AsofJoin(Join):
+    """Backward as-of join (qeg_asof_create): per probe row the build row of
+    the same key with the greatest time <= the probe's time (within
+    `tolerance` when given). build / build_finish / probe / fetch as Join."""
+
+    def __init__(self, ctx, probe_types, build_types, probe_keys, build_keys, probe_time, build_time,
+                 asof_type=INNER, tolerance=None):
+        self.ctx = ctx
+        self.probe_types = list(probe_types)
+        self.build_types = list(build_types)
+        pt = (ctypes.c_int32 * max(1, len(probe_types)))(*probe_types)
+        bt = (ctypes.c_int32 * max(1, len(build_types)))(*build_types)
+        pk = (ctypes.c_uint32 * max(1, len(probe_keys)))(*probe_keys)
+        bk = (ctypes.c_uint32 * max(1, len(build_keys)))(*build_keys)
+        p = ctypes.c_void_p()
+        self.p = None
+        _check(lib().qeg_asof_create(ctx.p, pt, len(probe_types), bt, len(build_types), pk, bk, len(probe_keys),
+                                     probe_time, build_time, asof_type, 0 if tolerance is None else 1,
+                                     0 if tolerance is None else int(tolerance), ctypes.byref(p)), ctx.p)
+        self.p = p
+        self.rows = 0
 
 
 def join_count_sum_noalloc(stream, build_key, probe_key, probe_val, out):

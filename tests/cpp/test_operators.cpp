@@ -1,4 +1,4 @@
-// Drives qe::gpu::GpuAggregate / GpuHashJoin through the reference's pull
+// Drives qe::gpu::GpuAggregate / GpuHashJoin / GpuWindow / GpuAsofJoin through the reference's pull
 // interface (Operator::open/next/close, Batch/Column views) exactly as a plan
 // tree would, and checks the drained results against values computed here on
 // the CPU and against expectations written in the reference's own tests.
@@ -343,6 +343,122 @@ void test_join_str_keys() {
   CHECK((got == std::multiset<std::pair<std::string, int64_t>>{{"MSFT", 3}, {"AAPL", 2}, {"AAPL", 2}}));
 }
 
+void test_window_tumbling() {
+  // tests/window_differential_test.cpp make_input of the reference, width 10.
+  TestTable t;
+  t.schema.fields = {{"c0", Type::I32}, {"c1", Type::TS}, {"c2", Type::I64}, {"c3", Type::F64}};
+  t.cols.push_back(make_col<int32_t>(Type::I32, {1, 1, 1, 2, 2, 1}));
+  t.cols.push_back(make_col<int64_t>(Type::TS, {0, 5, 12, 3, 21, 30}));
+  t.cols.push_back(make_col<int64_t>(Type::I64, {10, 20, 30, 40, 50, 60}, {2}));
+  t.cols.push_back(make_col<double>(Type::F64, {1.5, 2.5, 3.5, 4.5, 5.5, 6.5}));
+  gpu::GpuWindow w(std::make_unique<TestScan>(t, 64), tsx::WindowMode::Tumbling, {0}, 1, 10,
+                   {AggSpec::count_star("n"), AggSpec::sum(2, "s"), AggSpec::avg(3, "a")});
+  const Schema sch = w.output_schema();
+  CHECK(sch.fields.size() == 5 && sch.fields[1].first == "c1" && sch.fields[1].second == Type::TS);
+  auto rows = drain(w);
+  std::set<std::tuple<int64_t, int64_t, int64_t, bool, int64_t>> got;
+  for (Row& r : rows) got.insert({r[0].i, r[1].i, r[2].i, r[3].null, r[3].null ? 0 : r[3].i});
+  // (key, bucket, n, sum null?, sum): t 0,5 -> 0; 12 -> 10 (NULL value); 30 -> 30; key 2: 3 -> 0, 21 -> 20
+  CHECK((got == std::set<std::tuple<int64_t, int64_t, int64_t, bool, int64_t>>{
+                    {1, 0, 2, false, 30}, {1, 10, 1, true, 0}, {1, 30, 1, false, 60}, {2, 0, 1, false, 40},
+                    {2, 20, 1, false, 50}}));
+  // 5000 one-row buckets cross the 2048-row output batch; zero partition keys.
+  TestTable big;
+  big.schema.fields = {{"t", Type::I64}};
+  std::vector<int64_t> tv(10000);
+  for (int i = 0; i < 10000; ++i) tv[i] = i;
+  big.cols.push_back(make_col(Type::I64, tv));
+  gpu::GpuWindow wb(std::make_unique<TestScan>(big, 2048), tsx::WindowMode::Tumbling, {}, 0, 2,
+                    {AggSpec::count_star("n")});
+  auto brows = drain(wb);
+  CHECK(brows.size() == 5000);
+  int64_t total = 0;
+  for (Row& r : brows) total += r[1].i;
+  CHECK(total == 10000);
+  // Sliding mode and bad widths / time types are rejected.
+  for (int bad = 0; bad < 3; ++bad) {
+    bool threw = false;
+    try {
+      if (bad == 0)
+        gpu::GpuWindow x(std::make_unique<TestScan>(t, 64), tsx::WindowMode::Sliding, {0}, 1, 2,
+                         {AggSpec::count_star("n")});
+      else if (bad == 1)
+        gpu::GpuWindow x(std::make_unique<TestScan>(t, 64), tsx::WindowMode::Tumbling, {0}, 1, 0,
+                         {AggSpec::count_star("n")});
+      else
+        gpu::GpuWindow x(std::make_unique<TestScan>(t, 64), tsx::WindowMode::Tumbling, {0}, 3, 10,
+                         {AggSpec::count_star("n")});
+    } catch (const std::invalid_argument&) {
+      threw = true;
+    }
+    CHECK(threw);
+  }
+}
+
+void test_asof_join() {
+  // tests/asof_differential_test.cpp make_build / make_probe of the reference.
+  TestTable b, p;
+  b.schema.fields = {{"c0", Type::I32}, {"c1", Type::TS}, {"c2", Type::I64}};
+  b.cols.push_back(make_col<int32_t>(Type::I32, {1, 1, 1, 2}));
+  b.cols.push_back(make_col<int64_t>(Type::TS, {10, 20, 30, 15}));
+  b.cols.push_back(make_col<int64_t>(Type::I64, {100, 200, 300, 150}));
+  p.schema.fields = {{"c0", Type::I32}, {"c1", Type::TS}};
+  p.cols.push_back(make_col<int32_t>(Type::I32, {1, 1, 1, 2, 3, 1}));
+  p.cols.push_back(make_col<int64_t>(Type::TS, {5, 10, 25, 15, 99, 50}));
+  using R = std::tuple<int64_t, int64_t, bool, int64_t>;
+  for (auto type : {tsx::AsofType::Inner, tsx::AsofType::Left}) {
+    for (int tol = 0; tol < 2; ++tol) {
+      std::optional<int64_t> t;
+      if (tol) t = 10;
+      gpu::GpuAsofJoin j(std::make_unique<TestScan>(p, 64), std::make_unique<TestScan>(b, 64), {0}, {0}, 1, 1, type,
+                         t);
+      CHECK(j.output_schema().fields.size() == 5);
+      auto rows = drain(j);
+      std::multiset<R> got;
+      for (Row& r : rows) got.insert({r[0].i, r[1].i, r[4].null, r[4].null ? 0 : r[4].i});
+      // (1,5) precedes every build row; (1,10) takes the equal time; with
+      // tolerance 10, (1,50) -> t30 is 20 back and is dropped.
+      std::multiset<R> exp = {{1, 10, false, 100}, {2, 15, false, 150}, {1, 25, false, 200}};
+      if (!tol) exp.insert({1, 50, false, 300});
+      if (type == tsx::AsofType::Left) {
+        exp.insert({1, 5, true, 0});
+        exp.insert({3, 99, true, 0});
+        if (tol) exp.insert({1, 50, true, 0});
+      }
+      CHECK(got == exp);
+    }
+  }
+  // Zero partition keys, and a probe side of 5000 rows crossing output batches.
+  TestTable gb, gp;
+  gb.schema.fields = {{"t", Type::TS}, {"v", Type::I64}};
+  gb.cols.push_back(make_col<int64_t>(Type::TS, {10, 20, 30}));
+  gb.cols.push_back(make_col<int64_t>(Type::I64, {100, 200, 300}));
+  gp.schema.fields = {{"t", Type::TS}};
+  std::vector<int64_t> pt(5000);
+  for (int i = 0; i < 5000; ++i) pt[i] = i % 40;
+  gp.cols.push_back(make_col(Type::TS, pt));
+  gpu::GpuAsofJoin g(std::make_unique<TestScan>(gp, 2048), std::make_unique<TestScan>(gb, 64), {}, {}, 0, 0,
+                     tsx::AsofType::Inner);
+  auto rows = drain(g);
+  int64_t s = 0;
+  for (Row& r : rows) s += r[2].i;
+  // per 40 probe times: 10 match t10 (100), 10 t20 (200), 10 t30 (300), 10 none
+  CHECK(rows.size() == 3750);
+  CHECK(s == 125 * (10 * 100 + 10 * 200 + 10 * 300));
+  bool threw = false;
+  try {
+    TestTable f;
+    f.schema.fields = {{"k", Type::I32}, {"t", Type::F64}};
+    f.cols.push_back(make_col<int32_t>(Type::I32, {1}));
+    f.cols.push_back(make_col<double>(Type::F64, {1.0}));
+    gpu::GpuAsofJoin bad(std::make_unique<TestScan>(f, 64), std::make_unique<TestScan>(b, 64), {0}, {0}, 1, 1,
+                         tsx::AsofType::Inner);
+  } catch (const std::invalid_argument&) {
+    threw = true;
+  }
+  CHECK(threw);
+}
+
 int main() {
   try {
     test_aggregate_edge_table();
@@ -351,6 +467,8 @@ int main() {
     test_aggregate_errors_and_global_empty();
     test_join_edge_cases();
     test_join_str_keys();
+    test_window_tumbling();
+    test_asof_join();
   } catch (const std::exception& e) {
     std::fprintf(stderr, "exception: %s\n", e.what());
     return 2;

@@ -4,8 +4,10 @@ oracle/_ref/libqe_ref.so by `make -C oracle ref`).
 
 Cases:
   * the hand-built edge tables of the reference's tests/aggregate_differential_test.cpp,
-    tests/join_differential_test.cpp, tests/oracle_zero_row_test.cpp and the
-    F64-key case of tests/hashtable_test.cpp, restated as inputs;
+    tests/join_differential_test.cpp, tests/oracle_zero_row_test.cpp, the
+    F64-key case of tests/hashtable_test.cpp, and the tumbling-window and as-of
+    edge tables of tests/window_differential_test.cpp and
+    tests/asof_differential_test.cpp, restated as inputs;
   * seeded random GROUP BY and join cases in the shape of the reference's
     generators (bounded magnitudes, ~15% NULLs);
   * the splitmix64 row-hash fold at boundary inputs (ops/hash_scalar.cpp).
@@ -82,6 +84,122 @@ def join_case(name, probe, build, pk, bk, jt):
             "probe_keys": pk, "build_keys": bk, "join_type": jt, "types": ref_t, "rows": enc_rows(ref_t, ref_rows)}
 
 
+def window_case(name, cols, keys, time_col, width, aggs):
+    ref_t, ref_rows = O.ref_window_tumbling(cols, keys, time_col, width, aggs, 2048, mode=0)
+    ind_t, ind_rows = O.ref_window_tumbling(cols, keys, time_col, width, aggs, 2048, mode=1)
+    m = O.compare(ref_t, ref_rows, ind_t, ind_rows)
+    assert m is None, (name, m)
+    for bs in (64, 256):
+        bt, brows = O.ref_window_tumbling(cols, keys, time_col, width, aggs, bs, mode=0)
+        assert O.compare(ref_t, ref_rows, bt, brows) is None, (name, bs)
+    return {"kind": "window", "name": name, "columns": [enc_col(c) for c in cols], "keys": keys,
+            "time_col": time_col, "width": width, "aggs": [list(a) for a in aggs], "types": ref_t,
+            "rows": enc_rows(ref_t, ref_rows)}
+
+
+def asof_case(name, probe, build, pk, bk, pt, bt, jt, tol, unique_build=True):
+    """Expected rows: the reference's AsofJoin operator. Its independent oracle
+    must agree where build (key, time) pairs are unique (the reference leaves
+    the pick among equal build times to its stable sort)."""
+    ref_t, ref_rows = O.ref_asof_join(probe, build, pk, bk, pt, bt, jt, tol, 2048, mode=0)
+    if unique_build:
+        ind_t, ind_rows = O.ref_asof_join(probe, build, pk, bk, pt, bt, jt, tol, 2048, mode=1)
+        m = O.compare(ref_t, ref_rows, ind_t, ind_rows)
+        assert m is None, (name, m)
+    for bs in (64, 256):
+        b_t, brows = O.ref_asof_join(probe, build, pk, bk, pt, bt, jt, tol, bs, mode=0)
+        assert O.compare(ref_t, ref_rows, b_t, brows) is None, (name, bs)
+    return {"kind": "asof", "name": name, "probe": [enc_col(c) for c in probe], "build": [enc_col(c) for c in build],
+            "probe_keys": pk, "build_keys": bk, "probe_time": pt, "build_time": bt, "join_type": jt,
+            "tolerance": tol, "types": ref_t, "rows": enc_rows(ref_t, ref_rows)}
+
+
+def tsx_cases(rng):
+    """Tumbling-window and as-of cases: the reference tests' edge tables, then
+    seeded tick-like random cases."""
+    cases = []
+    win = [col(O.I32, [1, 1, 1, 2, 2, 1]), col(O.TS, [0, 5, 12, 3, 21, 30]),
+           col(O.I64, [10, 20, 30, 40, 50, 60], nulls=[2]), col(O.F64, [1.5, 2.5, 3.5, 4.5, 5.5, 6.5])]
+    all_aggs = [(O.COUNT_STAR, 0), (O.COUNT, 2), (O.SUM, 2), (O.MIN, 2), (O.MAX, 2), (O.AVG, 3)]
+    cases.append(window_case("window_edge_single_key_w10", win, [0], 1, 10, all_aggs))
+    cases.append(window_case("window_edge_zero_keys_w8", win, [], 1, 8, all_aggs))
+    cases.append(window_case("window_edge_width_1", win, [0], 1, 1, all_aggs))
+    nullk = [col(O.I32, [1, 1, 7, 7], nulls=[2, 3]), col(O.TS, [0, 10, 5, 20]), col(O.I64, [100, 200, 300, 400])]
+    cases.append(window_case("window_edge_null_keys_group_together", nullk, [0], 1, 10,
+                             [(O.COUNT_STAR, 0), (O.SUM, 2)]))
+    cases.append(window_case("window_edge_empty", [col(O.I32, []), col(O.TS, [])], [0], 1, 10, [(O.COUNT_STAR, 0)]))
+    i32ts = [col(O.I32, [1, 1, 1, 2]), col(O.I32, [7, 7, 9, 7]), col(O.I32, [0, 11, 4, 25]),
+             col(O.I64, [100, 200, 300, 400])]
+    cases.append(window_case("window_edge_i32_time_composite", i32ts, [0, 1], 2, 10,
+                             [(O.COUNT_STAR, 0), (O.SUM, 3), (O.MIN, 2)]))
+    nan_w = [col(O.I32, [1, 1, 1, 1, 2, 2, 2, 2]), col(O.TS, [0, 5, 12, 17, 1, 6, 11, 21]),
+             col(O.F64, [3.0, NAN, NAN, NAN, NAN, 2.0, 0.0, 4.0], nulls=[6])]
+    cases.append(window_case("window_edge_nan_minmax", nan_w, [0], 1, 10, [(O.MIN, 2), (O.MAX, 2), (O.COUNT, 2)]))
+    # Negative times: C++ truncating division, (-15 / 10) * 10 = -10.
+    cases.append(window_case("window_edge_negative_time", [col(O.I32, [1, 1, 1, 1, 1]),
+                                                           col(O.I64, [-15, -5, -1, 0, 4]), col(O.I64, [1, 2, 3, 4, 5])],
+                             [0], 1, 10, [(O.COUNT_STAR, 0), (O.SUM, 2)]))
+    cases.append(window_case("window_edge_null_time", [col(O.I32, [1, 1, 2]), col(O.TS, [3, 0, 14], nulls=[1]),
+                                                       col(O.I64, [1, 2, 3])], [0], 1, 10,
+                             [(O.COUNT_STAR, 0), (O.SUM, 2)]))
+    for it in range(12):
+        n = int(rng.integers(0, 400))
+        tt = [O.TS, O.I64, O.I32][it % 3]
+        cols = [gen_column(rng, O.I32, n, 10, int(rng.integers(1, 8))),
+                col(tt, rng.integers(0, 1000, n).tolist(), nulls=np.flatnonzero(rng.random(n) < 0.05).tolist()),
+                gen_column(rng, O.I64, n, 10), gen_column(rng, O.F64, n, 10)]
+        keys = [0] if it % 2 == 0 else []
+        aggs = [(O.COUNT_STAR, 0), (O.SUM, 2), (O.MIN, 2), (O.MAX, 3), (O.AVG, 3), (O.COUNT, 3)]
+        cases.append(window_case("window_random_%02d" % it, cols, keys, 1, int(rng.choice([1, 7, 50, 250, 5000])),
+                                 aggs))
+    # --- as-of edge tables (tests/asof_differential_test.cpp) ------------------
+    build = [col(O.I32, [1, 1, 1, 2]), col(O.TS, [10, 20, 30, 15]), col(O.I64, [100, 200, 300, 150])]
+    probe = [col(O.I32, [1, 1, 1, 2, 3, 1]), col(O.TS, [5, 10, 25, 15, 99, 50])]
+    for jt in (O.INNER, O.LEFT):
+        sfx = "_left" if jt else "_inner"
+        cases.append(asof_case("asof_edge_single_key" + sfx, probe, build, [0], [0], 1, 1, jt, None))
+        cases.append(asof_case("asof_edge_tolerance_10" + sfx, probe, build, [0], [0], 1, 1, jt, 10))
+        cases.append(asof_case("asof_edge_zero_keys" + sfx, [col(O.TS, [5, 25, 35])],
+                               [col(O.TS, [10, 20, 30]), col(O.I64, [100, 200, 300])], [], [], 0, 0, jt, None))
+        cases.append(asof_case("asof_edge_empty_build" + sfx, probe, [col(O.I32, []), col(O.TS, [])], [0], [0], 1, 1,
+                               jt, None))
+        cases.append(asof_case("asof_edge_nulls_never_match" + sfx,
+                               [col(O.I32, [1, 2, 2, 9], nulls=[3]), col(O.TS, [25, 30, 0, 50], nulls=[2])],
+                               [col(O.I32, [1, 1, 2, 7], nulls=[3]), col(O.TS, [10, 20, 0, 5], nulls=[2]),
+                                col(O.I64, [100, 200, 999, 777])], [0], [0], 1, 1, jt, None))
+    cases.append(asof_case("asof_edge_empty_probe", [col(O.I32, []), col(O.TS, [])], build, [0], [0], 1, 1, O.INNER,
+                           None))
+    cases.append(asof_case("asof_edge_composite_key", [col(O.I32, [1, 1]), col(O.I32, [7, 9]), col(O.TS, [25, 25])],
+                           [col(O.I32, [1, 1, 1]), col(O.I32, [7, 7, 9]), col(O.TS, [10, 20, 10])], [0, 1], [0, 1],
+                           2, 2, O.INNER, None))
+    # Equal build times within a key: the build row drained last wins.
+    cases.append(asof_case("asof_edge_equal_build_times",
+                           [col(O.I32, [1, 1, 2]), col(O.TS, [20, 9, 40])],
+                           [col(O.I32, [1, 1, 1, 2, 2]), col(O.TS, [10, 20, 10, 40, 40]),
+                            col(O.I64, [1, 2, 3, 4, 5])], [0], [0], 1, 1, O.LEFT, None, unique_build=False))
+    # I32 time on the probe side against TS on the build side.
+    cases.append(asof_case("asof_edge_i32_probe_time", [col(O.I32, [1, 1, 2]), col(O.I32, [15, 35, 20])], build,
+                           [0], [0], 1, 1, O.LEFT, None))
+    for it in range(16):
+        nsym = int(rng.integers(1, 12))
+        nb, npr = int(rng.integers(0, 300)), int(rng.integers(0, 300))
+        # unique (key, time) on the build side, times >= 0
+        pairs = rng.permutation(nsym * 2000)[:nb]
+        bsym, bts = (pairs % nsym).tolist(), (pairs // nsym).tolist()
+        build = [col(O.I32, bsym, nulls=np.flatnonzero(rng.random(nb) < 0.05).tolist()),
+                 col(O.TS, bts, nulls=np.flatnonzero(rng.random(nb) < 0.05).tolist()),
+                 gen_column(rng, O.F64, nb, 10)]
+        probe = [col(O.I32, rng.integers(0, nsym + 2, npr).tolist(),
+                     nulls=np.flatnonzero(rng.random(npr) < 0.05).tolist()),
+                 col(O.TS, rng.integers(0, 2100, npr).tolist(), nulls=np.flatnonzero(rng.random(npr) < 0.05).tolist()),
+                 gen_column(rng, O.I64, npr, 10)]
+        tol = None if it % 3 else int(rng.integers(0, 300))
+        keys = [0] if it % 4 != 3 else []
+        cases.append(asof_case("asof_random_%02d" % it, probe, build, keys, keys, 1, 1, int(rng.integers(0, 2)), tol,
+                               unique_build=bool(keys)))
+    return cases
+
+
 def main():
     if not O.ref_available():
         sys.exit("oracle/_ref/libqe_ref.so is missing: run `make -C oracle ref` where the reference tree exists")
@@ -148,6 +266,7 @@ def main():
         probe = [gen_column(rng, t, npr, 10, card * 2) for t in kt] + [gen_column(rng, O.F64, npr, 10)]
         cases.append(join_case("join_random_%02d" % it, probe, build, list(range(nk)), list(range(nk)),
                                int(rng.integers(0, 2))))
+    cases += tsx_cases(np.random.default_rng(20260616))
     # --- hash fold pins (ops/hash_scalar.cpp) ----------------------------------
     R = O.ref()
     seeds = [0, 1, 0x51E57A11AB1E5EED, 2**64 - 1]

@@ -262,3 +262,38 @@ def test_partitioned_join_materialises_pairs(ctx):
     j.close()
     gt, grows = gpu_rows(res, ot)
     assert_same(gt, grows, ot, orows, "partitioned join pairs")
+
+
+@pytest.mark.parametrize("jt", [O.INNER, O.LEFT])
+def test_device_fetch_matches_host_fetch(ctx, jt):
+    # Device output buffers take the single-pass gather (values and packed
+    # validity written directly); it must equal the host fetch bit for bit,
+    # including ranges that start inside a validity word and STR code maps.
+    import torch
+
+    rng = np.random.default_rng(77)
+    nb, npr = 5000, 20000
+    d = ["k%02d" % i for i in range(40)]
+    build = [gen_column(rng, O.I64, nb, 10, 3000), gen_column(rng, O.F64, nb, 10), gen_column(rng, O.I32, nb, 20),
+             O.TCol(O.STR, rng.integers(0, 40, nb).astype(np.int32), rng.random(nb) > 0.1, d)]
+    probe = [gen_column(rng, O.I64, npr, 10, 4000), gen_column(rng, O.BOOL, npr, 10),
+             O.TCol(O.STR, rng.integers(0, 40, npr).astype(np.int32), rng.random(npr) > 0.1, d[::-1])]
+    canon = StrCanon(d)
+    j = qeg.Join(ctx, [c.type for c in probe], [c.type for c in build], [0], [0], jt)
+    try:
+        j.build([to_gpu(c, canon) for c in build])
+        j.build_finish()
+        n = j.probe([to_gpu(c, canon) for c in probe])
+        assert n > 1000
+        for first, count in ((0, n), (37, n - 100), (n - 1, 1)):
+            host = j.fetch(first, count)
+            dev = j.fetch_device(first, count)
+            torch.cuda.synchronize()
+            for (hv, hvalid), (dv, dw) in zip(host, dev):
+                dvals = dv[:count].cpu().numpy()
+                words = dw.cpu().numpy().view(np.uint64)
+                dvalid = np.unpackbits(words.view(np.uint8), bitorder="little")[:count].astype(bool)
+                assert np.array_equal(dvalid, hvalid)
+                assert np.array_equal(dvals[dvalid].view(np.uint8), np.asarray(hv)[hvalid].view(np.uint8))
+    finally:
+        j.close()

@@ -35,6 +35,20 @@ def test_oracle_matches_reference_golden(case):
     if case["kind"] == "groupby":
         cols = [dec_col(c) for c in case["columns"]]
         t, rows = O.groupby(cols, case["keys"], [tuple(a) for a in case["aggs"]])
+    elif case["kind"] == "window":
+        cols = [dec_col(c) for c in case["columns"]]
+        t, rows = O.window_tumbling(cols, case["keys"], case["time_col"], case["width"],
+                                    [tuple(a) for a in case["aggs"]])
+    elif case["kind"] == "asof":
+        probe = [dec_col(c) for c in case["probe"]]
+        build = [dec_col(c) for c in case["build"]]
+        t, rows = O.asof_join(probe, build, case["probe_keys"], case["build_keys"], case["probe_time"],
+                              case["build_time"], case["join_type"], case["tolerance"])
+        # The reference emits as-of rows in its sorted probe order, the
+        # restatement in probe order: compare as multisets.
+        assert t == types
+        assert O.compare(t, rows, types, exp) is None
+        return
     else:
         probe = [dec_col(c) for c in case["probe"]]
         build = [dec_col(c) for c in case["build"]]
@@ -63,6 +77,20 @@ def test_known_answers_from_reference_tests():
     assert len(by["hashtable_f64_key_canonicalisation"]["rows"]) == 3
     assert by["agg_zero_row_global"]["rows"] == [[0, 0, None, None, None, None]]
     assert by["agg_zero_row_keyed"]["rows"] == []
+    # Tumbling window edge table: key 1 rows at t 0, 5 -> bucket 0; t 12 -> 10;
+    # t 30 -> 30; key 2 at t 3 -> 0 and t 21 -> 20.
+    rows = dec_rows(by["window_edge_single_key_w10"]["types"], by["window_edge_single_key_w10"]["rows"])
+    assert sorted((r[0], r[1], r[2]) for r in rows) == [(1, 0, 2), (1, 10, 1), (1, 30, 1), (2, 0, 1), (2, 20, 1)]
+    rows = dec_rows(by["window_edge_negative_time"]["types"], by["window_edge_negative_time"]["rows"])
+    assert sorted(r[1] for r in rows) == [-10, 0]
+    # As-of edge table: probe (1,5) has no preceding build row; (1,10) takes the
+    # equal-time row (boundary >=); (1,25) -> t20; (2,15) -> t15; key 3 has no
+    # partition; (1,50) -> t30.
+    rows = dec_rows(by["asof_edge_single_key_left"]["types"], by["asof_edge_single_key_left"]["rows"])
+    got = sorted((r[0], r[1], r[4]) for r in rows)
+    assert got == [(1, 5, None), (1, 10, 100), (1, 25, 200), (1, 50, 300), (2, 15, 150), (3, 99, None)]
+    rows = dec_rows(by["asof_edge_equal_build_times"]["types"], by["asof_edge_equal_build_times"]["rows"])
+    assert sorted((r[0], r[1], r[4]) for r in rows) == [(1, 9, None), (1, 20, 2), (2, 40, 5)]
 
 
 @pytest.mark.skipif(not O.ref_available(), reason="reference library not built in this checkout")
@@ -89,6 +117,43 @@ def test_oracle_vs_live_reference_random():
         t2, r2 = O.ref_join(probe, build, list(range(nk)), list(range(nk)), jt)
         assert t1 == t2
         same_ordered(t1, r1, r2)
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference library not built in this checkout")
+def test_tsx_oracle_vs_live_reference_random():
+    """Tumbling window and as-of join restatements against the reference's
+    operators on seeded tick-like tables (duplicate build times included)."""
+    rng = np.random.default_rng(321)
+    for it in range(20):
+        n = int(rng.integers(0, 4000))
+        tt = [O.TS, O.I64, O.I32][it % 3]
+        cols = [gen_column(rng, O.I32, n, 5, int(rng.integers(1, 30))),
+                O.TCol(tt, rng.integers(-500, 100000, n).astype(np.int32 if tt == O.I32 else np.int64),
+                       rng.random(n) > 0.03),
+                gen_column(rng, O.I64, n, 10), gen_column(rng, O.F64, n, 10)]
+        keys = [[0], [], [0, 2]][it % 3]
+        aggs = [(O.COUNT_STAR, 0), (O.SUM, 2), (O.MIN, 3), (O.MAX, 2), (O.AVG, 3), (O.COUNT, 3)]
+        w = int(rng.choice([1, 10, 1000, 77777]))
+        t1, r1 = O.window_tumbling(cols, keys, 1, w, aggs)
+        t2, r2 = O.ref_window_tumbling(cols, keys, 1, w, aggs, int(rng.choice([64, 2048])))
+        assert t1 == t2
+        same_ordered(t1, r1, r2)
+    for it in range(20):
+        nsym = int(rng.integers(1, 40))
+        nb, npr = int(rng.integers(0, 3000)), int(rng.integers(0, 3000))
+        build = [gen_column(rng, O.I32, nb, 5, nsym),
+                 O.TCol(O.TS, rng.integers(0, 50000, nb).astype(np.int64), rng.random(nb) > 0.03),
+                 gen_column(rng, O.F64, nb, 10)]
+        probe = [gen_column(rng, O.I32, npr, 5, nsym + 3),
+                 O.TCol(O.I64, rng.integers(-100, 52000, npr).astype(np.int64), rng.random(npr) > 0.03),
+                 gen_column(rng, O.I64, npr, 10)]
+        keys = [0] if it % 4 else []
+        tol = None if it % 2 else int(rng.integers(0, 2000))
+        jt = int(rng.integers(0, 2))
+        t1, r1 = O.asof_join(probe, build, keys, keys, 1, 1, jt, tol)
+        t2, r2 = O.ref_asof_join(probe, build, keys, keys, 1, 1, jt, tol, int(rng.choice([64, 2048])))
+        assert t1 == t2
+        assert O.compare(t1, r1, t2, r2) is None
 
 
 def test_parallel_port_matches_single_thread():
