@@ -548,8 +548,8 @@ def run_window_bench(args, dev, local):
     import qeg
     import oracle as O
 
-    W = TickWorkload(dev)
-    name = "window_trades200M_sym10k_1min"
+    W = TickWorkload(dev, n=args.ticks, m=args.ticks // 4)
+    name = "window_trades%dM_sym10k_1min" % (W.n // 1_000_000)
     ctx = qeg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
     aggs = [(qeg.COUNT_STAR, 0), (qeg.SUM, 3), (qeg.MIN, 2), (qeg.MAX, 2), (qeg.AVG, 2)]
@@ -633,8 +633,8 @@ def run_asof_bench(args, dev, local):
     import qeg
     import oracle as O
 
-    W = TickWorkload(dev)
-    name = "asof_trades200M_quotes50M_sym10k"
+    W = TickWorkload(dev, n=args.ticks, m=args.ticks // 4)
+    name = "asof_trades%dM_quotes%dM_sym10k" % (W.n // 1_000_000, W.m // 1_000_000)
     ctx = qeg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
     ptypes = [qeg.I32, qeg.TS, qeg.F64, qeg.I32]
@@ -876,6 +876,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--agg-rows", type=int, default=None)
+    ap.add_argument("--ticks", type=int, default=200_000_000, help="trades of the window/asof workloads")
     ap.add_argument("--variants", default=None)
     ap.add_argument("--cpu-probe-rows", type=int, default=1 << 25)
     ap.add_argument("--build-rows", type=int, default=1 << 24)

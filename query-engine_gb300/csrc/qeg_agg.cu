@@ -35,6 +35,15 @@ __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t* p) {
   return v;
 }
 
+// Acquire load: a state word published after the key words (a fence, then
+// the atomic exchange of the tag) makes those key words visible to the loads
+// that follow it.
+__device__ __forceinline__ uint64_t ld_acquire(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
   uint32_t v;
   asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -66,29 +75,6 @@ __device__ __forceinline__ void load_values(const AggK& P, uint64_t p, bool (&vv
           vb[c] = static_cast<uint64_t>(int_value(col, p));
       }
     }
-  }
-}
-
-// Applies one row to the field block `f` with atomics (row count + every
-// value field).
-template <int NV>
-__device__ __forceinline__ void apply_row(uint64_t* f, const AggK& P, const bool (&vv)[kMaxVals],
-                                          const uint64_t (&vb)[kMaxVals]) {
-  atomicAdd(reinterpret_cast<unsigned long long*>(f), 1ull);  // F_ROWS is field 0
-#pragma unroll 1
-  for (int fi = 1; fi < P.nfields; ++fi) {
-    const uint8_t kind = P.fkind[fi];
-    const int c = P.fcol[fi];
-    bool v = false;
-    uint64_t b = 0;
-#pragma unroll
-    for (int j = 0; j < NV; ++j) {
-      if (j == c) {
-        v = vv[j];
-        b = vb[j];
-      }
-    }
-    field_apply(f + fi, kind, field_contrib(kind, v, b));
   }
 }
 
@@ -161,7 +147,7 @@ __device__ __forceinline__ uint64_t* global_rowN(const AggK& P, const uint64_t* 
   uint64_t s = __umul64hi(h, P.cap);
   for (int t = 0; t < P.probe_limit; ++t) {
     uint64_t* r = P.table + s * W;
-    uint64_t st = ld_relaxed(r);
+    uint64_t st = ld_acquire(r);
     if (st == 0) {
       const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, 1ull);
       if (old == 0) {
@@ -180,10 +166,9 @@ __device__ __forceinline__ uint64_t* global_rowN(const AggK& P, const uint64_t* 
         atomicOr(P.err, kDevSpinTimeout);
         return nullptr;
       }
-      st = ld_relaxed(r);
+      st = ld_acquire(r);
     }
     if (st == tag) {
-      __threadfence();
       bool eq = ld_relaxed(r + 1) == nullmask;
       for (int j = 0; eq && j < P.nkeys; ++j) eq = ld_relaxed(r + 2 + j) == words[j];
       if (eq) return r;
@@ -440,24 +425,46 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       if (P.full_flag) track_full(P, lane, iter, inserted != ins0, pending, full);
       continue;
     }
-    // MODE 2: composite key, global table only, one lane per row.
-    if (!live) continue;
+    // MODE 2: composite key, global table only. Lanes with the same key tuple
+    // combine like MODE 1: they match on the tuple hash, then every lane
+    // checks its words against the match group's first lane (a lane that
+    // differs -- a hash collision inside the warp -- goes alone), and the
+    // group's leader finds the row and applies the combined fields.
     uint64_t words[kMaxKeys];
-    uint64_t nullmask = 0, h = kHashSeed;
+    uint64_t nullmask = live ? 0 : ~0ull, h = kHashSeed;
 #pragma unroll
     for (int j = 0; j < kMaxKeys; ++j) {
-      if (j < P.nkeys) {
+      words[j] = 0;
+      if (live && j < P.nkeys) {
         const bool kv = col_valid(P.key[j], p);
         words[j] = kv ? key_word(P.key[j], p) : 0;
         if (!kv) nullmask |= 1ull << j;
         h = hash_fold(h, kv ? words[j] : 0x9E3779B97F4A7C15ull);
       }
     }
-    uint64_t* r = global_rowN(P, words, nullmask, h, inserted);
-    if (r)
-      apply_row<NV>(r + fo, P, vv, vb);
-    else
+    const unsigned same = __match_any_sync(0xffffffffu, live ? h : ~static_cast<uint64_t>(lane));
+    const int ref = __ffs(same) - 1;
+    bool eq = __shfl_sync(0xffffffffu, nullmask, ref) == nullmask;
+#pragma unroll
+    for (int j = 0; j < kMaxKeys; ++j)
+      if (j < P.nkeys) eq &= __shfl_sync(0xffffffffu, words[j], ref) == words[j];
+    const unsigned eqmask = __ballot_sync(0xffffffffu, eq);
+    unsigned peers = (live && eq) ? (same & eqmask & livemask) : (1u << lane);
+    const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
+    uint64_t* f = nullptr;
+    if (leader) {
+      uint64_t* r = global_rowN(P, words, nullmask, h, inserted);
+      if (r) f = r + fo;
+    }
+    const unsigned placed = __ballot_sync(0xffffffffu, f != nullptr);
+    const bool ok = live && ((placed >> (__ffs(peers) - 1)) & 1u);
+    if (live && !ok) {
       spill_row(P, p);
+      peers = 1u << lane;
+    }
+    const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
+    if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader && ok, kRowGlobal, peers, pp, vv, vb);
+    else warp_apply<NV>(f, leader && ok, kRowGlobal, peers, pp, P, vv, vb);
   }
 
   // Fold the warp-private rows into the CTA table.

@@ -57,6 +57,14 @@ __device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t* p) {
   return v;
 }
 
+// Acquire load of a composite row's state word: the key words published
+// before its tag (a fence, then the atomic exchange) are visible after it.
+__device__ __forceinline__ uint64_t ld_acquire64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
 // Loads the key tuple of row p. Returns false when any key column is NULL.
 // Slot hash of a key tuple: one splitmix64 round for a single key word, the
 // seeded fold of every word for composite keys.
@@ -99,7 +107,7 @@ __device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w,
   uint64_t s = h & (T.cap - 1);
   for (uint64_t t = 0; t < T.cap; ++t) {
     uint64_t* r = T.keys + s * T.kw;
-    uint64_t st = ld_relaxed64(r);
+    uint64_t st = ld_acquire64(r);
     if (st == 0) {
       if (!INSERT) return -1;
       const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, 1ull);
@@ -117,10 +125,9 @@ __device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w,
         atomicOr(err, kDevSpinTimeout);
         return -1;
       }
-      st = ld_relaxed64(r);
+      st = ld_acquire64(r);
     }
     if (st == tag) {
-      __threadfence();
       bool eq = true;
       for (int j = 0; eq && j < T.nkeys; ++j) eq = ld_relaxed64(r + 1 + j) == w[j];
       if (eq) return static_cast<int64_t>(s);
@@ -133,6 +140,7 @@ __device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w,
 struct BuildK {
   DevCol key[kMaxKeys];
   int nkeys;
+  int no_count;  // insert keys only (the as-of join needs no per-slot row counts)
   uint64_t n;
   JTable T;
   uint32_t* fill;
@@ -158,6 +166,7 @@ __global__ void build_count_kernel(BuildK P) {
         continue;
       }
     }
+    if (P.no_count) continue;
     if (atomicAdd(&P.T.cnt[s], 1u) != 0) dup = 1;
     else ++fresh;
   }
@@ -187,10 +196,9 @@ __global__ void build_scatter_kernel(BuildK P) {
   }
 }
 
-// Dense build: sets one bit per key value; a bit that was already set means
-// the build keys are not unique.
-// Sets the bit of every non-NULL build key (fire-and-forget reductions; the
-// distinct count comes from a population count of the bitmap afterwards).
+// Dense build: sets the bit of every non-NULL build key (fire-and-forget
+// reductions; the distinct count, and so uniqueness, comes from a population
+// count of the bitmap afterwards).
 __global__ void dense_mark_kernel(BuildK P, unsigned long long* __restrict__ bits) {
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
     if (!col_valid(P.key[0], r)) continue;
@@ -1058,7 +1066,6 @@ struct AsofItemsK {
   uint64_t* lo;
   uint32_t* hi;
   uint32_t* val;
-  uint32_t* cnt;  // matchable rows per slot
   uint32_t* err;
 };
 
@@ -1075,7 +1082,6 @@ __global__ void asof_items_kernel(const AsofItemsK P) {
       if (s >= 0) {
         slot = static_cast<uint32_t>(s);
         rel = static_cast<uint64_t>(int_value(P.ts, r)) - static_cast<uint64_t>(P.tmin);
-        atomicAdd(P.cnt + s, 1u);
       }
     }
     P.lo[r] = rel;
@@ -1084,11 +1090,40 @@ __global__ void asof_items_kernel(const AsofItemsK P) {
   }
 }
 
+// Sets *unsorted when some row's time is below the previous row's (times
+// without NULLs): a build side in time order only needs sorting by slot.
+__global__ void time_order_kernel(DevCol ts, uint64_t n, unsigned int* unsorted) {
+  bool bad = false;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i + 1 < n; i += (uint64_t)gridDim.x * blockDim.x)
+    bad |= int_value(ts, i) > int_value(ts, i + 1);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(unsorted, 1u);
+}
+
+// Partition runs of the sorted items: run [beg[s], end[s]) of every slot that
+// has matchable rows (the arrays start zeroed: absent slots are empty), and
+// the sample array (every kAsofSample-th sorted time) of the two-level search.
+constexpr int kAsofSample = 32;
+
+__global__ void asof_runs_kernel(const uint32_t* __restrict__ hi, const uint64_t* __restrict__ lo, uint64_t n,
+                                 uint32_t nslots, uint32_t* __restrict__ beg, uint32_t* __restrict__ end,
+                                 uint64_t* __restrict__ samp) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t s = hi[i];
+    if (i % kAsofSample == 0) samp[i / kAsofSample] = lo[i];
+    if (s >= nslots) continue;
+    if (i == 0 || hi[i - 1] != s) beg[s] = static_cast<uint32_t>(i);
+    if (i + 1 == n || hi[i + 1] != s) end[s] = static_cast<uint32_t>(i + 1);
+  }
+}
+
 // Probe: a probe row with non-NULL keys and timestamp t finds its partition,
 // then the last build timestamp <= t by binary search over the partition's
 // run (the reference walks a cursor over the sorted probe side to the same
 // row, tsx/asof.cpp:269-296); with a tolerance the match is kept only when
-// t - tb <= tolerance in uint64 arithmetic (tsx/asof.cpp:283-293).
+// t - tb <= tolerance in uint64 arithmetic (tsx/asof.cpp:283-293). The search
+// runs in two levels: over the samples inside the run (every 32nd sorted
+// time, small enough to stay in L2), then over the <= 32 times between two
+// samples (one or two cache lines).
 struct AsofProbeK {
   DevCol key[kMaxKeys];
   int nkeys;
@@ -1098,7 +1133,9 @@ struct AsofProbeK {
   int64_t tmin;
   const uint64_t* ats;   // sorted timestamps - tmin
   const uint32_t* arow;  // build rows in the same order
-  const uint64_t* aoff;  // partition runs: [aoff[s], aoff[s+1])
+  const uint32_t* abeg;  // partition runs: [abeg[s], aend[s])
+  const uint32_t* aend;
+  const uint64_t* asamp;  // ats[i * kAsofSample]
   int left, tol_set;
   uint64_t tol;
   uint32_t* match;
@@ -1119,10 +1156,21 @@ __global__ void asof_probe_kernel(const AsofProbeK P) {
       }
       if (s >= 0) {
         const int64_t t = int_value(P.ts, p);
-        const uint64_t b = P.aoff[s], e = P.aoff[s + 1];
+        const uint64_t b = P.abeg[s], e = P.aend[s];
         if (e > b && t >= P.tmin) {
           const uint64_t rel = static_cast<uint64_t>(t) - static_cast<uint64_t>(P.tmin);
           uint64_t lo = b, hi = e;  // first position whose timestamp is > t
+          const uint64_t ib = (b + kAsofSample - 1) / kAsofSample, ie = (e - 1) / kAsofSample;
+          if (ib <= ie) {  // samples inside the run narrow [lo, hi) to <= 32 positions
+            uint64_t l = ib, r = ie + 1;
+            while (l < r) {
+              const uint64_t mid = l + ((r - l) >> 1);
+              if (P.asamp[mid] <= rel) l = mid + 1;
+              else r = mid;
+            }
+            if (l > ib) lo = (l - 1) * kAsofSample + 1;
+            if (l <= ie) hi = l * kAsofSample;
+          }
           while (lo < hi) {
             const uint64_t mid = lo + ((hi - lo) >> 1);
             if (P.ats[mid] <= rel) lo = mid + 1;
@@ -1224,6 +1272,80 @@ __global__ void gather_out_kernel(const void* __restrict__ src, const uint64_t* 
   }
 }
 
+// All output columns in one pass: a warp loads the probe and build row
+// indices of its 64 output rows once, then writes every column's values and
+// validity word for them (the per-column kernel above re-reads the indices
+// once per column).
+constexpr int kMaxGatherCols = 32;
+
+struct GatherCol {
+  const void* src;
+  const uint64_t* bits;
+  const uint8_t* bytes;
+  const int32_t* code_map;
+  void* out;
+  uint64_t* words;
+  int width;
+  int side;  // 0 probe, 1 build
+};
+
+struct GatherK {
+  GatherCol c[kMaxGatherCols];
+  int ncols;
+  const uint32_t* idx[2];
+  uint64_t n;
+  unsigned int* flags;  // per column: set when a NULL was written
+};
+
+__device__ __forceinline__ bool gather_one(const GatherCol& c, uint32_t r, uint64_t k) {
+  bool ok = r != kNullRow;
+  if (ok) {
+    if (c.bits) ok = (c.bits[r >> 6] >> (r & 63)) & 1ull;
+    else if (c.bytes) ok = c.bytes[r];
+  }
+  if (c.width == 8) {
+    static_cast<uint64_t*>(c.out)[k] = r == kNullRow ? 0 : static_cast<const uint64_t*>(c.src)[r];
+  } else if (c.width == 4) {
+    uint32_t v = 0;
+    if (r != kNullRow) {
+      v = static_cast<const uint32_t*>(c.src)[r];
+      if (c.code_map) v = ok ? static_cast<uint32_t>(c.code_map[static_cast<int32_t>(v)]) : 0;
+    }
+    static_cast<uint32_t*>(c.out)[k] = v;
+  } else {
+    static_cast<uint8_t*>(c.out)[k] = r == kNullRow ? 0 : static_cast<const uint8_t*>(c.src)[r];
+  }
+  return ok;
+}
+
+__global__ void __launch_bounds__(256) gather_cols_kernel(const GatherK P) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint64_t nw = (P.n + 63) / 64;
+  const uint64_t nwarps = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t w = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w < nw; w += nwarps) {
+    const uint64_t k0 = w * 64 + lane, k1 = k0 + 32;
+    const bool in0 = k0 < P.n, in1 = k1 < P.n;
+    uint32_t r[2][2];
+#pragma unroll
+    for (int sd = 0; sd < 2; ++sd) {
+      r[sd][0] = in0 ? P.idx[sd][k0] : kNullRow;
+      r[sd][1] = in1 ? P.idx[sd][k1] : kNullRow;
+    }
+    for (int c = 0; c < P.ncols; ++c) {
+      const GatherCol& col = P.c[c];
+      const int sd = col.side;
+      const bool ok0 = in0 ? gather_one(col, r[sd][0], k0) : true;
+      const bool ok1 = in1 ? gather_one(col, r[sd][1], k1) : true;
+      const unsigned b0 = __ballot_sync(0xffffffffu, ok0), b1 = __ballot_sync(0xffffffffu, ok1);
+      if (lane == 0) {
+        const uint64_t word = static_cast<uint64_t>(b0) | (static_cast<uint64_t>(b1) << 32);
+        if (col.words) col.words[w] = word;
+        if (word != ~0ull) atomicOr(P.flags + c, 1u);
+      }
+    }
+  }
+}
+
 // Appends a batch column into the build store: values are copied, validity is
 // expanded to a byte per row; STR codes are translated to value ids.
 __global__ void store_append_kernel(DevCol c, uint64_t n, int width, void* __restrict__ dst,
@@ -1292,7 +1414,7 @@ struct JoinState {
   int64_t tol = 0;
   int64_t tmin = 0;
   uint32_t aslots = 0;
-  DevBuf ats, arow, aoff, tbits, amatch;
+  DevBuf ats, arow, abeg, aend, asamp, tbits, amatch;
   void asof_build();
   void asof_probe(uint64_t n);
 
@@ -1458,7 +1580,7 @@ void JoinState::finish_build() {
     bitmap.alloc(((cap + 63) / 64) * 8, ctx->stream);
     QEG_CUDA(cudaMemsetAsync(bitmap.get(), 0, ((cap + 63) / 64) * 8, ctx->stream));
     P.T = table();
-    if (nbuild) {
+    if (nbuild && !asof) {  // the as-of join maps keys to slots only
       dense_mark_kernel<<<g, 256, 0, ctx->stream>>>(P, bitmap.get<unsigned long long>());
       const uint64_t nw = (cap + 63) / 64;
       popc_kernel<<<grid_for(ctx, nw, 256, 8), 256, 0, ctx->stream>>>(bitmap.get<unsigned long long>(), nw,
@@ -1467,6 +1589,7 @@ void JoinState::finish_build() {
       QEG_CUDA(cudaGetLastError());
     }
   } else {
+    P.no_count = asof ? 1 : 0;
     build_hash(P);
   }
   // The radix-partitioned join probes the same table (single key only).
@@ -1481,7 +1604,7 @@ void JoinState::finish_build() {
   distinct = d[1];
   // Dense: the keys are unique when every non-NULL key set its own bit.
   unique = strategy == QEG_JOIN_DENSE ? (distinct == nonnull ? 1 : 0) : ((d[0] & 0xffffffffull) ? 0 : 1);
-  if (strategy == QEG_JOIN_DENSE && !unique) count_dense();
+  if (strategy == QEG_JOIN_DENSE && !unique && !asof) count_dense();
   csr_built = false;
   acc.alloc(24, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(acc.get(), 0, 24, ctx->stream));
@@ -1522,9 +1645,19 @@ void JoinState::asof_build() {
   while (lo_bits < 64 && (range >> lo_bits) != 0) ++lo_bits;
   while (hi_bits < 32 && (static_cast<uint64_t>(aslots) >> hi_bits) != 0) ++hi_bits;
 
-  DevBuf cntb((ns + 1) * 4, ctx->stream);
-  QEG_CUDA(cudaMemsetAsync(cntb.get(), 0, (ns + 1) * 4, ctx->stream));
   const uint64_t n = nbuild;
+  // A build side already in time order (no NULL times) only needs its stable
+  // sort by slot: time order within every slot is kept.
+  if (n > 1 && r[2] == n) {
+    DevBuf flag(4, ctx->stream);
+    QEG_CUDA(cudaMemsetAsync(flag.get(), 0, 4, ctx->stream));
+    time_order_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(ts, n, flag.get<unsigned int>());
+    ctx->launches++;
+    uint32_t unsorted = 1;
+    QEG_CUDA(cudaMemcpyAsync(&unsorted, flag.get(), 4, cudaMemcpyDeviceToHost, ctx->stream));
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (!unsorted) lo_bits = 0;
+  }
   DevBuf a_lo(std::max<uint64_t>(n, 1) * 8, ctx->stream), b_lo(std::max<uint64_t>(n, 1) * 8, ctx->stream);
   DevBuf a_hi(std::max<uint64_t>(n, 1) * 4, ctx->stream), b_hi(std::max<uint64_t>(n, 1) * 4, ctx->stream);
   DevBuf a_val(std::max<uint64_t>(n, 1) * 4, ctx->stream), b_val(std::max<uint64_t>(n, 1) * 4, ctx->stream);
@@ -1540,7 +1673,6 @@ void JoinState::asof_build() {
     P.lo = a_lo.get<uint64_t>();
     P.hi = a_hi.get<uint32_t>();
     P.val = a_val.get<uint32_t>();
-    P.cnt = cntb.get<uint32_t>();
     P.err = static_cast<uint32_t*>(ctx->dev_err.get());
     asof_items_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(P);
     ctx->launches++;
@@ -1549,8 +1681,17 @@ void JoinState::asof_build() {
   SortItems A{a_lo.get<uint64_t>(), a_hi.get<uint32_t>(), a_val.get<uint32_t>()};
   SortItems B{b_lo.get<uint64_t>(), b_hi.get<uint32_t>(), b_val.get<uint32_t>()};
   const SortItems R = radix_sort_items(ctx, A, B, n, lo_bits, hi_bits);
-  aoff.alloc((ns + 1) * 8, ctx->stream);
-  exclusive_scan(ctx, cntb.get<uint32_t>(), ns, aoff.get<uint64_t>());
+  abeg.alloc(ns * 4, ctx->stream);
+  aend.alloc(ns * 4, ctx->stream);
+  asamp.alloc((n / kAsofSample + 1) * 8, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(abeg.get(), 0, ns * 4, ctx->stream));
+  QEG_CUDA(cudaMemsetAsync(aend.get(), 0, ns * 4, ctx->stream));
+  if (n) {
+    asof_runs_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(
+        R.hi, R.lo, n, aslots, abeg.get<uint32_t>(), aend.get<uint32_t>(), asamp.get<uint64_t>());
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
   // Keep the sorted timestamps and rows; the slot words are no longer needed.
   const bool in_a = R.lo == A.lo;
   ats = in_a ? std::move(a_lo) : std::move(b_lo);
@@ -1729,7 +1870,9 @@ void JoinState::asof_probe(uint64_t n) {
   P.tmin = tmin;
   P.ats = ats.get<uint64_t>();
   P.arow = arow.get<uint32_t>();
-  P.aoff = aoff.get<uint64_t>();
+  P.abeg = abeg.get<uint32_t>();
+  P.aend = aend.get<uint32_t>();
+  P.asamp = asamp.get<uint64_t>();
   P.left = join_type == QEG_LEFT;
   P.tol_set = tol_set;
   P.tol = static_cast<uint64_t>(tol);
@@ -1946,7 +2089,36 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
       DevBuf flags(ncol * 4, ctx->stream);
       QEG_CUDA(cudaMemsetAsync(flags.get(), 0, ncol * 4, ctx->stream));
       const unsigned gw = grid_for(ctx, (count + 63) / 64 * 32, 256, 8);
-      for (size_t c = 0; c < ncol; ++c) {
+      if (ncol <= static_cast<size_t>(kMaxGatherCols)) {
+        GatherK G{};
+        G.ncols = static_cast<int>(ncol);
+        G.idx[0] = st.out_probe.get<uint32_t>() + first;
+        G.idx[1] = st.out_build.get<uint32_t>() + first;
+        G.n = count;
+        G.flags = flags.get<unsigned int>();
+        for (size_t c = 0; c < ncol; ++c) {
+          const bool pc = c < st.ptypes.size();
+          const size_t bc = pc ? 0 : c - st.ptypes.size();
+          GatherCol& g = G.c[c];
+          g.width = static_cast<int>(type_width(pc ? st.ptypes[c] : st.btypes[bc]));
+          g.side = pc ? 0 : 1;
+          g.out = outs[c].data;
+          g.words = outs[c].validity;
+          if (pc) {
+            const StagedCol& sc = st.probe_staged[c];
+            g.src = sc.dev.data;
+            g.bits = sc.dev.all_valid ? nullptr : sc.dev.validity;
+            g.code_map = st.ptypes[c] == QEG_STR ? sc.dev.code_map : nullptr;
+          } else {
+            g.src = st.bvals[bc].get();
+            g.bytes = st.bvalid[bc].get<uint8_t>();
+          }
+        }
+        gather_cols_kernel<<<gw, 256, 0, ctx->stream>>>(G);
+        ctx->launches++;
+        QEG_CUDA(cudaGetLastError());
+      }
+      for (size_t c = 0; c < ncol && ncol > static_cast<size_t>(kMaxGatherCols); ++c) {
         const bool pc = c < st.ptypes.size();
         const size_t bc = pc ? 0 : c - st.ptypes.size();
         const int w = static_cast<int>(type_width(pc ? st.ptypes[c] : st.btypes[bc]));
