@@ -1145,8 +1145,78 @@ struct AsofProbeK {
   uint32_t* err;
 };
 
-__global__ void asof_probe_kernel(const AsofProbeK P) {
-  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < P.n; p += (uint64_t)gridDim.x * blockDim.x) {
+// First position in [b, e) whose time is > rel (e when none): a search that
+// starts at a hint inside the run and gallops outward (1, 2, 4, ...
+// positions) before a binary search of the bracket -- a few loads in the same
+// cache lines when the hint is close, as it is for a probe side in time order.
+__device__ __forceinline__ uint64_t asof_gallop(const uint64_t* __restrict__ ats, uint64_t b, uint64_t e,
+                                                uint64_t h, uint64_t rel) {
+  uint64_t lo, hi;
+  if (ats[h] <= rel) {
+    lo = h + 1;
+    uint64_t d = 1;
+    while (lo + d - 1 < e && ats[lo + d - 1] <= rel) {
+      lo += d;
+      d <<= 1;
+    }
+    hi = lo + d - 1 < e ? lo + d - 1 : e;
+  } else {
+    hi = h;
+    uint64_t d = 1;
+    while (hi >= b + d && ats[hi - d] > rel) {
+      hi -= d;
+      d <<= 1;
+    }
+    lo = hi >= b + d ? hi - d + 1 : b;
+  }
+  while (lo < hi) {
+    const uint64_t mid = lo + ((hi - lo) >> 1);
+    if (ats[mid] <= rel) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// First position in [b, e) whose time is > rel, from scratch: over the
+// samples inside the run (every kAsofSample-th sorted time, small enough to
+// stay in L2), then over the <= kAsofSample times between two samples.
+__device__ __forceinline__ uint64_t asof_sampled(const AsofProbeK& P, uint64_t b, uint64_t e, uint64_t rel) {
+  uint64_t lo = b, hi = e;
+  const uint64_t ib = (b + kAsofSample - 1) / kAsofSample, ie = (e - 1) / kAsofSample;
+  if (ib <= ie) {
+    uint64_t l = ib, r = ie + 1;
+    while (l < r) {
+      const uint64_t mid = l + ((r - l) >> 1);
+      if (P.asamp[mid] <= rel) l = mid + 1;
+      else r = mid;
+    }
+    if (l > ib) lo = (l - 1) * kAsofSample + 1;
+    if (l <= ie) hi = l * kAsofSample;
+  }
+  while (lo < hi) {
+    const uint64_t mid = lo + ((hi - lo) >> 1);
+    if (P.ats[mid] <= rel) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Each CTA walks one contiguous range of probe rows and keeps, per slot (a
+// direct-mapped table in shared memory), the position its last search ended
+// at: on a probe side in time order the next search of that slot starts a few
+// positions away. A hint is only a starting point (any position of the run
+// gives the same answer), so races between warps on it are harmless.
+constexpr int kAsofHintBits = 11;
+constexpr int kAsofHints = 1 << kAsofHintBits;
+
+__global__ void __launch_bounds__(256) asof_probe_kernel(const AsofProbeK P) {
+  __shared__ uint32_t hslot[kAsofHints], hpos[kAsofHints];
+  for (int i = threadIdx.x; i < kAsofHints; i += blockDim.x) hslot[i] = 0xffffffffu;
+  __syncthreads();
+  const uint64_t chunk = ((P.n + gridDim.x - 1) / gridDim.x + 255) / 256 * 256;
+  const uint64_t c0 = blockIdx.x * chunk;
+  const uint64_t c1 = c0 + chunk < P.n ? c0 + chunk : P.n;
+  for (uint64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x) {
     uint32_t m = kNullRow;
     if (col_valid(P.ts, p)) {
       int64_t s = 0;
@@ -1159,24 +1229,14 @@ __global__ void asof_probe_kernel(const AsofProbeK P) {
         const uint64_t b = P.abeg[s], e = P.aend[s];
         if (e > b && t >= P.tmin) {
           const uint64_t rel = static_cast<uint64_t>(t) - static_cast<uint64_t>(P.tmin);
-          uint64_t lo = b, hi = e;  // first position whose timestamp is > t
-          const uint64_t ib = (b + kAsofSample - 1) / kAsofSample, ie = (e - 1) / kAsofSample;
-          if (ib <= ie) {  // samples inside the run narrow [lo, hi) to <= 32 positions
-            uint64_t l = ib, r = ie + 1;
-            while (l < r) {
-              const uint64_t mid = l + ((r - l) >> 1);
-              if (P.asamp[mid] <= rel) l = mid + 1;
-              else r = mid;
-            }
-            if (l > ib) lo = (l - 1) * kAsofSample + 1;
-            if (l <= ie) hi = l * kAsofSample;
-          }
-          while (lo < hi) {
-            const uint64_t mid = lo + ((hi - lo) >> 1);
-            if (P.ats[mid] <= rel) lo = mid + 1;
-            else hi = mid;
-          }
-          if (lo > b && (!P.tol_set || rel - P.ats[lo - 1] <= P.tol)) m = P.arow[lo - 1];
+          const uint32_t hi = (static_cast<uint32_t>(s) * 2654435761u) >> (32 - kAsofHintBits);
+          const uint32_t hp = hpos[hi];
+          const bool hit = hslot[hi] == static_cast<uint32_t>(s) && hp >= b && hp < e;
+          const uint64_t j = hit ? asof_gallop(P.ats, b, e, hp, rel) : asof_sampled(P, b, e, rel);
+          const uint32_t nh = static_cast<uint32_t>(j < e ? j : e - 1);
+          hslot[hi] = static_cast<uint32_t>(s);
+          hpos[hi] = nh;
+          if (j > b && (!P.tol_set || rel - P.ats[j - 1] <= P.tol)) m = P.arow[j - 1];
         }
       }
     }

@@ -240,3 +240,22 @@ def test_asof_rejects_bad_arguments(ctx):
     with pytest.raises(qeg.QegError):  # the count/sum sink is not an as-of join
         j.probe_count_sum(to_gpu(O.TCol(O.I64, np.arange(4))), to_gpu(O.TCol(O.I64, np.arange(4))))
     j.close()
+
+
+@pytest.mark.parametrize("jt", [O.INNER, O.LEFT])
+def test_asof_time_ordered_sides(ctx, jt):
+    # A build side in time order without NULL times takes the slot-only sort;
+    # equal times within a symbol must still resolve to the last built row.
+    # The probe side in time order exercises the galloping search from the
+    # per-CTA hints; a shuffled copy of it must give the same rows.
+    rng = np.random.default_rng(15)
+    nb, npr = 300000, 600000
+    bts = np.sort(rng.integers(0, 10 ** 9, nb) // 1000 * 1000)  # many equal times
+    build = [O.TCol(O.I32, zipf(rng, nb, 300).astype(np.int32), rng.random(nb) > 0.01), O.TCol(O.TS, bts),
+             O.TCol(O.I64, np.arange(nb))]
+    pts = np.sort(rng.integers(-1000, 10 ** 9 + 1000, npr))
+    probe = [O.TCol(O.I32, zipf(rng, npr, 320).astype(np.int32), rng.random(npr) > 0.01), O.TCol(O.TS, pts)]
+    check_asof(ctx, probe, build, [0], [0], 1, 1, jt, None if jt == O.LEFT else 50000)
+    perm = rng.permutation(npr)
+    shuffled = [O.TCol(c.type, c.values[perm], None if c.valid is None else c.valid[perm]) for c in probe]
+    check_asof(ctx, shuffled, build, [0], [0], 1, 1, jt)
