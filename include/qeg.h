@@ -121,7 +121,9 @@ typedef struct qeg_agg_config {
   int32_t block_threads;     /* 0 = tuned                                   */
   int32_t rows_per_thread;   /* 0 = tuned                                   */
   int32_t smem_slots;        /* 0 = tuned                                   */
-  int32_t hot_keys;          /* register-resident heavy hitters; -1 = tuned */
+  int32_t hot_keys;          /* > 0: preload that many sketch heavy hitters into the
+                                  CTA tables (the hottest 32 in warp-private rows);
+                                  0 or -1: first-come CTA tables (the default) */
 } qeg_agg_config;
 
 typedef struct qeg_join_config {

@@ -848,7 +848,13 @@ void AggState::set_field_columns(AggK& P) const {
     for (int k = 0; k < cnf[c]; ++k) P.fcol[cfirst[c] + k] = static_cast<uint8_t>(c);
 }
 
-int AggState::block_threads() const { return cfg.block_threads > 0 ? cfg.block_threads : 512; }
+// 1024-thread CTAs for the single-key private-table strategy (one CTA per SM
+// with a 2048-slot table: measured 1.28x faster than 512 threads on a 512M-row
+// Zipf(1.1) GROUP BY), 512 otherwise.
+int AggState::block_threads() const {
+  if (cfg.block_threads > 0) return cfg.block_threads;
+  return (mode == 1 && strategy == QEG_AGG_SMEM) ? 1024 : 512;
+}
 
 int AggState::warp_hot() const {
   if (mode != 1 || nhot <= 0 || smem_slots <= 0) return 0;
@@ -1036,7 +1042,7 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   if (mode == 0) {
     want = 1;
   } else if (cfg.expected_groups > 0) {
-    if (cfg.hot_keys != 0 && mode == 1) estimate_groups(staged, nrows, len, dsel);  // heavy hitters only
+    if (cfg.hot_keys > 0 && mode == 1) estimate_groups(staged, nrows, len, dsel);  // heavy hitters only
     want = static_cast<uint64_t>(static_cast<double>(cfg.expected_groups) / kTargetLoad) + 64;
     est_groups = static_cast<double>(cfg.expected_groups);
   } else if (cfg.sizing == QEG_SIZE_FIXED) {
@@ -1075,11 +1081,12 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   }
   nhot = 0;
   if (strategy == QEG_AGG_SMEM && mode == 1) {
-    // Many groups but a heavy head: preload the heavy hitters found by the
-    // sketch and keep the private table read-only, so its slots hold the keys
-    // that carry the rows instead of whichever keys arrived first. A smaller
-    // table then keeps two CTAs per SM; first-come tables get 2048 slots.
-    const bool preload = cfg.hot_keys != 0 && est_groups > 1024 && !heavy_candidates.empty();
+    // First-come private tables of 2048 slots by default: on a heavy head the
+    // hot keys arrive first and keep their slots. Preloading the sketch's
+    // heavy hitters into a read-only table (hot_keys > 0) is kept as an
+    // option; measured on GB300 it is slower than the first-come table
+    // (34.1 vs 29.9 ms on 512M Zipf(1.1) rows with 1024-thread CTAs).
+    const bool preload = cfg.hot_keys > 0 && est_groups > 1024 && !heavy_candidates.empty();
     smem_slots = cfg.smem_slots > 0 ? static_cast<int>(next_pow2(cfg.smem_slots)) : (preload ? 1024 : 2048);
     smem_slots = std::min(smem_slots, slots);
     smem_insert = 1;

@@ -607,7 +607,7 @@ double AggState::estimate_groups(const std::vector<StagedCol>& staged, uint64_t 
     return static_cast<double>(std::min<uint64_t>(std::max<uint64_t>(nrows, 1), 1ull << 22));
   }
   SketchResult s;
-  const int want_heavy = (cfg.hot_keys != 0) ? 4096 : 0;
+  const int want_heavy = (cfg.hot_keys > 0) ? 4096 : 0;
   sketch_key_column(ctx, key_col(staged, 0), dsel, nrows, len, 1u << 20, want_heavy, s);
   double groups = 0, share = 0;
   if (learned_estimate(ctx, s, &groups, &share)) {

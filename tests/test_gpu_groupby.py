@@ -187,3 +187,26 @@ def test_str_keys_group_by_value_across_dictionaries(ctx):
     assert rows == {"AAPL": (3, 15, "AAPL"), "MSFT": (2, 22, "MSFT"), "GOOG": (2, 33, "GOOG"),
                     "IBM": (1, 7, "IBM")}
     a.close()
+
+
+@pytest.mark.parametrize("hot", [0, 512, 64])
+@pytest.mark.parametrize("block", [0, 512])
+def test_skewed_sketch_path_with_and_without_preloaded_hot_keys(ctx, hot, block):
+    # 6M rows (above the sketch threshold), Zipf(1.2) keys over 2M values:
+    # the learned sizing path, first-come CTA tables (hot = 0) and the
+    # preloaded read-only heavy-hitter tables with warp-private rows for the
+    # hottest keys (hot > 0), with the default and a forced block size.
+    rng = np.random.default_rng(40 + hot + block)
+    n, dom = 6 << 20, 2 << 20
+    w = np.arange(1, dom + 1, dtype=np.float64) ** -1.2
+    cdf = np.cumsum(w)
+    cdf /= cdf[-1]
+    ranks = np.minimum(np.searchsorted(cdf, rng.random(n)), dom - 1)
+    key = O.TCol(O.I64, (ranks.astype(np.int64) * 0x5851F42D4C957F2D % (1 << 62)) - (1 << 61))
+    v1 = O.TCol(O.I64, rng.integers(-(1 << 31), 1 << 31, n))
+    v2 = O.TCol(O.F64, rng.normal(0, 1e3, n), rng.random(n) > 0.05)
+    aggs = [(O.COUNT_STAR, 0), (O.SUM, 1), (O.SUM, 2), (O.MIN, 1), (O.MAX, 1), (O.AVG, 2)]
+    cfg = qeg.agg_config(sizing=qeg.SIZE_LEARNED, hot_keys=hot, block_threads=block)
+    ot, orows = O.groupby([key, v1, v2], [0], aggs, 1 << 23)
+    gt, grows = run_gpu(ctx, [key, v1, v2], [0], aggs, config=cfg)
+    assert_same(gt, grows, ot, orows, "hot %d block %d" % (hot, block))
