@@ -231,10 +231,27 @@ __global__ void minmax_kernel(DevCol c, uint64_t n, unsigned long long* out /* [
     mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
     cnt += __shfl_down_sync(0xffffffffu, cnt, o);
   }
-  if ((threadIdx.x & 31) == 0 && cnt) {
-    atomicMin(out + 0, mn);
-    atomicMax(out + 1, mx);
-    atomicAdd(out + 2, cnt);
+  // One set of global atomics per CTA (per-warp atomics on three words
+  // serialise at the L2).
+  __shared__ unsigned long long smn[32], smx[32], scn[32];
+  const unsigned warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    smn[warp] = mn;
+    smx[warp] = mx;
+    scn[warp] = cnt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (unsigned w = 1; w < nwarps; ++w) {
+      mn = min(mn, smn[w]);
+      mx = max(mx, smx[w]);
+      cnt += scn[w];
+    }
+    if (cnt) {
+      atomicMin(out + 0, mn);
+      atomicMax(out + 1, mx);
+      atomicAdd(out + 2, cnt);
+    }
   }
 }
 
@@ -1522,16 +1539,21 @@ struct JoinState {
       }
       bcap = ncap;
     }
+    bool host_input = false;
     for (int c = 0; c < ncols; ++c) {
       StagedCol s;
       stage_column(ctx, cols[c], s);
+      host_input = host_input || s.data.get() || s.validity.get() || s.code_map.get();
       const int w = static_cast<int>(type_width(btypes[c]));
       store_append_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(
           s.dev, n, w, bvals[c].get<uint8_t>() + nbuild * w, bvalid[c].get<uint8_t>() + nbuild);
       ctx->launches++;
       QEG_CUDA(cudaGetLastError());
     }
-    QEG_CUDA(cudaStreamSynchronize(ctx->stream));  // staged inputs die with this scope
+    // Host inputs: their copies must finish before the call returns (the
+    // caller may reuse its buffers). Staged device copies are freed in stream
+    // order, after the kernels that read them.
+    if (host_input) QEG_CUDA(cudaStreamSynchronize(ctx->stream));
     nbuild += n;
   }
 
