@@ -586,11 +586,15 @@ __device__ __forceinline__ void store_typed(void* base, uint64_t i, int32_t t, u
 // Compacts occupied rows into dense output columns (keys, then aggregates),
 // applying the reference's finalisation (ops/agg_internal.h:169-229).
 template <int MODE>
-__global__ void finalize_kernel(const AggK P, const FinK F) {
+__global__ void __launch_bounds__(1024) finalize_kernel(const AggK P, const FinK F) {
   const int W = P.row_words;
   const int fo = (MODE == 2) ? 2 + P.nkeys : 1;
   const uint64_t total = (MODE == 0) ? 1 : (MODE == 1 ? P.cap + 2 : P.cap);
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  // Output positions: one atomic per CTA and pass (the warps' counts are
+  // prefixed in shared memory), not one per warp -- a sparse table of tens of
+  // millions of slots would otherwise serialise on the counter.
+  __shared__ unsigned long long wpos[32];
   for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < total; base += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t s = base + threadIdx.x;
     bool occ = false;
@@ -602,10 +606,21 @@ __global__ void finalize_kernel(const AggK P, const FinK F) {
       else occ = r[0] >= 2;
     }
     const unsigned m = __ballot_sync(0xffffffffu, occ);
-    if (m == 0) continue;
-    unsigned long long wbase = 0;
-    if (lane == 0) wbase = atomicAdd(F.out_count, static_cast<unsigned long long>(__popc(m)));
-    wbase = __shfl_sync(0xffffffffu, wbase, 0);
+    if (lane == 0) wpos[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long run = 0;
+      for (int w = 0; w < nwarps; ++w) {
+        const unsigned long long c = wpos[w];
+        wpos[w] = run;
+        run += c;
+      }
+      const unsigned long long b = run ? atomicAdd(F.out_count, run) : 0;
+      for (int w = 0; w < nwarps; ++w) wpos[w] += b;
+    }
+    __syncthreads();
+    const unsigned long long wbase = wpos[warp];
+    __syncthreads();  // wpos is rewritten by the next pass
     if (!occ) continue;
     const uint64_t o = wbase + __popc(m & ((1u << lane) - 1u));
     if (o >= F.out_cap) {
@@ -1142,10 +1157,10 @@ void AggState::finish(uint64_t* nrows_out) {
   F.out_cap = out_cap;
   AggK P = kparams_base();
   const uint64_t total = (mode == 0) ? 1 : (mode == 1 ? cap + 2 : cap);
-  const unsigned g = grid_for(ctx, total, 256, 8);
-  if (mode == 0) finalize_kernel<0><<<g, 256, 0, ctx->stream>>>(P, F);
-  else if (mode == 1) finalize_kernel<1><<<g, 256, 0, ctx->stream>>>(P, F);
-  else finalize_kernel<2><<<g, 256, 0, ctx->stream>>>(P, F);
+  const unsigned g = grid_for(ctx, total, 1024, 2);
+  if (mode == 0) finalize_kernel<0><<<g, 1024, 0, ctx->stream>>>(P, F);
+  else if (mode == 1) finalize_kernel<1><<<g, 1024, 0, ctx->stream>>>(P, F);
+  else finalize_kernel<2><<<g, 1024, 0, ctx->stream>>>(P, F);
   ctx->launches++;
   QEG_CUDA(cudaGetLastError());
   unsigned long long n = 0;
