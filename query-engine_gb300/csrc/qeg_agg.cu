@@ -1057,7 +1057,9 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   if (mode == 0) {
     want = 1;
   } else if (cfg.expected_groups > 0) {
-    if (cfg.hot_keys > 0 && mode == 1) estimate_groups(staged, nrows, len, dsel);  // heavy hitters only
+    // The sketch still runs for its skew estimate (the private-table strategy
+    // needs the heavy-hitter share) and, with hot_keys > 0, the heavy hitters.
+    if (mode == 1 && (cfg.hot_keys > 0 || nrows >= kSketchMinRows)) estimate_groups(staged, nrows, len, dsel);
     want = static_cast<uint64_t>(static_cast<double>(cfg.expected_groups) / kTargetLoad) + 64;
     est_groups = static_cast<double>(cfg.expected_groups);
   } else if (cfg.sizing == QEG_SIZE_FIXED) {
