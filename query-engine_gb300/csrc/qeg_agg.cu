@@ -296,7 +296,7 @@ constexpr uint32_t kSpecCount = 0u;
 // warp-private rows for the hottest keys); measured on GB300 over 64M rows
 // this runs 1.3x faster than every lane applying its own row with atomics,
 // for a 1024-group column as for a Zipf(1.1) column with preloaded heavy
-// hitters. The composite-key kernel (MODE 2) applies rows per lane.
+// hitters. The composite-key kernel (MODE 2) combines peers the same way.
 template <int MODE, int NV, uint32_t SPEC>
 __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   extern __shared__ uint64_t sm[];

@@ -1086,16 +1086,27 @@ struct AsofItemsK {
   uint32_t* err;
 };
 
+// Partition slot of row p: 0 without keys, -1 for a NULL key or a key the
+// table does not hold. A dense table needs no hash.
+__device__ __forceinline__ int64_t asof_slot(const DevCol* key, int nkeys, const JTable& T, uint64_t p,
+                                             uint32_t* err) {
+  if (nkeys == 0) return 0;
+  if (T.strategy == QEG_JOIN_DENSE) {
+    if (!col_valid(key[0], p)) return -1;
+    const int64_t v = dense_value(key[0], p);
+    const uint64_t s = static_cast<uint64_t>(v) - static_cast<uint64_t>(T.dmin);
+    return (v < T.dmin || s >= T.cap) ? -1 : static_cast<int64_t>(s);
+  }
+  uint64_t w[kMaxKeys], h;
+  return load_key(key, nkeys, p, w, h) ? probe_slot(T, key, p, w, h, err) : -1;
+}
+
 __global__ void asof_items_kernel(const AsofItemsK P) {
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
     uint32_t slot = P.nslots;
     uint64_t rel = 0;
     if (col_valid(P.ts, r)) {
-      int64_t s = 0;
-      if (P.nkeys > 0) {
-        uint64_t w[kMaxKeys], h;
-        s = load_key(P.key, P.nkeys, r, w, h) ? probe_slot(P.T, P.key, r, w, h, P.err) : -1;
-      }
+      const int64_t s = asof_slot(P.key, P.nkeys, P.T, r, P.err);
       if (s >= 0) {
         slot = static_cast<uint32_t>(s);
         rel = static_cast<uint64_t>(int_value(P.ts, r)) - static_cast<uint64_t>(P.tmin);
@@ -1236,11 +1247,7 @@ __global__ void __launch_bounds__(256) asof_probe_kernel(const AsofProbeK P) {
   for (uint64_t p = c0 + threadIdx.x; p < c1; p += blockDim.x) {
     uint32_t m = kNullRow;
     if (col_valid(P.ts, p)) {
-      int64_t s = 0;
-      if (P.nkeys > 0) {
-        uint64_t w[kMaxKeys], h;
-        s = load_key(P.key, P.nkeys, p, w, h) ? probe_slot(P.T, P.key, p, w, h, P.err) : -1;
-      }
+      const int64_t s = asof_slot(P.key, P.nkeys, P.T, p, P.err);
       if (s >= 0) {
         const int64_t t = int_value(P.ts, p);
         const uint64_t b = P.abeg[s], e = P.aend[s];
