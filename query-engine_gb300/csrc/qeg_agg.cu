@@ -290,6 +290,11 @@ constexpr uint32_t kSpecF64 = 4u | spec_field(1, 0, 0) | spec_field(2, F_SUMF, 0
 constexpr uint32_t kSpecF64Nulls = 4u | spec_field(1, F_NULLS, 0) | spec_field(2, F_SUMF, 0) |
                                    spec_field(3, F_MINF, 0) | spec_field(4, F_MAXF, 0);
 constexpr uint32_t kSpecCount = 0u;
+// SUM over an integer column plus SUM/MIN/MAX over an F64 column (bar-style
+// aggregates: volume, then mean/low/high price), without NULL counts.
+constexpr uint32_t kSpecIntSumF64Stats = 6u | spec_field(1, 0, 0) | spec_field(2, F_SUMI, 0) | spec_field(3, 0, 1) |
+                                         spec_field(4, F_SUMF, 1) | spec_field(5, F_MINF, 1) |
+                                         spec_field(6, F_MAXF, 1);
 
 // The global (MODE 0) and single-key (MODE 1) kernels combine the rows of a
 // warp that share a group before applying them (warp peer aggregation, with
@@ -769,6 +774,9 @@ void AggState::plan(const int32_t* col_types, int ncols, const uint32_t* key_col
     if (std::find(v.begin(), v.end(), F_NULLS) == v.end()) v.insert(v.begin(), F_NULLS);
     if (kind != F_NULLS && std::find(v.begin(), v.end(), kind) == v.end()) v.push_back(kind);
   }
+  // Fields of a column in kind order (NULLS, sums, MINs, MAXes) whatever the
+  // order of the aggregates, so equal field sets share a specialised kernel.
+  for (auto& v : per_col) std::sort(v.begin(), v.end());
   cfirst.assign(val_cols.size(), 0);
   cnf.assign(val_cols.size(), 0);
   for (size_t c = 0; c < val_cols.size(); ++c) {
@@ -913,10 +921,12 @@ void AggState::launch(const AggK& P, uint64_t nrows) {
    : spec == kSpecF64         ? agg_kernel<M, 1, kSpecF64>                    \
    : spec == kSpecF64Nulls    ? agg_kernel<M, 1, kSpecF64Nulls>               \
    : spec == kSpecCount       ? agg_kernel<M, 1, kSpecCount>                  \
+   : spec == kSpecIntSumF64Stats ? agg_kernel<M, 2, kSpecIntSumF64Stats>      \
                               : nullptr)
   const uint32_t spec = field_spec(P);
   if (mode == 0) kern = QEG_AGG_SPEC(0);
   else if (mode == 1) kern = QEG_AGG_SPEC(1);
+  else kern = QEG_AGG_SPEC(2);
   if (kern == nullptr) {
     if (mode == 0) kern = QEG_AGG_VARIANT(0);
     else if (mode == 1) kern = QEG_AGG_VARIANT(1);
