@@ -1007,6 +1007,18 @@ def main():
         v, dt, cres = cpu_reference(sample, threads, args.cpu_probe_rows, W.nbuild)
         cpu = {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
                "sample": "full 2^24-row build + first %d probe rows (%.1f s)" % (args.cpu_probe_rows, dt)}
+        # Second reference point: the single-threaded operator tree (scan ->
+        # join -> aggregate, the restatement of Plan::lower + drain).
+        import oracle as O
+
+        k1 = min(args.cpu_probe_rows, 1 << 23)
+        t0 = time.perf_counter()
+        r1 = O.join_count_sum(O.TCol(O.I64, sample[0].values[:k1], sample[0].valid[:k1]),
+                              O.TCol(O.I64, sample[1].values[:k1]), sample[2])
+        dt1 = time.perf_counter() - t0
+        cpu["single_thread"] = {"value": (W.nbuild + k1) / dt1, "unit": "rows/s", "cores": 1,
+                                "sample": "full 2^24-row build + first %d probe rows (%.1f s), count %d"
+                                          % (k1, dt1, r1[0])}
 
     if rank == 0:
         strategy_name = {1: "hash", 2: "partitioned", 3: "dense"}.get(st["strategy"], str(st["strategy"]))
