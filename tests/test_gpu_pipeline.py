@@ -57,8 +57,10 @@ def oracle_pipeline(trades, symbols, aggs):
     return O.groupby(cols, [4], aggs)
 
 
+@pytest.mark.parametrize("lanes", ["1", "0"])
 @pytest.mark.parametrize("seed,nulls,dup", [(1, True, False), (2, False, False), (3, True, True)])
-def test_pipeline_matches_operator_chain(ctx, seed, nulls, dup):
+def test_pipeline_matches_operator_chain(ctx, seed, nulls, dup, lanes, monkeypatch):
+    monkeypatch.setenv("QEG_PIPE_LANES", lanes)
     trades, symbols = make_case(seed, nulls=nulls, dup_syms=dup)
     aggs = [(O.COUNT_STAR, 0), (O.AVG, 1), (O.SUM, 2), (O.MIN, 1), (O.MAX, 2), (O.COUNT, 1)]
     ot, orows = oracle_pipeline(trades, symbols, aggs)
@@ -92,11 +94,14 @@ def test_pipeline_integer_keys_and_filter_on_int(ctx):
     assert_same(gt, grows, ot, orows)
 
 
+@pytest.mark.parametrize("lanes", ["1", "0"])
 @pytest.mark.parametrize("seed,nulls", [(4, False), (5, True)])
-def test_pipeline_trades_aggregates_specialised_kernel(ctx, seed, nulls):
+def test_pipeline_trades_aggregates_specialised_kernel(ctx, seed, nulls, lanes, monkeypatch):
     """The trades workload's exact aggregate list -- COUNT(*), AVG(price),
     SUM(qty) -- runs the field-set-specialised kernel (with NULL counts when
-    the columns have NULLs); device-resident columns as in the benchmark."""
+    the columns have NULLs); device-resident columns as in the benchmark;
+    per-lane shared reductions (the default) and warp peer aggregation."""
+    monkeypatch.setenv("QEG_PIPE_LANES", lanes)
     trades, symbols = make_case(seed, nulls=nulls)
     aggs = [(O.COUNT_STAR, 0), (O.AVG, 1), (O.SUM, 2)]
     ot, orows = oracle_pipeline(trades, symbols, aggs)
