@@ -516,6 +516,208 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
   if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
 }
 
+// ---------------------------------------------------------------------------
+// Composite keys with a CTA-private table (QEG_AGG_SMEM in mode 2; the
+// default for the tumbling window's (keys..., bucket)). Each CTA walks one
+// contiguous range of rows and keeps the groups it meets in a shared-memory
+// table of composite rows ([state][null mask][key words][fields], the global
+// row format), which it flushes into the global table whenever half of it is
+// in use, and at the end. On input with locality -- tick data in time order,
+// where only the current buckets' groups are live -- most rows cost
+// shared-memory reductions, and the global table sees one merge per (CTA,
+// group, flush) instead of one per row. Groups that miss the private table
+// (probe limit, or no free slot while the global table is full) take the
+// global path and spill as usual; partial rows that cannot be merged at the
+// final flush go to the partial-row list, merged after the host grows the
+// table.
+// ---------------------------------------------------------------------------
+constexpr int kPrivProbe = 16;
+
+// Composite-row hash of a row's key words and NULL mask (the kernels' rule).
+__device__ __forceinline__ uint64_t row_hashN(const AggK& P, const uint64_t* words, uint64_t nullmask) {
+  uint64_t h = kHashSeed;
+  for (int j = 0; j < P.nkeys; ++j) h = hash_fold(h, ((nullmask >> j) & 1ull) ? 0x9E3779B97F4A7C15ull : words[j]);
+  return h;
+}
+
+// The private-table slot of a key tuple (found, or claimed when `may_insert`),
+// or -1. A claim publishes the key words before the row's tag (fence within
+// the CTA); a lookup that sees a claim in progress waits for it, bounded.
+__device__ __forceinline__ int priv_row(uint64_t* sm, int S, int SW, const AggK& P, const uint64_t* words,
+                                        uint64_t nullmask, uint64_t h, unsigned* used, bool may_insert) {
+  const uint64_t tag = (h >> 32) | 2ull;
+  int s = static_cast<int>(h & static_cast<uint64_t>(S - 1));
+  for (int t = 0; t < kPrivProbe; ++t) {
+    uint64_t* r = &sm[s * SW];
+    uint64_t st = ld_volatile_shared(r);
+    if (st == 0) {
+      if (!may_insert) return -1;
+      const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, 1ull);
+      if (old == 0) {
+        r[1] = nullmask;
+        for (int j = 0; j < P.nkeys; ++j) r[2 + j] = words[j];
+        __threadfence_block();
+        atomicExch(reinterpret_cast<unsigned long long*>(r), static_cast<unsigned long long>(tag));
+        atomicAdd(used, 1u);
+        return s;
+      }
+      st = old;
+    }
+    int spins = 0;
+    while (st == 1) {
+      if (++spins > kSpinLimit) {
+        atomicOr(P.err, kDevSpinTimeout);
+        return -1;
+      }
+      st = ld_volatile_shared(r);
+    }
+    if (st == tag) {
+      __threadfence_block();
+      bool eq = ld_volatile_shared(r + 1) == nullmask;
+      for (int j = 0; eq && j < P.nkeys; ++j) eq = ld_volatile_shared(r + 2 + j) == words[j];
+      if (eq) return s;
+    }
+    s = (s + 1) & (S - 1);
+  }
+  return -1;
+}
+
+// Merges the private table into the global table (every thread of the CTA
+// calls it). Rows that merge are cleared; the rest stay (global table full)
+// or, at the final flush, go to the partial-row list.
+__device__ __forceinline__ void priv_flush(uint64_t* sm, int S, int SW, const AggK& P, unsigned* used,
+                                           unsigned* left, int* gfull, bool final, unsigned long long& inserted) {
+  const int W = P.row_words;
+  const int fo = 2 + P.nkeys;
+  if (threadIdx.x == 0) *left = 0;
+  __syncthreads();
+  for (int slot = threadIdx.x; slot < S; slot += blockDim.x) {
+    uint64_t* src = &sm[slot * SW];
+    if (src[0] < 2) continue;
+    uint64_t words[kMaxKeys];
+    for (int j = 0; j < P.nkeys; ++j) words[j] = src[2 + j];
+    uint64_t* dst = global_rowN(P, words, src[1], row_hashN(P, words, src[1]), inserted);
+    if (dst) {
+      merge_fields(dst + fo, src + fo, P);
+    } else if (final) {
+      const unsigned long long i = atomicAdd(P.counters + 1, 1ull);
+      if (i < P.part_cap) {
+        for (int w = 0; w < W; ++w) P.spill_parts[i * W + w] = src[w];
+      } else {
+        atomicOr(P.err, kDevSpillOverflow);
+      }
+    } else {
+      atomicAdd(left, 1u);
+      continue;
+    }
+    for (int w = 0; w < W; ++w) src[w] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *used = *left;
+    if (*left >= static_cast<unsigned>(S / 2)) *gfull = 1;
+  }
+  __syncthreads();
+}
+
+template <int NV, uint32_t SPEC>
+__global__ void __launch_bounds__(512, 2) agg2_private_kernel(const AggK P) {
+  extern __shared__ uint64_t sm[];
+  const int W = P.row_words;
+  const int SW = W | 1;
+  const int S = P.smem_slots;
+  const int fo = 2 + P.nkeys;
+  const unsigned lane = threadIdx.x & 31u;
+  __shared__ unsigned s_used, s_left;
+  __shared__ int s_gfull;
+  for (int i = threadIdx.x; i < S * SW; i += blockDim.x) sm[i] = 0;
+  if (threadIdx.x == 0) {
+    s_used = 0;
+    s_gfull = 0;
+  }
+  __syncthreads();
+  unsigned long long inserted = 0;
+  const uint64_t per = (P.nrows + gridDim.x - 1) / gridDim.x;
+  const uint64_t chunk = (per + blockDim.x - 1) / blockDim.x * blockDim.x;
+  const uint64_t r0 = static_cast<uint64_t>(blockIdx.x) * chunk;
+  const uint64_t r1 = r0 + chunk < P.nrows ? r0 + chunk : P.nrows;
+  // Block-uniform loop: every thread makes the same passes (the flush check
+  // synchronises the CTA after each one).
+  for (uint64_t base = r0; base < r1; base += blockDim.x) {
+    const uint64_t i = base + threadIdx.x;
+    bool live = i < r1;
+    uint64_t p = i;
+    if (live && P.sel) {
+      p = P.sel[i];
+      if (p >= P.len) {
+        atomicOr(P.err, kDevBadInput);
+        live = false;
+      }
+    }
+    bool vv[kMaxVals];
+    uint64_t vb[kMaxVals];
+#pragma unroll
+    for (int c = 0; c < kMaxVals; ++c) {
+      vv[c] = false;
+      vb[c] = 0;
+    }
+    if (live) load_values<NV>(P, p, vv, vb);
+    const unsigned livemask = __ballot_sync(0xffffffffu, live);
+    uint64_t words[kMaxKeys];
+    uint64_t nullmask = live ? 0 : ~0ull, h = kHashSeed;
+#pragma unroll
+    for (int j = 0; j < kMaxKeys; ++j) {
+      words[j] = 0;
+      if (live && j < P.nkeys) {
+        const bool kv = col_valid(P.key[j], p);
+        words[j] = kv ? key_word(P.key[j], p) : 0;
+        if (!kv) nullmask |= 1ull << j;
+        h = hash_fold(h, kv ? words[j] : 0x9E3779B97F4A7C15ull);
+      }
+    }
+    // Peers: lanes with the same key tuple (hash match, then an exact check
+    // against the match group's first lane), as in agg_kernel's mode 2.
+    const unsigned same = __match_any_sync(0xffffffffu, live ? h : ~static_cast<uint64_t>(lane));
+    const int ref = __ffs(same) - 1;
+    bool eq = __shfl_sync(0xffffffffu, nullmask, ref) == nullmask;
+#pragma unroll
+    for (int j = 0; j < kMaxKeys; ++j)
+      if (j < P.nkeys) eq &= __shfl_sync(0xffffffffu, words[j], ref) == words[j];
+    const unsigned eqmask = __ballot_sync(0xffffffffu, eq);
+    unsigned peers = (live && eq) ? (same & eqmask & livemask) : (1u << lane);
+    const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
+    uint64_t* f = nullptr;
+    int space = kRowGlobal;
+    if (leader) {
+      const int slot = priv_row(sm, S, SW, P, words, nullmask, h, &s_used, s_gfull == 0);
+      if (slot >= 0) {
+        f = &sm[slot * SW + fo];
+        space = kRowShared;
+      } else {
+        uint64_t* r = global_rowN(P, words, nullmask, h, inserted);
+        if (r) f = r + fo;
+      }
+    }
+    const unsigned placed = __ballot_sync(0xffffffffu, f != nullptr);
+    const bool ok = live && ((placed >> (__ffs(peers) - 1)) & 1u);
+    if (live && !ok) {
+      spill_row(P, p);
+      peers = 1u << lane;
+    }
+    const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
+    if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader && ok, space, peers, pp, vv, vb);
+    else warp_apply<NV>(f, leader && ok, space, peers, pp, P, vv, vb);
+    // One CTA-wide decision (a barrier that also ORs the predicate), so every
+    // thread enters the flush, or none does.
+    if (__syncthreads_or(threadIdx.x == 0 && s_used >= static_cast<unsigned>(S / 2) && s_gfull == 0))
+      priv_flush(sm, S, SW, P, &s_used, &s_left, &s_gfull, false, inserted);
+  }
+  __syncthreads();
+  priv_flush(sm, S, SW, P, &s_used, &s_left, &s_gfull, true, inserted);
+  for (int o = 16; o > 0; o >>= 1) inserted += __shfl_down_sync(0xffffffffu, inserted, o);
+  if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
+}
+
 // Re-inserts every occupied row of `old` into the (zeroed) table of P.
 template <int MODE>
 __global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, uint64_t old_cap) {
@@ -560,19 +762,31 @@ __global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, ui
   if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
 }
 
-// Merges spilled partial rows (single-key mode) into the table.
+// Merges spilled partial rows (single-key rows, or composite rows of the
+// composite private tables) into the table.
+template <int MODE>
 __global__ void merge_parts_kernel(const AggK P, const uint64_t* __restrict__ parts, uint64_t n) {
   const int W = P.row_words;
   unsigned long long inserted = 0;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t* src = parts + i * W;
-    const uint64_t k = src[0];
-    uint64_t* dst = global_row1(P, true, k, key_hash1(k), inserted, P.probe_limit);
+    uint64_t* dst;
+    int fo;
+    if (MODE == 2) {
+      uint64_t words[kMaxKeys];
+      for (int j = 0; j < P.nkeys; ++j) words[j] = src[2 + j];
+      dst = global_rowN(P, words, src[1], row_hashN(P, words, src[1]), inserted);
+      fo = 2 + P.nkeys;
+    } else {
+      const uint64_t k = src[0];
+      dst = global_row1(P, true, k, key_hash1(k), inserted, P.probe_limit);
+      fo = 1;
+    }
     if (!dst) {
       atomicOr(P.err, kDevSpillOverflow);
       continue;
     }
-    merge_fields(dst + 1, src + 1, P);
+    merge_fields(dst + fo, src + fo, P);
   }
   for (int o = 16; o > 0; o >>= 1) inserted += __shfl_down_sync(0xffffffffu, inserted, o);
   if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
@@ -901,7 +1115,39 @@ size_t AggState::smem_bytes(int block) const {
   return b;
 }
 
+void AggState::launch_private(const AggK& P, uint64_t nrows) {
+  void (*kern)(AggK) = nullptr;
+  const int nv = static_cast<int>(val_cols.size());
+  const uint32_t spec = field_spec(P);
+  if (spec == kSpecIntF64) kern = agg2_private_kernel<2, kSpecIntF64>;
+  else if (spec == kSpecIntF64Nulls) kern = agg2_private_kernel<2, kSpecIntF64Nulls>;
+  else if (spec == kSpecF64) kern = agg2_private_kernel<1, kSpecF64>;
+  else if (spec == kSpecF64Nulls) kern = agg2_private_kernel<1, kSpecF64Nulls>;
+  else if (spec == kSpecCount) kern = agg2_private_kernel<1, kSpecCount>;
+  else if (spec == kSpecIntSumF64Stats) kern = agg2_private_kernel<2, kSpecIntSumF64Stats>;
+  else if (nv <= 1) kern = agg2_private_kernel<1, kGenericSpec>;
+  else if (nv <= 2) kern = agg2_private_kernel<2, kGenericSpec>;
+  else if (nv <= 4) kern = agg2_private_kernel<4, kGenericSpec>;
+  else kern = agg2_private_kernel<8, kGenericSpec>;
+  const int block = 512;
+  const size_t sb = static_cast<size_t>(smem_slots) * (row_words | 1) * 8;
+  if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+  int per_sm = 1;
+  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
+  require(per_sm > 0, "aggregate kernel does not fit on an SM with this configuration");
+  // Each CTA walks one contiguous range; a few thousand rows at least.
+  uint64_t grid = std::min<uint64_t>((nrows + 4095) / 4096, static_cast<uint64_t>(ctx->sms) * per_sm);
+  if (grid == 0) grid = 1;
+  kern<<<(unsigned)grid, block, sb, ctx->stream>>>(P);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+}
+
 void AggState::launch(const AggK& P, uint64_t nrows) {
+  if (mode == 2 && strategy == QEG_AGG_SMEM) {
+    launch_private(P, nrows);
+    return;
+  }
   const int block = block_threads();
   const size_t sb = smem_bytes(block);
   if (mode == 1)  // running insert count and table-full flag
@@ -1038,7 +1284,12 @@ void AggState::consume(const qeg_column* cols, int ncols, const uint32_t* sel, u
     QEG_CUDA(cudaMemsetAsync(counters.get(), 0, 16, ctx->stream));
     if (nparts) {
       AggK Q = kparams_base();
-      merge_parts_kernel<<<grid_for(ctx, nparts, 256, 8), 256, 0, ctx->stream>>>(Q, parts_copy.get<uint64_t>(), nparts);
+      if (mode == 2)
+        merge_parts_kernel<2><<<grid_for(ctx, nparts, 256, 8), 256, 0, ctx->stream>>>(Q, parts_copy.get<uint64_t>(),
+                                                                                      nparts);
+      else
+        merge_parts_kernel<1><<<grid_for(ctx, nparts, 256, 8), 256, 0, ctx->stream>>>(Q, parts_copy.get<uint64_t>(),
+                                                                                      nparts);
       ctx->launches++;
       QEG_CUDA(cudaGetLastError());
     }
@@ -1094,7 +1345,12 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
 
   // Strategy.
   strategy = cfg.strategy;
-  if (mode == 2) strategy = QEG_AGG_GLOBAL;
+  // Composite keys: CTA-private tables with periodic flushes when asked for,
+  // and by default for the tumbling window, whose input is tick data in time
+  // order; the global table alone otherwise.
+  if (mode == 2)
+    strategy = (cfg.strategy == QEG_AGG_SMEM || (cfg.strategy == QEG_AGG_AUTO && bucket_width > 0)) ? QEG_AGG_SMEM
+                                                                                                      : QEG_AGG_GLOBAL;
   if (mode == 0) strategy = QEG_AGG_SMEM;
   // Leave room for the warp-private rows (<= 32 KB) and the slot ranks.
   const int max_slots =
@@ -1126,6 +1382,14 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
       QEG_CUDA(cudaStreamSynchronize(ctx->stream));
       smem_insert = 0;
     }
+  } else if (strategy == QEG_AGG_SMEM && mode == 2) {
+    // Two 512-thread CTAs per SM, each with its table.
+    const size_t row_bytes = static_cast<size_t>(row_words | 1) * 8;
+    int fit = 1;
+    while (static_cast<size_t>(fit) * 2 * row_bytes <= ctx->smem_optin / 2 - 2048) fit *= 2;
+    smem_slots = cfg.smem_slots > 0 ? static_cast<int>(next_pow2(cfg.smem_slots)) : 1024;
+    smem_slots = std::max(64, std::min(smem_slots, fit));
+    smem_insert = 1;
   } else {
     smem_slots = 0;
   }

@@ -147,6 +147,7 @@ struct AggState {
   void set_field_columns(AggK& P) const;
   uint32_t field_spec(const AggK& P) const;  // qeg_warpagg.cuh field-set code
   void launch(const AggK& P, uint64_t nrows);
+  void launch_private(const AggK& P, uint64_t nrows);  // composite keys, CTA-private tables
   void read_counters(uint64_t out[3]);
   void grow(uint64_t new_cap);
   void first_consume(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len, const uint32_t* dsel);

@@ -210,3 +210,23 @@ def test_skewed_sketch_path_with_and_without_preloaded_hot_keys(ctx, hot, block)
     ot, orows = O.groupby([key, v1, v2], [0], aggs, 1 << 23)
     gt, grows = run_gpu(ctx, [key, v1, v2], [0], aggs, config=cfg)
     assert_same(gt, grows, ot, orows, "hot %d block %d" % (hot, block))
+
+
+@pytest.mark.parametrize("slots,cap", [(64, 1024), (1024, 0), (128, 4096)])
+def test_composite_keys_private_tables_with_flushes(ctx, slots, cap):
+    # Composite keys through CTA-private tables that flush into the global
+    # table whenever half full: tiny private tables force many flushes, a tiny
+    # fixed global table forces the global-full path (rows spill, partial rows
+    # of the final flush go to the partial-row list, grow and replay).
+    rng = np.random.default_rng(50 + slots)
+    n = 400000
+    k1 = O.TCol(O.I32, rng.integers(0, 300, n).astype(np.int32), rng.random(n) > 0.03)
+    k2 = O.TCol(O.I64, np.sort(rng.integers(0, 2000, n)), rng.random(n) > 0.03)  # ordered, like time buckets
+    v1 = O.TCol(O.F64, rng.normal(0, 10, n), rng.random(n) > 0.1)
+    v2 = O.TCol(O.I64, rng.integers(-1000, 1000, n))
+    aggs = [(O.COUNT_STAR, 0), (O.SUM, 2), (O.AVG, 2), (O.MIN, 3), (O.MAX, 3), (O.COUNT, 2)]
+    cfg = qeg.agg_config(strategy=qeg.AGG_SMEM, smem_slots=slots,
+                         sizing=qeg.SIZE_FIXED if cap else qeg.SIZE_LEARNED, initial_capacity=cap)
+    ot, orows = O.groupby([k1, k2, v1, v2], [0, 1], aggs, 1 << 20)
+    gt, grows = run_gpu(ctx, [k1, k2, v1, v2], [0, 1], aggs, config=cfg)
+    assert_same(gt, grows, ot, orows, "slots %d cap %d" % (slots, cap))
