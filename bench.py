@@ -1061,18 +1061,20 @@ def run_reference(args, threads):
     for _ in range(max(0, min(args.warmup, 1))):
         cpu_reference(sample, threads, rows, 1 << 24)
     vals, times = [], []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(1, min(args.steps, 5))):
         v, dt, res = cpu_reference(sample, threads, rows, 1 << 24)
         vals.append(v)
         times.append(dt)
     v = float(np.mean(vals))
+    ms = np.array(times) * 1e3
     print(json.dumps({
         "impl": "reference", "metric": "rows/s hash join (build+probe rows), inner join COUNT(*)+SUM(payload)",
         "value": v, "unit": "rows/s", "n_gpus": args.gpus, "steps": len(vals), "warmup": args.warmup,
         "ms_per_step": float(np.mean(times)) * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded)",
         "config": {"workload": "join_16Mx256M_count_sum", "build_rows": 1 << 24, "probe_rows": 1 << 28,
-                   "sampled_probe_rows": rows},
+                   "sampled_probe_rows": rows, "ms_p50": float(np.percentile(ms, 50)),
+                   "ms_p99": float(np.percentile(ms, 99))},
         "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
                          "sample": "full 2^24-row build + first %d probe rows per step" % rows},
         "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
