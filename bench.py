@@ -298,6 +298,26 @@ def run_agg_bench(args, dev, local):
                      "launches_per_step": (ctx.launches - launches0) / args.steps}
     clocks = clk.summary(tw0, time.time())
     clk.__exit__(None, None, None)
+    check = None
+    if W.kind == "skew":
+        # Full-size property check ("checksum of checksums"): the per-group
+        # aggregates must add up to the column totals -- counts to the row
+        # count, integer sums exactly, the extreme MIN/MAX to the column's,
+        # F64 sums within 1e-9 of the sum of magnitudes.
+        a = qeg.Aggregate(ctx, [c.type for c in W.cols], [0], W.aggs, variants[next(iter(variants))])
+        a.consume(W.cols)
+        a.finish()
+        res = a.fetch_torch()
+        ctx.synchronize()
+        a.close()
+        cnt, s1, s2, mn, mx = (res[i][0] for i in range(1, 6))
+        tol = 1e-9 * float(W.v2.abs().sum())
+        check = {"count_total": int(cnt.sum()) == W.n,
+                 "sum_i64_exact": int(s1.sum()) == int(W.v1.sum()),
+                 "sum_f64_within": abs(float(s2.sum()) - float(W.v2.sum())) <= tol,
+                 "min_max": int(mn.min()) == int(W.v1.min()) and int(mx.max()) == int(W.v1.max())}
+        assert all(check.values()), check
+        del res
     cpu = None
     if not args.no_cpu:
         cpu = cpu_agg_baseline(W, os.cpu_count() or 1)
@@ -307,7 +327,7 @@ def run_agg_bench(args, dev, local):
         "metric": "rows/s hash aggregate (%s)" % W.name, "value": best["rows_per_s"], "unit": "rows/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["ms_per_step"],
         "higher_is_better": True, "dtype": "int64+f64", "data": "synthetic (seeded, generated on the GPU)",
-        "config": {"workload": W.name, "rows": W.n, "groups": W.groups},
+        "config": {"workload": W.name, "rows": W.n, "groups": W.groups, "full_size_check": check},
         "roofline": {"bound": "hbm", "achieved": best["gb_per_s"], "peak": peak, "peak_kind": kind,
                      "unit": "GB/s", "frac": best["gb_per_s"] / peak},
         "variants": out,

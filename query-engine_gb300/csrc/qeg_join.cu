@@ -1133,14 +1133,13 @@ __global__ void time_order_kernel(DevCol ts, uint64_t n, unsigned int* unsorted)
 constexpr int kAsofSample = 32;
 
 __global__ void asof_runs_kernel(const uint32_t* __restrict__ hi, const uint64_t* __restrict__ lo, uint64_t n,
-                                 uint32_t nslots, uint32_t* __restrict__ beg, uint32_t* __restrict__ end,
-                                 uint64_t* __restrict__ samp) {
+                                 uint32_t nslots, uint2* __restrict__ runs, uint64_t* __restrict__ samp) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t s = hi[i];
     if (i % kAsofSample == 0) samp[i / kAsofSample] = lo[i];
     if (s >= nslots) continue;
-    if (i == 0 || hi[i - 1] != s) beg[s] = static_cast<uint32_t>(i);
-    if (i + 1 == n || hi[i + 1] != s) end[s] = static_cast<uint32_t>(i + 1);
+    if (i == 0 || hi[i - 1] != s) runs[s].x = static_cast<uint32_t>(i);
+    if (i + 1 == n || hi[i + 1] != s) runs[s].y = static_cast<uint32_t>(i + 1);
   }
 }
 
@@ -1161,8 +1160,7 @@ struct AsofProbeK {
   int64_t tmin;
   const uint64_t* ats;   // sorted timestamps - tmin
   const uint32_t* arow;  // build rows in the same order
-  const uint32_t* abeg;  // partition runs: [abeg[s], aend[s])
-  const uint32_t* aend;
+  const uint2* aruns;  // partition runs: [aruns[s].x, aruns[s].y)
   const uint64_t* asamp;  // ats[i * kAsofSample]
   int left, tol_set;
   uint64_t tol;
@@ -1177,28 +1175,29 @@ struct AsofProbeK {
 // starts at a hint inside the run and gallops outward (1, 2, 4, ...
 // positions) before a binary search of the bracket -- a few loads in the same
 // cache lines when the hint is close, as it is for a probe side in time order.
-__device__ __forceinline__ uint64_t asof_gallop(const uint64_t* __restrict__ ats, uint64_t b, uint64_t e,
-                                                uint64_t h, uint64_t rel) {
-  uint64_t lo, hi;
+__device__ __forceinline__ uint32_t asof_gallop(const uint64_t* __restrict__ ats, uint32_t b, uint32_t e,
+                                                uint32_t h, uint64_t rel) {
+  // Positions are 32-bit; the step and the sums that could pass 2^32 are not.
+  uint32_t lo, hi;
   if (ats[h] <= rel) {
     lo = h + 1;
     uint64_t d = 1;
     while (lo + d - 1 < e && ats[lo + d - 1] <= rel) {
-      lo += d;
+      lo += static_cast<uint32_t>(d);
       d <<= 1;
     }
-    hi = lo + d - 1 < e ? lo + d - 1 : e;
+    hi = static_cast<uint32_t>(lo + d - 1 < e ? lo + d - 1 : e);
   } else {
     hi = h;
     uint64_t d = 1;
     while (hi >= b + d && ats[hi - d] > rel) {
-      hi -= d;
+      hi -= static_cast<uint32_t>(d);
       d <<= 1;
     }
-    lo = hi >= b + d ? hi - d + 1 : b;
+    lo = hi >= b + d ? static_cast<uint32_t>(hi - d + 1) : b;
   }
   while (lo < hi) {
-    const uint64_t mid = lo + ((hi - lo) >> 1);
+    const uint32_t mid = lo + ((hi - lo) >> 1);
     if (ats[mid] <= rel) lo = mid + 1;
     else hi = mid;
   }
@@ -1208,13 +1207,14 @@ __device__ __forceinline__ uint64_t asof_gallop(const uint64_t* __restrict__ ats
 // First position in [b, e) whose time is > rel, from scratch: over the
 // samples inside the run (every kAsofSample-th sorted time, small enough to
 // stay in L2), then over the <= kAsofSample times between two samples.
-__device__ __forceinline__ uint64_t asof_sampled(const AsofProbeK& P, uint64_t b, uint64_t e, uint64_t rel) {
-  uint64_t lo = b, hi = e;
-  const uint64_t ib = (b + kAsofSample - 1) / kAsofSample, ie = (e - 1) / kAsofSample;
+__device__ __forceinline__ uint32_t asof_sampled(const AsofProbeK& P, uint32_t b, uint32_t e, uint64_t rel) {
+  uint32_t lo = b, hi = e;
+  const uint32_t ib = static_cast<uint32_t>((static_cast<uint64_t>(b) + kAsofSample - 1) / kAsofSample);
+  const uint32_t ie = (e - 1) / kAsofSample;
   if (ib <= ie) {
-    uint64_t l = ib, r = ie + 1;
+    uint32_t l = ib, r = ie + 1;
     while (l < r) {
-      const uint64_t mid = l + ((r - l) >> 1);
+      const uint32_t mid = l + ((r - l) >> 1);
       if (P.asamp[mid] <= rel) l = mid + 1;
       else r = mid;
     }
@@ -1222,7 +1222,7 @@ __device__ __forceinline__ uint64_t asof_sampled(const AsofProbeK& P, uint64_t b
     if (l <= ie) hi = l * kAsofSample;
   }
   while (lo < hi) {
-    const uint64_t mid = lo + ((hi - lo) >> 1);
+    const uint32_t mid = lo + ((hi - lo) >> 1);
     if (P.ats[mid] <= rel) lo = mid + 1;
     else hi = mid;
   }
@@ -1250,13 +1250,14 @@ __global__ void __launch_bounds__(256) asof_probe_kernel(const AsofProbeK P) {
       const int64_t s = asof_slot(P.key, P.nkeys, P.T, p, P.err);
       if (s >= 0) {
         const int64_t t = int_value(P.ts, p);
-        const uint64_t b = P.abeg[s], e = P.aend[s];
+        const uint2 run = P.aruns[s];
+        const uint32_t b = run.x, e = run.y;
         if (e > b && t >= P.tmin) {
           const uint64_t rel = static_cast<uint64_t>(t) - static_cast<uint64_t>(P.tmin);
           const uint32_t hi = (static_cast<uint32_t>(s) * 2654435761u) >> (32 - kAsofHintBits);
           const uint32_t hp = hpos[hi];
           const bool hit = hslot[hi] == static_cast<uint32_t>(s) && hp >= b && hp < e;
-          const uint64_t j = hit ? asof_gallop(P.ats, b, e, hp, rel) : asof_sampled(P, b, e, rel);
+          const uint32_t j = hit ? asof_gallop(P.ats, b, e, hp, rel) : asof_sampled(P, b, e, rel);
           const uint32_t nh = static_cast<uint32_t>(j < e ? j : e - 1);
           hslot[hi] = static_cast<uint32_t>(s);
           hpos[hi] = nh;
@@ -1498,7 +1499,7 @@ struct JoinState {
   int64_t tol = 0;
   int64_t tmin = 0;
   uint32_t aslots = 0;
-  DevBuf ats, arow, abeg, aend, asamp, tbits, amatch;
+  DevBuf ats, arow, aruns, asamp, tbits, amatch;
   void asof_build();
   void asof_probe(uint64_t n);
 
@@ -1770,14 +1771,12 @@ void JoinState::asof_build() {
   SortItems A{a_lo.get<uint64_t>(), a_hi.get<uint32_t>(), a_val.get<uint32_t>()};
   SortItems B{b_lo.get<uint64_t>(), b_hi.get<uint32_t>(), b_val.get<uint32_t>()};
   const SortItems R = radix_sort_items(ctx, A, B, n, lo_bits, hi_bits);
-  abeg.alloc(ns * 4, ctx->stream);
-  aend.alloc(ns * 4, ctx->stream);
+  aruns.alloc(ns * 8, ctx->stream);
   asamp.alloc((n / kAsofSample + 1) * 8, ctx->stream);
-  QEG_CUDA(cudaMemsetAsync(abeg.get(), 0, ns * 4, ctx->stream));
-  QEG_CUDA(cudaMemsetAsync(aend.get(), 0, ns * 4, ctx->stream));
+  QEG_CUDA(cudaMemsetAsync(aruns.get(), 0, ns * 8, ctx->stream));
   if (n) {
     asof_runs_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(
-        R.hi, R.lo, n, aslots, abeg.get<uint32_t>(), aend.get<uint32_t>(), asamp.get<uint64_t>());
+        R.hi, R.lo, n, aslots, aruns.get<uint2>(), asamp.get<uint64_t>());
     ctx->launches++;
     QEG_CUDA(cudaGetLastError());
   }
@@ -1959,8 +1958,7 @@ void JoinState::asof_probe(uint64_t n) {
   P.tmin = tmin;
   P.ats = ats.get<uint64_t>();
   P.arow = arow.get<uint32_t>();
-  P.abeg = abeg.get<uint32_t>();
-  P.aend = aend.get<uint32_t>();
+  P.aruns = aruns.get<uint2>();
   P.asamp = asamp.get<uint64_t>();
   P.left = join_type == QEG_LEFT;
   P.tol_set = tol_set;
