@@ -852,6 +852,12 @@ __global__ void __launch_bounds__(1024) finalize_kernel(const AggK P, const FinK
       if (MODE == 1) {
         isnull = (s == P.cap + 1);
         w = (s == P.cap) ? 0 : r[0];
+        if (F.packed_width > 0) {  // (partition key, bucket index) packed in one word
+          isnull = false;
+          w = j == 0 ? static_cast<uint64_t>(static_cast<uint32_t>(w >> 32))
+                     : static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(w))) *
+                                             F.packed_width);
+        }
       } else {
         isnull = (r[1] >> j) & 1ull;
         w = r[2 + j];
@@ -1019,7 +1025,135 @@ void AggState::plan(const int32_t* col_types, int ncols, const uint32_t* key_col
 DevCol AggState::key_col(const std::vector<StagedCol>& staged, size_t j) const {
   DevCol c = staged[keys[j]].dev;
   c.bucket = (bucket_width > 0 && j + 1 == keys.size()) ? bucket_width : 0;
+  if (packed && j == 0) {
+    c.type = kPackedKey;
+    c.all_valid = 1;
+    c.validity = nullptr;
+    c.data2 = staged[keys[1]].dev.data;
+    c.type2 = staged[keys[1]].dev.type;
+    c.bucket = bucket_width;
+  }
   return c;
+}
+
+namespace {
+// Smallest and largest value of an integer column (valid rows), as
+// order-preserving encodings: out[0] = min, out[1] = max.
+__global__ void int_range_kernel(DevCol c, uint64_t n, unsigned long long* out) {
+  unsigned long long mn = ~0ull, mx = 0;
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
+    if (!col_valid(c, r)) continue;
+    const unsigned long long e = enc_i64(int_value(c, r));
+    mn = e < mn ? e : mn;
+    mx = e > mx ? e : mx;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = min(mn, __shfl_down_sync(0xffffffffu, mn, o));
+    mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  }
+  __shared__ unsigned long long smn[32], smx[32];
+  const unsigned warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    smn[warp] = mn;
+    smx[warp] = mx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (unsigned w = 1; w < nwarps; ++w) {
+      mn = min(mn, smn[w]);
+      mx = max(mx, smx[w]);
+    }
+    atomicMin(out + 0, mn);
+    atomicMax(out + 1, mx);
+  }
+}
+
+// Packed window rows -> composite rows: every occupied single-key row (and
+// the key-0 side row) is decoded into (partition key, bucket start) key words
+// and inserted into the new composite table with its fields.
+__global__ void unpack_kernel(const AggK P, const uint64_t* __restrict__ old, uint64_t old_cap, int old_w,
+                              int64_t width, int32_t time_type) {
+  unsigned long long inserted = 0;
+  const int fo = 2 + P.nkeys;
+  for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < old_cap + 2;
+       s += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t* src = old + s * old_w;
+    uint64_t k;
+    if (s < old_cap) {
+      k = src[0];
+      if (k == 0) continue;
+    } else {
+      if (src[1] == 0) continue;  // side rows: occupied when their row count is not zero
+      if (s == old_cap + 1) {     // a NULL key cannot be packed
+        atomicOr(P.err, kDevBadInput);
+        continue;
+      }
+      k = 0;
+    }
+    uint64_t words[kMaxKeys] = {};
+    words[0] = static_cast<uint32_t>(k >> 32);
+    const int64_t b = static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(k))) * width;
+    words[1] = time_type == kI32 ? static_cast<uint64_t>(static_cast<uint32_t>(static_cast<int32_t>(b)))
+                                 : static_cast<uint64_t>(b);
+    uint64_t* dst = global_rowN(P, words, 0, row_hashN(P, words, 0), inserted);
+    if (!dst) {
+      atomicOr(P.err, kDevSpillOverflow);
+      continue;
+    }
+    for (int f = 0; f < P.nfields; ++f) dst[fo + f] = src[1 + f];
+  }
+  for (int o = 16; o > 0; o >>= 1) inserted += __shfl_down_sync(0xffffffffu, inserted, o);
+  if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
+}
+}  // namespace
+
+// The batch can keep (or start) the packed key: both key columns without
+// NULLs and every bucket index of the time column within int32.
+bool AggState::can_pack(const std::vector<StagedCol>& staged, uint64_t len) {
+  if (!packable || staged.empty()) return false;
+  const DevCol& a = staged[keys[0]].dev;
+  const DevCol& t = staged[keys[1]].dev;
+  if (!a.all_valid || !t.all_valid) return false;
+  if (len == 0) return true;
+  DevBuf mm(16, ctx->stream);
+  const unsigned long long init[2] = {~0ull, 0ull};
+  QEG_CUDA(cudaMemcpyAsync(mm.get(), init, 16, cudaMemcpyHostToDevice, ctx->stream));
+  int_range_kernel<<<grid_for(ctx, len, 256, 4), 256, 0, ctx->stream>>>(t, len, mm.get<unsigned long long>());
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+  unsigned long long r[2];
+  QEG_CUDA(cudaMemcpyAsync(r, mm.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int64_t qmin = dec_i64(r[0]) / bucket_width, qmax = dec_i64(r[1]) / bucket_width;
+  return qmin >= INT32_MIN && qmax <= INT32_MAX;
+}
+
+// Converts the packed single-key table into composite rows (same capacity),
+// after which the window runs as an ordinary composite-key GROUP BY.
+void AggState::unpack() {
+  DevBuf old;
+  old.swap(table);
+  const uint64_t old_cap = cap;
+  const int old_w = row_words;
+  packed = false;
+  mode = 2;
+  row_words = 2 + static_cast<int>(keys.size()) + nfields;
+  strategy = QEG_AGG_GLOBAL;
+  smem_slots = 0;
+  nhot = 0;
+  alloc_table(old_cap);
+  part_cap = static_cast<uint64_t>(ctx->sms) * 32 * 2 + 64;
+  spill_parts.alloc(part_cap * row_words * 8, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(counters.get<uint8_t>() + 16, 0, 8, ctx->stream));
+  AggK P = kparams_base();
+  const unsigned g = grid_for(ctx, old_cap + 2, 256, 8);
+  unpack_kernel<<<g, 256, 0, ctx->stream>>>(P, old.get<uint64_t>(), old_cap, old_w, bucket_width, types[keys[1]]);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+  uint64_t c[3];
+  read_counters(c);
+  check_device_error(ctx);
+  inserted = c[2];
 }
 
 AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel, uint64_t nrows,
@@ -1257,6 +1391,7 @@ void AggState::consume(const qeg_column* cols, int ncols, const uint32_t* sel, u
   const uint32_t* dsel = nullptr;
   stage_sel(ctx, sel, sel_len, selbuf, &dsel);
   if (!table.get()) first_consume(staged, nrows, len, dsel);
+  else if (packed && !can_pack(staged, len)) unpack();
   if (nrows > spill_cap) {  // a later, larger batch: the spill list must hold all of it
     spill_cap = nrows;
     spill_rows.alloc(spill_cap * 4, ctx->stream);
@@ -1306,9 +1441,12 @@ void AggState::consume(const qeg_column* cols, int ncols, const uint32_t* sel, u
 
 void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len,
                              const uint32_t* dsel) {
-  (void)staged;
-  (void)len;
-  (void)dsel;
+  // A window with one I32 partition key starts packed when the batch allows.
+  if (packable && can_pack(staged, len)) {
+    packed = true;
+    mode = 1;
+    row_words = 1 + nfields;
+  }
   // Sizing. QEG_SIZE_FIXED: the configured (or default) first capacity, grown on
   // overflow. QEG_SIZE_LEARNED: the estimator's group count (see qeg_estimate),
   // falling back to the row count bound when no estimate is available.
@@ -1429,6 +1567,7 @@ void AggState::finish(uint64_t* nrows_out) {
   QEG_CUDA(cudaMemsetAsync(cnt.get(), 0, 8, ctx->stream));
   F.out_count = cnt.get<unsigned long long>();
   F.out_cap = out_cap;
+  F.packed_width = packed ? bucket_width : 0;
   AggK P = kparams_base();
   const uint64_t total = (mode == 0) ? 1 : (mode == 1 ? cap + 2 : cap);
   const unsigned g = grid_for(ctx, total, 1024, 2);
@@ -1514,6 +1653,7 @@ qeg_status qeg_window_create(qeg_ctx* ctx, const int32_t* col_types, int ncols, 
                  "block_threads must be 0 or a multiple of 32 in [32, 1024]");
     a->st.plan(col_types, ncols, k.data(), nkeys + 1, aggs, naggs);
     a->st.bucket_width = width;
+    a->st.packable = nkeys == 1 && col_types[key_cols[0]] == QEG_I32;
     *out = a.release();
   });
 }

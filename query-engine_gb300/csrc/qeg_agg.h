@@ -73,6 +73,7 @@ struct FinK {
   int naggs;
   unsigned long long* out_count;
   uint64_t out_cap;
+  int64_t packed_width;  // > 0: single-key rows hold packed (partition key, bucket index) words
 };
 
 // Key-column sketch: the estimator's inputs and the heavy-hitter candidates.
@@ -130,6 +131,11 @@ struct AggState {
   // Tumbling window (qeg_window_create): the last key is the time column, read
   // as its bucket's lower edge with this width; 0 for a plain GROUP BY.
   int64_t bucket_width = 0;
+  // A window with one I32 partition key may pack (key, bucket index) into one
+  // key word and take the single-key path while every batch allows it (no
+  // NULLs in either column, bucket indexes within int32); a batch that does
+  // not converts the table to composite rows.
+  bool packable = false, packed = false;
 
   bool finished = false;
   uint64_t nout = 0;
@@ -140,6 +146,8 @@ struct AggState {
   AggK kparams(const std::vector<StagedCol>& staged, const uint32_t* sel, uint64_t nrows, uint64_t len) const;
   AggK kparams_base() const;
   DevCol key_col(const std::vector<StagedCol>& staged, size_t j) const;
+  bool can_pack(const std::vector<StagedCol>& staged, uint64_t len);
+  void unpack();
   void alloc_table(uint64_t new_cap);
   size_t smem_bytes(int block) const;
   int warp_hot() const;

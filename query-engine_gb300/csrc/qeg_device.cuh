@@ -18,6 +18,9 @@
 namespace qeg {
 
 enum ColType : int32_t { kI32 = 0, kI64 = 1, kF64 = 2, kBOOL = 3, kTS = 4, kSTR = 5 };
+// Internal key type (never a column type): a tumbling window's I32 partition
+// key and bucket index packed into one key word (see key_word).
+constexpr int32_t kPackedKey = 16;
 
 constexpr uint64_t kCanonNaN = 0x7ff8000000000000ull;
 constexpr uint64_t kHashSeed = 0x51E57A11AB1E5EEDull;
@@ -34,6 +37,12 @@ struct DevCol {
   // edge of the value's bucket, (v / bucket) * bucket with C++ truncating
   // division, in the column's own type (tsx/window.cpp:318-330).
   int64_t bucket;
+  // kPackedKey: `data` is the I32 partition key, `data2` the time column of
+  // type `type2`; the key word is (partition key << 32) | (t / bucket) as a
+  // 32-bit index (both columns without NULLs, the index within int32).
+  const void* data2;
+  int32_t type2;
+  int32_t pad_;
 };
 
 __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
@@ -73,6 +82,14 @@ __device__ __forceinline__ uint64_t key_word(const DevCol& c, uint64_t p) {
       return static_cast<uint64_t>(v);
     }
     case kBOOL: return __ldg(static_cast<const uint8_t*>(c.data) + p);
+    case kPackedKey: {
+      const int32_t a = __ldg(static_cast<const int32_t*>(c.data) + p);
+      const long long t = c.type2 == kI32 ? static_cast<long long>(__ldg(static_cast<const int32_t*>(c.data2) + p))
+                                          : __ldg(static_cast<const long long*>(c.data2) + p);
+      const long long q = t / c.bucket;
+      return (static_cast<uint64_t>(static_cast<uint32_t>(a)) << 32) |
+             static_cast<uint32_t>(static_cast<int32_t>(q));
+    }
     case kF64: {
       const uint64_t b = static_cast<uint64_t>(__ldg(static_cast<const long long*>(c.data) + p));
       const uint64_t mag = b & 0x7fffffffffffffffull;

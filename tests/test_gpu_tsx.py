@@ -259,3 +259,63 @@ def test_asof_time_ordered_sides(ctx, jt):
     perm = rng.permutation(npr)
     shuffled = [O.TCol(c.type, c.values[perm], None if c.valid is None else c.valid[perm]) for c in probe]
     check_asof(ctx, shuffled, build, [0], [0], 1, 1, jt)
+
+
+def ticks_nonull(rng, n, nsym, t0=0, span=10 ** 12):
+    sym = zipf(rng, n, nsym).astype(np.int32)
+    t = np.sort(rng.integers(t0, t0 + span, n)) + rng.integers(-1000, 1000, n)
+    return [O.TCol(O.I32, sym), O.TCol(O.TS, t.astype(np.int64)), O.TCol(O.F64, rng.lognormal(4.6, 0.3, n)),
+            O.TCol(O.I32, rng.integers(1, 10000, n).astype(np.int32))]
+
+
+def test_window_packed_key_path(ctx):
+    # An I32 partition key and a TS time without NULLs: (sym, bucket index)
+    # packed into one key word (single-key kernels, sketch, learned sizing),
+    # including the (0, 0) group whose packed word is 0.
+    rng = np.random.default_rng(20)
+    cols = ticks_nonull(rng, 2 << 20, 400, t0=-5 * 10 ** 9)
+    cols[0].values[:1000] = 0
+    cols[1].values[:1000] = np.arange(1000)
+    aggs = [(O.COUNT_STAR, 0), (O.SUM, 3), (O.MIN, 2), (O.MAX, 2), (O.AVG, 2)]
+    check_window(ctx, cols, [0], 1, 60 * 10 ** 9, aggs=aggs)
+    check_window(ctx, cols, [0], 1, 10 ** 9, aggs=aggs, chunks=3)
+    # 5M rows: the sketch and learned sizing run on the packed words.
+    big = ticks_nonull(rng, 5 << 20, 3000, span=10 ** 11)
+    check_window(ctx, big, [0], 1, 10 ** 8, aggs=aggs)
+
+
+@pytest.mark.parametrize("second", ["nulls", "wide_times"])
+def test_window_packed_then_unpacked(ctx, second):
+    # The first batch packs; the second does not allow it (a NULL partition
+    # key, or bucket indexes beyond int32), so the table converts to composite
+    # rows mid-aggregation; the result must still be the oracle's.
+    rng = np.random.default_rng(21)
+    a = ticks_nonull(rng, 300000, 200)
+    b = ticks_nonull(rng, 300000, 200)
+    width = 10 ** 6
+    if second == "nulls":
+        b[0].valid = rng.random(300000) > 0.05
+    else:
+        b[1].values[::7] = np.int64(1) << 60
+    cols = [O.TCol(x.type, np.concatenate([x.values, y.values]),
+                   None if x.valid is None and y.valid is None else
+                   np.concatenate([np.ones(x.n, bool) if x.valid is None else x.valid,
+                                   np.ones(y.n, bool) if y.valid is None else y.valid])) for x, y in zip(a, b)]
+    aggs = [(O.COUNT_STAR, 0), (O.SUM, 3), (O.MIN, 2), (O.MAX, 2)]
+    w = qeg.Window(ctx, [c.type for c in cols], [0], 1, width, aggs)
+    try:
+        for part in (a, b):
+            w.consume([to_gpu(c) for c in part])
+        w.finish()
+        gt, grows = gpu_rows(w.fetch(), w.result_types)
+    finally:
+        w.close()
+    ot, orows = O.window_tumbling(cols, [0], 1, width, aggs)
+    assert_same(gt, grows, ot, orows, second)
+
+
+def test_window_unpackable_from_the_start(ctx):
+    # Bucket indexes beyond int32 (width 1 on 2^40-scale times): composite keys.
+    rng = np.random.default_rng(22)
+    cols = ticks_nonull(rng, 200000, 100, t0=1 << 40, span=1 << 20)
+    check_window(ctx, cols, [0], 1, 1, aggs=[(O.COUNT_STAR, 0), (O.SUM, 3)])
