@@ -1125,6 +1125,10 @@ bool AggState::can_pack(const std::vector<StagedCol>& staged, uint64_t len) {
   QEG_CUDA(cudaMemcpyAsync(r, mm.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
   QEG_CUDA(cudaStreamSynchronize(ctx->stream));
   const int64_t qmin = dec_i64(r[0]) / bucket_width, qmax = dec_i64(r[1]) / bucket_width;
+  if (!table.get()) {
+    pack_qmin = qmin;
+    pack_qmax = qmax;
+  }
   return qmin >= INT32_MIN && qmax <= INT32_MAX;
 }
 

@@ -136,6 +136,7 @@ struct AggState {
   // NULLs in either column, bucket indexes within int32); a batch that does
   // not converts the table to composite rows.
   bool packable = false, packed = false;
+  int64_t pack_qmin = 0, pack_qmax = 0;  // bucket-index range of the first packed batch
 
   bool finished = false;
   uint64_t nout = 0;

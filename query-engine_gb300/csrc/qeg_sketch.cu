@@ -608,6 +608,18 @@ double AggState::estimate_groups(const std::vector<StagedCol>& staged, uint64_t 
   }
   SketchResult s;
   const int want_heavy = (cfg.hot_keys > 0) ? 4096 : 0;
+  if (packed) {
+    // A packed window's (partition key, bucket) words are clustered by time,
+    // which a strided sample cannot extrapolate: estimate the partition key's
+    // distinct count instead and multiply by the buckets the time range
+    // spans (at most one group per row).
+    sketch_key_column(ctx, staged[keys[0]].dev, dsel, nrows, len, 1u << 20, 0, s);
+    double keys_est = 0, share = 0;
+    if (!learned_estimate(ctx, s, &keys_est, &share)) keys_est = classic_estimate(s);
+    hot_share = 0;
+    const double buckets = static_cast<double>(pack_qmax - pack_qmin + 1);
+    return std::max(1.0, std::min(static_cast<double>(nrows), std::max(keys_est, 1.0) * buckets));
+  }
   sketch_key_column(ctx, key_col(staged, 0), dsel, nrows, len, 1u << 20, want_heavy, s);
   double groups = 0, share = 0;
   if (learned_estimate(ctx, s, &groups, &share)) {
