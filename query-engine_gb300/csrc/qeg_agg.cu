@@ -854,7 +854,7 @@ __global__ void __launch_bounds__(1024) finalize_kernel(const AggK P, const FinK
         w = (s == P.cap) ? 0 : r[0];
         if (F.packed_width > 0) {  // (partition key, bucket index) packed in one word
           isnull = false;
-          w = j == 0 ? static_cast<uint64_t>(static_cast<uint32_t>(w >> 32))
+          w = j == 0 ? static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(w >> 32))))
                      : static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(w))) *
                                              F.packed_width);
         }
@@ -1026,6 +1026,7 @@ DevCol AggState::key_col(const std::vector<StagedCol>& staged, size_t j) const {
   DevCol c = staged[keys[j]].dev;
   c.bucket = (bucket_width > 0 && j + 1 == keys.size()) ? bucket_width : 0;
   if (packed && j == 0) {
+    c.type1 = c.type;
     c.type = kPackedKey;
     c.all_valid = 1;
     c.validity = nullptr;
@@ -1072,7 +1073,7 @@ __global__ void int_range_kernel(DevCol c, uint64_t n, unsigned long long* out) 
 // the key-0 side row) is decoded into (partition key, bucket start) key words
 // and inserted into the new composite table with its fields.
 __global__ void unpack_kernel(const AggK P, const uint64_t* __restrict__ old, uint64_t old_cap, int old_w,
-                              int64_t width, int32_t time_type) {
+                              int64_t width, int32_t key_type, int32_t time_type) {
   unsigned long long inserted = 0;
   const int fo = 2 + P.nkeys;
   for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < old_cap + 2;
@@ -1091,7 +1092,9 @@ __global__ void unpack_kernel(const AggK P, const uint64_t* __restrict__ old, ui
       k = 0;
     }
     uint64_t words[kMaxKeys] = {};
-    words[0] = static_cast<uint32_t>(k >> 32);
+    const int32_t a = static_cast<int32_t>(static_cast<uint32_t>(k >> 32));
+    words[0] = key_type == kI32 ? static_cast<uint64_t>(static_cast<uint32_t>(a))
+                                : static_cast<uint64_t>(static_cast<int64_t>(a));
     const int64_t b = static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(k))) * width;
     words[1] = time_type == kI32 ? static_cast<uint64_t>(static_cast<uint32_t>(static_cast<int32_t>(b)))
                                  : static_cast<uint64_t>(b);
@@ -1108,22 +1111,29 @@ __global__ void unpack_kernel(const AggK P, const uint64_t* __restrict__ old, ui
 }  // namespace
 
 // The batch can keep (or start) the packed key: both key columns without
-// NULLs and every bucket index of the time column within int32.
+// NULLs, the key's values (an I64/TS key) and every bucket index of the time
+// column within int32.
 bool AggState::can_pack(const std::vector<StagedCol>& staged, uint64_t len) {
   if (!packable || staged.empty()) return false;
   const DevCol& a = staged[keys[0]].dev;
   const DevCol& t = staged[keys[1]].dev;
   if (!a.all_valid || !t.all_valid) return false;
   if (len == 0) return true;
-  DevBuf mm(16, ctx->stream);
-  const unsigned long long init[2] = {~0ull, 0ull};
-  QEG_CUDA(cudaMemcpyAsync(mm.get(), init, 16, cudaMemcpyHostToDevice, ctx->stream));
+  const bool wide_key = a.type != kI32;
+  DevBuf mm(32, ctx->stream);
+  const unsigned long long init[4] = {~0ull, 0ull, ~0ull, 0ull};
+  QEG_CUDA(cudaMemcpyAsync(mm.get(), init, 32, cudaMemcpyHostToDevice, ctx->stream));
   int_range_kernel<<<grid_for(ctx, len, 256, 4), 256, 0, ctx->stream>>>(t, len, mm.get<unsigned long long>());
   ctx->launches++;
+  if (wide_key) {
+    int_range_kernel<<<grid_for(ctx, len, 256, 4), 256, 0, ctx->stream>>>(a, len, mm.get<unsigned long long>() + 2);
+    ctx->launches++;
+  }
   QEG_CUDA(cudaGetLastError());
-  unsigned long long r[2];
-  QEG_CUDA(cudaMemcpyAsync(r, mm.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
+  unsigned long long r[4];
+  QEG_CUDA(cudaMemcpyAsync(r, mm.get(), 32, cudaMemcpyDeviceToHost, ctx->stream));
   QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (wide_key && (dec_i64(r[2]) < INT32_MIN || dec_i64(r[3]) > INT32_MAX)) return false;
   const int64_t qmin = dec_i64(r[0]) / bucket_width, qmax = dec_i64(r[1]) / bucket_width;
   if (!table.get()) {
     pack_qmin = qmin;
@@ -1151,7 +1161,8 @@ void AggState::unpack() {
   QEG_CUDA(cudaMemsetAsync(counters.get<uint8_t>() + 16, 0, 8, ctx->stream));
   AggK P = kparams_base();
   const unsigned g = grid_for(ctx, old_cap + 2, 256, 8);
-  unpack_kernel<<<g, 256, 0, ctx->stream>>>(P, old.get<uint64_t>(), old_cap, old_w, bucket_width, types[keys[1]]);
+  unpack_kernel<<<g, 256, 0, ctx->stream>>>(P, old.get<uint64_t>(), old_cap, old_w, bucket_width, types[keys[0]],
+                                            types[keys[1]]);
   ctx->launches++;
   QEG_CUDA(cudaGetLastError());
   uint64_t c[3];
@@ -1657,7 +1668,8 @@ qeg_status qeg_window_create(qeg_ctx* ctx, const int32_t* col_types, int ncols, 
                  "block_threads must be 0 or a multiple of 32 in [32, 1024]");
     a->st.plan(col_types, ncols, k.data(), nkeys + 1, aggs, naggs);
     a->st.bucket_width = width;
-    a->st.packable = nkeys == 1 && col_types[key_cols[0]] == QEG_I32;
+    const int32_t kt = nkeys == 1 ? col_types[key_cols[0]] : -1;
+    a->st.packable = kt == QEG_I32 || kt == QEG_I64 || kt == QEG_TS;
     *out = a.release();
   });
 }

@@ -37,12 +37,13 @@ struct DevCol {
   // edge of the value's bucket, (v / bucket) * bucket with C++ truncating
   // division, in the column's own type (tsx/window.cpp:318-330).
   int64_t bucket;
-  // kPackedKey: `data` is the I32 partition key, `data2` the time column of
-  // type `type2`; the key word is (partition key << 32) | (t / bucket) as a
-  // 32-bit index (both columns without NULLs, the index within int32).
+  // kPackedKey: `data` is the partition key (type `type1`), `data2` the time
+  // column (type `type2`); the key word is (key << 32) | (t / bucket), both
+  // halves as 32-bit integers (no NULLs, key values and bucket indexes within
+  // int32).
   const void* data2;
   int32_t type2;
-  int32_t pad_;
+  int32_t type1;
 };
 
 __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
@@ -83,7 +84,8 @@ __device__ __forceinline__ uint64_t key_word(const DevCol& c, uint64_t p) {
     }
     case kBOOL: return __ldg(static_cast<const uint8_t*>(c.data) + p);
     case kPackedKey: {
-      const int32_t a = __ldg(static_cast<const int32_t*>(c.data) + p);
+      const int32_t a = c.type1 == kI32 ? __ldg(static_cast<const int32_t*>(c.data) + p)
+                                        : static_cast<int32_t>(__ldg(static_cast<const long long*>(c.data) + p));
       const long long t = c.type2 == kI32 ? static_cast<long long>(__ldg(static_cast<const int32_t*>(c.data2) + p))
                                           : __ldg(static_cast<const long long*>(c.data2) + p);
       const long long q = t / c.bucket;

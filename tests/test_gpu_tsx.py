@@ -319,3 +319,13 @@ def test_window_unpackable_from_the_start(ctx):
     rng = np.random.default_rng(22)
     cols = ticks_nonull(rng, 200000, 100, t0=1 << 40, span=1 << 20)
     check_window(ctx, cols, [0], 1, 1, aggs=[(O.COUNT_STAR, 0), (O.SUM, 3)])
+
+
+@pytest.mark.parametrize("shift", [0, 40])
+def test_window_packed_i64_partition_keys(ctx, shift):
+    # I64 partition keys: packed when their values fit in int32 (shift 0,
+    # including negative keys), composite keys otherwise (shift 40).
+    rng = np.random.default_rng(23 + shift)
+    cols = ticks_nonull(rng, 500000, 300)
+    cols[0] = O.TCol(O.I64, (cols[0].values.astype(np.int64) - 150) << shift)
+    check_window(ctx, cols, [0], 1, 10 ** 9, aggs=[(O.COUNT_STAR, 0), (O.SUM, 3), (O.MIN, 2), (O.MAX, 2)])
