@@ -1433,8 +1433,14 @@ __global__ void __launch_bounds__(256) gather_cols_kernel(const GatherK P) {
 
 // Appends a batch column into the build store: values are copied, validity is
 // expanded to a byte per row; STR codes are translated to value ids.
+// RANGE (the single integer key of a build): the same pass also folds the
+// key's smallest and largest value and its non-NULL count into range[0..2]
+// (order-preserving encodings; one set of atomics per CTA), so the dense /
+// hash decision needs no separate pass over the key.
+template <bool RANGE>
 __global__ void store_append_kernel(DevCol c, uint64_t n, int width, void* __restrict__ dst,
-                                    uint8_t* __restrict__ dvalid) {
+                                    uint8_t* __restrict__ dvalid, unsigned long long* __restrict__ range) {
+  unsigned long long mn = ~0ull, mx = 0, cnt = 0;
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
     const bool ok = col_valid(c, r);
     dvalid[r] = ok ? 1 : 0;
@@ -1446,6 +1452,38 @@ __global__ void store_append_kernel(DevCol c, uint64_t n, int width, void* __res
       static_cast<uint32_t*>(dst)[r] = __ldg(static_cast<const unsigned int*>(c.data) + r);
     } else {
       static_cast<uint8_t*>(dst)[r] = __ldg(static_cast<const uint8_t*>(c.data) + r);
+    }
+    if (RANGE && ok) {
+      const unsigned long long e = enc_i64(int_value(c, r));
+      mn = e < mn ? e : mn;
+      mx = e > mx ? e : mx;
+      ++cnt;
+    }
+  }
+  if (!RANGE) return;
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = min(mn, __shfl_down_sync(0xffffffffu, mn, o));
+    mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  }
+  __shared__ unsigned long long smn[32], smx[32], scn[32];
+  const unsigned warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    smn[warp] = mn;
+    smx[warp] = mx;
+    scn[warp] = cnt;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (unsigned w = 1; w < nwarps; ++w) {
+      mn = min(mn, smn[w]);
+      mx = max(mx, smx[w]);
+      cnt += scn[w];
+    }
+    if (cnt) {
+      atomicMin(range + 0, mn);
+      atomicMax(range + 1, mx);
+      atomicAdd(range + 2, cnt);
     }
   }
 }
@@ -1500,6 +1538,7 @@ struct JoinState {
   int64_t tmin = 0;
   uint32_t aslots = 0;
   DevBuf ats, arow, aruns, asamp, tbits, amatch;
+  DevBuf krange;  // single integer key: [min enc, max enc, non-NULL count] over the appended batches
   void asof_build();
   void asof_probe(uint64_t n);
 
@@ -1548,13 +1587,24 @@ struct JoinState {
       bcap = ncap;
     }
     bool host_input = false;
+    const int range_col = (bkeys.size() == 1 && dense_capable(btypes[bkeys[0]])) ? static_cast<int>(bkeys[0]) : -1;
+    if (range_col >= 0 && !krange.get()) {
+      krange.alloc(24, ctx->stream);  // {min = ~0, max = 0, count = 0}
+      QEG_CUDA(cudaMemsetAsync(krange.get(), 0xff, 8, ctx->stream));
+      QEG_CUDA(cudaMemsetAsync(krange.get<uint8_t>() + 8, 0, 16, ctx->stream));
+    }
     for (int c = 0; c < ncols; ++c) {
       StagedCol s;
       stage_column(ctx, cols[c], s);
       host_input = host_input || s.data.get() || s.validity.get() || s.code_map.get();
       const int w = static_cast<int>(type_width(btypes[c]));
-      store_append_kernel<<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(
-          s.dev, n, w, bvals[c].get<uint8_t>() + nbuild * w, bvalid[c].get<uint8_t>() + nbuild);
+      if (c == range_col)
+        store_append_kernel<true><<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(
+            s.dev, n, w, bvals[c].get<uint8_t>() + nbuild * w, bvalid[c].get<uint8_t>() + nbuild,
+            krange.get<unsigned long long>());
+      else
+        store_append_kernel<false><<<grid_for(ctx, n, 256, 8), 256, 0, ctx->stream>>>(
+            s.dev, n, w, bvals[c].get<uint8_t>() + nbuild * w, bvalid[c].get<uint8_t>() + nbuild, nullptr);
       ctx->launches++;
       QEG_CUDA(cudaGetLastError());
     }
@@ -1641,13 +1691,9 @@ void JoinState::finish_build() {
   nonnull = nbuild;
   if (nk == 1 && dense_capable(btypes[bkeys[0]]) && nbuild > 0 &&
       (cfg.strategy == QEG_JOIN_AUTO || cfg.strategy == QEG_JOIN_DENSE)) {
-    DevBuf mm(24, ctx->stream);
-    unsigned long long init[3] = {~0ull, 0ull, 0ull};
-    QEG_CUDA(cudaMemcpyAsync(mm.get(), init, 24, cudaMemcpyHostToDevice, ctx->stream));
-    minmax_kernel<<<grid_for(ctx, nbuild, 256, 8), 256, 0, ctx->stream>>>(P.key[0], nbuild, mm.get<unsigned long long>());
-    ctx->launches++;
+    // The key's range was folded in while the batches were appended.
     unsigned long long r[3];
-    QEG_CUDA(cudaMemcpyAsync(r, mm.get(), 24, cudaMemcpyDeviceToHost, ctx->stream));
+    QEG_CUDA(cudaMemcpyAsync(r, krange.get(), 24, cudaMemcpyDeviceToHost, ctx->stream));
     QEG_CUDA(cudaStreamSynchronize(ctx->stream));
     nonnull = r[2];
     if (r[2] > 0) {
