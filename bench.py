@@ -327,7 +327,8 @@ def run_agg_bench(args, dev, local):
         "metric": "rows/s hash aggregate (%s)" % W.name, "value": best["rows_per_s"], "unit": "rows/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["ms_per_step"],
         "higher_is_better": True, "dtype": "int64+f64", "data": "synthetic (seeded, generated on the GPU)",
-        "config": {"workload": W.name, "rows": W.n, "groups": W.groups, "full_size_check": check},
+        "config": {"workload": W.name, "rows": W.n, "groups": W.groups, "seed": SEED + 3, "M": "2^20",
+                   "full_size_check": check},
         "roofline": {"bound": "hbm", "achieved": best["gb_per_s"], "peak": peak, "peak_kind": kind,
                      "unit": "GB/s", "frac": best["gb_per_s"] / peak},
         "variants": out,
@@ -503,7 +504,7 @@ def run_pipeline_bench(args, dev, local):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
         "data": "synthetic (seeded, generated on the GPU); inputs 3.2 GB > L2",
-        "config": {"workload": W.name, "rows": W.n, "groups": ngroups},
+        "config": {"workload": W.name, "rows": W.n, "groups": ngroups, "seed": SEED + 5},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                      "peak_kind": kind, "note": "whole call (translation tables, kernel, result copy)"},
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
@@ -642,7 +643,8 @@ def run_window_bench(args, dev, local):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+int64+f64",
         "data": "synthetic (seeded, generated on the GPU); inputs %.1f GB > L2" % (W.n * W.trade_bytes / 1e9),
-        "config": {"workload": name, "rows": W.n, "groups": ng, "width_ns": WINDOW_NS, "stats": stats},
+        "config": {"workload": name, "rows": W.n, "groups": ng, "width_ns": WINDOW_NS, "stats": stats,
+                   "seed": SEED + 7},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                      "peak_kind": kind, "note": "24 B per trade row read once; whole call"},
         "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks,
@@ -740,6 +742,7 @@ def run_asof_bench(args, dev, local):
         "data": "synthetic (seeded, generated on the GPU); inputs %.1f GB > L2"
                 % ((W.n * W.trade_bytes + W.m * W.quote_bytes) / 1e9),
         "config": {"workload": name, "trades": W.n, "quotes": W.m, "matched": matched, "phases": phases,
+                   "seed": SEED + 7,
                    "output": "all 8 columns gathered into HBM buffers"},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                      "peak_kind": kind,
@@ -831,7 +834,8 @@ def run_batch_bench(args, dev, local):
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
         "data": "synthetic (seeded, generated on the GPU); inputs %.1f GB > L2" % (W.n * W.row_bytes / 1e9),
-        "config": {"workload": W.name, "queries": len(groups), "rows": W.n, "tuning": tpath,
+        "config": {"workload": W.name, "queries": len(groups), "rows": W.n, "seed": SEED + 4,
+                   "tuning": os.path.relpath(tpath, REPO) if tpath else None,
                    "block_threads": block or 512},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                      "peak_kind": kind, "note": "graph replay (aggregate + finalize) time"},
@@ -1047,7 +1051,8 @@ def main():
             "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int64", "data": "synthetic (seeded, generated on the GPU)",
-            "config": {"workload": W.name, "build_rows": W.nbuild, "probe_rows": W.nprobe,
+            "config": {"workload": W.name, "build_rows": W.nbuild, "probe_rows": W.nprobe, "seed": SEED + 2,
+                       "M": "2^20",
                        "null_keys": "2% both sides", "probe_hit_rate": 0.5, "strategy": strategy_name,
                        "l2": "inputs exceed L2 (4.3 GB probe side), no flush", "parallelism": "replicas"
                        if world > 1 else "single GPU", "result": {"count": res[0], "sum": res[1]}},
