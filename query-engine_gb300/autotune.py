@@ -28,7 +28,7 @@ import torch  # noqa: E402
 import qeg  # noqa: E402
 
 BUCKETS = [2.0, 6.0, 10.0, 14.0, 17.0, 20.0]  # upper bounds on log2(groups)
-SLOTS = [0, 256, 1024, 4096]
+SLOTS = [0, 256, 1024, 2048, 4096]
 ITEMS = [1 << 13, 1 << 14, 1 << 16]
 PEER = [0, 1]
 BLOCKS = [256, 512, 1024]
