@@ -813,18 +813,28 @@ __global__ void __launch_bounds__(1024) finalize_kernel(const AggK P, const FinK
   // prefixed in shared memory), not one per warp -- a sparse table of tens of
   // millions of slots would otherwise serialise on the counter.
   __shared__ unsigned long long wpos[32];
-  for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x; base < total; base += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t s = base + threadIdx.x;
-    bool occ = false;
-    const uint64_t* r = nullptr;
-    if (s < total) {
-      r = P.table + s * W;
-      if (MODE == 0) occ = true;
-      else if (MODE == 1) occ = (s < P.cap) ? (r[0] != 0) : (r[1] != 0);
-      else occ = r[0] >= 2;
+  // kFinPer slots per thread and pass: fewer passes, so fewer barriers.
+  constexpr int kFinPer = 4;
+  const uint64_t span = static_cast<uint64_t>(blockDim.x) * kFinPer;
+  for (uint64_t base = blockIdx.x * span; base < total; base += gridDim.x * span) {
+    bool occk[kFinPer];
+    unsigned mk[kFinPer];
+    unsigned cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kFinPer; ++k) {
+      const uint64_t sk = base + static_cast<uint64_t>(k) * blockDim.x + threadIdx.x;
+      bool o = false;
+      if (sk < total) {
+        const uint64_t* rk = P.table + sk * W;
+        if (MODE == 0) o = true;
+        else if (MODE == 1) o = (sk < P.cap) ? (rk[0] != 0) : (rk[1] != 0);
+        else o = rk[0] >= 2;
+      }
+      occk[k] = o;
+      mk[k] = __ballot_sync(0xffffffffu, o);
+      cnt += __popc(mk[k]);
     }
-    const unsigned m = __ballot_sync(0xffffffffu, occ);
-    if (lane == 0) wpos[warp] = __popc(m);
+    if (lane == 0) wpos[warp] = cnt;
     __syncthreads();
     if (threadIdx.x == 0) {
       unsigned long long run = 0;
@@ -837,78 +847,85 @@ __global__ void __launch_bounds__(1024) finalize_kernel(const AggK P, const FinK
       for (int w = 0; w < nwarps; ++w) wpos[w] += b;
     }
     __syncthreads();
-    const unsigned long long wbase = wpos[warp];
+    unsigned long long wbase = wpos[warp];
     __syncthreads();  // wpos is rewritten by the next pass
-    if (!occ) continue;
-    const uint64_t o = wbase + __popc(m & ((1u << lane) - 1u));
-    if (o >= F.out_cap) {
-      atomicOr(P.err, kDevSpillOverflow);
-      continue;
-    }
-    // keys
-    for (int j = 0; j < P.nkeys; ++j) {
-      bool isnull;
-      uint64_t w;
-      if (MODE == 1) {
-        isnull = (s == P.cap + 1);
-        w = (s == P.cap) ? 0 : r[0];
-        if (F.packed_width > 0) {  // (partition key, bucket index) packed in one word
-          isnull = false;
-          w = j == 0 ? static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(w >> 32))))
-                     : static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(w))) *
-                                             F.packed_width);
-        }
-      } else {
-        isnull = (r[1] >> j) & 1ull;
-        w = r[2 + j];
+    for (int k = 0; k < kFinPer; ++k) {
+      const unsigned m = mk[k];
+      const unsigned long long kbase = wbase;
+      wbase += __popc(m);
+      if (!occk[k]) continue;
+      const uint64_t s = base + static_cast<uint64_t>(k) * blockDim.x + threadIdx.x;
+      const uint64_t* r = P.table + s * W;
+      const uint64_t o = kbase + __popc(m & ((1u << lane) - 1u));
+      if (o >= F.out_cap) {
+        atomicOr(P.err, kDevSpillOverflow);
+        continue;
       }
-      F.valid[j][o] = isnull ? 0 : 1;
-      store_typed(F.vals[j], o, F.rtype[j], isnull ? 0 : w);
-    }
-    // aggregates
-    const uint64_t* f = r + fo;
-    const uint64_t rows = f[0];
-    for (int a = 0; a < F.naggs; ++a) {
-      const int oc = P.nkeys + a;
-      const int vf = F.vfield[a];
-      const uint64_t nulls = F.nfield[a] >= 0 ? f[F.nfield[a]] : 0;
-      const uint64_t nn = rows - nulls;
-      const int32_t rt = F.rtype[oc];
-      uint8_t ok = 1;
-      uint64_t w = 0;
-      switch (F.func[a]) {
-        case 0: w = rows; break;  // COUNT(*)
-        case 1: w = nn; break;    // COUNT(col)
-        case 2:                   // SUM
-          if (nn == 0) ok = 0;
-          else w = f[vf];
-          break;
-        case 5: {  // AVG = sum / non-null count, in double (ops/agg_internal.h:217-227)
-          if (nn == 0) {
-            ok = 0;
-          } else {
-            const double sum = (P.fkind[vf] == F_SUMF) ? __longlong_as_double(static_cast<long long>(f[vf]))
-                                                        : static_cast<double>(static_cast<int64_t>(f[vf]));
-            w = static_cast<uint64_t>(__double_as_longlong(sum / static_cast<double>(nn)));
+      // keys
+      for (int j = 0; j < P.nkeys; ++j) {
+        bool isnull;
+        uint64_t w;
+        if (MODE == 1) {
+          isnull = (s == P.cap + 1);
+          w = (s == P.cap) ? 0 : r[0];
+          if (F.packed_width > 0) {  // (partition key, bucket index) packed in one word
+            isnull = false;
+            w = j == 0 ? static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(w >> 32))))
+                       : static_cast<uint64_t>(static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(w))) *
+                                               F.packed_width);
           }
-          break;
+        } else {
+          isnull = (r[1] >> j) & 1ull;
+          w = r[2 + j];
         }
-        default: {  // MIN / MAX
-          if (nn == 0) {
-            ok = 0;
+        F.valid[j][o] = isnull ? 0 : 1;
+        store_typed(F.vals[j], o, F.rtype[j], isnull ? 0 : w);
+      }
+      // aggregates
+      const uint64_t* f = r + fo;
+      const uint64_t rows = f[0];
+      for (int a = 0; a < F.naggs; ++a) {
+        const int oc = P.nkeys + a;
+        const int vf = F.vfield[a];
+        const uint64_t nulls = F.nfield[a] >= 0 ? f[F.nfield[a]] : 0;
+        const uint64_t nn = rows - nulls;
+        const int32_t rt = F.rtype[oc];
+        uint8_t ok = 1;
+        uint64_t w = 0;
+        switch (F.func[a]) {
+          case 0: w = rows; break;  // COUNT(*)
+          case 1: w = nn; break;    // COUNT(col)
+          case 2:                   // SUM
+            if (nn == 0) ok = 0;
+            else w = f[vf];
+            break;
+          case 5: {  // AVG = sum / non-null count, in double (ops/agg_internal.h:217-227)
+            if (nn == 0) {
+              ok = 0;
+            } else {
+              const double sum = (P.fkind[vf] == F_SUMF) ? __longlong_as_double(static_cast<long long>(f[vf]))
+                                                          : static_cast<double>(static_cast<int64_t>(f[vf]));
+              w = static_cast<uint64_t>(__double_as_longlong(sum / static_cast<double>(nn)));
+            }
             break;
           }
-          const uint8_t k = P.fkind[vf];
-          const uint64_t e = f[vf];
-          if (k == F_MINF) w = dec_f64_bits(~e);
-          else if (k == F_MAXF) w = dec_f64_bits(e);
-          else if (k == F_MINI) w = static_cast<uint64_t>(dec_i64(~e));
-          else w = static_cast<uint64_t>(dec_i64(e));
-          break;
+          default: {  // MIN / MAX
+            if (nn == 0) {
+              ok = 0;
+              break;
+            }
+            const uint8_t fk = P.fkind[vf];
+            const uint64_t e = f[vf];
+            if (fk == F_MINF) w = dec_f64_bits(~e);
+            else if (fk == F_MAXF) w = dec_f64_bits(e);
+            else if (fk == F_MINI) w = static_cast<uint64_t>(dec_i64(~e));
+            else w = static_cast<uint64_t>(dec_i64(e));
+            break;
+          }
         }
+        F.valid[oc][o] = ok;
+        store_typed(F.vals[oc], o, rt, ok ? w : 0);
       }
-      F.valid[oc][o] = ok;
-      store_typed(F.vals[oc], o, rt, ok ? w : 0);
     }
   }
 }
