@@ -20,6 +20,7 @@
 // the probe limit are spilled (row index) and re-run after the host grows the
 // table (rehash) -- the GPU form of HashTable::grow (ops/hashtable.cpp:75-91).
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 
 #include "qeg_agg.h"
@@ -1210,7 +1211,15 @@ AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel
   P.len = len;
   P.smem_slots = smem_slots;
   P.smem_insert = smem_insert;
-  P.smem_probe = 8;
+  // Private-table slots a lookup probes before it takes the global table
+  // (QEG_AGG_SMEM_PROBE overrides).
+  {
+    static const int probe = [] {
+      const char* e = std::getenv("QEG_AGG_SMEM_PROBE");
+      return e ? std::max(1, std::min(64, std::atoi(e))) : 8;
+    }();
+    P.smem_probe = probe;
+  }
   P.hot = hot_keys_dev.get<uint64_t>();
   P.nhot = nhot;
   P.warp_hot = warp_hot();
