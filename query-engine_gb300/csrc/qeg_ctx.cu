@@ -170,6 +170,10 @@ void qeg_ctx_destroy(qeg_ctx* ctx) {
   ctx->mlp.reset();
   cudaStreamSynchronize(ctx->stream);
   cudaStreamDestroy(ctx->stream);
+  if (ctx->side) {
+    cudaStreamSynchronize(ctx->side);
+    cudaStreamDestroy(ctx->side);
+  }
   delete ctx;
 }
 

@@ -108,6 +108,7 @@ struct qeg_ctx {
   std::string err;
   uint64_t launches = 0;
   qeg::DevBuf dev_err;  // uint32 device error word (qeg::DevError bits)
+  cudaStream_t side = nullptr;  // copies that overlap the context stream's kernels (created on first use)
   std::shared_ptr<qeg::Mlp> mlp;  // the learned estimator, when weights are loaded
 };
 

@@ -1380,6 +1380,7 @@ struct GatherCol {
   uint64_t* words;
   int width;
   int side;  // 0 probe, 1 build
+  int flag;  // index of the column's NULL flag
 };
 
 struct GatherK {
@@ -1433,10 +1434,27 @@ __global__ void __launch_bounds__(256) gather_cols_kernel(const GatherK P) {
       if (lane == 0) {
         const uint64_t word = static_cast<uint64_t>(b0) | (static_cast<uint64_t>(b1) << 32);
         if (col.words) col.words[w] = word;
-        if (word != ~0ull) atomicOr(P.flags + c, 1u);
+        if (word != ~0ull) atomicOr(P.flags + col.flag, 1u);
       }
     }
   }
+}
+
+// Validity words copied from an aligned source range: padding bits of the
+// last word set, and the column's NULL flag raised when any bit is clear.
+__global__ void words_finish_kernel(uint64_t* __restrict__ words, uint64_t nw, uint64_t count,
+                                    unsigned int* __restrict__ flag) {
+  bool null_seen = false;
+  const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < nw; i += step) {
+    uint64_t w = words[i];
+    if (i + 1 == nw && (count & 63)) {
+      w |= ~0ull << (count & 63);
+      words[i] = w;
+    }
+    null_seen |= w != ~0ull;
+  }
+  if (__any_sync(0xffffffffu, null_seen) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
 }
 
 // Appends a batch column into the build store: values are copied, validity is
@@ -1540,6 +1558,7 @@ struct JoinState {
   // as-of join (qeg_asof_create): time columns, tolerance, and the build side
   // sorted by (partition slot, timestamp)
   bool asof = false;
+  bool probe_identity = false;  // output row k of the last probe is probe row k (LEFT as-of)
   uint32_t ptime = 0, btime = 0;
   int32_t tol_set = 0;
   int64_t tol = 0;
@@ -2034,6 +2053,7 @@ void JoinState::asof_probe(uint64_t n) {
     QEG_CUDA(cudaGetLastError());
     check_device_error(ctx);
     nout = n;
+    probe_identity = true;
     return;
   }
   amatch.alloc(n * 4, ctx->stream);
@@ -2178,6 +2198,7 @@ qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64
     require(n < 0xffffffffull, "a probe batch holds at most 2^32-2 rows");
     st.probe_staged.clear();
     st.probe_staged.resize(ncols);
+    st.probe_identity = false;
     for (int c = 0; c < ncols; ++c) stage_column(ctx, cols[c], st.probe_staged[c]);
     st.nout = 0;
     if (n == 0) {
@@ -2235,17 +2256,58 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
       DevBuf flags(ncol * 4, ctx->stream);
       QEG_CUDA(cudaMemsetAsync(flags.get(), 0, ncol * 4, ctx->stream));
       const unsigned gw = grid_for(ctx, (count + 63) / 64 * 32, 256, 8);
+      // Output row k = probe row first + k (LEFT as-of) with a word-aligned
+      // start: probe columns are plain copies, made by the copy engines on a
+      // side stream while the gather kernel fills the build columns.
+      std::vector<char> copied(ncol, 0);
+      cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+      DevBuf tmp_words;
+      if (st.probe_identity && first % 64 == 0) {
+        const uint64_t nw = (count + 63) / 64;
+        auto copyable = [&](size_t c) { return !(st.ptypes[c] == QEG_STR && st.probe_staged[c].dev.code_map); };
+        size_t ntmp = 0;  // copied columns with NULLs but no validity output: words still needed for the flag
+        for (size_t c = 0; c < st.ptypes.size(); ++c)
+          ntmp += copyable(c) && !st.probe_staged[c].dev.all_valid && !outs[c].validity;
+        if (ntmp) tmp_words.alloc(ntmp * nw * 8, ctx->stream);  // before ev_in: ordered ahead of the side stream
+        if (!ctx->side) QEG_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        QEG_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
+        QEG_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
+        QEG_CUDA(cudaEventRecord(ev_in, ctx->stream));
+        QEG_CUDA(cudaStreamWaitEvent(ctx->side, ev_in, 0));
+        size_t itmp = 0;
+        for (size_t c = 0; c < st.ptypes.size(); ++c) {
+          if (!copyable(c)) continue;  // dictionary codes need translating: gathered below
+          const StagedCol& sc = st.probe_staged[c];
+          const size_t w = type_width(st.ptypes[c]);
+          QEG_CUDA(cudaMemcpyAsync(outs[c].data, static_cast<const uint8_t*>(sc.dev.data) + first * w, count * w,
+                                   cudaMemcpyDeviceToDevice, ctx->side));
+          if (sc.dev.all_valid) {
+            if (outs[c].validity) QEG_CUDA(cudaMemsetAsync(outs[c].validity, 0xff, nw * 8, ctx->side));
+          } else {
+            uint64_t* words = outs[c].validity ? outs[c].validity : tmp_words.get<uint64_t>() + nw * itmp++;
+            QEG_CUDA(cudaMemcpyAsync(words, sc.dev.validity + first / 64, nw * 8, cudaMemcpyDeviceToDevice,
+                                     ctx->side));
+            words_finish_kernel<<<grid_for(ctx, nw, 256, 4), 256, 0, ctx->side>>>(words, nw, count,
+                                                                                 flags.get<unsigned int>() + c);
+            ctx->launches++;
+            QEG_CUDA(cudaGetLastError());
+          }
+          copied[c] = 1;
+        }
+        QEG_CUDA(cudaEventRecord(ev_out, ctx->side));
+      }
       if (ncol <= static_cast<size_t>(kMaxGatherCols)) {
         GatherK G{};
-        G.ncols = static_cast<int>(ncol);
         G.idx[0] = st.out_probe.get<uint32_t>() + first;
         G.idx[1] = st.out_build.get<uint32_t>() + first;
         G.n = count;
         G.flags = flags.get<unsigned int>();
         for (size_t c = 0; c < ncol; ++c) {
+          if (copied[c]) continue;
           const bool pc = c < st.ptypes.size();
           const size_t bc = pc ? 0 : c - st.ptypes.size();
-          GatherCol& g = G.c[c];
+          GatherCol& g = G.c[G.ncols++];
+          g.flag = static_cast<int>(c);
           g.width = static_cast<int>(type_width(pc ? st.ptypes[c] : st.btypes[bc]));
           g.side = pc ? 0 : 1;
           g.out = outs[c].data;
@@ -2260,9 +2322,16 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
             g.bytes = st.bvalid[bc].get<uint8_t>();
           }
         }
-        gather_cols_kernel<<<gw, 256, 0, ctx->stream>>>(G);
-        ctx->launches++;
-        QEG_CUDA(cudaGetLastError());
+        if (G.ncols > 0) {
+          gather_cols_kernel<<<gw, 256, 0, ctx->stream>>>(G);
+          ctx->launches++;
+          QEG_CUDA(cudaGetLastError());
+        }
+      }
+      if (ev_out) {
+        QEG_CUDA(cudaStreamWaitEvent(ctx->stream, ev_out, 0));
+        QEG_CUDA(cudaEventDestroy(ev_in));
+        QEG_CUDA(cudaEventDestroy(ev_out));
       }
       for (size_t c = 0; c < ncol && ncol > static_cast<size_t>(kMaxGatherCols); ++c) {
         const bool pc = c < st.ptypes.size();

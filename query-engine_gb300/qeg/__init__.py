@@ -439,10 +439,12 @@ class Join:
         _check(lib().qeg_join_fetch(self.p, first, count, outs), self.ctx.p)
         return [(v[:count], unpack_validity(w, count)) for v, w, _ in keep]
 
-    def fetch_device(self, first=0, count=None, bufs=None):
+    def fetch_device(self, first=0, count=None, bufs=None, flags=None):
         """Like fetch(), into torch CUDA tensors [(values, validity words)]:
         one gather pass per column straight into them. `bufs` (a previous
-        result, large enough) is reused when given."""
+        result, large enough) is reused when given; a validity entry of None
+        asks for no words. `flags` (a list) receives each column's all-valid
+        flag."""
         import torch
 
         if count is None:
@@ -455,9 +457,13 @@ class Join:
                      torch.empty(max(1, (count + 63) // 64), dtype=torch.int64, device="cuda")) for t in types]
             torch.cuda.synchronize()  # the library writes them on its own stream
         outs = (OutColumn * len(types))()
+        av = (ctypes.c_int32 * len(types))()
         for i, (v, w) in enumerate(bufs):
-            outs[i] = OutColumn(v.data_ptr(), w.data_ptr(), None)
+            outs[i] = OutColumn(v.data_ptr(), None if w is None else w.data_ptr(),
+                                ctypes.addressof(av) + 4 * i)
         _check(lib().qeg_join_fetch(self.p, first, count, outs), self.ctx.p)
+        if flags is not None:
+            flags[:] = [bool(x) for x in av]
         return bufs
 
     def probe_count_sum(self, key, val):

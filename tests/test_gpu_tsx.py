@@ -329,3 +329,48 @@ def test_window_packed_i64_partition_keys(ctx, shift):
     cols = ticks_nonull(rng, 500000, 300)
     cols[0] = O.TCol(O.I64, (cols[0].values.astype(np.int64) - 150) << shift)
     check_window(ctx, cols, [0], 1, 10 ** 9, aggs=[(O.COUNT_STAR, 0), (O.SUM, 3), (O.MIN, 2), (O.MAX, 2)])
+
+
+@pytest.mark.parametrize("dev_inputs", [False, True])
+def test_asof_left_device_fetch_matches_host_fetch(ctx, dev_inputs):
+    # A LEFT as-of emits probe row k as output row k: from a word-aligned start
+    # the probe columns are plain copies on a side stream (values, validity
+    # words with the tail padded, the NULL flag), from any other start they are
+    # gathered; STR probe codes under a dictionary are always gathered.
+    import torch
+
+    rng = np.random.default_rng(22)
+    nb, npr = 50000, 200003
+    build = ticks(rng, nb, 100)
+    probe = ticks(rng, npr, 120)
+    probe.append(O.TCol(O.I64, rng.integers(0, 99, npr)))  # no NULLs
+    names = ["S%03d" % i for i in range(40)]
+    probe.append(O.TCol(O.STR, rng.integers(0, 40, npr).astype(np.int32), rng.random(npr) > 0.1,
+                        list(rng.permutation(names))))
+    canon = StrCanon(names)
+    j = qeg.AsofJoin(ctx, [c.type for c in probe], [c.type for c in build], [0], [0], 1, 1, O.LEFT, None)
+    try:
+        j.build([to_gpu(c) for c in build])
+        j.build_finish()
+        pcols = [to_gpu(c, canon, device=dev_inputs) for c in probe]  # read again by the fetches
+        n = j.probe(pcols)
+        assert n == npr
+        for first, count, words in ((0, n, True), (64, n - 64 - 5, True), (37, n - 100, True), (n - 1, 1, True),
+                                    (128, 1000, False)):
+            host = j.fetch(first, count)
+            flags = []
+            dev = j.fetch_device(first, count, flags=flags)
+            if not words:
+                dev = j.fetch_device(first, count, bufs=[(v, None) for v, _ in dev], flags=flags)
+            torch.cuda.synchronize()
+            for c, ((hv, hvalid), (dv, dw), f) in enumerate(zip(host, dev, flags)):
+                assert f == bool(np.all(hvalid)), (first, c)
+                if words:
+                    w = dw.cpu().numpy().view(np.uint64)
+                    bits = np.unpackbits(w.view(np.uint8), bitorder="little")
+                    assert np.all(bits[count:]), (first, c)  # tail padding is valid
+                    assert np.array_equal(bits[:count].astype(bool), hvalid), (first, c)
+                dvals = dv[:count].cpu().numpy()
+                assert np.array_equal(dvals[hvalid].view(np.uint8), np.asarray(hv)[hvalid].view(np.uint8)), (first, c)
+    finally:
+        j.close()
