@@ -557,9 +557,10 @@ class TickWorkload:
         return [qeg.Col(src.sym, None, qeg.I32), qeg.Col(src.ts, None, qeg.TS), qeg.Col(src.price, None, qeg.F64),
                 qeg.Col(src.qty, None, qeg.I32)]
 
-    def quotes(self, qeg):
-        return [qeg.Col(self.qsym, None, qeg.I32), qeg.Col(self.qts, None, qeg.TS), qeg.Col(self.bid, None, qeg.F64),
-                qeg.Col(self.ask, None, qeg.F64)]
+    def quotes(self, qeg, src=None):
+        src = src or self
+        return [qeg.Col(src.qsym, None, qeg.I32), qeg.Col(src.qts, None, qeg.TS), qeg.Col(src.bid, None, qeg.F64),
+                qeg.Col(src.ask, None, qeg.F64)]
 
 
 WINDOW_NS = 60 * 10 ** 9
@@ -699,6 +700,7 @@ def run_asof_bench(args, dev, local):
     clk.__exit__(None, None, None)
     ms = e0.elapsed_time(e1) / args.steps
     launches = (ctx.launches - launches0) / args.steps
+    rows = W.n + W.m
     phases = {"build_sort_ms": ev[0].elapsed_time(ev[1]), "probe_ms": ev[1].elapsed_time(ev[2]),
               "fetch_ms": ev[2].elapsed_time(ev[3])}
     # Check every output row against torch: quotes sorted stably by (sym, ts),
@@ -720,6 +722,53 @@ def run_asof_bench(args, dev, local):
     assert bool((out_ts[okp] == W.qts[cand[okp]]).all()) and bool((out_bid[okp] == W.bid[cand[okp]]).all())
     matched = int(okp.sum())
     del qkey, qsorted, qorder, tkey, pos, cand, okp, valid
+    e2e = None
+    if not args.no_e2e:
+        # Host-resident trades and quotes (page-locked), all 8 output columns
+        # back into page-locked host buffers reused across steps.
+        host = type("H", (), {})()
+        for a in ("sym", "ts", "price", "qty", "qsym", "qts", "bid", "ask"):
+            setattr(host, a, getattr(W, a).cpu().pin_memory())
+
+        def host_step(out, tm=None):
+            t = [time.perf_counter()]
+            j = qeg.AsofJoin(ctx, ptypes, btypes, [0], [0], 1, 1, qeg.LEFT)
+            j.build(W.quotes(qeg, host))
+            j.build_finish()
+            if tm is not None:
+                ctx.synchronize()
+                t.append(time.perf_counter())
+            nh = j.probe(W.trades(qeg, host))
+            if tm is not None:
+                ctx.synchronize()
+                t.append(time.perf_counter())
+            out = j.fetch_pinned(0, nh, out)
+            j.close()
+            if tm is not None:
+                t.append(time.perf_counter())
+                tm.update({k: round((t[i + 1] - t[i]) * 1e3, 2) for i, k in
+                           enumerate(("build_ms", "probe_ms", "fetch_ms"))})
+            return nh, out
+
+        nh, out = host_step(None)
+        nh, out = host_step(out)  # the memory pool has grown to the host path's staging buffers
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            nh, out = host_step(out)
+        e2e_s = (time.perf_counter() - t0) / 3
+        e2e_phases = {}
+        host_step(out, e2e_phases)  # one more, synchronised between phases
+        nw = (nh + 63) // 64
+        assert nh == W.n and torch.equal(out[5][1][:nw], bufs[0][5][1][:nw].cpu())
+        hv = ((out[5][1][:nw].view(torch.uint8).unsqueeze(1) >> torch.arange(8, dtype=torch.uint8)) & 1)
+        hv = hv.flatten()[:nh].bool()
+        assert torch.equal(out[5][0][:nh][hv], bufs[0][5][0][:n].cpu()[hv]), "host fetch differs from device fetch"
+        e2e = {"value": rows / e2e_s, "unit": "rows/s",
+               "h2d_bytes_per_step": W.n * W.trade_bytes + W.m * W.quote_bytes,
+               "d2h_bytes_per_step": int(sum(nh * v.element_size() + (nh + 63) // 64 * 8 for v, _ in out)),
+               "phases": e2e_phases}
+        del host, out
     cpu = None
     if not args.no_cpu:
         k, kq = 1 << 22, 1 << 20
@@ -733,7 +782,6 @@ def run_asof_bench(args, dev, local):
         cpu = {"value": (k + kq) / dt, "unit": "rows/s", "cores": 1, "kind": "port",
                "sample": "first %d trades x first %d quotes (the same time prefix, %.1f s); the AsofJoin "
                          "operator is single-threaded" % (k, kq, dt)}
-    rows = W.n + W.m
     alg = W.n * W.trade_bytes + W.m * W.quote_bytes + W.n * (W.trade_bytes + W.quote_bytes + 8 / 8)
     gbs = alg / (ms / 1e3) / 1e9
     peak, kind = peaks()
@@ -749,7 +797,7 @@ def run_asof_bench(args, dev, local):
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                      "peak_kind": kind,
                      "note": "inputs read once + output (52 B/row + validity) written once; whole step"},
-        "e2e": None, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks,
+        "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks,
     }))
 
 

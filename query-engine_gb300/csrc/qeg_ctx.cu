@@ -173,6 +173,8 @@ void qeg_ctx_destroy(qeg_ctx* ctx) {
   if (ctx->side) {
     cudaStreamSynchronize(ctx->side);
     cudaStreamDestroy(ctx->side);
+    cudaEventDestroy(ctx->side_in);
+    cudaEventDestroy(ctx->side_out);
   }
   delete ctx;
 }

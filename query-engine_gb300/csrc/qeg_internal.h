@@ -109,6 +109,7 @@ struct qeg_ctx {
   uint64_t launches = 0;
   qeg::DevBuf dev_err;  // uint32 device error word (qeg::DevError bits)
   cudaStream_t side = nullptr;  // copies that overlap the context stream's kernels (created on first use)
+  cudaEvent_t side_in = nullptr, side_out = nullptr;  // fork / join of the side stream
   std::shared_ptr<qeg::Mlp> mlp;  // the learned estimator, when weights are loaded
 };
 

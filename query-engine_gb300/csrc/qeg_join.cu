@@ -2251,6 +2251,25 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
     for (size_t c = 0; c < ncol; ++c)
       dev_out = dev_out && outs[c].data && is_device_ptr(outs[c].data) &&
                 (!outs[c].validity || is_device_ptr(outs[c].validity));
+    // Column c of the output as a gather-kernel column writing into out/words.
+    auto gather_col = [&](GatherCol& g, size_t c, void* out, uint64_t* words) {
+      const bool pc = c < st.ptypes.size();
+      const size_t bc = pc ? 0 : c - st.ptypes.size();
+      g.flag = static_cast<int>(c);
+      g.width = static_cast<int>(type_width(pc ? st.ptypes[c] : st.btypes[bc]));
+      g.side = pc ? 0 : 1;
+      g.out = out;
+      g.words = words;
+      if (pc) {
+        const StagedCol& sc = st.probe_staged[c];
+        g.src = sc.dev.data;
+        g.bits = sc.dev.all_valid ? nullptr : sc.dev.validity;
+        g.code_map = st.ptypes[c] == QEG_STR ? sc.dev.code_map : nullptr;
+      } else {
+        g.src = st.bvals[bc].get();
+        g.bytes = st.bvalid[bc].get<uint8_t>();
+      }
+    };
     if (dev_out) {
       // One pass per column into the caller's device buffers, one sync.
       DevBuf flags(ncol * 4, ctx->stream);
@@ -2260,7 +2279,7 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
       // start: probe columns are plain copies, made by the copy engines on a
       // side stream while the gather kernel fills the build columns.
       std::vector<char> copied(ncol, 0);
-      cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+      bool forked = false;
       DevBuf tmp_words;
       if (st.probe_identity && first % 64 == 0) {
         const uint64_t nw = (count + 63) / 64;
@@ -2269,11 +2288,14 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
         for (size_t c = 0; c < st.ptypes.size(); ++c)
           ntmp += copyable(c) && !st.probe_staged[c].dev.all_valid && !outs[c].validity;
         if (ntmp) tmp_words.alloc(ntmp * nw * 8, ctx->stream);  // before ev_in: ordered ahead of the side stream
-        if (!ctx->side) QEG_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
-        QEG_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
-        QEG_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
-        QEG_CUDA(cudaEventRecord(ev_in, ctx->stream));
-        QEG_CUDA(cudaStreamWaitEvent(ctx->side, ev_in, 0));
+        if (!ctx->side) {
+          QEG_CUDA(cudaEventCreateWithFlags(&ctx->side_in, cudaEventDisableTiming));
+          QEG_CUDA(cudaEventCreateWithFlags(&ctx->side_out, cudaEventDisableTiming));
+          QEG_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        }
+        QEG_CUDA(cudaEventRecord(ctx->side_in, ctx->stream));
+        QEG_CUDA(cudaStreamWaitEvent(ctx->side, ctx->side_in, 0));
+        forked = true;
         size_t itmp = 0;
         for (size_t c = 0; c < st.ptypes.size(); ++c) {
           if (!copyable(c)) continue;  // dictionary codes need translating: gathered below
@@ -2294,7 +2316,7 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
           }
           copied[c] = 1;
         }
-        QEG_CUDA(cudaEventRecord(ev_out, ctx->side));
+        QEG_CUDA(cudaEventRecord(ctx->side_out, ctx->side));
       }
       if (ncol <= static_cast<size_t>(kMaxGatherCols)) {
         GatherK G{};
@@ -2302,37 +2324,15 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
         G.idx[1] = st.out_build.get<uint32_t>() + first;
         G.n = count;
         G.flags = flags.get<unsigned int>();
-        for (size_t c = 0; c < ncol; ++c) {
-          if (copied[c]) continue;
-          const bool pc = c < st.ptypes.size();
-          const size_t bc = pc ? 0 : c - st.ptypes.size();
-          GatherCol& g = G.c[G.ncols++];
-          g.flag = static_cast<int>(c);
-          g.width = static_cast<int>(type_width(pc ? st.ptypes[c] : st.btypes[bc]));
-          g.side = pc ? 0 : 1;
-          g.out = outs[c].data;
-          g.words = outs[c].validity;
-          if (pc) {
-            const StagedCol& sc = st.probe_staged[c];
-            g.src = sc.dev.data;
-            g.bits = sc.dev.all_valid ? nullptr : sc.dev.validity;
-            g.code_map = st.ptypes[c] == QEG_STR ? sc.dev.code_map : nullptr;
-          } else {
-            g.src = st.bvals[bc].get();
-            g.bytes = st.bvalid[bc].get<uint8_t>();
-          }
-        }
+        for (size_t c = 0; c < ncol; ++c)
+          if (!copied[c]) gather_col(G.c[G.ncols++], c, outs[c].data, outs[c].validity);
         if (G.ncols > 0) {
           gather_cols_kernel<<<gw, 256, 0, ctx->stream>>>(G);
           ctx->launches++;
           QEG_CUDA(cudaGetLastError());
         }
       }
-      if (ev_out) {
-        QEG_CUDA(cudaStreamWaitEvent(ctx->stream, ev_out, 0));
-        QEG_CUDA(cudaEventDestroy(ev_in));
-        QEG_CUDA(cudaEventDestroy(ev_out));
-      }
+      if (forked) QEG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->side_out, 0));
       for (size_t c = 0; c < ncol && ncol > static_cast<size_t>(kMaxGatherCols); ++c) {
         const bool pc = c < st.ptypes.size();
         const size_t bc = pc ? 0 : c - st.ptypes.size();
@@ -2353,6 +2353,49 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
                                                       outs[c].validity, flags.get<unsigned int>() + c);
         ctx->launches++;
         QEG_CUDA(cudaGetLastError());
+      }
+      std::vector<uint32_t> f(ncol);
+      QEG_CUDA(cudaMemcpyAsync(f.data(), flags.get(), ncol * 4, cudaMemcpyDeviceToHost, ctx->stream));
+      QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (size_t c = 0; c < ncol; ++c)
+        if (outs[c].all_valid) *outs[c].all_valid = f[c] ? 0 : 1;
+      return;
+    }
+    if (ncol <= static_cast<size_t>(kMaxGatherCols)) {
+      // Host (or mixed) outputs: chunks of rows gathered in one pass into
+      // device staging buffers, each column then copied out; one sync.
+      const uint64_t chunk = std::min<uint64_t>((count + 63) / 64 * 64, uint64_t{1} << 24);
+      const uint64_t cw = chunk / 64;
+      size_t row_bytes = 0;
+      std::vector<size_t> vofs(ncol);
+      for (size_t c = 0; c < ncol; ++c) {
+        vofs[c] = row_bytes * chunk;
+        row_bytes += type_width(c < st.ptypes.size() ? st.ptypes[c] : st.btypes[c - st.ptypes.size()]);
+      }
+      DevBuf vals(row_bytes * chunk, ctx->stream), words(ncol * cw * 8, ctx->stream), flags(ncol * 4, ctx->stream);
+      QEG_CUDA(cudaMemsetAsync(flags.get(), 0, ncol * 4, ctx->stream));
+      for (uint64_t off = 0; off < count; off += chunk) {
+        const uint64_t n = std::min(chunk, count - off);
+        GatherK G{};
+        G.ncols = static_cast<int>(ncol);
+        G.idx[0] = st.out_probe.get<uint32_t>() + first + off;
+        G.idx[1] = st.out_build.get<uint32_t>() + first + off;
+        G.n = n;
+        G.flags = flags.get<unsigned int>();
+        for (size_t c = 0; c < ncol; ++c)
+          gather_col(G.c[c], c, vals.get<uint8_t>() + vofs[c], words.get<uint64_t>() + c * cw);
+        gather_cols_kernel<<<grid_for(ctx, (n + 63) / 64 * 32, 256, 8), 256, 0, ctx->stream>>>(G);
+        ctx->launches++;
+        QEG_CUDA(cudaGetLastError());
+        for (size_t c = 0; c < ncol; ++c) {
+          const size_t w = static_cast<size_t>(G.c[c].width);
+          if (outs[c].data)
+            QEG_CUDA(cudaMemcpyAsync(static_cast<uint8_t*>(outs[c].data) + off * w, vals.get<uint8_t>() + vofs[c],
+                                     n * w, cudaMemcpyDefault, ctx->stream));
+          if (outs[c].validity)  // off is a multiple of 64: whole words
+            QEG_CUDA(cudaMemcpyAsync(outs[c].validity + off / 64, words.get<uint64_t>() + c * cw, (n + 63) / 64 * 8,
+                                     cudaMemcpyDefault, ctx->stream));
+        }
       }
       std::vector<uint32_t> f(ncol);
       QEG_CUDA(cudaMemcpyAsync(f.data(), flags.get(), ncol * 4, cudaMemcpyDeviceToHost, ctx->stream));

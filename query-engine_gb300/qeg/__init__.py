@@ -439,6 +439,27 @@ class Join:
         _check(lib().qeg_join_fetch(self.p, first, count, outs), self.ctx.p)
         return [(v[:count], unpack_validity(w, count)) for v, w, _ in keep]
 
+    def fetch_pinned(self, first=0, count=None, bufs=None):
+        """Like fetch(), into page-locked host tensors [(values, validity
+        words)]: gathered on the device in row chunks, copied at the host
+        link's speed. `bufs` (a previous result, large enough) is reused when
+        given: pinning memory is slow."""
+        import torch
+
+        if count is None:
+            count = self.rows - first
+        types = self.probe_types + self.build_types
+        tdt = {I32: torch.int32, I64: torch.int64, F64: torch.float64, BOOL: torch.uint8, TS: torch.int64,
+               STR: torch.int32}
+        if bufs is None or any(v.numel() < count for v, _ in bufs):
+            bufs = [(torch.empty(max(count, 1), dtype=tdt[t], pin_memory=True),
+                     torch.empty(max(1, (count + 63) // 64), dtype=torch.int64, pin_memory=True)) for t in types]
+        outs = (OutColumn * len(types))()
+        for i, (v, w) in enumerate(bufs):
+            outs[i] = OutColumn(v.data_ptr(), w.data_ptr(), None)
+        _check(lib().qeg_join_fetch(self.p, first, count, outs), self.ctx.p)
+        return bufs
+
     def fetch_device(self, first=0, count=None, bufs=None, flags=None):
         """Like fetch(), into torch CUDA tensors [(values, validity words)]:
         one gather pass per column straight into them. `bufs` (a previous

@@ -297,3 +297,39 @@ def test_device_fetch_matches_host_fetch(ctx, jt):
                 assert np.array_equal(dvals[dvalid].view(np.uint8), np.asarray(hv)[hvalid].view(np.uint8))
     finally:
         j.close()
+
+
+def test_host_fetch_in_row_chunks(ctx):
+    # Host outputs are gathered on the device 2^24 rows at a time and copied
+    # out chunk by chunk: a fetch over more than one chunk (pageable numpy and
+    # page-locked torch buffers) must equal the device fetch bit for bit.
+    import torch
+
+    rng = np.random.default_rng(78)
+    nb, npr = 1 << 16, (1 << 24) + 4099
+    bkey = rng.permutation(nb).astype(np.int64)
+    build = [O.TCol(O.I64, bkey), O.TCol(O.F64, rng.random(nb), rng.random(nb) > 0.1)]
+    probe = [O.TCol(O.I64, rng.integers(0, nb + nb // 4, npr), rng.random(npr) > 0.02),
+             O.TCol(O.I32, rng.integers(0, 1000, npr).astype(np.int32))]
+    j = qeg.Join(ctx, [c.type for c in probe], [c.type for c in build], [0], [0], O.LEFT)
+    try:
+        j.build([to_gpu(c) for c in build])
+        j.build_finish()
+        pcols = [to_gpu(c) for c in probe]
+        n = j.probe(pcols)
+        assert n == npr
+        for first, count in ((0, n), (64 * 5, n - 64 * 5 - 3), (3, (1 << 24) + 1)):
+            dev = j.fetch_device(first, count)
+            host = j.fetch(first, count)
+            pinned = j.fetch_pinned(first, count)
+            torch.cuda.synchronize()
+            for (hv, hvalid), (pv, pw), (dv, dw) in zip(host, pinned, dev):
+                nw = (count + 63) // 64
+                assert torch.equal(pw[:nw], dw[:nw].cpu())
+                dvalid = np.unpackbits(dw[:nw].cpu().numpy().view(np.uint8), bitorder="little")[:count].astype(bool)
+                assert np.array_equal(dvalid, hvalid)
+                dvals = dv[:count].cpu().numpy()
+                assert np.array_equal(dvals[dvalid], np.asarray(hv)[dvalid])
+                assert np.array_equal(dvals[dvalid], pv[:count].numpy()[dvalid])
+    finally:
+        j.close()
