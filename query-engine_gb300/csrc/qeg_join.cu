@@ -534,6 +534,108 @@ __global__ void __launch_bounds__(256, 4) probe_sink_pipe_kernel(const SinkK P) 
   }
 }
 
+// Dense-table, unique-key sink with a small register footprint, so that
+// more warps per SM keep the probe stream in flight. A warp owns tiles of
+// U x 64 rows (lane i takes rows 2i and 2i+1 of each 64-row chunk: one
+// contiguous span per load instruction, one validity word per chunk); with
+// PRE the next tile's loads are issued before the current tile's lookups.
+// Tile indexes are 32-bit (the host launches it for fewer than 2^31 tiles).
+template <typename KT, typename VT, int U, bool PRE, int MINB>
+__global__ void __launch_bounds__(256, MINB) probe_sink_dense_kernel(const SinkK P) {
+  const KT* keys = static_cast<const KT*>(P.key);
+  const VT* vals = static_cast<const VT*>(P.val);
+  const unsigned lane = threadIdx.x & 31u;
+  constexpr uint32_t kTile = 64u * U;
+  const uint32_t ntiles = static_cast<uint32_t>(P.n / kTile);
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  uint32_t cnt = 0, seen = 0;
+  unsigned long long sum = 0;
+  KT k[U][2];
+  VT v[U][2];
+  uint64_t kw[U], vw[U];
+  auto load_tile = [&](uint32_t tile) {
+    const uint64_t base = static_cast<uint64_t>(tile) * kTile;
+#pragma unroll
+    for (int c = 0; c < U; ++c) {
+      load2(keys + base + c * 64 + 2 * lane, k[c]);
+      load2(vals + base + c * 64 + 2 * lane, v[c]);
+      kw[c] = P.kvalid ? __ldg(P.kvalid + (base >> 6) + c) : ~0ull;
+      vw[c] = P.vvalid ? __ldg(P.vvalid + (base >> 6) + c) : ~0ull;
+    }
+  };
+  auto consume = [&](const KT (&ck)[U][2], const VT (&cv)[U][2], const uint64_t (&ckw)[U], const uint64_t (&cvw)[U]) {
+#pragma unroll
+    for (int c = 0; c < U; ++c)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const uint64_t s = static_cast<uint64_t>(static_cast<int64_t>(ck[c][j])) - static_cast<uint64_t>(P.T.dmin);
+        const bool kv = (ckw[c] >> (2 * lane + j)) & 1ull;
+        const uint32_t hit = (kv && s < P.T.cap) ? static_cast<uint32_t>((__ldg(P.T.bitmap + (s >> 6)) >> (s & 63)) & 1ull) : 0u;
+        cnt += hit;
+        if (hit && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
+          sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j]));
+          seen = 1;
+        }
+      }
+  };
+  if (PRE) {
+    if (t < ntiles) load_tile(t);
+    for (; t < ntiles; t += nwarps) {
+      KT ck[U][2];
+      VT cv[U][2];
+      uint64_t ckw[U], cvw[U];
+#pragma unroll
+      for (int c = 0; c < U; ++c) {
+        ck[c][0] = k[c][0];
+        ck[c][1] = k[c][1];
+        cv[c][0] = v[c][0];
+        cv[c][1] = v[c][1];
+        ckw[c] = kw[c];
+        cvw[c] = vw[c];
+      }
+      if (t + nwarps < ntiles) load_tile(t + nwarps);
+      consume(ck, cv, ckw, cvw);
+    }
+  } else {
+    for (; t < ntiles; t += nwarps) {
+      load_tile(t);
+      consume(k, v, kw, vw);
+    }
+  }
+  // Rows after the last full tile, one per thread.
+  for (uint64_t r = static_cast<uint64_t>(ntiles) * kTile + static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+       r < P.n; r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const bool kv = !P.kvalid || ((P.kvalid[r >> 6] >> (r & 63)) & 1ull);
+    const uint64_t mm = kv ? sink_lookup<KT, QEG_JOIN_DENSE, true>(P.T, keys[r]) : 0;
+    cnt += static_cast<uint32_t>(mm);
+    if (mm && (!P.vvalid || ((P.vvalid[r >> 6] >> (r & 63)) & 1ull))) {
+      sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r]));
+      seen = 1;
+    }
+  }
+  unsigned long long c64 = cnt;
+  for (int o = 16; o > 0; o >>= 1) {
+    c64 += __shfl_down_sync(0xffffffffu, c64, o);
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    seen |= __shfl_down_sync(0xffffffffu, seen, o);
+  }
+  __shared__ unsigned long long s_acc[3];
+  if (threadIdx.x == 0) s_acc[0] = s_acc[1] = s_acc[2] = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_acc[0], c64);
+    atomicAdd(&s_acc[1], sum);
+    atomicOr(&s_acc[2], static_cast<unsigned long long>(seen));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_acc[0]) atomicAdd(P.acc + 0, s_acc[0]);
+    if (s_acc[1]) atomicAdd(P.acc + 1, s_acc[1]);
+    if (s_acc[2]) atomicOr(P.acc + 2, s_acc[2]);
+  }
+}
+
 // cp.async-staged sink. Each warp streams its tiles of 128 rows through a
 // private ring of kAsyncStages shared-memory stages filled with 16-byte
 // cp.async copies (keys, payloads, and the two validity words per column), so
@@ -2491,13 +2593,17 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       // 1.38 ms for 256M dense-table probes; 5.9 against 10.4 ms hashed).
       auto al16 = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };
       const char* tma_env = getenv("QEG_SINK_TMA");
-      // The register-pipelined kernel with 128-row warp tiles is the default:
-      // on GB300 it streams the 256M-row probe side at 74% of the measured HBM
-      // copy bandwidth, against 61% for the 4-rows-per-thread kernel and 41%
-      // with 256-row tiles (which spill). QEG_SINK_PIPE=0|2|4 picks one for
-      // measurement.
+      // Dense table with unique build keys: the 32-register kernel at 8 CTAs
+      // of 256 per SM (full occupancy) streams the 256M-row probe side at 96%
+      // of the measured HBM copy bandwidth on GB300. The same kernel with the
+      // next tile's loads issued early, or at 6 CTAs per SM, measured 88-96%;
+      // the 64-register pipelined kernel with 128-row warp tiles (4 CTAs per
+      // SM) 73%, and 81% at 6 CTAs per SM (40 registers, spilling). Every other
+      // table takes the pipelined kernel. QEG_SINK_PIPE=0|1|2|4|8 picks one
+      // for measurement.
+      const bool lean_ok = dense && st.unique && n / 64 < (uint64_t{1} << 31);
       const char* pipe_env = getenv("QEG_SINK_PIPE");
-      const int pipe = pipe_env ? atoi(pipe_env) : 2;
+      const int pipe = pipe_env ? atoi(pipe_env) : (lean_ok ? 1 : 2);
       const bool use_tma = n >= static_cast<uint64_t>(kTileRows) * ctx->sms * 2 && al16(S.kvalid) && al16(S.vvalid) &&
                            tma_env != nullptr && tma_env[0] == '1';
       auto launch_async = [&](void (*kern)(SinkK), size_t sb) {
@@ -2533,6 +2639,8 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       else if (dense) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, false, 2>);                           \
       else if (st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_HASH, true, 2>);                         \
       else launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_HASH, false, 2>);                                       \
+    } else if (pipe == 1 && lean_ok) {                                                                             \
+      launch(probe_sink_dense_kernel<KT, VT, 1, false, 8>);                                                        \
     } else if (pipe == 4) {                                                                                        \
       if (dense && st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, true, 4>);                    \
       else if (dense) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, false, 4>);                           \

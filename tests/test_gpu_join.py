@@ -151,14 +151,16 @@ def test_random_joins(ctx, seed):
 
 @pytest.mark.parametrize("strategy", [qeg.JOIN_AUTO, qeg.JOIN_HASH, qeg.JOIN_DENSE])
 @pytest.mark.parametrize("dup", [False, True])
-@pytest.mark.parametrize("kernel", ["default", "pipe0", "pipe4", "pipe8", "tma"])
+@pytest.mark.parametrize("kernel", ["default", "pipe0", "pipe2", "pipe4", "pipe8", "tma"])
 def test_count_sum_sink(ctx, strategy, dup, kernel, monkeypatch):
     """The 16M x 256M join workload's shape at 1/64 scale: unique (or
     duplicated) build keys, probe keys half hits and half from a disjoint
     range, 2% NULL keys on both sides, SUM over an int64 payload. `kernel`
-    picks the sink kernel: the default (128-row pipelined warp tiles), the
-    4-rows-per-thread kernel, 256-row tiles, the cp.async-staged kernel, or the
-    opt-in TMA-staged kernel (each 2M-row half is large enough for it)."""
+    picks the sink kernel: the default (the full-occupancy kernel for a dense
+    table of unique keys, else 128-row pipelined warp tiles), the
+    4-rows-per-thread kernel, 128-row or 256-row pipelined tiles, the
+    cp.async-staged kernel, or the opt-in TMA-staged kernel (each 2M-row half
+    is large enough for it)."""
     if kernel == "tma":
         monkeypatch.setenv("QEG_SINK_TMA", "1")
     elif kernel != "default":
@@ -188,6 +190,38 @@ def test_count_sum_sink(ctx, strategy, dup, kernel, monkeypatch):
         assert st["strategy"] == qeg.JOIN_HASH
     else:
         assert st["strategy"] == qeg.JOIN_DENSE
+
+
+@pytest.mark.parametrize("kt,vt", [(O.I64, O.I64), (O.I32, O.I64), (O.I64, O.I32), (O.I32, O.I32)])
+@pytest.mark.parametrize("kernel", ["default", "pipe2"])
+def test_count_sum_dense_types_and_tails(ctx, kt, vt, kernel, monkeypatch):
+    # Dense table of unique keys over every key/payload width, probe sides
+    # whose length is not a multiple of the 64-row chunk (the per-row tail),
+    # NULLs in keys and payloads, negative keys and payloads, and one probe
+    # batch with no payload NULLs at all.
+    if kernel != "default":
+        monkeypatch.setenv("QEG_SINK_PIPE", kernel[-1])
+    rng = np.random.default_rng(31 + kt + 3 * vt)
+    nb = 50000
+    bkey = rng.permutation(nb).astype(np.int64) - 20000
+    build = O.TCol(kt, bkey.astype(np.int32 if kt == O.I32 else np.int64), rng.random(nb) >= 0.05)
+    j = qeg.Join(ctx, [kt, vt], [kt], [0], [0], strategy=qeg.JOIN_DENSE)
+    j.build([to_gpu(build)])
+    j.build_finish()
+    exp = [0, 0]
+    for npr, vnull in ((1000003, 0.03), (64 * 1000 + 63, 0.0), (17, 0.5)):
+        pkey = rng.integers(-30000, nb, npr)
+        pkey = pkey.astype(np.int32 if kt == O.I32 else np.int64)
+        pval = rng.integers(-(1 << 30), 1 << 30, npr).astype(np.int32 if vt == O.I32 else np.int64)
+        pk = O.TCol(kt, pkey, rng.random(npr) >= 0.02)
+        pv = O.TCol(vt, pval, (rng.random(npr) >= vnull) if vnull else None)
+        c, sm = O.join_count_sum(pk, pv, build)
+        exp = [exp[0] + c, (exp[1] or 0) + (sm or 0)]
+        j.probe_count_sum(to_gpu(pk), to_gpu(pv))
+    got = j.count_sum()
+    assert j.stats()["strategy"] == qeg.JOIN_DENSE
+    j.close()
+    assert got == tuple(exp)
 
 
 def test_count_sum_sparse_keys_use_hash(ctx):
