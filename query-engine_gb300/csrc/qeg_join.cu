@@ -534,14 +534,15 @@ __global__ void __launch_bounds__(256, 4) probe_sink_pipe_kernel(const SinkK P) 
   }
 }
 
-// Dense-table, unique-key sink with a small register footprint, so that
-// more warps per SM keep the probe stream in flight. A warp owns tiles of
-// U x 64 rows (lane i takes rows 2i and 2i+1 of each 64-row chunk: one
-// contiguous span per load instruction, one validity word per chunk); with
-// PRE the next tile's loads are issued before the current tile's lookups.
-// Tile indexes are 32-bit (the host launches it for fewer than 2^31 tiles).
-template <typename KT, typename VT, int U, bool PRE, int MINB>
-__global__ void __launch_bounds__(256, MINB) probe_sink_dense_kernel(const SinkK P) {
+// Sink with a small register footprint, so that more warps per SM keep the
+// probe stream (and, for hashed tables, the random table reads) in flight. A
+// warp owns tiles of U x 64 rows (lane i takes rows 2i and 2i+1 of each
+// 64-row chunk: one contiguous span per load instruction, one validity word
+// per chunk); with PRE the next tile's loads are issued before the current
+// tile's lookups. Tile indexes are 32-bit (the host launches it for fewer
+// than 2^31 tiles).
+template <typename KT, typename VT, int STRAT, bool UNIQUE, int U, bool PRE, int MINB>
+__global__ void __launch_bounds__(256, MINB) probe_sink_lean_kernel(const SinkK P) {
   const KT* keys = static_cast<const KT*>(P.key);
   const VT* vals = static_cast<const VT*>(P.val);
   const unsigned lane = threadIdx.x & 31u;
@@ -549,7 +550,10 @@ __global__ void __launch_bounds__(256, MINB) probe_sink_dense_kernel(const SinkK
   const uint32_t ntiles = static_cast<uint32_t>(P.n / kTile);
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  uint32_t cnt = 0, seen = 0;
+  // Matches per thread fit 32 bits for unique build keys (one per row).
+  using Cnt = typename std::conditional<UNIQUE, uint32_t, unsigned long long>::type;
+  Cnt cnt = 0;
+  uint32_t seen = 0;
   unsigned long long sum = 0;
   KT k[U][2];
   VT v[U][2];
@@ -569,13 +573,24 @@ __global__ void __launch_bounds__(256, MINB) probe_sink_dense_kernel(const SinkK
     for (int c = 0; c < U; ++c)
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
-        const uint64_t s = static_cast<uint64_t>(static_cast<int64_t>(ck[c][j])) - static_cast<uint64_t>(P.T.dmin);
         const bool kv = (ckw[c] >> (2 * lane + j)) & 1ull;
-        const uint32_t hit = (kv && s < P.T.cap) ? static_cast<uint32_t>((__ldg(P.T.bitmap + (s >> 6)) >> (s & 63)) & 1ull) : 0u;
-        cnt += hit;
-        if (hit && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
-          sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j]));
-          seen = 1;
+        if (STRAT == QEG_JOIN_DENSE && UNIQUE) {
+          // Branch-free bitmap probe (a select, not a divergent call).
+          const uint64_t s = static_cast<uint64_t>(static_cast<int64_t>(ck[c][j])) - static_cast<uint64_t>(P.T.dmin);
+          const uint32_t hit =
+              (kv && s < P.T.cap) ? static_cast<uint32_t>((__ldg(P.T.bitmap + (s >> 6)) >> (s & 63)) & 1ull) : 0u;
+          cnt += hit;
+          if (hit && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
+            sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j]));
+            seen = 1;
+          }
+        } else {
+          const uint64_t m = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, ck[c][j]) : 0;
+          cnt += static_cast<Cnt>(m);
+          if (m && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
+            sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j])) * m;
+            seen = 1;
+          }
         }
       }
   };
@@ -607,10 +622,10 @@ __global__ void __launch_bounds__(256, MINB) probe_sink_dense_kernel(const SinkK
   for (uint64_t r = static_cast<uint64_t>(ntiles) * kTile + static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
        r < P.n; r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
     const bool kv = !P.kvalid || ((P.kvalid[r >> 6] >> (r & 63)) & 1ull);
-    const uint64_t mm = kv ? sink_lookup<KT, QEG_JOIN_DENSE, true>(P.T, keys[r]) : 0;
-    cnt += static_cast<uint32_t>(mm);
+    const uint64_t mm = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, keys[r]) : 0;
+    cnt += static_cast<Cnt>(mm);
     if (mm && (!P.vvalid || ((P.vvalid[r >> 6] >> (r & 63)) & 1ull))) {
-      sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r]));
+      sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r])) * mm;
       seen = 1;
     }
   }
@@ -2593,15 +2608,17 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       // 1.38 ms for 256M dense-table probes; 5.9 against 10.4 ms hashed).
       auto al16 = [](const void* p) { return p == nullptr || reinterpret_cast<uintptr_t>(p) % 16 == 0; };
       const char* tma_env = getenv("QEG_SINK_TMA");
-      // Dense table with unique build keys: the 32-register kernel at 8 CTAs
-      // of 256 per SM (full occupancy) streams the 256M-row probe side at 96%
-      // of the measured HBM copy bandwidth on GB300. The same kernel with the
-      // next tile's loads issued early, or at 6 CTAs per SM, measured 88-96%;
-      // the 64-register pipelined kernel with 128-row warp tiles (4 CTAs per
-      // SM) 73%, and 81% at 6 CTAs per SM (40 registers, spilling). Every other
-      // table takes the pipelined kernel. QEG_SINK_PIPE=0|1|2|4|8 picks one
-      // for measurement.
-      const bool lean_ok = dense && st.unique && n / 64 < (uint64_t{1} << 31);
+      // The lean kernel is the default. Dense table with unique build keys: 32
+      // registers at 8 CTAs of 256 per SM (full occupancy) stream the 256M-row
+      // probe side at 96% of the measured HBM copy bandwidth on GB300. The
+      // same kernel with the next tile's loads issued early, or at 6 CTAs per
+      // SM, measured 88-96%; the 64-register pipelined kernel with 128-row
+      // warp tiles (4 CTAs per SM) 73%, and 81% at 6 CTAs per SM (40
+      // registers, spilling). Hashed tables: 40 registers at 6 CTAs per SM
+      // (the probe loop spills 76 B at 32 registers) probe 256M rows against
+      // 16M unique keys in 4.4 ms, against 5.5 ms at 8 CTAs and 5.6 ms for the
+      // pipelined kernel. QEG_SINK_PIPE=0|1|2|4|8 picks one for measurement.
+      const bool lean_ok = n / 64 < (uint64_t{1} << 31);
       const char* pipe_env = getenv("QEG_SINK_PIPE");
       const int pipe = pipe_env ? atoi(pipe_env) : (lean_ok ? 1 : 2);
       const bool use_tma = n >= static_cast<uint64_t>(kTileRows) * ctx->sms * 2 && al16(S.kvalid) && al16(S.vvalid) &&
@@ -2640,7 +2657,10 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       else if (st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_HASH, true, 2>);                         \
       else launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_HASH, false, 2>);                                       \
     } else if (pipe == 1 && lean_ok) {                                                                             \
-      launch(probe_sink_dense_kernel<KT, VT, 1, false, 8>);                                                        \
+      if (dense && st.unique) launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_DENSE, true, 1, false, 8>);          \
+      else if (dense) launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_DENSE, false, 1, false, 8>);                 \
+      else if (st.unique) launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_HASH, true, 1, false, 6>);               \
+      else launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_HASH, false, 1, false, 6>);                             \
     } else if (pipe == 4) {                                                                                        \
       if (dense && st.unique) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, true, 4>);                    \
       else if (dense) launch(probe_sink_pipe_kernel<KT, VT, QEG_JOIN_DENSE, false, 4>);                           \
