@@ -156,9 +156,9 @@ def test_count_sum_sink(ctx, strategy, dup, kernel, monkeypatch):
     """The 16M x 256M join workload's shape at 1/64 scale: unique (or
     duplicated) build keys, probe keys half hits and half from a disjoint
     range, 2% NULL keys on both sides, SUM over an int64 payload. `kernel`
-    picks the sink kernel: the default (the full-occupancy kernel for a dense
-    table of unique keys, else 128-row pipelined warp tiles), the
-    4-rows-per-thread kernel, 128-row or 256-row pipelined tiles, the
+    picks the sink kernel: the default (the small-register kernel at high
+    occupancy, for every table kind), the 4-rows-per-thread kernel, 128-row
+    or 256-row pipelined warp tiles, the
     cp.async-staged kernel, or the opt-in TMA-staged kernel (each 2M-row half
     is large enough for it)."""
     if kernel == "tma":
