@@ -202,7 +202,12 @@ qeg_status qeg_window_create(qeg_ctx* ctx, const int32_t* col_types, int ncols,
  *               probe rows once, build columns NULL)
  * fetch       ~ HashJoin::next (ops/join.cpp:260-299): output rows
  *               [first, first+count) of the last probed batch, probe columns
- *               then build columns                                          */
+ *               then build columns. Device output buffers: one gather pass
+ *               straight into them (a LEFT as-of join from a row that is a
+ *               multiple of 64 copies its probe columns on a side stream).
+ *               Host (or mixed) buffers: gathered on the device in chunks of
+ *               2^24 rows and copied out; page-locked host memory copies at
+ *               the host link's speed. One stream synchronisation per call. */
 qeg_status qeg_join_create(qeg_ctx* ctx, const int32_t* probe_types, int nprobe,
                            const int32_t* build_types, int nbuild, const uint32_t* probe_keys,
                            const uint32_t* build_keys, int nkeys, int32_t join_type,
