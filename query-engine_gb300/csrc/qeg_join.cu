@@ -1879,8 +1879,7 @@ void JoinState::finish_build() {
   }
   uint64_t d[2] = {0, 0};
   QEG_CUDA(cudaMemcpyAsync(d, dup.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
-  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
-  check_device_error(ctx);
+  check_device_error(ctx);  // its synchronisation also lands d
   distinct = d[1];
   // Dense: the keys are unique when every non-NULL key set its own bit.
   unique = strategy == QEG_JOIN_DENSE ? (distinct == nonnull ? 1 : 0) : ((d[0] & 0xffffffffull) ? 0 : 1);
@@ -1974,8 +1973,7 @@ void JoinState::asof_build() {
   const bool in_a = R.lo == A.lo;
   ats = in_a ? std::move(a_lo) : std::move(b_lo);
   arow = in_a ? std::move(a_val) : std::move(b_val);
-  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
-  check_device_error(ctx);
+  check_device_error(ctx);  // synchronises the stream
 }
 
 // One global hash table of the build keys (+ per-slot row counts).
@@ -2112,8 +2110,7 @@ void JoinState::ensure_csr() {
     ctx->launches++;
     QEG_CUDA(cudaGetLastError());
   }
-  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
-  check_device_error(ctx);
+  check_device_error(ctx);  // synchronises the stream
   csr_built = true;
 }
 
