@@ -11,11 +11,20 @@ One step = build the join table from the resident build side, then probe the
 whole probe side through the fused COUNT/SUM sink. `value` is rows/s over
 build + probe rows with inputs resident in HBM (inputs exceed L2, so no flush
 is needed); `e2e` is the same metric through the C ABI from pinned host
-buffers, host->device copies inside the timed region.
+buffers, host->device copies inside the timed region. `full_size_parity`
+compares the result with a torch computation that uses no library kernel and
+with the oracle run on the whole workload (the CPU baseline's run).
+
+The default run adds sub-objects for the other workloads of the metric, each
+with its roofline, clocks and full-size parity: `sparse_keys` (the same join
+with keys spread over int64, so the hash table is used), `plain_agg` (1M rows,
+1024 keys), `skew_agg` (512M Zipf rows, learned vs plain sizing), `batch`
+(4096 GROUP BY queries in one persistent kernel) and `pipeline` (filter ->
+join -> GROUP BY over 200M trades).
 
 --impl reference times the reference's CPU algorithm (the oracle's port of its
-morsel-parallel engine, with all host threads) on a bounded sample of the same
-workload. --workload selects other workloads of the engine for measurement.
+morsel-parallel engine, with all host threads) on the whole join workload.
+--workload selects one other workload of the engine for measurement.
 """
 import argparse
 import json
@@ -38,6 +47,9 @@ SEED = 20260615
 # from one ncu capture on a 64M-row probe side; the traffic grows in
 # proportion to the probe rows (the 2 MiB dense bitmap stays in L2).
 SINK_TRAFFIC_PER_ROW = (1082.670e6 + 3.291e6) / (1 << 26)
+# The same figure for the hashed-table sink of the sparse-key join (None: not
+# captured for the current kernel).
+HASH_SINK_TRAFFIC_PER_ROW = None
 
 
 def replica_throughput(total_ms, rows_per_rank, steps, world, device):
@@ -134,14 +146,47 @@ def pack_bits_torch(valid):
 
 
 # ---------------------------------------------------------------------------
+# Full-size parity helpers: independent torch computations of each workload's
+# result, computed without the library's kernels.
+# ---------------------------------------------------------------------------
+def unpack_bits_torch(words, n):
+    """int64 validity words (bit i of word i/64, LSB-first) -> bool [n]."""
+    b = words.contiguous().view(torch.uint8)
+    bits = (b.unsqueeze(1) >> torch.arange(8, device=b.device, dtype=torch.uint8)) & 1
+    return bits.reshape(-1)[:n].bool()
+
+
+def f64_close_torch(a, b):
+    """The reference's F64 comparator (oracle/result_set.h:53-54,
+    oracle/result_set.cpp:84-92): |a-b| <= 1e-9 + 1e-9*max(|a|,|b|), NaN equal
+    to NaN. Returns the number of mismatches."""
+    tol = 1e-9 + 1e-9 * torch.maximum(a.abs(), b.abs())
+    ok = ((a - b).abs() <= tol) | (torch.isnan(a) & torch.isnan(b))
+    return int((~ok).sum())
+
+
+# ---------------------------------------------------------------------------
 # Workload: 16M x 256M inner join, COUNT(*) + SUM(probe payload)
 # ---------------------------------------------------------------------------
-class JoinWorkload:
-    name = "join_16Mx256M_count_sum"
+# Odd multiplier and offset of the bijection on 64-bit integers that turns the
+# dense key set into a sparse one (k -> k*MUL + ADD mod 2^64): keys stay unique,
+# the probe side's disjoint range stays disjoint, and the key range spans all
+# of int64, so no direct-address table applies.
+SPARSE_MUL = 0x9E3779B97F4A7C15 - (1 << 64)
+SPARSE_ADD = 0x2545F4914F6CDD1D
 
-    def __init__(self, dev, nbuild=1 << 24, nprobe=1 << 28, seed=SEED + 2):
+
+class JoinWorkload:
+    """`sparse=False`: the join of the task's shape -- build keys a random
+    permutation of 0..nbuild-1. `sparse=True`: the same rows with every key (build
+    and probe) pushed through the odd-multiplier bijection, so the build side is
+    16M unique keys spread over all of int64 and the join takes the hash table."""
+
+    def __init__(self, dev, nbuild=1 << 24, nprobe=1 << 28, seed=SEED + 2, sparse=False):
         g = torch.Generator(device=dev)
         g.manual_seed(seed)
+        self.sparse = sparse
+        self.name = "join_%dMx%dM_count_sum%s" % (nbuild >> 20, nprobe >> 20, "_sparse_keys" if sparse else "")
         self.nbuild, self.nprobe = nbuild, nprobe
         self.bkey = torch.randperm(nbuild, generator=g, device=dev, dtype=torch.int64)
         self.bvalid = pack_bits_torch(torch.rand(nbuild, generator=g, device=dev) >= 0.02)
@@ -152,6 +197,9 @@ class JoinWorkload:
         del inb, out, hit
         self.pvalid = pack_bits_torch(torch.rand(nprobe, generator=g, device=dev) >= 0.02)
         self.pval = torch.randint(0, 1 << 20, (nprobe,), generator=g, device=dev, dtype=torch.int64)
+        if sparse:
+            self.bkey.mul_(SPARSE_MUL).add_(SPARSE_ADD)
+            self.pkey.mul_(SPARSE_MUL).add_(SPARSE_ADD)
         torch.cuda.synchronize()
 
     def rows(self):
@@ -161,19 +209,27 @@ class JoinWorkload:
         # key 8 B + payload 8 B + 1/8 B validity per probe row
         return self.nprobe * 16 + (self.nprobe + 7) // 8
 
+    def algorithmic_build_bytes(self):
+        return self.nbuild * 8 + (self.nbuild + 7) // 8
+
     def h2d_bytes(self):
         return self.nbuild * 8 + self.bvalid.numel() * 8 + self.nprobe * 16 + self.pvalid.numel() * 8
 
     def run(self, qeg, ctx, strategy, events=None, host=None):
+        """One step: build the table from the build side, probe the whole probe
+        side through the COUNT/SUM sink. `events` = [build start, probe start,
+        probe end, stream] (CUDA events recorded on the library's stream)."""
         src = host if host is not None else self
         j = qeg.Join(ctx, [qeg.I64, qeg.I64], [qeg.I64], [0], [0], strategy=strategy)
+        if events:
+            events[0].record(events[3])
         j.build([qeg.Col(src.bkey, src.bvalid, qeg.I64)])
         j.build_finish()
         if events:
-            events[0].record(events[2])
+            events[1].record(events[3])
         j.probe_count_sum(qeg.Col(src.pkey, src.pvalid, qeg.I64), qeg.Col(src.pval, None, qeg.I64))
         if events:
-            events[1].record(events[2])
+            events[2].record(events[3])
         res = j.count_sum()
         st = j.stats()
         j.close()
@@ -188,17 +244,35 @@ class JoinWorkload:
             setattr(h, k, getattr(self, k).cpu().pin_memory())
         return h
 
-    def cpu_sample(self, probe_rows):
+    def cpu_columns(self, probe_rows):
+        """The first `probe_rows` probe rows and the whole build side as oracle
+        columns: (probe key, probe payload, build key, build payload)."""
         import oracle as O
 
         bk = self.bkey.cpu().numpy()
-        bv = np.unpackbits(self.bvalid.cpu().numpy().view(np.uint8), bitorder="little")[: self.nbuild].astype(bool)
+        bv = unpack_bits_torch(self.bvalid, self.nbuild).cpu().numpy()
         pk = self.pkey[:probe_rows].cpu().numpy()
-        pv = np.unpackbits(self.pvalid[: (probe_rows + 63) // 64].cpu().numpy().view(np.uint8),
-                           bitorder="little")[:probe_rows].astype(bool)
+        pv = unpack_bits_torch(self.pvalid[: (probe_rows + 63) // 64], probe_rows).cpu().numpy()
         pval = self.pval[:probe_rows].cpu().numpy()
         return (O.TCol(O.I64, pk, pv), O.TCol(O.I64, pval), O.TCol(O.I64, bk, bv),
                 O.TCol(O.I64, np.zeros(self.nbuild, np.int64)))
+
+    def expected_torch(self, chunk=1 << 25):
+        """COUNT(*) and SUM(probe payload) of the inner join, from torch alone:
+        the non-NULL build keys sorted, each non-NULL probe key's multiplicity
+        found by two binary searches. NULL keys never match (kNeverMatch,
+        ops/hashtable.cpp:135-163)."""
+        bs = torch.sort(self.bkey[unpack_bits_torch(self.bvalid, self.nbuild)]).values
+        count = 0
+        total = 0
+        for a in range(0, self.nprobe, chunk):
+            b = min(self.nprobe, a + chunk)
+            pk = self.pkey[a:b]
+            pm = unpack_bits_torch(self.pvalid[a // 64:(b + 63) // 64], b - a)
+            m = (torch.searchsorted(bs, pk, right=True) - torch.searchsorted(bs, pk)) * pm
+            count += int(m.sum())
+            total += int((m * self.pval[a:b]).sum())
+        return count, (total if count else None)
 
 
 def zipf_keys(n, domain, s, g, dev, chunk=1 << 25):
@@ -233,6 +307,7 @@ class AggWorkload:
         g = torch.Generator(device=dev)
         g.manual_seed(seed)
         self.kind = kind
+        self.seed = seed
         if kind == "skew":
             self.n = nrows or (512 << 20)
             self.name = "skew_agg_%dM_zipf1.1_over_64M" % (self.n >> 20)
@@ -255,21 +330,92 @@ class AggWorkload:
         torch.cuda.synchronize()
         self.groups = int(torch.unique(self.key).numel())
 
-    def run(self, qeg, ctx, config):
+    def run(self, qeg, ctx, config, batch_rows=None):
         a = qeg.Aggregate(ctx, [c.type for c in self.cols], [0], self.aggs, config)
-        a.consume(self.cols)
+        if batch_rows is None:
+            a.consume(self.cols)
+        else:
+            for s in range(0, self.n, batch_rows):
+                e = min(self.n, s + batch_rows)
+                a.consume([qeg.Col(c.values[s:e], None if c.validity is None else c.validity[s // 64:(e + 63) // 64],
+                                   c.type) for c in self.cols])
         n = a.finish()
         st = a.stats()
         a.close()
         return n, st
 
+    def parity(self, qeg, ctx, config):
+        """Full-size parity of one GROUP BY run. `skew`: every group's COUNT,
+        SUM(I64), MIN and MAX exactly and SUM(F64) within the reference's
+        epsilon against a torch reduction (torch.unique + index_add /
+        scatter_reduce, no library kernel). `agg1m`: every cell against the
+        oracle at the workload's own shape, 2048-row batches (results within
+        the reference's comparator, oracle/result_set.cpp:129-187)."""
+        import oracle as O
 
-def run_agg_bench(args, dev, local):
+        if self.kind != "skew":
+            a = qeg.Aggregate(ctx, [c.type for c in self.cols], [0], self.aggs, config)
+            for s in range(0, self.n, 2048):
+                e = min(self.n, s + 2048)
+                a.consume([qeg.Col(c.values[s:e], None if c.validity is None else c.validity[s // 64:(e + 63) // 64],
+                                   c.type) for c in self.cols])
+            a.finish()
+            got = a.fetch()
+            a.close()
+            key = self.key.cpu().numpy()
+            val = self.v.cpu().numpy()
+            valid = unpack_bits_torch(self.valid, self.n).cpu().numpy()
+            et, erows = O.groupby([O.TCol(O.I64, key), O.TCol(O.F64, val, valid)], [0], self.aggs, 2048)
+            types = [O.I64, O.I64, O.F64, O.F64, O.F64, O.F64]
+            rows = list(zip(*[[None if not ok else (float(v) if t == O.F64 else int(v)) for v, ok in zip(vs, va)]
+                              for (vs, va), t in zip(got, types)]))
+            msg = O.compare(types, rows, et, erows)
+            return {"cells_vs_oracle_2048_row_batches": msg is None, "groups": len(erows),
+                    "mismatch": msg}
+        a = qeg.Aggregate(ctx, [c.type for c in self.cols], [0], self.aggs, config)
+        a.consume(self.cols)
+        ng = a.finish()
+        res = a.fetch_torch()
+        ctx.synchronize()
+        a.close()
+        gkey, order = torch.sort(res[0][0])
+        cols = [res[i][0][order] for i in range(1, 6)]
+        allvalid = all(bool(unpack_bits_torch(res[i][1], ng).all()) for i in range(6))
+        del res
+        uniq, inv, cnt = torch.unique(self.key, sorted=True, return_inverse=True, return_counts=True)
+        G = uniq.numel()
+        s1 = torch.zeros(G, dtype=torch.int64, device=uniq.device).index_add_(0, inv, self.v1)
+        s2 = torch.zeros(G, dtype=torch.float64, device=uniq.device).index_add_(0, inv, self.v2)
+        mn = torch.full((G,), 1 << 62, dtype=torch.int64, device=uniq.device).scatter_reduce_(0, inv, self.v1, "amin")
+        mx = torch.full((G,), -(1 << 62), dtype=torch.int64, device=uniq.device).scatter_reduce_(0, inv, self.v1,
+                                                                                                   "amax")
+        del inv
+        same_keys = ng == G and bool(torch.equal(gkey, uniq))
+        out = {"groups": G, "keys_exact": same_keys, "all_valid": allvalid}
+        if same_keys:
+            out["count_exact"] = bool(torch.equal(cols[0], cnt))
+            out["sum_i64_exact"] = bool(torch.equal(cols[1], s1))
+            out["sum_f64_mismatches"] = f64_close_torch(cols[2], s2)
+            out["min_exact"] = bool(torch.equal(cols[3], mn))
+            out["max_exact"] = bool(torch.equal(cols[4], mx))
+        out["ok"] = bool(same_keys and allvalid and out["count_exact"] and out["sum_i64_exact"]
+                         and out["sum_f64_mismatches"] == 0 and out["min_exact"] and out["max_exact"])
+        del uniq, cnt, s1, s2, mn, mx, cols, gkey, order
+        torch.cuda.empty_cache()
+        return out
+
+
+def run_agg_bench(args, dev, local, kind=None, emit=True):
+    """GROUP BY workload `kind` (skew | agg1m). Returns (and with `emit`
+    prints) one JSON object."""
     import qeg
 
-    W = AggWorkload(dev, args.workload, nrows=args.agg_rows)
+    kind = kind or args.workload
+    W = AggWorkload(dev, kind, nrows=args.agg_rows)
     ctx = qeg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
+    steps = args.steps if emit else min(args.steps, 10)
+    warm = args.warmup if emit else max(3, min(args.warmup, 3))
     variants = {
         "learned": qeg.agg_config(sizing=qeg.SIZE_LEARNED, hot_keys=-1),
         "plain_fixed": qeg.agg_config(sizing=qeg.SIZE_FIXED, initial_capacity=1 << 20),
@@ -281,63 +427,68 @@ def run_agg_bench(args, dev, local):
     clk = ClockSampler(local).__enter__()
     tw0 = time.time()
     for name, cfg in variants.items():
-        for _ in range(args.warmup):
+        for _ in range(warm):
             W.run(qeg, ctx, cfg)
         ctx.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         launches0 = ctx.launches
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             n, st = W.run(qeg, ctx, cfg)
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / args.steps
+        ms = e0.elapsed_time(e1) / steps
         assert n == W.groups, (name, n, W.groups)
         out[name] = {"ms_per_step": ms, "rows_per_s": W.n / (ms / 1e3), "groups": n, "stats": st,
                      "gb_per_s": W.n * W.row_bytes / (ms / 1e3) / 1e9,
-                     "launches_per_step": (ctx.launches - launches0) / args.steps}
+                     "launches_per_step": (ctx.launches - launches0) / steps}
+    if kind == "agg1m":
+        # The workload's own batching: 2048-row batches through consume().
+        cfg = next(iter(variants.values()))
+        W.run(qeg, ctx, cfg, batch_rows=2048)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            W.run(qeg, ctx, cfg, batch_rows=2048)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+        out["batches_2048"] = {"ms_per_step": ms, "rows_per_s": W.n / (ms / 1e3)}
     clocks = clk.summary(tw0, time.time())
     clk.__exit__(None, None, None)
-    check = None
-    if W.kind == "skew":
-        # Full-size property check ("checksum of checksums"): the per-group
-        # aggregates must add up to the column totals -- counts to the row
-        # count, integer sums exactly, the extreme MIN/MAX to the column's,
-        # F64 sums within 1e-9 of the sum of magnitudes.
-        a = qeg.Aggregate(ctx, [c.type for c in W.cols], [0], W.aggs, variants[next(iter(variants))])
-        a.consume(W.cols)
-        a.finish()
-        res = a.fetch_torch()
-        ctx.synchronize()
-        a.close()
-        cnt, s1, s2, mn, mx = (res[i][0] for i in range(1, 6))
-        tol = 1e-9 * float(W.v2.abs().sum())
-        check = {"count_total": int(cnt.sum()) == W.n,
-                 "sum_i64_exact": int(s1.sum()) == int(W.v1.sum()),
-                 "sum_f64_within": abs(float(s2.sum()) - float(W.v2.sum())) <= tol,
-                 "min_max": int(mn.min()) == int(W.v1.min()) and int(mx.max()) == int(W.v1.max())}
-        assert all(check.values()), check
-        del res
+    parity = W.parity(qeg, ctx, variants[next(iter(variants))])
+    ok = parity.get("ok", parity.get("cells_vs_oracle_2048_row_batches"))
+    assert ok, parity
     cpu = None
     if not args.no_cpu:
         cpu = cpu_agg_baseline(W, os.cpu_count() or 1)
-    peak, kind = peaks()
+    peak, pkind = peaks()
     best = out["learned"] if "learned" in out else next(iter(out.values()))
-    print(json.dumps({
+    line = {
         "metric": "rows/s hash aggregate (%s)" % W.name, "value": best["rows_per_s"], "unit": "rows/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": best["ms_per_step"],
+        "n_gpus": 1, "steps": steps, "warmup": warm, "ms_per_step": best["ms_per_step"],
         "higher_is_better": True, "dtype": "int64+f64", "data": "synthetic (seeded, generated on the GPU)",
-        "config": {"workload": W.name, "rows": W.n, "groups": W.groups, "seed": SEED + 3, "M": "2^20",
-                   "full_size_check": check},
-        "roofline": {"bound": "hbm", "achieved": best["gb_per_s"], "peak": peak, "peak_kind": kind,
-                     "unit": "GB/s", "frac": best["gb_per_s"] / peak},
+        "config": {"workload": W.name, "rows": W.n, "groups": W.groups, "seed": W.seed, "M": "2^20",
+                   "l2": "inputs exceed L2, no flush" if W.n * W.row_bytes > 2e8 else
+                   "inputs fit L2 (a correctness-sized workload)"},
+        "roofline": {"bound": "hbm", "achieved": best["gb_per_s"], "peak": peak, "peak_kind": pkind,
+                     "unit": "GB/s", "frac": best["gb_per_s"] / peak,
+                     "algorithmic_bytes_per_row": W.row_bytes},
         "variants": out,
+        "full_size_parity": parity,
         "cpu_baseline": cpu,
         "gpu_launches": out[next(iter(out))]["launches_per_step"] if out else None,
         "clocks": clocks,
         "learned_vs_plain": (out["plain_fixed"]["ms_per_step"] / best["ms_per_step"]
                              if "plain_fixed" in out else None),
-    }))
+    }
+    ctx.close()
+    del W
+    torch.cuda.empty_cache()
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -454,13 +605,44 @@ class PipelineWorkload:
         return h
 
 
-def run_pipeline_bench(args, dev, local):
+def pipeline_parity_torch(W, res):
+    """Every sector's COUNT(*) and SUM(qty) exactly and AVG(price) within the
+    reference's epsilon, against torch alone: the filter as a mask, each
+    trade's sector through the symbol VALUE (code -> canonical id -> symbol
+    row), bincount / index_add per sector."""
+    keep = W.price > 100
+    row_of_id = torch.argsort(W.bmap)  # canonical id -> symbol-table row
+    sec = W.sector[row_of_id[W.tmap[W.sym.long()].long()]].long()[keep]
+    cnt = torch.bincount(sec, minlength=32)
+    sq = torch.zeros(32, dtype=torch.int64, device=sec.device).index_add_(0, sec, W.qty[keep].long())
+    sp = torch.zeros(32, dtype=torch.float64, device=sec.device).index_add_(0, sec, W.price[keep])
+    present = cnt > 0
+    gkey = torch.as_tensor(np.asarray(res[0][0]), device=sec.device).long()
+    order = torch.argsort(gkey)
+    gkey = gkey[order]
+    gcnt = torch.as_tensor(np.asarray(res[1][0]), device=sec.device)[order]
+    gavg = torch.as_tensor(np.asarray(res[2][0]), device=sec.device)[order]
+    gsum = torch.as_tensor(np.asarray(res[3][0]), device=sec.device)[order]
+    want = torch.nonzero(present).flatten()
+    same = bool(torch.equal(gkey, want))
+    out = {"sectors": int(present.sum()), "keys_exact": same}
+    if same:
+        out["count_exact"] = bool(torch.equal(gcnt.long(), cnt[want]))
+        out["sum_qty_exact"] = bool(torch.equal(gsum.long(), sq[want]))
+        out["avg_price_mismatches"] = f64_close_torch(gavg.double(), sp[want] / cnt[want].double())
+    out["ok"] = bool(same and out["count_exact"] and out["sum_qty_exact"] and out["avg_price_mismatches"] == 0)
+    return out
+
+
+def run_pipeline_bench(args, dev, local, emit=True):
     import qeg
 
     W = PipelineWorkload(dev)
     ctx = qeg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    for _ in range(max(args.warmup, 0)):
+    steps = args.steps if emit else min(args.steps, 10)
+    warm = args.warmup if emit else max(3, min(args.warmup, 3))
+    for _ in range(max(warm, 0)):
         types, res = W.run(qeg, ctx)
     clk = ClockSampler(local).__enter__()
     torch.cuda.synchronize()
@@ -468,22 +650,16 @@ def run_pipeline_bench(args, dev, local):
     launches0 = ctx.launches
     tw0 = time.time()
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         types, res = W.run(qeg, ctx)
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = clk.summary(tw0, time.time())
     clk.__exit__(None, None, None)
-    ms = e0.elapsed_time(e1) / args.steps
-    launches = (ctx.launches - launches0) / args.steps
-    # Check against a torch computation of the same query.
-    keep = W.price > 100
-    sec = W.sector[W.bmap.argsort()][W.tmap[W.sym.long()].long()]  # sector of each trade's symbol
-    cnt = torch.bincount(sec[keep].long(), minlength=32)
-    ngroups = int((cnt > 0).sum())
-    got_cnt = dict(zip(res[0][0].tolist(), res[1][0].tolist()))
-    assert all(got_cnt[s] == int(cnt[s]) for s in range(32) if int(cnt[s]) > 0), "pipeline counts differ"
-    assert len(got_cnt) == ngroups
+    ms = e0.elapsed_time(e1) / steps
+    launches = (ctx.launches - launches0) / steps
+    parity = pipeline_parity_torch(W, res)
+    assert parity["ok"], parity
     e2e = None
     if not args.no_e2e:
         host = W.host_copy()
@@ -499,16 +675,23 @@ def run_pipeline_bench(args, dev, local):
     rows_s = W.n / (ms / 1e3)
     gbs = W.n * W.row_bytes / (ms / 1e3) / 1e9
     peak, kind = peaks()
-    print(json.dumps({
+    line = {
         "metric": "rows/s fused filter->join->aggregate (%s)" % W.name, "value": rows_s, "unit": "rows/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "n_gpus": 1, "steps": steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
         "data": "synthetic (seeded, generated on the GPU); inputs 3.2 GB > L2",
-        "config": {"workload": W.name, "rows": W.n, "groups": ngroups, "seed": SEED + 5},
+        "config": {"workload": W.name, "rows": W.n, "groups": parity["sectors"], "seed": SEED + 5},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                      "peak_kind": kind, "note": "whole call (translation tables, kernel, result copy)"},
+        "full_size_parity": parity,
         "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
-    }))
+    }
+    ctx.close()
+    del W
+    torch.cuda.empty_cache()
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 class TickWorkload:
@@ -811,19 +994,53 @@ def load_tuning():
         return [], 0, None
 
 
-def run_batch_bench(args, dev, local):
+def batch_parity_oracle(W, b, groups, stats, nrandom=16, seed=SEED + 44):
+    """Every cell of a fixed sample of the batch's queries against the oracle
+    (the restatement of the reference's GROUP BY, oracle/result_set.cpp:129-187
+    comparator): the 8 largest queries, every query that overflowed its table
+    and was re-run, and `nrandom` seeded random ones."""
+    import oracle as O
+
+    nq = len(groups)
+    sizes = np.diff(W.offsets.astype(np.int64))
+    fell = [q for q in range(nq) if stats[q]["fell_back"]]
+    largest = [int(q) for q in np.argsort(-sizes, kind="stable")[:8]]
+    rng = np.random.default_rng(seed)
+    rand = [int(q) for q in rng.choice(nq, nrandom, replace=False)]
+    sample = sorted(set(largest + fell + rand))
+    types = [O.I32, O.I64, O.F64, O.F64, O.F64, O.F64]
+    bad = []
+    rows_checked = 0
+    for q in sample:
+        a, z = int(W.offsets[q]), int(W.offsets[q + 1])
+        et, erows = O.groupby([O.TCol(O.I32, W.key[a:z].cpu().numpy()), O.TCol(O.F64, W.val[a:z].cpu().numpy())],
+                              [0], W.aggs)
+        got = b.fetch(q)
+        rows = list(zip(*[[None if not ok else (float(v) if t == O.F64 else int(v)) for v, ok in zip(vs, va)]
+                          for (vs, va), t in zip(got, types)]))
+        msg = O.compare(types, rows, et, erows)
+        rows_checked += z - a
+        if msg or int(groups[q]) != len(erows):
+            bad.append((q, msg))
+    return {"queries_vs_oracle": len(sample), "largest": largest, "overflowed": fell, "rows_checked": rows_checked,
+            "mismatches": bad, "ok": not bad}
+
+
+def run_batch_bench(args, dev, local, emit=True):
     import qeg
 
     W = BatchWorkload(dev)
     ctx = qeg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
+    steps = args.steps if emit else min(args.steps, 10)
+    warm = args.warmup if emit else max(3, min(args.warmup, 3))
     tuning, block, tpath = load_tuning()
     k, v = W.cols()
     t0 = time.perf_counter()
     b = qeg.Batch(ctx, W.offsets, k, v, W.aggs, tuning=tuning, block_threads=block)
     ctx.synchronize()
     plan_s = time.perf_counter() - t0
-    for _ in range(max(args.warmup, 0)):
+    for _ in range(max(warm, 0)):
         b.run()
         groups = b.finish()
     clk = ClockSampler(local).__enter__()
@@ -832,21 +1049,24 @@ def run_batch_bench(args, dev, local):
     launches0 = ctx.launches
     tw0 = time.time()
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         b.run()
         groups = b.finish()
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = clk.summary(tw0, time.time())
     clk.__exit__(None, None, None)
-    ms = e0.elapsed_time(e1) / args.steps
-    launches = (ctx.launches - launches0) / args.steps
+    ms = e0.elapsed_time(e1) / steps
+    launches = (ctx.launches - launches0) / steps
     stats = [b.stats(q) for q in range(len(groups))]
     fell = sum(st["fell_back"] for st in stats)
     # Exact group counts (torch.unique per query) for the estimate report.
     true = np.array([int(torch.unique(W.key[int(W.offsets[q]):int(W.offsets[q + 1])]).numel())
                      for q in range(len(groups))])
-    assert np.array_equal(true, groups.astype(np.int64)), "batch group counts differ from torch.unique"
+    parity = {"group_counts_vs_torch_unique": bool(np.array_equal(true, groups.astype(np.int64)))}
+    parity.update(batch_parity_oracle(W, b, groups, stats))
+    parity["ok"] = parity["ok"] and parity["group_counts_vs_torch_unique"]
+    assert parity["ok"], parity
     est = np.array([st["est_groups"] for st in stats])
     fb = [q for q in range(len(groups)) if stats[q]["fell_back"]]
     fell_ratio = sorted(float(true[q] / max(est[q], 1.0)) for q in fb)
@@ -879,16 +1099,17 @@ def run_batch_bench(args, dev, local):
         pms = (time.perf_counter() - p0) * 1e3
         plain = {"ms_per_step": pms, "rows_per_s": W.n / (pms / 1e3)}
     peak, kind = peaks()
-    print(json.dumps({
+    line = {
         "metric": "rows/s batched hash aggregate (%s)" % W.name, "value": rows_s, "unit": "rows/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "n_gpus": 1, "steps": steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64",
         "data": "synthetic (seeded, generated on the GPU); inputs %.1f GB > L2" % (W.n * W.row_bytes / 1e9),
         "config": {"workload": W.name, "queries": len(groups), "rows": W.n, "seed": SEED + 4,
                    "tuning": os.path.relpath(tpath, REPO) if tpath else None,
                    "block_threads": block or 512},
         "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
-                     "peak_kind": kind, "note": "graph replay (aggregate + finalize) time"},
+                     "peak_kind": kind, "note": "graph replay (aggregate + finalize) time, 12 B per row"},
+        "full_size_parity": parity,
         "gpu_launches": launches, "clocks": clocks, "plan_s": plan_s,
         "estimate_log2_error": {"median": float(np.median(lerr)), "p90": float(np.percentile(lerr, 90))},
         "fell_back_queries": int(fell),
@@ -897,7 +1118,13 @@ def run_batch_bench(args, dev, local):
                                     "max": fell_ratio[-1] if fell_ratio else None},
         "plain_sequential": plain,
         "batched_vs_plain": (plain["ms_per_step"] / ms) if plain else None,
-    }))
+    }
+    ctx.close()
+    del W
+    torch.cuda.empty_cache()
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def cpu_agg_baseline(W, threads, sample_rows=1 << 23):
@@ -925,8 +1152,9 @@ def cpu_agg_baseline(W, threads, sample_rows=1 << 23):
 
 def cpu_reference(sample, threads, probe_rows, nbuild):
     """Times the oracle's port of the reference's morsel-parallel engine
-    (exec/parallel.cpp) on the sample: each morsel's private tree rebuilds the
-    build side, so morsels are sized to one per thread."""
+    (exec/parallel.cpp:374-599) on the given probe rows: each morsel's private
+    tree rebuilds the whole build side (exec/parallel.cpp:101-105), so morsels
+    are sized to one per thread. Returns (rows/s, seconds, (count, sum))."""
     import oracle as O
 
     pk, pv, bk, bv = sample
@@ -938,6 +1166,179 @@ def cpu_reference(sample, threads, probe_rows, nbuild):
     return (nbuild + probe_rows) / dt, dt, res
 
 
+def run_join_bench(args, dev, local, world, rank, threads, sparse=False, sub=False):
+    """The join workload: one step = build + probe through the COUNT/SUM sink.
+    Returns the JSON object (rank 0) with roofline, e2e, CPU baseline and the
+    full-size parity check. `sub` = a secondary line: fewer steps, no CPU arms."""
+    import qeg
+
+    strat = {"auto": qeg.JOIN_AUTO, "hash": qeg.JOIN_HASH, "dense": qeg.JOIN_DENSE,
+             "partitioned": qeg.JOIN_PARTITIONED}[args.strategy]
+    steps = min(args.steps, 10) if sub else args.steps
+    warm = max(3, min(args.warmup, 3)) if sub else args.warmup
+    W = JoinWorkload(dev, args.build_rows, args.probe_rows, sparse=sparse)
+    ctx = qeg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    step_ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    clk = ClockSampler(local).__enter__()
+    for _ in range(max(warm, 0)):
+        res, st = W.run(qeg, ctx, strat)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    phase_ev = []
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    tw0 = time.time()
+    step_ev[0].record(stream)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pe = [torch.cuda.Event(enable_timing=True) for _ in range(3)] + [stream]
+        res, st = W.run(qeg, ctx, strat, events=pe)
+        phase_ev.append(pe)
+    step_ev[1].record(stream)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = clk.summary(tw0, time.time())
+    clk.__exit__(None, None, None)
+    barrier()
+    launches = ctx.launches - launches0
+    total_ms, value = replica_throughput(step_ev[0].elapsed_time(step_ev[1]), W.rows(), steps, world, dev)
+    build_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in phase_ev]))
+    probe_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in phase_ev]))
+    ms_per_step = total_ms / steps
+    peak, peak_kind = peaks()
+    achieved = W.algorithmic_probe_bytes() / (probe_ms / 1e3) / 1e9
+    strategy_name = {1: "hash", 2: "partitioned", 3: "dense"}.get(st["strategy"], str(st["strategy"]))
+
+    # Full-size parity: the result against torch alone (no library kernel).
+    exp = W.expected_torch()
+    parity = {"count_sum_vs_torch": res == exp, "expected": {"count": exp[0], "sum": exp[1]}}
+
+    e2e = None
+    if not args.no_e2e:
+        host = W.host_copy()
+        W.run(qeg, ctx, strat, host=host)
+        torch.cuda.synchronize()
+        # Each step timed on its own (the result read back ends it); the
+        # median is reported with every step's time: the host link is shared
+        # with the machine's other work.
+        n_e2e = 3 if sub else max(5, min(args.steps, 10))
+        step_s = []
+        for _ in range(n_e2e):
+            t1 = time.perf_counter()
+            r2, _ = W.run(qeg, ctx, strat, host=host)
+            step_s.append(time.perf_counter() - t1)
+            assert r2 == res
+        dt = float(np.median(step_s))
+        e2e = {"value": W.rows() / dt, "unit": "rows/s", "h2d_bytes_per_step": W.h2d_bytes(),
+               "d2h_bytes_per_step": 24, "steps": n_e2e, "stat": "median of per-step times",
+               "step_ms": [round(x * 1e3, 2) for x in step_s],
+               "min_ms": round(min(step_s) * 1e3, 2), "max_ms": round(max(step_s) * 1e3, 2)}
+        del host
+
+    # The other strategies on the same data (same step definition).
+    alts = {}
+    if args.strategy == "auto":
+        names = (("hash", qeg.JOIN_HASH), ("partitioned", qeg.JOIN_PARTITIONED))
+        for name, sid in names:
+            if name == strategy_name:
+                continue
+            tt = []
+            for i in range(3):
+                e = [torch.cuda.Event(enable_timing=True) for _ in range(3)] + [stream]
+                a0 = torch.cuda.Event(enable_timing=True)
+                a1 = torch.cuda.Event(enable_timing=True)
+                a0.record(stream)
+                ares, _ = W.run(qeg, ctx, sid, events=e)
+                a1.record(stream)
+                torch.cuda.synchronize()
+                assert ares == res, (name, ares, res)
+                if i:
+                    tt.append((a0.elapsed_time(a1), e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])))
+            step = float(np.mean([x[0] for x in tt]))
+            bms = float(np.mean([x[1] for x in tt]))
+            pms = float(np.mean([x[2] for x in tt]))
+            alts[name] = {"strategy": name, "value": W.rows() / (step / 1e3), "ms_per_step": step,
+                          "build_ms": bms, "probe_ms": pms,
+                          "probe_gbs": W.algorithmic_probe_bytes() / (pms / 1e3) / 1e9,
+                          "probe_frac": W.algorithmic_probe_bytes() / (pms / 1e3) / 1e9 / peak}
+            parity[name + "_equal"] = True
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and not sub:
+        # The reference's algorithm (the oracle's port of its morsel-parallel
+        # engine) on the WHOLE workload, every host thread: one run, which is
+        # also a full-size parity check against the oracle.
+        sample = W.cpu_columns(W.nprobe)
+        v, dt, cres = cpu_reference(sample, threads, W.nprobe, W.nbuild)
+        parity["count_sum_vs_oracle"] = cres == res
+        cpu = {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
+               "sample": "the whole workload (%d build + %d probe rows, %.1f s, one run)"
+                         % (W.nbuild, W.nprobe, dt)}
+        # Second reference point: the single-threaded operator tree (scan ->
+        # join -> aggregate, the restatement of Plan::lower + drain).
+        import oracle as O
+
+        k1 = min(W.nprobe, 1 << 23)
+        t1 = time.perf_counter()
+        r1 = O.join_count_sum(O.TCol(O.I64, sample[0].values[:k1], sample[0].valid[:k1]),
+                              O.TCol(O.I64, sample[1].values[:k1]), sample[2])
+        dt1 = time.perf_counter() - t1
+        cpu["single_thread"] = {"value": (W.nbuild + k1) / dt1, "unit": "rows/s", "cores": 1,
+                                "sample": "full %d-row build + first %d probe rows (%.1f s), count %d"
+                                          % (W.nbuild, k1, dt1, r1[0])}
+        del sample
+    ok = all(v for k, v in parity.items() if k != "expected")
+    assert ok, parity
+    kernel = {"dense": "probe_sink_lean_kernel (dense, unique keys)",
+              "hash": "probe_sink_lean_kernel (hash table)"}.get(strategy_name, "probe_sink_pipe_kernel")
+    out = {
+        "metric": "rows/s hash join (build+probe rows), inner join COUNT(*)+SUM(payload)",
+        "value": value, "unit": "rows/s", "n_gpus": world, "steps": steps, "warmup": warm,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int64", "data": "synthetic (seeded, generated on the GPU)",
+        "config": {"workload": W.name, "build_rows": W.nbuild, "probe_rows": W.nprobe, "seed": SEED + 2,
+                   "M": "2^20", "keys": "sparse (odd-multiplier bijection over int64)" if sparse
+                   else "dense (permutation of 0..build_rows-1)",
+                   "null_keys": "2% both sides", "probe_hit_rate": 0.5, "strategy": strategy_name,
+                   "l2": "inputs exceed L2 (4.3 GB probe side), no flush", "parallelism": "replicas"
+                   if world > 1 else "single GPU", "result": {"count": res[0], "sum": res[1]}},
+        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": (SINK_TRAFFIC_PER_ROW * W.nprobe if strategy_name == "dense"
+                                 else HASH_SINK_TRAFFIC_PER_ROW * W.nprobe if HASH_SINK_TRAFFIC_PER_ROW
+                                 else None),
+                     "traffic_source": "ncu dram bytes of the same sink on a 64M-row probe side, scaled by "
+                                       "probe rows",
+                     "probe_ms": probe_ms, "algorithmic_bytes": W.algorithmic_probe_bytes(),
+                     "build_ms": build_ms,
+                     "build_probe_frac": (W.algorithmic_probe_bytes() + W.algorithmic_build_bytes())
+                     / ((build_ms + probe_ms) / 1e3) / 1e9 / peak},
+        "full_size_parity": parity,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "wall_s": wall,
+    }
+    for name, a in alts.items():
+        out[name + "_strategy"] = a
+    ctx.close()
+    del W
+    torch.cuda.empty_cache()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -946,13 +1347,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="join")
     ap.add_argument("--strategy", default="auto", choices=["auto", "hash", "dense", "partitioned"])
+    ap.add_argument("--sparse", action="store_true", help="join workload: sparse keys (hash table)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="join workload: skip the secondary workloads of the default run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--agg-rows", type=int, default=None)
     ap.add_argument("--ticks", type=int, default=200_000_000, help="trades of the window/asof workloads")
     ap.add_argument("--variants", default=None)
-    ap.add_argument("--cpu-probe-rows", type=int, default=1 << 25)
     ap.add_argument("--build-rows", type=int, default=1 << 24)
     ap.add_argument("--probe-rows", type=int, default=1 << 28)
     args = ap.parse_args()
@@ -974,7 +1377,6 @@ def main():
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    import qeg
 
     if args.workload in ("skew", "agg1m"):
         run_agg_bench(args, dev, local)
@@ -992,172 +1394,74 @@ def main():
         run_asof_bench(args, dev, local)
         return
 
-    strat = {"auto": qeg.JOIN_AUTO, "hash": qeg.JOIN_HASH, "dense": qeg.JOIN_DENSE,
-             "partitioned": qeg.JOIN_PARTITIONED}[args.strategy]
-    W = JoinWorkload(dev, args.build_rows, args.probe_rows)
-    ctx = qeg.Context(local)
-    stream = torch.cuda.ExternalStream(ctx.stream)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    step_ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-
-    clk = ClockSampler(local).__enter__()
-    for _ in range(max(args.warmup, 0)):
-        res, st = W.run(qeg, ctx, strat)
-    torch.cuda.synchronize()
-    ctx.synchronize()
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-
-    probe_ms = []
-    barrier()
-    torch.cuda.synchronize()
-    launches0 = ctx.launches
-    tw0 = time.time()
-    step_ev[0].record(stream)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        pe = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), stream]
-        res, st = W.run(qeg, ctx, strat, events=pe)
-        probe_ms.append(pe)
-    step_ev[1].record(stream)
-    torch.cuda.synchronize()
-    ctx.synchronize()
-    wall = time.perf_counter() - t0
-    clocks = clk.summary(tw0, time.time())
-    clk.__exit__(None, None, None)
-    barrier()
-    launches = ctx.launches - launches0
-    total_ms, value = replica_throughput(step_ev[0].elapsed_time(step_ev[1]), W.rows(), args.steps, world, dev)
-    kms = [a.elapsed_time(b) for a, b, _ in probe_ms]
-    probe_avg_ms = float(np.mean(kms))
-    ms_per_step = total_ms / args.steps
-    peak, peak_kind = peaks()
-    achieved = W.algorithmic_probe_bytes() / (probe_avg_ms / 1e3) / 1e9
-
-    e2e = None
-    if not args.no_e2e:
-        host = W.host_copy()
-        W.run(qeg, ctx, strat, host=host)
-        torch.cuda.synchronize()
-        # Each step timed on its own (the result read back ends it); the
-        # median is reported: the host link is shared with the machine's other
-        # work, and a transient slowdown of one step does not move it.
-        n_e2e = max(3, min(args.steps, 5))
-        step_s = []
-        for _ in range(n_e2e):
-            t0 = time.perf_counter()
-            r2, _ = W.run(qeg, ctx, strat, host=host)
-            step_s.append(time.perf_counter() - t0)
-            assert r2 == res
-        dt = float(np.median(step_s))
-        e2e = {"value": W.rows() / dt, "unit": "rows/s", "h2d_bytes_per_step": W.h2d_bytes(),
-               "d2h_bytes_per_step": 24, "steps": n_e2e, "stat": "median of per-step times",
-               "step_ms": [round(x * 1e3, 2) for x in step_s]}
-        del host
-
-    # hash and radix-partitioned strategies on the same data (same step definition)
-    alts = {}
-    if args.strategy == "auto":
-        for name, sid in (("hash", qeg.JOIN_HASH), ("partitioned", qeg.JOIN_PARTITIONED)):
-            tt = []
-            for i in range(3):
-                e = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True), stream]
-                a0 = torch.cuda.Event(enable_timing=True)
-                a1 = torch.cuda.Event(enable_timing=True)
-                a0.record(stream)
-                ares, _ = W.run(qeg, ctx, sid, events=e)
-                a1.record(stream)
-                torch.cuda.synchronize()
-                assert ares == res, (name, ares, res)
-                if i:
-                    tt.append((a0.elapsed_time(a1), e[0].elapsed_time(e[1])))
-            step = float(np.mean([x[0] for x in tt]))
-            pms = float(np.mean([x[1] for x in tt]))
-            alts[name] = {"strategy": name, "value": W.rows() / (step / 1e3), "ms_per_step": step,
-                          "probe_ms": pms, "probe_gbs": W.algorithmic_probe_bytes() / (pms / 1e3) / 1e9}
-
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        sample = W.cpu_sample(args.cpu_probe_rows)
-        v, dt, cres = cpu_reference(sample, threads, args.cpu_probe_rows, W.nbuild)
-        cpu = {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
-               "sample": "full 2^24-row build + first %d probe rows (%.1f s)" % (args.cpu_probe_rows, dt)}
-        # Second reference point: the single-threaded operator tree (scan ->
-        # join -> aggregate, the restatement of Plan::lower + drain).
-        import oracle as O
-
-        k1 = min(args.cpu_probe_rows, 1 << 23)
-        t0 = time.perf_counter()
-        r1 = O.join_count_sum(O.TCol(O.I64, sample[0].values[:k1], sample[0].valid[:k1]),
-                              O.TCol(O.I64, sample[1].values[:k1]), sample[2])
-        dt1 = time.perf_counter() - t0
-        cpu["single_thread"] = {"value": (W.nbuild + k1) / dt1, "unit": "rows/s", "cores": 1,
-                                "sample": "full 2^24-row build + first %d probe rows (%.1f s), count %d"
-                                          % (k1, dt1, r1[0])}
-
+    t_start = time.perf_counter()
+    out = run_join_bench(args, dev, local, world, rank, threads, sparse=args.sparse)
+    if world == 1 and not args.headline_only and not args.sparse:
+        # The default run also measures, each on its own data and each with
+        # its full-size parity check: the same join over sparse keys (the hash
+        # table), the 1M-row plain GROUP BY, the 512M-row skewed GROUP BY
+        # (learned vs plain sizing), the 4096-query batch and the fused
+        # filter -> join -> aggregate pipeline.
+        sub = argparse.Namespace(**vars(args))
+        sub.no_cpu = True
+        out["sparse_keys"] = run_join_bench(sub, dev, local, world, rank, threads, sparse=True, sub=True)
+        sub.no_cpu = args.no_cpu
+        out["plain_agg"] = run_agg_bench(sub, dev, local, kind="agg1m", emit=False)
+        out["skew_agg"] = run_agg_bench(sub, dev, local, kind="skew", emit=False)
+        out["batch"] = run_batch_bench(sub, dev, local, emit=False)
+        out["pipeline"] = run_pipeline_bench(sub, dev, local, emit=False)
+        fsp = {"join": out["full_size_parity"]}
+        for k in ("sparse_keys", "plain_agg", "skew_agg", "batch", "pipeline"):
+            fsp[k] = out[k]["full_size_parity"]
+        out["full_size_parity_all"] = all(
+            v.get("ok", all(x for kk, x in v.items() if kk not in ("expected",) and isinstance(x, bool)))
+            for v in fsp.values())
+    out["bench_wall_s"] = time.perf_counter() - t_start
     if rank == 0:
-        strategy_name = {1: "hash", 2: "partitioned", 3: "dense"}.get(st["strategy"], str(st["strategy"]))
-        out = {
-            "metric": "rows/s hash join (build+probe rows), inner join COUNT(*)+SUM(payload)",
-            "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int64", "data": "synthetic (seeded, generated on the GPU)",
-            "config": {"workload": W.name, "build_rows": W.nbuild, "probe_rows": W.nprobe, "seed": SEED + 2,
-                       "M": "2^20",
-                       "null_keys": "2% both sides", "probe_hit_rate": 0.5, "strategy": strategy_name,
-                       "l2": "inputs exceed L2 (4.3 GB probe side), no flush", "parallelism": "replicas"
-                       if world > 1 else "single GPU", "result": {"count": res[0], "sum": res[1]}},
-            "roofline": {"bound": "hbm", "kernel": "probe_sink_dense_kernel" if strategy_name == "dense"
-                         else "probe_sink_pipe_kernel", "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": SINK_TRAFFIC_PER_ROW * W.nprobe if strategy_name == "dense" else None,
-                         "traffic_source": "ncu dram bytes of the dense sink on a 64M-row probe side "
-                                           "(16.18 B/row), scaled by probe rows",
-                         "probe_ms": probe_avg_ms, "algorithmic_bytes": W.algorithmic_probe_bytes()},
-            "cpu_baseline": cpu,
-            "e2e": e2e,
-            "gpu_launches": int(launches),
-            "clocks": clocks,
-            "wall_s": wall,
-        }
-        for name, a in alts.items():
-            out[name + "_strategy"] = a
         print(json.dumps(out))
 
 
 def run_reference(args, threads):
+    """The reference arm: the reference's CPU algorithm for this path (the
+    oracle's port of its morsel-parallel engine, exec/parallel.cpp:374-599) on
+    the host cores with every thread, on the WHOLE join workload (16M build +
+    256M probe rows) per step. The reference itself compiles only where its
+    source tree is present, so the port stands in for it."""
     dev = torch.device("cuda", 0) if torch.cuda.is_available() else None
     if dev is None:
         print(json.dumps({"impl": "reference", "unavailable": "no GPU to generate the synthetic data on"}))
         return
-    W = JoinWorkload(dev)
-    rows = args.cpu_probe_rows
-    sample = W.cpu_sample(rows)
+    W = JoinWorkload(dev, args.build_rows, args.probe_rows)
+    name, nbuild, nprobe = W.name, W.nbuild, W.nprobe
+    sample = W.cpu_columns(nprobe)
     del W
     torch.cuda.empty_cache()
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_reference(sample, threads, rows, 1 << 24)
+    warm = max(0, min(args.warmup, 1))
+    steps = max(1, min(args.steps, 3))
+    for _ in range(warm):
+        cpu_reference(sample, threads, nprobe, nbuild)
     vals, times = [], []
-    for _ in range(max(1, min(args.steps, 5))):
-        v, dt, res = cpu_reference(sample, threads, rows, 1 << 24)
+    for _ in range(steps):
+        v, dt, res = cpu_reference(sample, threads, nprobe, nbuild)
         vals.append(v)
         times.append(dt)
-    v = float(np.mean(vals))
     ms = np.array(times) * 1e3
+    total_s = float(np.sum(times))
+    v = (nbuild + nprobe) * steps / total_s
     print(json.dumps({
         "impl": "reference", "metric": "rows/s hash join (build+probe rows), inner join COUNT(*)+SUM(payload)",
-        "value": v, "unit": "rows/s", "n_gpus": args.gpus, "steps": len(vals), "warmup": args.warmup,
-        "ms_per_step": float(np.mean(times)) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "value": v, "unit": "rows/s", "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+        "ms_per_step": float(np.mean(ms)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded)",
-        "config": {"workload": "join_16Mx256M_count_sum", "build_rows": 1 << 24, "probe_rows": 1 << 28,
-                   "sampled_probe_rows": rows, "ms_p50": float(np.percentile(ms, 50)),
-                   "ms_p99": float(np.percentile(ms, 99))},
+        "config": {"workload": name, "build_rows": nbuild, "probe_rows": nprobe,
+                   "keys": "dense (permutation of 0..build_rows-1)", "null_keys": "2% both sides",
+                   "probe_hit_rate": 0.5, "result": {"count": res[0], "sum": res[1]},
+                   "ms_p50": float(np.percentile(ms, 50)), "ms_p99": float(np.percentile(ms, 99)),
+                   "steps_note": "each step is the whole workload (%.0f s); steps capped at 3 to keep the run "
+                                 "within a few minutes" % float(np.mean(times))},
         "cpu_baseline": {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
-                         "sample": "full 2^24-row build + first %d probe rows per step" % rows},
+                         "sample": "the whole workload per step (%d build + %d probe rows), morsels of "
+                                   "probe_rows/threads, each rebuilding the build side" % (nbuild, nprobe)},
         "e2e": {"value": v, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 

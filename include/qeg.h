@@ -149,6 +149,13 @@ void* qeg_ctx_stream(qeg_ctx* ctx);
 qeg_status qeg_ctx_synchronize(qeg_ctx* ctx);
 /* Number of kernels this context has launched (for launch accounting). */
 uint64_t qeg_ctx_kernel_launches(const qeg_ctx* ctx);
+/* Failure-detection check, no counterpart in the reference (whose CPU hash
+ * table never waits on another thread; its analogue is the bounded probe of
+ * ops/hashtable.h:84-89). Runs the bounded wait that every composite-key table
+ * uses on a row state word that is claimed and never published, giving up
+ * after `polls` polls (0..2^20). Expected result: QEG_ERR_TIMEOUT, with the
+ * context still usable afterwards. */
+qeg_status qeg_ctx_check_bounded_wait(qeg_ctx* ctx, int32_t polls);
 
 /* ---- hash aggregation: replaces qe::Aggregate (ops/aggregate.h:102-144) ----
  * create  ~ Aggregate::Aggregate + open()'s setup (ops/aggregate.cpp:206-241)
@@ -360,20 +367,26 @@ void qeg_batch_destroy(qeg_batch* batch);
 
 /* ---- join COUNT/SUM sink without device allocation ------------------------
  * No counterpart in the reference (whose CPU operators allocate freely).
- * For callers that must not call cudaMalloc -- code running during CUDA graph
- * capture, engines whose device memory belongs to another allocator, paths
- * that cannot risk an allocation stall at query time -- this runs the inner
- * join's COUNT(*) / SUM(probe_val) sink entirely in a fixed scratch area built
- * into the library: a file-scope static __device__ array of about 24 MiB that
- * every GPU loading the library holds until the process exits. It allocates
- * nothing: no cudaMalloc/cudaFree, no library allocator.
+ * For callers that must not call cudaMalloc -- engines whose device memory
+ * belongs to another allocator (a fixed arena that a stray cudaMalloc would
+ * fragment or exceed), plugins in a host application that accounts for every
+ * device byte, paths that cannot risk an allocation stall or failure at query
+ * time -- this runs the inner join's COUNT(*) / SUM(probe_val) sink entirely
+ * in a fixed scratch area built into the library: a file-scope static
+ * __device__ array of about 24 MiB that every GPU loading the library holds
+ * until the process exits. It allocates nothing: no cudaMalloc/cudaFree, no
+ * library allocator.
  *   - All columns and `out` must be device pointers (no staging copies).
  *   - The build side is limited to 1,048,576 rows; larger builds are rejected
  *     with QEG_ERR_INVALID before any GPU work (use qeg_join_build instead).
+ *   - A STR key's `code_map` is used when `code_map_len` > 0 (as everywhere
+ *     else); a code outside [0, code_map_len) skips its row and sets bit 1 of
+ *     out[3].
  *   - Work is enqueued on `cuda_stream` (a cudaStream_t; NULL = the legacy
  *     default stream) and not synchronised; out[0] = matched row count,
  *     out[1] = SUM of the probe payload, out[2] = 1 if that SUM is non-NULL,
- *     out[3] = nonzero if the scratch table overflowed.
+ *     out[3] = 0, or bit 0 if the scratch table overflowed, bit 1 if a STR
+ *     code was out of range.
  *   - The first call on a device looks up the scratch's device address (with
  *     that device current); make it before any stream capture begins.
  *   - Every call shares the one scratch array and clears what must start at

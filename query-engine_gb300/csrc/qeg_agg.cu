@@ -161,14 +161,8 @@ __device__ __forceinline__ uint64_t* global_rowN(const AggK& P, const uint64_t* 
       }
       st = old;
     }
-    int spins = 0;
-    while (st == 1) {
-      if (++spins > kSpinLimit) {
-        atomicOr(P.err, kDevSpinTimeout);
-        return nullptr;
-      }
-      st = ld_acquire(r);
-    }
+    st = wait_published(r, st, kSpinLimit, P.err);
+    if (st == kRowClaimed) return nullptr;
     if (st == tag) {
       bool eq = ld_relaxed(r + 1) == nullmask;
       for (int j = 0; eq && j < P.nkeys; ++j) eq = ld_relaxed(r + 2 + j) == words[j];

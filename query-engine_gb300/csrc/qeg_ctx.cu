@@ -26,6 +26,14 @@ __global__ void pack_validity_kernel(const uint8_t* __restrict__ valid, uint64_t
   }
 }
 
+// One thread waits, with the bounded wait every composite-key table uses, on
+// a row state word that is claimed and never published.
+__global__ void stuck_claim_kernel(uint64_t* word, int polls, uint32_t* err) {
+  *word = kRowClaimed;
+  __threadfence();
+  wait_published(word, kRowClaimed, polls, err);
+}
+
 }  // namespace
 
 void stage_column(qeg_ctx* ctx, const qeg_column& c, StagedCol& out) {
@@ -193,5 +201,17 @@ qeg_status qeg_ctx_synchronize(qeg_ctx* ctx) {
 }
 
 uint64_t qeg_ctx_kernel_launches(const qeg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+qeg_status qeg_ctx_check_bounded_wait(qeg_ctx* ctx, int32_t polls) {
+  return qeg::guarded(ctx, [&] {
+    qeg::require(ctx != nullptr, "ctx is NULL");
+    qeg::require(polls >= 0 && polls <= (1 << 20), "polls must lie in [0, 2^20]");
+    qeg::DevBuf word(8, ctx->stream);
+    qeg::stuck_claim_kernel<<<1, 1, 0, ctx->stream>>>(word.get<uint64_t>(), polls, ctx->dev_err.get<uint32_t>());
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+    qeg::check_device_error(ctx);
+  });
+}
 
 }  // extern "C"

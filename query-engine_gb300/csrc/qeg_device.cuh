@@ -162,4 +162,23 @@ enum DevError : uint32_t {
   kDevBadInput = 1u << 2,      // an index outside its column (sel / code map)
 };
 
+// State word of a composite-key row in global memory: 0 empty, 1 claimed (the
+// key words are being written), otherwise the published tag.
+constexpr uint64_t kRowClaimed = 1;
+
+// Waits until the global state word at `r` (last read as `st`) leaves the
+// claimed state, polling at most `limit` times with acquire loads. Returns the
+// state it then holds; on running out it raises kDevSpinTimeout in *err and
+// returns kRowClaimed, and the caller gives up on the row.
+__device__ __forceinline__ uint64_t wait_published(const uint64_t* r, uint64_t st, int limit, uint32_t* err) {
+  for (int spins = 0; st == kRowClaimed; ++spins) {
+    if (spins >= limit) {
+      atomicOr(err, kDevSpinTimeout);
+      return kRowClaimed;
+    }
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(st) : "l"(r) : "memory");
+  }
+  return st;
+}
+
 }  // namespace qeg

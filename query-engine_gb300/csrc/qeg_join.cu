@@ -119,14 +119,8 @@ __device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w,
       }
       st = old;
     }
-    int spins = 0;
-    while (st == 1) {
-      if (++spins > kSpinLimit) {
-        atomicOr(err, kDevSpinTimeout);
-        return -1;
-      }
-      st = ld_acquire64(r);
-    }
+    st = wait_published(r, st, kSpinLimit, err);
+    if (st == kRowClaimed) return -1;
     if (st == tag) {
       bool eq = true;
       for (int j = 0; eq && j < T.nkeys; ++j) eq = ld_relaxed64(r + 1 + j) == w[j];

@@ -1,9 +1,10 @@
 // qeg_noalloc.cu -- the inner-join COUNT(*)/SUM(probe payload) sink for callers
 // that cannot allocate device memory.
 //
-// Some callers of this library may not call cudaMalloc at all: code running
-// while a CUDA graph is being captured, engines whose device memory is owned
-// by another allocator (a fixed arena handed out at start-up), and latency-
+// Some callers of this library may not call cudaMalloc at all: engines whose
+// device memory is owned by another allocator (a fixed arena handed out at
+// start-up, which a stray cudaMalloc would fragment or exceed), plugins hosted
+// by an application that accounts for every device byte itself, and latency-
 // critical paths that must not risk an allocation stall or failure at query
 // time. For them, qeg_join_count_sum_noalloc runs the whole join sink in a
 // fixed scratch area that is part of this library's image: a file-scope
@@ -58,12 +59,35 @@ void* scratch_address(int device) {
 
 __device__ __forceinline__ uint64_t slot_hash(uint64_t k) { return hash_fold(kHashSeed, k) & (kCap - 1); }
 
+// out[3] flags.
+constexpr unsigned long long kFlagOverflow = 1ull;  // the scratch table filled up
+constexpr unsigned long long kFlagBadCode = 2ull;   // a STR code outside its code map
+
+// Key word of row p: key_word(), except that a STR code is checked against its
+// code map's length before the map is read (an out-of-range code raises
+// kFlagBadCode and the row is skipped). `cm_len` is 0 when there is no map.
+__device__ __forceinline__ bool na_key_word(const DevCol& c, uint64_t cm_len, uint64_t p, uint64_t& w,
+                                            unsigned long long* acc) {
+  if (c.type == kSTR && c.code_map) {
+    const int32_t code = __ldg(static_cast<const int32_t*>(c.data) + p);
+    if (code < 0 || static_cast<uint64_t>(code) >= cm_len) {
+      atomicOr(acc + 3, kFlagBadCode);
+      return false;
+    }
+    w = static_cast<uint32_t>(__ldg(c.code_map + code));
+    return true;
+  }
+  w = key_word(c, p);
+  return true;
+}
+
 // Counts the build rows of every distinct non-NULL key (key word 0 -> slot kCap).
-__global__ void noalloc_build_kernel(DevCol key, uint64_t n, unsigned long long* keys, uint32_t* cnt,
+__global__ void noalloc_build_kernel(DevCol key, uint64_t cm_len, uint64_t n, unsigned long long* keys, uint32_t* cnt,
                                      unsigned long long* acc) {
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x) {
     if (!col_valid(key, r)) continue;
-    const uint64_t k = key_word(key, r);
+    uint64_t k;
+    if (!na_key_word(key, cm_len, r, k, acc)) continue;
     uint64_t s = kCap;
     if (k != 0) {
       s = slot_hash(k);
@@ -74,7 +98,7 @@ __global__ void noalloc_build_kernel(DevCol key, uint64_t n, unsigned long long*
         s = (s + 1) & (kCap - 1);
       }
       if (t == kCap) {  // cannot happen below the row limit; reported, never hangs
-        atomicOr(acc + 3, 1ull);
+        atomicOr(acc + 3, kFlagOverflow);
         continue;
       }
     }
@@ -82,12 +106,13 @@ __global__ void noalloc_build_kernel(DevCol key, uint64_t n, unsigned long long*
   }
 }
 
-__global__ void noalloc_probe_kernel(DevCol key, DevCol val, uint64_t n, const unsigned long long* keys,
-                                     const uint32_t* cnt, unsigned long long* acc) {
+__global__ void noalloc_probe_kernel(DevCol key, uint64_t cm_len, DevCol val, uint64_t n,
+                                     const unsigned long long* keys, const uint32_t* cnt, unsigned long long* acc) {
   unsigned long long c = 0, sum = 0, seen = 0;
   for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
     if (!col_valid(key, p)) continue;
-    const uint64_t k = key_word(key, p);
+    uint64_t k;
+    if (!na_key_word(key, cm_len, p, k, acc)) continue;
     uint64_t m = 0;
     if (k == 0) {
       m = cnt[kCap];
@@ -136,7 +161,9 @@ DevCol device_column(const qeg_column& c, const char* what) {
   d.all_valid = (c.all_valid || c.validity == nullptr) ? 1 : 0;
   d.data = c.data;
   d.validity = d.all_valid ? nullptr : c.validity;
-  d.code_map = (c.type == QEG_STR) ? c.code_map : nullptr;
+  // As in the allocating path: a STR column's code map is used only when it
+  // has entries.
+  d.code_map = (c.type == QEG_STR && c.code_map != nullptr && c.code_map_len > 0) ? c.code_map : nullptr;
   if (c.len > 0) {
     require(is_device_ptr(c.data), std::string(what) + ": data must be a device pointer (no staging copies here)");
     require(d.all_valid || is_device_ptr(c.validity), std::string(what) + ": validity must be a device pointer");
@@ -180,12 +207,12 @@ qeg_status qeg_join_count_sum_noalloc(void* stream, const qeg_column* build_key,
     const uint64_t nb = build_key->len, np = probe_key->len;
     if (nb > 0) {
       const unsigned g = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((nb + 255) / 256, sms * 8ull)));
-      noalloc_build_kernel<<<g, 256, 0, s>>>(bk, nb, keys, cnt, acc);
+      noalloc_build_kernel<<<g, 256, 0, s>>>(bk, bk.code_map ? build_key->code_map_len : 0, nb, keys, cnt, acc);
       QEG_CUDA(cudaGetLastError());
     }
     if (nb > 0 && np > 0) {
       const unsigned g = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((np + 255) / 256, sms * 8ull)));
-      noalloc_probe_kernel<<<g, 256, 0, s>>>(pk, pv, np, keys, cnt, acc);
+      noalloc_probe_kernel<<<g, 256, 0, s>>>(pk, pk.code_map ? probe_key->code_map_len : 0, pv, np, keys, cnt, acc);
       QEG_CUDA(cudaGetLastError());
     }
     noalloc_result_kernel<<<1, 1, 0, s>>>(acc, out);

@@ -98,6 +98,7 @@ def lib():
             "qeg_join_stats": (i32, [vp, P(i32), P(i32), P(u64)]),
             "qeg_join_destroy": (None, [vp]),
             "qeg_join_count_sum_noalloc": (i32, [vp, vp, vp, vp, vp]),
+            "qeg_ctx_check_bounded_wait": (i32, [vp, i32]),
             "qeg_filter_join_agg": (i32, [vp, vp, c, vp, c, vp, u64, vp, P(u64)]),
             "qeg_sketch": (i32, [vp, vp, u64, vp, P(ctypes.c_double), P(ctypes.c_double)]),
             "qeg_sketch_batch": (i32, [vp, vp, ctypes.c_uint32, vp, u64, vp, vp]),
@@ -208,6 +209,11 @@ class Context:
 
     def synchronize(self):
         _check(lib().qeg_ctx_synchronize(self.p), self.p)
+
+    def check_bounded_wait(self, polls):
+        """Runs the composite-key tables' bounded wait on a row that stays
+        claimed (qeg_ctx_check_bounded_wait); raises QegError(TIMEOUT)."""
+        _check(lib().qeg_ctx_check_bounded_wait(self.p, polls), self.p)
 
     @property
     def launches(self):
