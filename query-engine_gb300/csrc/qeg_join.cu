@@ -35,6 +35,12 @@ namespace qeg {
 namespace {
 
 constexpr uint32_t kNullRow = 0xffffffffu;  // ops/join_internal.h:31
+// Hashed single-key tables of at least this many bytes (too large to stay in
+// L2 beside the probe stream) get a Bloom filter of kBloomBitsPerKey bits per
+// build row: 16 bits and four bits per key in one 64-bit word give a false
+// positive rate of about 0.5%, in 32 MB for 16M build rows.
+constexpr uint64_t kBloomMinTableBytes = 32ull << 20;
+constexpr uint64_t kBloomBitsPerKey = 16;
 
 struct JTable {
   int strategy;    // QEG_JOIN_HASH / QEG_JOIN_DENSE
@@ -49,6 +55,10 @@ struct JTable {
   const uint64_t* bitmap;  // dense and unique: one bit per slot
   int unique;
   int shift;  // hash, single key: home slot = hash >> shift (64 - log2 cap)
+  // Hash, single key: a blocked Bloom filter of the build keys (nullptr: none).
+  // Key hash h selects word h >> bshift and sets the four bits bloom_mask(h).
+  const uint64_t* bloom;
+  int bshift;
 };
 
 __device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t* p) {
@@ -69,6 +79,13 @@ __device__ __forceinline__ uint64_t ld_acquire64(const uint64_t* p) {
 // Slot hash of a key tuple: one splitmix64 round for a single key word, the
 // seeded fold of every word for composite keys.
 __device__ __forceinline__ uint64_t single_key_hash(uint64_t k) { return mix64(k ^ kHashSeed); }
+
+// Bits of a key in its Bloom filter word: four positions from the low 24 bits
+// of the key hash (the word is chosen by its top bits, the table's home slot by
+// its top bits too, so the positions are independent of both).
+__device__ __forceinline__ uint64_t bloom_mask(uint64_t h) {
+  return (1ull << (h & 63)) | (1ull << ((h >> 6) & 63)) | (1ull << ((h >> 12) & 63)) | (1ull << ((h >> 18) & 63));
+}
 
 __device__ __forceinline__ bool load_key(const DevCol* kc, int nk, uint64_t p, uint64_t* w, uint64_t& h) {
   h = kHashSeed;
@@ -142,6 +159,7 @@ struct BuildK {
   uint32_t* dup;
   unsigned long long* distinct;
   uint32_t* err;
+  unsigned long long* bloom;  // single key: the Bloom filter to fill (nullptr: none)
 };
 
 __global__ void build_count_kernel(BuildK P) {
@@ -150,6 +168,7 @@ __global__ void build_count_kernel(BuildK P) {
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t w[kMaxKeys], h;
     if (!load_key(P.key, P.nkeys, r, w, h)) continue;
+    if (P.bloom) atomicOr(P.bloom + (h >> P.T.bshift), static_cast<unsigned long long>(bloom_mask(h)));
     int64_t s;
     if (P.T.strategy == QEG_JOIN_DENSE) {
       s = dense_value(P.key[0], r) - P.T.dmin;
@@ -309,6 +328,80 @@ __device__ __forceinline__ uint64_t sink_lookup(const JTable& T, KT key) {
       g = (g + 4) & (T.cap - 1);
     }
     return 0;
+  }
+}
+
+// Hashed single-key lookup of key word k (nonzero, home slot `home`) whose
+// first 32-byte slot group {a, b} (the aligned group holding the home slot) the
+// caller has already loaded: resolves within it when it can, else walks on.
+template <bool UNIQUE>
+__device__ __forceinline__ uint64_t hashed_resolve(const JTable& T, uint64_t k, uint64_t home, ulonglong2 a,
+                                                   ulonglong2 b) {
+  uint64_t g = home & ~3ull;
+  int skip = static_cast<int>(home & 3);
+  const ulonglong2* base = reinterpret_cast<const ulonglong2*>(T.keys);
+  for (uint64_t t = 0; t < T.cap; t += 4) {
+    if (t) {
+      a = __ldg(base + (g >> 1));
+      b = __ldg(base + (g >> 1) + 1);
+    }
+    const uint64_t c[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i < skip) continue;
+      if (c[i] == k) return UNIQUE ? 1 : __ldg(T.cnt + g + i);
+      if (c[i] == 0) return 0;
+    }
+    skip = 0;
+    g = (g + 4) & (T.cap - 1);
+  }
+  return 0;
+}
+
+// Match multiplicities of two probe keys against a hashed single-key table,
+// with every memory access of the two rows issued before any is consumed: the
+// two Bloom filter words (when the table has a filter), then the first slot
+// group of each row that passed it. kv: the key is non-NULL.
+template <typename KT, bool UNIQUE, bool BLOOM>
+__device__ __forceinline__ void hashed_lookup2(const JTable& T, const KT (&key)[2], const bool (&kv)[2],
+                                               uint64_t (&m)[2]) {
+  uint64_t k[2], h[2];
+  bool go[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    k[j] = sizeof(KT) == 4 ? static_cast<uint64_t>(static_cast<uint32_t>(key[j])) : static_cast<uint64_t>(key[j]);
+    h[j] = single_key_hash(k[j]);
+    go[j] = kv[j];
+  }
+  if (BLOOM) {
+    uint64_t fw[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) fw[j] = go[j] ? __ldg(T.bloom + (h[j] >> T.bshift)) : 0;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const uint64_t bm = bloom_mask(h[j]);
+      go[j] = go[j] && (fw[j] & bm) == bm;
+    }
+  }
+  const ulonglong2* base = reinterpret_cast<const ulonglong2*>(T.keys);
+  ulonglong2 a[2], b[2];
+  uint64_t home[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    home[j] = h[j] >> T.shift;
+    a[j] = make_ulonglong2(0, 0);
+    b[j] = make_ulonglong2(0, 0);
+    if (go[j] && k[j] != 0) {
+      const uint64_t g = home[j] & ~3ull;
+      a[j] = __ldg(base + (g >> 1));
+      b[j] = __ldg(base + (g >> 1) + 1);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    if (!go[j]) m[j] = 0;
+    else if (k[j] == 0) m[j] = __ldg(T.cnt + T.cap);
+    else m[j] = hashed_resolve<UNIQUE>(T, k[j], home[j], a[j], b[j]);
   }
 }
 
@@ -535,7 +628,7 @@ __global__ void __launch_bounds__(256, 4) probe_sink_pipe_kernel(const SinkK P) 
 // per chunk); with PRE the next tile's loads are issued before the current
 // tile's lookups. Tile indexes are 32-bit (the host launches it for fewer
 // than 2^31 tiles).
-template <typename KT, typename VT, int STRAT, bool UNIQUE, int U, bool PRE, int MINB>
+template <typename KT, typename VT, int STRAT, bool UNIQUE, int U, bool PRE, int MINB, bool BLOOM = false>
 __global__ void __launch_bounds__(256, MINB) probe_sink_lean_kernel(const SinkK P) {
   const KT* keys = static_cast<const KT*>(P.key);
   const VT* vals = static_cast<const VT*>(P.val);
@@ -563,30 +656,49 @@ __global__ void __launch_bounds__(256, MINB) probe_sink_lean_kernel(const SinkK 
     }
   };
   auto consume = [&](const KT (&ck)[U][2], const VT (&cv)[U][2], const uint64_t (&ckw)[U], const uint64_t (&cvw)[U]) {
+    if constexpr (STRAT == QEG_JOIN_HASH) {
+      // Hashed table: the lane's two rows of a chunk are looked up together.
 #pragma unroll
-    for (int c = 0; c < U; ++c)
+      for (int c = 0; c < U; ++c) {
+        const bool kv[2] = {((ckw[c] >> (2 * lane)) & 1ull) != 0, ((ckw[c] >> (2 * lane + 1)) & 1ull) != 0};
+        uint64_t m[2];
+        hashed_lookup2<KT, UNIQUE, BLOOM>(P.T, ck[c], kv, m);
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
-        const bool kv = (ckw[c] >> (2 * lane + j)) & 1ull;
-        if (STRAT == QEG_JOIN_DENSE && UNIQUE) {
-          // Branch-free bitmap probe (a select, not a divergent call).
-          const uint64_t s = static_cast<uint64_t>(static_cast<int64_t>(ck[c][j])) - static_cast<uint64_t>(P.T.dmin);
-          const uint32_t hit =
-              (kv && s < P.T.cap) ? static_cast<uint32_t>((__ldg(P.T.bitmap + (s >> 6)) >> (s & 63)) & 1ull) : 0u;
-          cnt += hit;
-          if (hit && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
-            sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j]));
-            seen = 1;
-          }
-        } else {
-          const uint64_t m = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, ck[c][j]) : 0;
-          cnt += static_cast<Cnt>(m);
-          if (m && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
-            sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j])) * m;
+        for (int j = 0; j < 2; ++j) {
+          cnt += static_cast<Cnt>(m[j]);
+          if (m[j] && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
+            sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j])) * m[j];
             seen = 1;
           }
         }
       }
+    } else {
+#pragma unroll
+      for (int c = 0; c < U; ++c)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const bool kv = (ckw[c] >> (2 * lane + j)) & 1ull;
+          if (STRAT == QEG_JOIN_DENSE && UNIQUE) {
+            // Branch-free bitmap probe (a select, not a divergent call).
+            const uint64_t s =
+                static_cast<uint64_t>(static_cast<int64_t>(ck[c][j])) - static_cast<uint64_t>(P.T.dmin);
+            const uint32_t hit =
+                (kv && s < P.T.cap) ? static_cast<uint32_t>((__ldg(P.T.bitmap + (s >> 6)) >> (s & 63)) & 1ull) : 0u;
+            cnt += hit;
+            if (hit && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
+              sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j]));
+              seen = 1;
+            }
+          } else {
+            const uint64_t m = kv ? sink_lookup<KT, STRAT, UNIQUE>(P.T, ck[c][j]) : 0;
+            cnt += static_cast<Cnt>(m);
+            if (m && ((cvw[c] >> (2 * lane + j)) & 1ull)) {
+              sum += static_cast<unsigned long long>(static_cast<int64_t>(cv[c][j])) * m;
+              seen = 1;
+            }
+          }
+        }
+    }
   };
   if (PRE) {
     if (t < ntiles) load_tile(t);
@@ -1650,6 +1762,8 @@ struct JoinState {
   // table
   int strategy = QEG_JOIN_HASH;
   DevBuf keys, cnt, off, rows, bitmap;
+  DevBuf bloom;  // hashed single-key tables larger than kBloomMinTableBytes
+  int bloom_shift = 64;
   uint64_t cap = 0, distinct = 0, nonnull = 0;
   int64_t dmin = 0;
   int unique = 1;
@@ -1697,6 +1811,8 @@ struct JoinState {
     T.rows = rows.get<uint32_t>();
     T.bitmap = bitmap.get<uint64_t>();
     T.unique = unique;
+    T.bloom = bloom.get<uint64_t>();
+    T.bshift = bloom_shift;
     return T;
   }
 
@@ -1979,6 +2095,24 @@ void JoinState::build_hash(BuildK& P) {
   keys.alloc(krows * kw * 8, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(keys.get(), 0, krows * kw * 8, ctx->stream));
   alloc_counts();
+  // A single-key table too large to stay in L2 gets a Bloom filter of
+  // kBloomBitsPerKey bits per build row (an L2-resident word per probe row):
+  // probe keys that miss it skip the table. QEG_JOIN_BLOOM=0 turns it off,
+  // =1 gives every single-key table one (for tests and measurement).
+  bloom.release();
+  bloom_shift = 64;
+  const char* bloom_env = getenv("QEG_JOIN_BLOOM");
+  const int bloom_mode = bloom_env ? atoi(bloom_env) : -1;
+  const bool want_bloom = bloom_mode == 1 || (bloom_mode != 0 && krows * 8 >= kBloomMinTableBytes);
+  if (nk == 1 && !asof && want_bloom) {
+    const uint64_t words = next_pow2(std::max<uint64_t>(64, (nbuild * kBloomBitsPerKey + 63) / 64));
+    int lg = 0;
+    while ((1ull << lg) < words) ++lg;
+    bloom.alloc(words * 8, ctx->stream);
+    QEG_CUDA(cudaMemsetAsync(bloom.get(), 0, words * 8, ctx->stream));
+    bloom_shift = 64 - lg;
+    P.bloom = bloom.get<unsigned long long>();
+  }
   P.T = table();
   if (nbuild) {
     build_count_kernel<<<grid_for(ctx, nbuild, 256, 8), 256, 0, ctx->stream>>>(P);
@@ -2610,6 +2744,10 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       // 16M unique keys in 4.4 ms, against 5.5 ms at 8 CTAs and 5.6 ms for the
       // pipelined kernel. QEG_SINK_PIPE=0|1|2|4|8 picks one for measurement.
       const bool lean_ok = n / 64 < (uint64_t{1} << 31);
+      const bool bloomed = st.bloom.get() != nullptr;
+      // CTAs per SM of the hashed sink (QEG_SINK_HASH_MINB=4|6|8, for measurement).
+      const char* minb_env = getenv("QEG_SINK_HASH_MINB");
+      const int hash_minb = minb_env ? atoi(minb_env) : 6;
       const char* pipe_env = getenv("QEG_SINK_PIPE");
       const int pipe = pipe_env ? atoi(pipe_env) : (lean_ok ? 1 : 2);
       const bool use_tma = n >= static_cast<uint64_t>(kTileRows) * ctx->sms * 2 && al16(S.kvalid) && al16(S.vvalid) &&
@@ -2650,6 +2788,12 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
     } else if (pipe == 1 && lean_ok) {                                                                             \
       if (dense && st.unique) launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_DENSE, true, 1, false, 8>);          \
       else if (dense) launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_DENSE, false, 1, false, 8>);                 \
+      else if (bloomed && st.unique && hash_minb == 4)                                                            \
+        launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_HASH, true, 1, false, 4, true>);                            \
+      else if (bloomed && st.unique && hash_minb == 8)                                                            \
+        launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_HASH, true, 1, false, 8, true>);                            \
+      else if (bloomed && st.unique) launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_HASH, true, 1, false, 6, true>); \
+      else if (bloomed) launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_HASH, false, 1, false, 6, true>);          \
       else if (st.unique) launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_HASH, true, 1, false, 6>);               \
       else launch(probe_sink_lean_kernel<KT, VT, QEG_JOIN_HASH, false, 1, false, 6>);                             \
     } else if (pipe == 4) {                                                                                        \

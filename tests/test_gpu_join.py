@@ -240,6 +240,64 @@ def test_count_sum_sparse_keys_use_hash(ctx):
     j.close()
 
 
+@pytest.mark.parametrize("bloom", ["0", "1"])
+@pytest.mark.parametrize("kt,vt", [(O.I64, O.I64), (O.I32, O.I64), (O.I64, O.I32), (O.I32, O.I32)])
+@pytest.mark.parametrize("dup", [False, True])
+def test_count_sum_hashed_bloom_filter(ctx, bloom, kt, vt, dup, monkeypatch):
+    """The hashed COUNT/SUM sink with (QEG_JOIN_BLOOM=1) and without (=0) the
+    build keys' Bloom filter in front of the table: sparse keys over the whole
+    key width (with key 0 on both sides, which has its own table slot), 2%
+    NULL keys, payload NULLs, duplicated build keys, and probe sides whose
+    length is not a multiple of the 64-row chunk."""
+    monkeypatch.setenv("QEG_JOIN_BLOOM", bloom)
+    rng = np.random.default_rng(7 + kt + 5 * vt + 11 * dup)
+    dt = np.int32 if kt == O.I32 else np.int64
+    nb = 70_001
+    lim = (1 << 31) - 1 if kt == O.I32 else (1 << 62)
+    bkey = rng.integers(-lim, lim, nb).astype(dt)
+    if dup:
+        bkey[nb // 2:] = bkey[: nb - nb // 2]
+    bkey[5] = 0
+    build = O.TCol(kt, bkey, rng.random(nb) >= 0.02)
+    j = qeg.Join(ctx, [kt, vt], [kt], [0], [0], strategy=qeg.JOIN_HASH)
+    j.build([to_gpu(build)])
+    j.build_finish()
+    exp = [0, None]
+    for npr, vnull in ((1_000_003, 0.03), (64 * 999 + 5, 0.0)):
+        pkey = np.where(rng.random(npr) < 0.5, bkey[rng.integers(0, nb, npr)],
+                        rng.integers(-lim, lim, npr).astype(dt)).astype(dt)
+        pkey[:3] = 0
+        pval = rng.integers(-(1 << 30), 1 << 30, npr).astype(np.int32 if vt == O.I32 else np.int64)
+        pk = O.TCol(kt, pkey, rng.random(npr) >= 0.02)
+        pv = O.TCol(vt, pval, (rng.random(npr) >= vnull) if vnull else None)
+        c, sm = O.join_count_sum(pk, pv, build)
+        exp = [exp[0] + c, sm if exp[1] is None else (exp[1] + (sm or 0))]
+        j.probe_count_sum(to_gpu(pk), to_gpu(pv))
+    got = j.count_sum()
+    assert j.stats()["strategy"] == qeg.JOIN_HASH
+    j.close()
+    assert got == tuple(exp)
+
+
+def test_count_sum_bloom_filter_by_table_size(ctx):
+    """Without an override the filter comes with tables of 32 MB or more (here
+    2^21 build rows, a 2^22-slot table): the result is unchanged."""
+    rng = np.random.default_rng(12)
+    nb, npr = 1 << 21, 1 << 22
+    bkey = rng.integers(-(1 << 62), 1 << 62, nb).astype(np.int64)
+    pkey = np.where(rng.random(npr) < 0.5, bkey[rng.integers(0, nb, npr)], rng.integers(-(1 << 62), 1 << 62, npr))
+    pval = rng.integers(0, 1 << 20, npr).astype(np.int64)
+    pvalid = rng.random(npr) >= 0.02
+    exp = O.join_count_sum(O.TCol(O.I64, pkey.astype(np.int64), pvalid), O.TCol(O.I64, pval), O.TCol(O.I64, bkey))
+    j = qeg.Join(ctx, [O.I64, O.I64], [O.I64], [0], [0])
+    j.build([qeg.Col(bkey)])
+    j.build_finish()
+    j.probe_count_sum(qeg.Col(pkey.astype(np.int64), qeg.pack_validity(pvalid)), qeg.Col(pval))
+    assert j.count_sum() == exp
+    assert j.stats()["strategy"] == qeg.JOIN_HASH
+    j.close()
+
+
 @pytest.mark.parametrize("dup", [False, True])
 @pytest.mark.parametrize("ktype", [O.I64, O.I32])
 @pytest.mark.parametrize("bits", [0, 6])
