@@ -420,7 +420,11 @@ def run_agg_bench(args, dev, local, kind=None, emit=True):
         "learned": qeg.agg_config(sizing=qeg.SIZE_LEARNED, hot_keys=-1),
         "plain_fixed": qeg.agg_config(sizing=qeg.SIZE_FIXED, initial_capacity=1 << 20),
         "exact_size": qeg.agg_config(expected_groups=W.groups, hot_keys=-1),
+        # learned sizing held to the private-table strategy (no partitioning)
+        "learned_private": qeg.agg_config(strategy=qeg.AGG_SMEM, sizing=qeg.SIZE_LEARNED, hot_keys=-1),
     }
+    if kind == "agg1m":
+        del variants["learned_private"]
     if args.variants:
         variants = {k: v for k, v in variants.items() if k in args.variants.split(",")}
     out = {}
@@ -1127,6 +1131,27 @@ def run_batch_bench(args, dev, local, emit=True):
     return line
 
 
+def operator_bench(timeout=600):
+    """The drop-in operators through the reference's pull interface
+    (Operator::open/next/close over a Scan of 2048-row host batches, output
+    drained on the host): the 1M-row plain GROUP BY through GpuAggregate and
+    the 16M x 256M join through GpuHashJoin. Runs the C++ driver
+    query-engine_gb300/host/bench_operators.cpp (built by the package build)."""
+    import qeg  # noqa: F401  (loads libqeg.so first)
+    import build as qbuild
+
+    exe = qbuild.build_operator_bench()
+    out = {}
+    for name, argv in (("agg", ["agg", str(1 << 20), "5"]),
+                       ("join", ["join", str(1 << 24), str(1 << 28), "2"])):
+        r = subprocess.run([exe] + argv, capture_output=True, text=True, timeout=timeout)
+        try:
+            out[name] = json.loads(r.stdout.strip().splitlines()[-1])
+        except Exception:
+            out[name] = {"error": (r.stdout + r.stderr)[-500:], "rc": r.returncode}
+    return out
+
+
 def cpu_agg_baseline(W, threads, sample_rows=1 << 23):
     """Times the oracle's port of the reference's morsel-parallel GROUP BY
     (exec/parallel.cpp:402-599, per-worker partial tables and a serial merge)
@@ -1410,9 +1435,12 @@ def main():
         out["skew_agg"] = run_agg_bench(sub, dev, local, kind="skew", emit=False)
         out["batch"] = run_batch_bench(sub, dev, local, emit=False)
         out["pipeline"] = run_pipeline_bench(sub, dev, local, emit=False)
+        out["operators"] = operator_bench()
         fsp = {"join": out["full_size_parity"]}
         for k in ("sparse_keys", "plain_agg", "skew_agg", "batch", "pipeline"):
             fsp[k] = out[k]["full_size_parity"]
+        fsp["operators_agg"] = {"ok": bool(out["operators"].get("agg", {}).get("check_counts_vs_host"))}
+        fsp["operators_join"] = {"ok": bool(out["operators"].get("join", {}).get("check_count_sum_vs_host"))}
         out["full_size_parity_all"] = all(
             v.get("ok", all(x for kk, x in v.items() if kk not in ("expected",) and isinstance(x, bool)))
             for v in fsp.values())

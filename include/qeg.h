@@ -72,6 +72,9 @@ typedef int32_t qeg_status;
 #define QEG_AGG_AUTO 0   /* chosen from the key-column sketch + estimator     */
 #define QEG_AGG_SMEM 1   /* shared-memory private tables + global merge       */
 #define QEG_AGG_GLOBAL 2 /* global-atomic table only                          */
+#define QEG_AGG_PARTITIONED 3 /* single key: private tables, the other rows split
+                                 by key-hash partition and aggregated one
+                                 partition per CTA in shared memory           */
 
 /* Table sizing. */
 #define QEG_SIZE_LEARNED 0 /* capacity from the learned estimator             */
@@ -149,6 +152,12 @@ void* qeg_ctx_stream(qeg_ctx* ctx);
 qeg_status qeg_ctx_synchronize(qeg_ctx* ctx);
 /* Number of kernels this context has launched (for launch accounting). */
 uint64_t qeg_ctx_kernel_launches(const qeg_ctx* ctx);
+/* Page-locked host memory for staging columns and receiving results (no
+ * counterpart in the reference, whose buffers are ordinary aligned heap memory,
+ * core/buffer.cpp:23): copies between it and the device run at the host link's
+ * full speed. `*out` is NULL when bytes == 0. qeg_host_free(NULL) is a no-op. */
+qeg_status qeg_host_alloc(uint64_t bytes, void** out);
+void qeg_host_free(void* p);
 /* Failure-detection check, no counterpart in the reference (whose CPU hash
  * table never waits on another thread; its analogue is the bounded probe of
  * ops/hashtable.h:84-89). Runs the bounded wait that every composite-key table

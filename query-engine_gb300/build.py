@@ -70,5 +70,23 @@ def build(verbose=False, jobs=None):
     return LIB
 
 
+def build_operator_bench():
+    """Compiles the operator benchmark driver (host/bench_operators.cpp with
+    host/gpu_operators.cpp, linked with libqeg.so) into _build/; returns its
+    path. Rebuilt when a source is newer."""
+    lib = build()
+    out = os.path.join(BUILD, "bench_operators")
+    srcs = [os.path.join(HERE, "host", f) for f in ("bench_operators.cpp", "gpu_operators.cpp")]
+    deps = srcs + [os.path.join(HERE, "host", f) for f in ("gpu_operators.h", "qe_contract.h")] + [lib]
+    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
+        return out
+    cmd = ["g++", "-std=c++17", "-O2", "-o", out] + srcs + ["-I" + INCLUDE, "-L" + HERE, "-lqeg",
+                                                          "-Wl,-rpath," + HERE]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("operator bench build failed:\n%s%s" % (r.stdout, r.stderr))
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose=True))

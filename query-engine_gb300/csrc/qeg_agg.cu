@@ -53,6 +53,11 @@ __device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
 
 // Probe length for new keys once the global table is nearly full.
 constexpr int kFullProbe = 16;
+// The partitioned strategy is chosen (QEG_AGG_AUTO) for inputs of at least
+// kPartMinRows rows whose estimated global table would take kPartMinTableBytes
+// or more (half of L2: its random rows would mostly come from DRAM).
+constexpr uint64_t kPartMinRows = 1ull << 22;
+constexpr uint64_t kPartMinTableBytes = 64ull << 20;
 
 __device__ __forceinline__ uint64_t ld_volatile_shared(const uint64_t* p) {
   return *reinterpret_cast<const volatile uint64_t*>(p);
@@ -179,6 +184,45 @@ __device__ __forceinline__ void spill_row(const AggK& P, uint64_t p) {
     P.spill_rows[i] = static_cast<uint32_t>(p);
   else
     atomicOr(P.err, kDevSpillOverflow);
+}
+
+// Row of key word k (nonzero) in a finished single-key table, or nullptr.
+__device__ __forceinline__ uint64_t* find_row1(uint64_t* table, uint64_t cap, int W, uint64_t k) {
+  uint64_t s = __umul64hi(key_hash1(k), cap);
+  for (uint64_t t = 0; t < cap; ++t) {
+    uint64_t* r = table + s * W;
+    const uint64_t cur = r[0];
+    if (cur == k) return r;
+    if (cur == 0) return nullptr;
+    if (++s == cap) s = 0;
+  }
+  return nullptr;
+}
+
+// Partitioned first pass: lanes with `mine` append their row (key word and
+// the values of the NV value columns) to the region of the key's hash
+// partition; lanes of one partition share one reservation. Returns false for
+// a lane whose region is full (the caller spills that row). Every lane of the
+// warp calls it.
+template <int NV>
+__device__ __forceinline__ bool pool_append(const AggK& P, bool mine, uint64_t k, const uint64_t (&vb)[kMaxVals],
+                                            unsigned lane) {
+  const uint32_t part = mine ? static_cast<uint32_t>(key_hash1(k) >> P.part_shift) : 0xffffffffu;
+  const unsigned same = __match_any_sync(0xffffffffu, part);
+  const int first = __ffs(same) - 1;
+  unsigned long long base = 0;
+  if (mine && static_cast<int>(lane) == first)
+    base = atomicAdd(P.part_fill + part, static_cast<unsigned long long>(__popc(same)));
+  base = __shfl_sync(0xffffffffu, base, first);
+  if (!mine) return false;
+  const uint64_t pos = base + static_cast<unsigned>(__popc(same & ((1u << lane) - 1u)));
+  if (pos >= P.part_rows) return false;
+  const uint64_t at = static_cast<uint64_t>(part) * P.part_rows + pos;
+  P.pool_key[at] = k;
+#pragma unroll
+  for (int c = 0; c < NV; ++c)
+    if (c < P.nvals) P.pool_val[c][at] = vb[c];
+  return true;
 }
 
 // Merges one field block `src` (a partial aggregate) into `dst`.
@@ -394,6 +438,7 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       // The leader finds (or places) the group's row.
       uint64_t* f = nullptr;
       int space = kRowGlobal;
+      bool to_pool = false;
       const unsigned long long ins0 = inserted;
       if (leader) {
         const uint64_t h = key_hash1(k);
@@ -407,18 +452,25 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
             f = &sm[srow * SW + 1];
             space = kRowShared;
           }
+        } else if (P.pool_key) {
+          to_pool = true;  // (a NULL key or key word 0 always has its side row)
         } else {
           uint64_t* r = global_row1(P, kv, k, h, inserted, full ? kFullProbe : P.probe_limit);
           if (r) f = r + 1;
         }
       }
+      // Partitioned first pass: every row of a group without a private row
+      // goes to its partition's region.
+      bool pooled = false;
+      if (P.pool_key) {
+        const unsigned pm = __ballot_sync(0xffffffffu, to_pool);
+        if (pm) pooled = pool_append<NV>(P, live && ((pm >> (__ffs(peers) - 1)) & 1u), k, vb, lane);
+      }
       // A group whose row could not be placed spills each of its rows.
       const unsigned placed = __ballot_sync(0xffffffffu, f != nullptr);
       const bool ok = live && ((placed >> (__ffs(peers) - 1)) & 1u);
-      if (live && !ok) {
-        spill_row(P, p);
-        peers = 1u << lane;
-      }
+      if (live && !ok && !pooled) spill_row(P, p);
+      if (live && !ok) peers = 1u << lane;
       const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
       if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader && ok, space, peers, pp, vv, vb);
       else warp_apply<NV>(f, leader && ok, space, peers, pp, P, vv, vb);
@@ -758,6 +810,126 @@ __global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, ui
 
 // Merges spilled partial rows (single-key rows, or composite rows of the
 // composite private tables) into the table.
+// Slot of key word k (nonzero) in a CTA table of S slots (power of two) with
+// row stride SW, inserting it when absent; -1 when more than S / 2 slots are
+// probed (the table is too full).
+__device__ __forceinline__ int part_smem_slot(uint64_t* sm, int S, int SW, uint64_t k, uint64_t h) {
+  uint64_t s = h & (S - 1);
+  for (int t = 0; t < S / 2; ++t) {
+    const uint64_t cur = ld_volatile_shared(&sm[s * SW]);
+    if (cur == k) return static_cast<int>(s);
+    if (cur == 0) {
+      const unsigned long long old =
+          atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * SW]), 0ull, static_cast<unsigned long long>(k));
+      if (old == 0 || old == k) return static_cast<int>(s);
+    }
+    s = (s + 1) & (S - 1);
+  }
+  return -1;
+}
+
+// Partitioned strategy, second pass: each CTA takes partitions in turn and
+// aggregates the partition's pool rows (every key nonzero and non-NULL, every
+// value present) in a shared-memory table with warp peer aggregation, then
+// appends the table's groups to the tail rows with one reservation per CTA and
+// clears the rows it used. A partition with more groups than the table holds
+// is listed as failed and appends nothing (the host aggregates it into the
+// global table instead), so the pass can be re-run with a larger tail buffer.
+template <int NV, uint32_t SPEC>
+__global__ void __launch_bounds__(1024) part_agg_kernel(const AggK P, const PartB B) {
+  extern __shared__ uint64_t sm[];
+  __shared__ int s_fail;
+  __shared__ unsigned long long s_wbase[32];
+  const int W = P.row_words, SW = W | 1, S = B.slots;
+  const unsigned lane = threadIdx.x & 31u;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int i = threadIdx.x; i < S * SW; i += blockDim.x) sm[i] = 0;
+  for (uint32_t part = blockIdx.x; part < B.nparts; part += gridDim.x) {
+    if (threadIdx.x == 0) s_fail = 0;
+    __syncthreads();
+    const uint64_t begin = static_cast<uint64_t>(part) * B.part_rows;
+    const uint64_t fill = B.part_fill[part];
+    const uint64_t n = fill < B.part_rows ? fill : B.part_rows;
+    for (uint64_t b = static_cast<uint64_t>(warp) * 32; b < n; b += static_cast<uint64_t>(nwarps) * 32) {
+      const uint64_t i = b + lane;
+      const bool live = i < n;
+      bool vv[kMaxVals];
+      uint64_t vb[kMaxVals];
+#pragma unroll
+      for (int c = 0; c < kMaxVals; ++c) {
+        vv[c] = false;
+        vb[c] = 0;
+      }
+      uint64_t k = 0;
+      if (live) {
+        k = __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_key + begin + i));
+#pragma unroll
+        for (int c = 0; c < NV; ++c)
+          if (c < P.nvals) {
+            vv[c] = true;
+            vb[c] = __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_val[c] + begin + i));
+          }
+      }
+      const unsigned livemask = __ballot_sync(0xffffffffu, live);
+      const unsigned same = __match_any_sync(0xffffffffu, k);
+      const unsigned peers = live ? (same & livemask) : (1u << lane);
+      const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
+      uint64_t* f = nullptr;
+      if (leader) {
+        const int slot = part_smem_slot(sm, S, SW, k, key_hash1(k));
+        if (slot >= 0) f = &sm[slot * SW + 1];
+        else s_fail = 1;
+      }
+      const unsigned placed = __ballot_sync(0xffffffffu, f != nullptr);
+      const bool ok = live && ((placed >> (__ffs(peers) - 1)) & 1u);
+      const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
+      if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader && ok, kRowShared, peers, pp, vv, vb);
+      else warp_apply<NV>(f, leader && ok, kRowShared, peers, pp, P, vv, vb);
+    }
+    __syncthreads();
+    const bool failed = s_fail != 0;
+    // Groups out: count the occupied slots per warp, one reservation per CTA.
+    unsigned cnt = 0;
+    for (int s0 = warp * 32; s0 < S; s0 += nwarps * 32) {
+      const int s = s0 + static_cast<int>(lane);
+      cnt += __popc(__ballot_sync(0xffffffffu, s < S && sm[s * SW] != 0));
+    }
+    if (lane == 0) s_wbase[warp] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long run = 0;
+      for (int w = 0; w < nwarps; ++w) {
+        const unsigned long long c = s_wbase[w];
+        s_wbase[w] = run;
+        run += c;
+      }
+      unsigned long long base = 0;
+      if (failed) {
+        const unsigned long long fi = atomicAdd(B.counters + 1, 1ull);
+        if (fi < B.nparts) B.failed[fi] = part;
+      } else if (run) {
+        base = atomicAdd(B.counters + 0, run);
+      }
+      for (int w = 0; w < nwarps; ++w) s_wbase[w] += base;
+    }
+    __syncthreads();
+    unsigned long long pos = s_wbase[warp];
+    for (int s0 = warp * 32; s0 < S; s0 += nwarps * 32) {
+      const int s = s0 + static_cast<int>(lane);
+      const bool occ = s < S && sm[s * SW] != 0;
+      const unsigned m = __ballot_sync(0xffffffffu, occ);
+      if (occ) {
+        const unsigned long long o = pos + __popc(m & ((1u << lane) - 1u));
+        if (!failed && o < B.tails_cap)
+          for (int w = 0; w < W; ++w) B.tails[o * W + w] = sm[s * SW + w];
+        for (int w = 0; w < W; ++w) sm[s * SW + w] = 0;
+      }
+      pos += __popc(m);
+    }
+    __syncthreads();
+  }
+}
+
 template <int MODE>
 __global__ void merge_parts_kernel(const AggK P, const uint64_t* __restrict__ parts, uint64_t n) {
   const int W = P.row_words;
@@ -824,6 +996,14 @@ __global__ void __launch_bounds__(1024) finalize_kernel(const AggK P, const FinK
         if (MODE == 0) o = true;
         else if (MODE == 1) o = (sk < P.cap) ? (rk[0] != 0) : (rk[1] != 0);
         else o = rk[0] >= 2;
+        if (MODE == 1 && o && F.merge_table && sk < P.cap) {
+          // The key also has a row in the second table: merge into it there.
+          uint64_t* m = find_row1(F.merge_table, F.merge_cap, W, rk[0]);
+          if (m) {
+            merge_fields(m + 1, rk + 1, P);
+            o = false;
+          }
+        }
       }
       occk[k] = o;
       mk[k] = __ballot_sync(0xffffffffu, o);
@@ -1258,7 +1438,7 @@ void AggState::set_field_columns(AggK& P) const {
 // Zipf(1.1) GROUP BY), 512 otherwise.
 int AggState::block_threads() const {
   if (cfg.block_threads > 0) return cfg.block_threads;
-  return (mode == 1 && strategy == QEG_AGG_SMEM) ? 1024 : 512;
+  return (mode == 1 && (strategy == QEG_AGG_SMEM || strategy == QEG_AGG_PARTITIONED)) ? 1024 : 512;
 }
 
 int AggState::warp_hot() const {
@@ -1434,8 +1614,25 @@ void AggState::consume(const qeg_column* cols, int ncols, const uint32_t* sel, u
   rows_seen += nrows;
   if (nrows == 0) return;
 
+  if (strategy == QEG_AGG_PARTITIONED) {
+    if (part_eligible(staged)) {
+      consume_partitioned(staged, nrows, len, dsel);
+      return;
+    }
+    // A batch the partitioned passes cannot take (NULL values): the groups so
+    // far join the global table and the rest runs the private-table path.
+    merge_tails();
+    strategy = QEG_AGG_SMEM;
+  }
   AggK P = kparams(staged, dsel, nrows, len);
   launch(P, nrows);
+  settle(staged, len);
+}
+
+// After a pass: while rows were spilled (their key found no slot within the
+// probe limit) or private-table rows could not be flushed, grow the global
+// table and replay them.
+void AggState::settle(const std::vector<StagedCol>& staged, uint64_t len) {
   uint64_t c[3];
   read_counters(c);
   check_device_error(ctx);
@@ -1507,6 +1704,19 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
     // estimate that is far too low is caught by overflow -> grow -> replay.
     want = static_cast<uint64_t>(std::max(kEstimateHeadroom * est_groups / kTargetLoad, 1024.0));
   }
+  // Partitioned strategy: asked for, or chosen when the estimate puts the
+  // global table far beyond L2 (every row outside the private tables would be
+  // a random DRAM round trip there). Its global table only takes the private
+  // tables' flushes, so it starts small.
+  bool go_part = false;
+  if (mode == 1 && part_eligible(staged)) {
+    if (cfg.strategy == QEG_AGG_PARTITIONED)
+      go_part = true;
+    else if (cfg.strategy == QEG_AGG_AUTO && nrows >= kPartMinRows && est_groups > 0 &&
+             est_groups / kTargetLoad * row_words * 8.0 >= static_cast<double>(kPartMinTableBytes))
+      go_part = true;
+  }
+  if (go_part) want = next_pow2(2ull * ctx->sms * (2048 + 2));
   alloc_table(want);
   counters.alloc(64, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(counters.get(), 0, 64, ctx->stream));
@@ -1516,7 +1726,7 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   spill_rows.alloc(spill_cap * 4, ctx->stream);
 
   // Strategy.
-  strategy = cfg.strategy;
+  strategy = go_part ? QEG_AGG_SMEM : (cfg.strategy == QEG_AGG_PARTITIONED ? QEG_AGG_AUTO : cfg.strategy);
   // Composite keys: CTA-private tables with periodic flushes when asked for,
   // the global table alone otherwise. (On the 200M-trade (sym, minute) window
   // the private tables measured slower, 39.3 vs 35.3 ms: the ~10k live groups
@@ -1566,6 +1776,179 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
   }
   part_cap = static_cast<uint64_t>(ctx->sms) * 32 * (smem_slots + 2) + 64;
   spill_parts.alloc(part_cap * row_words * 8, ctx->stream);
+  if (go_part && smem_slots > 0) setup_partitioned(nrows);
+}
+
+bool AggState::part_eligible(const std::vector<StagedCol>& staged) const {
+  if (mode != 1 || packed || packable || bucket_width != 0 || staged.size() != types.size()) return false;
+  for (uint32_t v : val_cols) {
+    if (v == keys[0]) return false;  // a key column that is also aggregated keeps its raw values
+    if (!staged[v].dev.all_valid) return false;
+  }
+  return true;
+}
+
+// Partition count and second-pass table size: the largest power-of-two table
+// of shared memory rows one CTA can hold (at most 8192 slots), and enough
+// partitions that each expects about 45% of that many groups.
+void AggState::setup_partitioned(uint64_t nrows) {
+  const size_t rb = static_cast<size_t>(row_words | 1) * 8;
+  pb_slots = 64;
+  while (pb_slots < 8192 && static_cast<size_t>(pb_slots) * 2 * rb <= ctx->smem_optin - 4096) pb_slots *= 2;
+  // Without an estimate the row count bounds the group count.
+  const double g = est_groups > 0 ? est_groups : std::max<double>(1.0, static_cast<double>(nrows));
+  int bits = static_cast<int>(std::ceil(std::log2(std::max(2.0, g / (0.45 * pb_slots)))));
+  if (const char* e = std::getenv("QEG_AGG_PART_BITS")) bits = std::atoi(e);
+  part_bits = std::max(1, std::min(bits, 17));
+  strategy = QEG_AGG_PARTITIONED;
+}
+
+// Region capacity of this batch: the rows expected outside the private tables
+// (1 - the estimator's heavy-hitter share), 1.5 times over per partition; a
+// row past a full region is spilled to the global table.
+void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len,
+                                   const uint32_t* dsel) {
+  if (ntails) merge_tails();  // an earlier batch's groups join the global table
+  const uint64_t np = 1ull << part_bits;
+  const double tail = std::min(1.0, std::max(0.05, 1.0 - hot_share));
+  part_rows = static_cast<uint64_t>(1.5 * tail * static_cast<double>(nrows) / static_cast<double>(np)) + 1024;
+  if (const char* e = std::getenv("QEG_AGG_PART_ROWS")) part_rows = std::max<uint64_t>(1, std::strtoull(e, nullptr, 10));
+  const size_t pool_bytes = np * part_rows * 8;
+  if (pool_key.bytes() < pool_bytes) {
+    pool_key.alloc(pool_bytes, ctx->stream);
+    pool_vals.clear();
+    pool_vals.resize(val_cols.size());
+    for (auto& b : pool_vals) b.alloc(pool_bytes, ctx->stream);
+  }
+  if (part_fill.bytes() < np * 8) part_fill.alloc(np * 8, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(part_fill.get(), 0, np * 8, ctx->stream));
+  AggK P = kparams(staged, dsel, nrows, len);
+  P.pool_key = pool_key.get<uint64_t>();
+  for (size_t c = 0; c < val_cols.size(); ++c) P.pool_val[c] = pool_vals[c].get<uint64_t>();
+  P.part_fill = part_fill.get<unsigned long long>();
+  P.part_rows = part_rows;
+  P.part_shift = 64 - part_bits;
+  launch(P, nrows);
+  settle(staged, len);
+  part_second_pass();
+}
+
+// The pool as kernel columns: key words (I64) and 8-byte values (F64 for F64
+// inputs, I64 for every other type), rows [first, first + n) of the pool.
+static std::vector<StagedCol> pool_columns(const AggState& st, uint64_t first) {
+  std::vector<StagedCol> ps(st.types.size());
+  DevCol k{};
+  k.type = QEG_I64;
+  k.all_valid = 1;
+  k.data = st.pool_key.get<uint64_t>() + first;
+  ps[st.keys[0]].dev = k;
+  for (size_t c = 0; c < st.val_cols.size(); ++c) {
+    DevCol v{};
+    v.type = st.types[st.val_cols[c]] == QEG_F64 ? QEG_F64 : QEG_I64;
+    v.all_valid = 1;
+    v.data = st.pool_vals[c].get<uint64_t>() + first;
+    ps[st.val_cols[c]].dev = v;
+  }
+  return ps;
+}
+
+void AggState::part_second_pass() {
+  const uint64_t np = 1ull << part_bits;
+  AggK P = kparams_base();
+  for (size_t c = 0; c < val_cols.size(); ++c) {
+    P.val[c].type = types[val_cols[c]] == QEG_F64 ? QEG_F64 : QEG_I64;
+    P.val[c].all_valid = 1;
+  }
+  const uint32_t spec = field_spec(P);
+  const int nv = static_cast<int>(val_cols.size());
+  void (*kern)(AggK, PartB) = nullptr;
+  if (spec == kSpecIntF64) kern = part_agg_kernel<2, kSpecIntF64>;
+  else if (spec == kSpecF64) kern = part_agg_kernel<1, kSpecF64>;
+  else if (spec == kSpecCount) kern = part_agg_kernel<1, kSpecCount>;
+  else if (spec == kSpecIntSumF64Stats) kern = part_agg_kernel<2, kSpecIntSumF64Stats>;
+  else if (nv <= 1) kern = part_agg_kernel<1, kGenericSpec>;
+  else if (nv <= 2) kern = part_agg_kernel<2, kGenericSpec>;
+  else if (nv <= 4) kern = part_agg_kernel<4, kGenericSpec>;
+  else kern = part_agg_kernel<8, kGenericSpec>;
+  const int block = 1024;
+  const size_t sb = static_cast<size_t>(pb_slots) * (row_words | 1) * 8;
+  if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+  int per_sm = 0;
+  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
+  require(per_sm > 0, "partitioned aggregate kernel does not fit on an SM");
+  const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(np, static_cast<uint64_t>(ctx->sms) * per_sm));
+  if (!part_counters.get()) part_counters.alloc(16, ctx->stream);
+  if (part_failed.bytes() < np * 4) part_failed.alloc(np * 4, ctx->stream);
+  if (tails_cap == 0) {
+    tails_cap = static_cast<uint64_t>(std::max(1.25 * est_groups, 4096.0));
+    tails.alloc((tails_cap + 2) * row_words * 8, ctx->stream);
+  }
+  PartB B{};
+  B.pool_key = pool_key.get<uint64_t>();
+  for (size_t c = 0; c < val_cols.size(); ++c) B.pool_val[c] = pool_vals[c].get<uint64_t>();
+  B.part_fill = part_fill.get<unsigned long long>();
+  B.part_rows = part_rows;
+  B.nparts = static_cast<uint32_t>(np);
+  B.slots = pb_slots;
+  B.counters = part_counters.get<unsigned long long>();
+  B.failed = part_failed.get<uint32_t>();
+  unsigned long long cnt[2];
+  for (int round = 0;; ++round) {
+    require(round < 4, "partitioned aggregate: tail buffer sizing failed");
+    B.tails = tails.get<uint64_t>();
+    B.tails_cap = tails_cap;
+    QEG_CUDA(cudaMemsetAsync(part_counters.get(), 0, 16, ctx->stream));
+    kern<<<grid, block, sb, ctx->stream>>>(P, B);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+    QEG_CUDA(cudaMemcpyAsync(cnt, part_counters.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (cnt[0] <= tails_cap) break;
+    // More groups than the tail buffer holds: size it to the count and re-run
+    // (the pass only reads the pool).
+    tails_cap = cnt[0] + cnt[0] / 8 + 4096;
+    tails.alloc((tails_cap + 2) * row_words * 8, ctx->stream);
+  }
+  ntails = cnt[0];
+  // Two empty rows after the tails: the finalize pass reads a single-key
+  // table's side rows there.
+  QEG_CUDA(cudaMemsetAsync(tails.get<uint64_t>() + ntails * row_words, 0, 2 * row_words * 8, ctx->stream));
+  const uint64_t nfailed = std::min<uint64_t>(cnt[1], np);
+  if (nfailed) {
+    std::vector<uint32_t> ids(nfailed);
+    QEG_CUDA(cudaMemcpyAsync(ids.data(), part_failed.get(), nfailed * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<unsigned long long> fills(np);
+    QEG_CUDA(cudaMemcpyAsync(fills.data(), part_fill.get(), np * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (uint32_t p : ids) {
+      const uint64_t n = std::min<uint64_t>(fills[p], part_rows);
+      if (n == 0) continue;
+      const std::vector<StagedCol> ps = pool_columns(*this, static_cast<uint64_t>(p) * part_rows);
+      if (n > spill_cap) {
+        spill_cap = n;
+        spill_rows.alloc(spill_cap * 4, ctx->stream);
+      }
+      AggK Q = kparams(ps, nullptr, n, n);
+      launch(Q, n);
+      settle(ps, n);
+    }
+  }
+}
+
+// Moves the tail rows into the global table (grown to hold them).
+void AggState::merge_tails() {
+  if (ntails == 0) return;
+  const uint64_t need = next_pow2(2 * (inserted + ntails));
+  if (cap < need) grow(need);
+  AggK Q = kparams_base();
+  merge_parts_kernel<1><<<grid_for(ctx, ntails, 256, 8), 256, 0, ctx->stream>>>(Q, tails.get<uint64_t>(), ntails);
+  ctx->launches++;
+  QEG_CUDA(cudaGetLastError());
+  uint64_t c[3];
+  read_counters(c);
+  check_device_error(ctx);
+  inserted = c[2];
+  ntails = 0;
 }
 
 void AggState::finish(uint64_t* nrows_out) {
@@ -1578,7 +1961,7 @@ void AggState::finish(uint64_t* nrows_out) {
     std::vector<StagedCol> none;
     first_consume(none, 0, 0, nullptr);
   }
-  const uint64_t out_cap = (mode == 0) ? 1 : std::max<uint64_t>(inserted + 2, 1);
+  const uint64_t out_cap = (mode == 0) ? 1 : std::max<uint64_t>(inserted + 2 + ntails, 1);
   const int ncolsout = static_cast<int>(keys.size() + aggs.size());
   out_vals.clear();
   out_valid.clear();
@@ -1604,6 +1987,19 @@ void AggState::finish(uint64_t* nrows_out) {
   F.out_cap = out_cap;
   F.packed_width = packed ? bucket_width : 0;
   AggK P = kparams_base();
+  if (mode == 1 && ntails > 0) {
+    // Partitioned strategy: the tail rows first, each merged into the global
+    // table instead when its key is there too; then the global table.
+    AggK T = P;
+    T.table = tails.get<uint64_t>();
+    T.cap = ntails;
+    FinK FT = F;
+    FT.merge_table = table.get<uint64_t>();
+    FT.merge_cap = cap;
+    finalize_kernel<1><<<grid_for(ctx, ntails + 2, 1024, 2), 1024, 0, ctx->stream>>>(T, FT);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
   const uint64_t total = (mode == 0) ? 1 : (mode == 1 ? cap + 2 : cap);
   const unsigned g = grid_for(ctx, total, 1024, 2);
   if (mode == 0) finalize_kernel<0><<<g, 1024, 0, ctx->stream>>>(P, F);

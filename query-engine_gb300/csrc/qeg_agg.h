@@ -60,6 +60,32 @@ struct AggK {
   uint32_t* full_flag;           // NULL: no table-full signal
   uint64_t full_at;              // running insert count that raises the flag
   uint32_t* err;
+  // Partitioned strategy, first pass (pool_key != nullptr): a row whose key is
+  // not in its CTA's private table is appended to the region of its key's
+  // hash partition (key word + each value column's 8-byte value) instead of
+  // going to the global table. Region p holds rows [p * part_rows,
+  // (p + 1) * part_rows) of the pool; a row past a full region is spilled.
+  uint64_t* pool_key;
+  uint64_t* pool_val[kMaxVals];
+  unsigned long long* part_fill;  // rows appended per partition (may pass part_rows)
+  uint64_t part_rows;
+  int part_shift;                 // partition of a key = key_hash1(key) >> part_shift
+};
+
+// Parameter block of the partitioned strategy's second pass (part_agg_kernel):
+// one CTA aggregates one partition's pool rows at a time in a shared-memory
+// table and appends its groups, as table rows, to `tails`.
+struct PartB {
+  const uint64_t* pool_key;
+  const uint64_t* pool_val[kMaxVals];
+  const unsigned long long* part_fill;
+  uint64_t part_rows;
+  uint32_t nparts;
+  int slots;                      // shared-memory table slots (power of two)
+  uint64_t* tails;                // row_words words per group
+  uint64_t tails_cap;
+  unsigned long long* counters;   // [0] groups appended (may pass tails_cap), [1] failed partitions
+  uint32_t* failed;               // ids of partitions whose groups did not fit the table
 };
 
 // Parameter block of the finalize kernel.
@@ -74,6 +100,11 @@ struct FinK {
   unsigned long long* out_count;
   uint64_t out_cap;
   int64_t packed_width;  // > 0: single-key rows hold packed (partition key, bucket index) words
+  // Single key: a second table of the same row format (nullptr: none). A row
+  // whose key is also there is merged into that row and not emitted; the
+  // second table is finalized after this one.
+  uint64_t* merge_table;
+  uint64_t merge_cap;
 };
 
 // Key-column sketch: the estimator's inputs and the heavy-hitter candidates.
@@ -138,6 +169,20 @@ struct AggState {
   bool packable = false, packed = false;
   int64_t pack_qmin = 0, pack_qmax = 0;  // bucket-index range of the first packed batch
 
+  // Partitioned strategy (QEG_AGG_PARTITIONED, single key): the first pass
+  // aggregates each CTA's first-come keys in its private table and appends
+  // every other row to its key-hash partition's region of the pool; the second
+  // pass aggregates one partition per CTA in shared memory into `tails`, rows
+  // of the table format. The global table holds the private tables' flushes,
+  // spilled rows and partitions whose groups did not fit; finish() merges tail
+  // rows whose key is also there and emits both.
+  int part_bits = 0;
+  uint64_t part_rows = 0;
+  int pb_slots = 0;
+  DevBuf pool_key, part_fill, part_failed, tails, part_counters;
+  std::vector<DevBuf> pool_vals;
+  uint64_t ntails = 0, tails_cap = 0;
+
   bool finished = false;
   uint64_t nout = 0;
   std::vector<DevBuf> out_vals, out_valid;
@@ -161,6 +206,12 @@ struct AggState {
   void grow(uint64_t new_cap);
   void first_consume(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len, const uint32_t* dsel);
   double estimate_groups(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len, const uint32_t* dsel);
+  void settle(const std::vector<StagedCol>& staged, uint64_t len);
+  bool part_eligible(const std::vector<StagedCol>& staged) const;
+  void setup_partitioned(uint64_t nrows);
+  void consume_partitioned(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len, const uint32_t* dsel);
+  void part_second_pass();
+  void merge_tails();
   void consume(const qeg_column* cols, int ncols, const uint32_t* sel, uint64_t sel_len);
   void finish(uint64_t* nrows_out);
   void fetch(uint64_t first, uint64_t count, const qeg_out_column* outs);

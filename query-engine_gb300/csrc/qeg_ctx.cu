@@ -155,6 +155,13 @@ qeg_status qeg_ctx_create(int device, qeg_ctx** out) {
     c->sms = p.multiProcessorCount;
     c->smem_optin = p.sharedMemPerBlockOptin;
     QEG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    // QEG_L2_FETCH_BYTES (32..128): the largest L2 fetch from DRAM on an L2
+    // miss, a limit of this process's CUDA context (for measuring random
+    // table reads; unset leaves the context's default).
+    if (const char* e = std::getenv("QEG_L2_FETCH_BYTES")) {
+      const size_t v = static_cast<size_t>(std::atoi(e));
+      if (v >= 32 && v <= 128) QEG_CUDA(cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, v));
+    }
     // Keep freed stream-ordered allocations cached in this process's pool, so a
     // query's tables and scratch are re-used instead of re-mapped every call.
     cudaMemPool_t pool;
@@ -201,6 +208,24 @@ qeg_status qeg_ctx_synchronize(qeg_ctx* ctx) {
 }
 
 uint64_t qeg_ctx_kernel_launches(const qeg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+qeg_status qeg_host_alloc(uint64_t bytes, void** out) {
+  return qeg::guarded(nullptr, [&] {
+    qeg::require(out != nullptr, "out is NULL");
+    *out = nullptr;
+    if (bytes == 0) return;
+    const cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      *out = nullptr;
+      throw qeg::Error(QEG_ERR_OOM, std::string("page-locked host allocation: ") + cudaGetErrorString(e));
+    }
+  });
+}
+
+void qeg_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
 
 qeg_status qeg_ctx_check_bounded_wait(qeg_ctx* ctx, int32_t polls) {
   return qeg::guarded(ctx, [&] {

@@ -101,8 +101,11 @@ __device__ __forceinline__ bool load_key(const DevCol* kc, int nk, uint64_t p, u
 __device__ __forceinline__ int64_t dense_value(const DevCol& c, uint64_t p) { return int_value(c, p); }
 
 // Finds (insert = true: or inserts) the slot of a key tuple. -1: absent / full.
+// `existed` (may be null) is set when an insert found the key already there.
+// Key word 0 of a single key has the side slot `cap`, which the caller tracks.
 template <bool INSERT>
-__device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w, uint64_t h, uint32_t* err) {
+__device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w, uint64_t h, uint32_t* err,
+                                             bool* existed = nullptr) {
   if (T.nkeys == 1) {
     const uint64_t k = w[0];
     if (k == 0) return static_cast<int64_t>(T.cap);
@@ -110,10 +113,14 @@ __device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w,
     for (uint64_t t = 0; t < T.cap; ++t) {
       uint64_t* r = T.keys + s;
       uint64_t cur = ld_relaxed64(r);
-      if (cur == k) return static_cast<int64_t>(s);
+      if (cur == k) {
+        if (existed) *existed = true;
+        return static_cast<int64_t>(s);
+      }
       if (cur == 0) {
         if (!INSERT) return -1;
         cur = atomicCAS(reinterpret_cast<unsigned long long*>(r), 0ull, static_cast<unsigned long long>(k));
+        if (cur == k && existed) *existed = true;
         if (cur == 0 || cur == k) return static_cast<int64_t>(s);
       }
       s = (s + 1) & (T.cap - 1);
@@ -141,7 +148,10 @@ __device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w,
     if (st == tag) {
       bool eq = true;
       for (int j = 0; eq && j < T.nkeys; ++j) eq = ld_relaxed64(r + 1 + j) == w[j];
-      if (eq) return static_cast<int64_t>(s);
+      if (eq) {
+        if (existed) *existed = true;
+        return static_cast<int64_t>(s);
+      }
     }
     s = (s + 1) & (T.cap - 1);
   }
@@ -152,6 +162,10 @@ struct BuildK {
   DevCol key[kMaxKeys];
   int nkeys;
   int no_count;  // insert keys only (the as-of join needs no per-slot row counts)
+  // Hash table, counts deferred: the insert itself tells a repeated key (only
+  // key word 0's side slot is counted); per-slot row counts are taken by a
+  // second pass when a probe needs them.
+  int presence;
   uint64_t n;
   JTable T;
   uint32_t* fill;
@@ -167,19 +181,25 @@ __global__ void build_count_kernel(BuildK P) {
   uint32_t dup = 0;
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t w[kMaxKeys], h;
+    bool existed = false;
     if (!load_key(P.key, P.nkeys, r, w, h)) continue;
     if (P.bloom) atomicOr(P.bloom + (h >> P.T.bshift), static_cast<unsigned long long>(bloom_mask(h)));
     int64_t s;
     if (P.T.strategy == QEG_JOIN_DENSE) {
       s = dense_value(P.key[0], r) - P.T.dmin;
     } else {
-      s = hash_slot<true>(P.T, w, h, P.err);
+      s = hash_slot<true>(P.T, w, h, P.err, &existed);
       if (s < 0) {
         atomicOr(P.err, kDevSpillOverflow);
         continue;
       }
     }
     if (P.no_count) continue;
+    if (P.presence && !(P.T.nkeys == 1 && static_cast<uint64_t>(s) == P.T.cap)) {
+      if (existed) dup = 1;
+      else ++fresh;
+      continue;
+    }
     if (atomicAdd(&P.T.cnt[s], 1u) != 0) dup = 1;
     else ++fresh;
   }
@@ -1893,9 +1913,10 @@ struct JoinState {
     QEG_CUDA(cudaMemsetAsync(cnt.get(), 0, slots() * 4, ctx->stream));
   }
   BuildK build_params(DevBuf& scratch);
-  void count_dense();
+  void count_rows();
   void ensure_csr();
   bool csr_built = false;
+  bool counts_ready = false;  // cnt holds every slot's build row count
 };
 
 namespace {
@@ -1993,8 +2014,10 @@ void JoinState::finish_build() {
   distinct = d[1];
   // Dense: the keys are unique when every non-NULL key set its own bit.
   unique = strategy == QEG_JOIN_DENSE ? (distinct == nonnull ? 1 : 0) : ((d[0] & 0xffffffffull) ? 0 : 1);
-  if (strategy == QEG_JOIN_DENSE && !unique && !asof) count_dense();
   csr_built = false;
+  counts_ready = strategy != QEG_JOIN_DENSE && asof;  // (the as-of join reads no counts)
+  // Repeated keys: the sinks read per-slot row counts.
+  if (!unique && !asof) count_rows();
   acc.alloc(24, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(acc.get(), 0, 24, ctx->stream));
   if (asof) asof_build();
@@ -2094,7 +2117,11 @@ void JoinState::build_hash(BuildK& P) {
   const uint64_t krows = nk == 1 ? cap + 1 : cap;
   keys.alloc(krows * kw * 8, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(keys.get(), 0, krows * kw * 8, ctx->stream));
-  alloc_counts();
+  // Row counts are deferred (P.presence): only key word 0's side slot of a
+  // single-key table is counted here.
+  cnt.alloc(slots() * 4, ctx->stream);
+  if (nk == 1) QEG_CUDA(cudaMemsetAsync(cnt.get<uint32_t>() + cap, 0, 4, ctx->stream));
+  P.presence = asof ? 0 : 1;
   // A single-key table too large to stay in L2 gets a Bloom filter of
   // kBloomBitsPerKey bits per build row (an L2-resident word per probe row):
   // probe keys that miss it skip the table. QEG_JOIN_BLOOM=0 turns it off,
@@ -2204,10 +2231,12 @@ BuildK JoinState::build_params(DevBuf& scratch) {
   return P;
 }
 
-// Per-value build row counts of a dense table (needed when keys repeat, and
-// by the pair-materialising probe).
-void JoinState::count_dense() {
+// Per-slot build row counts (needed when keys repeat, and by the
+// pair-materialising probe): a second pass over the build keys, which finds
+// every key's slot (a hash table is complete) and counts its rows.
+void JoinState::count_rows() {
   alloc_counts();
+  counts_ready = true;
   DevBuf scratch;
   BuildK P = build_params(scratch);
   if (nbuild) {
@@ -2222,7 +2251,7 @@ void JoinState::count_dense() {
 // pairs; the COUNT/SUM sink never needs them.
 void JoinState::ensure_csr() {
   if (csr_built) return;
-  if (!cnt.get()) count_dense();
+  if (!counts_ready) count_rows();
   const uint64_t n = slots();
   off.alloc((n + 1) * 8, ctx->stream);
   const uint64_t total = exclusive_scan(ctx, cnt.get<uint32_t>(), n, off.get<uint64_t>());

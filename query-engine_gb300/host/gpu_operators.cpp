@@ -2,6 +2,7 @@
 #include "gpu_operators.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <stdexcept>
@@ -46,10 +47,37 @@ Column HostColumn::view() const {
   return c;
 }
 
+PinnedBuf::~PinnedBuf() {
+  if (pinned_) qeg_host_free(p_);
+  else std::free(p_);
+}
+
+void PinnedBuf::reserve(std::size_t bytes) {
+  if (bytes <= cap_) return;
+  const std::size_t want = std::max<std::size_t>({bytes, cap_ * 2, 4096});
+  void* q = nullptr;
+  bool pinned = qeg_host_alloc(want, &q) == QEG_OK && q != nullptr;
+  if (!pinned) {
+    q = std::malloc(want);
+    if (!q) throw std::bad_alloc();
+  }
+  if (cap_) std::memcpy(q, p_, cap_);
+  if (pinned_) qeg_host_free(p_);
+  else std::free(p_);
+  p_ = static_cast<std::uint8_t*>(q);
+  cap_ = want;
+  pinned_ = pinned;
+}
+
 void Staging::reset(const std::vector<Type>& t) {
-  types = t;
-  vals.assign(t.size(), {});
-  valid.assign(t.size(), {});
+  if (types != t) {
+    types = t;
+    vals.clear();
+    valid.clear();
+    vals.resize(t.size());
+    valid.resize(t.size());
+    code_ids.assign(t.size(), {});
+  }
   any_null.assign(t.size(), false);
   rows = 0;
 }
@@ -58,28 +86,55 @@ void Staging::append(const Batch& b, const std::vector<StringDict*>& ids) {
   const std::size_t n = b.row_count;
   if (n == 0) return;
   const std::size_t new_rows = rows + n;
+  const std::size_t old_words = validity::words(rows), new_words = validity::words(new_rows);
   for (std::size_t c = 0; c < types.size(); ++c) {
     const Column& col = b.cols[c];
     const std::size_t w = byte_width(types[c]);
-    auto& v = vals[c];
-    auto& bits = valid[c];
-    v.resize(new_rows * w);
-    bits.resize(validity::words(new_rows), ~0ull);
-    for (std::size_t k = 0; k < n; ++k) {
-      const uint32_t p = sel_at(b.sel, k);
-      const std::size_t r = rows + k;
-      const bool ok = col.all_valid || validity::get_bit(col.validity, p);
-      if (!ok) {
-        validity::set_bit(bits.data(), r, false);
-        any_null[c] = true;
+    vals[c].reserve(new_rows * w);
+    valid[c].reserve(new_words * 8);
+    auto* bits = reinterpret_cast<std::uint64_t*>(valid[c].data());
+    // Words this batch starts: all valid until a NULL clears a bit.
+    for (std::size_t k = old_words; k < new_words; ++k) bits[k] = ~0ull;
+    std::uint8_t* dst = vals[c].data() + rows * w;
+    if (types[c] == Type::STR) {
+      // Codes -> canonical ids through the dictionary's table.
+      std::vector<std::int32_t>& tab = code_ids[c][col.dict];
+      for (std::size_t code = tab.size(); code < col.dict->size(); ++code)
+        tab.push_back(ids[c]->intern(col.dict->at(static_cast<std::int32_t>(code))));
+      const auto* codes = reinterpret_cast<const std::int32_t*>(col.data);
+      auto* out = reinterpret_cast<std::int32_t*>(dst);
+      for (std::size_t k = 0; k < n; ++k) {
+        const uint32_t p = sel_at(b.sel, k);
+        const bool ok = col.all_valid || validity::get_bit(col.validity, p);
+        const std::int32_t code = ok ? codes[p] : 0;
+        if (ok && (code < 0 || static_cast<std::size_t>(code) >= tab.size()))
+          throw std::invalid_argument("STR code outside its dictionary");
+        out[k] = ok ? tab[code] : 0;
       }
-      if (types[c] == Type::STR) {
-        int32_t id = 0;
-        if (ok) id = ids[c]->intern(col.dict->at(reinterpret_cast<const int32_t*>(col.data)[p]));
-        std::memcpy(v.data() + r * 4, &id, 4);
-      } else {
-        std::memcpy(v.data() + r * w, col.data + static_cast<std::size_t>(p) * w, w);
+    } else if (b.sel == nullptr) {
+      std::memcpy(dst, col.data, n * w);  // a contiguous range: one copy
+    } else {
+      for (std::size_t k = 0; k < n; ++k)
+        std::memcpy(dst + k * w, col.data + static_cast<std::size_t>(b.sel->idx[k]) * w, w);
+    }
+    if (col.all_valid) continue;
+    if (b.sel == nullptr && rows % 64 == 0) {
+      // Word-aligned destination: copy the batch's validity words.
+      const std::size_t nw = validity::words(n);
+      std::uint64_t any = ~0ull;
+      for (std::size_t k = 0; k < nw; ++k) {
+        std::uint64_t v = col.validity[k];
+        if (k + 1 == nw && (n & 63u)) v |= ~0ull << (n & 63u);  // rows past the batch stay valid
+        bits[rows / 64 + k] = v;
+        any &= v;
       }
+      if (any != ~0ull) any_null[c] = true;
+    } else {
+      for (std::size_t k = 0; k < n; ++k)
+        if (!validity::get_bit(col.validity, sel_at(b.sel, k))) {
+          validity::set_bit(bits, rows + k, false);
+          any_null[c] = true;
+        }
     }
   }
   rows = new_rows;
@@ -94,10 +149,44 @@ std::vector<qeg_column> Staging::columns() const {
     q.len = rows;
     q.data = vals[c].data();
     q.all_valid = any_null[c] ? 0 : 1;
-    q.validity = any_null[c] ? valid[c].data() : nullptr;
+    q.validity = any_null[c] ? words(c) : nullptr;
     out[c] = q;
   }
   return out;
+}
+
+void OutColumns::reserve(const std::vector<Type>& t, std::size_t rows) {
+  if (types != t) {
+    types = t;
+    vals.clear();
+    valid.clear();
+    vals.resize(t.size());
+    valid.resize(t.size());
+    dicts.assign(t.size(), nullptr);
+  }
+  all_valid.assign(t.size(), 1);
+  for (std::size_t c = 0; c < t.size(); ++c) {
+    vals[c].reserve(std::max<std::size_t>(1, rows) * byte_width(t[c]));
+    valid[c].reserve(std::max<std::size_t>(1, validity::words(rows)) * 8);
+  }
+}
+
+std::vector<qeg_out_column> OutColumns::outs() {
+  std::vector<qeg_out_column> o(types.size());
+  for (std::size_t c = 0; c < types.size(); ++c)
+    o[c] = {vals[c].data(), reinterpret_cast<std::uint64_t*>(valid[c].data()), &all_valid[c]};
+  return o;
+}
+
+Column OutColumns::view(std::size_t c, std::size_t first, std::size_t n) const {
+  Column v;
+  v.type = types[c];
+  v.len = n;
+  v.data = reinterpret_cast<const std::byte*>(vals[c].data() + first * byte_width(types[c]));
+  v.all_valid = all_valid[c] != 0;
+  v.validity = v.all_valid ? nullptr : reinterpret_cast<const std::uint64_t*>(valid[c].data()) + first / 64;
+  v.dict = dicts[c].get();
+  return v;
 }
 
 Device::Device(int device) {
@@ -227,9 +316,10 @@ void GpuAggregate::open() {
       std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return d.at(a) < d.at(b); });
       std::vector<int32_t> rank(d.size());
       for (std::size_t r = 0; r < order.size(); ++r) rank[order[r]] = static_cast<int32_t>(r);
-      auto* v = reinterpret_cast<int32_t*>(staging_.vals[c].data());
+      std::int32_t* v = staging_.str_ids(c);
+      const std::uint64_t* ok = staging_.words(c);
       for (std::size_t r = 0; r < staging_.rows; ++r)
-        if (validity::get_bit(staging_.valid[c].data(), r)) v[r] = rank[v[r]];
+        if (validity::get_bit(ok, r)) v[r] = rank[v[r]];
       rank_to_id[c] = std::move(order);
     }
   }
@@ -238,33 +328,24 @@ void GpuAggregate::open() {
   dev_->check(qeg_agg_finish(agg_, &n));
   nrows_ = n;
   const Schema out = output_schema();
-  result_.assign(out.fields.size(), {});
-  std::vector<qeg_out_column> outs(out.fields.size());
-  std::vector<int32_t> all_valid(out.fields.size(), 1);
-  for (std::size_t c = 0; c < out.fields.size(); ++c) {
-    HostColumn& h = result_[c];
-    h.type = out.fields[c].second;
-    h.len = nrows_;
-    h.data.resize(std::max<std::size_t>(1, nrows_ * byte_width(h.type)));
-    h.validity.resize(std::max<std::size_t>(1, validity::words(nrows_)));
-    outs[c] = {h.data.data(), h.validity.data(), &all_valid[c]};
-  }
+  std::vector<Type> otypes;
+  for (const auto& f : out.fields) otypes.push_back(f.second);
+  result_.reserve(otypes, nrows_);
+  std::vector<qeg_out_column> outs = result_.outs();
   dev_->check(qeg_agg_fetch(agg_, 0, nrows_, outs.data()));
   // STR results: ranks back to strings, published through an owned dict.
-  out_dicts_.assign(out.fields.size(), nullptr);
   for (std::size_t c = 0; c < out.fields.size(); ++c) {
-    if (all_valid[c]) result_[c].validity.clear();
     if (out.fields[c].second != Type::STR) continue;  // (a window has no STR outputs)
     const std::uint32_t src = c < key_cols_.size() ? key_cols_[c] : aggs_[c - key_cols_.size()].input_col;
     const StringDict& d = *str_ids_[src];
     auto dict = std::make_shared<StringDict>();
-    auto* v = reinterpret_cast<int32_t*>(result_[c].data.data());
+    auto* v = reinterpret_cast<std::int32_t*>(result_.vals[c].data());
+    const auto* ok = reinterpret_cast<const std::uint64_t*>(result_.valid[c].data());
     for (std::size_t r = 0; r < nrows_; ++r) {
-      if (!result_[c].validity.empty() && !validity::get_bit(result_[c].validity.data(), r)) continue;
+      if (!result_.all_valid[c] && !validity::get_bit(ok, r)) continue;
       v[r] = dict->intern(d.at(rank_to_id[src][v[r]]));
     }
-    out_dicts_[c] = dict;
-    result_[c].dict = dict;
+    result_.dicts[c] = dict;
   }
   cursor_ = 0;
 }
@@ -272,28 +353,8 @@ void GpuAggregate::open() {
 std::optional<Batch> GpuAggregate::next() {
   if (cursor_ >= nrows_) return std::nullopt;
   const std::size_t m = std::min(kOutBatch, nrows_ - cursor_);
-  current_.assign(result_.size(), {});
   Batch b;
-  for (std::size_t c = 0; c < result_.size(); ++c) {
-    const HostColumn& src = result_[c];
-    HostColumn& h = current_[c];
-    const std::size_t w = byte_width(src.type);
-    h.type = src.type;
-    h.len = m;
-    h.dict = src.dict;
-    h.data.assign(src.data.begin() + cursor_ * w, src.data.begin() + (cursor_ + m) * w);
-    if (!src.validity.empty()) {
-      h.validity.assign(validity::words(m), ~0ull);
-      bool any = false;
-      for (std::size_t r = 0; r < m; ++r)
-        if (!validity::get_bit(src.validity.data(), cursor_ + r)) {
-          validity::set_bit(h.validity.data(), r, false);
-          any = true;
-        }
-      if (!any) h.validity.clear();
-    }
-    b.cols.push_back(h.view());
-  }
+  for (std::size_t c = 0; c < result_.types.size(); ++c) b.cols.push_back(result_.view(c, cursor_, m));
   b.sel = nullptr;
   b.row_count = m;
   cursor_ += m;
@@ -428,52 +489,57 @@ void GpuHashJoin::open() {
   dev_->check(qeg_join_build_finish(join_));
   probe_stage_.reset(ptypes);
   probe_->open();
+  const Schema out = output_schema();
+  std::vector<Type> otypes;
+  for (const auto& f : out.fields) otypes.push_back(f.second);
+  out_.reserve(otypes, 0);
+  const std::size_t np = probe_schema_.fields.size();
+  for (std::size_t c = 0; c < otypes.size(); ++c)
+    if (otypes[c] == Type::STR) out_.dicts[c] = c < np ? probe_ids_[c] : build_ids_[c - np];
+  pending_ = fetched_ = chunk_ = cursor_ = 0;
 }
 
-bool GpuHashJoin::probe_next_batch() {
-  std::optional<Batch> b = probe_->next();
-  if (!b) return false;
+// Stages up to kProbeRows probe rows (whole batches) and probes them in one
+// call. False when the probe child is exhausted.
+bool GpuHashJoin::probe_next_chunk() {
   std::vector<StringDict*> pids(probe_stage_.types.size(), nullptr);
   for (std::size_t c = 0; c < pids.size(); ++c) pids[c] = probe_ids_[c].get();
   probe_stage_.reset(probe_stage_.types);
-  probe_stage_.append(*b, pids);
+  while (probe_stage_.rows < kProbeRows) {
+    std::optional<Batch> b = probe_->next();
+    if (!b) break;
+    probe_stage_.append(*b, pids);
+  }
+  if (probe_stage_.rows == 0) return false;
   const auto cols = probe_stage_.columns();
   uint64_t n = 0;
   dev_->check(qeg_join_probe(join_, cols.data(), static_cast<int>(cols.size()), &n));
   pending_ = n;
-  cursor_ = 0;
+  fetched_ = chunk_ = cursor_ = 0;
   return true;
 }
 
 std::optional<Batch> GpuHashJoin::next() {
-  while (cursor_ >= pending_) {
-    if (probe_done_ || !probe_next_batch()) {
+  while (cursor_ >= chunk_) {
+    if (fetched_ < pending_) {
+      // The next kFetchRows output rows into the page-locked chunk.
+      const std::uint64_t cnt = std::min<std::uint64_t>(kFetchRows, pending_ - fetched_);
+      out_.reserve(out_.types, cnt);
+      std::vector<qeg_out_column> outs = out_.outs();
+      dev_->check(qeg_join_fetch(join_, fetched_, cnt, outs.data()));
+      fetched_ += cnt;
+      chunk_ = cnt;
+      cursor_ = 0;
+      continue;
+    }
+    if (probe_done_ || !probe_next_chunk()) {
       probe_done_ = true;
       return std::nullopt;
     }
   }
-  const std::size_t m = std::min<std::uint64_t>(kOutBatch, pending_ - cursor_);
-  const Schema out = output_schema();
-  current_.assign(out.fields.size(), {});
-  std::vector<qeg_out_column> outs(out.fields.size());
-  std::vector<int32_t> all_valid(out.fields.size(), 1);
-  for (std::size_t c = 0; c < out.fields.size(); ++c) {
-    HostColumn& h = current_[c];
-    h.type = out.fields[c].second;
-    h.len = m;
-    h.data.resize(std::max<std::size_t>(1, m * byte_width(h.type)));
-    h.validity.resize(validity::words(m));
-    outs[c] = {h.data.data(), h.validity.data(), &all_valid[c]};
-  }
-  dev_->check(qeg_join_fetch(join_, cursor_, m, outs.data()));
+  const std::size_t m = std::min<std::uint64_t>(kOutBatch, chunk_ - cursor_);
   Batch b;
-  const std::size_t np = probe_schema_.fields.size();
-  for (std::size_t c = 0; c < out.fields.size(); ++c) {
-    HostColumn& h = current_[c];
-    if (all_valid[c]) h.validity.clear();
-    if (h.type == Type::STR) h.dict = c < np ? probe_ids_[c] : build_ids_[c - np];
-    b.cols.push_back(h.view());
-  }
+  for (std::size_t c = 0; c < out_.types.size(); ++c) b.cols.push_back(out_.view(c, cursor_, m));
   b.sel = nullptr;
   b.row_count = m;
   cursor_ += m;

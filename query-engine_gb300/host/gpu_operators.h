@@ -4,29 +4,38 @@
 // same constructor arguments, same output schema and column order, same
 // Batch/Column views; the work runs in libqeg.so (include/qeg.h).
 //
-//   GpuAggregate  open() drains the child into pinned host staging (selection
-//                 vectors applied, STR canonicalised by value), hands it to
-//                 the GPU in chunks, finishes; next() emits <= 2048 groups per
-//                 batch, keys then aggregates (ops/aggregate.cpp:439-493).
+//   GpuAggregate  open() drains the child into page-locked host staging
+//                 (selection vectors applied, contiguous ranges copied in
+//                 bulk, STR codes canonicalised by value through a table built
+//                 once per dictionary), hands it to the GPU in chunks of
+//                 kChunkRows, finishes and fetches the whole result into
+//                 page-locked memory; next() emits <= 2048 groups per batch as
+//                 views into it, keys then aggregates (ops/aggregate.cpp:439-493).
 //   GpuHashJoin   open() drains the build child into the GPU build store and
-//                 builds the table; next() probes one probe batch at a time
-//                 and emits <= 2048 output rows per batch, probe columns then
-//                 build columns (ops/join.cpp:260-299).
+//                 builds the table; next() probes kProbeRows staged probe rows
+//                 per GPU call, fetches the output kFetchRows at a time into
+//                 page-locked memory and emits <= 2048 output rows per batch as
+//                 views into it, probe columns then build columns
+//                 (ops/join.cpp:260-299).
 //   GpuWindow     qe::tsx::Window (tsx/window.h:82-100) in Tumbling mode: a
 //                 GpuAggregate over (keys..., bucket start of the time
 //                 column), output [keys..., bucket_start, aggregates...].
 //   GpuAsofJoin   qe::tsx::AsofJoin (tsx/asof.h:94-150): a GpuHashJoin whose
 //                 build side is sorted by (key, time) on the GPU and whose
 //                 probe takes the nearest preceding build row per probe row.
+// A returned Batch's views stay valid until the next next() or close(), as
+// ops/operator.h:14-22 requires.
 // Errors surface as the reference's exception types: std::invalid_argument,
 // std::overflow_error, std::bad_alloc, std::runtime_error otherwise.
 #pragma once
 
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <optional>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/qeg.h"
@@ -45,19 +54,67 @@ struct HostColumn {
   Column view() const;
 };
 
-// Host staging of rows pulled from a child: contiguous values and a packed
-// validity bitmap per column, STR values canonicalised by value into ids.
+// Page-locked host bytes (qeg_host_alloc), grown by doubling with their
+// contents kept; ordinary heap memory where page-locked memory is refused.
+class PinnedBuf {
+ public:
+  PinnedBuf() = default;
+  ~PinnedBuf();
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  PinnedBuf(PinnedBuf&& o) noexcept { swap(o); }
+  PinnedBuf& operator=(PinnedBuf&& o) noexcept {
+    swap(o);
+    return *this;
+  }
+  void reserve(std::size_t bytes);  // capacity >= bytes, contents kept
+  std::uint8_t* data() const { return p_; }
+  std::size_t capacity() const { return cap_; }
+
+ private:
+  void swap(PinnedBuf& o) noexcept {
+    std::swap(p_, o.p_);
+    std::swap(cap_, o.cap_);
+    std::swap(pinned_, o.pinned_);
+  }
+  std::uint8_t* p_ = nullptr;
+  std::size_t cap_ = 0;
+  bool pinned_ = false;
+};
+
+// Host staging of rows pulled from a child, in page-locked memory: contiguous
+// values and a packed validity bitmap per column. STR codes become canonical
+// ids through a code -> id table built once per source dictionary (extended
+// when the dictionary grows), not by interning every row.
 struct Staging {
   std::vector<Type> types;
-  std::vector<std::vector<std::uint8_t>> vals;
-  std::vector<std::vector<std::uint64_t>> valid;
+  std::vector<PinnedBuf> vals;
+  std::vector<PinnedBuf> valid;  // validity words
   std::vector<bool> any_null;
   std::size_t rows = 0;
-  void reset(const std::vector<Type>& t);
+  // Per column: source dictionary -> id of each of its codes.
+  std::vector<std::map<const StringDict*, std::vector<std::int32_t>>> code_ids;
+  void reset(const std::vector<Type>& t);  // empties the rows, keeps buffers and code tables
   // Appends the logical rows of `b`; STR columns go through `ids[c]` (value ->
   // canonical id; nullptr for non-STR columns).
   void append(const Batch& b, const std::vector<StringDict*>& ids);
   std::vector<qeg_column> columns() const;
+  std::int32_t* str_ids(std::size_t c) { return reinterpret_cast<std::int32_t*>(vals[c].data()); }
+  const std::uint64_t* words(std::size_t c) const { return reinterpret_cast<const std::uint64_t*>(valid[c].data()); }
+};
+
+// Output columns fetched from the GPU into page-locked memory; next() hands
+// out views of 2048-row slices (slice starts are multiples of 64, so a slice's
+// validity is the words from start / 64 on).
+struct OutColumns {
+  std::vector<Type> types;
+  std::vector<PinnedBuf> vals;
+  std::vector<PinnedBuf> valid;
+  std::vector<std::int32_t> all_valid;
+  std::vector<std::shared_ptr<const StringDict>> dicts;
+  void reserve(const std::vector<Type>& t, std::size_t rows);
+  std::vector<qeg_out_column> outs();
+  Column view(std::size_t c, std::size_t first, std::size_t n) const;
 };
 
 // One CUDA context per operator instance: operators are single-threaded
@@ -113,16 +170,16 @@ class GpuAggregate : public Operator {
   Staging staging_;
   bool has_str_ = false;
   std::vector<std::shared_ptr<StringDict>> str_ids_;  // per child column, STR only
-  std::vector<HostColumn> result_;                    // full result, keys then aggs
-  std::vector<std::shared_ptr<StringDict>> out_dicts_;
+  OutColumns result_;                                  // full result, keys then aggs
   std::size_t nrows_ = 0, cursor_ = 0;
-  std::vector<HostColumn> current_;
   bool opened_ = false;
 };
 
 class GpuHashJoin : public Operator {
  public:
-  static constexpr std::size_t kOutBatch = 2048;  // ops/join.h:73
+  static constexpr std::size_t kOutBatch = 2048;        // ops/join.h:73
+  static constexpr std::size_t kProbeRows = 8u << 20;   // probe rows staged per GPU probe call
+  static constexpr std::size_t kFetchRows = 1u << 20;   // output rows fetched per GPU call
 
   GpuHashJoin(std::unique_ptr<Operator> probe, std::unique_ptr<Operator> build, std::vector<std::uint32_t> probe_keys,
               std::vector<std::uint32_t> build_keys, JoinType type, qeg_join_config cfg = {}, int device = 0);
@@ -141,7 +198,7 @@ class GpuHashJoin : public Operator {
               tsx::AsofType type, std::optional<std::int64_t> tolerance, int device);
 
  private:
-  bool probe_next_batch();
+  bool probe_next_chunk();
 
   bool asof_ = false;
   std::uint32_t probe_time_ = 0, build_time_ = 0;
@@ -157,8 +214,11 @@ class GpuHashJoin : public Operator {
   qeg_join* join_ = nullptr;
   std::vector<std::shared_ptr<StringDict>> probe_ids_, build_ids_;  // STR columns
   Staging probe_stage_;
-  std::uint64_t pending_ = 0, cursor_ = 0;
-  std::vector<HostColumn> current_;
+  std::uint64_t pending_ = 0;   // output rows of the last probe call
+  std::uint64_t fetched_ = 0;   // of which fetched into out_
+  std::uint64_t chunk_ = 0;     // rows in out_
+  std::uint64_t cursor_ = 0;    // next row of out_ to emit
+  OutColumns out_;
   bool opened_ = false, probe_done_ = false;
 };
 

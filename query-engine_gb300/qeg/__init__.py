@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "libqeg.so")
 I32, I64, F64, BOOL, TS, STR = 0, 1, 2, 3, 4, 5
 COUNT_STAR, COUNT, SUM, MIN, MAX, AVG = 0, 1, 2, 3, 4, 5
 INNER, LEFT = 0, 1
-AGG_AUTO, AGG_SMEM, AGG_GLOBAL = 0, 1, 2
+AGG_AUTO, AGG_SMEM, AGG_GLOBAL, AGG_PARTITIONED = 0, 1, 2, 3
 SIZE_LEARNED, SIZE_FIXED = 0, 1
 JOIN_AUTO, JOIN_HASH, JOIN_PARTITIONED, JOIN_DENSE = 0, 1, 2, 3
 

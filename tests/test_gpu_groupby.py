@@ -230,3 +230,137 @@ def test_composite_keys_private_tables_with_flushes(ctx, slots, cap):
     ot, orows = O.groupby([k1, k2, v1, v2], [0, 1], aggs, 1 << 20)
     gt, grows = run_gpu(ctx, [k1, k2, v1, v2], [0, 1], aggs, config=cfg)
     assert_same(gt, grows, ot, orows, "slots %d cap %d" % (slots, cap))
+
+
+def _zipf_rows(rng, n, dom, s):
+    w = np.arange(1, dom + 1, dtype=np.float64) ** -s
+    cdf = np.cumsum(w)
+    cdf /= cdf[-1]
+    return np.minimum(np.searchsorted(cdf, rng.random(n)), dom - 1).astype(np.int64)
+
+
+@pytest.mark.parametrize("case", ["i64_skew", "i32_uniform", "f64_keys", "str_keys", "few_parts_fail",
+                                  "tiny_regions", "sel", "hot_preload", "count_only", "generic_fields"])
+def test_partitioned_strategy(ctx, case, monkeypatch):
+    """The partitioned GROUP BY (QEG_AGG_PARTITIONED): private tables in the
+    first pass, every other row to its key-hash partition's region, one
+    partition per CTA in shared memory in the second pass, tail rows merged
+    with the global table at finalize. Cases: skewed and uniform keys, F64
+    keys (-0.0 / NaN canonicalised), STR keys through a code map, NULL keys and
+    key 0 (side rows), 2 partitions of many groups (second-pass tables too
+    full: those partitions go to the global table), regions of 64 rows (rows
+    past them spill), a selection vector, preloaded heavy hitters, COUNT(*)
+    alone, and a field set without a specialised kernel."""
+    cases = ["i64_skew", "i32_uniform", "f64_keys", "str_keys", "few_parts_fail", "tiny_regions", "sel",
+             "hot_preload", "count_only", "generic_fields"]
+    rng = np.random.default_rng(900 + cases.index(case))
+    n = 300_000
+    aggs = [(O.COUNT_STAR, 0), (O.SUM, 1), (O.SUM, 2), (O.MIN, 1), (O.MAX, 1), (O.AVG, 2)]
+    kvalid = rng.random(n) > 0.02
+    sel = None
+    cfg = qeg.agg_config(strategy=qeg.AGG_PARTITIONED)
+    canon = None
+    if case == "i64_skew":
+        key = O.TCol(O.I64, _zipf_rows(rng, n, 100_000, 1.1) * 0x9E3779B97F4A7C1 - 12345, kvalid)
+        key.values[:50] = 0
+    elif case == "i32_uniform":
+        key = O.TCol(O.I32, rng.integers(-(1 << 30), 1 << 30, n).astype(np.int32) % 40_000, kvalid)
+    elif case == "f64_keys":
+        vals = rng.integers(0, 20_000, n).astype(np.float64) - 10_000.5
+        vals[::97] = -0.0
+        vals[1::97] = 0.0
+        vals[2::89] = np.nan
+        key = O.TCol(O.F64, vals, kvalid)
+    elif case == "str_keys":
+        d = ["S%05d" % i for i in range(30_000)]
+        key = O.TCol(O.STR, rng.integers(0, len(d), n).astype(np.int32), kvalid, d)
+        aggs = [(O.COUNT_STAR, 0), (O.SUM, 1), (O.MAX, 1), (O.MIN, 2)]
+    elif case == "few_parts_fail":
+        monkeypatch.setenv("QEG_AGG_PART_BITS", "1")
+        key = O.TCol(O.I64, rng.integers(0, 60_000, n).astype(np.int64), kvalid)
+    elif case == "tiny_regions":
+        monkeypatch.setenv("QEG_AGG_PART_ROWS", "64")
+        key = O.TCol(O.I64, rng.integers(0, 50_000, n).astype(np.int64), kvalid)
+    elif case == "sel":
+        key = O.TCol(O.I64, rng.integers(0, 50_000, n).astype(np.int64), kvalid)
+        sel = np.sort(rng.choice(n, n // 3, replace=False)).astype(np.uint32)
+    elif case == "hot_preload":
+        key = O.TCol(O.I64, _zipf_rows(rng, n, 80_000, 1.2), kvalid)
+        cfg = qeg.agg_config(strategy=qeg.AGG_PARTITIONED, hot_keys=64, expected_groups=60_000)
+    elif case == "count_only":
+        key = O.TCol(O.I64, rng.integers(0, 70_000, n).astype(np.int64), kvalid)
+        aggs = [(O.COUNT_STAR, 0)]
+    else:  # generic_fields: three value columns
+        key = O.TCol(O.I64, rng.integers(0, 45_000, n).astype(np.int64), kvalid)
+        aggs = [(O.COUNT_STAR, 0), (O.SUM, 1), (O.MIN, 2), (O.MAX, 3), (O.AVG, 3), (O.COUNT, 1)]
+    v1 = O.TCol(O.I64, rng.integers(-(1 << 31), 1 << 31, n).astype(np.int64))
+    v2 = O.TCol(O.F64, rng.normal(0, 1e3, n))
+    cols = [key, v1, v2]
+    if case == "generic_fields":
+        cols.append(O.TCol(O.I32, rng.integers(-1000, 1000, n).astype(np.int32)))
+    if case == "str_keys":
+        canon = StrCanon(key.dictionary)
+    sub = cols if sel is None else [O.TCol(c.type, c.values[sel], None if c.valid is None else c.valid[sel],
+                                           c.dictionary) for c in cols]
+    ot, orows = O.groupby(sub, [0], aggs, 1 << 20)
+    gcols = [to_gpu(c, canon) for c in cols]
+    a = qeg.Aggregate(ctx, [c.type for c in gcols], [0], aggs, cfg)
+    a.consume(gcols, sel)
+    a.finish()
+    st = a.stats()
+    res = a.fetch()
+    types = a.result_types
+    a.close()
+    assert st["strategy"] == qeg.AGG_PARTITIONED, st
+    gt, grows = gpu_rows(res, types, canon)
+    assert_same(gt, grows, ot, orows, case)
+
+
+def test_partitioned_strategy_multiple_batches_and_null_values(ctx):
+    """Several consume() calls: each batch's partitioned passes run after the
+    previous batch's tail rows moved into the global table; a batch with NULL
+    values ends the partitioned passes (its rows take the private-table path)."""
+    rng = np.random.default_rng(77)
+    aggs = [(O.COUNT_STAR, 0), (O.SUM, 1), (O.COUNT, 2), (O.AVG, 2), (O.MIN, 1)]
+    batches = []
+    for b in range(4):
+        n = 120_000 + 64 * b
+        key = O.TCol(O.I64, rng.integers(0, 60_000, n).astype(np.int64), rng.random(n) > 0.01)
+        v1 = O.TCol(O.I64, rng.integers(-1000, 1000, n).astype(np.int64))
+        v2 = O.TCol(O.F64, rng.normal(0, 1, n), (rng.random(n) > 0.2) if b == 2 else None)
+        batches.append([key, v1, v2])
+    whole = [O.TCol(t, np.concatenate([bt[i].values for bt in batches]),
+                    np.concatenate([bt[i].valid if bt[i].valid is not None else np.ones(bt[i].n, bool)
+                                    for bt in batches]))
+             for i, t in enumerate([O.I64, O.I64, O.F64])]
+    ot, orows = O.groupby(whole, [0], aggs, 1 << 20)
+    a = qeg.Aggregate(ctx, [O.I64, O.I64, O.F64], [0], aggs, qeg.agg_config(strategy=qeg.AGG_PARTITIONED))
+    for bt in batches:
+        a.consume([to_gpu(c) for c in bt])
+    a.finish()
+    res = a.fetch()
+    types = a.result_types
+    a.close()
+    gt, grows = gpu_rows(res, types)
+    assert_same(gt, grows, ot, orows)
+
+
+def test_partitioned_strategy_chosen_for_large_tables(ctx):
+    """QEG_AGG_AUTO takes the partitioned strategy when the estimated global
+    table is far larger than L2 (8M rows over ~6M keys): results unchanged."""
+    rng = np.random.default_rng(5)
+    n = 8 << 20
+    key = O.TCol(O.I64, rng.integers(0, 6_000_000, n).astype(np.int64) * 7919)
+    v = O.TCol(O.F64, rng.uniform(-1, 1, n))
+    aggs = [(O.COUNT_STAR, 0), (O.SUM, 1), (O.MAX, 1)]
+    ot, orows = O.groupby([key, v], [0], aggs, 1 << 23)
+    a = qeg.Aggregate(ctx, [O.I64, O.F64], [0], aggs, qeg.agg_config(sizing=qeg.SIZE_LEARNED))
+    a.consume([to_gpu(key), to_gpu(v)])
+    a.finish()
+    st = a.stats()
+    res = a.fetch()
+    types = a.result_types
+    a.close()
+    assert st["strategy"] == qeg.AGG_PARTITIONED, st
+    gt, grows = gpu_rows(res, types)
+    assert_same(gt, grows, ot, orows)
