@@ -201,8 +201,7 @@ __device__ __forceinline__ uint64_t* find_row1(uint64_t* table, uint64_t cap, in
 
 // Partitioned first pass: lanes with `mine` append their row (key word and
 // the values of the NV value columns) to the region of the key's hash
-// partition; lanes of one partition share one reservation. Returns false for
-// a lane whose region is full (the caller spills that row). Every lane of the
+// partition; lanes of one partition share one reservation. Every lane of the
 // warp calls it.
 template <int NV>
 __device__ __forceinline__ bool pool_append(const AggK& P, bool mine, uint64_t k, const uint64_t (&vb)[kMaxVals],
@@ -215,9 +214,8 @@ __device__ __forceinline__ bool pool_append(const AggK& P, bool mine, uint64_t k
     base = atomicAdd(P.part_fill + part, static_cast<unsigned long long>(__popc(same)));
   base = __shfl_sync(0xffffffffu, base, first);
   if (!mine) return false;
-  const uint64_t pos = base + static_cast<unsigned>(__popc(same & ((1u << lane) - 1u)));
-  if (pos >= P.part_rows) return false;
-  const uint64_t at = static_cast<uint64_t>(part) * P.part_rows + pos;
+  const uint64_t at = P.part_off[part] + base + static_cast<unsigned>(__popc(same & ((1u << lane) - 1u)));
+  if (at >= P.part_off[part + 1]) return false;  // (the histogram pass sized every region exactly)
   P.pool_key[at] = k;
 #pragma unroll
   for (int c = 0; c < NV; ++c)
@@ -810,6 +808,64 @@ __global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, ui
 
 // Merges spilled partial rows (single-key rows, or composite rows of the
 // composite private tables) into the table.
+// Partitioned strategy, sizing pass: rows per key-hash partition of every row
+// the first pass will append to the pool -- a non-NULL key other than key word
+// 0 that is not one of the preloaded heavy hitters (the same set the first
+// pass holds in its read-only private table; membership is exact there too).
+// Per CTA: the heavy hitters in a shared-memory key table of S slots, then
+// 32-bit partition counters, added to `hist` at the end.
+__global__ void __launch_bounds__(1024) part_hist_kernel(const AggK P, unsigned long long* hist) {
+  extern __shared__ uint64_t hs[];
+  const int S = P.smem_slots;
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(hs + S);
+  const uint32_t np = 1u << (64 - P.part_shift);
+  for (int i = threadIdx.x; i < S; i += blockDim.x) hs[i] = 0;
+  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) cnt[i] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < P.nhot; i += blockDim.x) {
+    const uint64_t k = P.hot[i];
+    if (k == 0) continue;
+    uint64_t s = key_hash1(k) & (S - 1);
+    for (int t = 0; t < S; ++t) {
+      const unsigned long long old =
+          atomicCAS(reinterpret_cast<unsigned long long*>(&hs[s]), 0ull, static_cast<unsigned long long>(k));
+      if (old == 0 || old == k) break;
+      s = (s + 1) & (S - 1);
+    }
+  }
+  __syncthreads();
+  const DevCol& kc = P.key[0];
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < P.nrows;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    uint64_t p = i;
+    if (P.sel) {
+      p = P.sel[i];
+      if (p >= P.len) continue;  // (the first pass reports it)
+    }
+    if (!col_valid(kc, p)) continue;
+    const uint64_t k = key_word(kc, p);
+    if (k == 0) continue;
+    const uint64_t h = key_hash1(k);
+    bool hot = false;
+    if (P.nhot > 0) {
+      uint64_t s = h & (S - 1);
+      for (int t = 0; t < S; ++t) {
+        const uint64_t cur = hs[s];
+        if (cur == k) {
+          hot = true;
+          break;
+        }
+        if (cur == 0) break;
+        s = (s + 1) & (S - 1);
+      }
+    }
+    if (!hot) atomicAdd(&cnt[h >> P.part_shift], 1u);
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
+    if (cnt[i]) atomicAdd(hist + i, static_cast<unsigned long long>(cnt[i]));
+}
+
 // Slot of key word k (nonzero) in a CTA table of S slots (power of two) with
 // row stride SW, inserting it when absent; -1 when more than S / 2 slots are
 // probed (the table is too full).
@@ -847,9 +903,8 @@ __global__ void __launch_bounds__(1024) part_agg_kernel(const AggK P, const Part
   for (uint32_t part = blockIdx.x; part < B.nparts; part += gridDim.x) {
     if (threadIdx.x == 0) s_fail = 0;
     __syncthreads();
-    const uint64_t begin = static_cast<uint64_t>(part) * B.part_rows;
-    const uint64_t fill = B.part_fill[part];
-    const uint64_t n = fill < B.part_rows ? fill : B.part_rows;
+    const uint64_t begin = B.part_off[part];
+    const uint64_t n = B.part_off[part + 1] - begin;
     for (uint64_t b = static_cast<uint64_t>(warp) * 32; b < n; b += static_cast<uint64_t>(nwarps) * 32) {
       const uint64_t i = b + lane;
       const bool live = i < n;
@@ -1392,7 +1447,9 @@ AggK AggState::kparams(const std::vector<StagedCol>& staged, const uint32_t* sel
       const char* e = std::getenv("QEG_AGG_SMEM_PROBE");
       return e ? std::max(1, std::min(64, std::atoi(e))) : 8;
     }();
-    P.smem_probe = probe;
+    // The partitioned strategy's read-only private table: exact membership
+    // (the sizing pass counts exactly the rows that miss it).
+    P.smem_probe = (strategy == QEG_AGG_PARTITIONED && !smem_insert) ? std::max(1, smem_slots) : probe;
   }
   P.hot = hot_keys_dev.get<uint64_t>();
   P.nhot = nhot;
@@ -1750,10 +1807,15 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
     // heavy hitters into a read-only table (hot_keys > 0) is kept as an
     // option; measured on GB300 it is slower than the first-come table
     // (34.1 vs 29.9 ms on 512M Zipf(1.1) rows with 1024-thread CTAs).
-    const bool preload = cfg.hot_keys > 0 && est_groups > 1024 && !heavy_candidates.empty();
-    smem_slots = cfg.smem_slots > 0 ? static_cast<int>(next_pow2(cfg.smem_slots)) : (preload ? 1024 : 2048);
+    // The partitioned strategy preloads the heavy hitters (when the sketch
+    // found any) into a read-only 2048-slot table: which rows reach the pool
+    // must not depend on the order rows arrive in, so a sizing pass can count
+    // them.
+    const bool preload = !heavy_candidates.empty() && (go_part || (cfg.hot_keys > 0 && est_groups > 1024));
+    smem_slots = cfg.smem_slots > 0 ? static_cast<int>(next_pow2(cfg.smem_slots))
+                                    : ((preload && !go_part) ? 1024 : 2048);
     smem_slots = std::min(smem_slots, slots);
-    smem_insert = 1;
+    smem_insert = go_part ? 0 : 1;
     if (preload) {
       const int want_hot = cfg.hot_keys > 0 ? cfg.hot_keys : smem_slots / 2;
       nhot = static_cast<int>(std::min<size_t>(heavy_candidates.size(), std::min(want_hot, smem_slots / 2)));
@@ -1799,21 +1861,46 @@ void AggState::setup_partitioned(uint64_t nrows) {
   const double g = est_groups > 0 ? est_groups : std::max<double>(1.0, static_cast<double>(nrows));
   int bits = static_cast<int>(std::ceil(std::log2(std::max(2.0, g / (0.45 * pb_slots)))));
   if (const char* e = std::getenv("QEG_AGG_PART_BITS")) bits = std::atoi(e);
-  part_bits = std::max(1, std::min(bits, 17));
+  // At most 2^15 partitions: the sizing pass keeps a 32-bit counter per
+  // partition in shared memory.
+  part_bits = std::max(1, std::min(bits, 15));
   strategy = QEG_AGG_PARTITIONED;
 }
 
-// Region capacity of this batch: the rows expected outside the private tables
-// (1 - the estimator's heavy-hitter share), 1.5 times over per partition; a
-// row past a full region is spilled to the global table.
+// One batch through the partitioned passes: the sizing pass counts the rows
+// of every partition that will go to the pool, a scan turns the counts into
+// exact regions, the first pass aggregates the heavy hitters in the private
+// tables and appends every other row to its region, the second pass
+// aggregates each partition in shared memory.
 void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len,
                                    const uint32_t* dsel) {
   if (ntails) merge_tails();  // an earlier batch's groups join the global table
   const uint64_t np = 1ull << part_bits;
-  const double tail = std::min(1.0, std::max(0.05, 1.0 - hot_share));
-  part_rows = static_cast<uint64_t>(1.5 * tail * static_cast<double>(nrows) / static_cast<double>(np)) + 1024;
-  if (const char* e = std::getenv("QEG_AGG_PART_ROWS")) part_rows = std::max<uint64_t>(1, std::strtoull(e, nullptr, 10));
-  const size_t pool_bytes = np * part_rows * 8;
+  AggK P = kparams(staged, dsel, nrows, len);
+  P.part_shift = 64 - part_bits;
+  if (part_hist.bytes() < np * 8) part_hist.alloc(np * 8, ctx->stream);
+  if (part_off.bytes() < (np + 1) * 8) part_off.alloc((np + 1) * 8, ctx->stream);
+  QEG_CUDA(cudaMemsetAsync(part_hist.get(), 0, np * 8, ctx->stream));
+  {
+    const size_t sb = static_cast<size_t>(smem_slots) * 8 + np * 4;
+    QEG_CUDA(cudaFuncSetAttribute(part_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+    int per_sm = 0;
+    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_hist_kernel, 1024, sb));
+    require(per_sm > 0, "partition sizing kernel does not fit on an SM");
+    const uint64_t grid = std::max<uint64_t>(
+        1, std::min<uint64_t>((nrows + 65535) / 65536, static_cast<uint64_t>(ctx->sms) * per_sm));
+    part_hist_kernel<<<(unsigned)grid, 1024, sb, ctx->stream>>>(P, part_hist.get<unsigned long long>());
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
+  // Region starts: a prefix sum of the (at most 2^15) counts on the host.
+  std::vector<uint64_t> offs(np + 1, 0);
+  QEG_CUDA(cudaMemcpyAsync(offs.data() + 1, part_hist.get(), np * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (uint64_t p = 0; p < np; ++p) offs[p + 1] += offs[p];
+  const uint64_t pooled = offs[np];
+  QEG_CUDA(cudaMemcpyAsync(part_off.get(), offs.data(), (np + 1) * 8, cudaMemcpyHostToDevice, ctx->stream));
+  const size_t pool_bytes = std::max<uint64_t>(pooled, 1) * 8;
   if (pool_key.bytes() < pool_bytes) {
     pool_key.alloc(pool_bytes, ctx->stream);
     pool_vals.clear();
@@ -1822,12 +1909,10 @@ void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_
   }
   if (part_fill.bytes() < np * 8) part_fill.alloc(np * 8, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(part_fill.get(), 0, np * 8, ctx->stream));
-  AggK P = kparams(staged, dsel, nrows, len);
   P.pool_key = pool_key.get<uint64_t>();
   for (size_t c = 0; c < val_cols.size(); ++c) P.pool_val[c] = pool_vals[c].get<uint64_t>();
   P.part_fill = part_fill.get<unsigned long long>();
-  P.part_rows = part_rows;
-  P.part_shift = 64 - part_bits;
+  P.part_off = part_off.get<uint64_t>();
   launch(P, nrows);
   settle(staged, len);
   part_second_pass();
@@ -1886,8 +1971,7 @@ void AggState::part_second_pass() {
   PartB B{};
   B.pool_key = pool_key.get<uint64_t>();
   for (size_t c = 0; c < val_cols.size(); ++c) B.pool_val[c] = pool_vals[c].get<uint64_t>();
-  B.part_fill = part_fill.get<unsigned long long>();
-  B.part_rows = part_rows;
+  B.part_off = part_off.get<uint64_t>();
   B.nparts = static_cast<uint32_t>(np);
   B.slots = pb_slots;
   B.counters = part_counters.get<unsigned long long>();
@@ -1917,13 +2001,13 @@ void AggState::part_second_pass() {
   if (nfailed) {
     std::vector<uint32_t> ids(nfailed);
     QEG_CUDA(cudaMemcpyAsync(ids.data(), part_failed.get(), nfailed * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    std::vector<unsigned long long> fills(np);
-    QEG_CUDA(cudaMemcpyAsync(fills.data(), part_fill.get(), np * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<uint64_t> offs(np + 1);
+    QEG_CUDA(cudaMemcpyAsync(offs.data(), part_off.get(), (np + 1) * 8, cudaMemcpyDeviceToHost, ctx->stream));
     QEG_CUDA(cudaStreamSynchronize(ctx->stream));
     for (uint32_t p : ids) {
-      const uint64_t n = std::min<uint64_t>(fills[p], part_rows);
+      const uint64_t n = offs[p + 1] - offs[p];
       if (n == 0) continue;
-      const std::vector<StagedCol> ps = pool_columns(*this, static_cast<uint64_t>(p) * part_rows);
+      const std::vector<StagedCol> ps = pool_columns(*this, offs[p]);
       if (n > spill_cap) {
         spill_cap = n;
         spill_rows.alloc(spill_cap * 4, ctx->stream);
@@ -2092,6 +2176,7 @@ qeg_status qeg_window_create(qeg_ctx* ctx, const int32_t* col_types, int ncols, 
 
 qeg_status qeg_agg_consume(qeg_agg* agg, const qeg_column* cols, int ncols, const uint32_t* sel,
                            uint64_t sel_len) {
+  qeg::NvtxRange nvtx_range("qeg_agg_consume");
   qeg_ctx* ctx = agg ? agg->st.ctx : nullptr;
   return qeg::guarded(ctx, [&] {
     qeg::require(agg != nullptr, "agg is NULL");
@@ -2101,6 +2186,7 @@ qeg_status qeg_agg_consume(qeg_agg* agg, const qeg_column* cols, int ncols, cons
 }
 
 qeg_status qeg_agg_finish(qeg_agg* agg, uint64_t* num_rows) {
+  qeg::NvtxRange nvtx_range("qeg_agg_finish");
   qeg_ctx* ctx = agg ? agg->st.ctx : nullptr;
   return qeg::guarded(ctx, [&] {
     qeg::require(agg != nullptr && num_rows != nullptr, "agg/num_rows is NULL");
@@ -2118,6 +2204,7 @@ qeg_status qeg_agg_result_types(const qeg_agg* agg, int32_t* types) {
 }
 
 qeg_status qeg_agg_fetch(qeg_agg* agg, uint64_t first, uint64_t count, const qeg_out_column* outs) {
+  qeg::NvtxRange nvtx_range("qeg_agg_fetch");
   qeg_ctx* ctx = agg ? agg->st.ctx : nullptr;
   return qeg::guarded(ctx, [&] {
     qeg::require(agg != nullptr, "agg is NULL");

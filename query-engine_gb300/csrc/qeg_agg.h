@@ -61,14 +61,14 @@ struct AggK {
   uint64_t full_at;              // running insert count that raises the flag
   uint32_t* err;
   // Partitioned strategy, first pass (pool_key != nullptr): a row whose key is
-  // not in its CTA's private table is appended to the region of its key's
-  // hash partition (key word + each value column's 8-byte value) instead of
-  // going to the global table. Region p holds rows [p * part_rows,
-  // (p + 1) * part_rows) of the pool; a row past a full region is spilled.
+  // not in its CTA's private table (read-only: the sketch's heavy hitters) is
+  // appended to the region of its key's hash partition (key word + each value
+  // column's 8-byte value) instead of going to the global table. Region p
+  // holds rows [part_off[p], part_off[p + 1]) of the pool.
   uint64_t* pool_key;
   uint64_t* pool_val[kMaxVals];
-  unsigned long long* part_fill;  // rows appended per partition (may pass part_rows)
-  uint64_t part_rows;
+  unsigned long long* part_fill;  // rows appended per partition
+  const uint64_t* part_off;       // [nparts + 1] region starts (exact: a histogram pass sized them)
   int part_shift;                 // partition of a key = key_hash1(key) >> part_shift
 };
 
@@ -78,8 +78,7 @@ struct AggK {
 struct PartB {
   const uint64_t* pool_key;
   const uint64_t* pool_val[kMaxVals];
-  const unsigned long long* part_fill;
-  uint64_t part_rows;
+  const uint64_t* part_off;       // [nparts + 1]
   uint32_t nparts;
   int slots;                      // shared-memory table slots (power of two)
   uint64_t* tails;                // row_words words per group
@@ -177,9 +176,8 @@ struct AggState {
   // spilled rows and partitions whose groups did not fit; finish() merges tail
   // rows whose key is also there and emits both.
   int part_bits = 0;
-  uint64_t part_rows = 0;
   int pb_slots = 0;
-  DevBuf pool_key, part_fill, part_failed, tails, part_counters;
+  DevBuf pool_key, part_fill, part_off, part_hist, part_failed, tails, part_counters;
   std::vector<DevBuf> pool_vals;
   uint64_t ntails = 0, tails_cap = 0;
 

@@ -659,6 +659,7 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
 }
 
 qeg_status qeg_batch_run(qeg_batch* b) {
+  qeg::NvtxRange nvtx_range("qeg_batch_run");
   qeg_ctx* ctx = b ? b->st.ctx : nullptr;
   return guarded(ctx, [&] {
     require(b != nullptr, "batch is NULL");
@@ -670,6 +671,7 @@ qeg_status qeg_batch_run(qeg_batch* b) {
 }
 
 qeg_status qeg_batch_finish(qeg_batch* b, uint64_t* groups) {
+  qeg::NvtxRange nvtx_range("qeg_batch_finish");
   qeg_ctx* ctx = b ? b->st.ctx : nullptr;
   return guarded(ctx, [&] {
     require(b != nullptr, "batch is NULL");

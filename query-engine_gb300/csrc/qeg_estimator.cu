@@ -39,7 +39,14 @@ std::vector<float> predict_host(qeg_ctx* ctx, const float* feats, uint32_t n) {
 // log2(1 + groups) = log2(1 + classic non-null groups) + 32 * out0.
 double learned_groups(const SketchResult& s, float out0) {
   const double classic = classic_estimate(s) - (s.null_frac > 0 ? 1.0 : 0.0);
-  const double lg = std::log2(1.0 + std::max(classic, 0.0)) + 32.0 * static_cast<double>(out0);
+  // The network's log2 correction, less a dead band of its own resolution:
+  // small corrections are noise of the BF16 network where the classic
+  // estimate is already close (a sample that covers most of the column),
+  // while the large ones fix its underestimates on sparsely sampled skewed
+  // columns. The band is chosen by the trainer on its training columns.
+  double c = 32.0 * static_cast<double>(out0);
+  c = c > kCorrectionDeadband ? c - kCorrectionDeadband : (c < -kCorrectionDeadband ? c + kCorrectionDeadband : 0.0);
+  const double lg = std::log2(1.0 + std::max(classic, 0.0)) + c;
   return std::exp2(std::min(40.0, std::max(0.0, lg))) - 1.0;
 }
 
@@ -95,6 +102,7 @@ extern "C" {
 
 qeg_status qeg_sketch(qeg_ctx* ctx, const qeg_column* key, uint64_t sample_rows, float* features,
                       double* classic_groups, double* top_share) {
+  qeg::NvtxRange nvtx_range("qeg_sketch");
   return guarded(ctx, [&] {
     require(ctx && key && features, "NULL argument");
     QEG_CUDA(cudaSetDevice(ctx->device));

@@ -10,10 +10,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/qeg.h"
 #include "qeg_device.cuh"
 
 namespace qeg {
+
+// A named NVTX range around one C-ABI call, for timelines of Nsight tools
+// (a no-op when no tool is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Error carrying a qeg_status; thrown inside the library, converted to a status
 // code at the C-ABI boundary (no exception crosses it).

@@ -2440,6 +2440,7 @@ qeg_status qeg_asof_create(qeg_ctx* ctx, const int32_t* probe_types, int nprobe,
 }
 
 qeg_status qeg_join_build(qeg_join* j, const qeg_column* cols, int ncols) {
+  qeg::NvtxRange nvtx_range("qeg_join_build");
   qeg_ctx* ctx = j ? j->st.ctx : nullptr;
   return guarded(ctx, [&] {
     require(j != nullptr && cols != nullptr, "join/cols is NULL");
@@ -2449,6 +2450,7 @@ qeg_status qeg_join_build(qeg_join* j, const qeg_column* cols, int ncols) {
 }
 
 qeg_status qeg_join_build_finish(qeg_join* j) {
+  qeg::NvtxRange nvtx_range("qeg_join_build_finish");
   qeg_ctx* ctx = j ? j->st.ctx : nullptr;
   return guarded(ctx, [&] {
     require(j != nullptr, "join is NULL");
@@ -2458,6 +2460,7 @@ qeg_status qeg_join_build_finish(qeg_join* j) {
 }
 
 qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64_t* out_rows) {
+  qeg::NvtxRange nvtx_range("qeg_join_probe");
   qeg_ctx* ctx = j ? j->st.ctx : nullptr;
   return guarded(ctx, [&] {
     require(j != nullptr && out_rows != nullptr, "join/out_rows is NULL");
@@ -2506,6 +2509,7 @@ qeg_status qeg_join_probe(qeg_join* j, const qeg_column* cols, int ncols, uint64
 }
 
 qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg_out_column* outs) {
+  qeg::NvtxRange nvtx_range("qeg_join_fetch");
   qeg_ctx* ctx = j ? j->st.ctx : nullptr;
   return guarded(ctx, [&] {
     require(j != nullptr && outs != nullptr, "join/outs is NULL");
@@ -2701,6 +2705,7 @@ qeg_status qeg_join_fetch(qeg_join* j, uint64_t first, uint64_t count, const qeg
 }
 
 qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, const qeg_column* probe_val) {
+  qeg::NvtxRange nvtx_range("qeg_join_probe_count_sum");
   qeg_ctx* ctx = j ? j->st.ctx : nullptr;
   return guarded(ctx, [&] {
     require(j != nullptr && probe_key != nullptr && probe_val != nullptr, "join/columns are NULL");

@@ -20,6 +20,11 @@ constexpr int kParams = kOffB3 + kOut;  // 9474
 // the this-many most frequent keys).
 constexpr int kHotTopK = 2048;
 
+// Dead band (log2 units) subtracted from the magnitude of the network's
+// group-count correction; train_estimator.py picks it on its training columns
+// (the value that minimises their mean absolute log2 error) and reports it.
+constexpr double kCorrectionDeadband = 0.125;
+
 struct Mlp {
   qeg_ctx* ctx = nullptr;
   DevBuf master, grad, m1, m2, wbf;         // params (fp32), grads, Adam moments, bf16 copy

@@ -234,6 +234,7 @@ extern "C" {
 qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe, const qeg_column* build, int nbuild,
                                const qeg_pipeline_desc* d, uint64_t out_capacity, const qeg_out_column* outs,
                                uint64_t* num_groups) {
+  qeg::NvtxRange nvtx_range("qeg_filter_join_agg");
   return guarded(ctx, [&] {
     require(ctx && probe && build && d && outs && num_groups, "NULL argument");
     require(nprobe >= 1 && nbuild >= 1, "both sides need columns");

@@ -607,7 +607,11 @@ double AggState::estimate_groups(const std::vector<StagedCol>& staged, uint64_t 
     return static_cast<double>(std::min<uint64_t>(std::max<uint64_t>(nrows, 1), 1ull << 22));
   }
   SketchResult s;
-  const int want_heavy = (cfg.hot_keys > 0) ? 4096 : 0;
+  // Heavy hitters are wanted for preloading (hot_keys > 0) and by the
+  // partitioned strategy, which the estimate may choose.
+  const bool part_possible = (cfg.strategy == QEG_AGG_AUTO || cfg.strategy == QEG_AGG_PARTITIONED) &&
+                             part_eligible(staged);
+  const int want_heavy = (cfg.hot_keys > 0 || part_possible) ? 4096 : 0;
   if (packed) {
     // A packed window's (partition key, bucket) words are clustered by time,
     // which a strided sample cannot extrapolate: estimate the partition key's

@@ -622,12 +622,21 @@ def sketch_batch(ctx, col, row_offsets, sample_rows=0):
     return f, c
 
 
-def learned_groups(classic, out0):
+# The library's dead band on the network's log2 correction (kCorrectionDeadband
+# in csrc/qeg_mlp.h).
+CORRECTION_DEADBAND = 0.125
+
+
+def learned_groups(classic, out0, deadband=CORRECTION_DEADBAND):
     """Group count from the classic estimate of a null-free key column and the
-    network's first output: log2(1 + g) = log2(1 + classic) + 32 * out0."""
+    network's first output, as the library computes it: log2(1 + g) =
+    log2(1 + classic) + c, where c is 32 * out0 moved toward zero by the dead
+    band (and 0 inside it)."""
     import math
 
-    return 2.0 ** min(40.0, max(0.0, math.log2(1.0 + max(classic, 0.0)) + 32.0 * out0)) - 1.0
+    c = 32.0 * out0
+    c = c - deadband if c > deadband else (c + deadband if c < -deadband else 0.0)
+    return 2.0 ** min(40.0, max(0.0, math.log2(1.0 + max(classic, 0.0)) + c)) - 1.0
 
 
 def estimator_init(ctx, seed):

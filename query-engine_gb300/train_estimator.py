@@ -141,6 +141,8 @@ def main():
     ap.add_argument("--out", default=os.path.join(HERE, "estimator_weights.f32"))
     ap.add_argument("--report", default=None)
     ap.add_argument("--seed", type=int, default=20260615)
+    ap.add_argument("--no-train", action="store_true",
+                    help="evaluate the weights already in --out (and pick the dead band) without training")
     args = ap.parse_args()
     dev = torch.device("cuda", 0)
     ctx = qeg.Context(0)
@@ -149,18 +151,34 @@ def main():
     X, T, C, D = build_set(ctx, rng, args.datasets, dev, args.seed)
     Xh, Th, Ch, Dh = build_set(ctx, rng, args.heldout, dev, args.seed + 1)
     t_data = time.time() - t0
-    qeg.estimator_init(ctx, args.seed)
     t1 = time.time()
     losses = []
-    for phase, lr in ((args.epochs // 2, 3e-3), (args.epochs // 4, 1e-3), (args.epochs - 3 * (args.epochs // 4), 3e-4)):
-        losses.append(qeg.estimator_train(ctx, X, T, phase, 64, lr, args.seed + len(losses)))
+    if args.no_train:
+        qeg.estimator_set_weights(ctx, np.fromfile(args.out, dtype="<f4"))
+    else:
+        qeg.estimator_init(ctx, args.seed)
+        for phase, lr in ((args.epochs // 2, 3e-3), (args.epochs // 4, 1e-3),
+                          (args.epochs - 3 * (args.epochs // 4), 3e-4)):
+            losses.append(qeg.estimator_train(ctx, X, T, phase, 64, lr, args.seed + len(losses)))
+        w = qeg.estimator_get_weights(ctx)
+        w.astype("<f4").tofile(args.out)
     t_train = time.time() - t1
-    w = qeg.estimator_get_weights(ctx)
-    w.astype("<f4").tofile(args.out)
+    # The dead band on the network's correction: the value that minimises the
+    # mean absolute log2 error on the TRAINING columns (the library's
+    # kCorrectionDeadband is set to it).
+    Yt = qeg.estimator_predict(ctx, X)
+    true_t = [d["groups"] for d in D]
+    bands = {}
+    for band in (0.0, 0.03, 0.06, 0.09, 0.125, 0.15, 0.2, 0.25, 0.3, 0.4, 0.5):
+        e = [log2_err(qeg.learned_groups(c, float(y[0]), band), t) for c, y, t in zip(C, Yt, true_t)]
+        bands[band] = {"mean": float(np.mean(e)), "median": float(np.median(e)), "p90": float(np.percentile(e, 90))}
+    best_band = min(bands, key=lambda b: bands[b]["mean"])
     Y = qeg.estimator_predict(ctx, Xh)
-    learned = [qeg.learned_groups(c, float(y[0])) for c, y in zip(Ch, Y)]
+    learned = [qeg.learned_groups(c, float(y[0]), best_band) for c, y in zip(Ch, Y)]
+    learned_raw = [qeg.learned_groups(c, float(y[0]), 0.0) for c, y in zip(Ch, Y)]
     true = [d["groups"] for d in Dh]
     e_learned = [log2_err(a, b) for a, b in zip(learned, true)]
+    e_raw = [log2_err(a, b) for a, b in zip(learned_raw, true)]
     e_classic = [log2_err(a, b) for a, b in zip(Ch, true)]
     share_err = [abs(float(y[1]) - d["top_share"]) for y, d in zip(Y, Dh)]
     by_kind = {}
@@ -179,6 +197,9 @@ def main():
                                        "classic": float(np.percentile(e_classic, 90))},
         "heldout_top_share_mae": float(np.mean(share_err)),
         "heldout_by_sketch": by_kind,
+        "correction_deadband": best_band,
+        "deadband_on_training_columns": {str(k): v for k, v in bands.items()},
+        "heldout_without_deadband": {"median": float(np.median(e_raw)), "p90": float(np.percentile(e_raw, 90))},
     }
     print(json.dumps(report))
     if args.report:

@@ -240,18 +240,20 @@ def _zipf_rows(rng, n, dom, s):
 
 
 @pytest.mark.parametrize("case", ["i64_skew", "i32_uniform", "f64_keys", "str_keys", "few_parts_fail",
-                                  "tiny_regions", "sel", "hot_preload", "count_only", "generic_fields"])
+                                  "zipf_preload", "sel", "hot_preload", "count_only", "generic_fields"])
 def test_partitioned_strategy(ctx, case, monkeypatch):
-    """The partitioned GROUP BY (QEG_AGG_PARTITIONED): private tables in the
-    first pass, every other row to its key-hash partition's region, one
-    partition per CTA in shared memory in the second pass, tail rows merged
-    with the global table at finalize. Cases: skewed and uniform keys, F64
-    keys (-0.0 / NaN canonicalised), STR keys through a code map, NULL keys and
-    key 0 (side rows), 2 partitions of many groups (second-pass tables too
-    full: those partitions go to the global table), regions of 64 rows (rows
-    past them spill), a selection vector, preloaded heavy hitters, COUNT(*)
-    alone, and a field set without a specialised kernel."""
-    cases = ["i64_skew", "i32_uniform", "f64_keys", "str_keys", "few_parts_fail", "tiny_regions", "sel",
+    """The partitioned GROUP BY (QEG_AGG_PARTITIONED): a sizing pass counts the
+    rows of every key-hash partition, the first pass aggregates the preloaded
+    heavy hitters in read-only private tables and appends every other row to
+    its partition's region, the second pass aggregates one partition per CTA
+    in shared memory, and finalize merges tail rows whose key the global table
+    also holds. Cases: skewed and uniform keys, F64 keys (-0.0 / NaN
+    canonicalised), STR keys through a code map, NULL keys and key 0 (side
+    rows), 2 partitions of many groups (second-pass tables too full: those
+    partitions go to the global table), the sketch's heavy hitters preloaded
+    (5M rows), a selection vector, 64 preloaded heavy hitters, COUNT(*) alone,
+    and a field set without a specialised kernel."""
+    cases = ["i64_skew", "i32_uniform", "f64_keys", "str_keys", "few_parts_fail", "zipf_preload", "sel",
              "hot_preload", "count_only", "generic_fields"]
     rng = np.random.default_rng(900 + cases.index(case))
     n = 300_000
@@ -278,9 +280,12 @@ def test_partitioned_strategy(ctx, case, monkeypatch):
     elif case == "few_parts_fail":
         monkeypatch.setenv("QEG_AGG_PART_BITS", "1")
         key = O.TCol(O.I64, rng.integers(0, 60_000, n).astype(np.int64), kvalid)
-    elif case == "tiny_regions":
-        monkeypatch.setenv("QEG_AGG_PART_ROWS", "64")
-        key = O.TCol(O.I64, rng.integers(0, 50_000, n).astype(np.int64), kvalid)
+    elif case == "zipf_preload":
+        # Above the sketch threshold: the sketch's heavy hitters (up to 1024)
+        # are preloaded into the read-only private tables.
+        n = 5 << 20
+        kvalid = rng.random(n) > 0.02
+        key = O.TCol(O.I64, _zipf_rows(rng, n, 500_000, 1.3) * 0x9E3779B97F4A7C1, kvalid)
     elif case == "sel":
         key = O.TCol(O.I64, rng.integers(0, 50_000, n).astype(np.int64), kvalid)
         sel = np.sort(rng.choice(n, n // 3, replace=False)).astype(np.uint32)
