@@ -58,6 +58,11 @@ constexpr int kFullProbe = 16;
 // or more (half of L2: its random rows would mostly come from DRAM).
 constexpr uint64_t kPartMinRows = 1ull << 22;
 constexpr uint64_t kPartMinTableBytes = 64ull << 20;
+// At most 2^kPartMaxBits partitions (the sizing pass keeps a 32-bit counter
+// per partition in shared memory), and QEG_AGG_AUTO partitions only while the
+// estimate averages at most kPartMaxFill of a second-pass table per partition.
+constexpr int kPartMaxBits = 15;
+constexpr double kPartMaxFill = 0.6;
 
 __device__ __forceinline__ uint64_t ld_volatile_shared(const uint64_t* p) {
   return *reinterpret_cast<const volatile uint64_t*>(p);
@@ -197,30 +202,6 @@ __device__ __forceinline__ uint64_t* find_row1(uint64_t* table, uint64_t cap, in
     if (++s == cap) s = 0;
   }
   return nullptr;
-}
-
-// Partitioned first pass: lanes with `mine` append their row (key word and
-// the values of the NV value columns) to the region of the key's hash
-// partition; lanes of one partition share one reservation. Every lane of the
-// warp calls it.
-template <int NV>
-__device__ __forceinline__ bool pool_append(const AggK& P, bool mine, uint64_t k, const uint64_t (&vb)[kMaxVals],
-                                            unsigned lane) {
-  const uint32_t part = mine ? static_cast<uint32_t>(key_hash1(k) >> P.part_shift) : 0xffffffffu;
-  const unsigned same = __match_any_sync(0xffffffffu, part);
-  const int first = __ffs(same) - 1;
-  unsigned long long base = 0;
-  if (mine && static_cast<int>(lane) == first)
-    base = atomicAdd(P.part_fill + part, static_cast<unsigned long long>(__popc(same)));
-  base = __shfl_sync(0xffffffffu, base, first);
-  if (!mine) return false;
-  const uint64_t at = P.part_off[part] + base + static_cast<unsigned>(__popc(same & ((1u << lane) - 1u)));
-  if (at >= P.part_off[part + 1]) return false;  // (the histogram pass sized every region exactly)
-  P.pool_key[at] = k;
-#pragma unroll
-  for (int c = 0; c < NV; ++c)
-    if (c < P.nvals) P.pool_val[c][at] = vb[c];
-  return true;
 }
 
 // Merges one field block `src` (a partial aggregate) into `dst`.
@@ -436,7 +417,6 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       // The leader finds (or places) the group's row.
       uint64_t* f = nullptr;
       int space = kRowGlobal;
-      bool to_pool = false;
       const unsigned long long ins0 = inserted;
       if (leader) {
         const uint64_t h = key_hash1(k);
@@ -450,25 +430,18 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
             f = &sm[srow * SW + 1];
             space = kRowShared;
           }
-        } else if (P.pool_key) {
-          to_pool = true;  // (a NULL key or key word 0 always has its side row)
         } else {
           uint64_t* r = global_row1(P, kv, k, h, inserted, full ? kFullProbe : P.probe_limit);
           if (r) f = r + 1;
         }
       }
-      // Partitioned first pass: every row of a group without a private row
-      // goes to its partition's region.
-      bool pooled = false;
-      if (P.pool_key) {
-        const unsigned pm = __ballot_sync(0xffffffffu, to_pool);
-        if (pm) pooled = pool_append<NV>(P, live && ((pm >> (__ffs(peers) - 1)) & 1u), k, vb, lane);
-      }
       // A group whose row could not be placed spills each of its rows.
       const unsigned placed = __ballot_sync(0xffffffffu, f != nullptr);
       const bool ok = live && ((placed >> (__ffs(peers) - 1)) & 1u);
-      if (live && !ok && !pooled) spill_row(P, p);
-      if (live && !ok) peers = 1u << lane;
+      if (live && !ok) {
+        spill_row(P, p);
+        peers = 1u << lane;
+      }
       const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
       if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader && ok, space, peers, pp, vv, vb);
       else warp_apply<NV>(f, leader && ok, space, peers, pp, P, vv, vb);
@@ -780,7 +753,8 @@ __global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, ui
       } else {
         const uint64_t k = src[0];
         if (k == 0) continue;
-        dst = global_row1(P, true, k, key_hash1(k), inserted, P.probe_limit);
+        // The new table has room for every row: probe as far as it takes.
+        dst = global_row1(P, true, k, key_hash1(k), inserted, static_cast<int>(P.cap < (1ull << 30) ? P.cap : (1ull << 30)));
       }
       if (!dst) {
         atomicOr(P.err, kDevSpillOverflow);
@@ -808,35 +782,87 @@ __global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, ui
 
 // Merges spilled partial rows (single-key rows, or composite rows of the
 // composite private tables) into the table.
-// Partitioned strategy, sizing pass: rows per key-hash partition of every row
-// the first pass will append to the pool -- a non-NULL key other than key word
-// 0 that is not one of the preloaded heavy hitters (the same set the first
-// pass holds in its read-only private table; membership is exact there too).
-// Per CTA: the heavy hitters in a shared-memory key table of S slots, then
-// 32-bit partition counters, added to `hist` at the end.
-__global__ void __launch_bounds__(1024) part_hist_kernel(const AggK P, unsigned long long* hist) {
-  extern __shared__ uint64_t hs[];
-  const int S = P.smem_slots;
-  uint32_t* cnt = reinterpret_cast<uint32_t*>(hs + S);
-  const uint32_t np = 1u << (64 - P.part_shift);
-  for (int i = threadIdx.x; i < S; i += blockDim.x) hs[i] = 0;
-  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) cnt[i] = 0;
+// ---------------------------------------------------------------------------
+// Partitioned strategy (QEG_AGG_PARTITIONED, single key). Three passes over
+// the batch: a sizing pass counts, per key-hash partition, the rows that are
+// not heavy hitters; the first pass aggregates the heavy hitters in read-only
+// per-CTA tables and appends every other row to its partition's region of the
+// pool; the second pass aggregates one partition per CTA in shared memory and
+// appends the groups to the tail rows. Heavy-hitter membership and partitions
+// use cheap multiplicative hashes (one 64-bit multiply); the global table and
+// the tail rows keep the table's own key hash.
+// ---------------------------------------------------------------------------
+constexpr uint64_t kHotMul = 0x9E3779B97F4A7C15ull;
+constexpr uint64_t kPartMul = 0xD1B54A32D192ED03ull;
+
+// Slot of key word k in a heavy-hitter table of 2^lg slots.
+__device__ __forceinline__ uint32_t hot_slot(uint64_t k, int lg) {
+  return static_cast<uint32_t>(((k ^ (k >> 29)) * kHotMul) >> (64 - lg));
+}
+// Partition hash of key word k: the partition is its top bits, a second-pass
+// table slot the bits below them.
+__device__ __forceinline__ uint64_t part_mix(uint64_t k) { return (k ^ (k >> 31)) * kPartMul; }
+
+// Parameters of the partitioned passes beyond AggK.
+struct PartA {
+  int hot_lg;                // heavy-hitter table: 2^hot_lg key slots
+  int nhot;                  // heavy hitters (ranks 0..nhot-1); rank nhot: NULL key, nhot + 1: key word 0
+  int rw;                    // field words per heavy-hitter row (odd)
+  unsigned long long* hist;  // sizing pass: rows per partition
+};
+
+// Builds the read-only heavy-hitter table in shared memory: key words (0 =
+// empty) and each slot's rank. All threads call it; ends with a barrier.
+__device__ __forceinline__ void load_hot_table(const AggK& P, const PartA& A, uint64_t* hk, uint16_t* hr) {
+  const int hs = 1 << A.hot_lg;
+  for (int i = threadIdx.x; i < hs; i += blockDim.x) hk[i] = 0;
   __syncthreads();
-  for (int i = threadIdx.x; i < P.nhot; i += blockDim.x) {
+  for (int i = threadIdx.x; i < A.nhot; i += blockDim.x) {
     const uint64_t k = P.hot[i];
-    if (k == 0) continue;
-    uint64_t s = key_hash1(k) & (S - 1);
-    for (int t = 0; t < S; ++t) {
+    if (k == 0) continue;  // (key word 0 has its own row)
+    uint32_t s = hot_slot(k, A.hot_lg);
+    for (int t = 0; t < hs; ++t) {
       const unsigned long long old =
-          atomicCAS(reinterpret_cast<unsigned long long*>(&hs[s]), 0ull, static_cast<unsigned long long>(k));
-      if (old == 0 || old == k) break;
-      s = (s + 1) & (S - 1);
+          atomicCAS(reinterpret_cast<unsigned long long*>(&hk[s]), 0ull, static_cast<unsigned long long>(k));
+      if (old == 0) {
+        hr[s] = static_cast<uint16_t>(i);
+        break;
+      }
+      if (old == k) break;  // (a repeated candidate keeps its first rank)
+      s = (s + 1) & (hs - 1);
     }
   }
   __syncthreads();
+}
+
+// Rank of key word k (nonzero) among the heavy hitters, or -1.
+__device__ __forceinline__ int hot_rank(const uint64_t* hk, const uint16_t* hr, int lg, uint64_t k) {
+  const uint32_t mask = (1u << lg) - 1u;
+  uint32_t s = hot_slot(k, lg);
+  for (uint32_t t = 0; t <= mask; ++t) {
+    const uint64_t cur = hk[s];
+    if (cur == k) return hr[s];
+    if (cur == 0) return -1;
+    s = (s + 1) & mask;
+  }
+  return -1;
+}
+
+// Sizing pass: rows per partition of every row that will reach the pool (a
+// non-NULL key other than key word 0 and not a heavy hitter). 32-bit counters
+// per CTA in shared memory, added to A.hist at the end.
+__global__ void __launch_bounds__(1024) part_hist_kernel(const AggK P, const PartA A) {
+  extern __shared__ uint64_t hsm[];
+  const int hs = 1 << A.hot_lg;
+  uint64_t* hk = hsm;
+  uint16_t* hr = reinterpret_cast<uint16_t*>(hk + hs);
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(hr + hs);
+  const uint32_t np = 1u << (64 - P.part_shift);
+  for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) cnt[i] = 0;
+  load_hot_table(P, A, hk, hr);
   const DevCol& kc = P.key[0];
-  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < P.nrows;
-       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < P.nrows; i += stride) {
     uint64_t p = i;
     if (P.sel) {
       p = P.sel[i];
@@ -845,58 +871,155 @@ __global__ void __launch_bounds__(1024) part_hist_kernel(const AggK P, unsigned 
     if (!col_valid(kc, p)) continue;
     const uint64_t k = key_word(kc, p);
     if (k == 0) continue;
-    const uint64_t h = key_hash1(k);
-    bool hot = false;
-    if (P.nhot > 0) {
-      uint64_t s = h & (S - 1);
-      for (int t = 0; t < S; ++t) {
-        const uint64_t cur = hs[s];
-        if (cur == k) {
-          hot = true;
-          break;
-        }
-        if (cur == 0) break;
-        s = (s + 1) & (S - 1);
-      }
-    }
-    if (!hot) atomicAdd(&cnt[h >> P.part_shift], 1u);
+    if (A.nhot > 0 && hot_rank(hk, hr, A.hot_lg, k) >= 0) continue;
+    atomicAdd(&cnt[part_mix(k) >> P.part_shift], 1u);
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
-    if (cnt[i]) atomicAdd(hist + i, static_cast<unsigned long long>(cnt[i]));
+    if (cnt[i]) atomicAdd(A.hist + i, static_cast<unsigned long long>(cnt[i]));
 }
 
-// Slot of key word k (nonzero) in a CTA table of S slots (power of two) with
-// row stride SW, inserting it when absent; -1 when more than S / 2 slots are
-// probed (the table is too full).
-__device__ __forceinline__ int part_smem_slot(uint64_t* sm, int S, int SW, uint64_t k, uint64_t h) {
-  uint64_t s = h & (S - 1);
-  for (int t = 0; t < S / 2; ++t) {
-    const uint64_t cur = ld_volatile_shared(&sm[s * SW]);
+// First pass. Heavy hitters (and the NULL key and key word 0, which always
+// have rows) aggregate into CTA rows by rank with warp peer aggregation; every
+// other row is appended to its partition's region (lanes of one partition
+// share one reservation). At the end each CTA merges its rows into the global
+// table.
+template <int NV, uint32_t SPEC>
+__global__ void __launch_bounds__(512) part_pass1_kernel(const AggK P, const PartA A) {
+  extern __shared__ uint64_t psm[];
+  const int hs = 1 << A.hot_lg;
+  uint64_t* hk = psm;
+  uint16_t* hr = reinterpret_cast<uint16_t*>(hk + hs);
+  uint64_t* rows = hk + hs + (hs * 2 + 7) / 8;  // (nhot + 2) rows of A.rw words
+  const int RW = A.rw;
+  const int nrow = A.nhot + 2;
+  for (int i = threadIdx.x; i < nrow * RW; i += blockDim.x) rows[i] = 0;
+  load_hot_table(P, A, hk, hr);
+  const unsigned lane = threadIdx.x & 31u;
+  const DevCol& kc = P.key[0];
+  const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t base = static_cast<uint64_t>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < P.nrows;
+       base += step) {
+    const uint64_t i = base + lane;
+    bool live = i < P.nrows;
+    uint64_t p = i;
+    if (live && P.sel) {
+      p = P.sel[i];
+      if (p >= P.len) {
+        atomicOr(P.err, kDevBadInput);
+        live = false;
+      }
+    }
+    bool vv[kMaxVals];
+    uint64_t vb[kMaxVals];
+#pragma unroll
+    for (int c = 0; c < kMaxVals; ++c) {
+      vv[c] = false;
+      vb[c] = 0;
+    }
+    if (live) load_values<NV>(P, p, vv, vb);
+    const bool kv = live && col_valid(kc, p);
+    const uint64_t k = kv ? key_word(kc, p) : 0;
+    int rank = -1;
+    if (live) rank = !kv ? A.nhot : (k == 0 ? A.nhot + 1 : (A.nhot > 0 ? hot_rank(hk, hr, A.hot_lg, k) : -1));
+    const bool hot = rank >= 0;
+    if (__ballot_sync(0xffffffffu, hot)) {
+      const unsigned peers = __match_any_sync(0xffffffffu, hot ? static_cast<unsigned>(rank) : (0x80000000u | lane));
+      const bool leader = hot && __ffs(peers) - 1 == static_cast<int>(lane);
+      const PeerPlan pp = plan_peers(peers, lane);
+      uint64_t* f = rows + static_cast<size_t>(hot ? rank : 0) * RW;
+      if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader, kRowShared, peers, pp, vv, vb);
+      else warp_apply<NV>(f, leader, kRowShared, peers, pp, P, vv, vb);
+    }
+    const bool cold = live && !hot;
+    if (__ballot_sync(0xffffffffu, cold)) {
+      const uint32_t part = cold ? static_cast<uint32_t>(part_mix(k) >> P.part_shift) : 0xffffffffu;
+      const unsigned same = __match_any_sync(0xffffffffu, part);
+      const int first = __ffs(same) - 1;
+      unsigned long long b = 0;
+      if (cold && static_cast<int>(lane) == first)
+        b = atomicAdd(P.part_fill + part, static_cast<unsigned long long>(__popc(same)));
+      b = __shfl_sync(0xffffffffu, b, first);
+      if (cold) {
+        const uint64_t at = P.part_off[part] + b + static_cast<unsigned>(__popc(same & ((1u << lane) - 1u)));
+        if (at < P.part_off[part + 1]) {
+          P.pool_key[at] = k;
+#pragma unroll
+          for (int c = 0; c < NV; ++c)
+            if (c < P.nvals) P.pool_val[c][at] = vb[c];
+        } else {
+          spill_row(P, p);  // (the sizing pass counted every such row: not reached)
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // Merge the CTA's rows into the global table.
+  unsigned long long inserted = 0;
+  const int W = P.row_words;
+  for (int r = threadIdx.x; r < nrow; r += blockDim.x) {
+    const uint64_t* src = rows + static_cast<size_t>(r) * RW;
+    if (src[0] == 0) continue;  // no row counted here
+    uint64_t* dst;
+    if (r == A.nhot) {
+      dst = P.table + (P.cap + 1) * W;
+    } else if (r == A.nhot + 1) {
+      dst = P.table + P.cap * W;
+    } else {
+      const uint64_t k = P.hot[r];
+      dst = global_row1(P, true, k, key_hash1(k), inserted, P.probe_limit);
+      if (!dst) {
+        const unsigned long long j = atomicAdd(P.counters + 1, 1ull);
+        if (j < P.part_cap) {
+          P.spill_parts[j * W] = k;
+          for (int w = 1; w < W; ++w) P.spill_parts[j * W + w] = src[w - 1];
+        } else {
+          atomicOr(P.err, kDevSpillOverflow);
+        }
+        continue;
+      }
+    }
+    merge_fields(dst + 1, src, P);
+  }
+  for (int o = 16; o > 0; o >>= 1) inserted += __shfl_down_sync(0xffffffffu, inserted, o);
+  if ((threadIdx.x & 31) == 0 && inserted) atomicAdd(P.counters + 2, inserted);
+}
+
+// Slot of key word k (nonzero, partition hash m) in a second-pass table of
+// S = 2^lgS slots with row stride SW, inserting it when absent; -1 when S / 2
+// slots were probed (the table is too full).
+__device__ __forceinline__ int part_smem_slot(uint64_t* sm, int lgS, int shift, int SW, uint64_t k, uint64_t m) {
+  const uint32_t mask = (1u << lgS) - 1u;
+  uint32_t s = static_cast<uint32_t>(m >> (shift - lgS)) & mask;
+  for (uint32_t t = 0; t <= (mask >> 1); ++t) {
+    const uint64_t cur = ld_volatile_shared(&sm[static_cast<size_t>(s) * SW]);
     if (cur == k) return static_cast<int>(s);
     if (cur == 0) {
-      const unsigned long long old =
-          atomicCAS(reinterpret_cast<unsigned long long*>(&sm[s * SW]), 0ull, static_cast<unsigned long long>(k));
+      const unsigned long long old = atomicCAS(reinterpret_cast<unsigned long long*>(&sm[static_cast<size_t>(s) * SW]),
+                                               0ull, static_cast<unsigned long long>(k));
       if (old == 0 || old == k) return static_cast<int>(s);
     }
-    s = (s + 1) & (S - 1);
+    s = (s + 1) & mask;
   }
   return -1;
 }
 
-// Partitioned strategy, second pass: each CTA takes partitions in turn and
-// aggregates the partition's pool rows (every key nonzero and non-NULL, every
-// value present) in a shared-memory table with warp peer aggregation, then
-// appends the table's groups to the tail rows with one reservation per CTA and
-// clears the rows it used. A partition with more groups than the table holds
-// is listed as failed and appends nothing (the host aggregates it into the
-// global table instead), so the pass can be re-run with a larger tail buffer.
+// Second pass: each CTA takes partitions in turn and aggregates the
+// partition's pool rows (every key nonzero and non-NULL, every value present)
+// in a shared-memory table with warp peer aggregation, each warp loading its
+// next rows before it works on the current ones; then it appends the table's
+// groups to the tail rows with one reservation per CTA and clears the rows it
+// used. A partition with more groups than the table holds is listed as failed
+// and appends nothing (the host aggregates it into the global table instead),
+// so the pass can be re-run with a larger tail buffer.
 template <int NV, uint32_t SPEC>
 __global__ void __launch_bounds__(1024) part_agg_kernel(const AggK P, const PartB B) {
   extern __shared__ uint64_t sm[];
   __shared__ int s_fail;
   __shared__ unsigned long long s_wbase[32];
   const int W = P.row_words, SW = W | 1, S = B.slots;
+  int lgS = 0;
+  while ((1 << lgS) < S) ++lgS;
   const unsigned lane = threadIdx.x & 31u;
   const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int i = threadIdx.x; i < S * SW; i += blockDim.x) sm[i] = 0;
@@ -905,34 +1028,38 @@ __global__ void __launch_bounds__(1024) part_agg_kernel(const AggK P, const Part
     __syncthreads();
     const uint64_t begin = B.part_off[part];
     const uint64_t n = B.part_off[part + 1] - begin;
-    for (uint64_t b = static_cast<uint64_t>(warp) * 32; b < n; b += static_cast<uint64_t>(nwarps) * 32) {
-      const uint64_t i = b + lane;
-      const bool live = i < n;
+    // Rows of this warp's first iteration.
+    uint64_t b = static_cast<uint64_t>(warp) * 32;
+    uint64_t nk = 0;
+    uint64_t nvb[kMaxVals];
+    auto load = [&](uint64_t at) {
+      const bool ok = at < n;
+      nk = ok ? __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_key + begin + at)) : 0;
+#pragma unroll
+      for (int c = 0; c < NV; ++c)
+        nvb[c] = (ok && c < P.nvals) ? __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_val[c] + begin + at))
+                                     : 0;
+    };
+    load(b + lane);
+    for (; b < n; b += static_cast<uint64_t>(nwarps) * 32) {
+      const bool live = b + lane < n;
+      const uint64_t k = nk;
       bool vv[kMaxVals];
       uint64_t vb[kMaxVals];
 #pragma unroll
       for (int c = 0; c < kMaxVals; ++c) {
-        vv[c] = false;
-        vb[c] = 0;
+        vv[c] = live && c < NV && c < P.nvals;
+        vb[c] = c < NV ? nvb[c] : 0;
       }
-      uint64_t k = 0;
-      if (live) {
-        k = __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_key + begin + i));
-#pragma unroll
-        for (int c = 0; c < NV; ++c)
-          if (c < P.nvals) {
-            vv[c] = true;
-            vb[c] = __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_val[c] + begin + i));
-          }
-      }
+      load(b + static_cast<uint64_t>(nwarps) * 32 + lane);  // the next iteration's rows, in flight meanwhile
       const unsigned livemask = __ballot_sync(0xffffffffu, live);
-      const unsigned same = __match_any_sync(0xffffffffu, k);
+      const unsigned same = __match_any_sync(0xffffffffu, live ? k : ~0ull - lane);
       const unsigned peers = live ? (same & livemask) : (1u << lane);
       const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
       uint64_t* f = nullptr;
       if (leader) {
-        const int slot = part_smem_slot(sm, S, SW, k, key_hash1(k));
-        if (slot >= 0) f = &sm[slot * SW + 1];
+        const int slot = part_smem_slot(sm, lgS, P.part_shift, SW, k, part_mix(k));
+        if (slot >= 0) f = &sm[static_cast<size_t>(slot) * SW + 1];
         else s_fail = 1;
       }
       const unsigned placed = __ballot_sync(0xffffffffu, f != nullptr);
@@ -947,7 +1074,7 @@ __global__ void __launch_bounds__(1024) part_agg_kernel(const AggK P, const Part
     unsigned cnt = 0;
     for (int s0 = warp * 32; s0 < S; s0 += nwarps * 32) {
       const int s = s0 + static_cast<int>(lane);
-      cnt += __popc(__ballot_sync(0xffffffffu, s < S && sm[s * SW] != 0));
+      cnt += __popc(__ballot_sync(0xffffffffu, s < S && sm[static_cast<size_t>(s) * SW] != 0));
     }
     if (lane == 0) s_wbase[warp] = cnt;
     __syncthreads();
@@ -971,13 +1098,13 @@ __global__ void __launch_bounds__(1024) part_agg_kernel(const AggK P, const Part
     unsigned long long pos = s_wbase[warp];
     for (int s0 = warp * 32; s0 < S; s0 += nwarps * 32) {
       const int s = s0 + static_cast<int>(lane);
-      const bool occ = s < S && sm[s * SW] != 0;
+      const bool occ = s < S && sm[static_cast<size_t>(s) * SW] != 0;
       const unsigned m = __ballot_sync(0xffffffffu, occ);
       if (occ) {
         const unsigned long long o = pos + __popc(m & ((1u << lane) - 1u));
         if (!failed && o < B.tails_cap)
-          for (int w = 0; w < W; ++w) B.tails[o * W + w] = sm[s * SW + w];
-        for (int w = 0; w < W; ++w) sm[s * SW + w] = 0;
+          for (int w = 0; w < W; ++w) B.tails[o * W + w] = sm[static_cast<size_t>(s) * SW + w];
+        for (int w = 0; w < W; ++w) sm[static_cast<size_t>(s) * SW + w] = 0;
       }
       pos += __popc(m);
     }
@@ -1000,7 +1127,8 @@ __global__ void merge_parts_kernel(const AggK P, const uint64_t* __restrict__ pa
       fo = 2 + P.nkeys;
     } else {
       const uint64_t k = src[0];
-      dst = global_row1(P, true, k, key_hash1(k), inserted, P.probe_limit);
+      // The caller sized the table for these rows: probe as far as it takes.
+      dst = global_row1(P, true, k, key_hash1(k), inserted, static_cast<int>(P.cap < (1ull << 30) ? P.cap : (1ull << 30)));
       fo = 1;
     }
     if (!dst) {
@@ -1770,8 +1898,9 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
     if (cfg.strategy == QEG_AGG_PARTITIONED)
       go_part = true;
     else if (cfg.strategy == QEG_AGG_AUTO && nrows >= kPartMinRows && est_groups > 0 &&
-             est_groups / kTargetLoad * row_words * 8.0 >= static_cast<double>(kPartMinTableBytes))
-      go_part = true;
+             est_groups / kTargetLoad * row_words * 8.0 >= static_cast<double>(kPartMinTableBytes) &&
+             est_groups <= kPartMaxFill * part_table_slots() * static_cast<double>(1u << kPartMaxBits))
+      go_part = true;  // (more groups than 2^15 second-pass tables hold: the global table)
   }
   if (go_part) want = next_pow2(2ull * ctx->sms * (2048 + 2));
   alloc_table(want);
@@ -1853,17 +1982,22 @@ bool AggState::part_eligible(const std::vector<StagedCol>& staged) const {
 // Partition count and second-pass table size: the largest power-of-two table
 // of shared memory rows one CTA can hold (at most 8192 slots), and enough
 // partitions that each expects about 45% of that many groups.
-void AggState::setup_partitioned(uint64_t nrows) {
+int AggState::part_table_slots() const {
   const size_t rb = static_cast<size_t>(row_words | 1) * 8;
-  pb_slots = 64;
-  while (pb_slots < 8192 && static_cast<size_t>(pb_slots) * 2 * rb <= ctx->smem_optin - 4096) pb_slots *= 2;
+  int slots = 64;
+  while (slots < 8192 && static_cast<size_t>(slots) * 2 * rb <= ctx->smem_optin - 4096) slots *= 2;
+  return slots;
+}
+
+void AggState::setup_partitioned(uint64_t nrows) {
+  pb_slots = part_table_slots();
   // Without an estimate the row count bounds the group count.
   const double g = est_groups > 0 ? est_groups : std::max<double>(1.0, static_cast<double>(nrows));
   int bits = static_cast<int>(std::ceil(std::log2(std::max(2.0, g / (0.45 * pb_slots)))));
   if (const char* e = std::getenv("QEG_AGG_PART_BITS")) bits = std::atoi(e);
   // At most 2^15 partitions: the sizing pass keeps a 32-bit counter per
   // partition in shared memory.
-  part_bits = std::max(1, std::min(bits, 15));
+  part_bits = std::max(1, std::min(bits, kPartMaxBits));
   strategy = QEG_AGG_PARTITIONED;
 }
 
@@ -1878,18 +2012,25 @@ void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_
   const uint64_t np = 1ull << part_bits;
   AggK P = kparams(staged, dsel, nrows, len);
   P.part_shift = 64 - part_bits;
+  PartA A{};
+  A.nhot = nhot;
+  A.hot_lg = 6;
+  while ((1 << A.hot_lg) < 2 * std::max(nhot, 1)) ++A.hot_lg;
+  A.rw = nfields | 1;
+  const size_t hot_bytes = (static_cast<size_t>(1) << A.hot_lg) * 8 + (((static_cast<size_t>(2) << A.hot_lg) + 7) / 8) * 8;
   if (part_hist.bytes() < np * 8) part_hist.alloc(np * 8, ctx->stream);
   if (part_off.bytes() < (np + 1) * 8) part_off.alloc((np + 1) * 8, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(part_hist.get(), 0, np * 8, ctx->stream));
+  A.hist = part_hist.get<unsigned long long>();
   {
-    const size_t sb = static_cast<size_t>(smem_slots) * 8 + np * 4;
+    const size_t sb = hot_bytes + np * 4;
     QEG_CUDA(cudaFuncSetAttribute(part_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
     int per_sm = 0;
     QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_hist_kernel, 1024, sb));
     require(per_sm > 0, "partition sizing kernel does not fit on an SM");
     const uint64_t grid = std::max<uint64_t>(
         1, std::min<uint64_t>((nrows + 65535) / 65536, static_cast<uint64_t>(ctx->sms) * per_sm));
-    part_hist_kernel<<<(unsigned)grid, 1024, sb, ctx->stream>>>(P, part_hist.get<unsigned long long>());
+    part_hist_kernel<<<(unsigned)grid, 1024, sb, ctx->stream>>>(P, A);
     ctx->launches++;
     QEG_CUDA(cudaGetLastError());
   }
@@ -1913,7 +2054,31 @@ void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_
   for (size_t c = 0; c < val_cols.size(); ++c) P.pool_val[c] = pool_vals[c].get<uint64_t>();
   P.part_fill = part_fill.get<unsigned long long>();
   P.part_off = part_off.get<uint64_t>();
-  launch(P, nrows);
+  {
+    const uint32_t spec = field_spec(P);
+    const int nv = static_cast<int>(val_cols.size());
+    void (*kern)(AggK, PartA) = nullptr;
+    if (spec == kSpecIntF64) kern = part_pass1_kernel<2, kSpecIntF64>;
+    else if (spec == kSpecIntF64Nulls) kern = part_pass1_kernel<2, kSpecIntF64Nulls>;
+    else if (spec == kSpecF64) kern = part_pass1_kernel<1, kSpecF64>;
+    else if (spec == kSpecF64Nulls) kern = part_pass1_kernel<1, kSpecF64Nulls>;
+    else if (spec == kSpecCount) kern = part_pass1_kernel<1, kSpecCount>;
+    else if (spec == kSpecIntSumF64Stats) kern = part_pass1_kernel<2, kSpecIntSumF64Stats>;
+    else if (nv <= 1) kern = part_pass1_kernel<1, kGenericSpec>;
+    else if (nv <= 2) kern = part_pass1_kernel<2, kGenericSpec>;
+    else if (nv <= 4) kern = part_pass1_kernel<4, kGenericSpec>;
+    else kern = part_pass1_kernel<8, kGenericSpec>;
+    const size_t sb = hot_bytes + static_cast<size_t>(nhot + 2) * A.rw * 8;
+    QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+    int per_sm = 0;
+    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 512, sb));
+    require(per_sm > 0, "partitioned first pass does not fit on an SM");
+    const uint64_t grid = std::max<uint64_t>(
+        1, std::min<uint64_t>((nrows + 8191) / 8192, static_cast<uint64_t>(ctx->sms) * per_sm));
+    kern<<<(unsigned)grid, 512, sb, ctx->stream>>>(P, A);
+    ctx->launches++;
+    QEG_CUDA(cudaGetLastError());
+  }
   settle(staged, len);
   part_second_pass();
 }

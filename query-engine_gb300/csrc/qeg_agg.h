@@ -206,6 +206,7 @@ struct AggState {
   double estimate_groups(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len, const uint32_t* dsel);
   void settle(const std::vector<StagedCol>& staged, uint64_t len);
   bool part_eligible(const std::vector<StagedCol>& staged) const;
+  int part_table_slots() const;
   void setup_partitioned(uint64_t nrows);
   void consume_partitioned(const std::vector<StagedCol>& staged, uint64_t nrows, uint64_t len, const uint32_t* dsel);
   void part_second_pass();

@@ -351,6 +351,25 @@ __device__ __forceinline__ uint64_t sink_lookup(const JTable& T, KT key) {
   }
 }
 
+// Loads a 64-bit word with an L2 evict-last policy: the Bloom filter (and
+// optionally the table) keeps its lines in L2 while the probe stream, loaded
+// evict-first, passes through.
+__device__ __forceinline__ uint64_t ld_keep_l2(const uint64_t* p, uint64_t pol) {
+  uint64_t v;
+  asm volatile("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ ulonglong2 ld_keep_l2x2(const ulonglong2* p, uint64_t pol) {
+  ulonglong2 v;
+  asm volatile("ld.global.nc.L2::cache_hint.v2.u64 {%0, %1}, [%2], %3;" : "=l"(v.x), "=l"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ uint64_t evict_last_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
 // Hashed single-key lookup of key word k (nonzero, home slot `home`) whose
 // first 32-byte slot group {a, b} (the aligned group holding the home slot) the
 // caller has already loaded: resolves within it when it can, else walks on.
@@ -384,7 +403,7 @@ __device__ __forceinline__ uint64_t hashed_resolve(const JTable& T, uint64_t k, 
 // group of each row that passed it. kv: the key is non-NULL.
 template <typename KT, bool UNIQUE, bool BLOOM>
 __device__ __forceinline__ void hashed_lookup2(const JTable& T, const KT (&key)[2], const bool (&kv)[2],
-                                               uint64_t (&m)[2]) {
+                                               uint64_t (&m)[2], uint64_t keep_pol, int keep_table) {
   uint64_t k[2], h[2];
   bool go[2];
 #pragma unroll
@@ -396,7 +415,7 @@ __device__ __forceinline__ void hashed_lookup2(const JTable& T, const KT (&key)[
   if (BLOOM) {
     uint64_t fw[2];
 #pragma unroll
-    for (int j = 0; j < 2; ++j) fw[j] = go[j] ? __ldg(T.bloom + (h[j] >> T.bshift)) : 0;
+    for (int j = 0; j < 2; ++j) fw[j] = go[j] ? ld_keep_l2(T.bloom + (h[j] >> T.bshift), keep_pol) : 0;
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
       const uint64_t bm = bloom_mask(h[j]);
@@ -413,8 +432,13 @@ __device__ __forceinline__ void hashed_lookup2(const JTable& T, const KT (&key)[
     b[j] = make_ulonglong2(0, 0);
     if (go[j] && k[j] != 0) {
       const uint64_t g = home[j] & ~3ull;
-      a[j] = __ldg(base + (g >> 1));
-      b[j] = __ldg(base + (g >> 1) + 1);
+      if (keep_table) {
+        a[j] = ld_keep_l2x2(base + (g >> 1), keep_pol);
+        b[j] = ld_keep_l2x2(base + (g >> 1) + 1, keep_pol);
+      } else {
+        a[j] = __ldg(base + (g >> 1));
+        b[j] = __ldg(base + (g >> 1) + 1);
+      }
     }
   }
 #pragma unroll
@@ -433,6 +457,7 @@ struct SinkK {
   uint64_t n;
   JTable T;
   unsigned long long* acc;  // [0] count, [1] sum, [2] any non-null payload matched
+  int keep_table;           // hashed table reads also evict-last in L2 (QEG_JOIN_TABLE_KEEP_L2=1)
 };
 
 template <typename T>
@@ -653,6 +678,7 @@ __global__ void __launch_bounds__(256, MINB) probe_sink_lean_kernel(const SinkK 
   const KT* keys = static_cast<const KT*>(P.key);
   const VT* vals = static_cast<const VT*>(P.val);
   const unsigned lane = threadIdx.x & 31u;
+  const uint64_t keep_pol = STRAT == QEG_JOIN_HASH ? evict_last_policy() : 0;
   constexpr uint32_t kTile = 64u * U;
   const uint32_t ntiles = static_cast<uint32_t>(P.n / kTile);
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -682,7 +708,7 @@ __global__ void __launch_bounds__(256, MINB) probe_sink_lean_kernel(const SinkK 
       for (int c = 0; c < U; ++c) {
         const bool kv[2] = {((ckw[c] >> (2 * lane)) & 1ull) != 0, ((ckw[c] >> (2 * lane + 1)) & 1ull) != 0};
         uint64_t m[2];
-        hashed_lookup2<KT, UNIQUE, BLOOM>(P.T, ck[c], kv, m);
+        hashed_lookup2<KT, UNIQUE, BLOOM>(P.T, ck[c], kv, m, keep_pol, P.keep_table);
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
           cnt += static_cast<Cnt>(m[j]);
@@ -937,7 +963,20 @@ struct PartK {
   unsigned long long* cursor;  // [P] next free row of each partition (pass 2)
   uint64_t* okey;              // key words, partition order
   int64_t* oval;               // payloads, partition order
+  const uint64_t* bloom;       // the table's Bloom filter: rows that miss it are dropped (nullptr: none)
+  int bshift;
 };
+
+// Partition of probe key word k, or -1 when the build side's Bloom filter
+// rules the key out.
+__device__ __forceinline__ int probe_part(const PartK& P, uint64_t k, uint64_t pol) {
+  const uint64_t h = single_key_hash(k);
+  if (P.bloom) {
+    const uint64_t bm = bloom_mask(h);
+    if ((ld_keep_l2(P.bloom + (h >> P.bshift), pol) & bm) != bm) return -1;
+  }
+  return static_cast<int>(h >> (64 - P.bits));
+}
 
 // Pass 1: partition sizes (shared-memory histogram per CTA, then reductions).
 template <typename KT>
@@ -947,9 +986,11 @@ __global__ void __launch_bounds__(512) ppart_hist_kernel(const PartK P) {
   for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) phist[i] = 0;
   __syncthreads();
   const KT* keys = static_cast<const KT*>(P.key);
+  const uint64_t pol = evict_last_policy();
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < P.n; r += (uint64_t)gridDim.x * blockDim.x) {
     if (P.kvalid && !((__ldg(P.kvalid + (r >> 6)) >> (r & 63)) & 1ull)) continue;
-    atomicAdd(phist + key_part(sink_word(__ldg(keys + r)), P.bits), 1u);
+    const int part = probe_part(P, sink_word(__ldg(keys + r)), pol);
+    if (part >= 0) atomicAdd(phist + part, 1u);
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
@@ -972,6 +1013,7 @@ __global__ void __launch_bounds__(512) ppart_scatter_kernel(const PartK P) {
   constexpr int kPer = kPartTile / 512;
   const KT* keys = static_cast<const KT*>(P.key);
   const VT* vals = static_cast<const VT*>(P.val);
+  const uint64_t pol = evict_last_policy();
   const uint64_t ntiles = (P.n + kPartTile - 1) / kPartTile;
   for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) cnt[i] = 0;
@@ -984,10 +1026,13 @@ __global__ void __launch_bounds__(512) ppart_scatter_kernel(const PartK P) {
       const uint64_t r = t * kPartTile + j * 512 + threadIdx.x;
       part[j] = 0xffffffffu;
       if (r < P.n && (!P.kvalid || ((__ldg(P.kvalid + (r >> 6)) >> (r & 63)) & 1ull))) {
-        k[j] = sink_word(__ldg(keys + r));
-        v[j] = static_cast<int64_t>(__ldg(vals + r));
-        part[j] = key_part(k[j], P.bits);
-        rank[j] = atomicAdd(cnt + part[j], 1u);
+        k[j] = sink_word(__ldcs(keys + r));
+        v[j] = static_cast<int64_t>(__ldcs(vals + r));
+        const int pp = probe_part(P, k[j], pol);
+        if (pp >= 0) {
+          part[j] = static_cast<uint32_t>(pp);
+          rank[j] = atomicAdd(cnt + part[j], 1u);
+        }
       }
     }
     __syncthreads();
@@ -2162,6 +2207,8 @@ void partitioned_sink(JoinState& st, const DevCol& key, const DevCol& val, uint6
   K.val = val.data;
   K.n = n;
   K.bits = st.part_bits;
+  K.bloom = st.bloom.get<uint64_t>();
+  K.bshift = st.bloom_shift;
   DevBuf hist(static_cast<size_t>(np) * 8, ctx->stream), cursor((static_cast<size_t>(np) + 1) * 8, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(hist.get(), 0, hist.bytes(), ctx->stream));
   K.hist = hist.get<unsigned long long>();
@@ -2745,6 +2792,7 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       S.n = n;
       S.T = st.table();
       S.acc = st.acc.get<unsigned long long>();
+      if (const char* e = getenv("QEG_JOIN_TABLE_KEEP_L2")) S.keep_table = atoi(e) != 0;
       if (st.strategy == QEG_JOIN_PARTITIONED && v.dev.all_valid) {
         // (Payload NULLs would need a partitioned validity column: the direct
         // hashed sink below handles them.)

@@ -302,12 +302,16 @@ def test_count_sum_bloom_filter_by_table_size(ctx):
 @pytest.mark.parametrize("ktype", [O.I64, O.I32])
 @pytest.mark.parametrize("bits", [0, 6])
 @pytest.mark.parametrize("vnulls", [False, True])
-def test_partitioned_count_sum_sink(ctx, dup, ktype, bits, vnulls):
+@pytest.mark.parametrize("bloom", ["0", "1"])
+def test_partitioned_count_sum_sink(ctx, dup, ktype, bits, vnulls, bloom, monkeypatch):
     """The radix-partitioned join (the probe side split by key-hash partition
     in one tile-sorted pass, then probed in partition order against the hash
     table) against the oracle: unique or duplicated build keys, NULL keys on
     both sides, 64-bit and 32-bit keys (negative values included), automatic
-    or fixed partition bits; with payload NULLs the direct hashed sink runs."""
+    or fixed partition bits, with and without the build keys' Bloom filter
+    (rows it rules out are not partitioned); with payload NULLs the direct
+    hashed sink runs."""
+    monkeypatch.setenv("QEG_JOIN_BLOOM", bloom)
     rng = np.random.default_rng(500 + dup + 2 * (ktype == O.I32) + bits + 7 * vnulls)
     nb, npr = 1 << 17, (1 << 21) + 77
     dt = np.int64 if ktype == O.I64 else np.int32
