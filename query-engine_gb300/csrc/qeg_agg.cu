@@ -2105,6 +2105,9 @@ static std::vector<StagedCol> pool_columns(const AggState& st, uint64_t first) {
 void AggState::part_second_pass() {
   const uint64_t np = 1ull << part_bits;
   AggK P = kparams_base();
+  // The second-pass table slot comes from the partition hash bits below the
+  // partition bits.
+  P.part_shift = 64 - part_bits;
   for (size_t c = 0; c < val_cols.size(); ++c) {
     P.val[c].type = types[val_cols[c]] == QEG_F64 ? QEG_F64 : QEG_I64;
     P.val[c].all_valid = 1;
