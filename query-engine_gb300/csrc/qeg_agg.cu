@@ -22,6 +22,8 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cmath>
+#include <cstring>
+#include <unordered_map>
 
 #include "qeg_agg.h"
 #include "qeg_warpagg.cuh"
@@ -63,6 +65,9 @@ constexpr uint64_t kPartMinTableBytes = 64ull << 20;
 // estimate averages at most kPartMaxFill of a second-pass table per partition.
 constexpr int kPartMaxBits = 15;
 constexpr double kPartMaxFill = 0.6;
+// ... and only while the sketch's heavy hitters cover less than this share of
+// the rows (a heavy head is better served by the CTA-private tables).
+constexpr double kPartMaxHotShare = 0.3;
 
 __device__ __forceinline__ uint64_t ld_volatile_shared(const uint64_t* p) {
   return *reinterpret_cast<const volatile uint64_t*>(p);
@@ -792,87 +797,98 @@ __global__ void rehash_kernel(const AggK P, const uint64_t* __restrict__ old, ui
 // use cheap multiplicative hashes (one 64-bit multiply); the global table and
 // the tail rows keep the table's own key hash.
 // ---------------------------------------------------------------------------
-constexpr uint64_t kHotMul = 0x9E3779B97F4A7C15ull;
 constexpr uint64_t kPartMul = 0xD1B54A32D192ED03ull;
 
-// Slot of key word k in a heavy-hitter table of 2^lg slots.
-__device__ __forceinline__ uint32_t hot_slot(uint64_t k, int lg) {
-  return static_cast<uint32_t>(((k ^ (k >> 29)) * kHotMul) >> (64 - lg));
-}
 // Partition hash of key word k: the partition is its top bits, a second-pass
 // table slot the bits below them.
 __device__ __forceinline__ uint64_t part_mix(uint64_t k) { return (k ^ (k >> 31)) * kPartMul; }
 
+// Hash of a hot-key lookup (its top bits pick the bucket) and the slot of a
+// key given its bucket's displacement d: the displacement is mixed in before
+// the final multiply, so each d places a bucket's keys independently.
+__host__ __device__ __forceinline__ uint64_t hot_phf_hash(uint64_t k) {
+  return (k ^ (k >> 29)) * 0x9E3779B97F4A7C15ull;
+}
+__host__ __device__ __forceinline__ uint32_t hot_phf_slot(uint64_t h, uint32_t d, int lgT) {
+  return static_cast<uint32_t>(((h ^ (static_cast<uint64_t>(d) * 0xC2B2AE3D27D4EB4Full)) * 0x94D049BB133111EBull) >>
+                               (64 - lgT));
+}
+
+// Heavy-hitter lookup: a perfect hash of the hot key words built on the host
+// (hot_phf_build; hash-and-displace), so a lookup is a fixed sequence of two
+// multiplies and three shared-memory loads with no probe loop. Layout (words
+// of 8 bytes): [2^lgT slot keys (0 = empty)][2^lgT u16 slot ranks][2^lgB u16
+// bucket displacements].
+__device__ __forceinline__ int phf_rank(const uint64_t* skey, const uint16_t* srank, const uint16_t* disp, int lgT,
+                                        int lgB, uint64_t k) {
+  const uint64_t h = hot_phf_hash(k);
+  const uint32_t b = static_cast<uint32_t>(h >> (64 - lgB));
+  const uint32_t s = hot_phf_slot(h, disp[b], lgT);
+  return skey[s] == k ? static_cast<int>(srank[s]) : -1;
+}
+
 // Parameters of the partitioned passes beyond AggK.
 struct PartA {
-  int hot_lg;                // heavy-hitter table: 2^hot_lg key slots
   int nhot;                  // heavy hitters (ranks 0..nhot-1); rank nhot: NULL key, nhot + 1: key word 0
   int rw;                    // field words per heavy-hitter row (odd)
+  int lgT, lgB;              // heavy-hitter perfect hash: 2^lgT slots, 2^lgB buckets
+  const uint64_t* phf;       // its words (phf_words of them)
+  int phf_words;
   unsigned long long* hist;  // sizing pass: rows per partition
 };
 
-// Builds the read-only heavy-hitter table in shared memory: key words (0 =
-// empty) and each slot's rank. All threads call it; ends with a barrier.
-__device__ __forceinline__ void load_hot_table(const AggK& P, const PartA& A, uint64_t* hk, uint16_t* hr) {
-  const int hs = 1 << A.hot_lg;
-  for (int i = threadIdx.x; i < hs; i += blockDim.x) hk[i] = 0;
-  __syncthreads();
-  for (int i = threadIdx.x; i < A.nhot; i += blockDim.x) {
-    const uint64_t k = P.hot[i];
-    if (k == 0) continue;  // (key word 0 has its own row)
-    uint32_t s = hot_slot(k, A.hot_lg);
-    for (int t = 0; t < hs; ++t) {
-      const unsigned long long old =
-          atomicCAS(reinterpret_cast<unsigned long long*>(&hk[s]), 0ull, static_cast<unsigned long long>(k));
-      if (old == 0) {
-        hr[s] = static_cast<uint16_t>(i);
-        break;
-      }
-      if (old == k) break;  // (a repeated candidate keeps its first rank)
-      s = (s + 1) & (hs - 1);
-    }
-  }
+// Copies the heavy-hitter perfect hash into shared memory. All threads call
+// it; ends with a barrier.
+__device__ __forceinline__ void load_phf(const PartA& A, uint64_t* sm) {
+  for (int i = threadIdx.x; i < A.phf_words; i += blockDim.x) sm[i] = __ldg(A.phf + i);
   __syncthreads();
 }
 
-// Rank of key word k (nonzero) among the heavy hitters, or -1.
-__device__ __forceinline__ int hot_rank(const uint64_t* hk, const uint16_t* hr, int lg, uint64_t k) {
-  const uint32_t mask = (1u << lg) - 1u;
-  uint32_t s = hot_slot(k, lg);
-  for (uint32_t t = 0; t <= mask; ++t) {
-    const uint64_t cur = hk[s];
-    if (cur == k) return hr[s];
-    if (cur == 0) return -1;
-    s = (s + 1) & mask;
-  }
-  return -1;
+// Rows each thread keeps in flight in the partitioned passes: fewer when
+// more value columns travel with each row (registers).
+template <int NV>
+constexpr int part_rows() {
+  return NV <= 2 ? 4 : (NV <= 4 ? 2 : 1);
 }
 
 // Sizing pass: rows per partition of every row that will reach the pool (a
 // non-NULL key other than key word 0 and not a heavy hitter). 32-bit counters
-// per CTA in shared memory, added to A.hist at the end.
+// per CTA in shared memory, added to A.hist at the end. Each thread has R
+// rows in flight per iteration (coalesced: row j of a tile is j * blockDim.x
+// + threadIdx.x), their key loads issued before any is used.
+template <int R>
 __global__ void __launch_bounds__(1024) part_hist_kernel(const AggK P, const PartA A) {
   extern __shared__ uint64_t hsm[];
-  const int hs = 1 << A.hot_lg;
-  uint64_t* hk = hsm;
-  uint16_t* hr = reinterpret_cast<uint16_t*>(hk + hs);
-  uint32_t* cnt = reinterpret_cast<uint32_t*>(hr + hs);
+  const int T = 1 << A.lgT;
+  const uint64_t* skey = hsm;
+  const uint16_t* srank = reinterpret_cast<const uint16_t*>(hsm + T);
+  const uint16_t* disp = srank + T;
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(hsm + A.phf_words);
   const uint32_t np = 1u << (64 - P.part_shift);
   for (uint32_t i = threadIdx.x; i < np; i += blockDim.x) cnt[i] = 0;
-  load_hot_table(P, A, hk, hr);
+  load_phf(A, hsm);
   const DevCol& kc = P.key[0];
-  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < P.nrows; i += stride) {
-    uint64_t p = i;
-    if (P.sel) {
-      p = P.sel[i];
-      if (p >= P.len) continue;  // (the first pass reports it)
+  const uint64_t tile = static_cast<uint64_t>(blockDim.x) * R;
+  for (uint64_t base = blockIdx.x * tile; base < P.nrows; base += static_cast<uint64_t>(gridDim.x) * tile) {
+    uint64_t kw[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const uint64_t i = base + static_cast<uint64_t>(j) * blockDim.x + threadIdx.x;
+      bool ok = i < P.nrows;
+      uint64_t p = i;
+      if (ok && P.sel) {
+        p = P.sel[i];
+        ok = p < P.len;  // (the first pass reports it)
+      }
+      ok = ok && col_valid(kc, p);
+      kw[j] = ok ? key_word(kc, p) : 0;
     }
-    if (!col_valid(kc, p)) continue;
-    const uint64_t k = key_word(kc, p);
-    if (k == 0) continue;
-    if (A.nhot > 0 && hot_rank(hk, hr, A.hot_lg, k) >= 0) continue;
-    atomicAdd(&cnt[part_mix(k) >> P.part_shift], 1u);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const uint64_t k = kw[j];
+      if (k != 0 && phf_rank(skey, srank, disp, A.lgT, A.lgB, k) < 0)
+        atomicAdd(&cnt[part_mix(k) >> P.part_shift], 1u);
+    }
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < np; i += blockDim.x)
@@ -880,75 +896,78 @@ __global__ void __launch_bounds__(1024) part_hist_kernel(const AggK P, const Par
 }
 
 // First pass. Heavy hitters (and the NULL key and key word 0, which always
-// have rows) aggregate into CTA rows by rank with warp peer aggregation; every
-// other row is appended to its partition's region (lanes of one partition
-// share one reservation). At the end each CTA merges its rows into the global
-// table.
-template <int NV, uint32_t SPEC>
+// have rows) aggregate into the CTA's rows by rank with warp peer aggregation
+// (matched on the 32-bit rank); every other row is appended to its
+// partition's region. R rows per thread are loaded before any is applied.
+// At the end each CTA merges its rows into the global table.
+template <int NV, uint32_t SPEC, int R>
 __global__ void __launch_bounds__(512) part_pass1_kernel(const AggK P, const PartA A) {
   extern __shared__ uint64_t psm[];
-  const int hs = 1 << A.hot_lg;
-  uint64_t* hk = psm;
-  uint16_t* hr = reinterpret_cast<uint16_t*>(hk + hs);
-  uint64_t* rows = hk + hs + (hs * 2 + 7) / 8;  // (nhot + 2) rows of A.rw words
+  const int T = 1 << A.lgT;
+  const uint64_t* skey = psm;
+  const uint16_t* srank = reinterpret_cast<const uint16_t*>(psm + T);
+  const uint16_t* disp = srank + T;
+  uint64_t* rows = psm + A.phf_words;  // (nhot + 2) rows of A.rw words
+  const unsigned lane = threadIdx.x & 31u;
   const int RW = A.rw;
   const int nrow = A.nhot + 2;
   for (int i = threadIdx.x; i < nrow * RW; i += blockDim.x) rows[i] = 0;
-  load_hot_table(P, A, hk, hr);
-  const unsigned lane = threadIdx.x & 31u;
+  load_phf(A, psm);
   const DevCol& kc = P.key[0];
-  const uint64_t step = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  for (uint64_t base = static_cast<uint64_t>(blockIdx.x) * blockDim.x + (threadIdx.x & ~31u); base < P.nrows;
-       base += step) {
-    const uint64_t i = base + lane;
-    bool live = i < P.nrows;
-    uint64_t p = i;
-    if (live && P.sel) {
-      p = P.sel[i];
-      if (p >= P.len) {
-        atomicOr(P.err, kDevBadInput);
-        live = false;
-      }
-    }
-    bool vv[kMaxVals];
-    uint64_t vb[kMaxVals];
+  const uint64_t tile = static_cast<uint64_t>(blockDim.x) * R;
+  for (uint64_t base = blockIdx.x * tile; base < P.nrows; base += static_cast<uint64_t>(gridDim.x) * tile) {
+    uint64_t pr[R], kw[R];
+    bool live[R], kv[R];
+    bool vv[R][kMaxVals];
+    uint64_t vb[R][kMaxVals];
 #pragma unroll
-    for (int c = 0; c < kMaxVals; ++c) {
-      vv[c] = false;
-      vb[c] = 0;
+    for (int j = 0; j < R; ++j) {
+      const uint64_t i = base + static_cast<uint64_t>(j) * blockDim.x + threadIdx.x;
+      live[j] = i < P.nrows;
+      uint64_t p = i;
+      if (live[j] && P.sel) {
+        p = P.sel[i];
+        if (p >= P.len) {
+          atomicOr(P.err, kDevBadInput);
+          live[j] = false;
+        }
+      }
+      pr[j] = p;
+#pragma unroll
+      for (int c = 0; c < kMaxVals; ++c) {
+        vv[j][c] = false;
+        vb[j][c] = 0;
+      }
+      if (live[j]) load_values<NV>(P, p, vv[j], vb[j]);
+      kv[j] = live[j] && col_valid(kc, p);
+      kw[j] = kv[j] ? key_word(kc, p) : 0;
     }
-    if (live) load_values<NV>(P, p, vv, vb);
-    const bool kv = live && col_valid(kc, p);
-    const uint64_t k = kv ? key_word(kc, p) : 0;
-    int rank = -1;
-    if (live) rank = !kv ? A.nhot : (k == 0 ? A.nhot + 1 : (A.nhot > 0 ? hot_rank(hk, hr, A.hot_lg, k) : -1));
-    const bool hot = rank >= 0;
-    if (__ballot_sync(0xffffffffu, hot)) {
-      const unsigned peers = __match_any_sync(0xffffffffu, hot ? static_cast<unsigned>(rank) : (0x80000000u | lane));
-      const bool leader = hot && __ffs(peers) - 1 == static_cast<int>(lane);
-      const PeerPlan pp = plan_peers(peers, lane);
-      uint64_t* f = rows + static_cast<size_t>(hot ? rank : 0) * RW;
-      if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader, kRowShared, peers, pp, vv, vb);
-      else warp_apply<NV>(f, leader, kRowShared, peers, pp, P, vv, vb);
-    }
-    const bool cold = live && !hot;
-    if (__ballot_sync(0xffffffffu, cold)) {
-      const uint32_t part = cold ? static_cast<uint32_t>(part_mix(k) >> P.part_shift) : 0xffffffffu;
-      const unsigned same = __match_any_sync(0xffffffffu, part);
-      const int first = __ffs(same) - 1;
-      unsigned long long b = 0;
-      if (cold && static_cast<int>(lane) == first)
-        b = atomicAdd(P.part_fill + part, static_cast<unsigned long long>(__popc(same)));
-      b = __shfl_sync(0xffffffffu, b, first);
-      if (cold) {
-        const uint64_t at = P.part_off[part] + b + static_cast<unsigned>(__popc(same & ((1u << lane) - 1u)));
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const uint64_t k = kw[j];
+      int rank = -1;
+      if (live[j]) rank = !kv[j] ? A.nhot : (k == 0 ? A.nhot + 1 : phf_rank(skey, srank, disp, A.lgT, A.lgB, k));
+      const bool hot = rank >= 0;
+      if (__ballot_sync(0xffffffffu, hot)) {
+        // Lanes of one rank combine their rows; the lowest applies them.
+        const unsigned peers = __match_any_sync(0xffffffffu, hot ? static_cast<unsigned>(rank) : (0x80000000u | lane));
+        const bool leader = hot && __ffs(peers) - 1 == static_cast<int>(lane);
+        const PeerPlan pp = plan_peers(peers, lane);
+        uint64_t* f = rows + static_cast<size_t>(hot ? rank : 0) * RW;
+        if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader, kRowShared, peers, pp, vv[j], vb[j]);
+        else warp_apply<NV>(f, leader, kRowShared, peers, pp, P, vv[j], vb[j]);
+      }
+      if (live[j] && !hot) {
+        // Partitions are many: lanes rarely share one, so each reserves alone.
+        const uint32_t part = static_cast<uint32_t>(part_mix(k) >> P.part_shift);
+        const uint64_t at = P.part_off[part] + atomicAdd(P.part_fill + part, 1ull);
         if (at < P.part_off[part + 1]) {
           P.pool_key[at] = k;
 #pragma unroll
           for (int c = 0; c < NV; ++c)
-            if (c < P.nvals) P.pool_val[c][at] = vb[c];
+            if (c < P.nvals) P.pool_val[c][at] = vb[j][c];
         } else {
-          spill_row(P, p);  // (the sizing pass counted every such row: not reached)
+          spill_row(P, pr[j]);  // (the sizing pass counted every such row: not reached)
         }
       }
     }
@@ -1006,13 +1025,14 @@ __device__ __forceinline__ int part_smem_slot(uint64_t* sm, int lgS, int shift, 
 
 // Second pass: each CTA takes partitions in turn and aggregates the
 // partition's pool rows (every key nonzero and non-NULL, every value present)
-// in a shared-memory table with warp peer aggregation, each warp loading its
-// next rows before it works on the current ones; then it appends the table's
-// groups to the tail rows with one reservation per CTA and clears the rows it
-// used. A partition with more groups than the table holds is listed as failed
-// and appends nothing (the host aggregates it into the global table instead),
-// so the pass can be re-run with a larger tail buffer.
-template <int NV, uint32_t SPEC>
+// in a shared-memory table, with R rows per thread loaded before any is
+// applied; lanes whose rows share a slot (a key) combine them first (warp peer
+// aggregation, matched on the 32-bit slot); then it appends the table's groups to
+// the tail rows with one reservation per CTA and clears the rows it used. A
+// partition with more groups than the table holds is listed as failed and
+// appends nothing (the host aggregates it into the global table instead), so
+// the pass can be re-run with a larger tail buffer.
+template <int NV, uint32_t SPEC, int R>
 __global__ void __launch_bounds__(1024) part_agg_kernel(const AggK P, const PartB B) {
   extern __shared__ uint64_t sm[];
   __shared__ int s_fail;
@@ -1028,45 +1048,46 @@ __global__ void __launch_bounds__(1024) part_agg_kernel(const AggK P, const Part
     __syncthreads();
     const uint64_t begin = B.part_off[part];
     const uint64_t n = B.part_off[part + 1] - begin;
-    // Rows of this warp's first iteration.
-    uint64_t b = static_cast<uint64_t>(warp) * 32;
-    uint64_t nk = 0;
-    uint64_t nvb[kMaxVals];
-    auto load = [&](uint64_t at) {
-      const bool ok = at < n;
-      nk = ok ? __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_key + begin + at)) : 0;
+    const uint64_t tile = static_cast<uint64_t>(blockDim.x) * R;
+    for (uint64_t b0 = 0; b0 < n; b0 += tile) {
+      uint64_t kw[R];
+      bool vv[R][kMaxVals];
+      uint64_t vb[R][kMaxVals];
 #pragma unroll
-      for (int c = 0; c < NV; ++c)
-        nvb[c] = (ok && c < P.nvals) ? __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_val[c] + begin + at))
-                                     : 0;
-    };
-    load(b + lane);
-    for (; b < n; b += static_cast<uint64_t>(nwarps) * 32) {
-      const bool live = b + lane < n;
-      const uint64_t k = nk;
-      bool vv[kMaxVals];
-      uint64_t vb[kMaxVals];
+      for (int j = 0; j < R; ++j) {
+        const uint64_t at = b0 + static_cast<uint64_t>(j) * blockDim.x + threadIdx.x;
+        const bool ok = at < n;
+        kw[j] = ok ? static_cast<uint64_t>(__ldcs(reinterpret_cast<const unsigned long long*>(B.pool_key + begin + at)))
+                   : 0;
 #pragma unroll
-      for (int c = 0; c < kMaxVals; ++c) {
-        vv[c] = live && c < NV && c < P.nvals;
-        vb[c] = c < NV ? nvb[c] : 0;
+        for (int c = 0; c < kMaxVals; ++c) {
+          vv[j][c] = ok && c < NV && c < P.nvals;
+          vb[j][c] = (ok && c < NV && c < P.nvals)
+                         ? static_cast<uint64_t>(
+                               __ldcs(reinterpret_cast<const unsigned long long*>(B.pool_val[c] + begin + at)))
+                         : 0;
+        }
       }
-      load(b + static_cast<uint64_t>(nwarps) * 32 + lane);  // the next iteration's rows, in flight meanwhile
-      const unsigned livemask = __ballot_sync(0xffffffffu, live);
-      const unsigned same = __match_any_sync(0xffffffffu, live ? k : ~0ull - lane);
-      const unsigned peers = live ? (same & livemask) : (1u << lane);
-      const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
-      uint64_t* f = nullptr;
-      if (leader) {
-        const int slot = part_smem_slot(sm, lgS, P.part_shift, SW, k, part_mix(k));
-        if (slot >= 0) f = &sm[static_cast<size_t>(slot) * SW + 1];
-        else s_fail = 1;
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        const uint64_t k = kw[j];
+        const bool live = k != 0;  // (pool keys are nonzero: zero marks a row past the partition's end)
+        int slot = -1;
+        if (live) {
+          slot = part_smem_slot(sm, lgS, P.part_shift, SW, k, part_mix(k));
+          if (slot < 0) s_fail = 1;
+        }
+        const bool ok = slot >= 0;
+        if (__ballot_sync(0xffffffffu, ok)) {
+          // A slot holds one key: lanes of one slot combine their rows.
+          const unsigned peers = __match_any_sync(0xffffffffu, ok ? static_cast<unsigned>(slot) : (0x80000000u | lane));
+          const bool leader = ok && __ffs(peers) - 1 == static_cast<int>(lane);
+          const PeerPlan pp = plan_peers(peers, lane);
+          uint64_t* f = &sm[static_cast<size_t>(ok ? slot : 0) * SW + 1];
+          if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader, kRowShared, peers, pp, vv[j], vb[j]);
+          else warp_apply<NV>(f, leader, kRowShared, peers, pp, P, vv[j], vb[j]);
+        }
       }
-      const unsigned placed = __ballot_sync(0xffffffffu, f != nullptr);
-      const bool ok = live && ((placed >> (__ffs(peers) - 1)) & 1u);
-      const PeerPlan pp = plan_peers(ok ? peers : (1u << lane), lane);
-      if constexpr (SPEC != kGenericSpec) spec_apply<SPEC, NV>(f, leader && ok, kRowShared, peers, pp, vv, vb);
-      else warp_apply<NV>(f, leader && ok, kRowShared, peers, pp, P, vv, vb);
     }
     __syncthreads();
     const bool failed = s_fail != 0;
@@ -1890,14 +1911,18 @@ void AggState::first_consume(const std::vector<StagedCol>& staged, uint64_t nrow
     want = static_cast<uint64_t>(std::max(kEstimateHeadroom * est_groups / kTargetLoad, 1024.0));
   }
   // Partitioned strategy: asked for, or chosen when the estimate puts the
-  // global table far beyond L2 (every row outside the private tables would be
-  // a random DRAM round trip there). Its global table only takes the private
-  // tables' flushes, so it starts small.
+  // global table far beyond L2 (every row would be a random DRAM round trip
+  // there) and the key column has no heavy head. With a heavy head the
+  // CTA-private tables absorb most rows and the rest reach the global table:
+  // on GB300, 512M Zipf(1.1) rows over 64M keys take 28.0 ms that way against
+  // 31.3 ms partitioned. Its global table only takes the private tables'
+  // flushes, so it starts small.
   bool go_part = false;
   if (mode == 1 && part_eligible(staged)) {
     if (cfg.strategy == QEG_AGG_PARTITIONED)
       go_part = true;
     else if (cfg.strategy == QEG_AGG_AUTO && nrows >= kPartMinRows && est_groups > 0 &&
+             hot_share < kPartMaxHotShare &&
              est_groups / kTargetLoad * row_words * 8.0 >= static_cast<double>(kPartMinTableBytes) &&
              est_groups <= kPartMaxFill * part_table_slots() * static_cast<double>(1u << kPartMaxBits))
       go_part = true;  // (more groups than 2^15 second-pass tables hold: the global table)
@@ -1999,6 +2024,84 @@ void AggState::setup_partitioned(uint64_t nrows) {
   // partition in shared memory.
   part_bits = std::max(1, std::min(bits, kPartMaxBits));
   strategy = QEG_AGG_PARTITIONED;
+  // The heavy hitters' perfect hash (ranks = positions in the candidate list).
+  std::vector<uint64_t> words;
+  hot_phf_build(heavy_candidates.data(), nhot, &phf_lgT, &phf_lgB, words);
+  phf_words = static_cast<int>(words.size());
+  phf_dev.alloc(words.size() * 8, ctx->stream);
+  QEG_CUDA(cudaMemcpyAsync(phf_dev.get(), words.data(), words.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+// Builds the perfect hash of the first n candidate key words (rank = index;
+// key word 0, which has a row of its own, and repeats are left out) by hash
+// and displace: 2^lgT slots for at least twice the keys, buckets of about four
+// keys by the hash's top bits, and for each bucket, largest first, the first
+// displacement that puts all its keys in free slots. Layout of `words`: slot
+// keys, then u16 slot ranks, then u16 bucket displacements.
+void hot_phf_build(const uint64_t* keys, int n, int* lgT_out, int* lgB_out, std::vector<uint64_t>& words) {
+  std::vector<std::pair<uint64_t, int>> ks;
+  {
+    std::unordered_map<uint64_t, int> seen;
+    for (int i = 0; i < n; ++i)
+      if (keys[i] != 0 && seen.emplace(keys[i], i).second) ks.emplace_back(keys[i], i);
+  }
+  int lgT = 6;
+  while ((size_t{1} << lgT) < 2 * ks.size()) ++lgT;
+  for (;; ++lgT) {
+    require(lgT <= 16, "heavy-hitter perfect hash could not be built");
+    const int lgB = lgT - 3;
+    const size_t T = size_t{1} << lgT, B = size_t{1} << lgB;
+    std::vector<std::vector<int>> buckets(B);
+    std::vector<uint64_t> hs(ks.size());
+    for (size_t i = 0; i < ks.size(); ++i) {
+      hs[i] = hot_phf_hash(ks[i].first);
+      buckets[hs[i] >> (64 - lgB)].push_back(static_cast<int>(i));
+    }
+    std::vector<uint32_t> order(B);
+    for (size_t b = 0; b < B; ++b) order[b] = static_cast<uint32_t>(b);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return buckets[a].size() > buckets[b].size(); });
+    std::vector<uint64_t> skey(T, 0);
+    std::vector<uint16_t> srank(T, 0), disp(B, 0);
+    bool ok = true;
+    for (uint32_t b : order) {
+      const auto& bk = buckets[b];
+      if (bk.empty()) break;
+      bool placed = false;
+      for (uint32_t d = 0; d < 65536 && !placed; ++d) {
+        std::vector<uint32_t> slots;
+        bool free_all = true;
+        for (int i : bk) {
+          const uint32_t sl = hot_phf_slot(hs[i], d, lgT);
+          if (skey[sl] != 0 || std::find(slots.begin(), slots.end(), sl) != slots.end()) {
+            free_all = false;
+            break;
+          }
+          slots.push_back(sl);
+        }
+        if (!free_all) continue;
+        for (size_t j = 0; j < bk.size(); ++j) {
+          skey[slots[j]] = ks[bk[j]].first;
+          srank[slots[j]] = static_cast<uint16_t>(ks[bk[j]].second);
+        }
+        disp[b] = static_cast<uint16_t>(d);
+        placed = true;
+      }
+      if (!placed) {
+        ok = false;
+        break;
+      }
+    }
+    if (!ok) continue;
+    words.assign(T + (T * 2 + B * 2 + 7) / 8, 0);
+    std::memcpy(words.data(), skey.data(), T * 8);
+    std::memcpy(reinterpret_cast<uint8_t*>(words.data() + T), srank.data(), T * 2);
+    std::memcpy(reinterpret_cast<uint8_t*>(words.data() + T) + T * 2, disp.data(), B * 2);
+    *lgT_out = lgT;
+    *lgB_out = lgB;
+    return;
+  }
 }
 
 // One batch through the partitioned passes: the sizing pass counts the rows
@@ -2014,23 +2117,26 @@ void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_
   P.part_shift = 64 - part_bits;
   PartA A{};
   A.nhot = nhot;
-  A.hot_lg = 6;
-  while ((1 << A.hot_lg) < 2 * std::max(nhot, 1)) ++A.hot_lg;
   A.rw = nfields | 1;
-  const size_t hot_bytes = (static_cast<size_t>(1) << A.hot_lg) * 8 + (((static_cast<size_t>(2) << A.hot_lg) + 7) / 8) * 8;
+  A.lgT = phf_lgT;
+  A.lgB = phf_lgB;
+  A.phf = phf_dev.get<uint64_t>();
+  A.phf_words = phf_words;
+  const size_t hot_bytes = static_cast<size_t>(phf_words) * 8;
   if (part_hist.bytes() < np * 8) part_hist.alloc(np * 8, ctx->stream);
   if (part_off.bytes() < (np + 1) * 8) part_off.alloc((np + 1) * 8, ctx->stream);
   QEG_CUDA(cudaMemsetAsync(part_hist.get(), 0, np * 8, ctx->stream));
   A.hist = part_hist.get<unsigned long long>();
   {
     const size_t sb = hot_bytes + np * 4;
-    QEG_CUDA(cudaFuncSetAttribute(part_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+    constexpr int kHistRows = 8;
+    QEG_CUDA(cudaFuncSetAttribute(part_hist_kernel<kHistRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
     int per_sm = 0;
-    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_hist_kernel, 1024, sb));
+    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_hist_kernel<kHistRows>, 1024, sb));
     require(per_sm > 0, "partition sizing kernel does not fit on an SM");
     const uint64_t grid = std::max<uint64_t>(
         1, std::min<uint64_t>((nrows + 65535) / 65536, static_cast<uint64_t>(ctx->sms) * per_sm));
-    part_hist_kernel<<<(unsigned)grid, 1024, sb, ctx->stream>>>(P, A);
+    part_hist_kernel<kHistRows><<<(unsigned)grid, 1024, sb, ctx->stream>>>(P, A);
     ctx->launches++;
     QEG_CUDA(cudaGetLastError());
   }
@@ -2058,16 +2164,16 @@ void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_
     const uint32_t spec = field_spec(P);
     const int nv = static_cast<int>(val_cols.size());
     void (*kern)(AggK, PartA) = nullptr;
-    if (spec == kSpecIntF64) kern = part_pass1_kernel<2, kSpecIntF64>;
-    else if (spec == kSpecIntF64Nulls) kern = part_pass1_kernel<2, kSpecIntF64Nulls>;
-    else if (spec == kSpecF64) kern = part_pass1_kernel<1, kSpecF64>;
-    else if (spec == kSpecF64Nulls) kern = part_pass1_kernel<1, kSpecF64Nulls>;
-    else if (spec == kSpecCount) kern = part_pass1_kernel<1, kSpecCount>;
-    else if (spec == kSpecIntSumF64Stats) kern = part_pass1_kernel<2, kSpecIntSumF64Stats>;
-    else if (nv <= 1) kern = part_pass1_kernel<1, kGenericSpec>;
-    else if (nv <= 2) kern = part_pass1_kernel<2, kGenericSpec>;
-    else if (nv <= 4) kern = part_pass1_kernel<4, kGenericSpec>;
-    else kern = part_pass1_kernel<8, kGenericSpec>;
+    if (spec == kSpecIntF64) kern = part_pass1_kernel<2, kSpecIntF64, part_rows<2>()>;
+    else if (spec == kSpecIntF64Nulls) kern = part_pass1_kernel<2, kSpecIntF64Nulls, part_rows<2>()>;
+    else if (spec == kSpecF64) kern = part_pass1_kernel<1, kSpecF64, part_rows<1>()>;
+    else if (spec == kSpecF64Nulls) kern = part_pass1_kernel<1, kSpecF64Nulls, part_rows<1>()>;
+    else if (spec == kSpecCount) kern = part_pass1_kernel<1, kSpecCount, part_rows<1>()>;
+    else if (spec == kSpecIntSumF64Stats) kern = part_pass1_kernel<2, kSpecIntSumF64Stats, part_rows<2>()>;
+    else if (nv <= 1) kern = part_pass1_kernel<1, kGenericSpec, part_rows<1>()>;
+    else if (nv <= 2) kern = part_pass1_kernel<2, kGenericSpec, part_rows<2>()>;
+    else if (nv <= 4) kern = part_pass1_kernel<4, kGenericSpec, part_rows<4>()>;
+    else kern = part_pass1_kernel<8, kGenericSpec, part_rows<8>()>;
     const size_t sb = hot_bytes + static_cast<size_t>(nhot + 2) * A.rw * 8;
     QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
     int per_sm = 0;
@@ -2115,14 +2221,14 @@ void AggState::part_second_pass() {
   const uint32_t spec = field_spec(P);
   const int nv = static_cast<int>(val_cols.size());
   void (*kern)(AggK, PartB) = nullptr;
-  if (spec == kSpecIntF64) kern = part_agg_kernel<2, kSpecIntF64>;
-  else if (spec == kSpecF64) kern = part_agg_kernel<1, kSpecF64>;
-  else if (spec == kSpecCount) kern = part_agg_kernel<1, kSpecCount>;
-  else if (spec == kSpecIntSumF64Stats) kern = part_agg_kernel<2, kSpecIntSumF64Stats>;
-  else if (nv <= 1) kern = part_agg_kernel<1, kGenericSpec>;
-  else if (nv <= 2) kern = part_agg_kernel<2, kGenericSpec>;
-  else if (nv <= 4) kern = part_agg_kernel<4, kGenericSpec>;
-  else kern = part_agg_kernel<8, kGenericSpec>;
+  if (spec == kSpecIntF64) kern = part_agg_kernel<2, kSpecIntF64, part_rows<2>()>;
+  else if (spec == kSpecF64) kern = part_agg_kernel<1, kSpecF64, part_rows<1>()>;
+  else if (spec == kSpecCount) kern = part_agg_kernel<1, kSpecCount, part_rows<1>()>;
+  else if (spec == kSpecIntSumF64Stats) kern = part_agg_kernel<2, kSpecIntSumF64Stats, part_rows<2>()>;
+  else if (nv <= 1) kern = part_agg_kernel<1, kGenericSpec, part_rows<1>()>;
+  else if (nv <= 2) kern = part_agg_kernel<2, kGenericSpec, part_rows<2>()>;
+  else if (nv <= 4) kern = part_agg_kernel<4, kGenericSpec, part_rows<4>()>;
+  else kern = part_agg_kernel<8, kGenericSpec, part_rows<8>()>;
   const int block = 1024;
   const size_t sb = static_cast<size_t>(pb_slots) * (row_words | 1) * 8;
   if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));

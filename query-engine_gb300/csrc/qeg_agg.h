@@ -118,6 +118,10 @@ struct SketchResult {
   std::vector<uint64_t> heavy;  // candidate heavy-hitter key words, most frequent first
 };
 
+// Perfect hash of the first n heavy-hitter key words (qeg_agg.cu): 2^lgT
+// slots, 2^lgB buckets, packed into `words` for the partitioned passes.
+void hot_phf_build(const uint64_t* keys, int n, int* lgT, int* lgB, std::vector<uint64_t>& words);
+
 // Builds the sketch of one key column (qeg_sketch.cu).
 void sketch_key_column(qeg_ctx* ctx, const DevCol& key, const uint32_t* sel, uint64_t nrows, uint64_t len,
                        uint64_t sample_target, int want_heavy, SketchResult& out);
@@ -177,6 +181,8 @@ struct AggState {
   // rows whose key is also there and emits both.
   int part_bits = 0;
   int pb_slots = 0;
+  DevBuf phf_dev;  // the heavy hitters' perfect hash (hot_phf_build)
+  int phf_lgT = 6, phf_lgB = 3, phf_words = 0;
   DevBuf pool_key, part_fill, part_off, part_hist, part_failed, tails, part_counters;
   std::vector<DevBuf> pool_vals;
   uint64_t ntails = 0, tails_cap = 0;

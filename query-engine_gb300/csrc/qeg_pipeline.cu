@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <unordered_map>
 
 #include "qeg_agg.h"
@@ -52,6 +53,12 @@ struct PipeK {
   uint64_t key_domain;   // slots in the translation table
   const uint32_t* kstart;  // [key_domain]
   const uint32_t* kcount;  // [key_domain]
+  // [key_domain]: the group id when the key matches exactly one build row,
+  // 0x80000000 | slot when it matches several (kstart / kcount), ~0 when none.
+  const uint32_t* kfirst;
+  // The same as u16 group ids (0xffff: no match, 0xfffe: several) when the
+  // groups number at most 65533, for the trades kernel's shared-memory copy.
+  const uint16_t* kf16;
   const uint32_t* glist;   // group ids
   DevCol val[kPipeMaxVals];
   int nvals;
@@ -220,6 +227,265 @@ __global__ void __launch_bounds__(512, SPEC == kGenericSpec ? 2 : 4) pipeline_ke
       if (kind >= F_MINI) atomicMax(P.state + gi, acc);
       else atomicAdd(P.state + gi, acc);
     }
+  }
+}
+
+// Raw word of row p of column c at its type's width (I32/STR zero-extended,
+// no code map), so loads of different columns and rows never wait on each
+// other; bits_int widens an integer column's word to int64.
+__device__ __forceinline__ uint64_t raw_bits(const DevCol& c, uint64_t p) {
+  switch (c.type) {
+    case kI32:
+    case kSTR: return static_cast<uint32_t>(__ldg(static_cast<const int32_t*>(c.data) + p));
+    case kBOOL: return __ldg(static_cast<const uint8_t*>(c.data) + p);
+    default: return static_cast<uint64_t>(__ldg(static_cast<const long long*>(c.data) + p));
+  }
+}
+__device__ __forceinline__ int64_t bits_int(int32_t type, uint64_t b) {
+  return (type == kI32 || type == kSTR) ? static_cast<int64_t>(static_cast<int32_t>(static_cast<uint32_t>(b)))
+                                        : static_cast<int64_t>(b);
+}
+__device__ __forceinline__ bool bit_valid(const DevCol& c, uint64_t p) {
+  if (c.all_valid) return true;
+  return (__ldg(c.validity + (p >> 6)) >> (p & 63)) & 1ull;
+}
+// The filter predicate on the filter column's raw word (a valid row).
+__device__ __forceinline__ bool filter_bits(const PipeK& P, uint64_t b) {
+  if (P.fcol.type == kF64) {
+    const double v = __longlong_as_double(static_cast<long long>(b));
+    const double l = P.flit_f;
+    switch (P.fop) {
+      case kLT: return v < l;
+      case kLE: return v <= l;
+      case kGT: return v > l;
+      case kGE: return v >= l;
+      case kEQ: return v == l;
+      default: return v != l;
+    }
+  }
+  if (P.fop == kNever) return false;
+  if (P.fop == kAlways) return true;
+  const int64_t v = bits_int(P.fcol.type, b);
+  const int64_t l = P.flit_i;
+  switch (P.fop) {
+    case kLT: return v < l;
+    case kLE: return v <= l;
+    case kGT: return v > l;
+    case kGE: return v >= l;
+    case kEQ: return v == l;
+    default: return v != l;
+  }
+}
+
+// Active fields of a field set: field 0 (the row count) and every field
+// whose kind is not 0, in field order ("compact" indexes).
+__host__ __device__ constexpr int spec_nactive(uint32_t spec) {
+  int n = 1;
+  for (int i = 1; i <= spec_n(spec); ++i)
+    if (spec_kind(spec, i) != 0) ++n;
+  return n;
+}
+// Field index of compact index c.
+__host__ __device__ constexpr int spec_active_field(uint32_t spec, int c) {
+  int k = 0;
+  for (int i = 1; i <= spec_n(spec); ++i)
+    if (spec_kind(spec, i) != 0 && ++k == c) return i;
+  return 0;
+}
+// Compact index of field i (a field whose kind is not 0).
+__host__ __device__ constexpr int spec_compact(uint32_t spec, int i) {
+  int k = 0;
+  for (int j = 1; j <= i; ++j)
+    if (spec_kind(spec, j) != 0) ++k;
+  return k;
+}
+
+// The same plan with thread-private aggregate states: every thread owns one
+// copy of every group's active fields in shared memory, word
+// (g * NA + c) * blockDim.x + threadIdx.x, so the lanes of a warp touch
+// consecutive words whatever their groups (no bank conflicts) and a row is
+// applied with plain loads and stores, no atomics and no combining across
+// lanes. (On GB300, 64-bit shared-memory reductions cost 10 clocks per warp
+// instruction for integers and 56 for F64 without contention, several times
+// more with it; a plain read-modify-write costs 2.) Each warp takes R chunks
+// of 32 consecutive rows per tile, all their loads issued before any row is
+// applied. At the end the copies are reduced warp by warp and added to the
+// global state. NA = the active field count (spec_nactive, or nfields for
+// the generic field set).
+template <uint32_t SPEC, int R, int FASTOP>
+__global__ void __launch_bounds__(256, 1) pipeline_lanes_kernel(const PipeK P, int NA) {
+  extern __shared__ unsigned long long acc[];
+  constexpr int NVR = SPEC == kGenericSpec ? kPipeMaxVals : 2;  // value columns a row carries
+  const int T = blockDim.x;
+  const int total = P.ngroups * NA;
+  for (int i = threadIdx.x; i < total * T; i += T) acc[i] = 0;
+  __syncthreads();
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint64_t tile = static_cast<uint64_t>(T) * R;
+  // The filter column is value column 0 (the trades plan filters on price):
+  // its loaded words serve both.
+  const bool fsame = P.fcol.type >= 0 && P.nvals > 0 && P.fcol.data == P.val[0].data &&
+                     P.fcol.type == P.val[0].type && P.fcol.validity == P.val[0].validity &&
+                     P.fcol.all_valid == P.val[0].all_valid;
+  if constexpr (FASTOP >= 0) {
+    // The trades shape: a 4-byte key (dictionary codes or I32), the F64
+    // filter column as value column 0, a 4-byte integer value column 1, no
+    // NULLs, fields rows / SUM(F64) / SUM(int) (kPipeSpecAvgSum), at most
+    // 65533 groups, every probe key matching at most one build row, and a
+    // translation domain the host put in shared memory as u16 group ids (kf16:
+    // 0xffff = no match). Each lane takes 4 consecutive rows per chunk
+    // with 16-byte loads, R / 4 chunks per tile, all loads of a full tile
+    // issued before any row is applied; the last partial tile goes row by row.
+    static_assert(SPEC == kPipeSpecAvgSum, "the trades kernel has one field set");
+    constexpr int C = R / 4;  // chunks of 4 rows per lane per tile
+    const int32_t* __restrict__ key = static_cast<const int32_t*>(P.key.data);
+    const double* __restrict__ price = static_cast<const double*>(P.val[0].data);
+    const int32_t* __restrict__ qty = static_cast<const int32_t*>(P.val[1].data);
+    const double lit = P.flit_f;
+    uint16_t* kf16 = reinterpret_cast<uint16_t*>(acc + static_cast<size_t>(total) * T);
+    for (uint64_t i = threadIdx.x; i < P.key_domain; i += T) kf16[i] = P.kf16[i];
+    __syncthreads();
+    auto pass_of = [&](double v) {
+      if constexpr (FASTOP == kLT) return v < lit;
+      else if constexpr (FASTOP == kLE) return v <= lit;
+      else if constexpr (FASTOP == kGT) return v > lit;
+      else if constexpr (FASTOP == kGE) return v >= lit;
+      else if constexpr (FASTOP == kEQ) return v == lit;
+      else return v != lit;
+    };
+    // Every key matches at most one build row here (the host checked), and
+    // 4-byte keys and their domain need 32-bit arithmetic only.
+    const int32_t kmin32 = static_cast<int32_t>(P.key_min);
+    const uint32_t dom32 = static_cast<uint32_t>(P.key_domain);
+    unsigned long long* const mine = acc + threadIdx.x;
+    const int gstride = 3 * T;
+    auto apply = [&](int32_t k, double v, int32_t q) {
+      const uint32_t sl = static_cast<uint32_t>(k) - static_cast<uint32_t>(kmin32);
+      if (!pass_of(v) || k < kmin32 || sl >= dom32) return;
+      const uint32_t g = kf16[sl];
+      if (g == 0xffffu) return;
+      unsigned long long* a = mine + g * gstride;
+      a[0] += 1;
+      a[T] = static_cast<unsigned long long>(__double_as_longlong(__longlong_as_double(static_cast<long long>(a[T])) + v));
+      a[2 * T] += static_cast<unsigned long long>(static_cast<long long>(q));
+    };
+    const uint64_t full = P.n / tile * tile;  // rows in full tiles
+    for (uint64_t base = blockIdx.x * tile; base < full; base += static_cast<uint64_t>(gridDim.x) * tile) {
+      int4 kv[C], qv[C];
+      double2 pv[C][2];
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        const uint64_t p = base + (static_cast<uint64_t>(warp) * C + c) * 128 + lane * 4;
+        kv[c] = __ldg(reinterpret_cast<const int4*>(key + p));
+        qv[c] = __ldg(reinterpret_cast<const int4*>(qty + p));
+        pv[c][0] = __ldg(reinterpret_cast<const double2*>(price + p));
+        pv[c][1] = __ldg(reinterpret_cast<const double2*>(price + p + 2));
+      }
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        apply(kv[c].x, pv[c][0].x, qv[c].x);
+        apply(kv[c].y, pv[c][0].y, qv[c].y);
+        apply(kv[c].z, pv[c][1].x, qv[c].z);
+        apply(kv[c].w, pv[c][1].y, qv[c].w);
+      }
+    }
+    // The rows after the last full tile (fewer than one tile), one per thread.
+    if (blockIdx.x == gridDim.x - 1)
+      for (uint64_t p = full + threadIdx.x; p < P.n; p += T) apply(__ldg(key + p), __ldg(price + p), __ldg(qty + p));
+  } else
+  for (uint64_t base = blockIdx.x * tile; base < P.n; base += static_cast<uint64_t>(gridDim.x) * tile) {
+    uint32_t slot[R];
+    bool vv[R][NVR];
+    uint64_t vb[R][NVR];
+    // Loads: every column word of every row of the tile, none of them behind a
+    // test of another load, so all of them are in flight together.
+    uint64_t fb[R], kb[R];
+    bool fok[R], kok[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const uint64_t p = base + (static_cast<uint64_t>(warp) * R + j) * 32 + lane;
+      const bool in = p < P.n;
+      fb[j] = (in && P.fcol.type >= 0 && !fsame) ? raw_bits(P.fcol, p) : 0;
+      fok[j] = in && (P.fcol.type < 0 || bit_valid(P.fcol, p));
+      kb[j] = in ? raw_bits(P.key, p) : 0;
+      kok[j] = in && bit_valid(P.key, p);
+#pragma unroll
+      for (int c = 0; c < NVR; ++c) {
+        const bool use = in && c < P.nvals;
+        vb[j][c] = use ? raw_bits(P.val[c], p) : 0;
+        vv[j][c] = use && bit_valid(P.val[c], p);
+      }
+    }
+    // Filter (a NULL operand drops the row), key -> translation slot.
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      bool ok = kok[j] && fok[j];  // NULL keys never join
+      if (ok && P.fcol.type >= 0) ok = filter_bits(P, fsame ? vb[j][0] : fb[j]);
+      uint64_t s = ~0ull;
+      if (ok) s = static_cast<uint64_t>(bits_int(P.key.type, kb[j]) - P.key_min);
+      slot[j] = s < P.key_domain ? static_cast<uint32_t>(s) : 0xffffffffu;
+      // Integer values as int64 bits (F64 values stay as their bits).
+#pragma unroll
+      for (int c = 0; c < NVR; ++c)
+        if (c < P.nvals && P.val[c].type != kF64) vb[j][c] = static_cast<uint64_t>(bits_int(P.val[c].type, vb[j][c]));
+    }
+    // The translation table (small: cached).
+    uint32_t gi[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) gi[j] = slot[j] != 0xffffffffu ? __ldg(P.kfirst + slot[j]) : 0xffffffffu;
+    // Apply.
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const uint32_t g0 = gi[j];
+      if (g0 == 0xffffffffu) continue;
+      const bool multi = (g0 & 0x80000000u) != 0;
+      uint32_t cnt = 1, s0 = 0;
+      if (multi) {
+        cnt = __ldg(P.kcount + (g0 & 0x7fffffffu));
+        s0 = __ldg(P.kstart + (g0 & 0x7fffffffu));
+      }
+      for (uint32_t m = 0; m < cnt; ++m) {
+        const uint32_t g = multi ? __ldg(P.glist + s0 + m) : g0;
+        unsigned long long* a = acc + static_cast<size_t>(g) * NA * T + threadIdx.x;
+        a[0] += 1;  // the row count
+        if constexpr (SPEC != kGenericSpec) {
+#pragma unroll
+          for (int i = 1; i <= spec_n(SPEC); ++i) {
+            const int kind = spec_kind(SPEC, i);
+            if (kind == 0) continue;
+            const int c = spec_col(SPEC, i);
+            unsigned long long* w = a + static_cast<size_t>(spec_compact(SPEC, i)) * T;
+            *w = field_combine(static_cast<uint8_t>(kind), *w, field_contrib(static_cast<uint8_t>(kind), vv[j][c], vb[j][c]));
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < NVR; ++c) {
+            if (c >= P.nvals) break;
+            for (int k = 0; k < P.cnf[c]; ++k) {
+              const int fi = P.cfirst[c] + k;
+              const uint8_t kind = P.fkind[fi];
+              unsigned long long* w = a + static_cast<size_t>(fi) * T;
+              *w = field_combine(kind, *w, field_contrib(kind, vv[j][c], vb[j][c]));
+            }
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // Reduce the thread copies of each (group, field) in one warp, then add the
+  // result to the global state (zero is every field's identity).
+  for (int pr = static_cast<int>(warp); pr < total; pr += static_cast<int>(nwarps)) {
+    const int g = pr / NA, c = pr % NA;
+    const int f = SPEC != kGenericSpec ? spec_active_field(SPEC, c) : c;
+    const uint8_t kind = SPEC != kGenericSpec ? static_cast<uint8_t>(f == 0 ? F_ROWS : spec_kind(SPEC, f)) : P.fkind[f];
+    const unsigned long long* src = acc + static_cast<size_t>(pr) * T;
+    uint64_t x = 0;
+    for (int t = static_cast<int>(lane); t < T; t += 32) x = field_combine(kind, x, src[t]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = field_combine(kind, x, __shfl_xor_sync(0xffffffffu, x, o));
+    if (lane == 0 && x) field_red<kRowGlobal>(reinterpret_cast<uint64_t*>(P.state + static_cast<size_t>(g) * P.nfields + f), kind, x);
   }
 }
 
@@ -496,16 +762,34 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
     P.key_domain = domain;
     for (size_t c = 0; c < vcols.size(); ++c) P.val[c] = staged[vcols[c]].dev;
     P.n = np;
+    // One-load translation for keys that match exactly one build row.
+    std::vector<uint32_t> kfirst(kstart.size(), 0xffffffffu);
+    for (uint64_t sl = 0; sl < domain; ++sl) {
+      if (kcount[sl] == 1) kfirst[sl] = glist[kstart[sl]];
+      else if (kcount[sl] > 1) kfirst[sl] = 0x80000000u | static_cast<uint32_t>(sl);
+    }
+    std::vector<uint16_t> kf16;
+    if (ngroups <= 65533) {
+      kf16.resize(kfirst.size());
+      for (size_t i = 0; i < kfirst.size(); ++i)
+        kf16[i] = kfirst[i] == 0xffffffffu ? 0xffffu : (kfirst[i] & 0x80000000u) ? 0xfffeu : static_cast<uint16_t>(kfirst[i]);
+    }
+    DevBuf dk16(std::max<size_t>(kf16.size(), 1) * 2, ctx->stream);
+    if (!kf16.empty())
+      QEG_CUDA(cudaMemcpyAsync(dk16.get(), kf16.data(), kf16.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
     DevBuf dk(kstart.size() * 4, ctx->stream), dc(kcount.size() * 4, ctx->stream),
-        dg(std::max<size_t>(glist.size(), 1) * 4, ctx->stream),
+        dkf(kfirst.size() * 4, ctx->stream), dg(std::max<size_t>(glist.size(), 1) * 4, ctx->stream),
         dstate(static_cast<size_t>(P.ngroups) * P.nfields * 8, ctx->stream);
     QEG_CUDA(cudaMemcpyAsync(dk.get(), kstart.data(), kstart.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     QEG_CUDA(cudaMemcpyAsync(dc.get(), kcount.data(), kcount.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    QEG_CUDA(cudaMemcpyAsync(dkf.get(), kfirst.data(), kfirst.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     if (!glist.empty())
       QEG_CUDA(cudaMemcpyAsync(dg.get(), glist.data(), glist.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     QEG_CUDA(cudaMemsetAsync(dstate.get(), 0, dstate.bytes(), ctx->stream));
     P.kstart = dk.get<uint32_t>();
     P.kcount = dc.get<uint32_t>();
+    P.kfirst = dkf.get<uint32_t>();
+    P.kf16 = kf16.empty() ? nullptr : dk16.get<uint16_t>();
     P.glist = dg.get<uint32_t>();
     P.state = dstate.get<unsigned long long>();
     const int block = 512;
@@ -524,28 +808,89 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
       if (spec == kPipeSpecAvgSum) kern = pipeline_kernel<kPipeSpecAvgSum>;
       else if (spec == kPipeSpecAvgSumNulls) kern = pipeline_kernel<kPipeSpecAvgSumNulls>;
     }
-    const size_t per_copy = static_cast<size_t>(P.ngroups) * (P.nfields | 1) * 8;
-    P.per_warp = per_copy * (block / 32) <= 96 * 1024 ? 1 : 0;
-    // Per-lane shared reductions by default (measured 2.95 vs 3.10 ms per
-    // 200M-row call against warp peer aggregation); QEG_PIPE_LANES=0 selects
-    // the peer-aggregating variant.
+    // Thread-private states (pipeline_lanes_kernel) while 256, 128 or 64
+    // threads' copies of every group's active fields fit in shared memory;
+    // QEG_PIPE_KERNEL=shared selects the shared-state kernel below.
     {
-      const char* e = std::getenv("QEG_PIPE_LANES");
-      P.lane_reds = e ? (std::atoi(e) != 0 ? 1 : 0) : 1;
+      const char* e = std::getenv("QEG_PIPE_KERNEL");
+      const bool want_lanes = !(e && std::strcmp(e, "shared") == 0);
+      uint32_t spec = kGenericSpec;
+      if (kern == pipeline_kernel<kPipeSpecAvgSum>) spec = kPipeSpecAvgSum;
+      else if (kern == pipeline_kernel<kPipeSpecAvgSumNulls>) spec = kPipeSpecAvgSumNulls;
+      const int na = spec == kGenericSpec ? P.nfields : spec_nactive(spec);
+      int T = 256;
+      while (T >= 64 && static_cast<size_t>(P.ngroups) * na * 8 * T > ctx->smem_optin) T >>= 1;
+      if (want_lanes && T >= 64) {
+        size_t lsb_fast = 0;
+        void (*lk)(PipeK, int) = spec == kPipeSpecAvgSum        ? pipeline_lanes_kernel<kPipeSpecAvgSum, 16, -1>
+                                 : spec == kPipeSpecAvgSumNulls ? pipeline_lanes_kernel<kPipeSpecAvgSumNulls, 16, -1>
+                                                                : pipeline_lanes_kernel<kGenericSpec, 8, -1>;
+        // The trades shape (see the kernel) takes the typed variant.
+        const bool key4 = P.key.type == kI32 || P.key.type == kSTR;
+        const bool fsame = P.fcol.type == kF64 && P.val[0].type == kF64 && P.fcol.data == P.val[0].data &&
+                           P.fcol.all_valid && P.val[0].all_valid;
+        // (16-byte loads: column starts 16-byte aligned; the u16 translation
+        // table beside the states in shared memory.)
+        const bool aligned = (reinterpret_cast<uintptr_t>(P.key.data) % 16) == 0 &&
+                             (reinterpret_cast<uintptr_t>(P.val[0].data) % 16) == 0 &&
+                             (reinterpret_cast<uintptr_t>(P.val[1].data) % 16) == 0;
+        const size_t fast_sb = static_cast<size_t>(P.ngroups) * na * 8 * T + ((domain * 2 + 15) / 16) * 16;
+        const bool single = std::none_of(kf16.begin(), kf16.end(), [](uint16_t x) { return x == 0xfffeu; });
+        if (spec == kPipeSpecAvgSum && key4 && P.key.all_valid && fsame && P.val[1].type == kI32 &&
+            P.val[1].all_valid && aligned && P.kf16 && single && domain < (1ull << 31) &&
+            fast_sb <= ctx->smem_optin) {
+          lsb_fast = fast_sb;
+          switch (P.fop) {
+            case kLT: lk = pipeline_lanes_kernel<kPipeSpecAvgSum, 16, kLT>; break;
+            case kLE: lk = pipeline_lanes_kernel<kPipeSpecAvgSum, 16, kLE>; break;
+            case kGT: lk = pipeline_lanes_kernel<kPipeSpecAvgSum, 16, kGT>; break;
+            case kGE: lk = pipeline_lanes_kernel<kPipeSpecAvgSum, 16, kGE>; break;
+            case kEQ: lk = pipeline_lanes_kernel<kPipeSpecAvgSum, 16, kEQ>; break;
+            case kNE: lk = pipeline_lanes_kernel<kPipeSpecAvgSum, 16, kNE>; break;
+            default: break;
+          }
+        }
+        const size_t lsb = lsb_fast ? lsb_fast : static_cast<size_t>(P.ngroups) * na * 8 * T;
+        if (lsb > 48 * 1024)
+          QEG_CUDA(cudaFuncSetAttribute(lk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsb));
+        int lper = 1;
+        QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lper, lk, T, lsb));
+        const int rows_per_tile = T * (spec == kGenericSpec ? 8 : 16);
+        const uint64_t lwant = (np + rows_per_tile - 1) / rows_per_tile;
+        const unsigned lgrid = static_cast<unsigned>(
+            std::max<uint64_t>(1, std::min<uint64_t>(lwant, static_cast<uint64_t>(ctx->sms) * std::max(lper, 1))));
+        if (np > 0 && domain > 0 && ngroups > 0) {
+          lk<<<lgrid, T, lsb, ctx->stream>>>(P, na);
+          ctx->launches++;
+          QEG_CUDA(cudaGetLastError());
+        }
+        kern = nullptr;  // done
+      }
     }
-    const size_t sb = P.per_warp ? per_copy * (block / 32) : per_copy;
-    require(sb <= ctx->smem_optin, "too many groups for the fused pipeline's shared-memory state");
-    if (sb > 48 * 1024)
-      QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-    int per_sm = 1;
-    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
-    const uint64_t want = (np + block * 16 - 1) / (block * 16);
-    const unsigned grid = static_cast<unsigned>(
-        std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
-    if (np > 0 && domain > 0 && ngroups > 0) {
-      kern<<<grid, block, sb, ctx->stream>>>(P);
-      ctx->launches++;
-      QEG_CUDA(cudaGetLastError());
+    if (kern) {
+      const size_t per_copy = static_cast<size_t>(P.ngroups) * (P.nfields | 1) * 8;
+      P.per_warp = per_copy * (block / 32) <= 96 * 1024 ? 1 : 0;
+      // Per-lane shared reductions by default (measured 2.95 vs 3.10 ms per
+      // 200M-row call against warp peer aggregation); QEG_PIPE_LANES=0 selects
+      // the peer-aggregating variant.
+      {
+        const char* e = std::getenv("QEG_PIPE_LANES");
+        P.lane_reds = e ? (std::atoi(e) != 0 ? 1 : 0) : 1;
+      }
+      const size_t sb = P.per_warp ? per_copy * (block / 32) : per_copy;
+      require(sb <= ctx->smem_optin, "too many groups for the fused pipeline's shared-memory state");
+      if (sb > 48 * 1024)
+        QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+      int per_sm = 1;
+      QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
+      const uint64_t want = (np + block * 16 - 1) / (block * 16);
+      const unsigned grid = static_cast<unsigned>(
+          std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
+      if (np > 0 && domain > 0 && ngroups > 0) {
+        kern<<<grid, block, sb, ctx->stream>>>(P);
+        ctx->launches++;
+        QEG_CUDA(cudaGetLastError());
+      }
     }
     std::vector<unsigned long long> st(static_cast<size_t>(P.ngroups) * P.nfields);
     QEG_CUDA(cudaMemcpyAsync(st.data(), dstate.get(), st.size() * 8, cudaMemcpyDeviceToHost, ctx->stream));

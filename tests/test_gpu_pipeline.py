@@ -57,10 +57,23 @@ def oracle_pipeline(trades, symbols, aggs):
     return O.groupby(cols, [4], aggs)
 
 
-@pytest.mark.parametrize("lanes", ["1", "0"])
+# The kernels of the fused pipeline: thread-private states (the default), and
+# the shared-state kernel with per-lane reductions or warp peer aggregation.
+KERNELS = {"private": {}, "shared_lanes": {"QEG_PIPE_KERNEL": "shared", "QEG_PIPE_LANES": "1"},
+           "shared_peers": {"QEG_PIPE_KERNEL": "shared", "QEG_PIPE_LANES": "0"}}
+
+
+def use_kernel(monkeypatch, kernel):
+    monkeypatch.delenv("QEG_PIPE_KERNEL", raising=False)
+    monkeypatch.delenv("QEG_PIPE_LANES", raising=False)
+    for k, v in KERNELS[kernel].items():
+        monkeypatch.setenv(k, v)
+
+
+@pytest.mark.parametrize("kernel", list(KERNELS))
 @pytest.mark.parametrize("seed,nulls,dup", [(1, True, False), (2, False, False), (3, True, True)])
-def test_pipeline_matches_operator_chain(ctx, seed, nulls, dup, lanes, monkeypatch):
-    monkeypatch.setenv("QEG_PIPE_LANES", lanes)
+def test_pipeline_matches_operator_chain(ctx, seed, nulls, dup, kernel, monkeypatch):
+    use_kernel(monkeypatch, kernel)
     trades, symbols = make_case(seed, nulls=nulls, dup_syms=dup)
     aggs = [(O.COUNT_STAR, 0), (O.AVG, 1), (O.SUM, 2), (O.MIN, 1), (O.MAX, 2), (O.COUNT, 1)]
     ot, orows = oracle_pipeline(trades, symbols, aggs)
@@ -94,14 +107,15 @@ def test_pipeline_integer_keys_and_filter_on_int(ctx):
     assert_same(gt, grows, ot, orows)
 
 
-@pytest.mark.parametrize("lanes", ["1", "0"])
+@pytest.mark.parametrize("kernel", list(KERNELS))
 @pytest.mark.parametrize("seed,nulls", [(4, False), (5, True)])
-def test_pipeline_trades_aggregates_specialised_kernel(ctx, seed, nulls, lanes, monkeypatch):
+def test_pipeline_trades_aggregates_specialised_kernel(ctx, seed, nulls, kernel, monkeypatch):
     """The trades workload's exact aggregate list -- COUNT(*), AVG(price),
-    SUM(qty) -- runs the field-set-specialised kernel (with NULL counts when
+    SUM(qty) -- runs the field-set-specialised kernels (with NULL counts when
     the columns have NULLs); device-resident columns as in the benchmark;
-    per-lane shared reductions (the default) and warp peer aggregation."""
-    monkeypatch.setenv("QEG_PIPE_LANES", lanes)
+    thread-private states (the default), and the shared-state kernel with
+    per-lane reductions or warp peer aggregation."""
+    use_kernel(monkeypatch, kernel)
     trades, symbols = make_case(seed, nulls=nulls)
     aggs = [(O.COUNT_STAR, 0), (O.AVG, 1), (O.SUM, 2)]
     ot, orows = oracle_pipeline(trades, symbols, aggs)
@@ -110,5 +124,38 @@ def test_pipeline_trades_aggregates_specialised_kernel(ctx, seed, nulls, lanes, 
     gb = [to_gpu(c, canon, device=True) for c in symbols]
     types, res = qeg.filter_join_agg(ctx, gp, gb, 0, 0, 4, aggs, filter_col=1, filter_op=qeg.CMP_GT,
                                      filter_value=100.0)
+    gt, grows = gpu_rows(res, types, canon)
+    assert_same(gt, grows, ot, orows)
+
+
+@pytest.mark.parametrize("op,dup", [(qeg.CMP_LT, True), (qeg.CMP_GE, False), (qeg.CMP_NE, True), (qeg.CMP_EQ, False)])
+def test_pipeline_trades_shape_typed_kernel_ops_and_repeated_keys(ctx, op, dup):
+    """The trades shape without NULLs (4-byte STR key, F64 filter column
+    aggregated as AVG, I32 SUM) takes the typed thread-private kernel for
+    every comparison; repeated symbols in the build side fan a row out to
+    several sectors."""
+    trades, symbols = make_case(6 + op, nulls=False, dup_syms=dup)
+    aggs = [(O.COUNT_STAR, 0), (O.AVG, 1), (O.SUM, 2)]
+    lit = float(np.round(trades[1].values[17], 6)) if op == qeg.CMP_EQ else 100.0
+    ops = {qeg.CMP_LT: np.less, qeg.CMP_GE: np.greater_equal, qeg.CMP_NE: np.not_equal, qeg.CMP_EQ: np.equal}
+    if op == qeg.CMP_EQ:
+        trades[1].values[::7] = lit  # rows that pass an equality test
+    ok = ops[op](trades[1].values, lit)
+    filt = [O.TCol(c.type, c.values[ok], None, c.dictionary) for c in trades]
+    jt, jrows = O.join(filt, symbols, [0], [0], O.INNER)
+    cols = []
+    for i, t in enumerate(jt):
+        vals = [r[i] for r in jrows]
+        if t == O.STR:
+            d = sorted(set(vals)) or ["?"]
+            cols.append(O.TCol(t, np.array([d.index(v) for v in vals], np.int32), None, d))
+        else:
+            dt = {O.I32: np.int32, O.I64: np.int64, O.F64: np.float64}[t]
+            cols.append(O.TCol(t, np.array(vals, dt)))
+    ot, orows = O.groupby(cols, [4], aggs)
+    canon = StrCanon(trades[0].dictionary + symbols[0].dictionary)
+    gp = [to_gpu(c, canon, device=True) for c in trades]
+    gb = [to_gpu(c, canon, device=True) for c in symbols]
+    types, res = qeg.filter_join_agg(ctx, gp, gb, 0, 0, 4, aggs, filter_col=1, filter_op=op, filter_value=lit)
     gt, grows = gpu_rows(res, types, canon)
     assert_same(gt, grows, ot, orows)
