@@ -330,6 +330,13 @@ qeg_status qeg_sketch_batch(qeg_ctx* ctx, const qeg_column* key, uint32_t nqueri
 qeg_status qeg_estimator_init(qeg_ctx* ctx, uint64_t seed);
 qeg_status qeg_estimator_set_weights(qeg_ctx* ctx, const float* params);
 qeg_status qeg_estimator_get_weights(qeg_ctx* ctx, float* params);
+/* The dead band (log2 units) taken off the magnitude of the network's
+ * correction: corrections within it are dropped, so the classic estimate
+ * stands where the network only adds noise. A weights file may carry it as
+ * one float32 after the QEG_MLP_PARAMS parameters; otherwise 0.125. No
+ * counterpart in the reference (the estimator is this library's). */
+qeg_status qeg_estimator_set_deadband(qeg_ctx* ctx, double band);
+qeg_status qeg_estimator_get_deadband(qeg_ctx* ctx, double* band);
 qeg_status qeg_estimator_predict(qeg_ctx* ctx, const float* features, uint32_t n, float* out);
 qeg_status qeg_estimator_grad(qeg_ctx* ctx, const float* x, const float* targets, uint32_t n, float* loss,
                               float* grad);

@@ -136,7 +136,7 @@ double classic_estimate(const SketchResult& s);
 // is loaded in this context.
 bool learned_estimate(qeg_ctx* ctx, const SketchResult& s, double* groups, double* hot_share);
 // Non-null group count from the network's first output for sketch `s`.
-double learned_groups(const SketchResult& s, float out0);
+double learned_groups(const SketchResult& s, float out0, double deadband);
 
 struct AggState {
   qeg_ctx* ctx = nullptr;

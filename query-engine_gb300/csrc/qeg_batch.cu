@@ -611,7 +611,7 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
       double g = classic_estimate(sk[q]);
       double share = sk[q].top_share[11];
       if (learned) {
-        g = learned_groups(sk[q], y[(size_t)q * kOut]) + (sk[q].null_frac > 0 ? 1.0 : 0.0);
+        g = learned_groups(sk[q], y[(size_t)q * kOut], ctx->mlp->deadband) + (sk[q].null_frac > 0 ? 1.0 : 0.0);
         g = std::max(g, sk[q].hll_estimate * 0.95);
         share = std::min(1.0, std::max(0.0, static_cast<double>(y[(size_t)q * kOut + 1])));
       }

@@ -37,7 +37,7 @@ std::vector<float> predict_host(qeg_ctx* ctx, const float* feats, uint32_t n) {
 
 // The network predicts a correction to the classic estimate in log space:
 // log2(1 + groups) = log2(1 + classic non-null groups) + 32 * out0.
-double learned_groups(const SketchResult& s, float out0) {
+double learned_groups(const SketchResult& s, float out0, double deadband) {
   const double classic = classic_estimate(s) - (s.null_frac > 0 ? 1.0 : 0.0);
   // The network's log2 correction, less a dead band of its own resolution:
   // small corrections are noise of the BF16 network where the classic
@@ -45,7 +45,7 @@ double learned_groups(const SketchResult& s, float out0) {
   // while the large ones fix its underestimates on sparsely sampled skewed
   // columns. The band is chosen by the trainer on its training columns.
   double c = 32.0 * static_cast<double>(out0);
-  c = c > kCorrectionDeadband ? c - kCorrectionDeadband : (c < -kCorrectionDeadband ? c + kCorrectionDeadband : 0.0);
+  c = c > deadband ? c - deadband : (c < -deadband ? c + deadband : 0.0);
   const double lg = std::log2(1.0 + std::max(classic, 0.0)) + c;
   return std::exp2(std::min(40.0, std::max(0.0, lg))) - 1.0;
 }
@@ -53,7 +53,7 @@ double learned_groups(const SketchResult& s, float out0) {
 bool learned_estimate(qeg_ctx* ctx, const SketchResult& s, double* groups, double* hot_share) {
   if (!ctx->mlp || !ctx->mlp->loaded) return false;
   const std::vector<float> y = predict_host(ctx, s.features, 1);
-  double g = learned_groups(s, y[0]);
+  double g = learned_groups(s, y[0], ctx->mlp->deadband);
   // Never below what the sample itself proves, never above the non-null rows.
   const double nonnull = s.total_rows * (1.0 - s.null_frac);
   g = std::max(g, s.hll_estimate * 0.95);
@@ -63,16 +63,21 @@ bool learned_estimate(qeg_ctx* ctx, const SketchResult& s, double* groups, doubl
   return true;
 }
 
-// Loads estimator weights from `path` (kParams little-endian float32).
+// Loads estimator weights from `path` (kParams little-endian float32, then
+// optionally the correction's dead band as one more float32).
 bool load_weights_file(qeg_ctx* ctx, const std::string& path) {
   std::ifstream f(path, std::ios::binary);
   if (!f) return false;
   std::vector<float> p(kParams);
   f.read(reinterpret_cast<char*>(p.data()), kParams * 4);
   if (f.gcount() != kParams * 4) return false;
+  float band = static_cast<float>(kCorrectionDeadband);
+  f.read(reinterpret_cast<char*>(&band), 4);
+  if (f.gcount() != 4 || !(band >= 0.0f && band <= 4.0f)) band = static_cast<float>(kCorrectionDeadband);
   Mlp& m = mlp_of(ctx);
   m.ensure(ctx, 1);
   m.set_master(p.data());
+  m.deadband = band;
   QEG_CUDA(cudaStreamSynchronize(ctx->stream));
   return true;
 }
@@ -156,6 +161,21 @@ qeg_status qeg_estimator_set_weights(qeg_ctx* ctx, const float* params) {
     m.ensure(ctx, 1);
     m.set_master(params);
     QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+qeg_status qeg_estimator_set_deadband(qeg_ctx* ctx, double band) {
+  return guarded(ctx, [&] {
+    require(ctx != nullptr, "NULL argument");
+    require(band >= 0.0 && band <= 4.0, "the dead band lies in [0, 4] (log2 units)");
+    mlp_of(ctx).deadband = band;
+  });
+}
+
+qeg_status qeg_estimator_get_deadband(qeg_ctx* ctx, double* band) {
+  return guarded(ctx, [&] {
+    require(ctx != nullptr && band != nullptr, "NULL argument");
+    *band = ctx->mlp ? ctx->mlp->deadband : kCorrectionDeadband;
   });
 }
 

@@ -572,6 +572,130 @@ __device__ __forceinline__ void load2(const T* p, T (&o)[2]) {
   }
 }
 
+// Probe sides the 32-bit tile counters of the lean and swept sinks cover.
+inline bool lean_sizes_ok(uint64_t n) { return n / 64 < (uint64_t{1} << 31); }
+
+// Hashed single-key COUNT/SUM sink in sweeps: launch `sweep` of `nsweeps`
+// handles only the probe rows whose key hash falls in the sweep's 1/nsweeps
+// of the hash range. The table's home slot is the top bits of the hash, so a
+// sweep's lookups stay in one contiguous window of the table, small enough to
+// stay in L2 while the probe stream passes through evict-first: every sweep
+// re-reads the probe keys, but a lookup is an L2 hit instead of a random DRAM
+// read (on GB300 a random 32-byte read from DRAM moves a whole 128-byte line).
+// A warp takes 128 rows per step (two 64-row chunks, lane i: rows 2i, 2i + 1
+// of each, all key loads issued first), hashes each key once, and queues the
+// rows of its sweep in shared memory, so the lookups then run with every lane
+// busy. Payloads and their validity are read only for rows that matched.
+constexpr int kSweepThreads = 256;
+template <typename KT, typename VT, bool UNIQUE>
+__global__ void __launch_bounds__(kSweepThreads, 6) probe_sink_sweep_kernel(const SinkK P, uint32_t sweep,
+                                                                            uint32_t nsweeps) {
+  constexpr int kRows = 128;  // rows per warp step
+  __shared__ uint64_t q_key[kSweepThreads / 32][kRows];
+  __shared__ uint64_t q_hash[kSweepThreads / 32][kRows];
+  __shared__ uint8_t q_row[kSweepThreads / 32][kRows];
+  const KT* keys = static_cast<const KT*>(P.key);
+  const VT* vals = static_cast<const VT*>(P.val);
+  const unsigned lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint32_t ntiles = static_cast<uint32_t>(P.n / kRows);
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const ulonglong2* tab = reinterpret_cast<const ulonglong2*>(P.T.keys);
+  const uint64_t mask = P.T.cap - 1;
+  using Cnt = typename std::conditional<UNIQUE, uint32_t, unsigned long long>::type;
+  Cnt cnt = 0;
+  uint32_t seen = 0;
+  unsigned long long sum = 0;
+  // Match multiplicity of key word k (hash h) in the table.
+  auto lookup = [&](uint64_t k, uint64_t h) -> uint64_t {
+    if (k == 0) return __ldg(P.T.cnt + P.T.cap);
+    const uint64_t home = h >> P.T.shift;
+    uint64_t g = home & ~3ull;
+    int skip = static_cast<int>(home & 3);
+    for (uint64_t t = 0; t <= mask; t += 4) {
+      const ulonglong2 a = __ldg(tab + (g >> 1));
+      const ulonglong2 b = __ldg(tab + (g >> 1) + 1);
+      const uint64_t c[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        if (i < skip) continue;
+        if (c[i] == k) return UNIQUE ? 1 : __ldg(P.T.cnt + g + i);
+        if (c[i] == 0) return 0;
+      }
+      skip = 0;
+      g = (g + 4) & mask;
+    }
+    return 0;
+  };
+  for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += nwarps) {
+    const uint64_t base = static_cast<uint64_t>(t) * kRows;
+    KT k[2][2];
+    uint64_t kw[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      load2(keys + base + c * 64 + 2 * lane, k[c]);
+      kw[c] = P.kvalid ? __ldg(P.kvalid + (base >> 6) + c) : ~0ull;
+    }
+    // Queue the rows of this sweep.
+    uint32_t nq = 0;
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const uint64_t kk = sizeof(KT) == 4 ? static_cast<uint64_t>(static_cast<uint32_t>(k[c][j]))
+                                            : static_cast<uint64_t>(k[c][j]);
+        const uint64_t h = single_key_hash(kk);
+        const bool go = ((kw[c] >> (2 * lane + j)) & 1ull) &&
+                        static_cast<uint32_t>(__umul64hi(h, nsweeps)) == sweep;
+        const unsigned bal = __ballot_sync(0xffffffffu, go);
+        if (go) {
+          const uint32_t at = nq + __popc(bal & ((1u << lane) - 1u));
+          q_key[wib][at] = kk;
+          q_hash[wib][at] = h;
+          q_row[wib][at] = static_cast<uint8_t>(c * 64 + 2 * lane + j);
+        }
+        nq += __popc(bal);
+      }
+    __syncwarp();
+    for (uint32_t i = lane; i < nq; i += 32) {
+      const uint64_t m = lookup(q_key[wib][i], q_hash[wib][i]);
+      if (!m) continue;
+      cnt += static_cast<Cnt>(m);
+      const uint64_t r = base + q_row[wib][i];
+      if (!P.vvalid || ((__ldg(P.vvalid + (r >> 6)) >> (r & 63)) & 1ull)) {
+        sum += static_cast<unsigned long long>(static_cast<int64_t>(__ldcs(vals + r))) * m;
+        seen = 1;
+      }
+    }
+    __syncwarp();
+  }
+  // Rows after the last full step, one per thread.
+  for (uint64_t r = static_cast<uint64_t>(ntiles) * kRows + static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+       r < P.n; r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    if (P.kvalid && !((P.kvalid[r >> 6] >> (r & 63)) & 1ull)) continue;
+    const uint64_t kk = sizeof(KT) == 4 ? static_cast<uint64_t>(static_cast<uint32_t>(keys[r]))
+                                        : static_cast<uint64_t>(keys[r]);
+    const uint64_t h = single_key_hash(kk);
+    if (static_cast<uint32_t>(__umul64hi(h, nsweeps)) != sweep) continue;
+    const uint64_t mm = lookup(kk, h);
+    cnt += static_cast<Cnt>(mm);
+    if (mm && (!P.vvalid || ((P.vvalid[r >> 6] >> (r & 63)) & 1ull))) {
+      sum += static_cast<unsigned long long>(static_cast<int64_t>(vals[r])) * mm;
+      seen = 1;
+    }
+  }
+  unsigned long long c64 = cnt;
+  for (int o = 16; o > 0; o >>= 1) {
+    c64 += __shfl_down_sync(0xffffffffu, c64, o);
+    sum += __shfl_down_sync(0xffffffffu, sum, o);
+    seen |= __shfl_down_sync(0xffffffffu, seen, o);
+  }
+  if (lane == 0) {
+    if (c64) atomicAdd(P.acc + 0, c64);
+    if (sum) atomicAdd(P.acc + 1, sum);
+    if (seen) atomicMax(P.acc + 2, 1ull);
+  }
+}
+
 // Software-pipelined sink. A warp owns tiles of U x 64 rows; in a tile, lane i
 // takes rows 2i and 2i+1 of every 64-row chunk, so each warp load instruction
 // reads one contiguous 256- or 512-byte span, and the chunk's validity is one
@@ -2800,6 +2924,39 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
         return;
       }
       const bool k8 = type_width(kt) == 8, v8 = type_width(vt) == 8, dense = st.strategy == QEG_JOIN_DENSE;
+      // Hashed tables: QEG_JOIN_SWEEPS=n > 1 probes in n sweeps over windows of
+      // the table (opt-in: on GB300 the 16M-key table's 64 MB windows reach a
+      // 73% L2 hit rate and each sweep re-reads the 2 GB key column, so 256M
+      // probes take 5.8 ms in 2 sweeps and 6.8 ms in 4, against 3.8 ms for
+      // the direct probe below).
+      if (st.strategy == QEG_JOIN_HASH && lean_sizes_ok(n)) {
+        uint64_t sweeps = 1;
+        if (const char* e = getenv("QEG_JOIN_SWEEPS")) sweeps = std::max(1, atoi(e));
+        if (sweeps > 1) {
+          auto sweep_all = [&](void (*kern)(SinkK, uint32_t, uint32_t)) {
+            int per_sm = 0;
+            QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSweepThreads, 0));
+            const uint64_t want = (n / 128 + 7) / 8;
+            const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(
+                1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
+            for (uint32_t w = 0; w < sweeps; ++w) {
+              kern<<<grid, kSweepThreads, 0, ctx->stream>>>(S, w, static_cast<uint32_t>(sweeps));
+              ctx->launches++;
+            }
+          };
+          if (k8 && v8) sweep_all(st.unique ? probe_sink_sweep_kernel<long long, long long, true>
+                                            : probe_sink_sweep_kernel<long long, long long, false>);
+          else if (k8) sweep_all(st.unique ? probe_sink_sweep_kernel<long long, int, true>
+                                           : probe_sink_sweep_kernel<long long, int, false>);
+          else if (v8) sweep_all(st.unique ? probe_sink_sweep_kernel<int, long long, true>
+                                           : probe_sink_sweep_kernel<int, long long, false>);
+          else sweep_all(st.unique ? probe_sink_sweep_kernel<int, int, true> : probe_sink_sweep_kernel<int, int, false>);
+          QEG_CUDA(cudaGetLastError());
+          if (k.data.get() || v.data.get() || k.validity.get() || v.validity.get())
+            QEG_CUDA(cudaStreamSynchronize(ctx->stream));  // staged inputs die with this scope
+          return;
+        }
+      }
       // One wave of resident blocks; each thread strides over the probe side.
       auto launch = [&](void (*kern)(SinkK)) {
         int per_sm = 0;

@@ -21,8 +21,9 @@ constexpr int kParams = kOffB3 + kOut;  // 9474
 constexpr int kHotTopK = 2048;
 
 // Dead band (log2 units) subtracted from the magnitude of the network's
-// group-count correction; train_estimator.py picks it on its training columns
-// (the value that minimises their mean absolute log2 error) and reports it.
+// group-count correction when the weights carry none: train_estimator.py
+// picks one on its training columns and stores it after the parameters in
+// the weights file (Mlp::deadband).
 constexpr double kCorrectionDeadband = 0.125;
 
 struct Mlp {
@@ -32,6 +33,7 @@ struct Mlp {
   int cap_batch = 0;
   int step = 0;
   bool loaded = false;
+  double deadband = kCorrectionDeadband;  // of the loaded weights
 
   void ensure(qeg_ctx* c, int max_batch);
   void set_master(const float* host);

@@ -105,6 +105,8 @@ def lib():
             "qeg_estimator_init": (i32, [vp, u64]),
             "qeg_estimator_set_weights": (i32, [vp, vp]),
             "qeg_estimator_get_weights": (i32, [vp, vp]),
+            "qeg_estimator_set_deadband": (i32, [vp, ctypes.c_double]),
+            "qeg_estimator_get_deadband": (i32, [vp, P(ctypes.c_double)]),
             "qeg_estimator_predict": (i32, [vp, vp, ctypes.c_uint32, vp]),
             "qeg_estimator_grad": (i32, [vp, vp, vp, ctypes.c_uint32, P(ctypes.c_float), vp]),
             "qeg_estimator_train": (i32, [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
@@ -647,6 +649,16 @@ def estimator_set_weights(ctx, params):
     p = np.ascontiguousarray(params, dtype=np.float32)
     assert p.size == MLP_PARAMS
     _check(lib().qeg_estimator_set_weights(ctx.p, p.ctypes.data), ctx.p)
+
+
+def estimator_set_deadband(ctx, band):
+    _check(lib().qeg_estimator_set_deadband(ctx.p, band), ctx.p)
+
+
+def estimator_get_deadband(ctx):
+    b = ctypes.c_double(0)
+    _check(lib().qeg_estimator_get_deadband(ctx.p, ctypes.byref(b)), ctx.p)
+    return b.value
 
 
 def estimator_get_weights(ctx):

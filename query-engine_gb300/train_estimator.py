@@ -154,25 +154,32 @@ def main():
     t1 = time.time()
     losses = []
     if args.no_train:
-        qeg.estimator_set_weights(ctx, np.fromfile(args.out, dtype="<f4"))
+        qeg.estimator_set_weights(ctx, np.fromfile(args.out, dtype="<f4")[:qeg.MLP_PARAMS])
     else:
         qeg.estimator_init(ctx, args.seed)
         for phase, lr in ((args.epochs // 2, 3e-3), (args.epochs // 4, 1e-3),
                           (args.epochs - 3 * (args.epochs // 4), 3e-4)):
             losses.append(qeg.estimator_train(ctx, X, T, phase, 64, lr, args.seed + len(losses)))
-        w = qeg.estimator_get_weights(ctx)
-        w.astype("<f4").tofile(args.out)
     t_train = time.time() - t1
-    # The dead band on the network's correction: the value that minimises the
-    # mean absolute log2 error on the TRAINING columns (the library's
-    # kCorrectionDeadband is set to it).
+    # The dead band on the network's correction, picked on the TRAINING
+    # columns: the smallest mean absolute log2 error among the bands whose
+    # median error is no worse than the classic estimator's (the network's
+    # small corrections are noise where the classic estimate is already
+    # close; its large ones fix the classic underestimates in the tail). It is
+    # stored after the parameters in the weights file and set in the context.
     Yt = qeg.estimator_predict(ctx, X)
     true_t = [d["groups"] for d in D]
+    classic_median_t = float(np.median([log2_err(c, t) for c, t in zip(C, true_t)]))
     bands = {}
-    for band in (0.0, 0.03, 0.06, 0.09, 0.125, 0.15, 0.2, 0.25, 0.3, 0.4, 0.5):
+    for band in (0.0, 0.03, 0.06, 0.09, 0.125, 0.15, 0.2, 0.25, 0.3, 0.4, 0.5, 0.75, 1.0):
         e = [log2_err(qeg.learned_groups(c, float(y[0]), band), t) for c, y, t in zip(C, Yt, true_t)]
         bands[band] = {"mean": float(np.mean(e)), "median": float(np.median(e)), "p90": float(np.percentile(e, 90))}
-    best_band = min(bands, key=lambda b: bands[b]["mean"])
+    ok = [b for b in bands if bands[b]["median"] <= classic_median_t] or list(bands)
+    best_band = min(ok, key=lambda b: bands[b]["mean"])
+    qeg.estimator_set_deadband(ctx, best_band)
+    if not args.no_train:
+        w = qeg.estimator_get_weights(ctx)
+        np.concatenate([w.astype("<f4"), np.array([best_band], "<f4")]).tofile(args.out)
     Y = qeg.estimator_predict(ctx, Xh)
     learned = [qeg.learned_groups(c, float(y[0]), best_band) for c, y in zip(Ch, Y)]
     learned_raw = [qeg.learned_groups(c, float(y[0]), 0.0) for c, y in zip(Ch, Y)]
@@ -198,6 +205,7 @@ def main():
         "heldout_top_share_mae": float(np.mean(share_err)),
         "heldout_by_sketch": by_kind,
         "correction_deadband": best_band,
+        "training_columns_classic_median": classic_median_t,
         "deadband_on_training_columns": {str(k): v for k, v in bands.items()},
         "heldout_without_deadband": {"median": float(np.median(e_raw)), "p90": float(np.percentile(e_raw, 90))},
     }

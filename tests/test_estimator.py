@@ -104,7 +104,8 @@ def test_learned_estimator_beats_classic_and_sizes_tables(monkeypatch):
             keys = zipf_column(torch, n, dom, s, seed)
             col = qeg.Col(keys, None, qeg.I64)
             f, classic, _ = qeg.sketch(ctx, col)
-            learned = qeg.learned_groups(classic, float(qeg.estimator_predict(ctx, f)[0][0]))
+            learned = qeg.learned_groups(classic, float(qeg.estimator_predict(ctx, f)[0][0]),
+                                         qeg.estimator_get_deadband(ctx))
             true = int(torch.unique(keys).numel())
             el.append(abs(math.log2(max(learned, 1)) - math.log2(true)))
             ec.append(abs(math.log2(max(classic, 1)) - math.log2(true)))

@@ -240,16 +240,19 @@ def test_count_sum_sparse_keys_use_hash(ctx):
     j.close()
 
 
-@pytest.mark.parametrize("bloom", ["0", "1"])
+@pytest.mark.parametrize("bloom,sweeps", [("0", "1"), ("1", "1"), ("0", "3"), ("1", "2")])
 @pytest.mark.parametrize("kt,vt", [(O.I64, O.I64), (O.I32, O.I64), (O.I64, O.I32), (O.I32, O.I32)])
 @pytest.mark.parametrize("dup", [False, True])
-def test_count_sum_hashed_bloom_filter(ctx, bloom, kt, vt, dup, monkeypatch):
+def test_count_sum_hashed_bloom_filter(ctx, bloom, sweeps, kt, vt, dup, monkeypatch):
     """The hashed COUNT/SUM sink with (QEG_JOIN_BLOOM=1) and without (=0) the
-    build keys' Bloom filter in front of the table: sparse keys over the whole
-    key width (with key 0 on both sides, which has its own table slot), 2%
-    NULL keys, payload NULLs, duplicated build keys, and probe sides whose
-    length is not a multiple of the 64-row chunk."""
+    build keys' Bloom filter in front of the table, probing directly
+    (QEG_JOIN_SWEEPS=1) or in sweeps over windows of the table's hash range
+    (=2, =3): sparse keys over the whole key width (with key 0 on both sides,
+    which has its own table slot), 2% NULL keys, payload NULLs, duplicated
+    build keys, and probe sides whose length is not a multiple of the 64-row
+    chunk."""
     monkeypatch.setenv("QEG_JOIN_BLOOM", bloom)
+    monkeypatch.setenv("QEG_JOIN_SWEEPS", sweeps)
     rng = np.random.default_rng(7 + kt + 5 * vt + 11 * dup)
     dt = np.int32 if kt == O.I32 else np.int64
     nb = 70_001
