@@ -414,8 +414,9 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
       const DevCol& kc = P.key[0];
       const bool kv = live && col_valid(kc, p);
       const uint64_t k = kv ? key_word(kc, p) : 0;
+      const bool key32 = kc.type == kI32 || kc.type == kSTR || kc.type == kBOOL;  // key words fit 32 bits
       // Peers: live lanes with the same key word and the same validity.
-      const unsigned same = __match_any_sync(0xffffffffu, k);
+      const unsigned same = match_word64(k, lane, key32);
       const unsigned vmask = __ballot_sync(0xffffffffu, kv);
       unsigned peers = live ? (same & livemask & (kv ? vmask : ~vmask)) : (1u << lane);
       const bool leader = live && __ffs(peers) - 1 == static_cast<int>(lane);
@@ -470,9 +471,14 @@ __global__ void __launch_bounds__(1024) agg_kernel(const AggK P) {
         h = hash_fold(h, kv ? words[j] : 0x9E3779B97F4A7C15ull);
       }
     }
-    const unsigned same = __match_any_sync(0xffffffffu, live ? h : ~static_cast<uint64_t>(lane));
+    // (Matched on a 32-bit fold of the tuple hash; the word check below
+    // drops any lane that collides.)
+    const uint64_t hm = live ? h : ~static_cast<uint64_t>(lane);
+    const unsigned same = __match_any_sync(0xffffffffu, static_cast<uint32_t>(hm ^ (hm >> 32)));
     const int ref = __ffs(same) - 1;
-    bool eq = __shfl_sync(0xffffffffu, nullmask, ref) == nullmask;
+    const uint64_t ref_h = __shfl_sync(0xffffffffu, hm, ref);
+    const uint64_t ref_nm = __shfl_sync(0xffffffffu, nullmask, ref);
+    bool eq = ref_h == hm && ref_nm == nullmask;
 #pragma unroll
     for (int j = 0; j < kMaxKeys; ++j)
       if (j < P.nkeys) eq &= __shfl_sync(0xffffffffu, words[j], ref) == words[j];
@@ -699,9 +705,14 @@ __global__ void __launch_bounds__(512, 2) agg2_private_kernel(const AggK P) {
     }
     // Peers: lanes with the same key tuple (hash match, then an exact check
     // against the match group's first lane), as in agg_kernel's mode 2.
-    const unsigned same = __match_any_sync(0xffffffffu, live ? h : ~static_cast<uint64_t>(lane));
+    // (Matched on a 32-bit fold of the tuple hash; the word check below
+    // drops any lane that collides.)
+    const uint64_t hm = live ? h : ~static_cast<uint64_t>(lane);
+    const unsigned same = __match_any_sync(0xffffffffu, static_cast<uint32_t>(hm ^ (hm >> 32)));
     const int ref = __ffs(same) - 1;
-    bool eq = __shfl_sync(0xffffffffu, nullmask, ref) == nullmask;
+    const uint64_t ref_h = __shfl_sync(0xffffffffu, hm, ref);
+    const uint64_t ref_nm = __shfl_sync(0xffffffffu, nullmask, ref);
+    bool eq = ref_h == hm && ref_nm == nullmask;
 #pragma unroll
     for (int j = 0; j < kMaxKeys; ++j)
       if (j < P.nkeys) eq &= __shfl_sync(0xffffffffu, words[j], ref) == words[j];

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(1024) batch_agg_kernel(const BatchK P) {
       unsigned peers = 1u << lane;
       if (Q.peer) {
         const unsigned livemask = __ballot_sync(0xffffffffu, live);
-        const unsigned same = __match_any_sync(0xffffffffu, k);
+        const unsigned same = match_word64(k, lane, P.key.type == kI32 || P.key.type == kSTR || P.key.type == kBOOL);
         const unsigned vmask = __ballot_sync(0xffffffffu, kv);
         if (live) peers = same & livemask & (kv ? vmask : ~vmask);
       }

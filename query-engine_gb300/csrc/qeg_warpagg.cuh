@@ -42,6 +42,21 @@ __device__ __forceinline__ PeerPlan plan_peers(unsigned peers, unsigned lane) {
   return pp;
 }
 
+// Lanes of the warp whose 64-bit word w equals this lane's (all lanes call
+// it). The match runs on a 32-bit fold of the word -- on GB300 a 64-bit
+// __match_any_sync costs twice a 32-bit one (106 against 53 clocks per warp
+// instruction per SM) -- and, unless the words are known to fit 32 bits, a
+// lane whose word differs from its match group's first lane's (a fold
+// collision) is left alone: exact, at worst less combining.
+__device__ __forceinline__ unsigned match_word64(uint64_t w, unsigned lane, bool fits32) {
+  const unsigned same = __match_any_sync(0xffffffffu, static_cast<uint32_t>(w ^ (w >> 32)));
+  if (fits32) return same;
+  const int ref = __ffs(same) - 1;
+  const bool eq = __shfl_sync(0xffffffffu, w, ref) == w;
+  const unsigned eqmask = __ballot_sync(0xffffffffu, eq);
+  return eq ? (same & eqmask) : (1u << lane);
+}
+
 // How a field merges: integer add (row / NULL counts, integer sums), F64 add
 // (F64 sums) or unsigned max (every MIN/MAX encoding). The kind of a field is
 // the same in every lane, so the branches below never diverge, and they are
