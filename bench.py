@@ -47,9 +47,9 @@ SEED = 20260615
 # from one ncu capture on a 64M-row probe side; the traffic grows in
 # proportion to the probe rows (the 2 MiB dense bitmap stays in L2).
 SINK_TRAFFIC_PER_ROW = (1082.670e6 + 3.291e6) / (1 << 26)
-# The same figure for the hashed-table sink of the sparse-key join (None: not
-# captured for the current kernel).
-HASH_SINK_TRAFFIC_PER_ROW = None
+# The same figure for the hashed-table sink of the sparse-key join (16M-key
+# table, 64M-row probe side): mostly whole 128-byte table lines, one per hit.
+HASH_SINK_TRAFFIC_PER_ROW = (5139.149e6 + 46.900e6) / (1 << 26)
 
 
 def replica_throughput(total_ms, rows_per_rank, steps, world, device):
@@ -422,9 +422,14 @@ def run_agg_bench(args, dev, local, kind=None, emit=True):
         "exact_size": qeg.agg_config(expected_groups=W.groups, hot_keys=-1),
         # learned sizing held to the private-table strategy (no partitioning)
         "learned_private": qeg.agg_config(strategy=qeg.AGG_SMEM, sizing=qeg.SIZE_LEARNED, hot_keys=-1),
+        # learned sizing with the radix-partitioned strategy (opt-in: heavy
+        # hitters in the CTA tables, every other row through key-hash
+        # partitions aggregated in shared memory)
+        "learned_partitioned": qeg.agg_config(strategy=qeg.AGG_PARTITIONED, sizing=qeg.SIZE_LEARNED, hot_keys=-1),
     }
     if kind == "agg1m":
         del variants["learned_private"]
+        del variants["learned_partitioned"]
     if args.variants:
         variants = {k: v for k, v in variants.items() if k in args.variants.split(",")}
     out = {}

@@ -159,3 +159,39 @@ def test_pipeline_trades_shape_typed_kernel_ops_and_repeated_keys(ctx, op, dup):
     types, res = qeg.filter_join_agg(ctx, gp, gb, 0, 0, 4, aggs, filter_col=1, filter_op=op, filter_value=lit)
     gt, grows = gpu_rows(res, types, canon)
     assert_same(gt, grows, ot, orows)
+
+
+@pytest.mark.parametrize("op", [qeg.CMP_LT, qeg.CMP_LE, qeg.CMP_GT, qeg.CMP_GE, qeg.CMP_EQ, qeg.CMP_NE])
+@pytest.mark.parametrize("lit", [0.0, -0.0, 100.0, float("inf")])
+def test_pipeline_typed_kernel_f64_filter_edges(ctx, op, lit):
+    """The typed kernel compares F64 values on the integer pipes: planted
+    -0.0, +0.0, NaNs, infinities and values equal to the literal must pass or
+    fail exactly as IEEE comparisons do (NaN fails all but !=, -0.0 == +0.0)."""
+    trades, symbols = make_case(40 + op, n=200_000, nulls=False)
+    v = trades[1].values
+    specials = [0.0, -0.0, float("nan"), -float("nan"), float("inf"), -float("inf"), lit, 100.0, -100.0]
+    for i, x in enumerate(specials):
+        v[i::97 + i] = x
+    aggs = [(O.COUNT_STAR, 0), (O.AVG, 1), (O.SUM, 2)]
+    ops = {qeg.CMP_LT: np.less, qeg.CMP_LE: np.less_equal, qeg.CMP_GT: np.greater,
+           qeg.CMP_GE: np.greater_equal, qeg.CMP_EQ: np.equal, qeg.CMP_NE: np.not_equal}
+    with np.errstate(invalid="ignore"):
+        ok = ops[op](v, lit)
+    filt = [O.TCol(c.type, c.values[ok], None, c.dictionary) for c in trades]
+    jt, jrows = O.join(filt, symbols, [0], [0], O.INNER)
+    cols = []
+    for i, t in enumerate(jt):
+        vals = [r[i] for r in jrows]
+        if t == O.STR:
+            d = sorted(set(vals)) or ["?"]
+            cols.append(O.TCol(t, np.array([d.index(x) for x in vals], np.int32), None, d))
+        else:
+            dt = {O.I32: np.int32, O.I64: np.int64, O.F64: np.float64}[t]
+            cols.append(O.TCol(t, np.array(vals, dt)))
+    ot, orows = O.groupby(cols, [4], aggs)
+    canon = StrCanon(trades[0].dictionary + symbols[0].dictionary)
+    gp = [to_gpu(c, canon, device=True) for c in trades]
+    gb = [to_gpu(c, canon, device=True) for c in symbols]
+    types, res = qeg.filter_join_agg(ctx, gp, gb, 0, 0, 4, aggs, filter_col=1, filter_op=op, filter_value=lit)
+    gt, grows = gpu_rows(res, types, canon)
+    assert_same(gt, grows, ot, orows)
