@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -111,6 +112,41 @@ struct Mlp;
 
 }  // namespace qeg
 
+namespace qeg {
+// Grow-only page-locked host buffer (one per context): small host<->device
+// staging that runs asynchronously on the context stream.
+class PinnedBuf {
+ public:
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() { release(); }
+  // At least `bytes` bytes (the previous contents are not kept).
+  void* reserve(size_t bytes) {
+    if (bytes > bytes_) {
+      release();
+      const size_t want = std::max<size_t>(bytes, size_t{1} << 16);
+      if (cudaHostAlloc(&ptr_, want, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        ptr_ = nullptr;
+        throw Error(QEG_ERR_OOM, "page-locked host buffer allocation failed");
+      }
+      bytes_ = want;
+    }
+    return ptr_;
+  }
+  void release() {
+    if (ptr_) cudaFreeHost(ptr_);
+    ptr_ = nullptr;
+    bytes_ = 0;
+  }
+
+ private:
+  void* ptr_ = nullptr;
+  size_t bytes_ = 0;
+};
+}  // namespace qeg
+
 struct qeg_ctx {
   int device = 0;
   int sms = 0;
@@ -122,6 +158,7 @@ struct qeg_ctx {
   cudaStream_t side = nullptr;  // copies that overlap the context stream's kernels (created on first use)
   cudaEvent_t side_in = nullptr, side_out = nullptr;  // fork / join of the side stream
   std::shared_ptr<qeg::Mlp> mlp;  // the learned estimator, when weights are loaded
+  qeg::PinnedBuf pinned_in, pinned_out;  // small staging of a call (device -> host, host -> device)
 };
 
 namespace qeg {

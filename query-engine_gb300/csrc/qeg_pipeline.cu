@@ -522,67 +522,88 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
     require(nb <= (1u << 22), "the fused pipeline takes a build side of at most 2^22 rows");
 
     // ---- host: the build side, the group ids, the probe-key translation ----
-    auto host_copy = [&](const void* src, size_t bytes) {
-      std::vector<uint8_t> h(bytes);
-      if (bytes) {
-        if (is_device_ptr(src)) {
-          QEG_CUDA(cudaMemcpy(h.data(), src, bytes, cudaMemcpyDeviceToHost));
-        } else {
-          std::memcpy(h.data(), src, bytes);
-        }
-      }
-      return h;
+    // The small build-side arrays (and the STR code maps) come to the host in
+    // one batch: device ones by asynchronous copies into the context's
+    // page-locked buffer and one stream synchronisation, host ones in place.
+    const qeg_column& bk = build[d->build_key];
+    const qeg_column& gcol = build[d->group_col - nprobe];
+    const bool bk_all = bk.all_valid || !bk.validity;
+    const bool g_all = gcol.all_valid || !gcol.validity;
+    struct Fetch {
+      const void* src;
+      size_t bytes, off;
+      bool dev;
     };
-    auto valid_at = [](const std::vector<uint8_t>& words, bool all_valid, uint64_t i) {
-      if (all_valid) return true;
+    std::vector<Fetch> fetches;
+    size_t fetch_bytes = 0;
+    auto want = [&](const void* src, size_t bytes) {
+      fetches.push_back(Fetch{src, bytes, fetch_bytes, bytes > 0 && is_device_ptr(src)});
+      fetch_bytes += (bytes + 15) & ~size_t{15};
+      return fetches.size() - 1;
+    };
+    const size_t f_bkv = want(bk.data, nb * type_width(bk.type));
+    const size_t f_bkw = bk_all ? SIZE_MAX : want(bk.validity, ((nb + 63) / 64) * 8);
+    const size_t f_gv = want(gcol.data, nb * type_width(gcol.type));
+    const size_t f_gw = g_all ? SIZE_MAX : want(gcol.validity, ((nb + 63) / 64) * 8);
+    size_t f_gcm = SIZE_MAX, f_bmap = SIZE_MAX, f_pmap = SIZE_MAX;
+    if (gcol.type == QEG_STR) {
+      require(gcol.code_map != nullptr, "STR group column needs a code map");
+      f_gcm = want(gcol.code_map, gcol.code_map_len * 4);
+    }
+    if (kt == QEG_STR) {
+      require(bk.code_map && probe[d->probe_key].code_map, "STR join keys need code maps");
+      f_bmap = want(bk.code_map, bk.code_map_len * 4);
+      f_pmap = want(probe[d->probe_key].code_map, probe[d->probe_key].code_map_len * 4);
+    }
+    uint8_t* fetched = static_cast<uint8_t*>(ctx->pinned_in.reserve(std::max<size_t>(fetch_bytes, 16)));
+    bool any_dev = false;
+    for (const Fetch& f : fetches) {
+      if (f.bytes == 0) continue;
+      if (f.dev) {
+        QEG_CUDA(cudaMemcpyAsync(fetched + f.off, f.src, f.bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        any_dev = true;
+      } else {
+        std::memcpy(fetched + f.off, f.src, f.bytes);
+      }
+    }
+    if (any_dev) QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+    auto at = [&](size_t i) -> const uint8_t* { return i == SIZE_MAX ? nullptr : fetched + fetches[i].off; };
+    auto valid_at = [](const uint8_t* words, uint64_t i) {
+      if (!words) return true;
       uint64_t w;
-      std::memcpy(&w, words.data() + (i >> 6) * 8, 8);
+      std::memcpy(&w, words + (i >> 6) * 8, 8);
       return ((w >> (i & 63)) & 1ull) != 0;
     };
-    auto ival = [](const std::vector<uint8_t>& v, int32_t t, uint64_t i) -> int64_t {
+    auto ival = [](const uint8_t* v, int32_t t, uint64_t i) -> int64_t {
       if (t == QEG_I32 || t == QEG_STR) {
         int32_t x;
-        std::memcpy(&x, v.data() + i * 4, 4);
+        std::memcpy(&x, v + i * 4, 4);
         return x;
       }
       if (t == QEG_BOOL) return v[i];
       int64_t x;
-      std::memcpy(&x, v.data() + i * 8, 8);
+      std::memcpy(&x, v + i * 8, 8);
       return x;
     };
-    const qeg_column& bk = build[d->build_key];
-    const qeg_column& gcol = build[d->group_col - nprobe];
-    const auto bkv = host_copy(bk.data, nb * type_width(bk.type));
-    const bool bk_all = bk.all_valid || !bk.validity;
-    const auto bkw = bk_all ? std::vector<uint8_t>() : host_copy(bk.validity, ((nb + 63) / 64) * 8);
-    const auto gv = host_copy(gcol.data, nb * type_width(gcol.type));
-    const bool g_all = gcol.all_valid || !gcol.validity;
-    const auto gw = g_all ? std::vector<uint8_t>() : host_copy(gcol.validity, ((nb + 63) / 64) * 8);
-    // Group ids over the distinct group values of build rows (NULL is a group).
-    std::unordered_map<uint64_t, uint32_t> gid;
+    const uint8_t* bkv = at(f_bkv);
+    const uint8_t* bkw = at(f_bkw);
+    const uint8_t* gv = at(f_gv);
+    const uint8_t* gw = at(f_gw);
+    const uint8_t* gcm = at(f_gcm);
+    // Group ids over the distinct group values of build rows (NULL is a
+    // group): a dense table over the value range for integer group columns
+    // spanning at most 2^20 values, a hash map otherwise.
     std::vector<uint64_t> gword;  // canonical group word per group
     std::vector<uint8_t> gnull;
     int32_t null_gid = -1;
     std::vector<int32_t> row_group(nb, -1);
-    std::vector<uint8_t> gcm;
-    if (gcol.type == QEG_STR) {
-      require(gcol.code_map != nullptr, "STR group column needs a code map");
-      gcm = host_copy(gcol.code_map, gcol.code_map_len * 4);
-    }
+    std::vector<uint64_t> words(nb);
     for (uint64_t b = 0; b < nb; ++b) {
-      if (!valid_at(gw, g_all, b)) {
-        if (null_gid < 0) {
-          null_gid = static_cast<int32_t>(gword.size());
-          gword.push_back(0);
-          gnull.push_back(1);
-        }
-        row_group[b] = null_gid;
-        continue;
-      }
+      if (!valid_at(gw, b)) continue;
       uint64_t w;
       if (gcol.type == QEG_F64) {
         double x;
-        std::memcpy(&x, gv.data() + b * 8, 8);
+        std::memcpy(&x, gv + b * 8, 8);
         uint64_t bits;
         std::memcpy(&bits, &x, 8);
         if (std::isnan(x)) bits = kCanonNaN;
@@ -592,10 +613,46 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
         const int32_t code = static_cast<int32_t>(ival(gv, QEG_STR, b));
         require(code >= 0 && static_cast<uint64_t>(code) < gcol.code_map_len, "STR code outside its code map");
         int32_t id;
-        std::memcpy(&id, gcm.data() + static_cast<size_t>(code) * 4, 4);
+        std::memcpy(&id, gcm + static_cast<size_t>(code) * 4, 4);
         w = static_cast<uint64_t>(static_cast<int64_t>(id));
       } else {
         w = static_cast<uint64_t>(ival(gv, gcol.type, b));
+      }
+      words[b] = w;
+    }
+    const bool gint = gcol.type == QEG_I32 || gcol.type == QEG_I64 || gcol.type == QEG_TS || gcol.type == QEG_BOOL ||
+                      gcol.type == QEG_STR;
+    int64_t gmin = INT64_MAX, gmax = INT64_MIN;
+    if (gint)
+      for (uint64_t b = 0; b < nb; ++b)
+        if (valid_at(gw, b)) {
+          gmin = std::min(gmin, static_cast<int64_t>(words[b]));
+          gmax = std::max(gmax, static_cast<int64_t>(words[b]));
+        }
+    const bool dense_groups =
+        gint && gmin <= gmax && static_cast<uint64_t>(gmax) - static_cast<uint64_t>(gmin) < (uint64_t{1} << 20);
+    std::vector<int32_t> dense_gid(dense_groups ? static_cast<size_t>(gmax - gmin) + 1 : 0, -1);
+    std::unordered_map<uint64_t, uint32_t> gid;
+    for (uint64_t b = 0; b < nb; ++b) {
+      if (!valid_at(gw, b)) {
+        if (null_gid < 0) {
+          null_gid = static_cast<int32_t>(gword.size());
+          gword.push_back(0);
+          gnull.push_back(1);
+        }
+        row_group[b] = null_gid;
+        continue;
+      }
+      const uint64_t w = words[b];
+      if (dense_groups) {
+        int32_t& g = dense_gid[static_cast<size_t>(static_cast<int64_t>(w) - gmin)];
+        if (g < 0) {
+          g = static_cast<int32_t>(gword.size());
+          gword.push_back(w);
+          gnull.push_back(0);
+        }
+        row_group[b] = g;
+        continue;
       }
       auto it = gid.find(w);
       if (it == gid.end()) {
@@ -609,13 +666,10 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
     // Build key -> value id (STR: by value through the code map).
     std::vector<int32_t> bmap, pmap;
     if (kt == QEG_STR) {
-      require(bk.code_map && probe[d->probe_key].code_map, "STR join keys need code maps");
-      const auto b = host_copy(bk.code_map, bk.code_map_len * 4);
-      const auto p = host_copy(probe[d->probe_key].code_map, probe[d->probe_key].code_map_len * 4);
       bmap.resize(bk.code_map_len);
       pmap.resize(probe[d->probe_key].code_map_len);
-      std::memcpy(bmap.data(), b.data(), b.size());
-      std::memcpy(pmap.data(), p.data(), p.size());
+      std::memcpy(bmap.data(), at(f_bmap), bmap.size() * 4);
+      std::memcpy(pmap.data(), at(f_pmap), pmap.size() * 4);
     }
     // (join value, group id) of every build row with a non-NULL key.
     std::vector<int64_t> bval;
@@ -624,7 +678,7 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
     bgrp.reserve(nb);
     int64_t vmin = INT64_MAX, vmax = INT64_MIN;
     for (uint64_t b = 0; b < nb; ++b) {
-      if (!valid_at(bkw, bk_all, b)) continue;
+      if (!valid_at(bkw, b)) continue;
       int64_t v = ival(bkv, bk.type, b);
       if (kt == QEG_STR) {
         require(v >= 0 && static_cast<uint64_t>(v) < bmap.size(), "STR code outside its code map");
@@ -774,23 +828,28 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
       for (size_t i = 0; i < kfirst.size(); ++i)
         kf16[i] = kfirst[i] == 0xffffffffu ? 0xffffu : (kfirst[i] & 0x80000000u) ? 0xfffeu : static_cast<uint16_t>(kfirst[i]);
     }
-    DevBuf dk16(std::max<size_t>(kf16.size(), 1) * 2, ctx->stream);
-    if (!kf16.empty())
-      QEG_CUDA(cudaMemcpyAsync(dk16.get(), kf16.data(), kf16.size() * 2, cudaMemcpyHostToDevice, ctx->stream));
-    DevBuf dk(kstart.size() * 4, ctx->stream), dc(kcount.size() * 4, ctx->stream),
-        dkf(kfirst.size() * 4, ctx->stream), dg(std::max<size_t>(glist.size(), 1) * 4, ctx->stream),
-        dstate(static_cast<size_t>(P.ngroups) * P.nfields * 8, ctx->stream);
-    QEG_CUDA(cudaMemcpyAsync(dk.get(), kstart.data(), kstart.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    QEG_CUDA(cudaMemcpyAsync(dc.get(), kcount.data(), kcount.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    QEG_CUDA(cudaMemcpyAsync(dkf.get(), kfirst.data(), kfirst.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    if (!glist.empty())
-      QEG_CUDA(cudaMemcpyAsync(dg.get(), glist.data(), glist.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    // The translation tables go to the device in one copy from the context's
+    // page-locked buffer into one device buffer: kstart, kcount, kfirst,
+    // glist (u32 each), then kf16 (u16); the state is zeroed beside them.
+    const size_t n_kst = kstart.size(), n_kfi = kfirst.size(), n_gl = std::max<size_t>(glist.size(), 1);
+    const size_t o_kst = 0, o_kct = o_kst + n_kst * 4, o_kfi = o_kct + n_kst * 4, o_gl = o_kfi + n_kfi * 4;
+    const size_t o_k16 = (o_gl + n_gl * 4 + 15) & ~size_t{15};
+    const size_t tbl_bytes = o_k16 + ((std::max<size_t>(kf16.size(), 1) * 2 + 15) & ~size_t{15});
+    uint8_t* tbl = static_cast<uint8_t*>(ctx->pinned_out.reserve(tbl_bytes));
+    std::memcpy(tbl + o_kst, kstart.data(), n_kst * 4);
+    std::memcpy(tbl + o_kct, kcount.data(), n_kst * 4);
+    std::memcpy(tbl + o_kfi, kfirst.data(), n_kfi * 4);
+    if (!glist.empty()) std::memcpy(tbl + o_gl, glist.data(), glist.size() * 4);
+    if (!kf16.empty()) std::memcpy(tbl + o_k16, kf16.data(), kf16.size() * 2);
+    DevBuf dtbl(tbl_bytes, ctx->stream), dstate(static_cast<size_t>(P.ngroups) * P.nfields * 8, ctx->stream);
+    QEG_CUDA(cudaMemcpyAsync(dtbl.get(), tbl, tbl_bytes, cudaMemcpyHostToDevice, ctx->stream));
     QEG_CUDA(cudaMemsetAsync(dstate.get(), 0, dstate.bytes(), ctx->stream));
-    P.kstart = dk.get<uint32_t>();
-    P.kcount = dc.get<uint32_t>();
-    P.kfirst = dkf.get<uint32_t>();
-    P.kf16 = kf16.empty() ? nullptr : dk16.get<uint16_t>();
-    P.glist = dg.get<uint32_t>();
+    uint8_t* dt = dtbl.get<uint8_t>();
+    P.kstart = reinterpret_cast<const uint32_t*>(dt + o_kst);
+    P.kcount = reinterpret_cast<const uint32_t*>(dt + o_kct);
+    P.kfirst = reinterpret_cast<const uint32_t*>(dt + o_kfi);
+    P.kf16 = kf16.empty() ? nullptr : reinterpret_cast<const uint16_t*>(dt + o_k16);
+    P.glist = reinterpret_cast<const uint32_t*>(dt + o_gl);
     P.state = dstate.get<unsigned long long>();
     const int block = 512;
     // The kernel for this field set: COUNT(*) with SUM/AVG over an F64 column
