@@ -1745,9 +1745,7 @@ void AggState::launch(const AggK& P, uint64_t nrows) {
   }
 #undef QEG_AGG_SPEC
 #undef QEG_AGG_VARIANT
-  int per_sm = 1;
-  if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
+  const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), block, sb);
   require(per_sm > 0, "aggregate kernel does not fit on an SM with this configuration");
   // Each CTA should aggregate a few thousand rows at least, so clearing and
   // flushing its private table (which touches occupied rows only) stays small.
@@ -1851,8 +1849,7 @@ void AggState::consume(const qeg_column* cols, int ncols, const uint32_t* sel, u
 // table and replay them.
 void AggState::settle(const std::vector<StagedCol>& staged, uint64_t len) {
   uint64_t c[3];
-  read_counters(c);
-  check_device_error(ctx);
+  read_words_and_error(ctx, counters.get(), 3, c);  // one synchronisation
   inserted = c[2];
   uint64_t nspill = c[0], nparts = c[1];
   int rounds = 0;
@@ -1880,8 +1877,7 @@ void AggState::settle(const std::vector<StagedCol>& staged, uint64_t len) {
       AggK Q = kparams(staged, rows_copy.get<uint32_t>(), nspill, len);
       launch(Q, nspill);
     }
-    read_counters(c);
-    check_device_error(ctx);
+    read_words_and_error(ctx, counters.get(), 3, c);
     inserted = c[2];
     nspill = c[0];
     nparts = c[1];

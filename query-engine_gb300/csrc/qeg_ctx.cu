@@ -1,4 +1,6 @@
 // qeg_ctx.cu -- context, staging of host inputs, result fetch, device error word.
+#include <mutex>
+
 #include "qeg_internal.h"
 
 thread_local std::string g_qeg_tls_err;
@@ -96,6 +98,62 @@ void check_device_error(qeg_ctx* ctx) {
   uint32_t e = 0;
   QEG_CUDA(cudaMemcpyAsync(&e, ctx->dev_err.get(), 4, cudaMemcpyDeviceToHost, ctx->stream));
   QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  raise_device_error(ctx, e);
+}
+
+void read_words_and_error(qeg_ctx* ctx, const void* dev_words, size_t nwords, uint64_t* out) {
+  uint8_t* pin = static_cast<uint8_t*>(ctx->pinned_in.reserve(nwords * 8 + 16));
+  if (nwords)
+    QEG_CUDA(cudaMemcpyAsync(pin + 16, dev_words, nwords * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaMemcpyAsync(pin, ctx->dev_err.get(), 4, cudaMemcpyDeviceToHost, ctx->stream));
+  QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  uint32_t e;
+  std::memcpy(&e, pin, 4);
+  if (nwords) std::memcpy(out, pin + 16, nwords * 8);
+  raise_device_error(ctx, e);
+}
+
+int blocks_per_sm(const void* kern, int block, size_t smem) {
+  int dev = 0;
+  QEG_CUDA(cudaGetDevice(&dev));
+  // The shared-memory attribute belongs to the function (for every thread of
+  // the process), so it is only ever raised: the largest size set so far is
+  // kept per (device, kernel), and a launch asking for more raises it. The
+  // occupancy answers are cached per (device, kernel, block, shared bytes).
+  struct Attr {
+    const void* kern;
+    int dev;
+    size_t smem;
+  };
+  struct Occ {
+    const void* kern;
+    int dev, block;
+    size_t smem;
+    int per_sm;
+  };
+  static std::mutex mu;
+  static std::vector<Attr> attrs;
+  static std::vector<Occ> occs;
+  std::lock_guard<std::mutex> lock(mu);
+  if (smem > 48 * 1024) {
+    Attr* a = nullptr;
+    for (Attr& x : attrs)
+      if (x.kern == kern && x.dev == dev) a = &x;
+    if (!a || a->smem < smem) {
+      QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+      if (a) a->smem = smem;
+      else attrs.push_back(Attr{kern, dev, smem});
+    }
+  }
+  for (const Occ& o : occs)
+    if (o.kern == kern && o.dev == dev && o.block == block && o.smem == smem) return o.per_sm;
+  int per_sm = 0;
+  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
+  occs.push_back(Occ{kern, dev, block, smem, per_sm});
+  return per_sm;
+}
+
+void raise_device_error(qeg_ctx* ctx, uint32_t e) {
   if (e == kDevOk) return;
   QEG_CUDA(cudaMemsetAsync(ctx->dev_err.get(), 0, 4, ctx->stream));
   if (e & kDevSpinTimeout)

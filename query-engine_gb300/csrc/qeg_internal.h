@@ -45,6 +45,11 @@ inline void cuda_check(cudaError_t e, const char* what) {
 inline void require(bool ok, const std::string& msg) {
   if (!ok) throw Error(QEG_ERR_INVALID, msg);
 }
+// The same for a message literal: the message string is only built on
+// failure (checks inside per-row host loops cost nothing when they pass).
+inline void require(bool ok, const char* msg) {
+  if (!ok) throw Error(QEG_ERR_INVALID, std::string(msg));
+}
 
 // Stream-ordered device buffer (cudaMallocAsync on the context stream).
 class DevBuf {
@@ -181,6 +186,19 @@ void stage_sel(qeg_ctx* ctx, const uint32_t* sel, uint64_t n, DevBuf& buf, const
 
 // Checks and clears the context's device error word (syncs the stream).
 void check_device_error(qeg_ctx* ctx);
+// Copies `nwords` 64-bit words from the device and the context's device error
+// word in one stream synchronisation, then checks the error word as
+// check_device_error does.
+void read_words_and_error(qeg_ctx* ctx, const void* dev_words, size_t nwords, uint64_t* out);
+// Throws the error an error word `e` (read from the device) stands for, after
+// clearing the device copy; returns for no error.
+void raise_device_error(qeg_ctx* ctx, uint32_t e);
+// Blocks per SM of `kern` at `block` threads and `smem` dynamic shared bytes
+// on the current device, after raising the kernel's shared-memory attribute to
+// `smem` when needed (never lowering it); cached per (device, kernel, block,
+// smem). Kernels launched through it must not have the attribute set
+// elsewhere.
+int blocks_per_sm(const void* kern, int block, size_t smem);
 
 inline unsigned grid_for(qeg_ctx* ctx, uint64_t work_items, int block, int blocks_per_sm) {
   const uint64_t want = (work_items + block - 1) / block;

@@ -2959,8 +2959,7 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       }
       // One wave of resident blocks; each thread strides over the probe side.
       auto launch = [&](void (*kern)(SinkK)) {
-        int per_sm = 0;
-        QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+        const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), 256, 0);
         const uint64_t want = (n / 8 + 255) / 256;
         const unsigned grid = static_cast<unsigned>(
             std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));

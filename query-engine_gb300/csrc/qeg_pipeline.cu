@@ -910,10 +910,7 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
           }
         }
         const size_t lsb = lsb_fast ? lsb_fast : static_cast<size_t>(P.ngroups) * na * 8 * T;
-        if (lsb > 48 * 1024)
-          QEG_CUDA(cudaFuncSetAttribute(lk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsb));
-        int lper = 1;
-        QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&lper, lk, T, lsb));
+        const int lper = blocks_per_sm(reinterpret_cast<const void*>(lk), T, lsb);
         const int rows_per_tile = T * (spec == kGenericSpec ? 8 : 16);
         const uint64_t lwant = (np + rows_per_tile - 1) / rows_per_tile;
         const unsigned lgrid = static_cast<unsigned>(
