@@ -1196,10 +1196,13 @@ def cpu_reference(sample, threads, probe_rows, nbuild):
     return (nbuild + probe_rows) / dt, dt, res
 
 
-def run_join_bench(args, dev, local, world, rank, threads, sparse=False, sub=False):
+def run_join_bench(args, dev, local, world, rank, threads, sparse=False, sub=False, cpu_later=None):
     """The join workload: one step = build + probe through the COUNT/SUM sink.
     Returns the JSON object (rank 0) with roofline, e2e, CPU baseline and the
-    full-size parity check. `sub` = a secondary line: fewer steps, no CPU arms."""
+    full-size parity check. `sub` = a secondary line: fewer steps, no CPU arms.
+    With `cpu_later` (a list), the CPU baseline is not run here: a function
+    that runs it and completes the returned object is appended instead, so a
+    caller can time its GPU workloads first."""
     import qeg
 
     strat = {"auto": qeg.JOIN_AUTO, "hash": qeg.JOIN_HASH, "dense": qeg.JOIN_DENSE,
@@ -1305,29 +1308,34 @@ def run_join_bench(args, dev, local, world, rank, threads, sparse=False, sub=Fal
             parity[name + "_equal"] = True
 
     cpu = None
+    cpu_job = None
     if rank == 0 and not args.no_cpu and not sub:
         # The reference's algorithm (the oracle's port of its morsel-parallel
         # engine) on the WHOLE workload, every host thread: one run, which is
         # also a full-size parity check against the oracle.
-        sample = W.cpu_columns(W.nprobe)
-        v, dt, cres = cpu_reference(sample, threads, W.nprobe, W.nbuild)
-        parity["count_sum_vs_oracle"] = cres == res
-        cpu = {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
-               "sample": "the whole workload (%d build + %d probe rows, %.1f s, one run)"
-                         % (W.nbuild, W.nprobe, dt)}
-        # Second reference point: the single-threaded operator tree (scan ->
-        # join -> aggregate, the restatement of Plan::lower + drain).
-        import oracle as O
+        sample = list(W.cpu_columns(W.nprobe))
+        nbuild, nprobe = W.nbuild, W.nprobe
 
-        k1 = min(W.nprobe, 1 << 23)
-        t1 = time.perf_counter()
-        r1 = O.join_count_sum(O.TCol(O.I64, sample[0].values[:k1], sample[0].valid[:k1]),
-                              O.TCol(O.I64, sample[1].values[:k1]), sample[2])
-        dt1 = time.perf_counter() - t1
-        cpu["single_thread"] = {"value": (W.nbuild + k1) / dt1, "unit": "rows/s", "cores": 1,
-                                "sample": "full %d-row build + first %d probe rows (%.1f s), count %d"
-                                          % (W.nbuild, k1, dt1, r1[0])}
-        del sample
+        def cpu_job(out):
+            import oracle as O
+
+            v, dt, cres = cpu_reference(sample, threads, nprobe, nbuild)
+            out["full_size_parity"]["count_sum_vs_oracle"] = cres == res
+            c = {"value": v, "unit": "rows/s", "cores": threads, "kind": "port",
+                 "sample": "the whole workload (%d build + %d probe rows, %.1f s, one run)" % (nbuild, nprobe, dt)}
+            # Second reference point: the single-threaded operator tree (scan
+            # -> join -> aggregate, the restatement of Plan::lower + drain).
+            k1 = min(nprobe, 1 << 23)
+            t1 = time.perf_counter()
+            r1 = O.join_count_sum(O.TCol(O.I64, sample[0].values[:k1], sample[0].valid[:k1]),
+                                  O.TCol(O.I64, sample[1].values[:k1]), sample[2])
+            dt1 = time.perf_counter() - t1
+            c["single_thread"] = {"value": (nbuild + k1) / dt1, "unit": "rows/s", "cores": 1,
+                                  "sample": "full %d-row build + first %d probe rows (%.1f s), count %d"
+                                            % (nbuild, k1, dt1, r1[0])}
+            out["cpu_baseline"] = c
+            sample.clear()
+            assert out["full_size_parity"]["count_sum_vs_oracle"], out["full_size_parity"]
     ok = all(v for k, v in parity.items() if k != "expected")
     assert ok, parity
     kernel = {"dense": "probe_sink_lean_kernel (dense, unique keys)",
@@ -1366,6 +1374,11 @@ def run_join_bench(args, dev, local, world, rank, threads, sparse=False, sub=Fal
     ctx.close()
     del W
     torch.cuda.empty_cache()
+    if cpu_job is not None:
+        if cpu_later is not None:
+            cpu_later.append(lambda: cpu_job(out))
+        else:
+            cpu_job(out)
     return out
 
 
@@ -1425,7 +1438,8 @@ def main():
         return
 
     t_start = time.perf_counter()
-    out = run_join_bench(args, dev, local, world, rank, threads, sparse=args.sparse)
+    cpu_later = []  # the join's CPU baseline runs after every GPU measurement
+    out = run_join_bench(args, dev, local, world, rank, threads, sparse=args.sparse, cpu_later=cpu_later)
     if world == 1 and not args.headline_only and not args.sparse:
         # The default run also measures, each on its own data and each with
         # its full-size parity check: the same join over sparse keys (the hash
@@ -1441,6 +1455,8 @@ def main():
         out["batch"] = run_batch_bench(sub, dev, local, emit=False)
         out["pipeline"] = run_pipeline_bench(sub, dev, local, emit=False)
         out["operators"] = operator_bench()
+        while cpu_later:
+            cpu_later.pop(0)()
         fsp = {"join": out["full_size_parity"]}
         for k in ("sparse_keys", "plain_agg", "skew_agg", "batch", "pipeline"):
             fsp[k] = out[k]["full_size_parity"]
@@ -1449,6 +1465,8 @@ def main():
         out["full_size_parity_all"] = all(
             v.get("ok", all(x for kk, x in v.items() if kk not in ("expected",) and isinstance(x, bool)))
             for v in fsp.values())
+    while cpu_later:
+        cpu_later.pop(0)()
     out["bench_wall_s"] = time.perf_counter() - t_start
     if rank == 0:
         print(json.dumps(out))

@@ -277,6 +277,10 @@ __device__ __forceinline__ bool filter_bits(const PipeK& P, uint64_t b) {
   }
 }
 
+// Largest CTA of the thread-private kernels (the typed trades kernel fits 320
+// threads' states for 32 groups beside its translation table).
+constexpr int kLanesMaxThreads = 384;
+
 // Active fields of a field set: field 0 (the row count) and every field
 // whose kind is not 0, in field order ("compact" indexes).
 __host__ __device__ constexpr int spec_nactive(uint32_t spec) {
@@ -313,13 +317,15 @@ __host__ __device__ constexpr int spec_compact(uint32_t spec, int i) {
 // global state. NA = the active field count (spec_nactive, or nfields for
 // the generic field set).
 template <uint32_t SPEC, int R, int FASTOP>
-__global__ void __launch_bounds__(256, 1) pipeline_lanes_kernel(const PipeK P, int NA) {
+__global__ void __launch_bounds__(kLanesMaxThreads, 1) pipeline_lanes_kernel(const PipeK P, int NA) {
   extern __shared__ unsigned long long acc[];
   constexpr int NVR = SPEC == kGenericSpec ? kPipeMaxVals : 2;  // value columns a row carries
   const int T = blockDim.x;
   const int total = P.ngroups * NA;
-  for (int i = threadIdx.x; i < total * T; i += T) acc[i] = 0;
-  __syncthreads();
+  if constexpr (FASTOP < 0) {
+    for (int i = threadIdx.x; i < total * T; i += T) acc[i] = 0;
+    __syncthreads();
+  }
   const unsigned lane = threadIdx.x & 31u;
   const unsigned warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const uint64_t tile = static_cast<uint64_t>(T) * R;
@@ -343,7 +349,15 @@ __global__ void __launch_bounds__(256, 1) pipeline_lanes_kernel(const PipeK P, i
     const double* __restrict__ price = static_cast<const double*>(P.val[0].data);
     const int32_t* __restrict__ qty = static_cast<const int32_t*>(P.val[1].data);
     const double lit = P.flit_f;
-    uint16_t* kf16 = reinterpret_cast<uint16_t*>(acc + static_cast<size_t>(total) * T);
+    // Shared memory: the row counts as u32 (a thread counts fewer than 2^32
+    // rows), [group][thread]; then the sums, [group][SUM(F64), SUM(int)]
+    // [thread]; then the u16 translation table. 20 bytes per group and
+    // thread instead of 24 leave room for more threads.
+    const size_t cnt_words = (static_cast<size_t>(P.ngroups) * T + 1) / 2;
+    uint32_t* const cnt = reinterpret_cast<uint32_t*>(acc);
+    unsigned long long* const sums = acc + cnt_words;
+    uint16_t* kf16 = reinterpret_cast<uint16_t*>(sums + static_cast<size_t>(P.ngroups) * 2 * T);
+    for (size_t i = threadIdx.x; i < cnt_words + static_cast<size_t>(P.ngroups) * 2 * T; i += T) acc[i] = 0;
     for (uint64_t i = threadIdx.x; i < P.key_domain; i += T) kf16[i] = P.kf16[i];
     __syncthreads();
     auto pass_of = [&](double v) {
@@ -358,17 +372,17 @@ __global__ void __launch_bounds__(256, 1) pipeline_lanes_kernel(const PipeK P, i
     // 4-byte keys and their domain need 32-bit arithmetic only.
     const int32_t kmin32 = static_cast<int32_t>(P.key_min);
     const uint32_t dom32 = static_cast<uint32_t>(P.key_domain);
-    unsigned long long* const mine = acc + threadIdx.x;
-    const int gstride = 3 * T;
+    uint32_t* const my_cnt = cnt + threadIdx.x;
+    unsigned long long* const my_sum = sums + threadIdx.x;
     auto apply = [&](int32_t k, double v, int32_t q) {
       const uint32_t sl = static_cast<uint32_t>(k) - static_cast<uint32_t>(kmin32);
       if (!pass_of(v) || k < kmin32 || sl >= dom32) return;
       const uint32_t g = kf16[sl];
       if (g == 0xffffu) return;
-      unsigned long long* a = mine + g * gstride;
-      a[0] += 1;
-      a[T] = static_cast<unsigned long long>(__double_as_longlong(__longlong_as_double(static_cast<long long>(a[T])) + v));
-      a[2 * T] += static_cast<unsigned long long>(static_cast<long long>(q));
+      my_cnt[g * T] += 1u;
+      unsigned long long* a = my_sum + 2 * g * T;
+      a[0] = static_cast<unsigned long long>(__double_as_longlong(__longlong_as_double(static_cast<long long>(a[0])) + v));
+      a[T] += static_cast<unsigned long long>(static_cast<long long>(q));
     };
     const uint64_t full = P.n / tile * tile;  // rows in full tiles
     for (uint64_t base = blockIdx.x * tile; base < full; base += static_cast<uint64_t>(gridDim.x) * tile) {
@@ -393,6 +407,22 @@ __global__ void __launch_bounds__(256, 1) pipeline_lanes_kernel(const PipeK P, i
     // The rows after the last full tile (fewer than one tile), one per thread.
     if (blockIdx.x == gridDim.x - 1)
       for (uint64_t p = full + threadIdx.x; p < P.n; p += T) apply(__ldg(key + p), __ldg(price + p), __ldg(qty + p));
+    __syncthreads();
+    // Reduce the thread copies (a warp per (group, field)) into the global
+    // state: rows, SUM(F64), SUM(int) are the field set's active fields 0-2.
+    for (int pr = static_cast<int>(warp); pr < P.ngroups * 3; pr += static_cast<int>(nwarps)) {
+      const int g = pr / 3, c = pr % 3;
+      const int f = spec_active_field(SPEC, c);
+      const uint8_t kind = static_cast<uint8_t>(c == 0 ? F_ROWS : spec_kind(SPEC, f));
+      uint64_t x = 0;
+      for (int t = static_cast<int>(lane); t < T; t += 32)
+        x = field_combine(kind, x, c == 0 ? static_cast<uint64_t>(cnt[g * T + t]) : sums[(2 * g + c - 1) * T + t]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x = field_combine(kind, x, __shfl_xor_sync(0xffffffffu, x, o));
+      if (lane == 0 && x)
+        field_red<kRowGlobal>(reinterpret_cast<uint64_t*>(P.state + static_cast<size_t>(g) * P.nfields + f), kind, x);
+    }
+    return;
   } else
   for (uint64_t base = blockIdx.x * tile; base < P.n; base += static_cast<uint64_t>(gridDim.x) * tile) {
     uint32_t slot[R];
@@ -893,12 +923,22 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
         const bool aligned = (reinterpret_cast<uintptr_t>(P.key.data) % 16) == 0 &&
                              (reinterpret_cast<uintptr_t>(P.val[0].data) % 16) == 0 &&
                              (reinterpret_cast<uintptr_t>(P.val[1].data) % 16) == 0;
-        const size_t fast_sb = static_cast<size_t>(P.ngroups) * na * 8 * T + ((domain * 2 + 15) / 16) * 16;
+        // Threads of the typed kernel: the most (a multiple of 32, at most
+        // kLanesMaxThreads) whose states (20 bytes per group and thread) and
+        // the translation table fit.
+        auto fast_bytes = [&](int t) {
+          const size_t cw = (static_cast<size_t>(P.ngroups) * t + 1) / 2;
+          return (cw + static_cast<size_t>(P.ngroups) * 2 * t) * 8 + ((domain * 2 + 15) / 16) * 16;
+        };
+        int T_fast = kLanesMaxThreads;
+        while (T_fast > 64 && fast_bytes(T_fast) > ctx->smem_optin) T_fast -= 32;
+        const size_t fast_sb = fast_bytes(T_fast);
         const bool single = std::none_of(kf16.begin(), kf16.end(), [](uint16_t x) { return x == 0xfffeu; });
         if (spec == kPipeSpecAvgSum && key4 && P.key.all_valid && fsame && P.val[1].type == kI32 &&
             P.val[1].all_valid && aligned && P.kf16 && single && domain < (1ull << 31) &&
             fast_sb <= ctx->smem_optin) {
           lsb_fast = fast_sb;
+          T = T_fast;
           switch (P.fop) {
             case kLT: lk = pipeline_lanes_kernel<kPipeSpecAvgSum, 16, kLT>; break;
             case kLE: lk = pipeline_lanes_kernel<kPipeSpecAvgSum, 16, kLE>; break;
