@@ -182,17 +182,27 @@ class JoinWorkload:
     and probe) pushed through the odd-multiplier bijection, so the build side is
     16M unique keys spread over all of int64 and the join takes the hash table."""
 
-    def __init__(self, dev, nbuild=1 << 24, nprobe=1 << 28, seed=SEED + 2, sparse=False):
+    def __init__(self, dev, nbuild=1 << 24, nprobe=1 << 28, seed=SEED + 2, sparse=False, distinct=None):
+        """`distinct` (with sparse=True): build keys drawn with repetition from
+        `distinct` values (0..distinct-1 before the bijection), so the build
+        side repeats each key nbuild / distinct times on average."""
         g = torch.Generator(device=dev)
         g.manual_seed(seed)
         self.sparse = sparse
-        self.name = "join_%dMx%dM_count_sum%s" % (nbuild >> 20, nprobe >> 20, "_sparse_keys" if sparse else "")
+        self.distinct = distinct
+        self.name = "join_%dMx%dM_count_sum%s" % (
+            nbuild >> 20, nprobe >> 20,
+            ("_repeated_keys_%dM_distinct" % (distinct >> 20)) if distinct else ("_sparse_keys" if sparse else ""))
         self.nbuild, self.nprobe = nbuild, nprobe
-        self.bkey = torch.randperm(nbuild, generator=g, device=dev, dtype=torch.int64)
+        if distinct:
+            self.bkey = torch.randint(0, distinct, (nbuild,), generator=g, device=dev, dtype=torch.int64)
+        else:
+            self.bkey = torch.randperm(nbuild, generator=g, device=dev, dtype=torch.int64)
         self.bvalid = pack_bits_torch(torch.rand(nbuild, generator=g, device=dev) >= 0.02)
         hit = torch.rand(nprobe, generator=g, device=dev) < 0.5
-        inb = torch.randint(0, nbuild, (nprobe,), generator=g, device=dev, dtype=torch.int64)
-        out = torch.randint(nbuild, 2 * nbuild, (nprobe,), generator=g, device=dev, dtype=torch.int64)
+        span = distinct or nbuild
+        inb = torch.randint(0, span, (nprobe,), generator=g, device=dev, dtype=torch.int64)
+        out = torch.randint(span, 2 * span, (nprobe,), generator=g, device=dev, dtype=torch.int64)
         self.pkey = torch.where(hit, inb, out)
         del inb, out, hit
         self.pvalid = pack_bits_torch(torch.rand(nprobe, generator=g, device=dev) >= 0.02)
@@ -215,12 +225,13 @@ class JoinWorkload:
     def h2d_bytes(self):
         return self.nbuild * 8 + self.bvalid.numel() * 8 + self.nprobe * 16 + self.pvalid.numel() * 8
 
-    def run(self, qeg, ctx, strategy, events=None, host=None):
+    def run(self, qeg, ctx, strategy, events=None, host=None, sizing=None):
         """One step: build the table from the build side, probe the whole probe
         side through the COUNT/SUM sink. `events` = [build start, probe start,
         probe end, stream] (CUDA events recorded on the library's stream)."""
         src = host if host is not None else self
-        j = qeg.Join(ctx, [qeg.I64, qeg.I64], [qeg.I64], [0], [0], strategy=strategy)
+        j = qeg.Join(ctx, [qeg.I64, qeg.I64], [qeg.I64], [0], [0], strategy=strategy,
+                     sizing=qeg.SIZE_LEARNED if sizing is None else sizing)
         if events:
             events[0].record(events[3])
         j.build([qeg.Col(src.bkey, src.bvalid, qeg.I64)])
@@ -1382,6 +1393,74 @@ def run_join_bench(args, dev, local, world, rank, threads, sparse=False, sub=Fal
     return out
 
 
+def run_join_sizing_bench(args, dev, local, emit=True):
+    """Learned vs plain table sizing of a hashed join whose build side repeats
+    its keys: 16M build rows over 1M distinct sparse keys, 256M probe rows
+    (half hits), COUNT(*) + SUM(payload). Plain sizing gives the table two
+    slots per build row (2^25); learned sizing sketches the build keys and
+    gives it four per estimated distinct key. One step = build + probe."""
+    import qeg
+
+    W = JoinWorkload(dev, args.build_rows, args.probe_rows, sparse=True, distinct=1 << 20)
+    ctx = qeg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    steps = min(args.steps, 10)
+    warm = max(3, min(args.warmup, 3))
+    peak, pkind = peaks()
+    exp = W.expected_torch()
+    out = {}
+    clk = ClockSampler(local).__enter__()
+    tw0 = time.time()
+    for name, sizing in (("learned", qeg.SIZE_LEARNED), ("plain_fixed", qeg.SIZE_FIXED)):
+        for _ in range(warm):
+            res, st = W.run(qeg, ctx, qeg.JOIN_AUTO, sizing=sizing)
+        ctx.synchronize()
+        evs = []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            pe = [torch.cuda.Event(enable_timing=True) for _ in range(3)] + [stream]
+            res, st = W.run(qeg, ctx, qeg.JOIN_AUTO, events=pe, sizing=sizing)
+            evs.append(pe)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        bms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+        pms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+        out[name] = {"ms_per_step": ms, "rows_per_s": W.rows() / (ms / 1e3), "build_ms": bms, "probe_ms": pms,
+                     "probe_frac": W.algorithmic_probe_bytes() / (pms / 1e3) / 1e9 / peak, "stats": st,
+                     "count_sum_vs_torch": res == exp}
+    clocks = clk.summary(tw0, time.time())
+    clk.__exit__(None, None, None)
+    parity = {"learned_vs_torch": out["learned"]["count_sum_vs_torch"],
+              "plain_vs_torch": out["plain_fixed"]["count_sum_vs_torch"],
+              "expected": {"count": exp[0], "sum": exp[1]}}
+    assert parity["learned_vs_torch"] and parity["plain_vs_torch"], parity
+    best = out["learned"]
+    line = {
+        "metric": "rows/s hash join (build+probe rows), inner join COUNT(*)+SUM(payload), learned vs plain sizing",
+        "value": best["rows_per_s"], "unit": "rows/s", "n_gpus": 1, "steps": steps, "warmup": warm,
+        "ms_per_step": best["ms_per_step"], "higher_is_better": True, "dtype": "int64",
+        "data": "synthetic (seeded, generated on the GPU)",
+        "config": {"workload": W.name, "build_rows": W.nbuild, "probe_rows": W.nprobe, "distinct_build_keys": 1 << 20,
+                   "seed": SEED + 2, "keys": "sparse (odd-multiplier bijection over int64), repeated on the build side",
+                   "null_keys": "2% both sides", "probe_hit_rate": 0.5},
+        "roofline": {"bound": "hbm", "kernel": "probe_sink_lean_kernel (hash table)",
+                     "achieved": W.algorithmic_probe_bytes() / (best["probe_ms"] / 1e3) / 1e9, "peak": peak,
+                     "peak_kind": pkind, "unit": "GB/s", "frac": best["probe_frac"], "probe_ms": best["probe_ms"]},
+        "variants": out,
+        "learned_vs_plain": out["plain_fixed"]["ms_per_step"] / best["ms_per_step"],
+        "full_size_parity": parity,
+        "clocks": clocks,
+    }
+    ctx.close()
+    del W
+    torch.cuda.empty_cache()
+    if emit:
+        print(json.dumps(line))
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1436,6 +1515,9 @@ def main():
     if args.workload == "asof":
         run_asof_bench(args, dev, local)
         return
+    if args.workload == "join_sizing":
+        run_join_sizing_bench(args, dev, local)
+        return
 
     t_start = time.perf_counter()
     cpu_later = []  # the join's CPU baseline runs after every GPU measurement
@@ -1449,6 +1531,7 @@ def main():
         sub = argparse.Namespace(**vars(args))
         sub.no_cpu = True
         out["sparse_keys"] = run_join_bench(sub, dev, local, world, rank, threads, sparse=True, sub=True)
+        out["repeated_keys"] = run_join_sizing_bench(sub, dev, local, emit=False)
         sub.no_cpu = args.no_cpu
         out["plain_agg"] = run_agg_bench(sub, dev, local, kind="agg1m", emit=False)
         out["skew_agg"] = run_agg_bench(sub, dev, local, kind="skew", emit=False)
@@ -1458,7 +1541,7 @@ def main():
         while cpu_later:
             cpu_later.pop(0)()
         fsp = {"join": out["full_size_parity"]}
-        for k in ("sparse_keys", "plain_agg", "skew_agg", "batch", "pipeline"):
+        for k in ("sparse_keys", "repeated_keys", "plain_agg", "skew_agg", "batch", "pipeline"):
             fsp[k] = out[k]["full_size_parity"]
         fsp["operators_agg"] = {"ok": bool(out["operators"].get("agg", {}).get("check_counts_vs_host"))}
         fsp["operators_join"] = {"ok": bool(out["operators"].get("join", {}).get("check_count_sum_vs_host"))}

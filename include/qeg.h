@@ -132,6 +132,11 @@ typedef struct qeg_agg_config {
 typedef struct qeg_join_config {
   int32_t strategy;       /* QEG_JOIN_*                                     */
   int32_t partition_bits; /* QEG_JOIN_PARTITIONED: 0 = tuned                */
+  int32_t sizing;         /* QEG_SIZE_LEARNED (0): a single-key hash table of
+                             a large build side is sized from the estimated
+                             distinct build keys (sketch + estimator), and
+                             rebuilt at full size if it overflows;
+                             QEG_SIZE_FIXED: two slots per build row       */
 } qeg_join_config;
 
 typedef struct qeg_ctx qeg_ctx;
@@ -264,6 +269,12 @@ qeg_status qeg_join_count_sum_result(qeg_join* j, int64_t* count, int64_t* sum,
  * number of distinct non-null build keys. */
 qeg_status qeg_join_stats(const qeg_join* j, int32_t* strategy, int32_t* partition_bits,
                           uint64_t* distinct_keys);
+/* Hash-table sizing of the build (no counterpart in the reference, whose
+ * HashTable grows from a fixed start): table slots, the estimated distinct
+ * build keys it was sized from (0 when sized from the row count), and how
+ * many times an estimate-sized table overflowed and was rebuilt at full
+ * size. Any pointer may be NULL. */
+qeg_status qeg_join_sizing_stats(const qeg_join* j, uint64_t* slots, double* est_distinct, int32_t* rebuilds);
 void qeg_join_destroy(qeg_join* j);
 
 /* ---- fused filter -> inner join -> GROUP BY --------------------------------

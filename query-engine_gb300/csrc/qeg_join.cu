@@ -24,6 +24,7 @@
 // then build columns (ops/join_internal.h:136-179). The COUNT(*)/SUM(payload)
 // sink is fused into one probe kernel.
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 
 #include "qeg_agg.h"
@@ -41,6 +42,15 @@ constexpr uint32_t kNullRow = 0xffffffffu;  // ops/join_internal.h:31
 // positive rate of about 0.5%, in 32 MB for 16M build rows.
 constexpr uint64_t kBloomMinTableBytes = 32ull << 20;
 constexpr uint64_t kBloomBitsPerKey = 16;
+// Learned sizing of hashed single-key builds (QEG_SIZE_LEARNED): build sides
+// of at least kJoinSketchMinRows rows are sketched, and the table gets
+// kJoinSlotsPerEstimatedKey slots per estimated distinct key (a power of two,
+// never more than the row count's two per row): load 0.25 at the estimate,
+// 0.5 at a two-fold underestimate. Inserts into such a table give up after
+// kEstimatedTableProbeLimit slots; an overflow rebuilds it at full size.
+constexpr uint64_t kJoinSketchMinRows = 1ull << 20;
+constexpr double kJoinSlotsPerEstimatedKey = 4.0;
+constexpr uint64_t kEstimatedTableProbeLimit = 1024;
 
 struct JTable {
   int strategy;    // QEG_JOIN_HASH / QEG_JOIN_DENSE
@@ -105,12 +115,14 @@ __device__ __forceinline__ int64_t dense_value(const DevCol& c, uint64_t p) { re
 // Key word 0 of a single key has the side slot `cap`, which the caller tracks.
 template <bool INSERT>
 __device__ __forceinline__ int64_t hash_slot(const JTable& T, const uint64_t* w, uint64_t h, uint32_t* err,
-                                             bool* existed = nullptr) {
+                                             bool* existed = nullptr, uint64_t limit = ~0ull) {
   if (T.nkeys == 1) {
     const uint64_t k = w[0];
     if (k == 0) return static_cast<int64_t>(T.cap);
     uint64_t s = h >> T.shift;  // home slot: the top bits of the hash
-    for (uint64_t t = 0; t < T.cap; ++t) {
+    // (`limit`: an insert into a table sized from an estimate gives up after
+    // that many slots; the build is then redone at full size.)
+    for (uint64_t t = 0; t < T.cap && t < limit; ++t) {
       uint64_t* r = T.keys + s;
       uint64_t cur = ld_relaxed64(r);
       if (cur == k) {
@@ -174,6 +186,10 @@ struct BuildK {
   unsigned long long* distinct;
   uint32_t* err;
   unsigned long long* bloom;  // single key: the Bloom filter to fill (nullptr: none)
+  // Single key, table sized from an estimate: inserts give up after
+  // probe_limit slots and raise *ovf (nullptr: full-size table, no limit).
+  uint32_t* ovf;
+  uint64_t probe_limit;
 };
 
 __global__ void build_count_kernel(BuildK P) {
@@ -188,9 +204,10 @@ __global__ void build_count_kernel(BuildK P) {
     if (P.T.strategy == QEG_JOIN_DENSE) {
       s = dense_value(P.key[0], r) - P.T.dmin;
     } else {
-      s = hash_slot<true>(P.T, w, h, P.err, &existed);
+      s = hash_slot<true>(P.T, w, h, P.err, &existed, P.ovf ? P.probe_limit : ~0ull);
       if (s < 0) {
-        atomicOr(P.err, kDevSpillOverflow);
+        if (P.ovf) atomicExch(P.ovf, 1u);  // the table is too small: the host rebuilds it
+        else atomicOr(P.err, kDevSpillOverflow);
         continue;
       }
     }
@@ -1942,6 +1959,8 @@ struct JoinState {
   std::vector<uint32_t> pkeys, bkeys;
   int32_t join_type = QEG_INNER;
   qeg_join_config cfg{};
+  double est_distinct = 0;  // distinct build keys the hash table was sized from (0: row count)
+  int32_t rebuilds = 0;     // estimate-sized tables that overflowed and were rebuilt
 
   // build store
   std::vector<DevBuf> bvals, bvalid;
@@ -2073,7 +2092,7 @@ struct JoinState {
   }
 
   void finish_build();
-  void build_hash(BuildK& P);
+  void build_hash(BuildK& P, uint64_t want_cap = 0);
   uint64_t slots() const {
     return strategy == QEG_JOIN_DENSE ? cap : (bkeys.size() == 1 ? cap + 1 : cap);
   }
@@ -2170,7 +2189,21 @@ void JoinState::finish_build() {
     }
   } else {
     P.no_count = asof ? 1 : 0;
-    build_hash(P);
+    uint64_t want_cap = 0;
+    est_distinct = 0;
+    if (cfg.sizing == QEG_SIZE_LEARNED && nk == 1 && !asof && nbuild >= kJoinSketchMinRows) {
+      // Table size from the estimated distinct build keys (the learned
+      // estimator, or the classic one without weights).
+      SketchResult sk;
+      sketch_key_column(ctx, store_key(0), nullptr, nbuild, nbuild, 1u << 20, 0, sk);
+      double g = 0, share = 0;
+      if (!learned_estimate(ctx, sk, &g, &share)) g = classic_estimate(sk);
+      if (const char* e = getenv("QEG_JOIN_EST_SCALE")) g *= atof(e);  // (tests: force a misestimate)
+      est_distinct = std::max(g, 1.0);
+      want_cap = std::max<uint64_t>(1024, next_pow2(static_cast<uint64_t>(std::ceil(kJoinSlotsPerEstimatedKey * est_distinct))));
+    }
+    P.ovf = dup.get<uint32_t>() + 1;
+    build_hash(P, want_cap);
   }
   // The radix-partitioned join probes the same table (single key only).
   if (strategy == QEG_JOIN_HASH && nk == 1 && cfg.strategy == QEG_JOIN_PARTITIONED) {
@@ -2180,6 +2213,16 @@ void JoinState::finish_build() {
   uint64_t d[2] = {0, 0};
   QEG_CUDA(cudaMemcpyAsync(d, dup.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
   check_device_error(ctx);  // its synchronisation also lands d
+  if (strategy != QEG_JOIN_DENSE && (d[0] >> 32) != 0) {
+    // The estimate-sized table overflowed: build again at full size.
+    ++rebuilds;
+    est_distinct = 0;
+    QEG_CUDA(cudaMemsetAsync(dup.get(), 0, 16, ctx->stream));
+    P.ovf = nullptr;
+    build_hash(P, 0);
+    QEG_CUDA(cudaMemcpyAsync(d, dup.get(), 16, cudaMemcpyDeviceToHost, ctx->stream));
+    check_device_error(ctx);
+  }
   distinct = d[1];
   // Dense: the keys are unique when every non-NULL key set its own bit.
   unique = strategy == QEG_JOIN_DENSE ? (distinct == nonnull ? 1 : 0) : ((d[0] & 0xffffffffull) ? 0 : 1);
@@ -2279,9 +2322,14 @@ void JoinState::asof_build() {
 }
 
 // One global hash table of the build keys (+ per-slot row counts).
-void JoinState::build_hash(BuildK& P) {
+void JoinState::build_hash(BuildK& P, uint64_t want_cap) {
   const int nk = static_cast<int>(bkeys.size());
-  cap = std::max<uint64_t>(1024, next_pow2(2 * std::max<uint64_t>(nbuild, 1)));
+  const uint64_t full = std::max<uint64_t>(1024, next_pow2(2 * std::max<uint64_t>(nbuild, 1)));
+  cap = (want_cap > 0 && want_cap < full) ? want_cap : full;
+  // An estimate-sized single-key table bounds its inserts' probes; a full-size
+  // one (two slots per build row) cannot overflow.
+  P.probe_limit = kEstimatedTableProbeLimit;
+  if (cap == full || nk != 1) P.ovf = nullptr;
   const int kw = nk == 1 ? 1 : 1 + nk;
   const uint64_t krows = nk == 1 ? cap + 1 : cap;
   keys.alloc(krows * kw * 8, ctx->stream);
@@ -2301,7 +2349,12 @@ void JoinState::build_hash(BuildK& P) {
   const int bloom_mode = bloom_env ? atoi(bloom_env) : -1;
   const bool want_bloom = bloom_mode == 1 || (bloom_mode != 0 && krows * 8 >= kBloomMinTableBytes);
   if (nk == 1 && !asof && want_bloom) {
-    const uint64_t words = next_pow2(std::max<uint64_t>(64, (nbuild * kBloomBitsPerKey + 63) / 64));
+    // Bits per distinct key: the estimate's (with a two-fold margin) when the
+    // table was sized from it, else the build rows'.
+    const uint64_t bkeys_n = (cap < full && est_distinct > 0)
+                                 ? std::min<uint64_t>(nbuild, static_cast<uint64_t>(2.0 * est_distinct) + 1)
+                                 : nbuild;
+    const uint64_t words = next_pow2(std::max<uint64_t>(64, (bkeys_n * kBloomBitsPerKey + 63) / 64));
     int lg = 0;
     while ((1ull << lg) < words) ++lg;
     bloom.alloc(words * 8, ctx->stream);
@@ -3095,6 +3148,16 @@ qeg_status qeg_join_stats(const qeg_join* j, int32_t* strategy, int32_t* partiti
     if (strategy) *strategy = j->st.strategy;
     if (partition_bits) *partition_bits = j->st.strategy == QEG_JOIN_PARTITIONED ? j->st.part_bits : 0;
     if (distinct_keys) *distinct_keys = j->st.distinct;
+  });
+}
+
+qeg_status qeg_join_sizing_stats(const qeg_join* j, uint64_t* slots, double* est_distinct, int32_t* rebuilds) {
+  qeg_ctx* ctx = j ? j->st.ctx : nullptr;
+  return guarded(ctx, [&] {
+    require(j != nullptr, "join is NULL");
+    if (slots) *slots = j->st.cap;
+    if (est_distinct) *est_distinct = j->st.est_distinct;
+    if (rebuilds) *rebuilds = j->st.rebuilds;
   });
 }
 

@@ -54,7 +54,7 @@ class AggConfig(ctypes.Structure):
 
 
 class JoinConfig(ctypes.Structure):
-    _fields_ = [("strategy", ctypes.c_int32), ("partition_bits", ctypes.c_int32)]
+    _fields_ = [("strategy", ctypes.c_int32), ("partition_bits", ctypes.c_int32), ("sizing", ctypes.c_int32)]
 
 
 _lib = None
@@ -96,6 +96,7 @@ def lib():
             "qeg_join_probe_count_sum": (i32, [vp, vp, vp]),
             "qeg_join_count_sum_result": (i32, [vp, P(ctypes.c_int64), P(ctypes.c_int64), P(i32)]),
             "qeg_join_stats": (i32, [vp, P(i32), P(i32), P(u64)]),
+            "qeg_join_sizing_stats": (i32, [vp, P(u64), P(ctypes.c_double), P(i32)]),
             "qeg_join_destroy": (None, [vp]),
             "qeg_join_count_sum_noalloc": (i32, [vp, vp, vp, vp, vp]),
             "qeg_ctx_check_bounded_wait": (i32, [vp, i32]),
@@ -405,7 +406,7 @@ class Join:
     """The GPU hash-join operator state behind one qeg_join."""
 
     def __init__(self, ctx, probe_types, build_types, probe_keys, build_keys, join_type=INNER,
-                 strategy=JOIN_AUTO, partition_bits=0):
+                 strategy=JOIN_AUTO, partition_bits=0, sizing=SIZE_LEARNED):
         self.ctx = ctx
         self.probe_types = list(probe_types)
         self.build_types = list(build_types)
@@ -413,7 +414,7 @@ class Join:
         bt = (ctypes.c_int32 * max(1, len(build_types)))(*build_types)
         pk = (ctypes.c_uint32 * len(probe_keys))(*probe_keys)
         bk = (ctypes.c_uint32 * len(build_keys))(*build_keys)
-        cfg = JoinConfig(strategy, partition_bits)
+        cfg = JoinConfig(strategy, partition_bits, sizing)
         p = ctypes.c_void_p()
         _check(lib().qeg_join_create(ctx.p, pt, len(probe_types), bt, len(build_types), pk, bk,
                                      len(probe_keys), join_type, ctypes.byref(cfg), ctypes.byref(p)), ctx.p)
@@ -509,7 +510,12 @@ class Join:
     def stats(self):
         st, pb, dk = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint64()
         _check(lib().qeg_join_stats(self.p, ctypes.byref(st), ctypes.byref(pb), ctypes.byref(dk)), self.ctx.p)
-        return {"strategy": st.value, "partition_bits": pb.value, "distinct_keys": dk.value}
+        out = {"strategy": st.value, "partition_bits": pb.value, "distinct_keys": dk.value}
+        slots, est, rb = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_int32()
+        _check(lib().qeg_join_sizing_stats(self.p, ctypes.byref(slots), ctypes.byref(est), ctypes.byref(rb)),
+               self.ctx.p)
+        out.update({"slots": slots.value, "est_distinct": est.value, "rebuilds": rb.value})
+        return out
 
     def close(self):
         if self.p:

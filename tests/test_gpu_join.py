@@ -432,3 +432,58 @@ def test_host_fetch_in_row_chunks(ctx):
                 assert np.array_equal(dvals[dvalid], pv[:count].numpy()[dvalid])
     finally:
         j.close()
+
+
+@pytest.mark.parametrize("kt", [O.I64, O.I32])
+@pytest.mark.parametrize("scale", [None, "0.001"])
+def test_learned_table_sizing_of_repeated_build_keys(ctx, kt, scale, monkeypatch):
+    """A 2M-row build side over about 100k distinct sparse keys: learned sizing
+    (the default) sketches the build keys and gives the table 4 slots per
+    estimated distinct key (a power of two, below the plain size) instead of
+    2 per build row; a forced underestimate
+    (QEG_JOIN_EST_SCALE) overflows the small table, which is rebuilt at full
+    size. COUNT/SUM and the materialised pairs (INNER and LEFT, a probe sample)
+    equal the oracle's and plain sizing's either way."""
+    if scale:
+        monkeypatch.setenv("QEG_JOIN_EST_SCALE", scale)
+    rng = np.random.default_rng(31 + kt)
+    dt = np.int32 if kt == O.I32 else np.int64
+    lim = (1 << 31) - 1 if kt == O.I32 else (1 << 62)
+    nb, nd, npr = 1 << 21, 100_000, 1 << 22
+    distinct = rng.integers(-lim, lim, nd).astype(dt)
+    bkey = distinct[rng.integers(0, nd, nb)]
+    bkey[7] = 0
+    build = O.TCol(kt, bkey, rng.random(nb) >= 0.02)
+    pkey = np.where(rng.random(npr) < 0.5, distinct[rng.integers(0, nd, npr)],
+                    rng.integers(-lim, lim, npr).astype(dt)).astype(dt)
+    pkey[:5] = 0
+    pval = rng.integers(-(1 << 30), 1 << 30, npr).astype(np.int64)
+    pk = O.TCol(kt, pkey, rng.random(npr) >= 0.02)
+    pv = O.TCol(O.I64, pval, rng.random(npr) >= 0.01)
+    exp = O.join_count_sum(pk, pv, build)
+    stats = {}
+    for sizing in (qeg.SIZE_LEARNED, qeg.SIZE_FIXED):
+        j = qeg.Join(ctx, [kt, O.I64], [kt], [0], [0], strategy=qeg.JOIN_HASH, sizing=sizing)
+        j.build([to_gpu(build)])
+        j.build_finish()
+        j.probe_count_sum(to_gpu(pk), to_gpu(pv))
+        got = j.count_sum()
+        stats[sizing] = j.stats()
+        j.close()
+        assert got == exp, (sizing, got, exp)
+    full = 1 << 22  # two slots per build row
+    assert stats[qeg.SIZE_FIXED]["slots"] == full and stats[qeg.SIZE_FIXED]["est_distinct"] == 0
+    learned = stats[qeg.SIZE_LEARNED]
+    if scale:
+        assert learned["rebuilds"] == 1 and learned["slots"] == full, learned
+    else:
+        assert learned["rebuilds"] == 0 and learned["slots"] < full, learned
+        assert 0.5 * nd < learned["est_distinct"] < 8 * nd, learned
+    # Pair materialisation over the same table (a probe sample, both join types).
+    m = 20_000
+    ps = [O.TCol(kt, pkey[:m], pk.valid[:m]), O.TCol(O.I64, pval[:m])]
+    bs = [build, O.TCol(O.I64, rng.integers(0, 1000, nb).astype(np.int64))]
+    for jt in (O.INNER, O.LEFT):
+        ot, orows = O.join(ps, bs, [0], [0], jt)
+        gt, grows = run_gpu(ctx, ps, bs, [0], [0], jt, strategy=qeg.JOIN_HASH)
+        assert_same(gt, grows, ot, orows, "join type %d" % jt)
