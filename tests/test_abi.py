@@ -67,3 +67,29 @@ def test_validity_packing_layout():
         assert (qeg.unpack_validity(w, n) == v).all()
         if n % 64:
             assert int(w[-1]) >> (n % 64) == (1 << (64 - n % 64)) - 1  # padding bits set
+
+
+def test_python_structs_match_the_c_layouts(tmp_path):
+    """Every parameter struct the Python binding passes across the C ABI has
+    the size and field offsets the C compiler gives include/qeg.h."""
+    structs = {"qeg_column": qeg.Column, "qeg_out_column": qeg.OutColumn, "qeg_agg_spec": qeg.AggSpec,
+               "qeg_agg_config": qeg.AggConfig, "qeg_join_config": qeg.JoinConfig,
+               "qeg_pipeline_desc": qeg.PipelineDesc, "qeg_batch_tuning": qeg.BatchTuning}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "qeg.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('  printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            lines.append('  printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        a, b, v = line.split()
+        got[(a, b)] = int(v)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)

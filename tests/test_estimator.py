@@ -121,3 +121,14 @@ def test_learned_estimator_beats_classic_and_sizes_tables(monkeypatch):
     assert np.median(el) < np.median(ec), (el, ec)
     assert max(el) < max(ec), (el, ec)
     assert sum(rl) < sum(rc), (rl, rc)
+
+
+def test_shipped_weights_file_carries_parameters_and_dead_band():
+    """estimator_weights.f32: QEG_MLP_PARAMS float32 parameters, then the dead
+    band of the correction (log2 units) that the trainer picked, in [0, 4]."""
+    if not os.path.exists(WEIGHTS):
+        pytest.skip("no trained estimator weights shipped")
+    w = np.fromfile(WEIGHTS, dtype="<f4")
+    assert w.size == qeg.MLP_PARAMS + 1
+    assert np.all(np.isfinite(w))
+    assert 0.0 <= float(w[-1]) <= 4.0
