@@ -32,6 +32,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <deque>
 #include <optional>
 #include <string>
 #include <string_view>
@@ -55,29 +56,43 @@ inline constexpr std::size_t byte_width(Type t) {
   return 0;
 }
 
+// A string dictionary with the reference's interface (intern / at / size):
+// codes are dense and handed out in first-seen order. The strings live in a
+// deque (stable addresses), and the lookup map's keys are views of them.
 class StringDict {
  public:
-  StringDict() { offsets_.push_back(0); }
+  StringDict() = default;
+  StringDict(const StringDict& o) : values_(o.values_) { reindex(); }
+  StringDict& operator=(const StringDict& o) {
+    if (this != &o) {
+      values_ = o.values_;
+      reindex();
+    }
+    return *this;
+  }
+  // (A moved deque keeps its elements where they are, so the views stay valid.)
+  StringDict(StringDict&&) noexcept = default;
+  StringDict& operator=(StringDict&&) noexcept = default;
+
   std::int32_t intern(std::string_view s) {
-    std::string key(s);
-    auto it = index_.find(key);
-    if (it != index_.end()) return it->second;
-    const auto code = static_cast<std::int32_t>(offsets_.size() - 1);
-    bytes_.insert(bytes_.end(), s.begin(), s.end());
-    offsets_.push_back(static_cast<std::uint32_t>(bytes_.size()));
-    index_.emplace(std::move(key), code);
+    const auto found = codes_.find(s);
+    if (found != codes_.end()) return found->second;
+    const auto code = static_cast<std::int32_t>(values_.size());
+    values_.emplace_back(s);
+    codes_.emplace(std::string_view(values_.back()), code);
     return code;
   }
-  std::string_view at(std::int32_t code) const {
-    const auto c = static_cast<std::size_t>(code);
-    return std::string_view(bytes_.data() + offsets_[c], offsets_[c + 1] - offsets_[c]);
-  }
-  std::size_t size() const noexcept { return offsets_.size() - 1; }
+  std::string_view at(std::int32_t code) const { return values_[static_cast<std::size_t>(code)]; }
+  std::size_t size() const noexcept { return values_.size(); }
 
  private:
-  std::vector<char> bytes_;
-  std::vector<std::uint32_t> offsets_;
-  std::unordered_map<std::string, std::int32_t> index_;
+  void reindex() {
+    codes_.clear();
+    for (std::size_t i = 0; i < values_.size(); ++i)
+      codes_.emplace(std::string_view(values_[i]), static_cast<std::int32_t>(i));
+  }
+  std::deque<std::string> values_;
+  std::unordered_map<std::string_view, std::int32_t> codes_;
 };
 
 struct Column {
