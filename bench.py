@@ -1151,7 +1151,8 @@ def operator_bench(timeout=600):
     """The drop-in operators through the reference's pull interface
     (Operator::open/next/close over a Scan of 2048-row host batches, output
     drained on the host): the 1M-row plain GROUP BY through GpuAggregate and
-    the 16M x 256M join through GpuHashJoin. Runs the C++ driver
+    the 16M x 256M join through GpuHashJoin; then the same two over GpuScans
+    of DeviceTables uploaded once (columns read in place). Runs the C++ driver
     query-engine_gb300/host/bench_operators.cpp (built by the package build)."""
     import qeg  # noqa: F401  (loads libqeg.so first)
     import build as qbuild
@@ -1159,7 +1160,9 @@ def operator_bench(timeout=600):
     exe = qbuild.build_operator_bench()
     out = {}
     for name, argv in (("agg", ["agg", str(1 << 20), "5"]),
-                       ("join", ["join", str(1 << 24), str(1 << 28), "2"])):
+                       ("join", ["join", str(1 << 24), str(1 << 28), "2"]),
+                       ("agg_resident", ["agg_resident", str(1 << 20), "5"]),
+                       ("join_resident", ["join_resident", str(1 << 24), str(1 << 28), "2"])):
         r = subprocess.run([exe] + argv, capture_output=True, text=True, timeout=timeout)
         try:
             out[name] = json.loads(r.stdout.strip().splitlines()[-1])
@@ -1518,6 +1521,9 @@ def main():
     if args.workload == "join_sizing":
         run_join_sizing_bench(args, dev, local)
         return
+    if args.workload == "operators":
+        print(json.dumps(operator_bench()))
+        return
 
     t_start = time.perf_counter()
     cpu_later = []  # the join's CPU baseline runs after every GPU measurement
@@ -1545,6 +1551,10 @@ def main():
             fsp[k] = out[k]["full_size_parity"]
         fsp["operators_agg"] = {"ok": bool(out["operators"].get("agg", {}).get("check_counts_vs_host"))}
         fsp["operators_join"] = {"ok": bool(out["operators"].get("join", {}).get("check_count_sum_vs_host"))}
+        fsp["operators_agg_resident"] = {
+            "ok": bool(out["operators"].get("agg_resident", {}).get("check_counts_vs_host"))}
+        fsp["operators_join_resident"] = {
+            "ok": bool(out["operators"].get("join_resident", {}).get("check_count_sum_vs_host"))}
         out["full_size_parity_all"] = all(
             v.get("ok", all(x for kk, x in v.items() if kk not in ("expected",) and isinstance(x, bool)))
             for v in fsp.values())

@@ -163,6 +163,17 @@ uint64_t qeg_ctx_kernel_launches(const qeg_ctx* ctx);
  * full speed. `*out` is NULL when bytes == 0. qeg_host_free(NULL) is a no-op. */
 qeg_status qeg_host_alloc(uint64_t bytes, void** out);
 void qeg_host_free(void* p);
+/* Device-resident columns, the GPU counterpart of the reference's in-memory
+ * Table (ops/table.h:24-47): device memory on the context's device that
+ * outlives the calls using it, filled once and read in place by every query
+ * (a qeg_column whose pointers are device pointers is used without a copy).
+ * qeg_dev_upload / qeg_dev_download copy `bytes` between host memory and
+ * such a buffer and return when the copy is complete. `*out` is NULL when
+ * bytes == 0; qeg_dev_free(NULL) is a no-op. */
+qeg_status qeg_dev_alloc(qeg_ctx* ctx, uint64_t bytes, void** out);
+qeg_status qeg_dev_upload(qeg_ctx* ctx, void* dst, const void* src, uint64_t bytes);
+qeg_status qeg_dev_download(qeg_ctx* ctx, void* dst, const void* src, uint64_t bytes);
+void qeg_dev_free(void* p);
 /* Failure-detection check, no counterpart in the reference (whose CPU hash
  * table never waits on another thread; its analogue is the bounded probe of
  * ops/hashtable.h:84-89). Runs the bounded wait that every composite-key table

@@ -285,6 +285,49 @@ void qeg_host_free(void* p) {
   if (p) cudaFreeHost(p);
 }
 
+qeg_status qeg_dev_alloc(qeg_ctx* ctx, uint64_t bytes, void** out) {
+  return qeg::guarded(ctx, [&] {
+    qeg::require(ctx != nullptr && out != nullptr, "ctx/out is NULL");
+    *out = nullptr;
+    if (bytes == 0) return;
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    const cudaError_t e = cudaMalloc(out, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      *out = nullptr;
+      throw qeg::Error(QEG_ERR_OOM, std::string("device allocation: ") + cudaGetErrorString(e));
+    }
+  });
+}
+
+qeg_status qeg_dev_upload(qeg_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
+  return qeg::guarded(ctx, [&] {
+    qeg::require(ctx != nullptr, "ctx is NULL");
+    if (bytes == 0) return;
+    qeg::require(dst != nullptr && src != nullptr, "dst/src is NULL");
+    qeg::require(qeg::is_device_ptr(dst), "upload destination is not device memory");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    QEG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+qeg_status qeg_dev_download(qeg_ctx* ctx, void* dst, const void* src, uint64_t bytes) {
+  return qeg::guarded(ctx, [&] {
+    qeg::require(ctx != nullptr, "ctx is NULL");
+    if (bytes == 0) return;
+    qeg::require(dst != nullptr && src != nullptr, "dst/src is NULL");
+    qeg::require(qeg::is_device_ptr(src), "download source is not device memory");
+    QEG_CUDA(cudaSetDevice(ctx->device));
+    QEG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    QEG_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+void qeg_dev_free(void* p) {
+  if (p) cudaFree(p);
+}
+
 qeg_status qeg_ctx_check_bounded_wait(qeg_ctx* ctx, int32_t polls) {
   return qeg::guarded(ctx, [&] {
     qeg::require(ctx != nullptr, "ctx is NULL");

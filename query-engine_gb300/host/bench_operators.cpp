@@ -7,6 +7,10 @@
 //                                         workload: I64 key uniform over 1024
 //                                         values, F64 value U[0,1000) with 5%
 //                                         NULLs; COUNT(*), SUM, AVG, MIN, MAX.
+//   bench_operators agg_resident <rows> <steps>
+//                                         the same GROUP BY over a DeviceTable
+//                                         uploaded once: GpuAggregate over a
+//                                         GpuScan reads the columns in place.
 //   bench_operators join <build> <probe> <steps>
 //                                         inner join of the 16M x 256M workload:
 //                                         build keys a permutation of
@@ -16,6 +20,9 @@
 //                                         probe payload U[0,2^20); the drain
 //                                         counts the output rows and sums the
 //                                         probe payload.
+//   bench_operators join_resident <build> <probe> <steps>
+//                                         the same join with both sides in
+//                                         DeviceTables uploaded once.
 //
 // Prints one JSON object: rows/s over the input rows (build + probe for the
 // join) of the median step, each step's seconds, and a check of the drained
@@ -114,7 +121,21 @@ double median(std::vector<double> t) {
   return t[t.size() / 2];
 }
 
-int run_agg(std::size_t n, int steps) {
+// Uploads a table once (the upload is not part of a step).
+std::shared_ptr<const gpu::DeviceTable> resident(const Table& t, double* seconds) {
+  const double t0 = now();
+  Scan s(t);
+  auto dt = gpu::DeviceTable::upload(s);
+  *seconds = now() - t0;
+  return dt;
+}
+
+std::unique_ptr<Operator> source(const Table& t, const std::shared_ptr<const gpu::DeviceTable>& dt) {
+  if (dt) return std::make_unique<gpu::GpuScan>(dt);
+  return std::make_unique<Scan>(t);
+}
+
+int run_agg(std::size_t n, int steps, bool in_place) {
   Rng r{20260616};
   Table t;
   t.schema.fields = {{"k", Type::I64}, {"v", Type::F64}};
@@ -134,12 +155,14 @@ int run_agg(std::size_t n, int steps) {
     ++cnt[k[i]];
     if (validity::get_bit(t.cols[1].validity.data(), i)) ++cntv[k[i]];
   }
+  double upload_s = 0;
+  const auto dt = in_place ? resident(t, &upload_s) : nullptr;
   std::vector<double> times;
   bool ok = true;
   std::size_t groups = 0, batches = 0;
   for (int s = 0; s < steps + 1; ++s) {
     const double t0 = now();
-    gpu::GpuAggregate agg(std::make_unique<Scan>(t), {0},
+    gpu::GpuAggregate agg(source(t, dt), {0},
                           {AggSpec::count_star("n"), AggSpec::sum(1, "s"), AggSpec::avg(1, "a"),
                            AggSpec::min(1, "lo"), AggSpec::max(1, "hi")});
     agg.open();
@@ -159,16 +182,17 @@ int run_agg(std::size_t n, int steps) {
     ok = ok && groups == 1024;
   }
   const double med = median(times);
-  std::printf("{\"workload\": \"plain_agg_1M_1024keys through GpuAggregate::open/next/close\", \"rows\": %zu, "
+  std::printf("{\"workload\": \"plain_agg_1M_1024keys through GpuAggregate::open/next/close%s\", \"rows\": %zu, "
               "\"value\": %.6g, \"unit\": \"rows/s\", \"groups\": %zu, \"output_batches\": %zu, "
-              "\"check_counts_vs_host\": %s, ",
-              n, n / med, groups, batches, ok ? "true" : "false");
+              "\"check_counts_vs_host\": %s, \"upload_s\": %.4f, ",
+              in_place ? " over a GpuScan of a DeviceTable" : "", n, n / med, groups, batches, ok ? "true" : "false",
+              upload_s);
   print_steps(times);
   std::printf("}\n");
   return ok ? 0 : 1;
 }
 
-int run_join(std::size_t nb, std::size_t np, int steps) {
+int run_join(std::size_t nb, std::size_t np, int steps, bool in_place) {
   Rng r{20260617};
   Table b, p;
   b.schema.fields = {{"bk", Type::I64}, {"bv", Type::I64}};
@@ -205,13 +229,16 @@ int run_join(std::size_t nb, std::size_t np, int steps) {
       ++want_n;
       want_s += pv[i];
     }
+  double up_b = 0, up_p = 0;
+  const auto dtb = in_place ? resident(b, &up_b) : nullptr;
+  const auto dtp = in_place ? resident(p, &up_p) : nullptr;
   std::vector<double> times;
   bool ok = true;
   std::int64_t got_n = 0, got_s = 0;
   std::size_t batches = 0;
   for (int s = 0; s < steps + 1; ++s) {
     const double t0 = now();
-    gpu::GpuHashJoin j(std::make_unique<Scan>(p), std::make_unique<Scan>(b), {0}, {0}, JoinType::Inner);
+    gpu::GpuHashJoin j(source(p, dtp), source(b, dtb), {0}, {0}, JoinType::Inner);
     j.open();
     got_n = got_s = 0;
     batches = 0;
@@ -230,11 +257,12 @@ int run_join(std::size_t nb, std::size_t np, int steps) {
     ok = ok && got_n == want_n && got_s == want_s;
   }
   const double med = median(times);
-  std::printf("{\"workload\": \"join_%zuMx%zuM through GpuHashJoin::open/next/close, output drained on the host\", "
-              "\"build_rows\": %zu, \"probe_rows\": %zu, \"value\": %.6g, \"unit\": \"rows/s\", "
-              "\"output_rows\": %lld, \"output_batches\": %zu, \"check_count_sum_vs_host\": %s, ",
-              nb >> 20, np >> 20, nb, np, (nb + np) / med, static_cast<long long>(got_n), batches,
-              ok ? "true" : "false");
+  std::printf("{\"workload\": \"join_%zuMx%zuM through GpuHashJoin::open/next/close%s, output drained on the "
+              "host\", \"build_rows\": %zu, \"probe_rows\": %zu, \"value\": %.6g, \"unit\": \"rows/s\", "
+              "\"output_rows\": %lld, \"output_batches\": %zu, \"check_count_sum_vs_host\": %s, "
+              "\"upload_s\": %.4f, ",
+              nb >> 20, np >> 20, in_place ? " over GpuScans of DeviceTables" : "", nb, np, (nb + np) / med,
+              static_cast<long long>(got_n), batches, ok ? "true" : "false", up_b + up_p);
   print_steps(times);
   std::printf("}\n");
   return ok ? 0 : 1;
@@ -245,14 +273,18 @@ int run_join(std::size_t nb, std::size_t np, int steps) {
 int main(int argc, char** argv) {
   const std::string w = argc > 1 ? argv[1] : "agg";
   try {
-    if (w == "agg") return run_agg(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : (1u << 20), argc > 3 ? std::atoi(argv[3]) : 5);
-    if (w == "join")
+    if (w == "agg" || w == "agg_resident")
+      return run_agg(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : (1u << 20), argc > 3 ? std::atoi(argv[3]) : 5,
+                     w == "agg_resident");
+    if (w == "join" || w == "join_resident")
       return run_join(argc > 2 ? std::strtoull(argv[2], nullptr, 10) : (1u << 24),
-                      argc > 3 ? std::strtoull(argv[3], nullptr, 10) : (1ull << 28), argc > 4 ? std::atoi(argv[4]) : 3);
+                      argc > 3 ? std::strtoull(argv[3], nullptr, 10) : (1ull << 28), argc > 4 ? std::atoi(argv[4]) : 3,
+                      w == "join_resident");
   } catch (const std::exception& e) {
     std::printf("{\"error\": \"%s\"}\n", e.what());
     return 2;
   }
-  std::fprintf(stderr, "usage: bench_operators agg <rows> <steps> | join <build> <probe> <steps>\n");
+  std::fprintf(stderr,
+               "usage: bench_operators agg|agg_resident <rows> <steps> | join|join_resident <build> <probe> <steps>\n");
   return 2;
 }

@@ -206,6 +206,126 @@ void Device::check(qeg_status s) const {
 }
 
 // ---------------------------------------------------------------------------
+// DeviceTable / GpuScan
+// ---------------------------------------------------------------------------
+std::shared_ptr<const DeviceTable> DeviceTable::upload(Operator& src, int device) {
+  std::shared_ptr<DeviceTable> t(new DeviceTable());
+  t->schema_ = src.output_schema();
+  t->dev_ = std::make_unique<Device>(device);
+  const std::size_t nc = t->schema_.fields.size();
+  std::vector<Type> types;
+  for (const auto& f : t->schema_.fields) types.push_back(f.second);
+  t->dicts_.assign(nc, nullptr);
+  std::vector<StringDict*> ids(nc, nullptr);
+  for (std::size_t c = 0; c < nc; ++c)
+    if (types[c] == Type::STR) {
+      t->dicts_[c] = std::make_shared<StringDict>();
+      ids[c] = t->dicts_[c].get();
+    }
+  // The source's rows into page-locked staging (selections applied, STR codes
+  // made the table dictionary's), then one copy per column.
+  Staging st;
+  st.reset(types);
+  src.open();
+  while (std::optional<Batch> b = src.next()) st.append(*b, ids);
+  src.close();
+  t->rows_ = st.rows;
+  t->data_.assign(nc, nullptr);
+  t->valid_.assign(nc, nullptr);
+  for (std::size_t c = 0; c < nc; ++c) {
+    const std::size_t bytes = st.rows * byte_width(types[c]);
+    t->dev_->check(qeg_dev_alloc(t->dev_->ctx(), bytes, &t->data_[c]));
+    t->dev_->check(qeg_dev_upload(t->dev_->ctx(), t->data_[c], st.vals[c].data(), bytes));
+    if (!st.any_null[c]) continue;
+    const std::size_t wbytes = validity::words(st.rows) * 8;
+    void* w = nullptr;
+    t->dev_->check(qeg_dev_alloc(t->dev_->ctx(), wbytes, &w));
+    t->valid_[c] = static_cast<std::uint64_t*>(w);
+    t->dev_->check(qeg_dev_upload(t->dev_->ctx(), w, st.valid[c].data(), wbytes));
+  }
+  return t;
+}
+
+DeviceTable::~DeviceTable() {
+  for (void* p : data_) qeg_dev_free(p);
+  for (std::uint64_t* p : valid_) qeg_dev_free(p);
+}
+
+std::vector<qeg_column> DeviceTable::columns(std::size_t first, std::size_t n,
+                                             const std::vector<std::vector<std::int32_t>>& code_maps) const {
+  if (first % 64 != 0 || first + n > rows_) throw std::invalid_argument("DeviceTable: slice out of range");
+  std::vector<qeg_column> out(schema_.fields.size());
+  for (std::size_t c = 0; c < out.size(); ++c) {
+    const Type t = schema_.fields[c].second;
+    qeg_column q{};
+    q.type = to_qeg(t);
+    q.len = n;
+    q.data = n ? static_cast<const std::uint8_t*>(data_[c]) + first * byte_width(t) : nullptr;
+    q.all_valid = valid_[c] ? 0 : 1;
+    q.validity = valid_[c] && n ? valid_[c] + first / 64 : nullptr;
+    if (t == Type::STR && c < code_maps.size() && !code_maps[c].empty()) {
+      q.code_map = code_maps[c].data();
+      q.code_map_len = code_maps[c].size();
+    }
+    out[c] = q;
+  }
+  return out;
+}
+
+void DeviceTable::download(std::size_t c, std::size_t first, std::size_t n, void* vals,
+                           std::uint64_t* words) const {
+  if (first % 64 != 0 || first + n > rows_) throw std::invalid_argument("DeviceTable: slice out of range");
+  if (n == 0) return;
+  const std::size_t w = byte_width(schema_.fields[c].second);
+  dev_->check(qeg_dev_download(dev_->ctx(), vals, static_cast<const std::uint8_t*>(data_[c]) + first * w, n * w));
+  if (valid_[c])
+    dev_->check(qeg_dev_download(dev_->ctx(), words, valid_[c] + first / 64, validity::words(n) * 8));
+}
+
+GpuScan::GpuScan(std::shared_ptr<const DeviceTable> table, std::size_t batch_size)
+    : table_(std::move(table)), batch_size_(batch_size) {
+  if (!table_) throw std::invalid_argument("GpuScan: table is NULL");
+  if (batch_size_ == 0 || batch_size_ % 64 != 0)  // ops/scan.cpp:11-19
+    throw std::invalid_argument("Scan batch_size must be a positive multiple of 64 (validity word alignment)");
+}
+
+void GpuScan::open() {
+  cursor_ = 0;
+  win_first_ = win_rows_ = 0;
+}
+
+void GpuScan::close() { cursor_ = table_->num_rows(); }
+
+Schema GpuScan::output_schema() const { return table_->schema(); }
+
+std::optional<Batch> GpuScan::next() {
+  const std::size_t total = table_->num_rows();
+  if (cursor_ >= total) return std::nullopt;
+  if (cursor_ < win_first_ || cursor_ >= win_first_ + win_rows_) {
+    // The next kFetchRows rows (a multiple of batch_size) into page-locked memory.
+    const std::size_t span = std::max(batch_size_, kFetchRows - kFetchRows % batch_size_);
+    win_first_ = cursor_;
+    win_rows_ = std::min(span, total - cursor_);
+    std::vector<Type> types;
+    for (const auto& f : table_->schema().fields) types.push_back(f.second);
+    out_.reserve(types, win_rows_);
+    for (std::size_t c = 0; c < types.size(); ++c) {
+      table_->download(c, win_first_, win_rows_, out_.vals[c].data(),
+                       reinterpret_cast<std::uint64_t*>(out_.valid[c].data()));
+      out_.all_valid[c] = table_->all_valid(c) ? 1 : 0;
+      out_.dicts[c] = table_->dict(c);
+    }
+  }
+  const std::size_t n = std::min(batch_size_, total - cursor_);
+  Batch b;
+  for (std::size_t c = 0; c < out_.types.size(); ++c) b.cols.push_back(out_.view(c, cursor_ - win_first_, n));
+  b.sel = nullptr;
+  b.row_count = n;
+  cursor_ += n;
+  return b;
+}
+
+// ---------------------------------------------------------------------------
 // GpuAggregate
 // ---------------------------------------------------------------------------
 GpuAggregate::GpuAggregate(std::unique_ptr<Operator> child, std::vector<std::uint32_t> key_cols,
@@ -268,11 +388,16 @@ void GpuAggregate::open() {
   if (opened_) return;
   opened_ = true;
   dev_ = std::make_unique<Device>(device_);
+  // A GpuScan child: its device columns are consumed where they lie, STR
+  // columns as codes with a code map; otherwise rows are staged on the host
+  // and STR columns arrive as canonical ids.
+  const auto* scan = dynamic_cast<const GpuScan*>(child_.get());
+  const DeviceTable* table = scan ? scan->table().get() : nullptr;
   std::vector<Type> types;
   std::vector<int32_t> qtypes;
   for (const auto& f : child_schema_.fields) {
     types.push_back(f.second);
-    qtypes.push_back(f.second == Type::STR ? QEG_I32 : to_qeg(f.second));
+    qtypes.push_back(f.second == Type::STR && !table ? QEG_I32 : to_qeg(f.second));
     if (f.second == Type::STR) has_str_ = true;
   }
   std::vector<qeg_agg_spec> specs;
@@ -298,16 +423,38 @@ void GpuAggregate::open() {
       ids[c] = str_ids_[c].get();
     }
 
-  // STR ids must be order-preserving for MIN/MAX by value: with STR columns
-  // the whole input is staged first and the ids re-ranked in string order.
-  child_->open();
-  while (std::optional<Batch> b = child_->next()) {
-    staging_.append(*b, ids);
-    if (!has_str_ && staging_.rows >= kChunkRows) flush();
-  }
-  child_->close();
+  // STR ids must be order-preserving for MIN/MAX by value: a STR value goes
+  // to the GPU as its rank in string order, and rank_to_id[c] maps it back.
   std::vector<std::vector<int32_t>> rank_to_id(types.size());
-  if (has_str_) {
+  if (table) {
+    std::vector<std::vector<int32_t>> ranks(types.size());
+    for (std::size_t c = 0; c < types.size(); ++c) {
+      if (types[c] != Type::STR) continue;
+      str_ids_[c] = table->dict(c);
+      const StringDict& d = *str_ids_[c];
+      std::vector<int32_t> order(d.size());
+      for (std::size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int32_t>(i);
+      std::sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return d.at(a) < d.at(b); });
+      ranks[c].resize(d.size());
+      for (std::size_t r = 0; r < order.size(); ++r) ranks[c][order[r]] = static_cast<int32_t>(r);
+      rank_to_id[c] = std::move(order);
+    }
+    child_->open();
+    const std::size_t rows = table->num_rows();
+    for (std::size_t first = 0; first < rows; first += kDeviceSliceRows) {
+      const auto cols = table->columns(first, std::min(kDeviceSliceRows, rows - first), ranks);
+      dev_->check(qeg_agg_consume(agg_, cols.data(), static_cast<int>(cols.size()), nullptr, 0));
+    }
+    child_->close();
+  } else {
+    child_->open();
+    while (std::optional<Batch> b = child_->next()) {
+      staging_.append(*b, ids);
+      if (!has_str_ && staging_.rows >= kChunkRows) flush();
+    }
+    child_->close();
+  }
+  if (has_str_ && !table) {
     for (std::size_t c = 0; c < types.size(); ++c) {
       if (!str_ids_[c]) continue;
       const StringDict& d = *str_ids_[c];
@@ -433,15 +580,29 @@ void GpuHashJoin::open() {
   probe_done_ = false;
   pending_ = cursor_ = 0;
   dev_ = std::make_unique<Device>(device_);
+  // A GpuScan child is read in place, its STR columns as codes with a code map
+  // into the join's value ids. Key columns pair up by type, so a STR key read
+  // in place needs the other side's in place too; otherwise that GpuScan runs
+  // as an ordinary child through host staging.
+  auto in_place = [](const std::unique_ptr<Operator>& op) -> const DeviceTable* {
+    const auto* scan = dynamic_cast<const GpuScan*>(op.get());
+    return scan ? scan->table().get() : nullptr;
+  };
+  const DeviceTable* build_table = in_place(build_);
+  probe_table_ = in_place(probe_);
+  probe_row_ = 0;
+  if ((build_table == nullptr) != (probe_table_ == nullptr))
+    for (std::size_t i = 0; i < build_keys_.size(); ++i)
+      if (build_schema_.fields[build_keys_[i]].second == Type::STR) build_table = probe_table_ = nullptr;
   std::vector<Type> ptypes, btypes;
   std::vector<int32_t> qp, qb;
   for (const auto& f : probe_schema_.fields) {
     ptypes.push_back(f.second);
-    qp.push_back(f.second == Type::STR ? QEG_I32 : to_qeg(f.second));
+    qp.push_back(f.second == Type::STR && !probe_table_ ? QEG_I32 : to_qeg(f.second));
   }
   for (const auto& f : build_schema_.fields) {
     btypes.push_back(f.second);
-    qb.push_back(f.second == Type::STR ? QEG_I32 : to_qeg(f.second));
+    qb.push_back(f.second == Type::STR && !build_table ? QEG_I32 : to_qeg(f.second));
   }
   if (asof_)
     dev_->check(qeg_asof_create(dev_->ctx(), qp.data(), static_cast<int>(qp.size()), qb.data(),
@@ -468,25 +629,47 @@ void GpuHashJoin::open() {
     if (btypes[c] == Type::STR && !build_ids_[c]) build_ids_[c] = std::make_shared<StringDict>();
   for (std::size_t c = 0; c < ptypes.size(); ++c)
     if (ptypes[c] == Type::STR && !probe_ids_[c]) probe_ids_[c] = std::make_shared<StringDict>();
-  std::vector<StringDict*> bids(btypes.size(), nullptr);
-  for (std::size_t c = 0; c < btypes.size(); ++c) bids[c] = build_ids_[c].get();
-  Staging bs;
-  bs.reset(btypes);
+  // Code maps of an in-place table: each code of its dictionary -> value id.
+  auto value_ids = [](const DeviceTable& t, const std::vector<std::shared_ptr<StringDict>>& ids) {
+    std::vector<std::vector<int32_t>> maps(ids.size());
+    for (std::size_t c = 0; c < ids.size(); ++c) {
+      if (!ids[c]) continue;
+      const StringDict& d = *t.dict(c);
+      for (std::size_t code = 0; code < d.size(); ++code)
+        maps[c].push_back(ids[c]->intern(d.at(static_cast<int32_t>(code))));
+    }
+    return maps;
+  };
   build_->open();
-  while (std::optional<Batch> b = build_->next()) {
-    bs.append(*b, bids);
-    if (bs.rows >= (8u << 20)) {
+  if (build_table) {
+    const auto maps = value_ids(*build_table, build_ids_);
+    const std::size_t rows = build_table->num_rows();
+    for (std::size_t first = 0; first < rows; first += kBuildSliceRows) {
+      const auto cols = build_table->columns(first, std::min(kBuildSliceRows, rows - first), maps);
+      dev_->check(qeg_join_build(join_, cols.data(), static_cast<int>(cols.size())));
+    }
+  } else {
+    std::vector<StringDict*> bids(btypes.size(), nullptr);
+    for (std::size_t c = 0; c < btypes.size(); ++c) bids[c] = build_ids_[c].get();
+    Staging bs;
+    bs.reset(btypes);
+    while (std::optional<Batch> b = build_->next()) {
+      bs.append(*b, bids);
+      if (bs.rows >= (8u << 20)) {
+        const auto cols = bs.columns();
+        dev_->check(qeg_join_build(join_, cols.data(), static_cast<int>(cols.size())));
+        bs.reset(btypes);
+      }
+    }
+    if (bs.rows) {
       const auto cols = bs.columns();
       dev_->check(qeg_join_build(join_, cols.data(), static_cast<int>(cols.size())));
-      bs.reset(btypes);
     }
   }
   build_->close();
-  if (bs.rows) {
-    const auto cols = bs.columns();
-    dev_->check(qeg_join_build(join_, cols.data(), static_cast<int>(cols.size())));
-  }
   dev_->check(qeg_join_build_finish(join_));
+  probe_maps_.clear();
+  if (probe_table_) probe_maps_ = value_ids(*probe_table_, probe_ids_);
   probe_stage_.reset(ptypes);
   probe_->open();
   const Schema out = output_schema();
@@ -502,6 +685,18 @@ void GpuHashJoin::open() {
 // Stages up to kProbeRows probe rows (whole batches) and probes them in one
 // call. False when the probe child is exhausted.
 bool GpuHashJoin::probe_next_chunk() {
+  if (probe_table_) {  // the next kProbeRows rows of the in-place table
+    const std::size_t rows = probe_table_->num_rows();
+    if (probe_row_ >= rows) return false;
+    const std::size_t n = std::min(kProbeRows, rows - probe_row_);
+    const auto cols = probe_table_->columns(probe_row_, n, probe_maps_);
+    probe_row_ += n;
+    uint64_t out = 0;
+    dev_->check(qeg_join_probe(join_, cols.data(), static_cast<int>(cols.size()), &out));
+    pending_ = out;
+    fetched_ = chunk_ = cursor_ = 0;
+    return true;
+  }
   std::vector<StringDict*> pids(probe_stage_.types.size(), nullptr);
   for (std::size_t c = 0; c < pids.size(); ++c) pids[c] = probe_ids_[c].get();
   probe_stage_.reset(probe_stage_.types);

@@ -23,6 +23,11 @@
 //   GpuAsofJoin   qe::tsx::AsofJoin (tsx/asof.h:94-150): a GpuHashJoin whose
 //                 build side is sorted by (key, time) on the GPU and whose
 //                 probe takes the nearest preceding build row per probe row.
+//   DeviceTable / GpuScan
+//                 qe::Table (ops/table.h:24-47) uploaded once and qe::Scan
+//                 (ops/scan.h:13-29) over it. A GpuAggregate or GpuHashJoin
+//                 whose child is a GpuScan reads the table's device columns
+//                 in place: no host staging, no copy per query.
 // A returned Batch's views stay valid until the next next() or close(), as
 // ops/operator.h:14-22 requires.
 // Errors surface as the reference's exception types: std::invalid_argument,
@@ -132,10 +137,74 @@ class Device {
   qeg_ctx* ctx_ = nullptr;
 };
 
+// A table resident in device memory: the reference's in-memory Table
+// (ops/table.h:24-47) uploaded once, then read in place by every GpuScan over
+// it. Each STR column holds codes of one table-owned dictionary (equal
+// strings, equal codes); a validity bitmap is kept only for a column that
+// holds a NULL.
+class DeviceTable {
+ public:
+  // Drains `src` (open, next until exhausted, close) into device memory.
+  static std::shared_ptr<const DeviceTable> upload(Operator& src, int device = 0);
+  ~DeviceTable();
+  DeviceTable(const DeviceTable&) = delete;
+  DeviceTable& operator=(const DeviceTable&) = delete;
+
+  const Schema& schema() const { return schema_; }
+  std::size_t num_rows() const { return rows_; }
+  const std::shared_ptr<StringDict>& dict(std::size_t c) const { return dicts_[c]; }
+  bool all_valid(std::size_t c) const { return valid_[c] == nullptr; }
+  // Rows [first, first + n) of every column as device-pointer views (`first`
+  // a multiple of 64). A STR column is QEG_STR with code_maps[c] (host memory,
+  // one entry per code of its dictionary) as its code map.
+  std::vector<qeg_column> columns(std::size_t first, std::size_t n,
+                                  const std::vector<std::vector<std::int32_t>>& code_maps) const;
+  // Copies rows [first, first + n) of column c (`first` a multiple of 64) to
+  // host memory: the values to `vals`, and the validity words to `words` when
+  // the column holds a NULL.
+  void download(std::size_t c, std::size_t first, std::size_t n, void* vals, std::uint64_t* words) const;
+
+ private:
+  DeviceTable() = default;
+  Schema schema_;
+  std::size_t rows_ = 0;
+  std::unique_ptr<Device> dev_;
+  std::vector<void*> data_;
+  std::vector<std::uint64_t*> valid_;
+  std::vector<std::shared_ptr<StringDict>> dicts_;
+};
+
+// qe::Scan (ops/scan.h:13-29) over a DeviceTable, with its batch_size check
+// and cursor rules. Under an ordinary parent it emits batch_size-row batches
+// copied back to page-locked host memory, kFetchRows rows per copy; as the
+// child of a GpuAggregate or GpuHashJoin it hands its table to the GPU where
+// it lies, with no host staging.
+class GpuScan : public Operator {
+ public:
+  static constexpr std::size_t kDefaultBatchSize = 2048;  // ops/scan.h:15
+  static constexpr std::size_t kFetchRows = 1u << 20;
+
+  explicit GpuScan(std::shared_ptr<const DeviceTable> table, std::size_t batch_size = kDefaultBatchSize);
+
+  void open() override;
+  std::optional<Batch> next() override;
+  void close() override;
+  Schema output_schema() const override;
+  const std::shared_ptr<const DeviceTable>& table() const { return table_; }
+
+ private:
+  std::shared_ptr<const DeviceTable> table_;
+  std::size_t batch_size_;
+  std::size_t cursor_ = 0;                      // next row to emit
+  std::size_t win_first_ = 0, win_rows_ = 0;    // rows held in out_
+  OutColumns out_;
+};
+
 class GpuAggregate : public Operator {
  public:
   static constexpr std::size_t kOutBatch = 2048;       // ops/aggregate.h:105
   static constexpr std::size_t kChunkRows = 8u << 20;  // rows staged per GPU call
+  static constexpr std::size_t kDeviceSliceRows = 1u << 30;  // GpuScan-child rows per GPU call
 
   GpuAggregate(std::unique_ptr<Operator> child, std::vector<std::uint32_t> key_cols, std::vector<AggSpec> aggs,
                qeg_agg_config cfg = {}, int device = 0);
@@ -180,6 +249,7 @@ class GpuHashJoin : public Operator {
   static constexpr std::size_t kOutBatch = 2048;        // ops/join.h:73
   static constexpr std::size_t kProbeRows = 8u << 20;   // probe rows staged per GPU probe call
   static constexpr std::size_t kFetchRows = 1u << 20;   // output rows fetched per GPU call
+  static constexpr std::size_t kBuildSliceRows = 1u << 30;  // GpuScan build rows per GPU call
 
   GpuHashJoin(std::unique_ptr<Operator> probe, std::unique_ptr<Operator> build, std::vector<std::uint32_t> probe_keys,
               std::vector<std::uint32_t> build_keys, JoinType type, qeg_join_config cfg = {}, int device = 0);
@@ -201,6 +271,11 @@ class GpuHashJoin : public Operator {
   bool probe_next_chunk();
 
   bool asof_ = false;
+  // A GpuScan probe child read in place: its table, the next row to probe and
+  // the STR code maps into the join's value ids.
+  const DeviceTable* probe_table_ = nullptr;
+  std::size_t probe_row_ = 0;
+  std::vector<std::vector<std::int32_t>> probe_maps_;
   std::uint32_t probe_time_ = 0, build_time_ = 0;
   std::optional<std::int64_t> tolerance_;
 

@@ -3,6 +3,7 @@
 // tree would, and checks the drained results against values computed here on
 // the CPU and against expectations written in the reference's own tests.
 // Exit code 0 = all checks passed.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -459,6 +460,149 @@ void test_asof_join() {
   CHECK(threw);
 }
 
+// A deterministic multi-batch source: dictionaries that differ per batch, a
+// selection vector, NULLs in every column type.
+std::unique_ptr<BatchSource> mixed_source(std::size_t batches, std::size_t rows_per_batch) {
+  auto src = std::make_unique<BatchSource>();
+  src->schema.fields = {{"sym", Type::STR}, {"k", Type::I64}, {"v", Type::F64}, {"q", Type::I32}};
+  std::mt19937_64 rng(7);
+  const std::vector<std::string> names = {"AAPL", "MSFT", "GOOG", "IBM", "ORCL", "NVDA", "AMD", "INTC"};
+  for (std::size_t b = 0; b < batches; ++b) {
+    std::vector<std::string> dict(names.begin() + static_cast<long>(b % 3), names.end());
+    std::vector<int32_t> codes(rows_per_batch), q(rows_per_batch);
+    std::vector<int64_t> k(rows_per_batch);
+    std::vector<double> v(rows_per_batch);
+    std::vector<std::size_t> nk, nv, ns;
+    for (std::size_t i = 0; i < rows_per_batch; ++i) {
+      codes[i] = static_cast<int32_t>(rng() % dict.size());
+      k[i] = static_cast<int64_t>(rng() % 3000) - 1000;
+      v[i] = static_cast<double>(rng() % 100000) / 8.0;
+      q[i] = static_cast<int32_t>(rng() % 1000);
+      if (rng() % 31 == 0) nk.push_back(i);
+      if (rng() % 17 == 0) nv.push_back(i);
+      if (rng() % 23 == 0) ns.push_back(i);
+    }
+    gpu::HostColumn sc = str_col(dict, codes);
+    if (!ns.empty()) {
+      sc.validity.assign(validity::words(rows_per_batch), ~0ull);
+      for (auto i : ns) validity::set_bit(sc.validity.data(), i, false);
+    }
+    src->batches.push_back({sc, make_col(Type::I64, k, nk), make_col(Type::F64, v, nv), make_col(Type::I32, q)});
+    std::vector<uint32_t> sel;
+    if (b % 2 == 1)
+      for (uint32_t i = 0; i < rows_per_batch; ++i)
+        if (i % 5 != 2) sel.push_back(i);
+    src->sels.push_back(sel);
+  }
+  return src;
+}
+
+std::vector<Row> sorted(std::vector<Row> r) {
+  std::sort(r.begin(), r.end());
+  return r;
+}
+
+// Equal row multisets; F64 cells within a relative 1e-12 (summation order).
+bool same_rows(std::vector<Row> a, std::vector<Row> b) {
+  a = sorted(std::move(a));
+  b = sorted(std::move(b));
+  if (a.size() != b.size()) return false;
+  for (std::size_t i = 0; i < a.size(); ++i) {
+    if (a[i].size() != b[i].size()) return false;
+    for (std::size_t c = 0; c < a[i].size(); ++c) {
+      const Cell &x = a[i][c], &y = b[i][c];
+      if (x.null != y.null || x.i != y.i || x.s != y.s) return false;
+      if (std::fabs(x.f - y.f) > 1e-12 * std::max(1.0, std::fabs(y.f))) return false;
+    }
+  }
+  return true;
+}
+
+void test_device_table_scan() {
+  // 90 batches of 2000 rows (odd batches filtered by a selection vector):
+  // 162000 logical rows, not a multiple of 64.
+  auto up_src = mixed_source(90, 2000);
+  auto table = gpu::DeviceTable::upload(*up_src);
+  CHECK(table->num_rows() == 162000);
+  CHECK(table->schema().fields.size() == 4);
+  // Scanned back through host memory: the source's rows in the source's order.
+  {
+    auto host = mixed_source(90, 2000);
+    const auto want = drain(*host);
+    for (std::size_t batch : {std::size_t{2048}, std::size_t{192}}) {
+      gpu::GpuScan scan(table, batch);
+      const auto got = drain(scan);
+      CHECK(got.size() == want.size());
+      bool eq = got.size() == want.size();
+      for (std::size_t i = 0; eq && i < got.size(); ++i)
+        for (std::size_t c = 0; eq && c < got[i].size(); ++c)
+          eq = !(got[i][c] < want[i][c]) && !(want[i][c] < got[i][c]);
+      CHECK(eq);
+    }
+  }
+  bool threw = false;
+  try {
+    gpu::GpuScan bad(table, 100);
+  } catch (const std::invalid_argument&) {
+    threw = true;
+  }
+  CHECK(threw);  // ops/scan.cpp:14-18
+  // GROUP BY read in place == GROUP BY through host staging.
+  const std::vector<AggSpec> by_sym = {AggSpec::count_star("n"), AggSpec::sum(1, "s"), AggSpec::avg(2, "a"),
+                                       AggSpec::min(0, "mn"), AggSpec::max(0, "mx"), AggSpec::count(1, "c")};
+  {
+    gpu::GpuAggregate dev(std::make_unique<gpu::GpuScan>(table), {0}, by_sym);
+    gpu::GpuAggregate host(mixed_source(90, 2000), {0}, by_sym);
+    const auto a = drain(dev), b = drain(host);
+    CHECK(a.size() == 9);  // 8 symbols and NULL
+    CHECK(same_rows(a, b));
+  }
+  {
+    const std::vector<AggSpec> by_k = {AggSpec::count_star("n"), AggSpec::sum(3, "q"), AggSpec::max(2, "m")};
+    gpu::GpuAggregate dev(std::make_unique<gpu::GpuScan>(table), {1, 3}, by_k);
+    gpu::GpuAggregate host(mixed_source(90, 2000), {1, 3}, by_k);
+    CHECK(same_rows(drain(dev), drain(host)));
+  }
+  // Joins: both sides in place (STR key), in-place probe with a host build
+  // (I64 key), and a STR key with only one side in place (staged).
+  auto dims = std::make_unique<BatchSource>();
+  dims->schema.fields = {{"sym", Type::STR}, {"sector", Type::I32}, {"k", Type::I64}};
+  dims->batches.push_back({str_col({"IBM", "AAPL", "NVDA", "XOM"}, {0, 1, 2, 3, 1}),
+                           make_col<int32_t>(Type::I32, {1, 2, 3, 4, 5}),
+                           make_col<int64_t>(Type::I64, {-1000, 5, 17, 1999, 5})});
+  dims->sels.push_back({});
+  auto dims_table = gpu::DeviceTable::upload(*dims);
+  auto host_dims = [&]() {
+    auto d = std::make_unique<BatchSource>();
+    d->schema = dims->schema;
+    d->batches = dims->batches;
+    d->sels = dims->sels;
+    return d;
+  };
+  for (JoinType jt : {JoinType::Inner, JoinType::Left}) {
+    gpu::GpuHashJoin dev(std::make_unique<gpu::GpuScan>(table), std::make_unique<gpu::GpuScan>(dims_table), {0}, {0},
+                         jt);
+    gpu::GpuHashJoin host(mixed_source(90, 2000), host_dims(), {0}, {0}, jt);
+    const auto a = drain(dev), b = drain(host);
+    CHECK(!a.empty());
+    CHECK(same_rows(a, b));
+    gpu::GpuHashJoin dev_k(std::make_unique<gpu::GpuScan>(table), host_dims(), {1}, {2}, jt);
+    gpu::GpuHashJoin host_k(mixed_source(90, 2000), host_dims(), {1}, {2}, jt);
+    CHECK(same_rows(drain(dev_k), drain(host_k)));
+    gpu::GpuHashJoin mixed(std::make_unique<gpu::GpuScan>(table), host_dims(), {0}, {0}, jt);
+    CHECK(same_rows(drain(mixed), b));
+  }
+  // An empty table: no batches, and a global aggregate of zero rows.
+  auto none = mixed_source(0, 0);
+  auto empty = gpu::DeviceTable::upload(*none);
+  CHECK(empty->num_rows() == 0);
+  gpu::GpuScan es(empty);
+  CHECK(drain(es).empty());
+  gpu::GpuAggregate g(std::make_unique<gpu::GpuScan>(empty), {}, {AggSpec::count_star("n"), AggSpec::sum(1, "s")});
+  const auto rows = drain(g);
+  CHECK(rows.size() == 1 && rows[0][0].i == 0 && rows[0][1].null);
+}
+
 int main() {
   try {
     test_aggregate_edge_table();
@@ -469,6 +613,7 @@ int main() {
     test_join_str_keys();
     test_window_tumbling();
     test_asof_join();
+    test_device_table_scan();
   } catch (const std::exception& e) {
     std::fprintf(stderr, "exception: %s\n", e.what());
     return 2;
