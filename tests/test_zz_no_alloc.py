@@ -109,6 +109,41 @@ def test_noalloc_sum_is_null_when_every_matched_payload_is_null():
     assert _noalloc(torch, bk, pk, pv) == exp
 
 
+def test_noalloc_call_captured_in_a_cuda_graph():
+    """The call enqueues only a memset and kernels, so a caller can capture it
+    in a CUDA graph (after one plain call on the device, which looks up the
+    scratch array's address) and replay it; each replay re-reads the columns."""
+    torch = pytest.importorskip("torch")
+    host = _case(5, 1 << 16, 1 << 20, dup=True, payload_nulls=0.1)
+    exp = _oracle(*host)
+    bk, pk, pv = _device_cols(torch, *host)
+    assert _noalloc(torch, bk, pk, pv) == exp  # the plain call before capture
+    s = torch.cuda.Stream()
+    out = torch.full((4,), -7, dtype=torch.int64, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(g, stream=s):
+        qeg.join_count_sum_noalloc(s.cuda_stream, bk, pk, pv, out)
+
+    def replay():
+        out.fill_(-7)
+        g.replay()
+        torch.cuda.synchronize()
+        got = out.cpu().tolist()
+        assert got[3] == 0
+        return got[0], (got[1] if got[2] else None)
+
+    assert replay() == exp
+    assert replay() == exp
+    # New payload values in the same buffer: the replay sums them.
+    pval2 = (host[4] * 3 + 1).astype(np.int64)
+    pv.values.copy_(torch.from_numpy(pval2))
+    torch.cuda.synchronize()
+    exp2 = _oracle(host[0], host[1], host[2], host[3], pval2, host[5])
+    assert exp2 != exp
+    assert replay() == exp2
+
+
 def _str_col(torch, codes, cmap, cm_len):
     """A raw STR column (codes + code map on the device) whose code_map_len
     is given explicitly; returns it with the tensors that back it."""
