@@ -1696,9 +1696,7 @@ void AggState::launch_private(const AggK& P, uint64_t nrows) {
   else kern = agg2_private_kernel<8, kGenericSpec>;
   const int block = 512;
   const size_t sb = static_cast<size_t>(smem_slots) * (row_words | 1) * 8;
-  if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-  int per_sm = 1;
-  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
+  const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), block, sb);
   require(per_sm > 0, "aggregate kernel does not fit on an SM with this configuration");
   // Each CTA walks one contiguous range; a few thousand rows at least.
   uint64_t grid = std::min<uint64_t>((nrows + 4095) / 4096, static_cast<uint64_t>(ctx->sms) * per_sm);
@@ -2141,9 +2139,7 @@ void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_
   {
     const size_t sb = hot_bytes + np * 4;
     constexpr int kHistRows = 8;
-    QEG_CUDA(cudaFuncSetAttribute(part_hist_kernel<kHistRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-    int per_sm = 0;
-    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, part_hist_kernel<kHistRows>, 1024, sb));
+    const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(part_hist_kernel<kHistRows>), 1024, sb);
     require(per_sm > 0, "partition sizing kernel does not fit on an SM");
     const uint64_t grid = std::max<uint64_t>(
         1, std::min<uint64_t>((nrows + 65535) / 65536, static_cast<uint64_t>(ctx->sms) * per_sm));
@@ -2186,9 +2182,7 @@ void AggState::consume_partitioned(const std::vector<StagedCol>& staged, uint64_
     else if (nv <= 4) kern = part_pass1_kernel<4, kGenericSpec, part_rows<4>()>;
     else kern = part_pass1_kernel<8, kGenericSpec, part_rows<8>()>;
     const size_t sb = hot_bytes + static_cast<size_t>(nhot + 2) * A.rw * 8;
-    QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-    int per_sm = 0;
-    QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 512, sb));
+    const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), 512, sb);
     require(per_sm > 0, "partitioned first pass does not fit on an SM");
     const uint64_t grid = std::max<uint64_t>(
         1, std::min<uint64_t>((nrows + 8191) / 8192, static_cast<uint64_t>(ctx->sms) * per_sm));
@@ -2242,9 +2236,7 @@ void AggState::part_second_pass() {
   else kern = part_agg_kernel<8, kGenericSpec, part_rows<8>()>;
   const int block = 1024;
   const size_t sb = static_cast<size_t>(pb_slots) * (row_words | 1) * 8;
-  if (sb > 48 * 1024) QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-  int per_sm = 0;
-  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
+  const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), block, sb);
   require(per_sm > 0, "partitioned aggregate kernel does not fit on an SM");
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(np, static_cast<uint64_t>(ctx->sms) * per_sm));
   if (!part_counters.get()) part_counters.alloc(16, ctx->stream);

@@ -645,7 +645,7 @@ qeg_status qeg_batch_create(qeg_ctx* ctx, uint32_t nqueries, const uint64_t* row
     }
     const size_t sb = S.smem_bytes(kBatchMaxSlots);
     require(sb <= ctx->smem_optin, "batch rows are too wide for the shared-memory tables");
-    QEG_CUDA(cudaFuncSetAttribute(S.agg_kernel_for(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+    raise_dynamic_smem(reinterpret_cast<const void*>(S.agg_kernel_for()), sb);
     S.rounds.resize(1);
     S.setup_round(S.rounds[0], all, caps);
     QEG_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -113,43 +113,57 @@ void read_words_and_error(qeg_ctx* ctx, const void* dev_words, size_t nwords, ui
   raise_device_error(ctx, e);
 }
 
+namespace {
+// The shared-memory attribute belongs to the function (for every thread of the
+// process), so it is only ever raised: the largest size set so far is kept
+// per (device, kernel), and a request for more raises it. A launch of `smem`
+// bytes after its own request therefore always fits, whatever other threads
+// request meanwhile. The occupancy answers are cached per (device, kernel,
+// block, shared bytes).
+struct SmemAttr {
+  const void* kern;
+  int dev;
+  size_t smem;
+};
+struct SmemOcc {
+  const void* kern;
+  int dev, block;
+  size_t smem;
+  int per_sm;
+};
+std::mutex g_smem_mu;
+std::vector<SmemAttr> g_smem_attrs;
+std::vector<SmemOcc> g_smem_occs;
+
+void raise_locked(const void* kern, int dev, size_t smem) {
+  if (smem <= 48 * 1024) return;
+  SmemAttr* a = nullptr;
+  for (SmemAttr& x : g_smem_attrs)
+    if (x.kern == kern && x.dev == dev) a = &x;
+  if (a && a->smem >= smem) return;
+  QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  if (a) a->smem = smem;
+  else g_smem_attrs.push_back(SmemAttr{kern, dev, smem});
+}
+}  // namespace
+
+void raise_dynamic_smem(const void* kern, size_t smem) {
+  int dev = 0;
+  QEG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_smem_mu);
+  raise_locked(kern, dev, smem);
+}
+
 int blocks_per_sm(const void* kern, int block, size_t smem) {
   int dev = 0;
   QEG_CUDA(cudaGetDevice(&dev));
-  // The shared-memory attribute belongs to the function (for every thread of
-  // the process), so it is only ever raised: the largest size set so far is
-  // kept per (device, kernel), and a launch asking for more raises it. The
-  // occupancy answers are cached per (device, kernel, block, shared bytes).
-  struct Attr {
-    const void* kern;
-    int dev;
-    size_t smem;
-  };
-  struct Occ {
-    const void* kern;
-    int dev, block;
-    size_t smem;
-    int per_sm;
-  };
-  static std::mutex mu;
-  static std::vector<Attr> attrs;
-  static std::vector<Occ> occs;
-  std::lock_guard<std::mutex> lock(mu);
-  if (smem > 48 * 1024) {
-    Attr* a = nullptr;
-    for (Attr& x : attrs)
-      if (x.kern == kern && x.dev == dev) a = &x;
-    if (!a || a->smem < smem) {
-      QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-      if (a) a->smem = smem;
-      else attrs.push_back(Attr{kern, dev, smem});
-    }
-  }
-  for (const Occ& o : occs)
+  std::lock_guard<std::mutex> lock(g_smem_mu);
+  raise_locked(kern, dev, smem);
+  for (const SmemOcc& o : g_smem_occs)
     if (o.kern == kern && o.dev == dev && o.block == block && o.smem == smem) return o.per_sm;
   int per_sm = 0;
   QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem));
-  occs.push_back(Occ{kern, dev, block, smem, per_sm});
+  g_smem_occs.push_back(SmemOcc{kern, dev, block, smem, per_sm});
   return per_sm;
 }
 

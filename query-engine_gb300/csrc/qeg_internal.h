@@ -193,11 +193,14 @@ void read_words_and_error(qeg_ctx* ctx, const void* dev_words, size_t nwords, ui
 // Throws the error an error word `e` (read from the device) stands for, after
 // clearing the device copy; returns for no error.
 void raise_device_error(qeg_ctx* ctx, uint32_t e);
+// Raises `kern`'s dynamic shared-memory attribute on the current device to
+// `smem` bytes when it is lower (never lowers it), under one process-wide
+// lock: operator instances in several threads launch the same kernels with
+// different sizes. Every setting of that attribute goes through here.
+void raise_dynamic_smem(const void* kern, size_t smem);
 // Blocks per SM of `kern` at `block` threads and `smem` dynamic shared bytes
-// on the current device, after raising the kernel's shared-memory attribute to
-// `smem` when needed (never lowering it); cached per (device, kernel, block,
-// smem). Kernels launched through it must not have the attribute set
-// elsewhere.
+// on the current device, after raise_dynamic_smem(kern, smem); cached per
+// (device, kernel, block, smem).
 int blocks_per_sm(const void* kern, int block, size_t smem);
 
 inline unsigned grid_for(qeg_ctx* ctx, uint64_t work_items, int block, int blocks_per_sm) {

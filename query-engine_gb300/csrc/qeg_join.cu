@@ -2404,9 +2404,7 @@ void partitioned_sink(JoinState& st, const DevCol& key, const DevCol& val, uint6
   K.okey = okey.get<uint64_t>();
   K.oval = oval.get<int64_t>();
   const size_t sb = static_cast<size_t>(kPartTile) * 18 + static_cast<size_t>(np) * 16 + 16;
-  QEG_CUDA(cudaFuncSetAttribute(ppart_scatter_kernel<KT, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-  int per_sm = 1;
-  QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ppart_scatter_kernel<KT, VT>, 512, sb));
+  const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(ppart_scatter_kernel<KT, VT>), 512, sb);
   const uint64_t ntiles = (n + kPartTile - 1) / kPartTile;
   const unsigned g = static_cast<unsigned>(
       std::max<uint64_t>(1, std::min<uint64_t>(ntiles, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
@@ -3044,9 +3042,7 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       const bool use_tma = n >= static_cast<uint64_t>(kTileRows) * ctx->sms * 2 && al16(S.kvalid) && al16(S.vvalid) &&
                            tma_env != nullptr && tma_env[0] == '1';
       auto launch_async = [&](void (*kern)(SinkK), size_t sb) {
-        QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb)));
-        int per_sm = 0;
-        QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, sb));
+        const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), 256, sb);
         const uint64_t want = (n / kAsyncTile + 7) / 8;
         const unsigned grid = static_cast<unsigned>(
             std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));
@@ -3054,7 +3050,7 @@ qeg_status qeg_join_probe_count_sum(qeg_join* j, const qeg_column* probe_key, co
       };
       auto launch_tma = [&](void (*kern)(SinkK, uint32_t*), size_t tile_bytes) {
         const size_t sb = tile_bytes * kStages;
-        QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sb)));
+        raise_dynamic_smem(reinterpret_cast<const void*>(kern), sb);
         kern<<<ctx->sms, kTmaThreads, sb, ctx->stream>>>(S, static_cast<uint32_t*>(ctx->dev_err.get()));
       };
 #define QEG_SINK(KT, VT)                                                                                           \

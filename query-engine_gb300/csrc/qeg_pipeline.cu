@@ -975,10 +975,7 @@ qeg_status qeg_filter_join_agg(qeg_ctx* ctx, const qeg_column* probe, int nprobe
       }
       const size_t sb = P.per_warp ? per_copy * (block / 32) : per_copy;
       require(sb <= ctx->smem_optin, "too many groups for the fused pipeline's shared-memory state");
-      if (sb > 48 * 1024)
-        QEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-      int per_sm = 1;
-      QEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, sb));
+      const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), block, sb);
       const uint64_t want = (np + block * 16 - 1) / (block * 16);
       const unsigned grid = static_cast<unsigned>(
           std::max<uint64_t>(1, std::min<uint64_t>(want, static_cast<uint64_t>(ctx->sms) * std::max(per_sm, 1))));

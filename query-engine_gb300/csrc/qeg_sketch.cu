@@ -233,7 +233,7 @@ void sketch_key_column(qeg_ctx* ctx, const DevCol& key, const uint32_t* sel, uin
   P.stats = P.cand_cnt + kCandGlobal;
   P.err = static_cast<uint32_t*>(ctx->dev_err.get());
   const size_t sb = words * 4 + kCandLocal * 12;
-  QEG_CUDA(cudaFuncSetAttribute(sketch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+  raise_dynamic_smem(reinterpret_cast<const void*>(sketch_kernel), sb);
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(nblocks, ctx->sms * 2ull));
   if (nblocks > 0) {
     sketch_kernel<<<grid, kSampleBlock, sb, ctx->stream>>>(P);
@@ -554,7 +554,7 @@ void batch_sketch(qeg_ctx* ctx, const DevCol& key, const uint64_t* d_offsets, co
   P.sample_target = sample_target;
   P.out = buf.get<BatchSketchOut>();
   const size_t sb = (kHllM + kCmsDepth * kCmsWidth) * 4 + kBSCand * 12;
-  QEG_CUDA(cudaFuncSetAttribute(batch_sketch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+  raise_dynamic_smem(reinterpret_cast<const void*>(batch_sketch_kernel), sb);
   batch_sketch_kernel<<<nq, kBSThreads, sb, ctx->stream>>>(P);
   ctx->launches++;
   QEG_CUDA(cudaGetLastError());

@@ -4,6 +4,7 @@
 // the CPU and against expectations written in the reference's own tests.
 // Exit code 0 = all checks passed.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -13,6 +14,7 @@
 #include <set>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -20,7 +22,7 @@
 
 using namespace qe;
 
-static int g_fail = 0;
+static std::atomic<int> g_fail{0};  // checks may fail on several threads
 #define CHECK(c)                                                        \
   do {                                                                  \
     if (!(c)) {                                                         \
@@ -497,6 +499,17 @@ std::unique_ptr<BatchSource> mixed_source(std::size_t batches, std::size_t rows_
   return src;
 }
 
+// A small dimension table: STR key with a repeated value, an I64 key.
+std::unique_ptr<BatchSource> dims_source() {
+  auto d = std::make_unique<BatchSource>();
+  d->schema.fields = {{"sym", Type::STR}, {"sector", Type::I32}, {"k", Type::I64}};
+  d->batches.push_back({str_col({"IBM", "AAPL", "NVDA", "XOM"}, {0, 1, 2, 3, 1}),
+                        make_col<int32_t>(Type::I32, {1, 2, 3, 4, 5}),
+                        make_col<int64_t>(Type::I64, {-1000, 5, 17, 1999, 5})});
+  d->sels.push_back({});
+  return d;
+}
+
 std::vector<Row> sorted(std::vector<Row> r) {
   std::sort(r.begin(), r.end());
   return r;
@@ -565,20 +578,9 @@ void test_device_table_scan() {
   }
   // Joins: both sides in place (STR key), in-place probe with a host build
   // (I64 key), and a STR key with only one side in place (staged).
-  auto dims = std::make_unique<BatchSource>();
-  dims->schema.fields = {{"sym", Type::STR}, {"sector", Type::I32}, {"k", Type::I64}};
-  dims->batches.push_back({str_col({"IBM", "AAPL", "NVDA", "XOM"}, {0, 1, 2, 3, 1}),
-                           make_col<int32_t>(Type::I32, {1, 2, 3, 4, 5}),
-                           make_col<int64_t>(Type::I64, {-1000, 5, 17, 1999, 5})});
-  dims->sels.push_back({});
+  auto dims = dims_source();
   auto dims_table = gpu::DeviceTable::upload(*dims);
-  auto host_dims = [&]() {
-    auto d = std::make_unique<BatchSource>();
-    d->schema = dims->schema;
-    d->batches = dims->batches;
-    d->sels = dims->sels;
-    return d;
-  };
+  auto host_dims = [] { return dims_source(); };
   for (JoinType jt : {JoinType::Inner, JoinType::Left}) {
     gpu::GpuHashJoin dev(std::make_unique<gpu::GpuScan>(table), std::make_unique<gpu::GpuScan>(dims_table), {0}, {0},
                          jt);
@@ -603,6 +605,57 @@ void test_device_table_scan() {
   CHECK(rows.size() == 1 && rows[0][0].i == 0 && rows[0][1].null);
 }
 
+void test_concurrent_instances() {
+  // Several operator instances in one process, one per thread, as the
+  // reference's morsel workers run them (exec/parallel.h:15-19): each owns its
+  // context, stream and buffers; two of them read one DeviceTable at a time.
+  auto up = mixed_source(90, 2000);
+  auto table = gpu::DeviceTable::upload(*up);
+  const std::vector<AggSpec> by_sym = {AggSpec::count_star("n"), AggSpec::sum(1, "s"), AggSpec::avg(2, "a"),
+                                       AggSpec::min(0, "mn"), AggSpec::max(0, "mx")};
+  const std::vector<AggSpec> by_k = {AggSpec::count_star("n"), AggSpec::sum(3, "q"), AggSpec::max(2, "m")};
+  auto run = [&](int kind) {
+    switch (kind) {
+      case 0: {
+        gpu::GpuAggregate a(std::make_unique<gpu::GpuScan>(table), {0}, by_sym);
+        return drain(a);
+      }
+      case 1: {
+        gpu::GpuAggregate a(mixed_source(90, 2000), {1, 3}, by_k);
+        return drain(a);
+      }
+      case 2: {
+        gpu::GpuHashJoin j(std::make_unique<gpu::GpuScan>(table), std::make_unique<gpu::GpuScan>(
+                               gpu::DeviceTable::upload(*dims_source())), {0}, {0}, JoinType::Left);
+        return drain(j);
+      }
+      default: {
+        gpu::GpuHashJoin j(mixed_source(90, 2000), dims_source(), {1}, {2}, JoinType::Inner);
+        return drain(j);
+      }
+    }
+  };
+  std::vector<std::vector<Row>> want;
+  for (int k = 0; k < 4; ++k) want.push_back(run(k));
+  std::atomic<int> mismatches{0}, errors{0};
+  std::vector<std::thread> workers;
+  for (int w = 0; w < 4; ++w)
+    workers.emplace_back([&, w] {
+      try {
+        for (int it = 0; it < 4; ++it) {
+          const int k = (w + it) % 4;
+          if (!same_rows(run(k), want[k])) ++mismatches;
+        }
+      } catch (const std::exception& e) {
+        std::fprintf(stderr, "worker %d: %s\n", w, e.what());
+        ++errors;
+      }
+    });
+  for (auto& t : workers) t.join();
+  CHECK(errors.load() == 0);
+  CHECK(mismatches.load() == 0);
+}
+
 int main() {
   try {
     test_aggregate_edge_table();
@@ -614,12 +667,13 @@ int main() {
     test_window_tumbling();
     test_asof_join();
     test_device_table_scan();
+    test_concurrent_instances();
   } catch (const std::exception& e) {
     std::fprintf(stderr, "exception: %s\n", e.what());
     return 2;
   }
   if (g_fail) {
-    std::fprintf(stderr, "%d check(s) failed\n", g_fail);
+    std::fprintf(stderr, "%d check(s) failed\n", g_fail.load());
     return 1;
   }
   std::printf("all operator checks passed\n");

@@ -17,7 +17,7 @@ def build_test_binary():
     os.makedirs(os.path.dirname(out), exist_ok=True)
     cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-o", out,
            os.path.join(REPO, "tests", "cpp", "test_operators.cpp"), os.path.join(PKG, "host", "gpu_operators.cpp"),
-           "-I" + os.path.join(REPO, "include"), "-L" + PKG, "-lqeg", "-Wl,-rpath," + PKG]
+           "-I" + os.path.join(REPO, "include"), "-L" + PKG, "-lqeg", "-Wl,-rpath," + PKG, "-pthread"]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return out
 
