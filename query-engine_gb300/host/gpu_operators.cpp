@@ -277,6 +277,7 @@ void DeviceTable::download(std::size_t c, std::size_t first, std::size_t n, void
   if (first % 64 != 0 || first + n > rows_) throw std::invalid_argument("DeviceTable: slice out of range");
   if (n == 0) return;
   const std::size_t w = byte_width(schema_.fields[c].second);
+  std::lock_guard<std::mutex> lock(download_mu_);
   dev_->check(qeg_dev_download(dev_->ctx(), vals, static_cast<const std::uint8_t*>(data_[c]) + first * w, n * w));
   if (valid_[c])
     dev_->check(qeg_dev_download(dev_->ctx(), words, valid_[c] + first / 64, validity::words(n) * 8));

@@ -38,6 +38,7 @@
 #include <cstdint>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <optional>
 #include <string>
 #include <utility>
@@ -161,7 +162,8 @@ class DeviceTable {
                                   const std::vector<std::vector<std::int32_t>>& code_maps) const;
   // Copies rows [first, first + n) of column c (`first` a multiple of 64) to
   // host memory: the values to `vals`, and the validity words to `words` when
-  // the column holds a NULL.
+  // the column holds a NULL. Safe to call from several threads (the copies
+  // share the table's context and take turns).
   void download(std::size_t c, std::size_t first, std::size_t n, void* vals, std::uint64_t* words) const;
 
  private:
@@ -169,6 +171,7 @@ class DeviceTable {
   Schema schema_;
   std::size_t rows_ = 0;
   std::unique_ptr<Device> dev_;
+  mutable std::mutex download_mu_;
   std::vector<void*> data_;
   std::vector<std::uint64_t*> valid_;
   std::vector<std::shared_ptr<StringDict>> dicts_;
