@@ -93,3 +93,21 @@ def test_python_structs_match_the_c_layouts(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_device_table_entry_points_reject_a_null_context():
+    """qeg_dev_alloc / qeg_dev_upload / qeg_dev_download check their arguments
+    before any CUDA call: a NULL context is QEG_ERR_INVALID with the message in
+    the thread's error slot, *out is left alone, and qeg_dev_free(NULL) is a
+    no-op. (Runs without a GPU.)"""
+    _ensure_built()
+    L = ctypes.CDLL(qeg.LIB_PATH)
+    L.qeg_last_error.restype = ctypes.c_char_p
+    out = ctypes.c_void_p(1234)
+    assert L.qeg_dev_alloc(None, ctypes.c_uint64(64), ctypes.byref(out)) == -1  # QEG_ERR_INVALID
+    assert b"NULL" in L.qeg_last_error(None)
+    assert out.value == 1234
+    buf = ctypes.create_string_buffer(16)
+    assert L.qeg_dev_upload(None, None, buf, ctypes.c_uint64(16)) == -1
+    assert L.qeg_dev_download(None, buf, None, ctypes.c_uint64(16)) == -1
+    L.qeg_dev_free(None)
