@@ -67,3 +67,18 @@ int main() {
     subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-I", PKG, str(src), "-o", str(exe)], check=True,
                    capture_output=True, text=True)
     subprocess.run([str(exe)], check=True)
+
+
+def test_host_staging_without_a_gpu():
+    """tests/cpp/test_staging.cpp: the operators' host staging (values and
+    validity words across random batches and selection vectors, STR codes to
+    canonical ids by value, the invalid-code error, output column views)
+    checked on the CPU; page-locked allocation falls back to the heap."""
+    out = os.path.join(PKG, "_build", "test_staging")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-o", out,
+           os.path.join(REPO, "tests", "cpp", "test_staging.cpp"), os.path.join(PKG, "host", "gpu_operators.cpp"),
+           "-I" + os.path.join(REPO, "include"), "-L" + PKG, "-lqeg", "-Wl,-rpath," + PKG, "-pthread"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    r = subprocess.run([out], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
